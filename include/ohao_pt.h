@@ -1,0 +1,220 @@
+/*
+ * ohao_pt.h -- C ABI of the GB300 path-tracing hot path.
+ *
+ * Drop-in for the Vulkan path-tracing pass of OHAO (Qervas/ohao_engine): the
+ * calls below take the same scene, material, light, environment and TLAS/BLAS
+ * data the reference binds to its RT pipeline, and replace
+ *   - the driver BLAS/TLAS build behind RTAccelerationStructure
+ *     (ohao/render/rt/rt_acceleration_structure.hpp:73-107),
+ *   - the inputs PathTracer binds (ohao/render/rt/path_tracer.hpp:124-194),
+ *   - PathTracer::render -> vkCmdTraceRaysKHR
+ *     (ohao/render/rt/path_tracer_render.cpp:687-731) and the GLSL programs
+ *     shaders/rt/pt_raygen.rgen, pt_closesthit.rchit, pt_miss.rmiss.
+ * Plain C: pointers, sizes and status codes; no exception crosses the ABI.
+ * A context is externally synchronised (one thread at a time), like the
+ * reference's single command buffer. Unless a parameter says "device", every
+ * pointer is host memory and is copied before the call returns.
+ */
+#ifndef OHAO_PT_H
+#define OHAO_PT_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef int32_t ohao_status;
+#define OHAO_OK 0
+#define OHAO_ERR_INVALID_ARG (-1)
+#define OHAO_ERR_OOM (-2)
+#define OHAO_ERR_CUDA (-3)
+#define OHAO_ERR_TIMEOUT (-4)      /* a bounded device-side wait gave up */
+#define OHAO_ERR_NOT_BUILT (-5)    /* render/trace before ohao_pt_build */
+#define OHAO_ERR_UNSUPPORTED (-6)
+#define OHAO_ERR_DEVICE_CHECK (-7) /* a device-side bounds/stack check fired */
+
+/* Same object as cudaStream_t (struct CUstream_st*); NULL = legacy stream. */
+typedef struct CUstream_st* ohao_stream;
+
+typedef struct ohao_pt_ctx ohao_pt_ctx;
+
+typedef struct ohao_pt_desc {
+    int32_t device;          /* CUDA device ordinal */
+    uint32_t flags;          /* reserved, 0 */
+    uint64_t flatten_limit;  /* instanced triangles up to which one flat BVH is
+                                built over world-space triangles; above it a
+                                two-level TLAS/BLAS is built. 0 = 2^25 */
+} ohao_pt_desc;
+
+/* GPULight, ohao/render/rt/gpu_light.hpp:10-16 (80 bytes, std430). */
+typedef struct ohao_gpu_light {
+    float position_type[4];    /* xyz position, w type (0 sphere,1 dir,2 spot,3 area) */
+    float color_intensity[4];
+    float dir_param[4];        /* xyz direction, w radius / inner angle */
+    float extra[4];            /* spot: w outer angle; area: xyz edge1 */
+    float extra2[4];           /* area: xyz edge2, w area */
+} ohao_gpu_light;
+
+/* RTInstance, rt_acceleration_structure.hpp:41-47; transform is the row-major
+ * 3x4 VkTransformMatrixKHR of buildTLAS (rt_acceleration_structure.cpp:437-445).
+ * custom_index is gl_InstanceCustomIndexEXT (24 bits): OHAO sets it to the
+ * global triangle offset, so globalTriID = custom_index + primitiveID. */
+typedef struct ohao_pt_instance {
+    uint32_t blas;
+    float transform[12];
+    uint32_t custom_index;
+    uint32_t mask;             /* instance skipped when (mask & 0xFF) == 0 */
+    uint32_t sbt_offset;       /* unused (one hit group) */
+} ohao_pt_instance;
+
+/* One camera view. Matrices are column-major (glm) like the reference push
+ * constants (pt_raygen.rgen:41-49). accum is a device RGBA32F image of
+ * width*height texels holding (mean radiance, sample count); history is the
+ * number of frames already in it (0 overwrites), the reference's
+ * historyFrameCount. path_radiance (device, optional) receives every path's
+ * radiance as [spp][height*width][4] floats. aov (device, optional) receives
+ * the last sample's first-hit albedo.rgb, normal*0.5+0.5, view depth and a
+ * hit flag as [height*width][8] floats. */
+typedef struct ohao_pt_view {
+    float inv_view[16];
+    float inv_proj[16];
+    uint32_t width;
+    uint32_t height;
+    uint32_t history;
+    uint32_t reserved;
+    float* accum;
+    float* path_radiance;
+    float* aov;
+} ohao_pt_view;
+
+#define OHAO_SAMPLER_PCG 0u
+#define OHAO_SAMPLER_SOBOL 1u
+
+/* flag bits keep the reference's PT_FLAG values (pt_raygen.rgen:56-60) */
+#define OHAO_PT_FLAG_FIREFLY_CLAMP (1u << 2)
+#define OHAO_PT_FLAG_ENV_FIXED_V (1u << 8)   /* not reference: un-mirrored env lookup */
+#define OHAO_PT_FLAG_PROFILE (1u << 16)      /* record per-kernel CUDA-event times */
+
+#define OHAO_PT_MODE_AUTO 0u
+#define OHAO_PT_MODE_WAVEFRONT 1u
+#define OHAO_PT_MODE_PERSISTENT 2u
+
+/* Per-call parameters: the reference's push constants and RTRenderSettings
+ * (path_tracer_render.cpp:687-719, rt_settings.hpp:17-35). Sample k of a
+ * pixel uses sample index sample_index_base + k (PathTracer::m_sampleIndex). */
+typedef struct ohao_pt_settings {
+    uint32_t spp;
+    uint32_t max_bounces;
+    uint32_t sample_index_base;
+    uint32_t sampler;          /* OHAO_SAMPLER_* */
+    uint32_t flags;            /* OHAO_PT_FLAG_* */
+    float clamp_luminance;     /* tuning.x */
+    float aniso_strength;      /* jitter.z */
+    float aniso_rotation;      /* jitter.w */
+    uint32_t mode;             /* OHAO_PT_MODE_* */
+    uint32_t reserved[7];
+} ohao_pt_settings;
+
+/* Per-kernel timings of the last profiled render/trace (CUDA events on the
+ * launching stream): total milliseconds and launch counts. */
+typedef struct ohao_pt_profile {
+    float extend_ms, shadow_ms, shade_ms, other_ms, total_ms;
+    uint32_t extend_launches, shadow_launches, shade_launches, other_launches;
+    uint64_t rays_closest, rays_shadow;
+} ohao_pt_profile;
+
+/* ---- lifecycle (PathTracer::init / destroy) ---- */
+ohao_status ohao_pt_create(const ohao_pt_desc* desc, ohao_pt_ctx** out);
+void ohao_pt_destroy(ohao_pt_ctx* ctx);
+const char* ohao_pt_last_error(const ohao_pt_ctx* ctx);
+const char* ohao_pt_version(void);
+
+/* ---- scene inputs ----
+ * Global geometry as OHAO's RT scene packer uploads it (rt_build.cpp:27-186):
+ * positions at pos_stride_bytes (12 packed, 100 for OHAO's Vertex), float4
+ * normals, float2 UVs (may be NULL), global pre-offset uint32 indices, one
+ * material id per global triangle (PathTracer::setNormalBuffer/setUVBuffer/
+ * setMaterialBuffers, path_tracer.hpp:124-133). */
+ohao_status ohao_pt_set_geometry(ohao_pt_ctx* ctx, const float* pos, uint32_t pos_stride_bytes, uint32_t nverts,
+                                 const float* normal4, const float* uv2, const uint32_t* indices, uint32_t ntris,
+                                 const uint32_t* mat_ids);
+/* RTAccelerationStructure::createBLAS (rt_acceleration_structure.cpp:205-300):
+ * one triangle geometry over indices [first_index, first_index+index_count). */
+ohao_status ohao_pt_create_blas(ohao_pt_ctx* ctx, uint32_t first_index, uint32_t index_count, uint32_t* out_blas);
+/* clearInstances + addInstance (rt_acceleration_structure.hpp:90-97). */
+ohao_status ohao_pt_set_instances(ohao_pt_ctx* ctx, const ohao_pt_instance* inst, uint32_t n);
+/* buildTLAS + the BLAS builds (rt_acceleration_structure.cpp:419-530): LBVH
+ * on the device; synchronous with respect to `stream`. */
+ohao_status ohao_pt_build(ohao_pt_ctx* ctx, ohao_stream stream);
+int32_t ohao_pt_is_two_level(const ohao_pt_ctx* ctx);
+/* Material table, 3 x vec4 per material (layout_meta.hpp:20-58). Slot 2 .yzw
+ * (unused by the reference) carries emissive RGB. Texture indices other than
+ * 0xFFFFFFFF are unsupported except diffuse index 0 = the tile albedo map. */
+ohao_status ohao_pt_set_materials(ohao_pt_ctx* ctx, const float* vec4x3, uint32_t n);
+/* updateRTMaterialParams (rt_build.cpp:313-389): rewrite records in place. */
+ohao_status ohao_pt_update_materials(ohao_pt_ctx* ctx, const float* vec4x3, uint32_t first, uint32_t n);
+/* Light SSBO (light_upload.cpp:153-300), at most 64 lights. */
+ohao_status ohao_pt_set_lights(ohao_pt_ctx* ctx, const ohao_gpu_light* lights, uint32_t n);
+/* HDR environment (RGBA32F w*h, row 0 = +Y in the CDF convention) with its
+ * marginal (h) / conditional (w*h) CDFs and integral (setEnvCDFBuffers,
+ * path_tracer.hpp:170-177); marg/cond NULL disables env importance sampling;
+ * rgba NULL removes the environment. intensity <= 0 means 1 (pt_miss.rmiss:65). */
+ohao_status ohao_pt_set_env(ohao_pt_ctx* ctx, const float* rgba, uint32_t w, uint32_t h, const float* marg,
+                            const float* cond, float integral, float intensity);
+/* Linear RGB tile albedo map (w*h*3 floats) read by materials whose diffuse
+ * texture index is 0, sampled bilinearly as ohao/render/diff/diff_map.hpp:40-67. */
+ohao_status ohao_pt_set_albedo_map(ohao_pt_ctx* ctx, const float* rgb, uint32_t w, uint32_t h);
+/* EnvCDF::build (ohao/render/rt/env_cdf.cpp:13-61), bit-identical. */
+ohao_status ohao_env_cdf_build(const float* rgba, int32_t w, int32_t h, float* marg, float* cond, float* integral);
+
+/* ---- render (PathTracer::render) ----
+ * Renders settings->spp samples per pixel into each view's device accum
+ * buffer on `stream`. n_views > 1 with mode AUTO uses the persistent
+ * multi-view kernel. */
+ohao_status ohao_pt_render(ohao_pt_ctx* ctx, const ohao_pt_view* views, uint32_t n_views,
+                           const ohao_pt_settings* settings, ohao_stream stream);
+/* Host-buffer variant (VulkanRenderer::getPixels analogue): views' device
+ * pointers are ignored; accumulation runs in library-owned device images
+ * seeded from and copied back to host_accum[i] (RGBA32F width*height). */
+ohao_status ohao_pt_render_host(ohao_pt_ctx* ctx, const ohao_pt_view* views, uint32_t n_views,
+                                const ohao_pt_settings* settings, float* const* host_accum, ohao_stream stream);
+ohao_status ohao_pt_get_profile(const ohao_pt_ctx* ctx, ohao_pt_profile* out);
+
+/* ---- traceRayEXT as a batch call ----
+ * rays: device, n x 8 floats (origin.xyz, tmin, dir.xyz, tmax).
+ * hits: device, n x 5 uint32 (t bits, u bits, v bits, instance, primitive);
+ * a miss has instance = primitive = 0xFFFFFFFF. any_hit != 0 writes 1/0 in
+ * hits[5i] (occluded). stats (device, optional): n x 2 uint32 nodes/triangles
+ * visited. */
+ohao_status ohao_pt_trace(ohao_pt_ctx* ctx, const float* rays, uint32_t n, uint32_t* hits, int32_t any_hit,
+                          uint32_t* stats, ohao_stream stream);
+
+/* ---- BVH inspection (tests / tools) ----
+ * which = -1: the flat BVH (or the TLAS when two-level); which = k: BLAS k.
+ * Nodes are ohao_bvh8_node; primitives are ohao_bvh_tri (uint32 instance ids
+ * for the TLAS). Host destination buffers. */
+typedef struct ohao_bvh8_node {
+    float origin[3];
+    int8_t exps[3];            /* per-axis power-of-two grid exponent */
+    uint8_t imask;             /* bit i: slot i is an internal child */
+    uint32_t child_base;       /* first internal child node */
+    uint32_t tri_base;         /* first primitive of this node's leaves */
+    uint8_t meta[8];           /* 0 empty; 0x80|rank internal; (count<<5)|offset leaf */
+    uint8_t qlo[3][8];
+    uint8_t qhi[3][8];
+} ohao_bvh8_node;               /* 80 bytes */
+typedef struct ohao_bvh_tri {
+    float v0[3]; uint32_t prim;
+    float v1[3]; uint32_t inst;
+    float v2[3]; uint32_t ref;
+} ohao_bvh_tri;                 /* 48 bytes */
+ohao_status ohao_pt_bvh_info(const ohao_pt_ctx* ctx, int32_t which, uint32_t* n_nodes, uint32_t* n_prims,
+                             uint32_t* height);
+ohao_status ohao_pt_bvh_download(ohao_pt_ctx* ctx, int32_t which, void* nodes, void* prims);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* OHAO_PT_H */

@@ -1,0 +1,310 @@
+"""GB300-native path-tracing hot path of the OHAO engine (Python host mirror).
+
+This package loads ``_lib/libohao_pt.so`` -- the C ABI declared in
+``include/ohao_pt.h`` -- and mirrors the reference's host objects around it:
+
+* :class:`PathTracer` -- PathTracer's inputs and render call
+  (``ohao/render/rt/path_tracer.hpp:61-194``) plus RTAccelerationStructure's
+  createBLAS / addInstance / buildTLAS (``rt_acceleration_structure.hpp:73-107``);
+* :class:`EnvCDF` -- ``ohao/render/rt/env_cdf.hpp:12-43``.
+
+Failures raise :class:`OhaoError` carrying the ABI status and message. There
+is no CPU fallback: without the compiled library every call raises.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+
+import numpy as np
+
+from . import scenes  # noqa: F401
+
+_PKG = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(_PKG, "_lib", "libohao_pt.so")
+
+OK = 0
+STATUS_NAMES = {0: "OK", -1: "INVALID_ARG", -2: "OOM", -3: "CUDA_ERROR", -4: "TIMEOUT", -5: "NOT_BUILT",
+                -6: "UNSUPPORTED", -7: "DEVICE_CHECK"}
+SAMPLER_PCG, SAMPLER_SOBOL = 0, 1
+FLAG_FIREFLY_CLAMP = 1 << 2
+FLAG_ENV_FIXED_V = 1 << 8
+FLAG_PROFILE = 1 << 16
+MODE_AUTO, MODE_WAVEFRONT, MODE_PERSISTENT = 0, 1, 2
+
+EXPORTED_SYMBOLS = [
+    "ohao_pt_create", "ohao_pt_destroy", "ohao_pt_last_error", "ohao_pt_version", "ohao_pt_set_geometry",
+    "ohao_pt_create_blas", "ohao_pt_set_instances", "ohao_pt_build", "ohao_pt_is_two_level",
+    "ohao_pt_set_materials", "ohao_pt_update_materials", "ohao_pt_set_lights", "ohao_pt_set_env",
+    "ohao_pt_set_albedo_map", "ohao_env_cdf_build", "ohao_pt_render", "ohao_pt_render_host",
+    "ohao_pt_get_profile", "ohao_pt_trace", "ohao_pt_bvh_info", "ohao_pt_bvh_download",
+]
+
+
+class OhaoError(RuntimeError):
+    def __init__(self, status: int, msg: str):
+        super().__init__(f"{STATUS_NAMES.get(status, status)}: {msg}")
+        self.status = status
+
+
+class _Desc(C.Structure):
+    _fields_ = [("device", C.c_int32), ("flags", C.c_uint32), ("flatten_limit", C.c_uint64)]
+
+
+class View(C.Structure):
+    """ohao_pt_view"""
+    _fields_ = [("inv_view", C.c_float * 16), ("inv_proj", C.c_float * 16), ("width", C.c_uint32),
+                ("height", C.c_uint32), ("history", C.c_uint32), ("reserved", C.c_uint32),
+                ("accum", C.c_void_p), ("path_radiance", C.c_void_p), ("aov", C.c_void_p)]
+
+
+class Settings(C.Structure):
+    """ohao_pt_settings"""
+    _fields_ = [("spp", C.c_uint32), ("max_bounces", C.c_uint32), ("sample_index_base", C.c_uint32),
+                ("sampler", C.c_uint32), ("flags", C.c_uint32), ("clamp_luminance", C.c_float),
+                ("aniso_strength", C.c_float), ("aniso_rotation", C.c_float), ("mode", C.c_uint32),
+                ("reserved", C.c_uint32 * 7)]
+
+
+class Profile(C.Structure):
+    _fields_ = [("extend_ms", C.c_float), ("shadow_ms", C.c_float), ("shade_ms", C.c_float),
+                ("other_ms", C.c_float), ("total_ms", C.c_float), ("extend_launches", C.c_uint32),
+                ("shadow_launches", C.c_uint32), ("shade_launches", C.c_uint32), ("other_launches", C.c_uint32),
+                ("rays_closest", C.c_uint64), ("rays_shadow", C.c_uint64)]
+
+
+_lib = None
+
+
+def load_library(path: str | None = None):
+    """Load libohao_pt.so; raises if it has not been built."""
+    global _lib
+    if _lib is not None and path is None:
+        return _lib
+    p = path or LIB_PATH
+    if not os.path.exists(p):
+        raise OhaoError(-5, f"{p} not built; run __graft_entry__.build() or python -m ohao_engine_gb300._build")
+    L = C.CDLL(p)
+    vp, u32, i32, f32 = C.c_void_p, C.c_uint32, C.c_int32, C.c_float
+    sigs = {
+        "ohao_pt_create": ([C.POINTER(_Desc), C.POINTER(vp)], i32),
+        "ohao_pt_destroy": ([vp], None),
+        "ohao_pt_last_error": ([vp], C.c_char_p),
+        "ohao_pt_version": ([], C.c_char_p),
+        "ohao_pt_set_geometry": ([vp, vp, u32, u32, vp, vp, vp, u32, vp], i32),
+        "ohao_pt_create_blas": ([vp, u32, u32, C.POINTER(u32)], i32),
+        "ohao_pt_set_instances": ([vp, vp, u32], i32),
+        "ohao_pt_build": ([vp, vp], i32),
+        "ohao_pt_is_two_level": ([vp], i32),
+        "ohao_pt_set_materials": ([vp, vp, u32], i32),
+        "ohao_pt_update_materials": ([vp, vp, u32, u32], i32),
+        "ohao_pt_set_lights": ([vp, vp, u32], i32),
+        "ohao_pt_set_env": ([vp, vp, u32, u32, vp, vp, f32, f32], i32),
+        "ohao_pt_set_albedo_map": ([vp, vp, u32, u32], i32),
+        "ohao_env_cdf_build": ([vp, i32, i32, vp, vp, vp], i32),
+        "ohao_pt_render": ([vp, C.POINTER(View), u32, C.POINTER(Settings), vp], i32),
+        "ohao_pt_render_host": ([vp, C.POINTER(View), u32, C.POINTER(Settings), C.POINTER(vp), vp], i32),
+        "ohao_pt_get_profile": ([vp, C.POINTER(Profile)], i32),
+        "ohao_pt_trace": ([vp, vp, u32, vp, i32, vp, vp], i32),
+        "ohao_pt_bvh_info": ([vp, i32, C.POINTER(u32), C.POINTER(u32), C.POINTER(u32)], i32),
+        "ohao_pt_bvh_download": ([vp, i32, vp, vp], i32),
+    }
+    for name, (args, res) in sigs.items():
+        fn = getattr(L, name)
+        fn.argtypes = args
+        fn.restype = res
+    if path is None:
+        _lib = L
+    return L
+
+
+def _ptr(a):
+    if a is None:
+        return None
+    if isinstance(a, np.ndarray):
+        return a.ctypes.data_as(C.c_void_p)
+    if hasattr(a, "data_ptr"):
+        return C.c_void_p(a.data_ptr())
+    return C.c_void_p(int(a))
+
+
+class EnvCDF:
+    """ohao::EnvCDF -- marginal + conditional luminance CDFs of an RGBA32F map."""
+
+    def __init__(self):
+        self.width = self.height = 0
+        self.integral = 0.0
+        self.marginal = np.zeros(0, np.float32)
+        self.conditional = np.zeros(0, np.float32)
+
+    def build(self, pixels: np.ndarray, width: int | None = None, height: int | None = None) -> "EnvCDF":
+        px = np.ascontiguousarray(pixels, np.float32)
+        h = height or px.shape[0]
+        w = width or px.shape[1]
+        self.marginal = np.zeros(h, np.float32)
+        self.conditional = np.zeros(w * h, np.float32)
+        integ = np.zeros(1, np.float32)
+        st = load_library().ohao_env_cdf_build(_ptr(px), w, h, _ptr(self.marginal), _ptr(self.conditional), _ptr(integ))
+        if st != OK:
+            raise OhaoError(st, "ohao_env_cdf_build failed")
+        self.width, self.height, self.integral = w, h, float(integ[0])
+        return self
+
+    def valid(self) -> bool:
+        return self.width > 0 and self.height > 0 and self.marginal.size > 0
+
+
+def make_view(view, accum=None, history: int = 0, path_radiance=None, aov=None) -> View:
+    v = View()
+    v.inv_view[:] = [float(x) for x in np.asarray(view.inv_view, np.float32)]
+    v.inv_proj[:] = [float(x) for x in np.asarray(view.inv_proj, np.float32)]
+    v.width, v.height, v.history = int(view.width), int(view.height), int(history)
+    v.accum = _ptr(accum).value if accum is not None else None
+    v.path_radiance = _ptr(path_radiance).value if path_radiance is not None else None
+    v.aov = _ptr(aov).value if aov is not None else None
+    return v
+
+
+def make_settings(spp=1, max_bounces=4, sample_index_base=0, sampler=SAMPLER_PCG, flags=0, clamp_luminance=0.0,
+                  aniso_strength=0.0, aniso_rotation=0.0, mode=MODE_AUTO) -> Settings:
+    s = Settings()
+    s.spp, s.max_bounces, s.sample_index_base, s.sampler = spp, max_bounces, sample_index_base, sampler
+    s.flags, s.clamp_luminance, s.aniso_strength, s.aniso_rotation, s.mode = (flags, clamp_luminance,
+                                                                             aniso_strength, aniso_rotation, mode)
+    return s
+
+
+class PathTracer:
+    """Context wrapper: scene inputs, LBVH/TLAS build and render on one GPU."""
+
+    def __init__(self, device: int = 0, flatten_limit: int = 0):
+        self._L = load_library()
+        d = _Desc(device, 0, flatten_limit)
+        h = C.c_void_p()
+        st = self._L.ohao_pt_create(C.byref(d), C.byref(h))
+        if st != OK:
+            raise OhaoError(st, "ohao_pt_create failed")
+        self.h = h
+        self._keep = {}
+
+    def close(self):
+        if getattr(self, "h", None):
+            self._L.ohao_pt_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def _ck(self, st: int, what: str):
+        if st != OK:
+            msg = self._L.ohao_pt_last_error(self.h)
+            raise OhaoError(st, f"{what}: {msg.decode() if msg else ''}")
+
+    # -- inputs --------------------------------------------------------------
+    def set_geometry(self, pos, normals, uvs, indices, mat_ids, pos_stride_bytes: int = 12):
+        pos = np.ascontiguousarray(pos, np.float32)
+        nrm = np.ascontiguousarray(normals, np.float32)
+        uv = None if uvs is None else np.ascontiguousarray(uvs, np.float32)
+        idx = np.ascontiguousarray(indices, np.uint32)
+        mid = np.ascontiguousarray(mat_ids, np.uint32)
+        nverts = pos.size * 4 // pos_stride_bytes
+        self._ck(self._L.ohao_pt_set_geometry(self.h, _ptr(pos), pos_stride_bytes, nverts, _ptr(nrm), _ptr(uv),
+                                              _ptr(idx), idx.size // 3, _ptr(mid)), "set_geometry")
+
+    def create_blas(self, first_index: int, index_count: int) -> int:
+        out = C.c_uint32()
+        self._ck(self._L.ohao_pt_create_blas(self.h, first_index, index_count, C.byref(out)), "create_blas")
+        return out.value
+
+    def set_instances(self, inst: np.ndarray):
+        inst = np.ascontiguousarray(inst, scenes.INSTANCE_DTYPE)
+        self._ck(self._L.ohao_pt_set_instances(self.h, _ptr(inst), inst.size), "set_instances")
+
+    def build(self, stream=None):
+        self._ck(self._L.ohao_pt_build(self.h, _ptr(stream) if stream is not None else None), "build")
+
+    @property
+    def two_level(self) -> bool:
+        return bool(self._L.ohao_pt_is_two_level(self.h))
+
+    def set_materials(self, mats):
+        m = np.ascontiguousarray(mats, np.float32).reshape(-1, 12)
+        self._ck(self._L.ohao_pt_set_materials(self.h, _ptr(m), m.shape[0]), "set_materials")
+
+    def update_materials(self, mats, first: int = 0):
+        m = np.ascontiguousarray(mats, np.float32).reshape(-1, 12)
+        self._ck(self._L.ohao_pt_update_materials(self.h, _ptr(m), first, m.shape[0]), "update_materials")
+
+    def set_lights(self, lights):
+        l = np.ascontiguousarray(lights, np.float32).reshape(-1, 20)
+        self._ck(self._L.ohao_pt_set_lights(self.h, _ptr(l), l.shape[0]), "set_lights")
+
+    def set_env(self, rgba, cdf: EnvCDF | None = None, intensity: float = 1.0, importance_sampling: bool = True):
+        if rgba is None:
+            self._ck(self._L.ohao_pt_set_env(self.h, None, 0, 0, None, None, 0.0, 0.0), "set_env")
+            return
+        env = np.ascontiguousarray(rgba, np.float32)
+        h, w = env.shape[:2]
+        if importance_sampling and cdf is None:
+            cdf = EnvCDF().build(env)
+        self._keep["env"] = (env, cdf)
+        self._ck(self._L.ohao_pt_set_env(self.h, _ptr(env), w, h, _ptr(cdf.marginal) if cdf else None,
+                                         _ptr(cdf.conditional) if cdf else None, cdf.integral if cdf else 0.0,
+                                         intensity), "set_env")
+
+    def set_albedo_map(self, rgb):
+        m = np.ascontiguousarray(rgb, np.float32)
+        self._ck(self._L.ohao_pt_set_albedo_map(self.h, _ptr(m), m.shape[1], m.shape[0]), "set_albedo_map")
+
+    def load_scene(self, sd, build: bool = True):
+        """Upload a :class:`scenes.SceneData` and build its BVH."""
+        self.set_geometry(sd.pos, sd.normals, sd.uvs, sd.indices, sd.mat_ids)
+        for fi, ic in sd.blas:
+            self.create_blas(fi, ic)
+        self.set_instances(sd.instances)
+        self.set_materials(sd.materials)
+        if sd.lights is not None and len(sd.lights):
+            self.set_lights(sd.lights)
+        if sd.env is not None:
+            self.set_env(sd.env, intensity=sd.env_intensity)
+        if sd.albedo_map is not None:
+            self.set_albedo_map(sd.albedo_map)
+        if build:
+            self.build()
+
+    # -- render --------------------------------------------------------------
+    def render(self, views, settings: Settings, stream=None):
+        arr = (View * len(views))(*views)
+        self._ck(self._L.ohao_pt_render(self.h, arr, len(views), C.byref(settings),
+                                        _ptr(stream) if stream is not None else None), "render")
+
+    def render_host(self, views, settings: Settings, host_accum, stream=None):
+        arr = (View * len(views))(*views)
+        ptrs = (C.c_void_p * len(views))(*[_ptr(a).value for a in host_accum])
+        self._ck(self._L.ohao_pt_render_host(self.h, arr, len(views), C.byref(settings), ptrs,
+                                             _ptr(stream) if stream is not None else None), "render_host")
+
+    def profile(self) -> Profile:
+        p = Profile()
+        self._ck(self._L.ohao_pt_get_profile(self.h, C.byref(p)), "get_profile")
+        return p
+
+    def trace(self, rays_dev, n: int, hits_dev, any_hit: bool = False, stats_dev=None, stream=None):
+        self._ck(self._L.ohao_pt_trace(self.h, _ptr(rays_dev), n, _ptr(hits_dev), int(any_hit), _ptr(stats_dev),
+                                       _ptr(stream) if stream is not None else None), "trace")
+
+    def bvh(self, which: int = -1):
+        nn, npr, hh = C.c_uint32(), C.c_uint32(), C.c_uint32()
+        self._ck(self._L.ohao_pt_bvh_info(self.h, which, C.byref(nn), C.byref(npr), C.byref(hh)), "bvh_info")
+        nodes = np.zeros(nn.value * 80, np.uint8)
+        pb = 4 if (which < 0 and self.two_level) else 48
+        prims = np.zeros(npr.value * pb, np.uint8)
+        self._ck(self._L.ohao_pt_bvh_download(self.h, which, _ptr(nodes), _ptr(prims)), "bvh_download")
+        return nodes, prims, hh.value
+
+
+def version() -> str:
+    return load_library().ohao_pt_version().decode()

@@ -1,0 +1,697 @@
+// abi.cpp -- host side of the C ABI (C++20): scene storage, acceleration
+// structure builds and render orchestration around the CUDA kernels.
+//
+// Mirrors the reference's host objects: the input setters of PathTracer
+// (ohao/render/rt/path_tracer.hpp:124-194), RTAccelerationStructure's
+// createBLAS / addInstance / buildTLAS (rt_acceleration_structure.hpp:73-107),
+// updateRTMaterialParams (ohao/gpu/vulkan/rt_build.cpp:313-389) and
+// EnvCDF::build (ohao/render/rt/env_cdf.cpp:13-61). Errors are status codes
+// plus a per-context message, never exceptions (the reference's
+// [[nodiscard]] bool + std::cerr convention, path_tracer.cpp:92-120).
+#include <algorithm>
+#include <cmath>
+#include <cstring>
+#include <memory>
+#include <new>
+#include <string>
+#include <vector>
+
+#include <cuda_runtime.h>
+
+#include "../../include/ohao_pt.h"
+#include "bvh_internal.hpp"
+#include "pt_types.hpp"
+
+namespace {
+
+using namespace ohao;
+
+// Sobol direction numbers, dimensions 0-3 x 32 bits: the table of
+// shaders/includes/rt/sampler_sobol_tables.glsl:10-47 (data, not derivable:
+// dimension 2 is not the textbook Joe-Kuo dimension).
+const uint32_t kSobolDirs[128] = {
+    0x80000000u, 0x40000000u, 0x20000000u, 0x10000000u, 0x08000000u, 0x04000000u, 0x02000000u, 0x01000000u,
+    0x00800000u, 0x00400000u, 0x00200000u, 0x00100000u, 0x00080000u, 0x00040000u, 0x00020000u, 0x00010000u,
+    0x00008000u, 0x00004000u, 0x00002000u, 0x00001000u, 0x00000800u, 0x00000400u, 0x00000200u, 0x00000100u,
+    0x00000080u, 0x00000040u, 0x00000020u, 0x00000010u, 0x00000008u, 0x00000004u, 0x00000002u, 0x00000001u,
+    0x80000000u, 0xC0000000u, 0xA0000000u, 0xF0000000u, 0x88000000u, 0xCC000000u, 0xAA000000u, 0xFF000000u,
+    0x80800000u, 0xC0C00000u, 0xA0A00000u, 0xF0F00000u, 0x88880000u, 0xCCCC0000u, 0xAAAA0000u, 0xFFFF0000u,
+    0x80008000u, 0xC000C000u, 0xA000A000u, 0xF000F000u, 0x88008800u, 0xCC00CC00u, 0xAA00AA00u, 0xFF00FF00u,
+    0x80808080u, 0xC0C0C0C0u, 0xA0A0A0A0u, 0xF0F0F0F0u, 0x88888888u, 0xCCCCCCCCu, 0xAAAAAAAAu, 0xFFFFFFFFu,
+    0x80000000u, 0x40000000u, 0xE0000000u, 0x50000000u, 0x98000000u, 0xBC000000u, 0xAE000000u, 0x25000000u,
+    0x5B800000u, 0x91400000u, 0x65600000u, 0x2E500000u, 0x91180000u, 0x88D40000u, 0xDD360000u, 0x02950000u,
+    0x4C888000u, 0x09EB4000u, 0x86CA6000u, 0x13B15000u, 0x42ADD800u, 0x3DF8D400u, 0x2FE57E00u, 0x56EB8100u,
+    0x8C41A680u, 0xE68455C0u, 0x3C9CE8E0u, 0xB44DBFF0u, 0x7C27F6C8u, 0x5239A6ACu, 0x853B0EDEu, 0x52EB2EF9u,
+    0x80000000u, 0xC0000000u, 0x20000000u, 0x50000000u, 0xF8000000u, 0x74000000u, 0xA2000000u, 0x93000000u,
+    0xD8800000u, 0x25400000u, 0x59E00000u, 0xE6D00000u, 0x78080000u, 0xB40C0000u, 0x82020000u, 0xC3050000u,
+    0x208F8000u, 0x51CBC000u, 0xFBEA2000u, 0x75AD5000u, 0xA00AF800u, 0x90077400u, 0xD800A200u, 0x25009300u,
+    0x59E08480u, 0xE6D0CEC0u, 0x78088520u, 0xB40CEBB0u, 0x82028348u, 0xC305C274u, 0x208FB552u, 0x51CB9AE9u,
+};
+
+struct DevBuf {
+    void* p = nullptr;
+    size_t n = 0;
+    DevBuf() = default;
+    DevBuf(const DevBuf&) = delete;
+    DevBuf& operator=(const DevBuf&) = delete;
+    DevBuf(DevBuf&& o) noexcept : p(o.p), n(o.n) { o.p = nullptr; o.n = 0; }
+    DevBuf& operator=(DevBuf&& o) noexcept {
+        if (this != &o) { release(); p = o.p; n = o.n; o.p = nullptr; o.n = 0; }
+        return *this;
+    }
+    ~DevBuf() { release(); }
+    void release() {
+        if (p) cudaFree(p);
+        p = nullptr;
+        n = 0;
+    }
+    cudaError_t ensure(size_t bytes) {
+        if (bytes <= n && p) return cudaSuccess;
+        release();
+        if (bytes == 0) bytes = 256;
+        cudaError_t e = cudaMalloc(&p, bytes);
+        if (e != cudaSuccess) { p = nullptr; return e; }
+        n = bytes;
+        return cudaSuccess;
+    }
+    template <class T> T* as() const { return static_cast<T*>(p); }
+};
+
+struct BvhDev {
+    DevBuf nodes, prims;   // prims: tri records (48 B) or TLAS instance ids
+    uint32_t nnodes = 0, nprims = 0, height = 0;
+    float root_box[6] = {0, 0, 0, 0, 0, 0};
+};
+
+struct BlasDesc {
+    uint32_t first_index, index_count;
+};
+
+}  // namespace
+
+struct ohao_pt_ctx {
+    int device = 0;
+    uint64_t flatten_limit = 1ull << 25;
+    std::string last_error;
+    // geometry
+    DevBuf pos, normals, uvs, indices, mat_ids, mats, lights, env, marg, cond, albedo_map;
+    uint32_t nverts = 0, ntris = 0, nmats = 0, nlights = 0;
+    std::vector<float> host_pos;          // packed, for host-side instance boxes
+    std::vector<uint32_t> host_indices;
+    uint32_t env_w = 0, env_h = 0;
+    bool has_env = false, has_cdf = false;
+    float env_intensity = 1.0f;
+    uint32_t map_w = 0, map_h = 0;
+    // acceleration structure
+    std::vector<BlasDesc> blas;
+    std::vector<ohao_pt_instance> instances;
+    bool built = false, two_level = false;
+    BvhDev flat;                          // flat BVH or TLAS
+    std::vector<BvhDev> blas_bvh;
+    DevBuf blas_nodes_all, blas_tris_all, blas_desc, inst_dev;
+    // scratch
+    DevBuf scratch, build_scratch, err_flag;
+    std::vector<DevBuf*> host_accum_bufs;
+    ohao_pt_profile profile{};
+    ~ohao_pt_ctx() {
+        for (auto* b : host_accum_bufs) delete b;
+    }
+};
+
+namespace {
+
+ohao_status fail(ohao_pt_ctx* c, ohao_status s, const std::string& msg) {
+    if (c) c->last_error = msg;
+    return s;
+}
+
+ohao_status cuda_fail(ohao_pt_ctx* c, cudaError_t e, const char* what) {
+    return fail(c, e == cudaErrorMemoryAllocation ? OHAO_ERR_OOM : OHAO_ERR_CUDA,
+                std::string(what) + ": " + cudaGetErrorString(e));
+}
+
+#define CK(expr, what)                                       \
+    do {                                                     \
+        cudaError_t e_ = (expr);                             \
+        if (e_ != cudaSuccess) return cuda_fail(ctx, e_, what); \
+    } while (0)
+
+ohao_status upload(ohao_pt_ctx* ctx, DevBuf& b, const void* src, size_t bytes, const char* what) {
+    CK(b.ensure(bytes), what);
+    if (bytes) CK(cudaMemcpy(b.p, src, bytes, cudaMemcpyHostToDevice), what);
+    return OHAO_OK;
+}
+
+void instance_matrices(const float x[12], float w2o[12], float nrm[9]) {
+    const double a = x[0], b = x[1], c = x[2], d = x[4], e = x[5], f = x[6], g = x[8], h = x[9], i = x[10];
+    const double A = e * i - f * h, B = -(d * i - f * g), C = d * h - e * g;
+    const double D = -(b * i - c * h), E = a * i - c * g, F = -(a * h - b * g);
+    const double G = b * f - c * e, H = -(a * f - c * d), I = a * e - b * d;
+    const double det = a * A + b * B + c * C;
+    const double inv[9] = {A / det, D / det, G / det, B / det, E / det, H / det, C / det, F / det, I / det};
+    const double t[3] = {x[3], x[7], x[11]};
+    for (int r = 0; r < 3; ++r) {
+        for (int k = 0; k < 3; ++k) w2o[r * 4 + k] = static_cast<float>(inv[r * 3 + k]);
+        w2o[r * 4 + 3] = static_cast<float>(-(inv[r * 3 + 0] * t[0] + inv[r * 3 + 1] * t[1] + inv[r * 3 + 2] * t[2]));
+    }
+    for (int r = 0; r < 3; ++r)
+        for (int k = 0; k < 3; ++k) nrm[r * 3 + k] = static_cast<float>(inv[k * 3 + r]);
+}
+
+void xform_point(const float m[12], const float p[3], float o[3]) {
+    for (int r = 0; r < 3; ++r) o[r] = ((m[r * 4 + 0] * p[0] + m[r * 4 + 1] * p[1]) + m[r * 4 + 2] * p[2]) + m[r * 4 + 3];
+}
+
+// World box of an instance: the 8 transformed corners of the BLAS box, padded
+// by 2^-20 of the coordinate magnitude so that rounding in the transform
+// cannot exclude geometry.
+void instance_world_box(const ohao_pt_instance& in, const float ob[6], float wb[6]) {
+    for (int a = 0; a < 3; ++a) { wb[a] = INFINITY; wb[3 + a] = -INFINITY; }
+    if (!(ob[0] <= ob[3])) return;
+    for (int c = 0; c < 8; ++c) {
+        const float p[3] = {(c & 1) ? ob[3] : ob[0], (c & 2) ? ob[4] : ob[1], (c & 4) ? ob[5] : ob[2]};
+        float w[3];
+        xform_point(in.transform, p, w);
+        for (int a = 0; a < 3; ++a) { wb[a] = std::min(wb[a], w[a]); wb[3 + a] = std::max(wb[3 + a], w[a]); }
+    }
+    for (int a = 0; a < 3; ++a) {
+        const float pad = (std::fabs(wb[a]) + std::fabs(wb[3 + a])) * 0x1p-20f;
+        wb[a] = wb[a] - pad;
+        wb[3 + a] = wb[3 + a] + pad;
+    }
+}
+
+ohao_status build_one(ohao_pt_ctx* ctx, const float* d_boxes, uint32_t n, BvhDev& out, cudaStream_t st) {
+    std::string err;
+    const size_t need = ohao::bvh_build_scratch_bytes(n);
+    CK(ctx->build_scratch.ensure(need), "BVH scratch");
+    CK(out.nodes.ensure(static_cast<size_t>(std::max(n, 1u)) * 80), "BVH nodes");
+    DevBuf order_tmp;
+    CK(order_tmp.ensure(static_cast<size_t>(std::max(n, 1u)) * 4), "BVH order");
+    DevBuf rb;
+    CK(rb.ensure(32), "BVH root box");
+    ohao::BvhBuildInfo info{};
+    const ohao_status s = ohao::bvh_build(d_boxes, n, ctx->build_scratch.p, ctx->build_scratch.n, out.nodes.as<uint4>(),
+                                          order_tmp.as<uint32_t>(), rb.as<float>(), &info, st, err);
+    if (s != OHAO_OK) return fail(ctx, s, err);
+    out.nnodes = info.nnodes;
+    out.height = info.height;
+    out.nprims = n;
+    if (n) CK(cudaMemcpy(out.root_box, rb.p, 24, cudaMemcpyDeviceToHost), "BVH root box");
+    // keep the order in prims temporarily (caller gathers records)
+    std::swap(out.prims.p, order_tmp.p);
+    std::swap(out.prims.n, order_tmp.n);
+    return OHAO_OK;
+}
+
+ohao::DScene make_scene(const ohao_pt_ctx* c) {
+    ohao::DScene s{};
+    s.nodes = c->flat.nodes.as<uint4>();
+    s.nnodes = c->flat.nnodes;
+    s.two_level = c->two_level ? 1 : 0;
+    if (c->two_level) {
+        s.tris = nullptr;
+        s.tlas_inst = c->flat.prims.as<uint32_t>();
+    } else {
+        s.tris = c->flat.prims.as<float4>();
+        s.tlas_inst = nullptr;
+    }
+    s.blas = c->blas_desc.as<ohao::DBlas>();
+    s.blas_nodes = c->blas_nodes_all.as<uint4>();
+    s.blas_tris = c->blas_tris_all.as<float4>();
+    s.inst = c->inst_dev.as<ohao::DInst>();
+    s.indices = c->indices.as<uint32_t>();
+    s.normals = c->normals.as<float4>();
+    s.uvs = c->uvs.as<float2>();
+    s.mat_ids = c->mat_ids.as<uint32_t>();
+    s.mats = c->mats.as<float4>();
+    s.lights = c->lights.as<float4>();
+    s.nlights = c->nlights;
+    s.env = c->env.as<float4>();
+    s.env_w = c->env_w;
+    s.env_h = c->env_h;
+    s.marg = c->marg.as<float>();
+    s.cond = c->cond.as<float>();
+    s.env_intensity = c->env_intensity;
+    s.has_env = c->has_env ? 1 : 0;
+    s.has_cdf = c->has_cdf ? 1 : 0;
+    s.albedo_map = c->albedo_map.as<float>();
+    s.map_w = c->map_w;
+    s.map_h = c->map_h;
+    return s;
+}
+
+ohao_status check_device_error(ohao_pt_ctx* ctx, cudaStream_t st) {
+    int flag = 0;
+    CK(cudaMemcpyAsync(&flag, ctx->err_flag.p, sizeof(int), cudaMemcpyDeviceToHost, st), "error flag");
+    CK(cudaStreamSynchronize(st), "stream sync");
+    if (flag) {
+        cudaMemsetAsync(ctx->err_flag.p, 0, sizeof(int), st);
+        return fail(ctx, OHAO_ERR_DEVICE_CHECK, "traversal stack limit exceeded on the device");
+    }
+    return OHAO_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+const char* ohao_pt_version(void) { return "ohao-gb300-pt 0.1 (sm_103a)"; }
+
+ohao_status ohao_pt_create(const ohao_pt_desc* desc, ohao_pt_ctx** out) {
+    if (!out) return OHAO_ERR_INVALID_ARG;
+    *out = nullptr;
+    auto* ctx = new (std::nothrow) ohao_pt_ctx();
+    if (!ctx) return OHAO_ERR_OOM;
+    if (desc) {
+        ctx->device = desc->device;
+        if (desc->flatten_limit) ctx->flatten_limit = desc->flatten_limit;
+    }
+    cudaError_t e = cudaSetDevice(ctx->device);
+    if (e != cudaSuccess) {
+        delete ctx;
+        return OHAO_ERR_CUDA;
+    }
+    e = ctx->err_flag.ensure(256);
+    if (e == cudaSuccess) e = cudaMemset(ctx->err_flag.p, 0, 256);
+    if (e != cudaSuccess) {
+        delete ctx;
+        return OHAO_ERR_CUDA;
+    }
+    ohao::upload_sobol_table(kSobolDirs);
+    *out = ctx;
+    return OHAO_OK;
+}
+
+void ohao_pt_destroy(ohao_pt_ctx* ctx) {
+    if (!ctx) return;
+    cudaSetDevice(ctx->device);
+    delete ctx;
+}
+
+const char* ohao_pt_last_error(const ohao_pt_ctx* ctx) { return ctx ? ctx->last_error.c_str() : "null context"; }
+
+ohao_status ohao_pt_set_geometry(ohao_pt_ctx* ctx, const float* pos, uint32_t pos_stride_bytes, uint32_t nverts,
+                                 const float* normal4, const float* uv2, const uint32_t* indices, uint32_t ntris,
+                                 const uint32_t* mat_ids) {
+    if (!ctx) return OHAO_ERR_INVALID_ARG;
+    if ((nverts && (!pos || !normal4)) || (ntris && (!indices || !mat_ids)) || pos_stride_bytes < 12)
+        return fail(ctx, OHAO_ERR_INVALID_ARG, "set_geometry: null array or stride < 12");
+    for (size_t i = 0; i < static_cast<size_t>(ntris) * 3; ++i)
+        if (indices[i] >= nverts) return fail(ctx, OHAO_ERR_INVALID_ARG, "set_geometry: index out of range");
+    ctx->host_pos.resize(static_cast<size_t>(nverts) * 3);
+    const auto* pb = reinterpret_cast<const uint8_t*>(pos);
+    for (uint32_t i = 0; i < nverts; ++i) std::memcpy(&ctx->host_pos[3 * static_cast<size_t>(i)], pb + static_cast<size_t>(i) * pos_stride_bytes, 12);
+    ctx->host_indices.assign(indices, indices + static_cast<size_t>(ntris) * 3);
+    std::vector<float> uvz;
+    if (!uv2) uvz.assign(static_cast<size_t>(nverts) * 2, 0.0f);
+    ohao_status s;
+    if ((s = upload(ctx, ctx->pos, ctx->host_pos.data(), ctx->host_pos.size() * 4, "positions")) != OHAO_OK) return s;
+    if ((s = upload(ctx, ctx->normals, normal4, static_cast<size_t>(nverts) * 16, "normals")) != OHAO_OK) return s;
+    if ((s = upload(ctx, ctx->uvs, uv2 ? uv2 : uvz.data(), static_cast<size_t>(nverts) * 8, "uvs")) != OHAO_OK) return s;
+    if ((s = upload(ctx, ctx->indices, indices, static_cast<size_t>(ntris) * 12, "indices")) != OHAO_OK) return s;
+    if ((s = upload(ctx, ctx->mat_ids, mat_ids, static_cast<size_t>(ntris) * 4, "material ids")) != OHAO_OK) return s;
+    ctx->nverts = nverts;
+    ctx->ntris = ntris;
+    ctx->built = false;
+    return OHAO_OK;
+}
+
+ohao_status ohao_pt_create_blas(ohao_pt_ctx* ctx, uint32_t first_index, uint32_t index_count, uint32_t* out_blas) {
+    if (!ctx || !out_blas) return OHAO_ERR_INVALID_ARG;
+    *out_blas = 0xFFFFFFFFu;   // INVALID_BLAS
+    if (index_count % 3 != 0 || static_cast<uint64_t>(first_index) + index_count > static_cast<uint64_t>(ctx->ntris) * 3)
+        return fail(ctx, OHAO_ERR_INVALID_ARG, "create_blas: index range outside the geometry");
+    ctx->blas.push_back({first_index, index_count});
+    *out_blas = static_cast<uint32_t>(ctx->blas.size() - 1);
+    ctx->built = false;
+    return OHAO_OK;
+}
+
+ohao_status ohao_pt_set_instances(ohao_pt_ctx* ctx, const ohao_pt_instance* inst, uint32_t n) {
+    if (!ctx || (n && !inst)) return OHAO_ERR_INVALID_ARG;
+    for (uint32_t i = 0; i < n; ++i)
+        if (inst[i].blas >= ctx->blas.size()) return fail(ctx, OHAO_ERR_INVALID_ARG, "set_instances: unknown BLAS handle");
+    ctx->instances.assign(inst, inst + n);
+    ctx->built = false;
+    return OHAO_OK;
+}
+
+int32_t ohao_pt_is_two_level(const ohao_pt_ctx* ctx) { return ctx && ctx->two_level ? 1 : 0; }
+
+ohao_status ohao_pt_build(ohao_pt_ctx* ctx, ohao_stream stream) {
+    if (!ctx) return OHAO_ERR_INVALID_ARG;
+    cudaStream_t st = reinterpret_cast<cudaStream_t>(stream);
+    CK(cudaSetDevice(ctx->device), "set device");
+    const uint32_t ninst = static_cast<uint32_t>(ctx->instances.size());
+    // per-instance device records
+    std::vector<ohao::DInst> di(std::max(ninst, 1u));
+    for (uint32_t i = 0; i < ninst; ++i) {
+        instance_matrices(ctx->instances[i].transform, di[i].w2o, di[i].nrm);
+        di[i].custom = ctx->instances[i].custom_index;
+        di[i].blas = ctx->instances[i].blas;
+        di[i].mask = ctx->instances[i].mask;
+    }
+    ohao_status s = upload(ctx, ctx->inst_dev, di.data(), di.size() * sizeof(ohao::DInst), "instances");
+    if (s != OHAO_OK) return s;
+    uint64_t total = 0;
+    for (const auto& in : ctx->instances)
+        if (in.mask & 0xFFu) total += ctx->blas[in.blas].index_count / 3;
+    if (total >= (1ull << 31) && total <= ctx->flatten_limit)
+        return fail(ctx, OHAO_ERR_UNSUPPORTED, "build: more than 2^31 instanced triangles in a flat BVH");
+    ctx->two_level = total > ctx->flatten_limit;
+    ctx->blas_bvh.clear();
+    DevBuf tv, tinst, tprim, boxes;
+    if (!ctx->two_level) {
+        const uint32_t n = static_cast<uint32_t>(total);
+        std::vector<uint32_t> first_index, tri_off, vis;
+        std::vector<float> o2w;
+        uint32_t acc = 0;
+        for (uint32_t i = 0; i < ninst; ++i) {
+            const auto& in = ctx->instances[i];
+            if (!(in.mask & 0xFFu)) continue;
+            vis.push_back(i);
+            first_index.push_back(ctx->blas[in.blas].first_index);
+            tri_off.push_back(acc);
+            acc += ctx->blas[in.blas].index_count / 3;
+            o2w.insert(o2w.end(), in.transform, in.transform + 12);
+        }
+        DevBuf dfi, dto, do2w;
+        if ((s = upload(ctx, dfi, first_index.data(), first_index.size() * 4, "build")) != OHAO_OK) return s;
+        if ((s = upload(ctx, dto, tri_off.data(), tri_off.size() * 4, "build")) != OHAO_OK) return s;
+        if ((s = upload(ctx, do2w, o2w.data(), o2w.size() * 4, "build")) != OHAO_OK) return s;
+        CK(tv.ensure(static_cast<size_t>(std::max(n, 1u)) * 36), "build");
+        CK(tinst.ensure(static_cast<size_t>(std::max(n, 1u)) * 4), "build");
+        CK(tprim.ensure(static_cast<size_t>(std::max(n, 1u)) * 4), "build");
+        CK(boxes.ensure(static_cast<size_t>(std::max(n, 1u)) * 24), "build");
+        ohao::launch_flat_triangles(ctx->pos.as<float>(), ctx->indices.as<uint32_t>(), dfi.as<uint32_t>(),
+                                    dto.as<uint32_t>(), do2w.as<float>(), static_cast<uint32_t>(vis.size()), n,
+                                    tv.as<float>(), tinst.as<uint32_t>(), tprim.as<uint32_t>(), boxes.as<float>(), st);
+        // map the visible-instance index back to the instance id
+        if (vis.size() != ninst) {
+            std::vector<uint32_t> h_inst(n);
+            CK(cudaMemcpyAsync(h_inst.data(), tinst.p, static_cast<size_t>(n) * 4, cudaMemcpyDeviceToHost, st), "build");
+            CK(cudaStreamSynchronize(st), "build");
+            for (auto& v : h_inst) v = vis[v];
+            CK(cudaMemcpy(tinst.p, h_inst.data(), static_cast<size_t>(n) * 4, cudaMemcpyHostToDevice), "build");
+        }
+        if ((s = build_one(ctx, boxes.as<float>(), n, ctx->flat, st)) != OHAO_OK) return s;
+        DevBuf recs;
+        CK(recs.ensure(static_cast<size_t>(std::max(n, 1u)) * 48), "build");
+        ohao::launch_gather_records(tv.as<float>(), tinst.as<uint32_t>(), tprim.as<uint32_t>(),
+                                    ctx->flat.prims.as<uint32_t>(), n, recs.as<float4>(), st);
+        CK(cudaStreamSynchronize(st), "build");
+        std::swap(ctx->flat.prims.p, recs.p);
+        std::swap(ctx->flat.prims.n, recs.n);
+        CK(ctx->blas_desc.ensure(sizeof(ohao::DBlas)), "build");
+    } else {
+        // BLAS builds
+        const uint32_t nb = static_cast<uint32_t>(ctx->blas.size());
+        ctx->blas_bvh.resize(nb);
+        std::vector<ohao::DBlas> desc(nb);
+        uint64_t node_total = 0, tri_total = 0;
+        for (uint32_t b = 0; b < nb; ++b) {
+            const uint32_t n = ctx->blas[b].index_count / 3;
+            CK(tv.ensure(static_cast<size_t>(std::max(n, 1u)) * 36), "build");
+            CK(tinst.ensure(static_cast<size_t>(std::max(n, 1u)) * 4), "build");
+            CK(tprim.ensure(static_cast<size_t>(std::max(n, 1u)) * 4), "build");
+            CK(boxes.ensure(static_cast<size_t>(std::max(n, 1u)) * 24), "build");
+            ohao::launch_blas_triangles(ctx->pos.as<float>(), ctx->indices.as<uint32_t>(), ctx->blas[b].first_index, n,
+                                        tv.as<float>(), tinst.as<uint32_t>(), tprim.as<uint32_t>(), boxes.as<float>(), st);
+            BvhDev& bv = ctx->blas_bvh[b];
+            if ((s = build_one(ctx, boxes.as<float>(), n, bv, st)) != OHAO_OK) return s;
+            DevBuf recs;
+            CK(recs.ensure(static_cast<size_t>(std::max(n, 1u)) * 48), "build");
+            ohao::launch_gather_records(tv.as<float>(), tinst.as<uint32_t>(), tprim.as<uint32_t>(), bv.prims.as<uint32_t>(),
+                                        n, recs.as<float4>(), st);
+            CK(cudaStreamSynchronize(st), "build");
+            std::swap(bv.prims.p, recs.p);
+            std::swap(bv.prims.n, recs.n);
+            desc[b] = {static_cast<uint32_t>(node_total), static_cast<uint32_t>(tri_total), bv.nnodes, n};
+            node_total += bv.nnodes;
+            tri_total += n;
+        }
+        CK(ctx->blas_nodes_all.ensure(std::max<uint64_t>(node_total, 1) * 80), "build");
+        CK(ctx->blas_tris_all.ensure(std::max<uint64_t>(tri_total, 1) * 48), "build");
+        for (uint32_t b = 0; b < nb; ++b) {
+            const BvhDev& bv = ctx->blas_bvh[b];
+            if (bv.nnodes)
+                CK(cudaMemcpyAsync(ctx->blas_nodes_all.as<char>() + static_cast<size_t>(desc[b].node_off) * 80, bv.nodes.p,
+                                   static_cast<size_t>(bv.nnodes) * 80, cudaMemcpyDeviceToDevice, st), "build");
+            if (bv.nprims)
+                CK(cudaMemcpyAsync(ctx->blas_tris_all.as<char>() + static_cast<size_t>(desc[b].tri_off) * 48, bv.prims.p,
+                                   static_cast<size_t>(bv.nprims) * 48, cudaMemcpyDeviceToDevice, st), "build");
+        }
+        if ((s = upload(ctx, ctx->blas_desc, desc.data(), desc.size() * sizeof(ohao::DBlas), "build")) != OHAO_OK) return s;
+        // TLAS over visible instances' world boxes
+        std::vector<float> ib;
+        std::vector<uint32_t> ids;
+        for (uint32_t i = 0; i < ninst; ++i) {
+            const auto& in = ctx->instances[i];
+            if (!(in.mask & 0xFFu) || ctx->blas_bvh[in.blas].nprims == 0) continue;
+            float wb[6];
+            const BvhDev& bv = ctx->blas_bvh[in.blas];
+            float ob[6];
+            if (bv.nprims) std::memcpy(ob, bv.root_box, 24);
+            else { ob[0] = ob[1] = ob[2] = INFINITY; ob[3] = ob[4] = ob[5] = -INFINITY; }
+            instance_world_box(in, ob, wb);
+            ib.insert(ib.end(), wb, wb + 6);
+            ids.push_back(i);
+        }
+        DevBuf dib;
+        if ((s = upload(ctx, dib, ib.data(), ib.size() * 4, "build")) != OHAO_OK) return s;
+        const uint32_t ni = static_cast<uint32_t>(ids.size());
+        if ((s = build_one(ctx, dib.as<float>(), ni, ctx->flat, st)) != OHAO_OK) return s;
+        std::vector<uint32_t> order(ni);
+        if (ni) CK(cudaMemcpy(order.data(), ctx->flat.prims.p, static_cast<size_t>(ni) * 4, cudaMemcpyDeviceToHost), "build");
+        for (auto& v : order) v = ids[v];
+        if (ni) CK(cudaMemcpy(ctx->flat.prims.p, order.data(), static_cast<size_t>(ni) * 4, cudaMemcpyHostToDevice), "build");
+    }
+    CK(cudaStreamSynchronize(st), "build");
+    ctx->built = true;
+    return OHAO_OK;
+}
+
+ohao_status ohao_pt_set_materials(ohao_pt_ctx* ctx, const float* m, uint32_t n) {
+    if (!ctx || (n && !m)) return OHAO_ERR_INVALID_ARG;
+    for (uint32_t i = 0; i < n; ++i) {
+        uint32_t tex[4];
+        std::memcpy(&tex[0], m + 12 * static_cast<size_t>(i) + 3, 4);   // diffuse
+        std::memcpy(&tex[1], m + 12 * static_cast<size_t>(i) + 6, 4);   // normal
+        std::memcpy(&tex[2], m + 12 * static_cast<size_t>(i) + 7, 4);   // emissive
+        std::memcpy(&tex[3], m + 12 * static_cast<size_t>(i) + 8, 4);   // rough/metal
+        if ((tex[0] != 0xFFFFFFFFu && tex[0] != 0u) || tex[1] != 0xFFFFFFFFu || tex[2] != 0xFFFFFFFFu || tex[3] != 0xFFFFFFFFu)
+            return fail(ctx, OHAO_ERR_UNSUPPORTED, "set_materials: bindless textures are not supported (only diffuse slot 0 = tile albedo map)");
+    }
+    ohao_status s = upload(ctx, ctx->mats, m, static_cast<size_t>(n) * 48, "materials");
+    if (s == OHAO_OK) ctx->nmats = n;
+    return s;
+}
+
+ohao_status ohao_pt_update_materials(ohao_pt_ctx* ctx, const float* m, uint32_t first, uint32_t n) {
+    if (!ctx || (n && !m)) return OHAO_ERR_INVALID_ARG;
+    if (static_cast<uint64_t>(first) + n > ctx->nmats) return fail(ctx, OHAO_ERR_INVALID_ARG, "update_materials: range outside the table");
+    if (n) CK(cudaMemcpy(ctx->mats.as<char>() + static_cast<size_t>(first) * 48, m, static_cast<size_t>(n) * 48, cudaMemcpyHostToDevice), "materials");
+    return OHAO_OK;
+}
+
+ohao_status ohao_pt_set_lights(ohao_pt_ctx* ctx, const ohao_gpu_light* l, uint32_t n) {
+    if (!ctx || (n && !l)) return OHAO_ERR_INVALID_ARG;
+    if (n > 64) return fail(ctx, OHAO_ERR_INVALID_ARG, "set_lights: at most 64 lights (MAX_GPU_LIGHTS)");
+    ohao_status s = upload(ctx, ctx->lights, l, static_cast<size_t>(n) * 80, "lights");
+    if (s == OHAO_OK) ctx->nlights = n;
+    return s;
+}
+
+ohao_status ohao_pt_set_env(ohao_pt_ctx* ctx, const float* rgba, uint32_t w, uint32_t h, const float* marg,
+                            const float* cond, float integral, float intensity) {
+    if (!ctx) return OHAO_ERR_INVALID_ARG;
+    (void)integral;
+    if (!rgba || w == 0 || h == 0) {
+        ctx->has_env = ctx->has_cdf = false;
+        ctx->env_w = ctx->env_h = 0;
+        return OHAO_OK;
+    }
+    ohao_status s = upload(ctx, ctx->env, rgba, static_cast<size_t>(w) * h * 16, "env");
+    if (s != OHAO_OK) return s;
+    ctx->has_cdf = marg && cond;
+    if (ctx->has_cdf) {
+        if ((s = upload(ctx, ctx->marg, marg, static_cast<size_t>(h) * 4, "env marginal")) != OHAO_OK) return s;
+        if ((s = upload(ctx, ctx->cond, cond, static_cast<size_t>(w) * h * 4, "env conditional")) != OHAO_OK) return s;
+    }
+    ctx->has_env = true;
+    ctx->env_w = w;
+    ctx->env_h = h;
+    ctx->env_intensity = intensity;
+    return OHAO_OK;
+}
+
+ohao_status ohao_pt_set_albedo_map(ohao_pt_ctx* ctx, const float* rgb, uint32_t w, uint32_t h) {
+    if (!ctx) return OHAO_ERR_INVALID_ARG;
+    if (!rgb || !w || !h) { ctx->map_w = ctx->map_h = 0; return OHAO_OK; }
+    ohao_status s = upload(ctx, ctx->albedo_map, rgb, static_cast<size_t>(w) * h * 12, "albedo map");
+    if (s == OHAO_OK) { ctx->map_w = w; ctx->map_h = h; }
+    return s;
+}
+
+ohao_status ohao_env_cdf_build(const float* px, int32_t w, int32_t h, float* marg, float* cond, float* integral) {
+    if (!px || !marg || !cond || !integral || w <= 0 || h <= 0) return OHAO_ERR_INVALID_ARG;
+    std::vector<float> rowSum(static_cast<size_t>(h), 0.0f);
+    const float kPi = 3.14159265358979323846f;
+    for (int y = 0; y < h; ++y) {
+        const float theta = kPi * (float(y) + 0.5f) / float(h);
+        const float sinT = std::sin(theta);
+        float acc = 0.0f;
+        for (int x = 0; x < w; ++x) {
+            const float* p = px + (static_cast<size_t>(y) * w + x) * 4;
+            const float lw = (0.2126f * p[0] + 0.7152f * p[1] + 0.0722f * p[2]) * sinT;
+            acc += lw;
+            cond[static_cast<size_t>(y) * w + x] = acc;
+        }
+        if (acc > 0.0f) {
+            for (int x = 0; x < w; ++x) cond[static_cast<size_t>(y) * w + x] /= acc;
+        } else {
+            for (int x = 0; x < w; ++x) cond[static_cast<size_t>(y) * w + x] = float(x + 1) / float(w);
+        }
+        rowSum[static_cast<size_t>(y)] = acc;
+    }
+    float total = 0.0f;
+    for (int y = 0; y < h; ++y) { total += rowSum[static_cast<size_t>(y)]; marg[y] = total; }
+    *integral = total;
+    if (total > 0.0f) for (int y = 0; y < h; ++y) marg[y] /= total;
+    else for (int y = 0; y < h; ++y) marg[y] = float(y + 1) / float(h);
+    return OHAO_OK;
+}
+
+static ohao_status validate_render(ohao_pt_ctx* ctx, const ohao_pt_view* views, uint32_t n_views,
+                                   const ohao_pt_settings* st) {
+    if (!ctx || !views || !st || n_views == 0) return fail(ctx, OHAO_ERR_INVALID_ARG, "render: null argument");
+    if (!ctx->built) return fail(ctx, OHAO_ERR_NOT_BUILT, "render before ohao_pt_build");
+    if (st->spp == 0) return fail(ctx, OHAO_ERR_INVALID_ARG, "render: spp must be >= 1");
+    if (st->max_bounces > 64) return fail(ctx, OHAO_ERR_INVALID_ARG, "render: max_bounces > 64");
+    if (st->sampler > 1) return fail(ctx, OHAO_ERR_INVALID_ARG, "render: unknown sampler");
+    if (st->mode == OHAO_PT_MODE_PERSISTENT) return fail(ctx, OHAO_ERR_UNSUPPORTED, "render: persistent mode not built yet");
+    for (uint32_t v = 0; v < n_views; ++v)
+        if (views[v].width == 0 || views[v].height == 0 || static_cast<uint64_t>(views[v].width) * views[v].height > (1ull << 31))
+            return fail(ctx, OHAO_ERR_INVALID_ARG, "render: bad view size");
+    return OHAO_OK;
+}
+
+static ohao_status render_views(ohao_pt_ctx* ctx, const ohao_pt_view* views, uint32_t n_views,
+                                const ohao_pt_settings* st, float* const* dev_accum, cudaStream_t cs) {
+    const bool profile = (st->flags & OHAO_PT_FLAG_PROFILE) != 0;
+    ohao::ProfileAcc acc;
+    const uint32_t cap = ohao::wavefront_default_capacity();
+    CK(ctx->scratch.ensure(ohao::wavefront_scratch_bytes(cap)), "render scratch");
+    ohao::DScene sc = make_scene(ctx);
+    ohao::PathParams pp{st->max_bounces, st->sampler, st->flags, st->clamp_luminance, st->aniso_strength,
+                        st->aniso_rotation, st->sample_index_base};
+    for (uint32_t v = 0; v < n_views; ++v) {
+        ohao::RenderView rv{};
+        std::memcpy(rv.vp.inv_view, views[v].inv_view, 64);
+        std::memcpy(rv.vp.inv_proj, views[v].inv_proj, 64);
+        rv.vp.width = views[v].width;
+        rv.vp.height = views[v].height;
+        rv.accum = dev_accum[v];
+        rv.history = views[v].history;
+        rv.path_out = views[v].path_radiance;
+        rv.aov = views[v].aov;
+        std::string err;
+        const ohao_status s = ohao::wavefront_render(sc, rv, pp, st->spp, ctx->scratch.p, ctx->scratch.n, cap, cs,
+                                                     profile, &acc, ctx->err_flag.as<int>(), err);
+        if (s != OHAO_OK) return fail(ctx, s, err);
+    }
+    if (profile) {
+        ohao_pt_profile& p = ctx->profile;
+        p.extend_ms = acc.extend_ms; p.shade_ms = acc.shade_ms; p.shadow_ms = acc.shadow_ms;
+        p.other_ms = acc.other_ms; p.total_ms = acc.total_ms;
+        p.extend_launches = acc.extend_launches; p.shade_launches = acc.shade_launches;
+        p.shadow_launches = acc.shadow_launches; p.other_launches = acc.other_launches;
+    }
+    return OHAO_OK;
+}
+
+ohao_status ohao_pt_render(ohao_pt_ctx* ctx, const ohao_pt_view* views, uint32_t n_views,
+                           const ohao_pt_settings* st, ohao_stream stream) {
+    ohao_status s = validate_render(ctx, views, n_views, st);
+    if (s != OHAO_OK) return s;
+    std::vector<float*> acc(n_views);
+    for (uint32_t v = 0; v < n_views; ++v) {
+        if (!views[v].accum) return fail(ctx, OHAO_ERR_INVALID_ARG, "render: view accum is null (use ohao_pt_render_host)");
+        acc[v] = views[v].accum;
+    }
+    cudaStream_t cs = reinterpret_cast<cudaStream_t>(stream);
+    CK(cudaSetDevice(ctx->device), "set device");
+    if ((s = render_views(ctx, views, n_views, st, acc.data(), cs)) != OHAO_OK) return s;
+    return check_device_error(ctx, cs);
+}
+
+ohao_status ohao_pt_render_host(ohao_pt_ctx* ctx, const ohao_pt_view* views, uint32_t n_views,
+                                const ohao_pt_settings* st, float* const* host_accum, ohao_stream stream) {
+    ohao_status s = validate_render(ctx, views, n_views, st);
+    if (s != OHAO_OK) return s;
+    if (!host_accum) return fail(ctx, OHAO_ERR_INVALID_ARG, "render_host: null host_accum");
+    cudaStream_t cs = reinterpret_cast<cudaStream_t>(stream);
+    CK(cudaSetDevice(ctx->device), "set device");
+    while (ctx->host_accum_bufs.size() < n_views) ctx->host_accum_bufs.push_back(new DevBuf());
+    std::vector<float*> acc(n_views);
+    for (uint32_t v = 0; v < n_views; ++v) {
+        if (!host_accum[v]) return fail(ctx, OHAO_ERR_INVALID_ARG, "render_host: null host buffer");
+        const size_t bytes = static_cast<size_t>(views[v].width) * views[v].height * 16;
+        CK(ctx->host_accum_bufs[v]->ensure(bytes), "host accum");
+        acc[v] = ctx->host_accum_bufs[v]->as<float>();
+        if (views[v].history > 0)
+            CK(cudaMemcpyAsync(acc[v], host_accum[v], bytes, cudaMemcpyHostToDevice, cs), "accum upload");
+    }
+    if ((s = render_views(ctx, views, n_views, st, acc.data(), cs)) != OHAO_OK) return s;
+    for (uint32_t v = 0; v < n_views; ++v) {
+        const size_t bytes = static_cast<size_t>(views[v].width) * views[v].height * 16;
+        CK(cudaMemcpyAsync(host_accum[v], acc[v], bytes, cudaMemcpyDeviceToHost, cs), "accum download");
+    }
+    return check_device_error(ctx, cs);
+}
+
+ohao_status ohao_pt_get_profile(const ohao_pt_ctx* ctx, ohao_pt_profile* out) {
+    if (!ctx || !out) return OHAO_ERR_INVALID_ARG;
+    *out = ctx->profile;
+    return OHAO_OK;
+}
+
+ohao_status ohao_pt_trace(ohao_pt_ctx* ctx, const float* rays, uint32_t n, uint32_t* hits, int32_t any_hit,
+                          uint32_t* stats, ohao_stream stream) {
+    if (!ctx || (n && (!rays || !hits))) return OHAO_ERR_INVALID_ARG;
+    if (!ctx->built) return fail(ctx, OHAO_ERR_NOT_BUILT, "trace before ohao_pt_build");
+    cudaStream_t cs = reinterpret_cast<cudaStream_t>(stream);
+    CK(cudaSetDevice(ctx->device), "set device");
+    std::string err;
+    const ohao_status s = ohao::trace_rays(make_scene(ctx), rays, n, hits, any_hit, stats, cs, ctx->err_flag.as<int>(), err);
+    if (s != OHAO_OK) return fail(ctx, s, err);
+    return check_device_error(ctx, cs);
+}
+
+ohao_status ohao_pt_bvh_info(const ohao_pt_ctx* ctx, int32_t which, uint32_t* n_nodes, uint32_t* n_prims,
+                             uint32_t* height) {
+    if (!ctx || !n_nodes || !n_prims || !height) return OHAO_ERR_INVALID_ARG;
+    if (!ctx->built) return OHAO_ERR_NOT_BUILT;
+    const BvhDev* b;
+    if (which < 0) b = &ctx->flat;
+    else if (ctx->two_level && static_cast<size_t>(which) < ctx->blas_bvh.size()) b = &ctx->blas_bvh[which];
+    else return OHAO_ERR_INVALID_ARG;
+    *n_nodes = b->nnodes;
+    *n_prims = b->nprims;
+    *height = b->height;
+    return OHAO_OK;
+}
+
+ohao_status ohao_pt_bvh_download(ohao_pt_ctx* ctx, int32_t which, void* nodes, void* prims) {
+    uint32_t nn, np, h;
+    ohao_status s = ohao_pt_bvh_info(ctx, which, &nn, &np, &h);
+    if (s != OHAO_OK) return s;
+    const BvhDev* b = which < 0 ? &ctx->flat : &ctx->blas_bvh[which];
+    const size_t pbytes = (which < 0 && ctx->two_level) ? 4 : 48;
+    if (nn && nodes) CK(cudaMemcpy(nodes, b->nodes.p, static_cast<size_t>(nn) * 80, cudaMemcpyDeviceToHost), "download");
+    if (np && prims) CK(cudaMemcpy(prims, b->prims.p, static_cast<size_t>(np) * pbytes, cudaMemcpyDeviceToHost), "download");
+    return OHAO_OK;
+}
+
+}  // extern "C"

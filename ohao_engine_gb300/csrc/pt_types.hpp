@@ -1,0 +1,94 @@
+// pt_types.hpp -- plain-old-data shared by the host context and the kernels.
+#pragma once
+#include <cstddef>
+#include <cstdint>
+#include <string>
+
+#include <cuda_runtime.h>
+
+#include "../../include/ohao_pt.h"
+
+namespace ohao {
+
+struct DInst {          // per instance, 96 bytes
+    float w2o[12];      // world-to-object 3x4, row-major
+    float nrm[9];       // transpose(inverse(mat3(object-to-world))), row-major
+    uint32_t custom;
+    uint32_t blas;
+    uint32_t mask;
+};
+static_assert(sizeof(DInst) == 96, "DInst layout");
+
+struct DBlas {
+    uint32_t node_off, tri_off, nnodes, ntris;
+};
+
+struct DScene {
+    // flat BVH, or the TLAS when two_level
+    const uint4* nodes;
+    const float4* tris;
+    const uint32_t* tlas_inst;
+    uint32_t nnodes;
+    int two_level;
+    const DBlas* blas;
+    const uint4* blas_nodes;
+    const float4* blas_tris;
+    const DInst* inst;
+    // shading data
+    const uint32_t* indices;
+    const float4* normals;
+    const float2* uvs;
+    const uint32_t* mat_ids;
+    const float4* mats;
+    const float4* lights;
+    uint32_t nlights;
+    const float4* env;
+    uint32_t env_w, env_h;
+    const float* marg;
+    const float* cond;
+    float env_intensity;
+    int has_env, has_cdf;
+    const float* albedo_map;
+    uint32_t map_w, map_h;
+};
+
+struct PathParams {
+    uint32_t max_bounces;
+    uint32_t sampler;
+    uint32_t flags;
+    float clamp_lum;
+    float aniso, aniso_rot;
+    uint32_t sample_base;
+};
+
+struct ViewParams {
+    float inv_view[16];
+    float inv_proj[16];
+    uint32_t width, height;
+};
+
+struct RenderView {
+    ViewParams vp;
+    float* accum;        // device RGBA32F
+    uint32_t history;
+    float* path_out;     // device [spp][npix][4] or null
+    float* aov;          // device [npix][8] or null
+};
+
+struct ProfileAcc {
+    float extend_ms = 0, shadow_ms = 0, shade_ms = 0, other_ms = 0, total_ms = 0;
+    uint32_t extend_launches = 0, shadow_launches = 0, shade_launches = 0, other_launches = 0;
+    uint64_t rays_closest = 0, rays_shadow = 0;
+};
+
+// wavefront.cu
+void upload_sobol_table(const uint32_t* dirs128);
+size_t wavefront_scratch_bytes(uint32_t capacity);
+uint32_t wavefront_default_capacity();
+ohao_status wavefront_render(const DScene& sc, const RenderView& view, const PathParams& pp, uint32_t spp,
+                             void* scratch, size_t scratch_bytes, uint32_t capacity, cudaStream_t st, bool profile,
+                             ProfileAcc* prof, int* d_err, std::string& err);
+ohao_status trace_rays(const DScene& sc, const float* rays, uint32_t n, uint32_t* hits, int any_hit, uint32_t* stats,
+                       cudaStream_t st, int* d_err, std::string& err);
+
+}  // namespace ohao

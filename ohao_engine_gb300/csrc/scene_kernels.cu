@@ -1,0 +1,109 @@
+// scene_kernels.cu -- triangle preparation for the BVH builds.
+//
+// Flat mode transforms every visible instance's triangles to world space
+// (x' = ((m0*x + m1*y) + m2*z) + m3 per row, the instance transform of
+// buildTLAS, rt_acceleration_structure.cpp:437-445); BLAS mode reads the
+// object-space triangles of one createBLAS index range
+// (rt_acceleration_structure.cpp:205-300). Boxes are per-triangle min/max.
+#include "bvh_internal.hpp"
+
+namespace ohao {
+
+namespace {
+
+__device__ __forceinline__ void tri_box(const float v[9], float* box) {
+#pragma unroll
+    for (int a = 0; a < 3; ++a) {
+        box[a] = fminf(fminf(v[a], v[3 + a]), v[6 + a]);
+        box[3 + a] = fmaxf(fmaxf(v[a], v[3 + a]), v[6 + a]);
+    }
+}
+
+__global__ void k_flat_tris(const float* __restrict__ pos, const uint32_t* __restrict__ indices,
+                            const uint32_t* __restrict__ inst_first_index, const uint32_t* __restrict__ inst_tri_offset,
+                            const float* __restrict__ o2w, uint32_t n_inst, uint32_t total, float* __restrict__ tv,
+                            uint32_t* __restrict__ tinst, uint32_t* __restrict__ tprim, float* __restrict__ boxes) {
+    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= total) return;
+    // last instance whose offset <= i
+    uint32_t lo = 0, hi = n_inst - 1;
+    while (lo < hi) {
+        const uint32_t mid = (lo + hi + 1) / 2;
+        if (inst_tri_offset[mid] <= i) lo = mid;
+        else hi = mid - 1;
+    }
+    const uint32_t ii = lo;
+    const uint32_t p = i - inst_tri_offset[ii];
+    const float* m = o2w + ii * 12;
+    float v[9];
+#pragma unroll
+    for (int k = 0; k < 3; ++k) {
+        const uint32_t vi = indices[inst_first_index[ii] + 3 * p + k];
+        const float x = pos[3 * vi], y = pos[3 * vi + 1], z = pos[3 * vi + 2];
+        v[3 * k + 0] = ((m[0] * x + m[1] * y) + m[2] * z) + m[3];
+        v[3 * k + 1] = ((m[4] * x + m[5] * y) + m[6] * z) + m[7];
+        v[3 * k + 2] = ((m[8] * x + m[9] * y) + m[10] * z) + m[11];
+    }
+#pragma unroll
+    for (int k = 0; k < 9; ++k) tv[static_cast<size_t>(i) * 9 + k] = v[k];
+    tinst[i] = ii;
+    tprim[i] = p;
+    tri_box(v, boxes + static_cast<size_t>(i) * 6);
+}
+
+__global__ void k_blas_tris(const float* __restrict__ pos, const uint32_t* __restrict__ indices, uint32_t first_index,
+                            uint32_t ntris, float* __restrict__ tv, uint32_t* __restrict__ tinst,
+                            uint32_t* __restrict__ tprim, float* __restrict__ boxes) {
+    const uint32_t p = blockIdx.x * blockDim.x + threadIdx.x;
+    if (p >= ntris) return;
+    float v[9];
+#pragma unroll
+    for (int k = 0; k < 3; ++k) {
+        const uint32_t vi = indices[first_index + 3 * p + k];
+        v[3 * k + 0] = pos[3 * vi];
+        v[3 * k + 1] = pos[3 * vi + 1];
+        v[3 * k + 2] = pos[3 * vi + 2];
+    }
+#pragma unroll
+    for (int k = 0; k < 9; ++k) tv[static_cast<size_t>(p) * 9 + k] = v[k];
+    tinst[p] = 0xFFFFFFFFu;
+    tprim[p] = p;
+    tri_box(v, boxes + static_cast<size_t>(p) * 6);
+}
+
+__global__ void k_gather(const float* __restrict__ tv, const uint32_t* __restrict__ tinst,
+                         const uint32_t* __restrict__ tprim, const uint32_t* __restrict__ order, uint32_t n,
+                         float4* __restrict__ recs) {
+    const uint32_t j = blockIdx.x * blockDim.x + threadIdx.x;
+    if (j >= n) return;
+    const uint32_t b = order[j];
+    const float* v = tv + static_cast<size_t>(b) * 9;
+    recs[static_cast<size_t>(j) * 3 + 0] = make_float4(v[0], v[1], v[2], __uint_as_float(tprim[b]));
+    recs[static_cast<size_t>(j) * 3 + 1] = make_float4(v[3], v[4], v[5], __uint_as_float(tinst[b]));
+    recs[static_cast<size_t>(j) * 3 + 2] = make_float4(v[6], v[7], v[8], __uint_as_float(b));
+}
+
+}  // namespace
+
+void launch_flat_triangles(const float* pos, const uint32_t* indices, const uint32_t* inst_first_index,
+                           const uint32_t* inst_tri_offset, const float* inst_o2w, uint32_t n_inst, uint32_t total,
+                           float* tri_verts, uint32_t* tri_inst, uint32_t* tri_prim, float* boxes, cudaStream_t st) {
+    if (total == 0) return;
+    k_flat_tris<<<(total + 255) / 256, 256, 0, st>>>(pos, indices, inst_first_index, inst_tri_offset, inst_o2w, n_inst,
+                                                     total, tri_verts, tri_inst, tri_prim, boxes);
+}
+
+void launch_blas_triangles(const float* pos, const uint32_t* indices, uint32_t first_index, uint32_t ntris,
+                           float* tri_verts, uint32_t* tri_inst, uint32_t* tri_prim, float* boxes, cudaStream_t st) {
+    if (ntris == 0) return;
+    k_blas_tris<<<(ntris + 255) / 256, 256, 0, st>>>(pos, indices, first_index, ntris, tri_verts, tri_inst, tri_prim,
+                                                     boxes);
+}
+
+void launch_gather_records(const float* tri_verts, const uint32_t* tri_inst, const uint32_t* tri_prim,
+                           const uint32_t* order, uint32_t n, float4* recs, cudaStream_t st) {
+    if (n == 0) return;
+    k_gather<<<(n + 255) / 256, 256, 0, st>>>(tri_verts, tri_inst, tri_prim, order, n, recs);
+}
+
+}  // namespace ohao

@@ -1,0 +1,297 @@
+// oracle_capi.cpp -- TEST INFRASTRUCTURE ONLY (the CPU oracle).
+//
+// extern "C" surface of the host oracle, loaded by tests/ (ctypes), by the
+// smoke check and by bench.py's CPU-baseline leg. Never linked into the
+// product library.
+#include "oracle_pt.hpp"
+#include <cstring>
+#include <memory>
+#include <vector>
+#ifdef _OPENMP
+#include <omp.h>
+#endif
+
+namespace orc {
+// Sobol direction numbers for dimensions 0-3 (32 per dimension), the table
+// the reference ships in shaders/includes/rt/sampler_sobol_tables.glsl:10-47
+// and ohao/render/rt/sobol_generator.cpp (kDirectionNumbers). Dimension 2 is
+// not the textbook Joe-Kuo dimension, so the values are data, not derived.
+const uint32_t kSobolDirs[128] = {
+    0x80000000u, 0x40000000u, 0x20000000u, 0x10000000u, 0x08000000u, 0x04000000u, 0x02000000u, 0x01000000u,
+    0x00800000u, 0x00400000u, 0x00200000u, 0x00100000u, 0x00080000u, 0x00040000u, 0x00020000u, 0x00010000u,
+    0x00008000u, 0x00004000u, 0x00002000u, 0x00001000u, 0x00000800u, 0x00000400u, 0x00000200u, 0x00000100u,
+    0x00000080u, 0x00000040u, 0x00000020u, 0x00000010u, 0x00000008u, 0x00000004u, 0x00000002u, 0x00000001u,
+    0x80000000u, 0xC0000000u, 0xA0000000u, 0xF0000000u, 0x88000000u, 0xCC000000u, 0xAA000000u, 0xFF000000u,
+    0x80800000u, 0xC0C00000u, 0xA0A00000u, 0xF0F00000u, 0x88880000u, 0xCCCC0000u, 0xAAAA0000u, 0xFFFF0000u,
+    0x80008000u, 0xC000C000u, 0xA000A000u, 0xF000F000u, 0x88008800u, 0xCC00CC00u, 0xAA00AA00u, 0xFF00FF00u,
+    0x80808080u, 0xC0C0C0C0u, 0xA0A0A0A0u, 0xF0F0F0F0u, 0x88888888u, 0xCCCCCCCCu, 0xAAAAAAAAu, 0xFFFFFFFFu,
+    0x80000000u, 0x40000000u, 0xE0000000u, 0x50000000u, 0x98000000u, 0xBC000000u, 0xAE000000u, 0x25000000u,
+    0x5B800000u, 0x91400000u, 0x65600000u, 0x2E500000u, 0x91180000u, 0x88D40000u, 0xDD360000u, 0x02950000u,
+    0x4C888000u, 0x09EB4000u, 0x86CA6000u, 0x13B15000u, 0x42ADD800u, 0x3DF8D400u, 0x2FE57E00u, 0x56EB8100u,
+    0x8C41A680u, 0xE68455C0u, 0x3C9CE8E0u, 0xB44DBFF0u, 0x7C27F6C8u, 0x5239A6ACu, 0x853B0EDEu, 0x52EB2EF9u,
+    0x80000000u, 0xC0000000u, 0x20000000u, 0x50000000u, 0xF8000000u, 0x74000000u, 0xA2000000u, 0x93000000u,
+    0xD8800000u, 0x25400000u, 0x59E00000u, 0xE6D00000u, 0x78080000u, 0xB40C0000u, 0x82020000u, 0xC3050000u,
+    0x208F8000u, 0x51CBC000u, 0xFBEA2000u, 0x75AD5000u, 0xA00AF800u, 0x90077400u, 0xD800A200u, 0x25009300u,
+    0x59E08480u, 0xE6D0CEC0u, 0x78088520u, 0xB40CEBB0u, 0x82028348u, 0xC305C274u, 0x208FB552u, 0x51CB9AE9u,
+};
+}  // namespace orc
+
+using namespace orc;
+
+struct AbiInstance {   // ohao_pt_instance (include/ohao_pt.h)
+    uint32_t blas;
+    float xform[12];
+    uint32_t custom_index;
+    uint32_t mask;
+    uint32_t sbt_offset;
+};
+static_assert(sizeof(AbiInstance) == 64, "instance record is 64 bytes");
+
+extern "C" {
+
+Scene* orc_scene_create() { return new Scene(); }
+void orc_scene_destroy(Scene* s) { delete s; }
+
+void orc_scene_set_geometry(Scene* s, const float* pos, uint32_t pos_stride_bytes, uint32_t nverts, const float* normal4,
+                            const float* uv2, const uint32_t* idx, uint32_t ntris, const uint32_t* matid) {
+    s->pos.resize(static_cast<size_t>(nverts) * 3);
+    const uint8_t* pb = reinterpret_cast<const uint8_t*>(pos);
+    for (uint32_t i = 0; i < nverts; ++i) std::memcpy(&s->pos[3 * i], pb + static_cast<size_t>(i) * pos_stride_bytes, 12);
+    s->normals.assign(normal4, normal4 + static_cast<size_t>(nverts) * 4);
+    if (uv2) s->uvs.assign(uv2, uv2 + static_cast<size_t>(nverts) * 2);
+    else s->uvs.assign(static_cast<size_t>(nverts) * 2, 0.0f);
+    s->indices.assign(idx, idx + static_cast<size_t>(ntris) * 3);
+    s->mat_ids.assign(matid, matid + ntris);
+}
+void orc_scene_set_materials(Scene* s, const float* m, uint32_t n) { s->mats.assign(m, m + static_cast<size_t>(n) * 12); }
+void orc_scene_set_lights(Scene* s, const float* l, uint32_t n) {
+    s->lights.resize(n);
+    if (n) std::memcpy(s->lights.data(), l, static_cast<size_t>(n) * 80);
+}
+void orc_scene_set_env(Scene* s, const float* rgba, uint32_t w, uint32_t h, const float* marg, const float* cond,
+                       float integral, float intensity) {
+    s->has_env = rgba != nullptr && w > 0 && h > 0;
+    s->has_cdf = s->has_env && marg != nullptr && cond != nullptr;
+    s->env_w = w; s->env_h = h;
+    if (s->has_env) s->env.assign(rgba, rgba + static_cast<size_t>(w) * h * 4);
+    if (s->has_cdf) {
+        s->marg.assign(marg, marg + h);
+        s->cond.assign(cond, cond + static_cast<size_t>(w) * h);
+    }
+    s->env_integral = integral;
+    s->env_intensity = intensity;
+}
+void orc_scene_set_albedo_map(Scene* s, const float* map, uint32_t w, uint32_t h) {
+    s->map_w = w; s->map_h = h;
+    s->albedo_map.assign(map, map + static_cast<size_t>(w) * h * 3);
+}
+uint32_t orc_scene_add_blas(Scene* s, uint32_t first_index, uint32_t index_count) {
+    Blas b;
+    b.first_index = first_index;
+    b.index_count = index_count;
+    s->blases.push_back(std::move(b));
+    return static_cast<uint32_t>(s->blases.size() - 1);
+}
+void orc_scene_set_instances(Scene* s, const AbiInstance* in, uint32_t n) {
+    s->instances.resize(n);
+    for (uint32_t i = 0; i < n; ++i) {
+        Instance& d = s->instances[i];
+        d.blas = in[i].blas;
+        std::memcpy(d.xform, in[i].xform, sizeof(d.xform));
+        d.custom = in[i].custom_index;
+        d.mask = in[i].mask;
+    }
+}
+// force_mode: 0 auto, 1 flat, 2 two-level
+void orc_scene_build(Scene* s, uint64_t flatten_limit, int force_mode) { s->build(flatten_limit, force_mode); }
+int orc_scene_two_level(const Scene* s) { return s->two_level ? 1 : 0; }
+
+// which = -1: flat BVH (or TLAS when two-level); which = k: BLAS k.
+void orc_bvh_sizes(const Scene* s, int which, uint32_t* nnodes, uint32_t* nprims, uint32_t* height) {
+    const WideBVH* b;
+    size_t np;
+    if (which < 0) {
+        b = s->two_level ? &s->tlas : &s->flat;
+        np = s->two_level ? s->tlas_inst.size() : s->flat_tris.size();
+    } else {
+        b = &s->blases[which].bvh;
+        np = s->blases[which].tris.size();
+    }
+    *nnodes = static_cast<uint32_t>(b->nodes.size());
+    *nprims = static_cast<uint32_t>(np);
+    *height = b->height;
+}
+void orc_bvh_copy(const Scene* s, int which, void* nodes, void* prims) {
+    if (which < 0) {
+        const WideBVH& b = s->two_level ? s->tlas : s->flat;
+        std::memcpy(nodes, b.nodes.data(), b.nodes.size() * sizeof(WideNode));
+        if (s->two_level) std::memcpy(prims, s->tlas_inst.data(), s->tlas_inst.size() * 4);
+        else std::memcpy(prims, s->flat_tris.data(), s->flat_tris.size() * sizeof(TriRec));
+    } else {
+        const Blas& bl = s->blases[which];
+        std::memcpy(nodes, bl.bvh.nodes.data(), bl.bvh.nodes.size() * sizeof(WideNode));
+        std::memcpy(prims, bl.tris.data(), bl.tris.size() * sizeof(TriRec));
+    }
+}
+
+// rays: n x 8 floats (o.xyz, tmin, d.xyz, tmax). hits: n x 5 u32
+// (t bits, u bits, v bits, instance, primitive) -- any-hit mode writes
+// hits[5i] = 1 when occluded. mode: 0 closest (BVH), 1 any (BVH),
+// 2 closest (brute force). stats (optional): per-ray nodes, tris.
+void orc_trace(const Scene* s, const float* rays, uint32_t n, uint32_t* hits, int mode, uint32_t* stats, int nthreads) {
+#ifdef _OPENMP
+    if (nthreads > 0) omp_set_num_threads(nthreads);
+#pragma omp parallel for schedule(dynamic, 256)
+#endif
+    for (int64_t i = 0; i < static_cast<int64_t>(n); ++i) {
+        const float* r = rays + i * 8;
+        TravStats st;
+        uint32_t* h = hits + i * 5;
+        if (mode == 1) {
+            bool occ = s->occluded(r, r + 4, r[3], r[7], &st);
+            h[0] = occ ? 1u : 0u; h[1] = h[2] = 0; h[3] = h[4] = 0xFFFFFFFFu;
+        } else {
+            HitRec hr = (mode == 2) ? s->closest_brute(r, r + 4, r[3], r[7]) : s->closest(r, r + 4, r[3], r[7], &st);
+            h[0] = f2u(hr.t); h[1] = f2u(hr.u); h[2] = f2u(hr.v); h[3] = hr.inst; h[4] = hr.prim;
+            if (!hr.hit()) { h[0] = h[1] = h[2] = 0; h[3] = h[4] = 0xFFFFFFFFu; }
+        }
+        if (stats) { stats[2 * i] = static_cast<uint32_t>(st.nodes); stats[2 * i + 1] = static_cast<uint32_t>(st.tris); }
+    }
+}
+
+struct AbiSettings {   // subset of ohao_pt_settings used by the oracle
+    uint32_t max_bounces, sampler, flags;
+    float clamp_lum, aniso, aniso_rot;
+};
+
+static Settings to_settings(const AbiSettings* a) {
+    Settings s;
+    s.max_bounces = a->max_bounces;
+    s.sampler = a->sampler;
+    s.flags = a->flags;
+    s.clamp_lum = a->clamp_lum;
+    s.aniso = a->aniso;
+    s.aniso_rot = a->aniso_rot;
+    return s;
+}
+
+// Per-path radiance for `npix` pixels (pixel ids y*W+x, or all pixels when
+// pix == NULL) x `spp` samples (sample index = sample_base + k). out is
+// [spp][npix][3] in Real (float when fp64 == 0, double otherwise).
+// stats (optional, u64 x 3): nodes, triangles, instances visited.
+void orc_render_paths(const Scene* s, const float* inv_view, const float* inv_proj, uint32_t width, uint32_t height,
+                      const AbiSettings* as, uint32_t sample_base, uint32_t spp, const uint32_t* pix, uint32_t npix,
+                      void* out, int fp64, int nthreads, uint64_t* stats) {
+    View vw;
+    std::memcpy(vw.inv_view, inv_view, 64);
+    std::memcpy(vw.inv_proj, inv_proj, 64);
+    vw.width = width; vw.height = height;
+    Settings st = to_settings(as);
+    const uint32_t np = pix ? npix : width * height;
+    const int64_t total = static_cast<int64_t>(np) * spp;
+    uint64_t tn = 0, tt = 0, ti = 0;
+#ifdef _OPENMP
+    if (nthreads > 0) omp_set_num_threads(nthreads);
+#pragma omp parallel for schedule(dynamic, 64) reduction(+ : tn, tt, ti)
+#endif
+    for (int64_t k = 0; k < total; ++k) {
+        uint32_t smp = static_cast<uint32_t>(k / np), pi = static_cast<uint32_t>(k % np);
+        uint32_t p = pix ? pix[pi] : pi;
+        uint32_t px = p % width, py = p / width;
+        TravStats ts;
+        if (fp64) {
+            PathTracer<double> pt(*s, st);
+            V3<double> r = pt.path(vw, px, py, sample_base + smp, stats ? &ts : nullptr);
+            double* o = static_cast<double*>(out) + k * 3;
+            o[0] = r.x; o[1] = r.y; o[2] = r.z;
+        } else {
+            PathTracer<float> pt(*s, st);
+            V3<float> r = pt.path(vw, px, py, sample_base + smp, stats ? &ts : nullptr);
+            float* o = static_cast<float*>(out) + k * 3;
+            o[0] = r.x; o[1] = r.y; o[2] = r.z;
+        }
+        tn += ts.nodes; tt += ts.tris; ti += ts.insts;
+    }
+    if (stats) { stats[0] = tn; stats[1] = tt; stats[2] = ti; }
+}
+
+// Progressive own-pixel accumulation of per-path radiance in sample order
+// (pt_raygen.rgen:1144-1186 with reprojection off): accum is RGBA32F
+// (mean, count) per pixel, updated in place; history = frames already in it.
+void orc_accumulate(const float* paths, uint32_t npix, uint32_t spp, float* accum, uint32_t history) {
+    for (uint32_t p = 0; p < npix; ++p) {
+        float* a = accum + 4 * static_cast<size_t>(p);
+        for (uint32_t k = 0; k < spp; ++k) {
+            const float* L = paths + (static_cast<size_t>(k) * npix + p) * 3;
+            if (history + k == 0) {
+                a[0] = L[0]; a[1] = L[1]; a[2] = L[2]; a[3] = 1.0f;
+            } else {
+                float cnt = a[3] + 1.0f;
+                a[0] = (a[0] * a[3] + L[0]) / cnt;
+                a[1] = (a[1] * a[3] + L[1]) / cnt;
+                a[2] = (a[2] * a[3] + L[2]) / cnt;
+                a[3] = cnt;
+            }
+        }
+    }
+}
+
+// EnvCDF::build restated (env_cdf.cpp:13-61): serial float sums.
+void orc_env_cdf_build(const float* px, int w, int h, float* marg, float* cond, float* integral) {
+    std::vector<float> rowSum(h, 0.0f);
+    const float kPi = 3.14159265358979323846f;
+    for (int y = 0; y < h; ++y) {
+        float theta = kPi * (float(y) + 0.5f) / float(h);
+        float sinT = std::sin(theta);
+        float acc = 0.0f;
+        for (int x = 0; x < w; ++x) {
+            const float* p = px + (static_cast<size_t>(y) * w + x) * 4;
+            float lw = (0.2126f * p[0] + 0.7152f * p[1] + 0.0722f * p[2]) * sinT;
+            acc += lw;
+            cond[static_cast<size_t>(y) * w + x] = acc;
+        }
+        if (acc > 0.0f) {
+            for (int x = 0; x < w; ++x) cond[static_cast<size_t>(y) * w + x] /= acc;
+        } else {
+            for (int x = 0; x < w; ++x) cond[static_cast<size_t>(y) * w + x] = float(x + 1) / float(w);
+        }
+        rowSum[y] = acc;
+    }
+    float total = 0.0f;
+    for (int y = 0; y < h; ++y) { total += rowSum[y]; marg[y] = total; }
+    *integral = total;
+    if (total > 0.0f) for (int y = 0; y < h; ++y) marg[y] /= total;
+    else for (int y = 0; y < h; ++y) marg[y] = float(y + 1) / float(h);
+}
+
+float orc_sobol_sample1d(uint32_t index, uint32_t dim) {   // SobolGenerator::sample1D
+    return static_cast<float>(sobol_int(index, dim) >> 8) * (1.0f / 16777216.0f);
+}
+uint32_t orc_owen_scramble(uint32_t v, uint32_t seed) { return owen_scramble(v, seed); }
+// getSample1D for pixel/sample, dims 0..n-1 (sampler 0 = PCG, 1 = Sobol)
+void orc_sampler_stream(uint32_t type, uint32_t px, uint32_t py, uint32_t sample, uint32_t n, float* out) {
+    Sampler s;
+    s.init(type, px, py, sample);
+    for (uint32_t d = 0; d < n; ++d) out[d] = s.s1(d);
+}
+// op: 0 sin, 1 cos, 2 atan2(y=in[2i], x=in[2i+1]), 3 asin, 4 acos
+void orc_math(int op, const float* in, uint32_t n, float* out) {
+    for (uint32_t i = 0; i < n; ++i) {
+        switch (op) {
+            case 0: out[i] = sin_f(in[i]); break;
+            case 1: out[i] = cos_f(in[i]); break;
+            case 2: out[i] = atan2_f(in[2 * i], in[2 * i + 1]); break;
+            case 3: out[i] = asin_f(in[i]); break;
+            default: out[i] = acos_f(in[i]); break;
+        }
+    }
+}
+int orc_num_threads() {
+#ifdef _OPENMP
+    return omp_get_max_threads();
+#else
+    return 1;
+#endif
+}
+
+}  // extern "C"

@@ -1,0 +1,183 @@
+"""ctypes binding of the host oracle -- TEST INFRASTRUCTURE ONLY.
+
+Loaded by tests/, by ``__graft_entry__.smoke()`` and by bench.py's CPU-baseline
+leg, always as the checker or the timed CPU baseline, never as part of the
+product path. ``build()`` compiles ``oracle/_build/liboracle.so`` with the
+Makefile beside this file.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+import subprocess
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(HERE, "_build", "liboracle.so")
+REF_PATH = os.path.join(HERE, "_ref", "libohao_ref.so")
+REF_ROOT = "/root/reference"
+
+_lib = None
+
+
+def build(ref: bool | None = None) -> None:
+    subprocess.run(["make", "-s", "-C", HERE, "all"], check=True)
+    if ref is None:
+        ref = os.path.isdir(os.path.join(REF_ROOT, "ohao"))
+    if ref:
+        subprocess.run(["make", "-s", "-C", HERE, "ref", f"REF_ROOT={REF_ROOT}"], check=True)
+
+
+def _p(a):
+    return None if a is None else a.ctypes.data_as(C.c_void_p)
+
+
+def lib():
+    global _lib
+    if _lib is None:
+        if not os.path.exists(LIB_PATH):
+            build(ref=False)
+        L = C.CDLL(LIB_PATH)
+        vp, u32, i32, f32, u64 = C.c_void_p, C.c_uint32, C.c_int, C.c_float, C.c_uint64
+        L.orc_scene_create.restype = vp
+        L.orc_scene_destroy.argtypes = [vp]
+        L.orc_scene_set_geometry.argtypes = [vp, vp, u32, u32, vp, vp, vp, u32, vp]
+        L.orc_scene_set_materials.argtypes = [vp, vp, u32]
+        L.orc_scene_set_lights.argtypes = [vp, vp, u32]
+        L.orc_scene_set_env.argtypes = [vp, vp, u32, u32, vp, vp, f32, f32]
+        L.orc_scene_set_albedo_map.argtypes = [vp, vp, u32, u32]
+        L.orc_scene_add_blas.argtypes = [vp, u32, u32]
+        L.orc_scene_add_blas.restype = u32
+        L.orc_scene_set_instances.argtypes = [vp, vp, u32]
+        L.orc_scene_build.argtypes = [vp, u64, i32]
+        L.orc_scene_two_level.argtypes = [vp]
+        L.orc_scene_two_level.restype = i32
+        L.orc_bvh_sizes.argtypes = [vp, i32, C.POINTER(u32), C.POINTER(u32), C.POINTER(u32)]
+        L.orc_bvh_copy.argtypes = [vp, i32, vp, vp]
+        L.orc_trace.argtypes = [vp, vp, u32, vp, i32, vp, i32]
+        L.orc_render_paths.argtypes = [vp, vp, vp, u32, u32, vp, u32, u32, vp, u32, vp, i32, i32, vp]
+        L.orc_accumulate.argtypes = [vp, u32, u32, vp, u32]
+        L.orc_env_cdf_build.argtypes = [vp, i32, i32, vp, vp, vp]
+        L.orc_sobol_sample1d.argtypes = [u32, u32]
+        L.orc_sobol_sample1d.restype = f32
+        L.orc_owen_scramble.argtypes = [u32, u32]
+        L.orc_owen_scramble.restype = u32
+        L.orc_sampler_stream.argtypes = [u32, u32, u32, u32, u32, vp]
+        L.orc_math.argtypes = [i32, vp, u32, vp]
+        L.orc_num_threads.restype = i32
+        _lib = L
+    return _lib
+
+
+def ref_lib():
+    """The reference's own helpers (only where the reference tree exists)."""
+    if not os.path.exists(REF_PATH):
+        return None
+    L = C.CDLL(REF_PATH)
+    L.ref_env_cdf_build.argtypes = [C.c_void_p, C.c_int, C.c_int, C.c_void_p, C.c_void_p, C.c_void_p]
+    L.ref_sobol_sample1d.argtypes = [C.c_uint32, C.c_uint32]
+    L.ref_sobol_sample1d.restype = C.c_float
+    L.ref_owen_scramble.argtypes = [C.c_uint32, C.c_uint32]
+    L.ref_owen_scramble.restype = C.c_uint32
+    L.ref_sobol_dirs.restype = C.POINTER(C.c_uint32)
+    return L
+
+
+def env_cdf(env: np.ndarray):
+    h, w = env.shape[:2]
+    e = np.ascontiguousarray(env, np.float32)
+    marg = np.zeros(h, np.float32)
+    cond = np.zeros(w * h, np.float32)
+    integ = np.zeros(1, np.float32)
+    lib().orc_env_cdf_build(_p(e), w, h, _p(marg), _p(cond), _p(integ))
+    return marg, cond, float(integ[0])
+
+
+SETTINGS_DTYPE = np.dtype([("max_bounces", "<u4"), ("sampler", "<u4"), ("flags", "<u4"),
+                           ("clamp_lum", "<f4"), ("aniso", "<f4"), ("aniso_rot", "<f4")])
+
+
+class OracleScene:
+    """Host oracle scene built from a :class:`ohao_engine_gb300.scenes.SceneData`."""
+
+    def __init__(self, sd, flatten_limit: int = 1 << 25, force_mode: int = 0, env_cdf_arrays=None):
+        L = lib()
+        self.sd = sd
+        self.h = L.orc_scene_create()
+        self._keep = []
+        pos = np.ascontiguousarray(sd.pos, np.float32)
+        nrm = np.ascontiguousarray(sd.normals, np.float32)
+        uv = np.ascontiguousarray(sd.uvs, np.float32)
+        idx = np.ascontiguousarray(sd.indices, np.uint32)
+        mid = np.ascontiguousarray(sd.mat_ids, np.uint32)
+        L.orc_scene_set_geometry(self.h, _p(pos), 12, pos.shape[0], _p(nrm), _p(uv), _p(idx), idx.size // 3, _p(mid))
+        mats = np.ascontiguousarray(sd.materials, np.float32)
+        L.orc_scene_set_materials(self.h, _p(mats), mats.shape[0])
+        lights = np.ascontiguousarray(sd.lights, np.float32)
+        L.orc_scene_set_lights(self.h, _p(lights), lights.shape[0])
+        if sd.env is not None:
+            env = np.ascontiguousarray(sd.env, np.float32)
+            marg, cond, integ = env_cdf_arrays if env_cdf_arrays is not None else env_cdf(env)
+            L.orc_scene_set_env(self.h, _p(env), env.shape[1], env.shape[0], _p(marg), _p(cond), integ,
+                                sd.env_intensity)
+        if sd.albedo_map is not None:
+            self.set_albedo_map(sd.albedo_map)
+        for fi, ic in sd.blas:
+            L.orc_scene_add_blas(self.h, fi, ic)
+        inst = np.ascontiguousarray(sd.instances)
+        L.orc_scene_set_instances(self.h, _p(inst), inst.size)
+        L.orc_scene_build(self.h, flatten_limit, force_mode)
+
+    def set_albedo_map(self, amap):
+        amap = np.ascontiguousarray(amap, np.float32)
+        lib().orc_scene_set_albedo_map(self.h, _p(amap), amap.shape[1], amap.shape[0])
+
+    def __del__(self):
+        try:
+            lib().orc_scene_destroy(self.h)
+        except Exception:
+            pass
+
+    @property
+    def two_level(self) -> bool:
+        return bool(lib().orc_scene_two_level(self.h))
+
+    def bvh(self, which: int = -1):
+        nn, npr, hh = C.c_uint32(), C.c_uint32(), C.c_uint32()
+        lib().orc_bvh_sizes(self.h, which, C.byref(nn), C.byref(npr), C.byref(hh))
+        nodes = np.zeros(nn.value * 80, np.uint8)
+        prim_bytes = 4 if (which < 0 and self.two_level) else 48
+        prims = np.zeros(npr.value * prim_bytes, np.uint8)
+        lib().orc_bvh_copy(self.h, which, _p(nodes), _p(prims))
+        return nodes, prims, hh.value
+
+    def trace(self, rays: np.ndarray, mode: int = 0, stats: bool = False, nthreads: int = 0):
+        rays = np.ascontiguousarray(rays, np.float32)
+        n = rays.shape[0]
+        hits = np.zeros((n, 5), np.uint32)
+        st = np.zeros((n, 2), np.uint32) if stats else None
+        lib().orc_trace(self.h, _p(rays), n, _p(hits), mode, _p(st), nthreads)
+        return (hits, st) if stats else hits
+
+    def render_paths(self, view, settings: dict, sample_base: int, spp: int, pixels=None, fp64=False,
+                     nthreads: int = 0, stats: bool = False):
+        st = np.zeros(1, SETTINGS_DTYPE)
+        for k in SETTINGS_DTYPE.names:
+            st[k] = settings.get(k, 0)
+        pix = None if pixels is None else np.ascontiguousarray(pixels, np.uint32)
+        npix = view.width * view.height if pix is None else pix.size
+        out = np.zeros((spp, npix, 3), np.float64 if fp64 else np.float32)
+        s = np.zeros(3, np.uint64) if stats else None
+        lib().orc_render_paths(self.h, _p(view.inv_view), _p(view.inv_proj), view.width, view.height, _p(st),
+                               sample_base, spp, _p(pix), npix, _p(out), int(fp64), nthreads, _p(s))
+        return (out, s) if stats else out
+
+
+def accumulate(paths: np.ndarray, accum: np.ndarray | None = None, history: int = 0):
+    spp, npix, _ = paths.shape
+    if accum is None:
+        accum = np.zeros((npix, 4), np.float32)
+    p = np.ascontiguousarray(paths, np.float32)
+    lib().orc_accumulate(_p(p), npix, spp, _p(accum), history)
+    return accum

@@ -1,0 +1,69 @@
+"""C-ABI library checks that need no GPU: it loads, exports every function
+include/ohao_pt.h declares, its host EnvCDF helper is bit-identical to the
+reference's EnvCDF::build, and device entry points fail with a status code
+(not a crash) when no CUDA device is usable."""
+import os
+import re
+
+import numpy as np
+import pytest
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+
+
+@pytest.fixture(scope="module")
+def og():
+    from ohao_engine_gb300 import _build
+    _build.build()
+    import ohao_engine_gb300 as og
+    og.load_library()
+    return og
+
+
+def header_functions():
+    src = open(os.path.join(ROOT, "include", "ohao_pt.h")).read()
+    src = re.sub(r"/\*.*?\*/", "", src, flags=re.S)
+    return sorted(set(re.findall(r"\b(ohao_[a-z0-9_]+)\s*\(", src)))
+
+
+def test_exports_every_declared_symbol(og):
+    import subprocess
+    names = header_functions()
+    assert len(names) >= 20
+    out = subprocess.run(["nm", "-D", "--defined-only", og.LIB_PATH], capture_output=True, text=True).stdout
+    exported = set(l.split()[-1] for l in out.splitlines() if l.strip())
+    missing = [n for n in names if n not in exported]
+    assert not missing, missing
+    assert sorted(og.EXPORTED_SYMBOLS) == names
+
+
+def test_struct_sizes_match_header(og):
+    import ctypes as C
+    assert C.sizeof(og.View) == 16 * 4 * 2 + 16 + 3 * 8
+    assert C.sizeof(og.Settings) == 64
+    from ohao_engine_gb300 import scenes
+    assert scenes.INSTANCE_DTYPE.itemsize == 64
+
+
+def test_env_cdf_helper_bit_identical(og, oracle):
+    rng = np.random.default_rng(5)
+    for shape in ((16, 32), (7, 13), (64, 128)):
+        env = rng.uniform(0, 4, shape + (4,)).astype(np.float32)
+        env[1] = 0.0   # a black row exercises the uniform fallback
+        a = og.EnvCDF().build(env)
+        m, c, i = oracle.env_cdf(env)
+        assert np.array_equal(a.marginal.view(np.uint32), m.view(np.uint32))
+        assert np.array_equal(a.conditional.view(np.uint32), c.view(np.uint32))
+        assert np.float32(a.integral).view(np.uint32) == np.float32(i).view(np.uint32)
+
+
+def test_version_string(og):
+    assert "sm_103a" in og.version()
+
+
+def test_no_device_reports_status(og):
+    import torch
+    if torch.cuda.is_available():
+        pytest.skip("a CUDA device is present")
+    with pytest.raises(og.OhaoError):
+        og.PathTracer()

@@ -1,0 +1,126 @@
+"""The oracle's helper layer pinned against the reference's own code and tests.
+
+* golden vectors in tests/golden/reference_kats.json were produced by the
+  reference's compiled ohao/render/rt/{sobol_generator,owen_scramble,env_cdf}.cpp
+  (tests/golden/make_golden.py);
+* the known-answer tests of tests/renderer/sobol_test.cpp:10-111 and
+  tests/renderer/env_cdf_test.cpp:9-61 restated as asserts;
+* when the reference checkout is present, the compiled reference helpers are
+  called directly as a third check.
+"""
+import json
+import os
+
+import numpy as np
+import pytest
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+KATS = json.load(open(os.path.join(HERE, "golden", "reference_kats.json")))
+
+
+def f32bits(x):
+    return int(np.float32(x).view(np.uint32))
+
+
+def test_sobol_matches_reference_golden(oracle):
+    L = oracle.lib()
+    for d in range(4):
+        got = [f32bits(L.orc_sobol_sample1d(i, d)) for i in KATS["sobol_index"]]
+        assert got == KATS["sobol_sample1d_bits"][str(d)], f"dim {d}"
+
+
+def test_sobol_known_answers(oracle):
+    """tests/renderer/sobol_test.cpp:10-66"""
+    L = oracle.lib()
+    dim2 = [0.0, 0.5, 0.25, 0.75, 0.875, 0.375, 0.625, 0.125]
+    dim3 = [0.0, 0.5, 0.75, 0.25, 0.125, 0.625, 0.875, 0.375]
+    jk = [(0.0, 0.0), (0.5, 0.5), (0.25, 0.75), (0.75, 0.25), (0.125, 0.625), (0.625, 0.125), (0.375, 0.375),
+          (0.875, 0.875)]
+    for i in range(8):
+        assert abs(L.orc_sobol_sample1d(i, 2) - dim2[i]) < 1e-5
+        assert abs(L.orc_sobol_sample1d(i, 3) - dim3[i]) < 1e-5
+        assert abs(L.orc_sobol_sample1d(i, 0) - jk[i][0]) < 1e-5
+        assert abs(L.orc_sobol_sample1d(i, 1) - jk[i][1]) < 1e-5
+    for d in range(4):
+        for i in range(128):
+            v = L.orc_sobol_sample1d(i, d)
+            assert 0.0 <= v < 1.0
+    v = L.orc_sobol_sample1d(2**31, 1)
+    assert 0.0 <= v < 1.0
+
+
+def test_owen_matches_reference_golden(oracle):
+    L = oracle.lib()
+    got = [L.orc_owen_scramble(v, s) for v, s in zip(KATS["owen_v"], KATS["owen_seed"])]
+    assert got == KATS["owen_out"]
+
+
+def test_owen_properties(oracle):
+    """tests/renderer/sobol_test.cpp:75-111"""
+    L = oracle.lib()
+    assert L.orc_owen_scramble(0xABCD1234, 0xDEADBEEF) == L.orc_owen_scramble(0xABCD1234, 0xDEADBEEF)
+    assert L.orc_owen_scramble(0x01234567, 1) != L.orc_owen_scramble(0x01234567, 2)
+    assert 0 <= L.orc_owen_scramble(0, 0xCAFEBABE) <= 0xFFFFFFFF
+    total = 0
+    for i in range(1, 1001):
+        v = (i * 0x9E3779B9) & 0xFFFFFFFF
+        total += bin(L.orc_owen_scramble(v, 1) ^ L.orc_owen_scramble(v, 2)).count("1")
+    assert 12000 < total < 20000
+
+
+@pytest.mark.parametrize("name", sorted(KATS["env_cdf"].keys()))
+def test_env_cdf_matches_reference_golden(oracle, name):
+    g = KATS["env_cdf"][name]
+    w, h = g["w"], g["h"]
+    px = np.array(g["pixels_bits"], np.uint32).view(np.float32).reshape(h, w, 4)
+    marg, cond, integ = oracle.env_cdf(px)
+    assert marg.view(np.uint32).tolist() == g["marg_bits"]
+    assert cond.view(np.uint32).tolist() == g["cond_bits"]
+    assert f32bits(integ) == g["integral_bits"]
+
+
+def test_env_cdf_known_answers(oracle):
+    """tests/renderer/env_cdf_test.cpp:9-61"""
+    marg, cond, integ = oracle.env_cdf(np.ones((16, 32, 4), np.float32))
+    assert integ > 0
+    assert abs(marg[-1] - 1.0) < 1e-4 and np.all(np.diff(marg) >= 0)
+    c = cond.reshape(16, 32)
+    assert np.all(np.abs(c[:, -1] - 1.0) < 1e-4) and np.all(np.diff(c, axis=1) >= 0)
+    px = np.full((8, 16, 4), 0.01, np.float32)
+    px[4, 10, :3] = 100.0
+    marg, cond, _ = oracle.env_cdf(px)
+    c = cond.reshape(8, 16)
+    assert c[4, 10] - c[4, 9] > 0.5
+    assert marg[4] - marg[3] > 0.5
+
+
+def test_reference_helpers_live(oracle):
+    """Direct comparison with the compiled reference helpers (reference checkout only)."""
+    R = oracle.ref_lib()
+    if R is None:
+        pytest.skip("reference helpers not built here (no reference checkout)")
+    L = oracle.lib()
+    rng = np.random.default_rng(3)
+    for _ in range(2000):
+        i = int(rng.integers(0, 2**32))
+        d = int(rng.integers(0, 4))
+        assert f32bits(L.orc_sobol_sample1d(i, d)) == f32bits(R.ref_sobol_sample1d(i, d))
+    env = rng.uniform(0, 3, (32, 64, 4)).astype(np.float32)
+    m1, c1, i1 = oracle.env_cdf(env)
+    m2 = np.zeros(32, np.float32)
+    c2 = np.zeros(64 * 32, np.float32)
+    i2 = np.zeros(1, np.float32)
+    R.ref_env_cdf_build(env.ctypes.data, 64, 32, m2.ctypes.data, c2.ctypes.data, i2.ctypes.data)
+    assert np.array_equal(m1.view(np.uint32), m2.view(np.uint32))
+    assert np.array_equal(c1.view(np.uint32), c2.view(np.uint32))
+    assert f32bits(i1) == f32bits(i2[0])
+
+
+def test_sobol_table_matches_reference_golden():
+    """The library's direction-number table equals the reference's table."""
+    import re
+    src = open(os.path.join(os.path.dirname(HERE), "ohao_engine_gb300", "csrc", "abi.cpp")).read()
+    body = src[src.index("kSobolDirs[128] = {"):]
+    body = body[:body.index("};")]
+    vals = [int(x, 16) for x in re.findall(r"0x([0-9A-Fa-f]{8})u", body)]
+    assert vals == KATS["sobol_dirs"]
