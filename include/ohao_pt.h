@@ -123,6 +123,8 @@ typedef struct ohao_pt_profile {
     float extend_ms, shadow_ms, shade_ms, other_ms, total_ms;
     uint32_t extend_launches, shadow_launches, shade_launches, other_launches;
     uint64_t rays_closest, rays_shadow;
+    uint64_t nodes_closest, tris_closest;   /* BVH nodes / triangles visited by closest-hit rays */
+    uint64_t nodes_shadow, tris_shadow;     /* ... by shadow (any-hit) rays */
 } ohao_pt_profile;
 
 /* ---- lifecycle (PathTracer::init / destroy) ---- */

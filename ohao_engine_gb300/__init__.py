@@ -70,7 +70,8 @@ class Profile(C.Structure):
     _fields_ = [("extend_ms", C.c_float), ("shadow_ms", C.c_float), ("shade_ms", C.c_float),
                 ("other_ms", C.c_float), ("total_ms", C.c_float), ("extend_launches", C.c_uint32),
                 ("shadow_launches", C.c_uint32), ("shade_launches", C.c_uint32), ("other_launches", C.c_uint32),
-                ("rays_closest", C.c_uint64), ("rays_shadow", C.c_uint64)]
+                ("rays_closest", C.c_uint64), ("rays_shadow", C.c_uint64), ("nodes_closest", C.c_uint64),
+                ("tris_closest", C.c_uint64), ("nodes_shadow", C.c_uint64), ("tris_shadow", C.c_uint64)]
 
 
 _lib = None

@@ -96,6 +96,7 @@ struct ohao_pt_ctx {
     // geometry
     DevBuf pos, normals, uvs, indices, mat_ids, mats, lights, env, marg, cond, albedo_map;
     uint32_t nverts = 0, ntris = 0, nmats = 0, nlights = 0;
+    uint32_t max_mat_id = 0;              // largest per-triangle material id
     std::vector<float> host_pos;          // packed, for host-side instance boxes
     std::vector<uint32_t> host_indices;
     uint32_t env_w = 0, env_h = 0;
@@ -311,6 +312,8 @@ ohao_status ohao_pt_set_geometry(ohao_pt_ctx* ctx, const float* pos, uint32_t po
     if ((s = upload(ctx, ctx->uvs, uv2 ? uv2 : uvz.data(), static_cast<size_t>(nverts) * 8, "uvs")) != OHAO_OK) return s;
     if ((s = upload(ctx, ctx->indices, indices, static_cast<size_t>(ntris) * 12, "indices")) != OHAO_OK) return s;
     if ((s = upload(ctx, ctx->mat_ids, mat_ids, static_cast<size_t>(ntris) * 4, "material ids")) != OHAO_OK) return s;
+    ctx->max_mat_id = 0;
+    for (uint32_t t = 0; t < ntris; ++t) ctx->max_mat_id = std::max(ctx->max_mat_id, mat_ids[t]);
     ctx->nverts = nverts;
     ctx->ntris = ntris;
     ctx->built = false;
@@ -357,6 +360,11 @@ ohao_status ohao_pt_build(ohao_pt_ctx* ctx, ohao_stream stream) {
     uint64_t total = 0;
     for (const auto& in : ctx->instances)
         if (in.mask & 0xFFu) total += ctx->blas[in.blas].index_count / 3;
+    for (const auto& in : ctx->instances) {
+        const uint64_t last = static_cast<uint64_t>(in.custom_index & 0xFFFFFFu) + ctx->blas[in.blas].index_count / 3;
+        if ((in.mask & 0xFFu) && last > ctx->ntris)
+            return fail(ctx, OHAO_ERR_INVALID_ARG, "build: custom_index + primitive id exceeds the global triangle count");
+    }
     if (total >= (1ull << 31) && total <= ctx->flatten_limit)
         return fail(ctx, OHAO_ERR_UNSUPPORTED, "build: more than 2^31 instanced triangles in a flat BVH");
     ctx->two_level = total > ctx->flatten_limit;
@@ -567,6 +575,8 @@ static ohao_status validate_render(ohao_pt_ctx* ctx, const ohao_pt_view* views, 
                                    const ohao_pt_settings* st) {
     if (!ctx || !views || !st || n_views == 0) return fail(ctx, OHAO_ERR_INVALID_ARG, "render: null argument");
     if (!ctx->built) return fail(ctx, OHAO_ERR_NOT_BUILT, "render before ohao_pt_build");
+    if (ctx->ntris && ctx->max_mat_id >= ctx->nmats)
+        return fail(ctx, OHAO_ERR_INVALID_ARG, "render: a triangle's material id is outside the material table");
     if (st->spp == 0) return fail(ctx, OHAO_ERR_INVALID_ARG, "render: spp must be >= 1");
     if (st->max_bounces > 64) return fail(ctx, OHAO_ERR_INVALID_ARG, "render: max_bounces > 64");
     if (st->sampler > 1) return fail(ctx, OHAO_ERR_INVALID_ARG, "render: unknown sampler");
@@ -607,6 +617,9 @@ static ohao_status render_views(ohao_pt_ctx* ctx, const ohao_pt_view* views, uin
         p.other_ms = acc.other_ms; p.total_ms = acc.total_ms;
         p.extend_launches = acc.extend_launches; p.shade_launches = acc.shade_launches;
         p.shadow_launches = acc.shadow_launches; p.other_launches = acc.other_launches;
+        p.rays_closest = acc.rays_closest; p.rays_shadow = acc.rays_shadow;
+        p.nodes_closest = acc.nodes_closest; p.tris_closest = acc.tris_closest;
+        p.nodes_shadow = acc.nodes_shadow; p.tris_shadow = acc.tris_shadow;
     }
     return OHAO_OK;
 }

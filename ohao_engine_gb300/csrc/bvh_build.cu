@@ -469,36 +469,55 @@ inline unsigned grid_for(size_t n, int block) { return static_cast<unsigned>((n 
         }                                                                                     \
     } while (0)
 
-size_t bvh_build_scratch_bytes(uint32_t n) {
-    const size_t nn = n ? n : 1;
-    const size_t tiles = (nn + kSortTile - 1) / kSortTile;
-    size_t b = 0;
-    b += 1024 * 6 * 4 + 64;                 // bounds partials + final
-    b += 4 * nn * 4;                        // keys/vals ping-pong
-    b += 16 * tiles * 4 + 64;               // digit histogram
-    b += 5 * nn * 4;                        // left,right,first,last,parent (parent 2n)
-    b += 2 * nn * 4;                        // parent tail
-    b += nn * 4;                            // arrive
-    b += (2 * nn) * sizeof(Box6) + 2 * nn * 4;  // boxes, sa
-    b += 2 * nn * 4;                        // wcount, wheight
-    b += 2 * nn * sizeof(Item) + 64;        // frontiers
-    return b + 64 * 32;
-}
-
 namespace {
-struct Carver {
-    char* p;
-    size_t left;
-    template <class T>
-    T* take(size_t count) {
-        size_t bytes = (count * sizeof(T) + 255) & ~size_t(255);
-        T* r = reinterpret_cast<T*>(p);
-        p += bytes;
-        left -= bytes;
-        return r;
+// Scratch layout of one build; with base == nullptr it only measures.
+struct BuildLayout {
+    float* partial;
+    float* cb;
+    uint32_t *keysA, *valsA, *keysB, *valsB, *hist;
+    uint32_t *left, *right, *first, *last, *parent, *arrive;
+    Box6* boxes;
+    float* sa;
+    uint32_t *wcount, *wheight;
+    Item *frontA, *frontB;
+    uint32_t* counts;
+    size_t bytes;
+
+    BuildLayout(char* base, uint32_t n) {
+        size_t off = 0;
+        auto take = [&](size_t count, size_t elem) {
+            char* r = base ? base + off : nullptr;
+            off += (count * elem + 255) & ~size_t(255);
+            return r;
+        };
+        const size_t nn = n ? n : 1;
+        const size_t tiles = (nn + kSortTile - 1) / kSortTile;
+        partial = reinterpret_cast<float*>(take(1024 * 6, 4));
+        cb = reinterpret_cast<float*>(take(8, 4));
+        keysA = reinterpret_cast<uint32_t*>(take(nn, 4));
+        valsA = reinterpret_cast<uint32_t*>(take(nn, 4));
+        keysB = reinterpret_cast<uint32_t*>(take(nn, 4));
+        valsB = reinterpret_cast<uint32_t*>(take(nn, 4));
+        hist = reinterpret_cast<uint32_t*>(take(16 * tiles, 4));
+        left = reinterpret_cast<uint32_t*>(take(nn, 4));
+        right = reinterpret_cast<uint32_t*>(take(nn, 4));
+        first = reinterpret_cast<uint32_t*>(take(nn, 4));
+        last = reinterpret_cast<uint32_t*>(take(nn, 4));
+        parent = reinterpret_cast<uint32_t*>(take(2 * nn, 4));
+        arrive = reinterpret_cast<uint32_t*>(take(nn, 4));
+        boxes = reinterpret_cast<Box6*>(take(2 * nn, sizeof(Box6)));
+        sa = reinterpret_cast<float*>(take(2 * nn, 4));
+        wcount = reinterpret_cast<uint32_t*>(take(nn, 4));
+        wheight = reinterpret_cast<uint32_t*>(take(nn, 4));
+        frontA = reinterpret_cast<Item*>(take(nn, sizeof(Item)));
+        frontB = reinterpret_cast<Item*>(take(nn, sizeof(Item)));
+        counts = reinterpret_cast<uint32_t*>(take(64, 4));
+        bytes = off;
     }
 };
 }  // namespace
+
+size_t bvh_build_scratch_bytes(uint32_t n) { return BuildLayout(nullptr, n).bytes; }
 
 ohao_status bvh_build(const float* d_boxes, uint32_t n, void* d_scratch, size_t scratch_bytes, uint4* d_nodes,
                       uint32_t* d_prim_order, float* d_root_box, BvhBuildInfo* info, cudaStream_t st, std::string& err) {
@@ -511,27 +530,17 @@ ohao_status bvh_build(const float* d_boxes, uint32_t n, void* d_scratch, size_t 
     }
     const Box6* prims = reinterpret_cast<const Box6*>(d_boxes);
     const size_t tiles = (static_cast<size_t>(n) + kSortTile - 1) / kSortTile;
-    Carver cv{static_cast<char*>(d_scratch), scratch_bytes};
-    float* partial = cv.take<float>(1024 * 6);
-    float* cb = cv.take<float>(8);
-    uint32_t* keysA = cv.take<uint32_t>(n);
-    uint32_t* valsA = cv.take<uint32_t>(n);
-    uint32_t* keysB = cv.take<uint32_t>(n);
-    uint32_t* valsB = cv.take<uint32_t>(n);
-    uint32_t* hist = cv.take<uint32_t>(16 * tiles);
-    uint32_t* left = cv.take<uint32_t>(n);
-    uint32_t* right = cv.take<uint32_t>(n);
-    uint32_t* first = cv.take<uint32_t>(n);
-    uint32_t* last = cv.take<uint32_t>(n);
-    uint32_t* parent = cv.take<uint32_t>(2 * static_cast<size_t>(n));
-    uint32_t* arrive = cv.take<uint32_t>(n);
-    Box6* boxes = cv.take<Box6>(2 * static_cast<size_t>(n));
-    float* sa = cv.take<float>(2 * static_cast<size_t>(n));
-    uint32_t* wcount = cv.take<uint32_t>(n);
-    uint32_t* wheight = cv.take<uint32_t>(n);
-    Item* frontA = cv.take<Item>(n);
-    Item* frontB = cv.take<Item>(n);
-    uint32_t* counts = cv.take<uint32_t>(64);
+    const BuildLayout L(static_cast<char*>(d_scratch), n);
+    float* partial = L.partial;
+    float* cb = L.cb;
+    uint32_t *keysA = L.keysA, *valsA = L.valsA, *keysB = L.keysB, *valsB = L.valsB, *hist = L.hist;
+    uint32_t *left = L.left, *right = L.right, *first = L.first, *last = L.last, *parent = L.parent;
+    uint32_t* arrive = L.arrive;
+    Box6* boxes = L.boxes;
+    float* sa = L.sa;
+    uint32_t *wcount = L.wcount, *wheight = L.wheight;
+    Item *frontA = L.frontA, *frontB = L.frontB;
+    uint32_t* counts = L.counts;
 
     const int nb_part = static_cast<int>(std::min<size_t>(1024, grid_for(n, 256)));
     k_cbounds_partial<<<nb_part, 256, 0, st>>>(prims, n, partial);

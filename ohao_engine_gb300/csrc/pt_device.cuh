@@ -268,6 +268,7 @@ template <bool kStats>
 OHAO_D void bvh_closest(const uint4* __restrict__ nodes, const float4* __restrict__ tris, const RayPre& r,
                         float tmin, float tmax, Hit& best, uint32_t inst_override, uint32_t* st_node, float* st_t,
                         int stack_base, TravCount& cnt, int& err) {
+    if (stack_base >= kStackSize) { err = 1; return; }
     int sp = stack_base;
     st_node[sp] = 0u;
     st_t[sp] = -INFINITY;
@@ -353,6 +354,7 @@ OHAO_D void bvh_closest(const uint4* __restrict__ nodes, const float4* __restric
 template <bool kStats>
 OHAO_D bool bvh_any(const uint4* __restrict__ nodes, const float4* __restrict__ tris, const RayPre& r, float tmin,
                     float tmax, uint32_t* st_node, int stack_base, TravCount& cnt, int& err) {
+    if (stack_base >= kStackSize) { err = 1; return false; }
     int sp = stack_base;
     st_node[sp++] = 0u;
     while (sp > stack_base) {

@@ -79,6 +79,7 @@ struct ProfileAcc {
     float extend_ms = 0, shadow_ms = 0, shade_ms = 0, other_ms = 0, total_ms = 0;
     uint32_t extend_launches = 0, shadow_launches = 0, shade_launches = 0, other_launches = 0;
     uint64_t rays_closest = 0, rays_shadow = 0;
+    uint64_t nodes_closest = 0, tris_closest = 0, nodes_shadow = 0, tris_shadow = 0;
 };
 
 // wavefront.cu

@@ -106,19 +106,28 @@ __global__ void k_generate(ViewParams vp, PathParams pp, uint32_t w0, uint32_t n
     s.q_ray[0][i] = i;
 }
 
-__global__ void __launch_bounds__(128) k_extend(DScene sc, Soa s, int cur, int* err) {
+// stats (profiling only): [0] rays, [1] nodes, [2] triangles
+template <bool kStats>
+__global__ void __launch_bounds__(128) k_extend(DScene sc, Soa s, int cur, int* err, unsigned long long* stats) {
     const uint32_t count = s.counts[cur];
     const uint32_t* q = s.q_ray[cur];
     int e = 0;
+    TravCount tc{0, 0};
+    uint32_t nr = 0;
     for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < count; i += gridDim.x * blockDim.x) {
         const uint32_t p = q[i];
         const float4 ro = s.ro[p], rd = s.rd[p];
-        TravCount tc{0, 0};
-        const Hit h = scene_closest<false>(sc, ld3(ro), ld3(rd), 0.001f, 10000.0f, tc, e);
+        const Hit h = scene_closest<kStats>(sc, ld3(ro), ld3(rd), 0.001f, 10000.0f, tc, e);
         s.hit[p] = make_float4(h.t, h.u, h.v, __uint_as_float(h.prim));
         s.hit_inst[p] = h.inst;
+        nr++;
     }
     if (e) atomicOr(err, 1);
+    if (kStats && nr) {
+        atomicAdd(stats + 0, static_cast<unsigned long long>(nr));
+        atomicAdd(stats + 1, static_cast<unsigned long long>(tc.nodes));
+        atomicAdd(stats + 2, static_cast<unsigned long long>(tc.tris));
+    }
 }
 
 __global__ void __launch_bounds__(128) k_shade(DScene sc, PathParams pp, ViewParams vp, uint32_t w0, uint32_t npix,
@@ -168,27 +177,37 @@ __global__ void __launch_bounds__(128) k_shade(DScene sc, PathParams pp, ViewPar
     }
 }
 
-__global__ void __launch_bounds__(128) k_shadow(DScene sc, Soa s, int* err) {
+// stats (profiling only): [3] shadow rays, [4] nodes, [5] triangles
+template <bool kStats>
+__global__ void __launch_bounds__(128) k_shadow(DScene sc, Soa s, int* err, unsigned long long* stats) {
     const uint32_t count = s.counts[2];
     int e = 0;
+    TravCount tc{0, 0};
+    uint32_t nr = 0;
     for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < count; i += gridDim.x * blockDim.x) {
         const uint32_t p = s.q_sh[i];
         const uint32_t f = s.flags[p];
         const V3 org = ld3(s.sh_org[p]);
         V3 rad = ld3(s.rad[p]);
-        TravCount tc{0, 0};
         if (f & kFlagShL) {
             const float4 d = s.shL[p];
-            if (!scene_occluded<false>(sc, org, ld3(d), 0.001f, d.w, tc, e)) rad = rad + ld3(s.shLc[p]);
+            nr++;
+            if (!scene_occluded<kStats>(sc, org, ld3(d), 0.001f, d.w, tc, e)) rad = rad + ld3(s.shLc[p]);
         }
         if (f & kFlagShE) {
             const float4 d = s.shE[p];
-            if (!scene_occluded<false>(sc, org, ld3(d), 0.001f, d.w, tc, e)) rad = rad + ld3(s.shEc[p]);
+            nr++;
+            if (!scene_occluded<kStats>(sc, org, ld3(d), 0.001f, d.w, tc, e)) rad = rad + ld3(s.shEc[p]);
         }
         s.rad[p] = f4(rad, 0.0f);
         s.flags[p] = f & ~(kFlagShL | kFlagShE);
     }
     if (e) atomicOr(err, 1);
+    if (kStats && nr) {
+        atomicAdd(stats + 3, static_cast<unsigned long long>(nr));
+        atomicAdd(stats + 4, static_cast<unsigned long long>(tc.nodes));
+        atomicAdd(stats + 5, static_cast<unsigned long long>(tc.tris));
+    }
 }
 
 __global__ void k_finalize(PathParams pp, uint32_t w0, uint32_t n, uint32_t npix, Soa s, float* accum,
@@ -245,19 +264,21 @@ __global__ void __launch_bounds__(128) k_trace(DScene sc, const float* __restric
     if (e) atomicOr(err, 1);
 }
 
+// Carves 256-byte aligned arrays out of one scratch block; with a null base
+// it only measures (off = bytes needed).
 struct Carve {
-    char* p;
+    char* base;
+    size_t off = 0;
     template <class T>
     T* take(size_t count) {
         const size_t bytes = (count * sizeof(T) + 255) & ~size_t(255);
-        T* r = reinterpret_cast<T*>(p);
-        p += bytes;
+        T* r = base ? reinterpret_cast<T*>(base + off) : nullptr;
+        off += bytes;
         return r;
     }
 };
 
-Soa carve_soa(void* base, uint32_t cap) {
-    Carve c{static_cast<char*>(base)};
+Soa carve_soa_at(Carve& c, uint32_t cap) {
     Soa s;
     s.rng = c.take<uint32_t>(cap);
     s.dim = c.take<uint32_t>(cap);
@@ -283,6 +304,11 @@ Soa carve_soa(void* base, uint32_t cap) {
     return s;
 }
 
+Soa carve_soa(void* base, uint32_t cap) {
+    Carve c{static_cast<char*>(base)};
+    return carve_soa_at(c, cap);
+}
+
 int g_num_sms = 0;
 int g_blocks_extend = 0, g_blocks_shade = 0, g_blocks_shadow = 0, g_blocks_trace = 0;
 
@@ -293,11 +319,11 @@ void init_launch_shapes() {
     cudaDeviceGetAttribute(&g_num_sms, cudaDevAttrMultiProcessorCount, dev);
     if (g_num_sms <= 0) g_num_sms = 152;
     int b = 0;
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, k_extend, 128, 0);
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, k_extend<false>, 128, 0);
     g_blocks_extend = std::max(1, b) * g_num_sms;
     cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, k_shade, 128, 0);
     g_blocks_shade = std::max(1, b) * g_num_sms;
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, k_shadow, 128, 0);
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, k_shadow<false>, 128, 0);
     g_blocks_shadow = std::max(1, b) * g_num_sms;
     cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, k_trace, 128, 0);
     g_blocks_trace = std::max(1, b) * g_num_sms;
@@ -344,8 +370,9 @@ struct EvTimer {
 void upload_sobol_table(const uint32_t* dirs128) { cudaMemcpyToSymbol(c_sobol_dirs, dirs128, 128 * sizeof(uint32_t)); }
 
 size_t wavefront_scratch_bytes(uint32_t cap) {
-    const size_t c = cap;
-    return 20 * ((c * 16 + 255) & ~size_t(255)) + 1024 * 4;
+    Carve c{nullptr};
+    carve_soa_at(c, cap);
+    return c.off;
 }
 
 uint32_t wavefront_default_capacity() { return 1u << 21; }
@@ -361,6 +388,8 @@ ohao_status wavefront_render(const DScene& sc, const RenderView& view, const Pat
     const uint32_t npix = view.vp.width * view.vp.height;
     const uint64_t total = static_cast<uint64_t>(npix) * spp;
     Soa s = carve_soa(scratch, capacity);
+    unsigned long long* dstats = reinterpret_cast<unsigned long long*>(s.counts + 16);
+    if (profile) cudaMemsetAsync(dstats, 0, 8 * sizeof(unsigned long long), st);
     const uint32_t niters = 1 + 2 * pp.max_bounces;
     EvTimer tm{profile, st, {}};
     cudaEvent_t t_all0 = nullptr, t_all1 = nullptr;
@@ -378,7 +407,8 @@ ohao_status wavefront_render(const DScene& sc, const RenderView& view, const Pat
         int cur = 0;
         for (uint32_t it = 0; it < niters; ++it) {
             tm.begin(0, a);
-            k_extend<<<g_blocks_extend, 128, 0, st>>>(sc, s, cur, d_err);
+            if (profile) k_extend<true><<<g_blocks_extend, 128, 0, st>>>(sc, s, cur, d_err, dstats);
+            else k_extend<false><<<g_blocks_extend, 128, 0, st>>>(sc, s, cur, d_err, nullptr);
             tm.end(0, a);
             cudaMemsetAsync(s.counts + (cur ^ 1), 0, 4, st);
             cudaMemsetAsync(s.counts + 2, 0, 4, st);
@@ -387,7 +417,8 @@ ohao_status wavefront_render(const DScene& sc, const RenderView& view, const Pat
                                                     spp - 1);
             tm.end(1, a);
             tm.begin(2, a);
-            k_shadow<<<g_blocks_shadow, 128, 0, st>>>(sc, s, d_err);
+            if (profile) k_shadow<true><<<g_blocks_shadow, 128, 0, st>>>(sc, s, d_err, dstats);
+            else k_shadow<false><<<g_blocks_shadow, 128, 0, st>>>(sc, s, d_err, nullptr);
             tm.end(2, a);
             cur ^= 1;
         }
@@ -407,6 +438,14 @@ ohao_status wavefront_render(const DScene& sc, const RenderView& view, const Pat
         float ms = 0;
         cudaEventElapsedTime(&ms, t_all0, t_all1);
         prof->total_ms += ms;
+        unsigned long long hs[8];
+        cudaMemcpy(hs, dstats, sizeof(hs), cudaMemcpyDeviceToHost);
+        prof->rays_closest += hs[0];
+        prof->nodes_closest += hs[1];
+        prof->tris_closest += hs[2];
+        prof->rays_shadow += hs[3];
+        prof->nodes_shadow += hs[4];
+        prof->tris_shadow += hs[5];
         cudaEventDestroy(t_all0);
         cudaEventDestroy(t_all1);
     }
