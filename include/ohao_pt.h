@@ -34,6 +34,7 @@ typedef int32_t ohao_status;
 #define OHAO_ERR_NOT_BUILT (-5)    /* render/trace before ohao_pt_build */
 #define OHAO_ERR_UNSUPPORTED (-6)
 #define OHAO_ERR_DEVICE_CHECK (-7) /* a device-side bounds/stack check fired */
+#define OHAO_ERR_TOO_LARGE (-8)    /* input beyond the fixed capacity of ohao_bvh_build_noalloc */
 
 /* Same object as cudaStream_t (struct CUstream_st*); NULL = legacy stream. */
 typedef struct CUstream_st* ohao_stream;
@@ -215,6 +216,27 @@ typedef struct ohao_bvh_tri {
 ohao_status ohao_pt_bvh_info(const ohao_pt_ctx* ctx, int32_t which, uint32_t* n_nodes, uint32_t* n_prims,
                              uint32_t* height);
 ohao_status ohao_pt_bvh_download(ohao_pt_ctx* ctx, int32_t which, void* nodes, void* prims);
+
+/* ---- BVH build that allocates nothing ----
+ * No counterpart in the reference (its BVH builds happen inside the Vulkan
+ * driver). For callers that cannot call cudaMalloc: a host application that
+ * gives the renderer a fixed memory budget and owns the rest of the GPU, or a
+ * per-frame rebuild of a small animated mesh (createBLASFromPositions,
+ * rt_acceleration_structure.cpp:322-400) where an allocation would
+ * synchronise the device. Builds the same 8-wide BVH as ohao_pt_build over n
+ * primitive boxes (device, 6 floats lo.xyz hi.xyz each), n <= 65536:
+ * d_nodes (device) receives up to n ohao_bvh8_node records, d_prim_order
+ * (device, n uint32) the box index of each leaf slot, d_root_box (device) 6
+ * floats; *out_nnodes / *out_height are written on the host. Larger n returns
+ * OHAO_ERR_TOO_LARGE. The build scratch is one fixed array in device memory
+ * (about 9.2 MB per GPU that loads the library, held until exit) shared by
+ * every call: calls that overlap on the GPU (other threads or streams) race
+ * on it and must be serialised by the caller. The first call on a device
+ * resolves the array's device address and should come before any stream
+ * capture. Synchronous with respect to `stream`. */
+#define OHAO_BVH_NOALLOC_MAX_PRIMS 65536u
+ohao_status ohao_bvh_build_noalloc(const float* d_boxes, uint32_t n, void* d_nodes, uint32_t* d_prim_order,
+                                   float* d_root_box, uint32_t* out_nnodes, uint32_t* out_height, ohao_stream stream);
 
 #ifdef __cplusplus
 }

@@ -37,7 +37,7 @@ EXPORTED_SYMBOLS = [
     "ohao_pt_create_blas", "ohao_pt_set_instances", "ohao_pt_build", "ohao_pt_is_two_level",
     "ohao_pt_set_materials", "ohao_pt_update_materials", "ohao_pt_set_lights", "ohao_pt_set_env",
     "ohao_pt_set_albedo_map", "ohao_env_cdf_build", "ohao_pt_render", "ohao_pt_render_host",
-    "ohao_pt_get_profile", "ohao_pt_trace", "ohao_pt_bvh_info", "ohao_pt_bvh_download",
+    "ohao_pt_get_profile", "ohao_pt_trace", "ohao_pt_bvh_info", "ohao_pt_bvh_download", "ohao_bvh_build_noalloc",
 ]
 
 
@@ -109,6 +109,7 @@ def load_library(path: str | None = None):
         "ohao_pt_trace": ([vp, vp, u32, vp, i32, vp, vp], i32),
         "ohao_pt_bvh_info": ([vp, i32, C.POINTER(u32), C.POINTER(u32), C.POINTER(u32)], i32),
         "ohao_pt_bvh_download": ([vp, i32, vp, vp], i32),
+        "ohao_bvh_build_noalloc": ([vp, u32, vp, vp, vp, C.POINTER(u32), C.POINTER(u32), vp], i32),
     }
     for name, (args, res) in sigs.items():
         fn = getattr(L, name)

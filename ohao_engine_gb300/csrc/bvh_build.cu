@@ -18,6 +18,7 @@
 #include "bvh_internal.hpp"
 
 #include <cstdio>
+#include <mutex>
 #include <vector>
 
 namespace ohao {
@@ -597,4 +598,71 @@ ohao_status bvh_build(const float* d_boxes, uint32_t n, void* d_scratch, size_t 
     return OHAO_OK;
 }
 
+// ---------------------------------------------------------------------------
+// Allocation-free build (ohao_bvh_build_noalloc)
+//
+// For callers that must not allocate device memory themselves: a host that
+// hands the renderer a fixed memory budget and keeps the rest of the GPU for
+// its own pool, or a per-frame rebuild of a small animated mesh where
+// cudaMalloc/cudaFree (which synchronise the device) would stall the other
+// streams. The build's scratch is one file-scope device array sized for
+// OHAO_BVH_NOALLOC_MAX_PRIMS primitives; every GPU that loads this library
+// holds it (about 9.2 MB) until the process exits.
+// ---------------------------------------------------------------------------
+namespace {
+constexpr uint32_t kNoAllocMaxPrims = OHAO_BVH_NOALLOC_MAX_PRIMS;
+// 140 bytes per primitive covers the sort, tree, box and frontier arrays;
+// 64 KB covers the fixed-size parts and the 256-byte alignment of each array.
+constexpr size_t kNoAllocScratchBytes = 140ull * kNoAllocMaxPrims + 64ull * 1024ull;
+static __device__ __align__(256) unsigned char g_noalloc_scratch[kNoAllocScratchBytes];
+
+constexpr int kNoAllocMaxDevices = 64;
+std::mutex g_noalloc_mu;
+void* g_noalloc_ptr[kNoAllocMaxDevices] = {};
+}  // namespace
+
+}  // namespace ohao
+
+extern "C" ohao_status ohao_bvh_build_noalloc(const float* d_boxes, uint32_t n, void* d_nodes, uint32_t* d_prim_order,
+                                              float* d_root_box, uint32_t* out_nnodes, uint32_t* out_height,
+                                              ohao_stream stream) {
+    using namespace ohao;
+    if (!out_nnodes || !out_height || (n && (!d_boxes || !d_nodes || !d_prim_order || !d_root_box)))
+        return OHAO_ERR_INVALID_ARG;
+    if (n > kNoAllocMaxPrims) {
+        std::fprintf(stderr, "[ohao] ohao_bvh_build_noalloc: %u primitives exceed the fixed capacity of %u\n", n,
+                     kNoAllocMaxPrims);
+        return OHAO_ERR_TOO_LARGE;
+    }
+    if (bvh_build_scratch_bytes(n) > kNoAllocScratchBytes) return OHAO_ERR_TOO_LARGE;
+    int dev = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess) return OHAO_ERR_CUDA;
+    if (dev < 0 || dev >= kNoAllocMaxDevices) return OHAO_ERR_UNSUPPORTED;
+    void* scratch = nullptr;
+    {
+        // First call on a device: resolve the device address of the array
+        // (the host-side symbol is only a stand-in), with that device current.
+        std::lock_guard<std::mutex> lk(g_noalloc_mu);
+        if (!g_noalloc_ptr[dev]) {
+            void* p = nullptr;
+            const cudaError_t e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
+            if (e != cudaSuccess || !p) return OHAO_ERR_CUDA;
+            g_noalloc_ptr[dev] = p;
+        }
+        scratch = g_noalloc_ptr[dev];
+    }
+    BvhBuildInfo info{};
+    std::string err;
+    const ohao_status s = bvh_build(d_boxes, n, scratch, kNoAllocScratchBytes, static_cast<uint4*>(d_nodes),
+                                    d_prim_order, d_root_box, &info, reinterpret_cast<cudaStream_t>(stream), err);
+    if (s != OHAO_OK) {
+        std::fprintf(stderr, "[ohao] ohao_bvh_build_noalloc: %s\n", err.c_str());
+        return s;
+    }
+    *out_nnodes = info.nnodes;
+    *out_height = info.height;
+    return OHAO_OK;
+}
+
+namespace ohao {
 }  // namespace ohao
