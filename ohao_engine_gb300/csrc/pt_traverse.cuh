@@ -1,0 +1,351 @@
+// pt_traverse.cuh -- 8-wide BVH traversal (closest hit and any hit).
+//
+// Node record: 80 bytes = 5 x uint4, the layout of ohao_bvh8_node:
+//   q0 = origin.xyz, (exponents x,y,z, internal mask)
+//   q1 = child_base, tri_base, meta[0..3], meta[4..7]
+//   q2 = qlo.x[0..7], qlo.y[0..7]   q3 = qlo.z[0..7], qhi.x[0..7]
+//   q4 = qhi.y[0..7], qhi.z[0..7]
+// Child boxes are tested in the node's quantised frame: one FMA per slab side
+// (t = q * (2^e / d) + (origin - o) / d) with per-axis conservative margins
+// folded into the offsets. Near/far planes are chosen once per node by
+// swapping the lo/hi byte words of axes with a negative direction. Bytes are
+// converted to float exactly with a byte permute into 2^23 + b and one add.
+//
+// Visit order (kept identical to the host oracle, so node/triangle visit
+// counts match): leaves of a node are tested first, in slot order; then the
+// nearest internal child is visited next and the others are pushed far to
+// near (ties: lower slot pushed first). Popped entries whose entry distance
+// exceeds the best hit (with a 2^-14 relative slack) are skipped. Any-hit
+// queries push internal children in slot order and return at the first hit.
+// The stack holds 64 (node, t_near) entries in local memory; overflow sets
+// the error flag instead of faulting.
+#pragma once
+
+namespace ohao {
+
+constexpr float kTravRelSlack = 0x1p-14f;
+constexpr float kTravAbsScale = 0x1p-21f;
+constexpr int kStackSize = 64;
+
+struct Hit {
+    float t, u, v;
+    uint32_t inst, prim;
+};
+
+OHAO_D bool key_less(uint32_t ia, uint32_t pa, uint32_t ib, uint32_t pb) {
+    return ia < ib || (ia == ib && pa < pb);
+}
+
+struct TravCount {
+    uint32_t nodes, tris;
+};
+
+struct NodeRec {
+    uint4 q0, q1, q2, q3, q4;
+};
+
+OHAO_D NodeRec load_node(const uint4* __restrict__ nodes, uint32_t ni) {
+    const uint4* p = nodes + static_cast<size_t>(ni) * 5;
+    NodeRec n;
+    n.q0 = __ldg(p);
+    n.q1 = __ldg(p + 1);
+    n.q2 = __ldg(p + 2);
+    n.q3 = __ldg(p + 3);
+    n.q4 = __ldg(p + 4);
+    return n;
+}
+
+OHAO_D uint32_t byte_of(uint32_t lo4, uint32_t hi4, int i) {
+    const uint32_t w = (i < 4) ? lo4 : hi4;
+    return (w >> ((i & 3) * 8)) & 0xFFu;
+}
+
+// exact uint8 -> float: bits (0x4B000000 | b) encode 2^23 + b
+OHAO_D float u8f(uint32_t word, int b) {
+    return __uint_as_float(__byte_perm(word, 0x4B000000u, 0x7440u | static_cast<uint32_t>(b))) - 8388608.0f;
+}
+
+// Hit mask of the 8 child boxes; tn[i] = conservative entry distance.
+OHAO_D uint32_t node_test(const NodeRec& n, const RayPre& r, float tmin, float tbest, float tn[8]) {
+    const float org[3] = {__uint_as_float(n.q0.x), __uint_as_float(n.q0.y), __uint_as_float(n.q0.z)};
+    float a[3], bn[3], bf[3];
+#pragma unroll
+    for (int k = 0; k < 3; ++k) {
+        const int e = static_cast<int>(static_cast<int8_t>((n.q0.w >> (8 * k)) & 0xFFu));
+        const float s = __int_as_float((e + 127) << 23);
+        a[k] = s * r.invd[k];
+        const float b = (org[k] - r.o[k]) * r.invd[k];
+        float m = 255.0f * fabsf(a[k]) + fabsf(b);
+        m = m * kTravAbsScale;
+        bn[k] = b - m;
+        bf[k] = b + m;
+    }
+    // near / far byte words per axis (slots 0-3, 4-7)
+    const bool nx = r.invd[0] < 0.0f, ny = r.invd[1] < 0.0f, nz = r.invd[2] < 0.0f;
+    const uint32_t nx0 = nx ? n.q3.z : n.q2.x, nx1 = nx ? n.q3.w : n.q2.y;
+    const uint32_t fx0 = nx ? n.q2.x : n.q3.z, fx1 = nx ? n.q2.y : n.q3.w;
+    const uint32_t ny0 = ny ? n.q4.x : n.q2.z, ny1 = ny ? n.q4.y : n.q2.w;
+    const uint32_t fy0 = ny ? n.q2.z : n.q4.x, fy1 = ny ? n.q2.w : n.q4.y;
+    const uint32_t nz0 = nz ? n.q4.z : n.q3.x, nz1 = nz ? n.q4.w : n.q3.y;
+    const uint32_t fz0 = nz ? n.q3.x : n.q4.z, fz1 = nz ? n.q3.y : n.q4.w;
+    const float tlimit = tbest + tbest * kTravRelSlack;
+    uint32_t hit = 0;
+#pragma unroll
+    for (int i = 0; i < 8; ++i) {
+        const int b = i & 3;
+        const float qnx = u8f(i < 4 ? nx0 : nx1, b), qfx = u8f(i < 4 ? fx0 : fx1, b);
+        const float qny = u8f(i < 4 ? ny0 : ny1, b), qfy = u8f(i < 4 ? fy0 : fy1, b);
+        const float qnz = u8f(i < 4 ? nz0 : nz1, b), qfz = u8f(i < 4 ? fz0 : fz1, b);
+        const float t0 = fmaxf(fmaxf(fmaf(qnx, a[0], bn[0]), fmaf(qny, a[1], bn[1])), fmaf(qnz, a[2], bn[2]));
+        const float t1 = fminf(fminf(fmaf(qfx, a[0], bf[0]), fmaf(qfy, a[1], bf[1])), fmaf(qfz, a[2], bf[2]));
+        tn[i] = t0;
+        const uint32_t meta = byte_of(n.q1.z, n.q1.w, i);
+        if (meta != 0u && t0 <= t1 && t0 <= tlimit && t1 >= tmin) hit |= 1u << i;
+    }
+    return hit;
+}
+
+OHAO_D float pick8(const float v[8], int i) {
+    float r = v[0];
+#pragma unroll
+    for (int k = 1; k < 8; ++k) r = (i == k) ? v[k] : r;
+    return r;
+}
+
+// Orders the internal children `rem`: pushes all but the nearest (far first,
+// ties: lower slot first) and returns the nearest in (cur, cur_tn).
+// Returns false on stack overflow.
+OHAO_D bool order_children(uint32_t rem, const float tn[8], const NodeRec& n, uint32_t* st_node, float* st_t, int& sp,
+                           uint32_t& cur, float& cur_tn) {
+    while (__popc(rem) > 1) {
+        float bt = 0.0f;
+        int bi = -1;
+#pragma unroll
+        for (int i = 0; i < 8; ++i)
+            if (((rem >> i) & 1u) && (bi < 0 || tn[i] > bt)) { bt = tn[i]; bi = i; }
+        if (sp >= kStackSize) return false;
+        st_node[sp] = n.q1.x + (byte_of(n.q1.z, n.q1.w, bi) & 7u);
+        st_t[sp] = bt;
+        sp++;
+        rem &= ~(1u << bi);
+    }
+    const int li = __ffs(rem) - 1;
+    cur = n.q1.x + (byte_of(n.q1.z, n.q1.w, li) & 7u);
+    cur_tn = pick8(tn, li);
+    return true;
+}
+
+// Closest hit in one BVH (flat, or a BLAS inside instance inst_override).
+template <bool kStats>
+OHAO_D void bvh_closest(const uint4* __restrict__ nodes, const float4* __restrict__ tris, const RayPre& r,
+                        float tmin, float tmax, Hit& best, uint32_t inst_override, uint32_t* st_node, float* st_t,
+                        int stack_base, TravCount& cnt, int& err) {
+    if (stack_base >= kStackSize) { err = 1; return; }
+    int sp = stack_base;
+    uint32_t cur = 0u;
+    float cur_tn = -INFINITY;
+    while (true) {
+        const float tb = best.prim != 0xFFFFFFFFu ? best.t : tmax;
+        if (cur_tn <= tb + tb * kTravRelSlack) {
+            const NodeRec n = load_node(nodes, cur);
+            if (kStats) cnt.nodes++;
+            float tn[8];
+            const uint32_t hit = node_test(n, r, tmin, tb, tn);
+            const uint32_t imask = n.q0.w >> 24;
+            uint32_t lm = hit & ~imask;
+            while (lm) {
+                const int i = __ffs(lm) - 1;
+                lm &= lm - 1;
+                const uint32_t meta = byte_of(n.q1.z, n.q1.w, i);
+                const uint32_t c = meta >> 5, off = meta & 31u;
+                for (uint32_t q = 0; q < c; ++q) {
+                    const float4* tp = tris + static_cast<size_t>(n.q1.y + off + q) * 3;
+                    const float4 v0 = __ldg(tp), v1 = __ldg(tp + 1), v2 = __ldg(tp + 2);
+                    if (kStats) cnt.tris++;
+                    float t, u, v;
+                    if (!tri_intersect(r, v0, v1, v2, tmin, tmax, t, u, v)) continue;
+                    const uint32_t prim = __float_as_uint(v0.w);
+                    const uint32_t inst = (inst_override != 0xFFFFFFFFu) ? inst_override : __float_as_uint(v1.w);
+                    if (best.prim == 0xFFFFFFFFu || t < best.t ||
+                        (t == best.t && key_less(inst, prim, best.inst, best.prim))) {
+                        best.t = t; best.u = u; best.v = v; best.inst = inst; best.prim = prim;
+                    }
+                }
+            }
+            const uint32_t rem = hit & imask;
+            if (rem) {
+                if (!order_children(rem, tn, n, st_node, st_t, sp, cur, cur_tn)) { err = 1; return; }
+                continue;
+            }
+        }
+        if (sp == stack_base) return;
+        sp--;
+        cur = st_node[sp];
+        cur_tn = st_t[sp];
+    }
+}
+
+// Any hit in one BVH.
+template <bool kStats>
+OHAO_D bool bvh_any(const uint4* __restrict__ nodes, const float4* __restrict__ tris, const RayPre& r, float tmin,
+                    float tmax, uint32_t* st_node, int stack_base, TravCount& cnt, int& err) {
+    if (stack_base >= kStackSize) { err = 1; return false; }
+    int sp = stack_base;
+    uint32_t cur = 0u;
+    while (true) {
+        const NodeRec n = load_node(nodes, cur);
+        if (kStats) cnt.nodes++;
+        float tn[8];
+        uint32_t m = node_test(n, r, tmin, tmax, tn);
+        const uint32_t imask = n.q0.w >> 24;
+        bool have = false;
+        uint32_t next = 0u;
+        while (m) {
+            const int i = __ffs(m) - 1;
+            m &= m - 1;
+            const uint32_t meta = byte_of(n.q1.z, n.q1.w, i);
+            if ((imask >> i) & 1u) {
+                if (have) {
+                    if (sp >= kStackSize) { err = 1; return false; }
+                    st_node[sp++] = next;
+                }
+                next = n.q1.x + (meta & 7u);
+                have = true;
+                continue;
+            }
+            const uint32_t c = meta >> 5, off = meta & 31u;
+            for (uint32_t q = 0; q < c; ++q) {
+                const float4* tp = tris + static_cast<size_t>(n.q1.y + off + q) * 3;
+                const float4 v0 = __ldg(tp), v1 = __ldg(tp + 1), v2 = __ldg(tp + 2);
+                if (kStats) cnt.tris++;
+                float t, u, v;
+                if (tri_intersect(r, v0, v1, v2, tmin, tmax, t, u, v)) return true;
+            }
+        }
+        if (have) { cur = next; continue; }
+        if (sp == stack_base) return false;
+        cur = st_node[--sp];
+    }
+}
+
+OHAO_D void xform_point(const float m[12], V3 p, V3& o) {
+    o.x = ((m[0] * p.x + m[1] * p.y) + m[2] * p.z) + m[3];
+    o.y = ((m[4] * p.x + m[5] * p.y) + m[6] * p.z) + m[7];
+    o.z = ((m[8] * p.x + m[9] * p.y) + m[10] * p.z) + m[11];
+}
+OHAO_D void xform_dir(const float m[12], V3 d, V3& o) {
+    o.x = (m[0] * d.x + m[1] * d.y) + m[2] * d.z;
+    o.y = (m[4] * d.x + m[5] * d.y) + m[6] * d.z;
+    o.z = (m[8] * d.x + m[9] * d.y) + m[10] * d.z;
+}
+
+// Scene-level closest hit (flat or two-level). tmax <= tmin means no hit.
+template <bool kStats>
+OHAO_D Hit scene_closest(const DScene& sc, V3 o, V3 d, float tmin, float tmax, TravCount& cnt, int& err) {
+    Hit best;
+    best.t = 0.0f; best.u = 0.0f; best.v = 0.0f;
+    best.inst = 0xFFFFFFFFu; best.prim = 0xFFFFFFFFu;
+    if (!(tmax > tmin) || sc.nnodes == 0) return best;
+    uint32_t st_node[kStackSize];
+    float st_t[kStackSize];
+    const RayPre r = ray_pre(o, d);
+    if (!sc.two_level) {
+        bvh_closest<kStats>(sc.nodes, sc.tris, r, tmin, tmax, best, 0xFFFFFFFFu, st_node, st_t, 0, cnt, err);
+        return best;
+    }
+    int sp = 0;
+    uint32_t cur = 0u;
+    float cur_tn = -INFINITY;
+    while (true) {
+        const float tb = best.prim != 0xFFFFFFFFu ? best.t : tmax;
+        if (cur_tn <= tb + tb * kTravRelSlack) {
+            const NodeRec n = load_node(sc.nodes, cur);
+            if (kStats) cnt.nodes++;
+            float tn[8];
+            const uint32_t hit = node_test(n, r, tmin, tb, tn);
+            const uint32_t imask = n.q0.w >> 24;
+            uint32_t lm = hit & ~imask;
+            while (lm) {
+                const int i = __ffs(lm) - 1;
+                lm &= lm - 1;
+                const uint32_t meta = byte_of(n.q1.z, n.q1.w, i);
+                const uint32_t c = meta >> 5, off = meta & 31u;
+                for (uint32_t q = 0; q < c; ++q) {
+                    const uint32_t ii = __ldg(sc.tlas_inst + n.q1.y + off + q);
+                    const DInst& in = sc.inst[ii];
+                    const DBlas bl = sc.blas[in.blas];
+                    V3 oo, od;
+                    xform_point(in.w2o, o, oo);
+                    xform_dir(in.w2o, d, od);
+                    const RayPre ro = ray_pre(oo, od);
+                    bvh_closest<kStats>(sc.blas_nodes + static_cast<size_t>(bl.node_off) * 5,
+                                        sc.blas_tris + static_cast<size_t>(bl.tri_off) * 3, ro, tmin, tmax, best, ii,
+                                        st_node, st_t, sp, cnt, err);
+                    if (err) return best;
+                }
+            }
+            const uint32_t rem = hit & imask;
+            if (rem) {
+                if (!order_children(rem, tn, n, st_node, st_t, sp, cur, cur_tn)) { err = 1; return best; }
+                continue;
+            }
+        }
+        if (sp == 0) return best;
+        sp--;
+        cur = st_node[sp];
+        cur_tn = st_t[sp];
+    }
+}
+
+template <bool kStats>
+OHAO_D bool scene_occluded(const DScene& sc, V3 o, V3 d, float tmin, float tmax, TravCount& cnt, int& err) {
+    if (!(tmax > tmin) || sc.nnodes == 0) return false;
+    uint32_t st_node[kStackSize];
+    const RayPre r = ray_pre(o, d);
+    if (!sc.two_level) return bvh_any<kStats>(sc.nodes, sc.tris, r, tmin, tmax, st_node, 0, cnt, err);
+    int sp = 0;
+    uint32_t cur = 0u;
+    while (true) {
+        const NodeRec n = load_node(sc.nodes, cur);
+        if (kStats) cnt.nodes++;
+        float tn[8];
+        uint32_t m = node_test(n, r, tmin, tmax, tn);
+        const uint32_t imask = n.q0.w >> 24;
+        bool have = false;
+        uint32_t next = 0u;
+        while (m) {
+            const int i = __ffs(m) - 1;
+            m &= m - 1;
+            const uint32_t meta = byte_of(n.q1.z, n.q1.w, i);
+            if ((imask >> i) & 1u) {
+                if (have) {
+                    if (sp >= kStackSize) { err = 1; return false; }
+                    st_node[sp++] = next;
+                }
+                next = n.q1.x + (meta & 7u);
+                have = true;
+                continue;
+            }
+            const uint32_t c = meta >> 5, off = meta & 31u;
+            for (uint32_t q = 0; q < c; ++q) {
+                const uint32_t ii = __ldg(sc.tlas_inst + n.q1.y + off + q);
+                const DInst& in = sc.inst[ii];
+                const DBlas bl = sc.blas[in.blas];
+                V3 oo, od;
+                xform_point(in.w2o, o, oo);
+                xform_dir(in.w2o, d, od);
+                const RayPre ro = ray_pre(oo, od);
+                if (bvh_any<kStats>(sc.blas_nodes + static_cast<size_t>(bl.node_off) * 5,
+                                    sc.blas_tris + static_cast<size_t>(bl.tri_off) * 3, ro, tmin, tmax, st_node, sp, cnt,
+                                    err))
+                    return true;
+                if (err) return false;
+            }
+        }
+        if (have) { cur = next; continue; }
+        if (sp == 0) return false;
+        cur = st_node[--sp];
+    }
+}
+
+}  // namespace ohao
