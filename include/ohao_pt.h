@@ -184,6 +184,14 @@ ohao_status ohao_pt_render(ohao_pt_ctx* ctx, const ohao_pt_view* views, uint32_t
 ohao_status ohao_pt_render_host(ohao_pt_ctx* ctx, const ohao_pt_view* views, uint32_t n_views,
                                 const ohao_pt_settings* settings, float* const* host_accum, ohao_stream stream);
 ohao_status ohao_pt_get_profile(const ohao_pt_ctx* ctx, ohao_pt_profile* out);
+/* Times the compiled launch shapes of the persistent multi-view kernel
+ * (block size, blocks per SM, pixels per work-queue claim) on these views
+ * and keeps the fastest for later renders of this context. The views'
+ * accumulators are overwritten. No counterpart in the reference. */
+ohao_status ohao_pt_autotune(ohao_pt_ctx* ctx, const ohao_pt_view* views, uint32_t n_views,
+                             const ohao_pt_settings* settings, float* best_ms, ohao_stream stream);
+/* Name of the persistent launch shape in use ("default" before autotune). */
+const char* ohao_pt_launch_config(const ohao_pt_ctx* ctx);
 
 /* ---- traceRayEXT as a batch call ----
  * rays: device, n x 8 floats (origin.xyz, tmin, dir.xyz, tmax).

@@ -38,6 +38,7 @@ EXPORTED_SYMBOLS = [
     "ohao_pt_set_materials", "ohao_pt_update_materials", "ohao_pt_set_lights", "ohao_pt_set_env",
     "ohao_pt_set_albedo_map", "ohao_env_cdf_build", "ohao_pt_render", "ohao_pt_render_host",
     "ohao_pt_get_profile", "ohao_pt_trace", "ohao_pt_bvh_info", "ohao_pt_bvh_download", "ohao_bvh_build_noalloc",
+    "ohao_pt_autotune", "ohao_pt_launch_config",
 ]
 
 
@@ -110,6 +111,8 @@ def load_library(path: str | None = None):
         "ohao_pt_bvh_info": ([vp, i32, C.POINTER(u32), C.POINTER(u32), C.POINTER(u32)], i32),
         "ohao_pt_bvh_download": ([vp, i32, vp, vp], i32),
         "ohao_bvh_build_noalloc": ([vp, u32, vp, vp, vp, C.POINTER(u32), C.POINTER(u32), vp], i32),
+        "ohao_pt_autotune": ([vp, C.POINTER(View), u32, C.POINTER(Settings), C.POINTER(f32), vp], i32),
+        "ohao_pt_launch_config": ([vp], C.c_char_p),
     }
     for name, (args, res) in sigs.items():
         fn = getattr(L, name)
@@ -288,6 +291,17 @@ class PathTracer:
         ptrs = (C.c_void_p * len(views))(*[_ptr(a).value for a in host_accum])
         self._ck(self._L.ohao_pt_render_host(self.h, arr, len(views), C.byref(settings), ptrs,
                                              _ptr(stream) if stream is not None else None), "render_host")
+
+    def autotune(self, views, settings: Settings, stream=None) -> float:
+        arr = (View * len(views))(*views)
+        ms = C.c_float()
+        self._ck(self._L.ohao_pt_autotune(self.h, arr, len(views), C.byref(settings), C.byref(ms),
+                                          _ptr(stream) if stream is not None else None), "autotune")
+        return ms.value
+
+    @property
+    def launch_config(self) -> str:
+        return self._L.ohao_pt_launch_config(self.h).decode()
 
     def profile(self) -> Profile:
         p = Profile()

@@ -26,28 +26,6 @@ namespace {
 
 using namespace ohao;
 
-// Sobol direction numbers, dimensions 0-3 x 32 bits: the table of
-// shaders/includes/rt/sampler_sobol_tables.glsl:10-47 (data, not derivable:
-// dimension 2 is not the textbook Joe-Kuo dimension).
-const uint32_t kSobolDirs[128] = {
-    0x80000000u, 0x40000000u, 0x20000000u, 0x10000000u, 0x08000000u, 0x04000000u, 0x02000000u, 0x01000000u,
-    0x00800000u, 0x00400000u, 0x00200000u, 0x00100000u, 0x00080000u, 0x00040000u, 0x00020000u, 0x00010000u,
-    0x00008000u, 0x00004000u, 0x00002000u, 0x00001000u, 0x00000800u, 0x00000400u, 0x00000200u, 0x00000100u,
-    0x00000080u, 0x00000040u, 0x00000020u, 0x00000010u, 0x00000008u, 0x00000004u, 0x00000002u, 0x00000001u,
-    0x80000000u, 0xC0000000u, 0xA0000000u, 0xF0000000u, 0x88000000u, 0xCC000000u, 0xAA000000u, 0xFF000000u,
-    0x80800000u, 0xC0C00000u, 0xA0A00000u, 0xF0F00000u, 0x88880000u, 0xCCCC0000u, 0xAAAA0000u, 0xFFFF0000u,
-    0x80008000u, 0xC000C000u, 0xA000A000u, 0xF000F000u, 0x88008800u, 0xCC00CC00u, 0xAA00AA00u, 0xFF00FF00u,
-    0x80808080u, 0xC0C0C0C0u, 0xA0A0A0A0u, 0xF0F0F0F0u, 0x88888888u, 0xCCCCCCCCu, 0xAAAAAAAAu, 0xFFFFFFFFu,
-    0x80000000u, 0x40000000u, 0xE0000000u, 0x50000000u, 0x98000000u, 0xBC000000u, 0xAE000000u, 0x25000000u,
-    0x5B800000u, 0x91400000u, 0x65600000u, 0x2E500000u, 0x91180000u, 0x88D40000u, 0xDD360000u, 0x02950000u,
-    0x4C888000u, 0x09EB4000u, 0x86CA6000u, 0x13B15000u, 0x42ADD800u, 0x3DF8D400u, 0x2FE57E00u, 0x56EB8100u,
-    0x8C41A680u, 0xE68455C0u, 0x3C9CE8E0u, 0xB44DBFF0u, 0x7C27F6C8u, 0x5239A6ACu, 0x853B0EDEu, 0x52EB2EF9u,
-    0x80000000u, 0xC0000000u, 0x20000000u, 0x50000000u, 0xF8000000u, 0x74000000u, 0xA2000000u, 0x93000000u,
-    0xD8800000u, 0x25400000u, 0x59E00000u, 0xE6D00000u, 0x78080000u, 0xB40C0000u, 0x82020000u, 0xC3050000u,
-    0x208F8000u, 0x51CBC000u, 0xFBEA2000u, 0x75AD5000u, 0xA00AF800u, 0x90077400u, 0xD800A200u, 0x25009300u,
-    0x59E08480u, 0xE6D0CEC0u, 0x78088520u, 0xB40CEBB0u, 0x82028348u, 0xC305C274u, 0x208FB552u, 0x51CB9AE9u,
-};
-
 struct DevBuf {
     void* p = nullptr;
     size_t n = 0;
@@ -114,7 +92,9 @@ struct ohao_pt_ctx {
     DevBuf scratch, build_scratch, err_flag;
     std::vector<DevBuf*> host_accum_bufs;
     ohao_pt_profile profile{};
+    ohao::PersistentState* persistent = nullptr;
     ~ohao_pt_ctx() {
+        if (persistent) ohao::persistent_destroy(persistent);
         for (auto* b : host_accum_bufs) delete b;
     }
 };
@@ -279,7 +259,6 @@ ohao_status ohao_pt_create(const ohao_pt_desc* desc, ohao_pt_ctx** out) {
         delete ctx;
         return OHAO_ERR_CUDA;
     }
-    ohao::upload_sobol_table(kSobolDirs);
     *out = ctx;
     return OHAO_OK;
 }
@@ -580,24 +559,17 @@ static ohao_status validate_render(ohao_pt_ctx* ctx, const ohao_pt_view* views, 
     if (st->spp == 0) return fail(ctx, OHAO_ERR_INVALID_ARG, "render: spp must be >= 1");
     if (st->max_bounces > 64) return fail(ctx, OHAO_ERR_INVALID_ARG, "render: max_bounces > 64");
     if (st->sampler > 1) return fail(ctx, OHAO_ERR_INVALID_ARG, "render: unknown sampler");
-    if (st->mode == OHAO_PT_MODE_PERSISTENT) return fail(ctx, OHAO_ERR_UNSUPPORTED, "render: persistent mode not built yet");
+    if (st->mode > OHAO_PT_MODE_PERSISTENT) return fail(ctx, OHAO_ERR_INVALID_ARG, "render: unknown mode");
     for (uint32_t v = 0; v < n_views; ++v)
         if (views[v].width == 0 || views[v].height == 0 || static_cast<uint64_t>(views[v].width) * views[v].height > (1ull << 31))
             return fail(ctx, OHAO_ERR_INVALID_ARG, "render: bad view size");
     return OHAO_OK;
 }
 
-static ohao_status render_views(ohao_pt_ctx* ctx, const ohao_pt_view* views, uint32_t n_views,
-                                const ohao_pt_settings* st, float* const* dev_accum, cudaStream_t cs) {
-    const bool profile = (st->flags & OHAO_PT_FLAG_PROFILE) != 0;
-    ohao::ProfileAcc acc;
-    const uint32_t cap = ohao::wavefront_default_capacity();
-    CK(ctx->scratch.ensure(ohao::wavefront_scratch_bytes(cap)), "render scratch");
-    ohao::DScene sc = make_scene(ctx);
-    ohao::PathParams pp{st->max_bounces, st->sampler, st->flags, st->clamp_luminance, st->aniso_strength,
-                        st->aniso_rotation, st->sample_index_base};
-    for (uint32_t v = 0; v < n_views; ++v) {
-        ohao::RenderView rv{};
+static std::vector<ohao::RenderView> to_render_views(const ohao_pt_view* views, uint32_t n, float* const* dev_accum) {
+    std::vector<ohao::RenderView> out(n);
+    for (uint32_t v = 0; v < n; ++v) {
+        ohao::RenderView& rv = out[v];
         std::memcpy(rv.vp.inv_view, views[v].inv_view, 64);
         std::memcpy(rv.vp.inv_proj, views[v].inv_proj, 64);
         rv.vp.width = views[v].width;
@@ -606,10 +578,46 @@ static ohao_status render_views(ohao_pt_ctx* ctx, const ohao_pt_view* views, uin
         rv.history = views[v].history;
         rv.path_out = views[v].path_radiance;
         rv.aov = views[v].aov;
+    }
+    return out;
+}
+
+static bool use_persistent(const ohao_pt_settings* st, uint32_t n_views) {
+    return st->mode == OHAO_PT_MODE_PERSISTENT || (st->mode == OHAO_PT_MODE_AUTO && n_views > 1);
+}
+
+static ohao_status ensure_persistent(ohao_pt_ctx* ctx) {
+    if (!ctx->persistent) ctx->persistent = ohao::persistent_create();
+    if (!ctx->persistent) return fail(ctx, OHAO_ERR_OOM, "persistent renderer: allocation failed");
+    return OHAO_OK;
+}
+
+static ohao_status render_views(ohao_pt_ctx* ctx, const ohao_pt_view* views, uint32_t n_views,
+                                const ohao_pt_settings* st, float* const* dev_accum, cudaStream_t cs) {
+    const bool profile = (st->flags & OHAO_PT_FLAG_PROFILE) != 0;
+    ohao::ProfileAcc acc;
+    ohao::DScene sc = make_scene(ctx);
+    ohao::PathParams pp{st->max_bounces, st->sampler, st->flags, st->clamp_luminance, st->aniso_strength,
+                        st->aniso_rotation, st->sample_index_base};
+    const std::vector<ohao::RenderView> rvs = to_render_views(views, n_views, dev_accum);
+    if (use_persistent(st, n_views)) {
+        ohao_status s = ensure_persistent(ctx);
+        if (s != OHAO_OK) return s;
+        if (n_views > ohao::persistent_max_views())
+            return fail(ctx, OHAO_ERR_INVALID_ARG, "render: more views than the persistent queue holds (1024)");
         std::string err;
-        const ohao_status s = ohao::wavefront_render(sc, rv, pp, st->spp, ctx->scratch.p, ctx->scratch.n, cap, cs,
-                                                     profile, &acc, ctx->err_flag.as<int>(), err);
+        s = ohao::persistent_render(ctx->persistent, sc, rvs.data(), n_views, pp, st->spp, ctx->flat.root_box, cs,
+                                    ctx->err_flag.as<int>(), profile, &acc, err);
         if (s != OHAO_OK) return fail(ctx, s, err);
+    } else {
+        const uint32_t cap = ohao::wavefront_default_capacity();
+        CK(ctx->scratch.ensure(ohao::wavefront_scratch_bytes(cap)), "render scratch");
+        for (uint32_t v = 0; v < n_views; ++v) {
+            std::string err;
+            const ohao_status s = ohao::wavefront_render(sc, rvs[v], pp, st->spp, ctx->scratch.p, ctx->scratch.n, cap,
+                                                         cs, profile, &acc, ctx->err_flag.as<int>(), err);
+            if (s != OHAO_OK) return fail(ctx, s, err);
+        }
     }
     if (profile) {
         ohao_pt_profile& p = ctx->profile;
@@ -622,6 +630,32 @@ static ohao_status render_views(ohao_pt_ctx* ctx, const ohao_pt_view* views, uin
         p.nodes_shadow = acc.nodes_shadow; p.tris_shadow = acc.tris_shadow;
     }
     return OHAO_OK;
+}
+
+ohao_status ohao_pt_autotune(ohao_pt_ctx* ctx, const ohao_pt_view* views, uint32_t n_views,
+                             const ohao_pt_settings* st, float* best_ms, ohao_stream stream) {
+    ohao_status s = validate_render(ctx, views, n_views, st);
+    if (s != OHAO_OK) return s;
+    if (n_views > ohao::persistent_max_views()) return fail(ctx, OHAO_ERR_INVALID_ARG, "autotune: too many views");
+    std::vector<float*> acc(n_views);
+    for (uint32_t v = 0; v < n_views; ++v) {
+        if (!views[v].accum) return fail(ctx, OHAO_ERR_INVALID_ARG, "autotune: view accum is null");
+        acc[v] = views[v].accum;
+    }
+    if ((s = ensure_persistent(ctx)) != OHAO_OK) return s;
+    cudaStream_t cs = reinterpret_cast<cudaStream_t>(stream);
+    ohao::PathParams pp{st->max_bounces, st->sampler, st->flags, st->clamp_luminance, st->aniso_strength,
+                        st->aniso_rotation, st->sample_index_base};
+    const std::vector<ohao::RenderView> rvs = to_render_views(views, n_views, acc.data());
+    std::string err;
+    s = ohao::persistent_autotune(ctx->persistent, make_scene(ctx), rvs.data(), n_views, pp, st->spp,
+                                  ctx->flat.root_box, cs, ctx->err_flag.as<int>(), best_ms, err);
+    if (s != OHAO_OK) return fail(ctx, s, err);
+    return check_device_error(ctx, cs);
+}
+
+const char* ohao_pt_launch_config(const ohao_pt_ctx* ctx) {
+    return ctx && ctx->persistent ? ohao::persistent_variant_name(ctx->persistent) : "default";
 }
 
 ohao_status ohao_pt_render(ohao_pt_ctx* ctx, const ohao_pt_view* views, uint32_t n_views,

@@ -16,7 +16,28 @@
 
 namespace ohao {
 
-__constant__ uint32_t c_sobol_dirs[128];
+// Sobol direction numbers, dimensions 0-3 x 32 bits: the table of
+// shaders/includes/rt/sampler_sobol_tables.glsl:10-47 (data, not derivable:
+// dimension 2 is not the textbook Joe-Kuo dimension). Initialised statically
+// so that every translation unit that includes this header carries it.
+__constant__ uint32_t c_sobol_dirs[128] = {
+    0x80000000u, 0x40000000u, 0x20000000u, 0x10000000u, 0x08000000u, 0x04000000u, 0x02000000u, 0x01000000u,
+    0x00800000u, 0x00400000u, 0x00200000u, 0x00100000u, 0x00080000u, 0x00040000u, 0x00020000u, 0x00010000u,
+    0x00008000u, 0x00004000u, 0x00002000u, 0x00001000u, 0x00000800u, 0x00000400u, 0x00000200u, 0x00000100u,
+    0x00000080u, 0x00000040u, 0x00000020u, 0x00000010u, 0x00000008u, 0x00000004u, 0x00000002u, 0x00000001u,
+    0x80000000u, 0xC0000000u, 0xA0000000u, 0xF0000000u, 0x88000000u, 0xCC000000u, 0xAA000000u, 0xFF000000u,
+    0x80800000u, 0xC0C00000u, 0xA0A00000u, 0xF0F00000u, 0x88880000u, 0xCCCC0000u, 0xAAAA0000u, 0xFFFF0000u,
+    0x80008000u, 0xC000C000u, 0xA000A000u, 0xF000F000u, 0x88008800u, 0xCC00CC00u, 0xAA00AA00u, 0xFF00FF00u,
+    0x80808080u, 0xC0C0C0C0u, 0xA0A0A0A0u, 0xF0F0F0F0u, 0x88888888u, 0xCCCCCCCCu, 0xAAAAAAAAu, 0xFFFFFFFFu,
+    0x80000000u, 0x40000000u, 0xE0000000u, 0x50000000u, 0x98000000u, 0xBC000000u, 0xAE000000u, 0x25000000u,
+    0x5B800000u, 0x91400000u, 0x65600000u, 0x2E500000u, 0x91180000u, 0x88D40000u, 0xDD360000u, 0x02950000u,
+    0x4C888000u, 0x09EB4000u, 0x86CA6000u, 0x13B15000u, 0x42ADD800u, 0x3DF8D400u, 0x2FE57E00u, 0x56EB8100u,
+    0x8C41A680u, 0xE68455C0u, 0x3C9CE8E0u, 0xB44DBFF0u, 0x7C27F6C8u, 0x5239A6ACu, 0x853B0EDEu, 0x52EB2EF9u,
+    0x80000000u, 0xC0000000u, 0x20000000u, 0x50000000u, 0xF8000000u, 0x74000000u, 0xA2000000u, 0x93000000u,
+    0xD8800000u, 0x25400000u, 0x59E00000u, 0xE6D00000u, 0x78080000u, 0xB40C0000u, 0x82020000u, 0xC3050000u,
+    0x208F8000u, 0x51CBC000u, 0xFBEA2000u, 0x75AD5000u, 0xA00AF800u, 0x90077400u, 0xD800A200u, 0x25009300u,
+    0x59E08480u, 0xE6D0CEC0u, 0x78088520u, 0xB40CEBB0u, 0x82028348u, 0xC305C274u, 0x208FB552u, 0x51CB9AE9u,
+};
 
 constexpr uint32_t kSamplerPCG = 0, kSamplerSobol = 1;
 constexpr uint32_t kFlagFirefly = 1u << 2;

@@ -83,7 +83,6 @@ struct ProfileAcc {
 };
 
 // wavefront.cu
-void upload_sobol_table(const uint32_t* dirs128);
 size_t wavefront_scratch_bytes(uint32_t capacity);
 uint32_t wavefront_default_capacity();
 ohao_status wavefront_render(const DScene& sc, const RenderView& view, const PathParams& pp, uint32_t spp,
@@ -91,5 +90,19 @@ ohao_status wavefront_render(const DScene& sc, const RenderView& view, const Pat
                              ProfileAcc* prof, int* d_err, std::string& err);
 ohao_status trace_rays(const DScene& sc, const float* rays, uint32_t n, uint32_t* hits, int any_hit, uint32_t* stats,
                        cudaStream_t st, int* d_err, std::string& err);
+
+// persistent.cu
+struct PersistentState;
+PersistentState* persistent_create();
+void persistent_destroy(PersistentState* s);
+uint32_t persistent_max_views();
+const char* persistent_variant_name(const PersistentState* s);
+// scene_box: 6 floats (lo.xyz, hi.xyz) bounding the scene, for ray reordering
+ohao_status persistent_render(PersistentState* s, const DScene& sc, const RenderView* views, uint32_t n,
+                              const PathParams& pp, uint32_t spp, const float* scene_box, cudaStream_t st, int* d_err,
+                              bool profile, ProfileAcc* prof, std::string& err);
+ohao_status persistent_autotune(PersistentState* s, const DScene& sc, const RenderView* views, uint32_t n,
+                                const PathParams& pp, uint32_t spp, const float* scene_box, cudaStream_t st, int* d_err,
+                                float* best_ms, std::string& err);
 
 }  // namespace ohao

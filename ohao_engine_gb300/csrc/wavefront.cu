@@ -14,8 +14,11 @@
 // Every kernel is a grid-stride loop over a device-side count, so the launch
 // sequence is fixed and does not read counts back to the host.
 #include "pt_path.cuh"
+#include "radix_sort.cuh"
 
 #include <algorithm>
+#include <cstddef>
+#include <cstring>
 #include <vector>
 
 namespace ohao {
@@ -42,8 +45,50 @@ struct Soa {
     float4* shEc;
     uint32_t* q_ray[2];
     uint32_t* q_sh;
-    uint32_t* counts;    // [0],[1] ray queue counts, [2] shadow count
+    uint32_t* counts;    // [0],[1] ray queue counts, [2] shadow count, [3] done count, [4] work claimed
+    // persistent pool only: slot -> (global pixel, sample), running mean, finished-path queue
+    uint32_t* pix;
+    uint32_t* smp;
+    float4* acc;
+    uint32_t* q_done;
+    // persistent pool only: ray-queue reordering (keys/values ping-pong, histogram)
+    uint32_t *skA, *svA, *skB, *svB, *shist;
 };
+
+// Persistent multi-view pool: per-call view table in device memory.
+constexpr uint32_t kMaxViews = 1024;
+constexpr uint32_t kIdle = 0xFFFFFFFFu;
+
+struct PView {
+    ViewParams vp;
+    float* accum;
+    float* path_out;
+    float* aov;
+    uint32_t history;
+    uint32_t pix_begin;
+    uint32_t npix;
+    uint32_t pad;
+};
+
+struct LaunchBlock {
+    uint32_t nviews;
+    uint32_t total_pix;
+    uint32_t spp;
+    uint32_t pad;
+    float box_lo[4];          // scene bounds for the ray-reordering key
+    float box_scale[4];       // 128 / extent per axis
+    PView views[kMaxViews];
+};
+
+__device__ __forceinline__ uint32_t find_view(const LaunchBlock* lb, uint32_t g) {
+    uint32_t lo = 0, hi = lb->nviews - 1;
+    while (lo < hi) {
+        const uint32_t mid = (lo + hi + 1) / 2;
+        if (lb->views[mid].pix_begin <= g) lo = mid;
+        else hi = mid - 1;
+    }
+    return lo;
+}
 
 constexpr uint32_t kFlagDelta = 1u << 10, kFlagShL = 1u << 11, kFlagShE = 1u << 12;
 
@@ -130,15 +175,36 @@ __global__ void __launch_bounds__(128) k_extend(DScene sc, Soa s, int cur, int* 
     }
 }
 
-__global__ void __launch_bounds__(128) k_shade(DScene sc, PathParams pp, ViewParams vp, uint32_t w0, uint32_t npix,
-                                               Soa s, int cur, float* aov, uint32_t aov_k) {
+// kPool: slot -> (pixel, sample) comes from the pool arrays and the view
+// table; finished paths are queued for regeneration. Otherwise a slot is
+// the sample-major index inside the wave [w0, w0 + n) of one view.
+template <bool kPool>
+__global__ void __launch_bounds__(128) k_shade(DScene sc, PathParams pp, ViewParams vp_plain, uint32_t w0,
+                                               uint32_t npix_plain, Soa s, int cur, float* aov_plain, uint32_t aov_k,
+                                               const LaunchBlock* lb) {
     const uint32_t count = s.counts[cur];
     const uint32_t* q = s.q_ray[cur];
     uint32_t* qn = s.q_ray[cur ^ 1];
     for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < count; i += gridDim.x * blockDim.x) {
         const uint32_t p = q[i];
-        const uint32_t lin = w0 + p;
-        const uint32_t k = lin / npix, pix = lin - k * npix;
+        uint32_t k, pix;
+        const ViewParams* vpp;
+        float* aov;
+        if (kPool) {
+            const uint32_t g = s.pix[p];
+            const PView& pv = lb->views[find_view(lb, g)];
+            k = s.smp[p];
+            pix = g - pv.pix_begin;
+            vpp = &pv.vp;
+            aov = pv.aov;
+        } else {
+            const uint32_t lin = w0 + p;
+            k = lin / npix_plain;
+            pix = lin - k * npix_plain;
+            vpp = &vp_plain;
+            aov = aov_plain;
+        }
+        const ViewParams& vp = *vpp;
         const uint32_t px = pix % vp.width, py = pix / vp.width;
         PathState ps;
         load_state(s, p, ps);
@@ -174,6 +240,122 @@ __global__ void __launch_bounds__(128) k_shade(DScene sc, PathParams pp, ViewPar
         if (slot != 0xFFFFFFFFu) qn[slot] = p;
         const uint32_t sslot = warp_push(s.counts + 2, extra != 0u);
         if (sslot != 0xFFFFFFFFu) s.q_sh[sslot] = p;
+        if (kPool) {
+            const uint32_t dslot = warp_push(s.counts + 3, !more);
+            if (dslot != 0xFFFFFFFFu) s.q_done[dslot] = p;
+        }
+    }
+}
+
+// Pool ray reordering: 24-bit key = direction octant (3 bits, most
+// significant) + Morton code of the origin on a 128^3 grid over the scene box.
+__device__ __forceinline__ uint32_t spread7(uint32_t v) {
+    v &= 0x7Fu;
+    v = (v | (v << 8)) & 0x0000F00Fu;
+    v = (v | (v << 4)) & 0x000C30C3u;
+    v = (v | (v << 2)) & 0x00249249u;
+    return v;
+}
+
+__global__ void k_ray_keys(const LaunchBlock* lb, Soa s, int cur) {
+    const uint32_t count = s.counts[cur];
+    const uint32_t* q = s.q_ray[cur];
+    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < count; i += gridDim.x * blockDim.x) {
+        const uint32_t p = q[i];
+        const float4 o = s.ro[p], d = s.rd[p];
+        const uint32_t oct = (d.x < 0.0f ? 4u : 0u) | (d.y < 0.0f ? 2u : 0u) | (d.z < 0.0f ? 1u : 0u);
+        const float fx = (o.x - lb->box_lo[0]) * lb->box_scale[0];
+        const float fy = (o.y - lb->box_lo[1]) * lb->box_scale[1];
+        const float fz = (o.z - lb->box_lo[2]) * lb->box_scale[2];
+        const uint32_t ix = static_cast<uint32_t>(fminf(fmaxf(fx, 0.0f), 127.0f));
+        const uint32_t iy = static_cast<uint32_t>(fminf(fmaxf(fy, 0.0f), 127.0f));
+        const uint32_t iz = static_cast<uint32_t>(fminf(fmaxf(fz, 0.0f), 127.0f));
+        s.skA[i] = (oct << 21) | (spread7(ix) << 2) | (spread7(iy) << 1) | spread7(iz);
+        s.svA[i] = p;
+    }
+}
+
+__global__ void k_copy_queue(Soa s, int cur) {
+    const uint32_t count = s.counts[cur];
+    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < count; i += gridDim.x * blockDim.x)
+        s.q_ray[cur][i] = s.svA[i];
+}
+
+// Pool: every slot starts idle and queued for regeneration.
+__global__ void k_pool_init(Soa s, uint32_t cap) {
+    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < cap; i += gridDim.x * blockDim.x) {
+        s.pix[i] = kIdle;
+        s.q_done[i] = i;
+    }
+    if (blockIdx.x == 0 && threadIdx.x == 0) {
+        s.counts[0] = 0;
+        s.counts[1] = 0;
+        s.counts[3] = cap;
+        s.counts[4] = 0;
+    }
+}
+
+// Pool regeneration (after the shadow pass of an iteration): a finished
+// path is folded into its slot's running mean in sample order; the slot
+// then starts the pixel's next sample, or writes the pixel and claims the
+// next pixel of the work queue (one atomic per warp). New primary rays are
+// appended to the ray queue of the coming iteration.
+__global__ void __launch_bounds__(128) k_regen(PathParams pp, const LaunchBlock* lb, Soa s, int cur) {
+    const uint32_t count = s.counts[3];
+    uint32_t* q = s.q_ray[cur];
+    const uint32_t total = lb->total_pix, spp = lb->spp;
+    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < count; i += gridDim.x * blockDim.x) {
+        const uint32_t p = s.q_done[i];
+        uint32_t g = s.pix[p];
+        uint32_t k = s.smp[p];
+        float4 acc = s.acc[p];
+        bool start = false;
+        if (g != kIdle) {
+            const PView& pv = lb->views[find_view(lb, g)];
+            const uint32_t pix = g - pv.pix_begin;
+            const V3 L = firefly(pp, ld3(s.rad[p]));
+            if (pv.path_out)
+                reinterpret_cast<float4*>(pv.path_out)[static_cast<size_t>(k) * pv.npix + pix] = f4(L, 0.0f);
+            if (pv.history + k == 0) {
+                acc = make_float4(L.x, L.y, L.z, 1.0f);
+            } else {
+                const float cnt = acc.w + 1.0f;
+                acc.x = (acc.x * acc.w + L.x) / cnt;
+                acc.y = (acc.y * acc.w + L.y) / cnt;
+                acc.z = (acc.z * acc.w + L.z) / cnt;
+                acc.w = cnt;
+            }
+            k++;
+            if (k < spp) {
+                start = true;
+            } else {
+                reinterpret_cast<float4*>(pv.accum)[pix] = acc;
+                g = kIdle;
+            }
+        }
+        const uint32_t claim = warp_push(s.counts + 4, g == kIdle);
+        if (g == kIdle && claim < total) {
+            g = claim;
+            k = 0;
+            const PView& pv = lb->views[find_view(lb, g)];
+            const uint32_t pix = g - pv.pix_begin;
+            acc = pv.history > 0 ? reinterpret_cast<const float4*>(pv.accum)[pix] : make_float4(0.f, 0.f, 0.f, 0.f);
+            start = true;
+        }
+        if (start) {
+            const PView& pv = lb->views[find_view(lb, g)];
+            const uint32_t pix = g - pv.pix_begin;
+            PathState ps;
+            path_start(pv.vp, pp, pix % pv.vp.width, pix / pv.vp.width, pp.sample_base + k, ps);
+            store_state(s, p, ps, 0u);
+        } else {
+            g = kIdle;
+        }
+        s.pix[p] = g;
+        s.smp[p] = k;
+        s.acc[p] = acc;
+        const uint32_t slot = warp_push(s.counts + cur, start);
+        if (slot != 0xFFFFFFFFu) q[slot] = p;
     }
 }
 
@@ -301,6 +483,15 @@ Soa carve_soa_at(Carve& c, uint32_t cap) {
     s.q_ray[1] = c.take<uint32_t>(cap);
     s.q_sh = c.take<uint32_t>(cap);
     s.counts = c.take<uint32_t>(64);
+    s.pix = c.take<uint32_t>(cap);
+    s.smp = c.take<uint32_t>(cap);
+    s.acc = c.take<float4>(cap);
+    s.q_done = c.take<uint32_t>(cap);
+    s.skA = c.take<uint32_t>(cap);
+    s.svA = c.take<uint32_t>(cap);
+    s.skB = c.take<uint32_t>(cap);
+    s.svB = c.take<uint32_t>(cap);
+    s.shist = c.take<uint32_t>(16 * static_cast<size_t>(rsort::tiles_for(cap)));
     return s;
 }
 
@@ -321,7 +512,7 @@ void init_launch_shapes() {
     int b = 0;
     cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, k_extend<false>, 128, 0);
     g_blocks_extend = std::max(1, b) * g_num_sms;
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, k_shade, 128, 0);
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, k_shade<false>, 128, 0);
     g_blocks_shade = std::max(1, b) * g_num_sms;
     cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, k_shadow<false>, 128, 0);
     g_blocks_shadow = std::max(1, b) * g_num_sms;
@@ -367,7 +558,6 @@ struct EvTimer {
 
 }  // namespace
 
-void upload_sobol_table(const uint32_t* dirs128) { cudaMemcpyToSymbol(c_sobol_dirs, dirs128, 128 * sizeof(uint32_t)); }
 
 size_t wavefront_scratch_bytes(uint32_t cap) {
     Carve c{nullptr};
@@ -413,8 +603,8 @@ ohao_status wavefront_render(const DScene& sc, const RenderView& view, const Pat
             cudaMemsetAsync(s.counts + (cur ^ 1), 0, 4, st);
             cudaMemsetAsync(s.counts + 2, 0, 4, st);
             tm.begin(1, a);
-            k_shade<<<g_blocks_shade, 128, 0, st>>>(sc, pp, view.vp, static_cast<uint32_t>(w0), npix, s, cur, view.aov,
-                                                    spp - 1);
+            k_shade<false><<<g_blocks_shade, 128, 0, st>>>(sc, pp, view.vp, static_cast<uint32_t>(w0), npix, s, cur,
+                                                           view.aov, spp - 1, nullptr);
             tm.end(1, a);
             tm.begin(2, a);
             if (profile) k_shadow<true><<<g_blocks_shadow, 128, 0, st>>>(sc, s, d_err, dstats);
@@ -462,6 +652,262 @@ ohao_status trace_rays(const DScene& sc, const float* rays, uint32_t n, uint32_t
         err = std::string("trace launch failed: ") + cudaGetErrorString(e);
         return OHAO_ERR_CUDA;
     }
+    return OHAO_OK;
+}
+
+// ---------------------------------------------------------------------------
+// Persistent multi-view pool
+//
+// One call renders all its views from one work queue of pixels (views
+// concatenated). A pool of `cap` path slots stays full: each iteration runs
+// regenerate -> extend -> shade -> shadow, where regenerate folds finished
+// paths into their pixel's running mean (samples of a pixel stay in one slot,
+// in sample order, so the result equals the per-view wavefront bit for bit)
+// and refills idle slots from the queue. A chunk of kChunk iterations is
+// captured once into a CUDA graph and replayed until the queue is drained;
+// the host reads four counters between chunks. The autotuner picks the pool
+// capacity.
+// ---------------------------------------------------------------------------
+namespace {
+constexpr int kChunk = 8;                       // iterations per graph replay (even)
+struct PoolVariant {
+    uint32_t cap;
+    bool reorder;
+    const char* name;
+};
+const PoolVariant kPool[] = {
+    {1u << 20, true, "pool_1M_sorted_chunk8"},  {1u << 21, true, "pool_2M_sorted_chunk8"},
+    {1u << 22, true, "pool_4M_sorted_chunk8"},  {1u << 21, false, "pool_2M_unsorted_chunk8"},
+    {1u << 22, false, "pool_4M_unsorted_chunk8"},
+};
+constexpr int kNumPool = sizeof(kPool) / sizeof(kPool[0]);
+constexpr int kDefaultPool = 1;
+constexpr uint64_t kMaxChunks = 1u << 20;       // bound on graph replays per call
+}  // namespace
+
+struct PersistentState {
+    LaunchBlock* d_lb = nullptr;
+    LaunchBlock* h_lb = nullptr;                // pinned staging
+    uint32_t* h_counts = nullptr;               // pinned readback
+    void* pool = nullptr;
+    size_t pool_bytes = 0;
+    uint32_t cap = 0;
+    int variant = -1;
+    cudaGraphExec_t graph = nullptr;
+    DScene graph_scene{};
+    PathParams graph_pp{};
+    int* graph_err = nullptr;
+    int graph_variant = -1;
+};
+
+PersistentState* persistent_create() {
+    auto* s = new PersistentState();
+    if (cudaMalloc(&s->d_lb, sizeof(LaunchBlock)) != cudaSuccess ||
+        cudaMallocHost(&s->h_lb, sizeof(LaunchBlock)) != cudaSuccess ||
+        cudaMallocHost(&s->h_counts, 64) != cudaSuccess) {
+        persistent_destroy(s);
+        return nullptr;
+    }
+    return s;
+}
+
+void persistent_destroy(PersistentState* s) {
+    if (!s) return;
+    if (s->graph) cudaGraphExecDestroy(s->graph);
+    if (s->pool) cudaFree(s->pool);
+    if (s->d_lb) cudaFree(s->d_lb);
+    if (s->h_lb) cudaFreeHost(s->h_lb);
+    if (s->h_counts) cudaFreeHost(s->h_counts);
+    delete s;
+}
+
+uint32_t persistent_max_views() { return kMaxViews; }
+
+const char* persistent_variant_name(const PersistentState* s) {
+    return s && s->variant >= 0 ? kPool[s->variant].name : "default";
+}
+
+namespace {
+
+ohao_status stage_views(PersistentState* s, const RenderView* views, uint32_t n, uint32_t spp, const float* box,
+                        cudaStream_t st, std::string& err) {
+    if (n == 0 || n > kMaxViews) {
+        err = "persistent render: view count outside [1, 1024]";
+        return OHAO_ERR_INVALID_ARG;
+    }
+    cudaStreamSynchronize(st);   // the pinned staging block may still be in flight
+    LaunchBlock& lb = *s->h_lb;
+    lb.nviews = n;
+    lb.spp = spp;
+    for (int a = 0; a < 3; ++a) {
+        const float ext = box[3 + a] - box[a];
+        lb.box_lo[a] = box[a];
+        lb.box_scale[a] = ext > 0.0f ? 128.0f / ext : 0.0f;
+    }
+    uint64_t off = 0;
+    for (uint32_t v = 0; v < n; ++v) {
+        PView& pv = lb.views[v];
+        pv.vp = views[v].vp;
+        pv.accum = views[v].accum;
+        pv.path_out = views[v].path_out;
+        pv.aov = views[v].aov;
+        pv.history = views[v].history;
+        pv.pix_begin = static_cast<uint32_t>(off);
+        pv.npix = views[v].vp.width * views[v].vp.height;
+        off += pv.npix;
+    }
+    if (off >= (1ull << 31)) {
+        err = "persistent render: more than 2^31 pixels in one call";
+        return OHAO_ERR_INVALID_ARG;
+    }
+    lb.total_pix = static_cast<uint32_t>(off);
+    const size_t bytes = offsetof(LaunchBlock, views) + sizeof(PView) * n;
+    if (cudaMemcpyAsync(s->d_lb, s->h_lb, bytes, cudaMemcpyHostToDevice, st) != cudaSuccess) {
+        err = "persistent render: view table upload failed";
+        return OHAO_ERR_CUDA;
+    }
+    return OHAO_OK;
+}
+
+void enqueue_chunk(const DScene& sc, const PathParams& pp, const LaunchBlock* lb, const Soa& s, uint32_t cap,
+                   bool reorder, int* d_err, cudaStream_t st) {
+    for (int it = 0; it < kChunk; ++it) {
+        const int cur = it & 1;
+        k_regen<<<g_blocks_shade, 128, 0, st>>>(pp, lb, s, cur);
+        if (reorder) {
+            k_ray_keys<<<g_blocks_shade, 128, 0, st>>>(lb, s, cur);
+            rsort::sort_pairs(s.skA, s.svA, s.skB, s.svB, s.shist, s.counts + cur, cap, 24, st);
+            k_copy_queue<<<g_blocks_shade, 128, 0, st>>>(s, cur);
+        }
+        k_extend<false><<<g_blocks_extend, 128, 0, st>>>(sc, s, cur, d_err, nullptr);
+        cudaMemsetAsync(s.counts + (cur ^ 1), 0, 4, st);
+        cudaMemsetAsync(s.counts + 2, 0, 8, st);   // shadow and done counts
+        k_shade<true><<<g_blocks_shade, 128, 0, st>>>(sc, pp, ViewParams{}, 0u, 1u, s, cur, nullptr, 0u, lb);
+        k_shadow<false><<<g_blocks_shadow, 128, 0, st>>>(sc, s, d_err, nullptr);
+    }
+}
+
+ohao_status run_pool(PersistentState* s, int variant, const DScene& sc, const PathParams& pp, cudaStream_t st,
+                     int* d_err, bool use_graph, std::string& err) {
+    init_launch_shapes();
+    const uint32_t cap = kPool[variant].cap;
+    const bool reorder = kPool[variant].reorder;
+    const size_t need = wavefront_scratch_bytes(cap);
+    if (s->pool_bytes < need) {
+        if (s->graph) { cudaGraphExecDestroy(s->graph); s->graph = nullptr; }
+        if (s->pool) cudaFree(s->pool);
+        s->pool = nullptr;
+        s->pool_bytes = 0;
+        if (cudaMalloc(&s->pool, need) != cudaSuccess) {
+            err = "persistent render: pool allocation failed";
+            return OHAO_ERR_OOM;
+        }
+        s->pool_bytes = need;
+    }
+    const Soa soa = carve_soa(s->pool, cap);
+    k_pool_init<<<g_blocks_shade, 128, 0, st>>>(soa, cap);
+    if (use_graph) {
+        const bool stale = !s->graph || s->graph_variant != variant || s->graph_err != d_err ||
+                           std::memcmp(&s->graph_scene, &sc, sizeof(DScene)) != 0 ||
+                           std::memcmp(&s->graph_pp, &pp, sizeof(PathParams)) != 0;
+        if (stale) {
+            if (s->graph) { cudaGraphExecDestroy(s->graph); s->graph = nullptr; }
+            cudaStream_t cap_st;
+            if (cudaStreamCreateWithFlags(&cap_st, cudaStreamNonBlocking) != cudaSuccess) {
+                err = "persistent: capture stream";
+                return OHAO_ERR_CUDA;
+            }
+            cudaGraph_t g = nullptr;
+            cudaStreamBeginCapture(cap_st, cudaStreamCaptureModeThreadLocal);
+            enqueue_chunk(sc, pp, s->d_lb, soa, cap, reorder, d_err, cap_st);
+            cudaError_t e = cudaStreamEndCapture(cap_st, &g);
+            if (e == cudaSuccess) e = cudaGraphInstantiate(&s->graph, g, 0);
+            if (g) cudaGraphDestroy(g);
+            cudaStreamDestroy(cap_st);
+            if (e != cudaSuccess) {
+                s->graph = nullptr;
+                err = std::string("persistent graph: ") + cudaGetErrorString(e);
+                return OHAO_ERR_CUDA;
+            }
+            s->graph_variant = variant;
+            s->graph_err = d_err;
+            s->graph_scene = sc;
+            s->graph_pp = pp;
+        }
+    }
+    for (uint64_t chunk = 0;; ++chunk) {
+        if (chunk >= kMaxChunks) {
+            err = "persistent render: work queue did not drain within the iteration bound";
+            return OHAO_ERR_TIMEOUT;
+        }
+        if (use_graph) {
+            const cudaError_t e = cudaGraphLaunch(s->graph, st);
+            if (e != cudaSuccess) { err = std::string("persistent graph launch: ") + cudaGetErrorString(e); return OHAO_ERR_CUDA; }
+        } else {
+            enqueue_chunk(sc, pp, s->d_lb, soa, cap, reorder, d_err, st);
+        }
+        cudaMemcpyAsync(s->h_counts, soa.counts, 5 * sizeof(uint32_t), cudaMemcpyDeviceToHost, st);
+        const cudaError_t e = cudaStreamSynchronize(st);
+        if (e != cudaSuccess) { err = std::string("persistent render: ") + cudaGetErrorString(e); return OHAO_ERR_CUDA; }
+        const uint32_t pending = s->h_counts[0], done = s->h_counts[3], claimed = s->h_counts[4];
+        if (pending == 0 && done == 0 && claimed >= s->h_lb->total_pix) break;
+    }
+    return OHAO_OK;
+}
+
+}  // namespace
+
+ohao_status persistent_render(PersistentState* s, const DScene& sc, const RenderView* views, uint32_t n,
+                              const PathParams& pp, uint32_t spp, const float* scene_box, cudaStream_t st, int* d_err,
+                              bool profile, ProfileAcc* prof, std::string& err) {
+    ohao_status r = stage_views(s, views, n, spp, scene_box, st, err);
+    if (r != OHAO_OK) return r;
+    cudaEvent_t e0 = nullptr, e1 = nullptr;
+    if (profile) {
+        cudaEventCreate(&e0);
+        cudaEventCreate(&e1);
+        cudaEventRecord(e0, st);
+    }
+    r = run_pool(s, s->variant >= 0 ? s->variant : kDefaultPool, sc, pp, st, d_err, true, err);
+    if (profile && prof) {
+        cudaEventRecord(e1, st);
+        cudaEventSynchronize(e1);
+        float ms = 0;
+        cudaEventElapsedTime(&ms, e0, e1);
+        prof->other_ms += ms;
+        prof->total_ms += ms;
+        prof->other_launches += 1;
+        cudaEventDestroy(e0);
+        cudaEventDestroy(e1);
+    }
+    return r;
+}
+
+ohao_status persistent_autotune(PersistentState* s, const DScene& sc, const RenderView* views, uint32_t n,
+                                const PathParams& pp, uint32_t spp, const float* scene_box, cudaStream_t st, int* d_err,
+                                float* best_ms, std::string& err) {
+    ohao_status r = stage_views(s, views, n, spp, scene_box, st, err);
+    if (r != OHAO_OK) return r;
+    float best = 1e30f;
+    int bi = kDefaultPool;
+    cudaEvent_t e0, e1;
+    cudaEventCreate(&e0);
+    cudaEventCreate(&e1);
+    for (int v = 0; v < kNumPool; ++v) {
+        cudaEventRecord(e0, st);
+        r = run_pool(s, v, sc, pp, st, d_err, false, err);
+        cudaEventRecord(e1, st);
+        cudaEventSynchronize(e1);
+        if (r != OHAO_OK) break;
+        float ms = 0;
+        cudaEventElapsedTime(&ms, e0, e1);
+        if (ms < best) { best = ms; bi = v; }
+    }
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    if (r != OHAO_OK) return r;
+    s->variant = bi;
+    if (best_ms) *best_ms = best;
     return OHAO_OK;
 }
 

@@ -186,3 +186,56 @@ def test_full_size_sphere_properties(gpu_lib, oracle):
     pix = np.sort(rng.choice(v.width * v.height, 4000, replace=False)).astype(np.uint32)
     o = orc.render_paths(v, dict(max_bounces=4, sampler=0), 0, 1, pixels=pix)
     assert_paths_match(g[:, pix], o, "sphere_1m subset")
+
+
+@pytest.mark.parametrize("two_level", [False, True])
+def test_persistent_multiview_matches_wavefront_and_oracle(gpu_lib, oracle, two_level):
+    """The persistent multi-view kernel produces the same paths and
+    accumulators as the per-view wavefront, bit for bit."""
+    import torch
+    og = gpu_lib
+    if two_level:
+        sd = small_instanced(side=20)
+        fl = 1
+        sd.views = [scenes.look_at_view(np.array([60.0, 10.0 * k, 40.0]), (0, 0, 0), width=16 + 4 * k, height=12 + 2 * k)
+                    for k in range(5)]
+    else:
+        sd = small_env_scene(freq=12)
+        fl = 0
+        sd.views = [scenes.look_at_view((0.5 * k, 0.6, 3.2), (0, -0.1, 0), width=20 + 6 * k, height=14 + 3 * k)
+                    for k in range(5)]
+    pt = gpu_tracer(og, sd, flatten_limit=fl)
+    orc = oracle.OracleScene(sd, flatten_limit=fl if fl else 1 << 25)
+    spp = 3
+    outs = {}
+    for mode in (og.MODE_WAVEFRONT, og.MODE_PERSISTENT):
+        accs, paths, views = [], [], []
+        for v in sd.views:
+            npix = v.width * v.height
+            a = torch.full((npix, 4), 7.0, dtype=torch.float32, device="cuda")
+            p = torch.zeros((spp, npix, 4), dtype=torch.float32, device="cuda")
+            accs.append(a)
+            paths.append(p)
+            views.append(og.make_view(v, accum=a, history=0, path_radiance=p))
+        pt.render(views, og.make_settings(spp=spp, max_bounces=4, sampler=1, sample_index_base=5, mode=mode))
+        torch.cuda.synchronize()
+        outs[mode] = ([a.cpu().numpy() for a in accs], [p.cpu().numpy()[:, :, :3] for p in paths])
+    for k, v in enumerate(sd.views):
+        assert np.array_equal(outs[og.MODE_WAVEFRONT][0][k], outs[og.MODE_PERSISTENT][0][k]), f"accum view {k}"
+        assert np.array_equal(outs[og.MODE_WAVEFRONT][1][k], outs[og.MODE_PERSISTENT][1][k]), f"paths view {k}"
+        o = orc.render_paths(v, dict(max_bounces=4, sampler=1), 5, spp)
+        assert_paths_match(outs[og.MODE_PERSISTENT][1][k], o, f"persistent view {k}")
+    # autotune picks a variant and renders stay identical
+    views = [og.make_view(v, accum=torch.zeros((v.width * v.height, 4), device="cuda")) for v in sd.views]
+    ms = pt.autotune(views, og.make_settings(spp=spp, max_bounces=4, sampler=1, sample_index_base=5))
+    assert ms > 0 and pt.launch_config != "default"
+    accs = []
+    views = []
+    for v in sd.views:
+        a = torch.zeros((v.width * v.height, 4), dtype=torch.float32, device="cuda")
+        accs.append(a)
+        views.append(og.make_view(v, accum=a))
+    pt.render(views, og.make_settings(spp=spp, max_bounces=4, sampler=1, sample_index_base=5, mode=og.MODE_PERSISTENT))
+    torch.cuda.synchronize()
+    for k in range(len(sd.views)):
+        assert np.array_equal(accs[k].cpu().numpy(), outs[og.MODE_WAVEFRONT][0][k])

@@ -119,8 +119,8 @@ def test_reference_helpers_live(oracle):
 def test_sobol_table_matches_reference_golden():
     """The library's direction-number table equals the reference's table."""
     import re
-    src = open(os.path.join(os.path.dirname(HERE), "ohao_engine_gb300", "csrc", "abi.cpp")).read()
-    body = src[src.index("kSobolDirs[128] = {"):]
+    src = open(os.path.join(os.path.dirname(HERE), "ohao_engine_gb300", "csrc", "pt_path.cuh")).read()
+    body = src[src.index("c_sobol_dirs[128] = {"):]
     body = body[:body.index("};")]
     vals = [int(x, 16) for x in re.findall(r"0x([0-9A-Fa-f]{8})u", body)]
     assert vals == KATS["sobol_dirs"]
