@@ -193,6 +193,33 @@ ohao_status ohao_pt_autotune(ohao_pt_ctx* ctx, const ohao_pt_view* views, uint32
 /* Name of the persistent launch shape in use ("default" before autotune). */
 const char* ohao_pt_launch_config(const ohao_pt_ctx* ctx);
 
+/* ---- Gradients (path replay) ----
+ * Replace the inverse lab's coordinate finite differences over the tile
+ * albedo map and material parameters (ohao/inverse/diff_fit.hpp:177-200,
+ * ohao/inverse/staged_fit.hpp:316-332; the map is ohao/render/diff/
+ * diff_map.hpp). Parameters: the linear albedo map of ohao_pt_set_albedo_map
+ * (read by materials whose diffuse texture index is 0) and every material's
+ * roughness. Sampling is detached: each path of the image is replayed from
+ * its own seed with its primal decisions, and BRDF values, albedo factors and
+ * MIS weights are differentiated. Not supported with the firefly clamp or
+ * max_bounces above 16. No counterpart call in the reference.
+ *
+ * ohao_pt_backward: d_grad_image[v] (device RGBA32F, A ignored) is dLoss/dI
+ * for the image that ohao_pt_render produced with the same views, settings
+ * and history 0. Overwrites d_grad_albedo_map (device, map_h*map_w*3 floats)
+ * and d_grad_roughness (device, one float per material); either may be NULL. */
+ohao_status ohao_pt_backward(ohao_pt_ctx* ctx, const ohao_pt_view* views, uint32_t n_views,
+                             const ohao_pt_settings* settings, const float* const* d_grad_image,
+                             float* d_grad_albedo_map, float* d_grad_roughness, ohao_stream stream);
+/* lossMulti (ohao/render/diff/diff_vk_forward.hpp:80-93) on linear radiance:
+ * renders every view into views[v].accum with history 0, loss = mean over
+ * views of the RGB mean squared error against d_targets[v] (device RGBA32F),
+ * written to *loss (host), and its gradients as for ohao_pt_backward. */
+ohao_status ohao_pt_adjoint(ohao_pt_ctx* ctx, const ohao_pt_view* views, uint32_t n_views,
+                                  const ohao_pt_settings* settings, const float* const* d_targets,
+                                  float* d_grad_albedo_map, float* d_grad_roughness, float* loss,
+                                  ohao_stream stream);
+
 /* ---- traceRayEXT as a batch call ----
  * rays: device, n x 8 floats (origin.xyz, tmin, dir.xyz, tmax).
  * hits: device, n x 5 uint32 (t bits, u bits, v bits, instance, primitive);

@@ -38,7 +38,7 @@ EXPORTED_SYMBOLS = [
     "ohao_pt_set_materials", "ohao_pt_update_materials", "ohao_pt_set_lights", "ohao_pt_set_env",
     "ohao_pt_set_albedo_map", "ohao_env_cdf_build", "ohao_pt_render", "ohao_pt_render_host",
     "ohao_pt_get_profile", "ohao_pt_trace", "ohao_pt_bvh_info", "ohao_pt_bvh_download", "ohao_bvh_build_noalloc",
-    "ohao_pt_autotune", "ohao_pt_launch_config",
+    "ohao_pt_autotune", "ohao_pt_launch_config", "ohao_pt_backward", "ohao_pt_adjoint",
 ]
 
 
@@ -113,6 +113,9 @@ def load_library(path: str | None = None):
         "ohao_bvh_build_noalloc": ([vp, u32, vp, vp, vp, C.POINTER(u32), C.POINTER(u32), vp], i32),
         "ohao_pt_autotune": ([vp, C.POINTER(View), u32, C.POINTER(Settings), C.POINTER(f32), vp], i32),
         "ohao_pt_launch_config": ([vp], C.c_char_p),
+        "ohao_pt_backward": ([vp, C.POINTER(View), u32, C.POINTER(Settings), C.POINTER(vp), vp, vp, vp], i32),
+        "ohao_pt_adjoint": ([vp, C.POINTER(View), u32, C.POINTER(Settings), C.POINTER(vp), vp, vp,
+                                   C.POINTER(f32), vp], i32),
     }
     for name, (args, res) in sigs.items():
         fn = getattr(L, name)
@@ -190,6 +193,7 @@ class PathTracer:
         if st != OK:
             raise OhaoError(st, "ohao_pt_create failed")
         self.h = h
+        self.device = device
         self._keep = {}
 
     def close(self):
@@ -298,6 +302,27 @@ class PathTracer:
         self._ck(self._L.ohao_pt_autotune(self.h, arr, len(views), C.byref(settings), C.byref(ms),
                                           _ptr(stream) if stream is not None else None), "autotune")
         return ms.value
+
+    # -- gradients -----------------------------------------------------------
+    def backward(self, views, settings: Settings, grad_images, grad_map=None, grad_rough=None, stream=None):
+        """d loss / d (albedo map, roughness) from per-view d loss / d image
+        (device RGBA32F); writes the device buffers grad_map / grad_rough."""
+        arr = (View * len(views))(*views)
+        ptrs = (C.c_void_p * len(views))(*[_ptr(g).value for g in grad_images])
+        self._ck(self._L.ohao_pt_backward(self.h, arr, len(views), C.byref(settings), ptrs, _ptr(grad_map),
+                                          _ptr(grad_rough), _ptr(stream) if stream is not None else None),
+                 "backward")
+
+    def adjoint(self, views, settings: Settings, targets, grad_map=None, grad_rough=None, stream=None) -> float:
+        """Renders the views (history 0), returns the multi-view RGB MSE against
+        the device RGBA32F targets and writes its gradients."""
+        arr = (View * len(views))(*views)
+        ptrs = (C.c_void_p * len(views))(*[_ptr(t).value for t in targets])
+        loss = C.c_float()
+        self._ck(self._L.ohao_pt_adjoint(self.h, arr, len(views), C.byref(settings), ptrs, _ptr(grad_map),
+                                               _ptr(grad_rough), C.byref(loss),
+                                               _ptr(stream) if stream is not None else None), "adjoint")
+        return loss.value
 
     @property
     def launch_config(self) -> str:

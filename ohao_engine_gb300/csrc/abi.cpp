@@ -90,6 +90,7 @@ struct ohao_pt_ctx {
     DevBuf blas_nodes_all, blas_tris_all, blas_desc, inst_dev;
     // scratch
     DevBuf scratch, build_scratch, err_flag;
+    DevBuf adj_scratch, adj_grads;        // backward: view table, loss cell; per-pixel loss gradients
     std::vector<DevBuf*> host_accum_bufs;
     ohao_pt_profile profile{};
     ohao::PersistentState* persistent = nullptr;
@@ -696,6 +697,85 @@ ohao_status ohao_pt_render_host(ohao_pt_ctx* ctx, const ohao_pt_view* views, uin
         CK(cudaMemcpyAsync(host_accum[v], acc[v], bytes, cudaMemcpyDeviceToHost, cs), "accum download");
     }
     return check_device_error(ctx, cs);
+}
+
+static ohao_status validate_backward(ohao_pt_ctx* ctx, const ohao_pt_view* views, uint32_t n_views,
+                                     const ohao_pt_settings* st) {
+    ohao_status s = validate_render(ctx, views, n_views, st);
+    if (s != OHAO_OK) return s;
+    if ((st->flags & OHAO_PT_FLAG_FIREFLY_CLAMP) && st->clamp_luminance > 0.0f)
+        return fail(ctx, OHAO_ERR_INVALID_ARG, "backward: the firefly clamp is not differentiable; clear the flag");
+    if (st->max_bounces > ohao::adjoint_max_bounces())
+        return fail(ctx, OHAO_ERR_INVALID_ARG, "backward: max_bounces above 16");
+    return OHAO_OK;
+}
+
+static ohao_status run_backward(ohao_pt_ctx* ctx, const std::vector<ohao::RenderView>& rvs, const float* const* grads,
+                                const ohao_pt_settings* st, float* d_grad_map, float* d_grad_rough, cudaStream_t cs) {
+    ohao::PathParams pp{st->max_bounces, st->sampler, st->flags, st->clamp_luminance, st->aniso_strength,
+                        st->aniso_rotation, st->sample_index_base};
+    const uint32_t n = static_cast<uint32_t>(rvs.size());
+    CK(ctx->adj_scratch.ensure(ohao::adjoint_scratch_bytes(n)), "backward scratch");
+    std::string err;
+    const ohao_status s = ohao::adjoint_backward(make_scene(ctx), rvs.data(), grads, n, pp, st->spp, ctx->nmats,
+                                                 ctx->adj_scratch.p, ctx->adj_scratch.n, d_grad_map, d_grad_rough, cs,
+                                                 ctx->err_flag.as<int>(), err);
+    if (s != OHAO_OK) return fail(ctx, s, err);
+    return check_device_error(ctx, cs);
+}
+
+ohao_status ohao_pt_backward(ohao_pt_ctx* ctx, const ohao_pt_view* views, uint32_t n_views,
+                             const ohao_pt_settings* st, const float* const* d_grad_image, float* d_grad_albedo_map,
+                             float* d_grad_roughness, ohao_stream stream) {
+    ohao_status s = validate_backward(ctx, views, n_views, st);
+    if (s != OHAO_OK) return s;
+    if (!d_grad_image) return fail(ctx, OHAO_ERR_INVALID_ARG, "backward: null image gradient list");
+    for (uint32_t v = 0; v < n_views; ++v)
+        if (!d_grad_image[v]) return fail(ctx, OHAO_ERR_INVALID_ARG, "backward: null image gradient");
+    cudaStream_t cs = reinterpret_cast<cudaStream_t>(stream);
+    CK(cudaSetDevice(ctx->device), "set device");
+    std::vector<float*> none(n_views, nullptr);
+    const std::vector<ohao::RenderView> rvs = to_render_views(views, n_views, none.data());
+    return run_backward(ctx, rvs, d_grad_image, st, d_grad_albedo_map, d_grad_roughness, cs);
+}
+
+ohao_status ohao_pt_adjoint(ohao_pt_ctx* ctx, const ohao_pt_view* views, uint32_t n_views,
+                                  const ohao_pt_settings* st, const float* const* d_targets,
+                                  float* d_grad_albedo_map, float* d_grad_roughness, float* loss,
+                                  ohao_stream stream) {
+    ohao_status s = validate_backward(ctx, views, n_views, st);
+    if (s != OHAO_OK) return s;
+    if (!d_targets) return fail(ctx, OHAO_ERR_INVALID_ARG, "adjoint: null target list");
+    std::vector<ohao_pt_view> fresh(views, views + n_views);
+    std::vector<float*> acc(n_views);
+    uint64_t total = 0;
+    for (uint32_t v = 0; v < n_views; ++v) {
+        if (!views[v].accum || !d_targets[v])
+            return fail(ctx, OHAO_ERR_INVALID_ARG, "adjoint: null accum or target");
+        fresh[v].history = 0;
+        acc[v] = views[v].accum;
+        total += static_cast<uint64_t>(views[v].width) * views[v].height;
+    }
+    cudaStream_t cs = reinterpret_cast<cudaStream_t>(stream);
+    CK(cudaSetDevice(ctx->device), "set device");
+    if ((s = render_views(ctx, fresh.data(), n_views, st, acc.data(), cs)) != OHAO_OK) return s;
+    CK(ctx->adj_grads.ensure(total * 16), "loss gradient images");
+    CK(ctx->adj_scratch.ensure(ohao::adjoint_scratch_bytes(n_views)), "backward scratch");
+    std::vector<float*> grads(n_views);
+    uint64_t off = 0;
+    for (uint32_t v = 0; v < n_views; ++v) {
+        grads[v] = ctx->adj_grads.as<float>() + off * 4;
+        off += static_cast<uint64_t>(views[v].width) * views[v].height;
+    }
+    const std::vector<ohao::RenderView> rvs = to_render_views(fresh.data(), n_views, acc.data());
+    std::string err;
+    float l = 0.0f;
+    s = ohao::adjoint_mse(rvs.data(), d_targets, n_views, ctx->adj_scratch.p, ctx->adj_scratch.n, grads.data(), &l, cs,
+                          err);
+    if (s != OHAO_OK) return fail(ctx, s, err);
+    if (loss) *loss = l;
+    std::vector<const float*> cgrads(grads.begin(), grads.end());
+    return run_backward(ctx, rvs, cgrads.data(), st, d_grad_albedo_map, d_grad_roughness, cs);
 }
 
 ohao_status ohao_pt_get_profile(const ohao_pt_ctx* ctx, ohao_pt_profile* out) {

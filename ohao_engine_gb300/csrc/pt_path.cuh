@@ -321,11 +321,16 @@ struct ShadowReq {
     bool valid;
 };
 
-// Analytic light NEE; contribution precomputed as if visible. thr == null at
-// bounce 0 (pt_raygen.rgen:305-434; 585-705; 893-1013).
-OHAO_D void nee_light(const DScene& sc, const PathParams& pp, Rng& rng, uint32_t& dim, V3 P, V3 N, V3 inDir, V3 albedo,
-                      float rough, float metal, V3 F0, const V3* thr, ShadowReq& req) {
-    req.valid = false;
+// Light choice and sample point of a light NEE (the draws and geometry of
+// pt_raygen.rgen:305-383), shared by the forward step and the adjoint.
+struct LightSample {
+    bool valid;       // NdotL > 0 && weight > 0
+    V3 L, Le;
+    float weight, shadowDist, NdotL, n;
+};
+
+OHAO_D LightSample sample_light(const DScene& sc, Rng& rng, uint32_t& dim, V3 P, V3 N) {
+    LightSample out;
     const uint32_t n = sc.nlights;
     uint32_t li = static_cast<uint32_t>(rng.s1(dim) * static_cast<float>(n));
     dim += 1;
@@ -402,8 +407,26 @@ OHAO_D void nee_light(const DScene& sc, const PathParams& pp, Rng& rng, uint32_t
         weight = lcos * ar / (ld * ld);
         shadowDist = ld - 0.02f;
     }
-    const float NdotL = gmaxf(dot(N, L), 0.0f);
-    if (!(NdotL > 0.0f && weight > 0.0f)) return;
+    out.NdotL = gmaxf(dot(N, L), 0.0f);
+    out.valid = out.NdotL > 0.0f && weight > 0.0f;
+    out.L = L;
+    out.Le = Le;
+    out.weight = weight;
+    out.shadowDist = shadowDist;
+    out.n = static_cast<float>(n);
+    return out;
+}
+
+// Analytic light NEE; contribution precomputed as if visible. thr == null at
+// bounce 0 (pt_raygen.rgen:305-434; 585-705; 893-1013).
+OHAO_D void nee_light(const DScene& sc, const PathParams& pp, Rng& rng, uint32_t& dim, V3 P, V3 N, V3 inDir, V3 albedo,
+                      float rough, float metal, V3 F0, const V3* thr, ShadowReq& req) {
+    req.valid = false;
+    const LightSample ls = sample_light(sc, rng, dim, P, N);
+    if (!ls.valid) return;
+    const V3 L = ls.L, Le = ls.Le;
+    const float NdotL = ls.NdotL, weight = ls.weight, shadowDist = ls.shadowDist;
+    const uint32_t n = sc.nlights;
     const V3 V = normalize(-inDir);
     const V3 H = normalize(L + V);
     const float NdotH = gmaxf(dot(N, H), 0.001f);
@@ -433,20 +456,38 @@ OHAO_D void nee_light(const DScene& sc, const PathParams& pp, Rng& rng, uint32_t
     req.contrib = firefly(pp, c);
 }
 
+// Env NEE sample (pt_raygen.rgen:439-451): direction, pdf, and the radiance
+// the miss shader returns for it.
+struct EnvSample {
+    bool valid;       // NdotL > 0 && pdf > 0
+    V3 dir, rad;
+    float pdf, NdotL;
+};
+
+OHAO_D EnvSample sample_env_nee(const DScene& sc, const PathParams& pp, Rng& rng, uint32_t& dim, V3 N) {
+    EnvSample out;
+    const float u1 = rng.s1(dim), u2 = rng.s1(dim + 1);
+    dim += 2;
+    sample_env(sc, u1, u2, out.dir, out.pdf);
+    out.NdotL = gmaxf(dot(N, out.dir), 0.0f);
+    out.valid = out.NdotL > 0.0f && out.pdf > 0.0f;
+    if (out.valid) {
+        Surf ms;
+        miss_shade(sc, pp, out.dir, ms);
+        out.rad = ms.color;
+    }
+    return out;
+}
+
 // Env NEE with balance MIS (pt_raygen.rgen:438-500, 708-763, 1016-1071).
 OHAO_D void nee_env(const DScene& sc, const PathParams& pp, Rng& rng, uint32_t& dim, V3 P, V3 N, V3 inDir, V3 albedo,
                     float rough, float metal, V3 F0, const V3* thr, ShadowReq& req) {
     req.valid = false;
-    const float u1 = rng.s1(dim), u2 = rng.s1(dim + 1);
-    dim += 2;
-    V3 envDir;
-    float envPdf;
-    sample_env(sc, u1, u2, envDir, envPdf);
-    const float NdotL = gmaxf(dot(N, envDir), 0.0f);
-    if (!(NdotL > 0.0f && envPdf > 0.0f)) return;
-    Surf ms;
-    miss_shade(sc, pp, envDir, ms);
-    const V3 envRad = ms.color;
+    const EnvSample es = sample_env_nee(sc, pp, rng, dim, N);
+    if (!es.valid) return;
+    const V3 envDir = es.dir;
+    const float envPdf = es.pdf, NdotL = es.NdotL;
+    const V3 envRad = es.rad;
     const V3 V = normalize(-inDir);
     const V3 H = normalize(envDir + V);
     const float NdotH = gmaxf(dot(N, H), 0.001f);

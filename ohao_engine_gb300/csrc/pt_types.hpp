@@ -105,4 +105,19 @@ ohao_status persistent_autotune(PersistentState* s, const DScene& sc, const Rend
                                 const PathParams& pp, uint32_t spp, const float* scene_box, cudaStream_t st, int* d_err,
                                 float* best_ms, std::string& err);
 
+// adjoint.cu
+uint32_t adjoint_max_bounces();
+size_t adjoint_scratch_bytes(uint32_t nviews);
+// Mean over views of the per-view RGB MSE between views[v].accum and
+// targets[v]; writes d loss / d pixel into grads_out[v] (device RGBA32F).
+ohao_status adjoint_mse(const RenderView* views, const float* const* targets, uint32_t nviews, void* scratch,
+                        size_t scratch_bytes, float* const* grads_out, float* loss_out, cudaStream_t st,
+                        std::string& err);
+// Path-replay gradient: grads[v] = d loss / d pixel of views[v]'s image (the
+// mean of spp paths from sample pp.sample_base); overwrites grad_map
+// (map_h*map_w*3) and grad_rough (nmats), either may be null.
+ohao_status adjoint_backward(const DScene& sc, const RenderView* views, const float* const* grads, uint32_t nviews,
+                             const PathParams& pp, uint32_t spp, uint32_t nmats, void* scratch, size_t scratch_bytes,
+                             float* grad_map, float* grad_rough, cudaStream_t st, int* d_err, std::string& err);
+
 }  // namespace ohao

@@ -4,6 +4,7 @@
 // smoke check and by bench.py's CPU-baseline leg. Never linked into the
 // product library.
 #include "oracle_pt.hpp"
+#include "oracle_adjoint.hpp"
 #include <cstring>
 #include <memory>
 #include <vector>
@@ -213,6 +214,33 @@ void orc_render_paths(const Scene* s, const float* inv_view, const float* inv_pr
         tn += ts.nodes; tt += ts.tris; ti += ts.insts;
     }
     if (stats) { stats[0] = tn; stats[1] = tt; stats[2] = ti; }
+}
+
+// Detached-sampling FP64 radiance (oracle_adjoint.hpp) for `npix` pixels x
+// `spp` samples: decisions with the scene's parameters, values with mats_e
+// (12 floats per material) and map_e (the tile albedo map, or NULL).
+// out is [spp][npix][3] double.
+void orc_detached_paths(const Scene* s, const float* inv_view, const float* inv_proj, uint32_t width, uint32_t height,
+                        const AbiSettings* as, uint32_t sample_base, uint32_t spp, const uint32_t* pix, uint32_t npix,
+                        const float* mats_e, const float* map_e, double* out, int nthreads) {
+    View vw;
+    std::memcpy(vw.inv_view, inv_view, 64);
+    std::memcpy(vw.inv_proj, inv_proj, 64);
+    vw.width = width; vw.height = height;
+    Settings st = to_settings(as);
+    const uint32_t np = pix ? npix : width * height;
+    const int64_t total = static_cast<int64_t>(np) * spp;
+#ifdef _OPENMP
+    if (nthreads > 0) omp_set_num_threads(nthreads);
+#pragma omp parallel for schedule(dynamic, 64)
+#endif
+    for (int64_t k = 0; k < total; ++k) {
+        uint32_t smp = static_cast<uint32_t>(k / np), pi = static_cast<uint32_t>(k % np);
+        uint32_t p = pix ? pix[pi] : pi;
+        DetachedPath dp(*s, st, mats_e, map_e);
+        V3<double> r = dp.path(vw, p % width, p / width, sample_base + smp);
+        out[k * 3 + 0] = r.x; out[k * 3 + 1] = r.y; out[k * 3 + 2] = r.z;
+    }
 }
 
 // Progressive own-pixel accumulation of per-path radiance in sample order

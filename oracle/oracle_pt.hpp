@@ -657,14 +657,15 @@ struct PathTracer {
         return c;
     }
 
-    // Analytic light NEE (pt_raygen.rgen:305-434 for bounce 0 with ggxD,
-    // 585-705 / 893-1013 for chain bounces with the inline D). Returns the
-    // unclamped contribution without throughput; `visible` reports the test.
-    struct NeeOut { bool valid = false; V3<R> contrib; };
-    NeeOut nee_light(Sampler& smp, uint32_t& dim, V3<R> P, V3<R> N, V3<R> inDir, V3<R> albedo, R rough, R metal,
-                     V3<R> F0, const V3<R>* thr, TravStats* ts) const {
-        const bool bounce0 = (thr == nullptr);
-        NeeOut out;
+    // Light choice and sample point of a light NEE (the draws and geometry of
+    // pt_raygen.rgen:305-383); valid = NdotL > 0 && weight > 0.
+    struct LightSmp {
+        bool valid = false;
+        V3<R> L, Le;
+        R weight = 0, shadowDist = 0, NdotL = 0, n = 0;
+    };
+    LightSmp sample_light(Sampler& smp, uint32_t& dim, V3<R> P, V3<R> N) const {
+        LightSmp out;
         const uint32_t n = static_cast<uint32_t>(sc.lights.size());
         uint32_t li = static_cast<uint32_t>(smp.s1(dim) * float(n));
         dim += 1;
@@ -734,10 +735,31 @@ struct PathTracer {
             weight = lcos * ar / (ld * ld);
             shadowDist = ld - R(0.02f);
         }
-        R NdotL = gmax(dot(N, L), R(0));
-        if (NdotL > R(0) && weight > R(0)) {
+        out.NdotL = gmax(dot(N, L), R(0));
+        out.valid = out.NdotL > R(0) && weight > R(0);
+        out.L = L;
+        out.Le = Le;
+        out.weight = weight;
+        out.shadowDist = shadowDist;
+        out.n = R(float(n));
+        return out;
+    }
+
+    // Analytic light NEE (pt_raygen.rgen:305-434 for bounce 0 with ggxD,
+    // 585-705 / 893-1013 for chain bounces with the inline D). Returns the
+    // unclamped contribution without throughput; `visible` reports the test.
+    struct NeeOut { bool valid = false; V3<R> contrib; };
+    NeeOut nee_light(Sampler& smp, uint32_t& dim, V3<R> P, V3<R> N, V3<R> inDir, V3<R> albedo, R rough, R metal,
+                     V3<R> F0, const V3<R>* thr, TravStats* ts) const {
+        const bool bounce0 = (thr == nullptr);
+        NeeOut out;
+        const LightSmp ls = sample_light(smp, dim, P, N);
+        const V3<R> L = ls.L, Le = ls.Le;
+        const R NdotL = ls.NdotL, weight = ls.weight;
+        const uint32_t n = static_cast<uint32_t>(sc.lights.size());
+        if (ls.valid) {
             Surf<R> sh;
-            if (shadow(P + N * R(0.01f), L, shadowDist, sh, ts)) {
+            if (shadow(P + N * R(0.01f), L, ls.shadowDist, sh, ts)) {
                 V3<R> V = normalize(-inDir);
                 V3<R> H = normalize(L + V);
                 R NdotH = gmax(dot(N, H), R(0.001f));
@@ -896,6 +918,23 @@ struct PathTracer {
                 lastDelta = false;
             }
         }
+    }
+
+    // Jittered camera ray direction (pt_raygen.rgen:138-163); origin = camera.
+    V3<R> camera_dir(const View& vw, uint32_t px, uint32_t py, Sampler& smp, uint32_t& dim) const {
+        R jx = R(smp.s1(dim)) - R(0.5f), jy = R(smp.s1(dim + 1)) - R(0.5f);
+        dim += 2;
+        R uvx = (R(float(px)) + R(0.5f) + jx + R(st.pix_jitter[0])) / R(float(vw.width));
+        R uvy = (R(float(py)) + R(0.5f) + jy + R(st.pix_jitter[1])) / R(float(vw.height));
+        R ndcx = uvx * R(2) - R(1), ndcy = uvy * R(2) - R(1);
+        const float* iv = vw.inv_view;
+        V3<R> fwd = -V3<R>(R(iv[8]), R(iv[9]), R(iv[10]));
+        V3<R> right{R(iv[0]), R(iv[1]), R(iv[2])};
+        V3<R> up{R(iv[4]), R(iv[5]), R(iv[6])};
+        R aspect = R(float(vw.width)) / R(float(vw.height));
+        R tanY = std::fabs(R(vw.inv_proj[5]));
+        R tanX = tanY * aspect;
+        return normalize(fwd + right * ndcx * tanX - up * ndcy * tanY);
     }
 
     // pt_raygen.rgen main(): one path sample; returns the clamped radiance.

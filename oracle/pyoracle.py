@@ -58,6 +58,7 @@ def lib():
         L.orc_trace.argtypes = [vp, vp, u32, vp, i32, vp, i32]
         L.orc_render_paths.argtypes = [vp, vp, vp, u32, u32, vp, u32, u32, vp, u32, vp, i32, i32, vp]
         L.orc_accumulate.argtypes = [vp, u32, u32, vp, u32]
+        L.orc_detached_paths.argtypes = [vp, vp, vp, u32, u32, vp, u32, u32, vp, u32, vp, vp, vp, i32]
         L.orc_env_cdf_build.argtypes = [vp, i32, i32, vp, vp, vp]
         L.orc_sobol_sample1d.argtypes = [u32, u32]
         L.orc_sobol_sample1d.restype = f32
@@ -172,6 +173,24 @@ class OracleScene:
         lib().orc_render_paths(self.h, _p(view.inv_view), _p(view.inv_proj), view.width, view.height, _p(st),
                                sample_base, spp, _p(pix), npix, _p(out), int(fp64), nthreads, _p(s))
         return (out, s) if stats else out
+
+    def detached_paths(self, view, settings: dict, sample_base: int, spp: int, pixels=None, materials=None,
+                       albedo_map=None, nthreads: int = 0):
+        """FP64 radiance of the detached-sampling estimator: sampling with the
+        scene's own parameters, values with ``materials`` (M,12) and
+        ``albedo_map`` (h,w,3); both default to the scene's. [spp, npix, 3]."""
+        st = np.zeros(1, SETTINGS_DTYPE)
+        for k in SETTINGS_DTYPE.names:
+            st[k] = settings.get(k, 0)
+        pix = None if pixels is None else np.ascontiguousarray(pixels, np.uint32)
+        npix = view.width * view.height if pix is None else pix.size
+        mats = np.ascontiguousarray(self.sd.materials if materials is None else materials, np.float32)
+        amap = self.sd.albedo_map if albedo_map is None else albedo_map
+        amap = None if amap is None else np.ascontiguousarray(amap, np.float32)
+        out = np.zeros((spp, npix, 3), np.float64)
+        lib().orc_detached_paths(self.h, _p(view.inv_view), _p(view.inv_proj), view.width, view.height, _p(st),
+                                 sample_base, spp, _p(pix), npix, _p(mats), _p(amap), _p(out), nthreads)
+        return out
 
 
 def accumulate(paths: np.ndarray, accum: np.ndarray | None = None, history: int = 0):

@@ -1,0 +1,162 @@
+"""Path-replay gradients (ohao_pt_backward / ohao_pt_adjoint) against
+central finite differences of the oracle's FP64 detached-sampling estimator.
+
+The loss is lossMulti on linear radiance (mean over views of the RGB MSE);
+d loss / d theta = sum_p dL/dI_p . dI_p/dtheta, and the finite difference
+uses the same dL/dI_p (from the device image) with I_p the oracle's mean of
+the same paths (same seeds). Tolerance: 1e-3 relative on parameters whose
+gradient is at least 1% of the largest tested one."""
+import numpy as np
+import pytest
+
+import pt_harness as H
+from ohao_engine_gb300 import scenes
+
+REL_TOL = 1e-3
+H_STEP = 1e-3
+
+CASES = [
+    ("studio_pcg", lambda: scenes.studio(freq=20, side=40), dict(max_bounces=3, sampler=0), 2),
+    ("studio_sobol_aniso", lambda: scenes.studio(freq=20, side=32),
+     dict(max_bounces=3, sampler=1, aniso_strength=0.6, aniso_rotation=0.4), 2),
+    ("small_env_many_mats", lambda: H.small_env_scene(), dict(max_bounces=4, sampler=0), 2),
+    ("cornell_lights", lambda: scenes.cornell(32, 32), dict(max_bounces=4, sampler=1), 2),
+]
+
+
+def _oracle_settings(st):
+    return dict(max_bounces=st["max_bounces"], sampler=st["sampler"], aniso=st.get("aniso_strength", 0.0),
+                aniso_rot=st.get("aniso_rotation", 0.0))
+
+
+def _setup(og, sd, st, spp, seed=7):
+    """Renders a target with perturbed parameters, then runs the adjoint at
+    the scene's own parameters. Returns device results and dL/dI."""
+    import torch
+    pt = H.gpu_tracer(og, sd)
+    view = sd.views[0]
+    npix = view.width * view.height
+    rng = np.random.default_rng(seed)
+    settings = og.make_settings(spp=spp, **st)
+    mats_t = sd.materials.copy()
+    mats_t[:, 4] = np.clip(mats_t[:, 4] + rng.uniform(-0.2, 0.2, mats_t.shape[0]).astype(np.float32), 0.1, 1.0)
+    pt.update_materials(mats_t)
+    if sd.albedo_map is not None:
+        pt.set_albedo_map(np.clip(sd.albedo_map + rng.uniform(-0.3, 0.3, sd.albedo_map.shape), 0.05, 1.0)
+                          .astype(np.float32))
+    target = torch.zeros((npix, 4), dtype=torch.float32, device="cuda")
+    pt.render([og.make_view(view, accum=target)], settings)
+    pt.update_materials(sd.materials)
+    if sd.albedo_map is not None:
+        pt.set_albedo_map(sd.albedo_map)
+    acc = torch.zeros((npix, 4), dtype=torch.float32, device="cuda")
+    nm = sd.materials.shape[0]
+    gmap = torch.zeros(sd.albedo_map.size if sd.albedo_map is not None else 1, dtype=torch.float32, device="cuda")
+    grough = torch.zeros(nm, dtype=torch.float32, device="cuda")
+    loss = pt.adjoint([og.make_view(view, accum=acc)], settings, [target], gmap, grough)
+    torch.cuda.synchronize()
+    I = acc.cpu().numpy()[:, :3].astype(np.float64)
+    T = target.cpu().numpy()[:, :3].astype(np.float64)
+    dLdI = 2.0 * (I - T) / (npix * 3)
+    return dict(pt=pt, settings=settings, loss=loss, I=I, T=T, dLdI=dLdI, gmap=gmap.cpu().numpy().astype(np.float64),
+                grough=grough.cpu().numpy().astype(np.float64), acc=acc, target=target)
+
+
+def _fd(o, sd, ost, spp, dLdI, which, k):
+    mats = sd.materials.copy()
+    amap = None if sd.albedo_map is None else sd.albedo_map.copy()
+    if which == "rough":
+        mp, mm = mats.copy(), mats.copy()
+        mp[k, 4] += np.float32(H_STEP)
+        mm[k, 4] -= np.float32(H_STEP)
+        step = float(mp[k, 4]) - float(mm[k, 4])
+        args_p, args_m = dict(materials=mp, albedo_map=amap), dict(materials=mm, albedo_map=amap)
+    else:
+        ap, am = amap.copy(), amap.copy()
+        ap.reshape(-1)[k] += np.float32(H_STEP)
+        am.reshape(-1)[k] -= np.float32(H_STEP)
+        step = float(ap.reshape(-1)[k]) - float(am.reshape(-1)[k])
+        args_p, args_m = dict(materials=mats, albedo_map=ap), dict(materials=mats, albedo_map=am)
+    Ip = o.detached_paths(sd.views[0], ost, 0, spp, **args_p).mean(axis=0)
+    Im = o.detached_paths(sd.views[0], ost, 0, spp, **args_m).mean(axis=0)
+    return float((dLdI * (Ip - Im)).sum() / step)
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("name,make,st,spp", CASES, ids=[c[0] for c in CASES])
+def test_adjoint_matches_detached_fd(gpu_lib, oracle, name, make, st, spp):
+    og = gpu_lib
+    sd = make()
+    r = _setup(og, sd, st, spp)
+    ost = _oracle_settings(st)
+    o = oracle.OracleScene(sd)
+    # the device image is the oracle's forward estimator (bit-exact per path)
+    fwd = o.render_paths(sd.views[0], ost, 0, spp, None, fp64=False).astype(np.float64).mean(axis=0)
+    assert np.allclose(r["I"], fwd, rtol=1e-5, atol=1e-6)
+    loss_ref = float(((r["I"] - r["T"]) ** 2).mean())
+    assert abs(r["loss"] - loss_ref) <= 1e-5 * loss_ref
+    rng = np.random.default_rng(11)
+    checks = []
+    live = np.nonzero((sd.materials[:, 4] > 0.04) & (np.abs(r["grough"]) > 0))[0]
+    if live.size:
+        gmax = np.abs(r["grough"][live]).max()
+        cand = live[np.abs(r["grough"][live]) >= 1e-2 * gmax]
+        for k in rng.choice(cand, size=min(12, cand.size), replace=False):
+            checks.append(("rough", int(k), r["grough"][k]))
+    if sd.albedo_map is not None:
+        g = r["gmap"]
+        cand = np.nonzero(np.abs(g) >= 1e-2 * np.abs(g).max())[0]
+        for k in rng.choice(cand, size=min(32, cand.size), replace=False):
+            checks.append(("map", int(k), g[k]))
+    assert len(checks) >= 4
+    bad = []
+    for which, k, gdev in checks:
+        gfd = _fd(o, sd, ost, spp, r["dLdI"], which, k)
+        if abs(gdev - gfd) > REL_TOL * abs(gfd):
+            bad.append((which, k, gdev, gfd))
+    assert not bad, f"{name}: {len(bad)}/{len(checks)} gradients off: {bad[:6]}"
+
+
+@pytest.mark.gpu
+def test_backward_from_image_gradient_equals_loss_backward(gpu_lib):
+    """ohao_pt_backward with dL/dI from the caller gives the gradients of
+    ohao_pt_adjoint, and the torch.autograd wrapper gives the same."""
+    import torch
+    og = gpu_lib
+    from ohao_engine_gb300 import diff
+    sd = scenes.studio(freq=20, side=32)
+    st = dict(max_bounces=3, sampler=1)
+    r = _setup(og, sd, st, 2)
+    pt, view = r["pt"], sd.views[0]
+    g_img = torch.zeros((view.width * view.height, 4), dtype=torch.float32, device="cuda")
+    g_img[:, :3] = torch.from_numpy(r["dLdI"].astype(np.float32)).cuda()
+    gmap = torch.zeros(sd.albedo_map.size, dtype=torch.float32, device="cuda")
+    grough = torch.zeros(sd.materials.shape[0], dtype=torch.float32, device="cuda")
+    pt.backward([og.make_view(view)], r["settings"], [g_img], gmap, grough)
+    torch.cuda.synchronize()
+    scale = np.abs(r["gmap"]).max()
+    assert np.allclose(gmap.cpu().numpy(), r["gmap"], rtol=1e-4, atol=1e-6 * scale)
+    assert np.allclose(grough.cpu().numpy(), r["grough"], rtol=1e-4, atol=1e-6 * np.abs(r["grough"]).max())
+    # autograd wrapper
+    amap = torch.from_numpy(sd.albedo_map.copy()).cuda().requires_grad_(True)
+    rough = torch.from_numpy(sd.materials[:, 4].copy()).cuda().requires_grad_(True)
+    img = diff.render(amap, rough, pt, sd.materials, [view], r["settings"])
+    tgt = r["target"][:, :3].reshape(1, view.height, view.width, 3)
+    loss = diff.multi_view_mse(img, tgt)
+    loss.backward()
+    assert abs(loss.item() - r["loss"]) <= 1e-5 * r["loss"]
+    assert np.allclose(amap.grad.cpu().numpy().reshape(-1), r["gmap"], rtol=1e-3, atol=1e-5 * scale)
+    assert np.allclose(rough.grad.cpu().numpy(), r["grough"], rtol=1e-3, atol=1e-5 * np.abs(r["grough"]).max())
+
+
+@pytest.mark.gpu
+def test_backward_rejects_firefly_clamp_and_deep_paths(gpu_lib):
+    import torch
+    og = gpu_lib
+    sd = scenes.studio(freq=10, side=16)
+    pt = H.gpu_tracer(og, sd)
+    view = sd.views[0]
+    g = torch.zeros((view.width * view.height, 4), dtype=torch.float32, device="cuda")
+    for kw in (dict(flags=og.FLAG_FIREFLY_CLAMP, clamp_luminance=4.0), dict(max_bounces=17)):
+        with pytest.raises(og.OhaoError):
+            pt.backward([og.make_view(view)], og.make_settings(spp=1, **kw), [g])
