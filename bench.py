@@ -43,7 +43,7 @@ def parse():
     ap.add_argument("--steps", type=int, default=10)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
-    ap.add_argument("--workload", default="sphere_1m", choices=["sphere_1m", "cornell", "instanced"])
+    ap.add_argument("--workload", default="sphere_1m", choices=["sphere_1m", "cornell", "instanced", "studio"])
     ap.add_argument("--cpu-seconds", type=float, default=12.0)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     return ap.parse_args()
@@ -426,12 +426,145 @@ def run_instanced(args):
     pt.close()
 
 
+def run_studio(args, fit_iters=80):
+    """Differentiable inverse fit: 200k-tri displaced sphere on a plane, 64x64
+    tile albedo map + 4 roughness regions, 8 train + 2 holdout views at
+    512x512, targets at 256 spp, gradient at 16 spp depth 3. A step is one
+    full gradient (12,288 map entries + 5 roughness values) of the multi-view
+    L2 loss through ohao_pt_adjoint. The coordinate-FD rate that it replaces
+    is 2 renders of the 8 train views per parameter, timed on the same GPU
+    with the same renderer."""
+    import torch
+    import ohao_engine_gb300 as og
+    from ohao_engine_gb300 import _build, scenes
+    from ohao_engine_gb300.fit import AdjointFit
+    torch.cuda.set_device(0)
+    if not os.path.exists(og.LIB_PATH):
+        _build.build()
+    og.load_library()
+    sd = scenes.studio()
+    train, hold = sd.views[:8], sd.views[8:]
+    pt = og.PathTracer(device=0)
+    pt.load_scene(sd)
+    ntris = sd.ntris
+    # ground-truth targets at 256 spp
+    tgt = [torch.zeros((v.width * v.height, 4), dtype=torch.float32, device="cuda") for v in sd.views]
+    st_t = og.make_settings(spp=256, max_bounces=3, sample_index_base=1 << 20, sampler=og.SAMPLER_PCG)
+    pt.render([og.make_view(v, accum=a) for v, a in zip(sd.views, tgt)], st_t)
+    torch.cuda.synchronize()
+    rng = np.random.default_rng(2)
+    gt_map = sd.albedo_map.copy()
+    init_map = np.clip(gt_map + rng.uniform(-0.4, 0.4, gt_map.shape), 0.0, 1.0).astype(np.float32)
+    rough_ids = np.arange(4)
+    gt_rough = sd.materials[rough_ids, 4].copy()
+    mats0 = sd.materials.copy()
+    mats0[rough_ids, 4] = np.clip(gt_rough + rng.uniform(-0.2, 0.2, 4), 0.05, 1.0).astype(np.float32)
+    fit = AdjointFit(pt, mats0, init_map, train, tgt[:8], spp=16, max_bounces=3, rough_ids=rough_ids, lr=0.03)
+    n_params = fit.theta.size
+    npix = sum(v.width * v.height for v in train)
+    st16 = og.make_settings(spp=16, max_bounces=3, sample_index_base=0, sampler=og.SAMPLER_PCG)
+    acc = [torch.zeros((v.width * v.height, 4), dtype=torch.float32, device="cuda") for v in train]
+    flush = torch.empty(64 * 1024 * 1024, dtype=torch.float32, device="cuda")
+    # timed: full gradients (render + loss + backward)
+    for k in range(args.warmup):
+        fit.gradient(sample_base=k * 16)
+    torch.cuda.synchronize()
+    clk = ClockSampler(0)
+    clk.start()
+    g_times = []
+    for k in range(args.steps):
+        flush.zero_()
+        e0 = torch.cuda.Event(enable_timing=True)
+        e1 = torch.cuda.Event(enable_timing=True)
+        e0.record()
+        vs = [og.make_view(v, accum=a) for v, a in zip(train, fit.accums)]
+        pt.adjoint(vs, fit.settings((args.warmup + k) * 16), fit.targets, fit.gmap, fit.grough)
+        e1.record()
+        e1.synchronize()
+        g_times.append(e0.elapsed_time(e1))
+    clocks = clk.stop()
+    # the forward render alone (what coordinate FD repeats twice per parameter)
+    r_times = []
+    for k in range(args.steps):
+        flush.zero_()
+        e0 = torch.cuda.Event(enable_timing=True)
+        e1 = torch.cuda.Event(enable_timing=True)
+        e0.record()
+        pt.render([og.make_view(v, accum=a) for v, a in zip(train, acc)], st16)
+        e1.record()
+        e1.synchronize()
+        r_times.append(e0.elapsed_time(e1))
+    t_grad = sum(g_times) / len(g_times) / 1e3
+    t_render = sum(r_times) / len(r_times) / 1e3
+    adj_rate = n_params / t_grad
+    fd_rate = 1.0 / (2.0 * t_render)
+    # end to end: targets uploaded from pinned host memory, gradients read back, every step
+    host_t = [t.cpu().pin_memory() for t in tgt[:8]]
+    host_g = torch.zeros(fit.gmap.numel() + fit.grough.numel(), dtype=torch.float32).pin_memory()
+    e2e_t = []
+    for k in range(args.steps):
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        for d, h in zip(fit.targets, host_t):
+            d.copy_(h, non_blocking=True)
+        vs = [og.make_view(v, accum=a) for v, a in zip(train, fit.accums)]
+        pt.adjoint(vs, fit.settings(k * 16), fit.targets, fit.gmap, fit.grough)
+        host_g[:fit.gmap.numel()].copy_(fit.gmap, non_blocking=True)
+        host_g[fit.gmap.numel():].copy_(fit.grough, non_blocking=True)
+        torch.cuda.synchronize()
+        e2e_t.append(time.perf_counter() - t0)
+    t_e2e = sum(e2e_t) / len(e2e_t)
+    # the fit itself
+    def holdout_loss():
+        hacc = [torch.zeros((v.width * v.height, 4), dtype=torch.float32, device="cuda") for v in hold]
+        pt.render([og.make_view(v, accum=a) for v, a in zip(hold, hacc)],
+                  og.make_settings(spp=64, max_bounces=3, sample_index_base=1 << 24, sampler=og.SAMPLER_PCG))
+        return float(np.mean([((a[:, :3] - t[:, :3]) ** 2).mean().item() for a, t in zip(hacc, tgt[8:])]))
+    map_rmse0 = float(np.sqrt(((fit.albedo_map - gt_map) ** 2).mean()))
+    hold0 = holdout_loss()
+    losses = []
+    t0 = time.time()
+    for _ in range(fit_iters):
+        losses.append(fit.step())
+    fit_s = time.time() - t0
+    map_rmse1 = float(np.sqrt(((fit.albedo_map - gt_map) ** 2).mean()))
+    hold1 = holdout_loss()
+    line = {"metric": "gradients/s of the multi-view L2 loss (path-replay adjoint) vs coordinate-FD gradients/s",
+            "value": adj_rate, "unit": "parameter-gradients/s", "n_gpus": 1, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": t_grad * 1e3, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded)",
+            "config": {"workload": f"studio: displaced sphere + plane ({ntris} tris), 64x64 tile albedo map, "
+                                   "4 roughness regions, 8 train views 512x512, gradient at 16 spp depth 3, PCG; "
+                                   "targets 256 spp", "params": int(n_params),
+                       "l2": "flushed between timed steps (256 MB write)"},
+            "adjoint": {"ms_per_gradient": t_grad * 1e3, "param_gradients_per_s": adj_rate,
+                        "paths_per_gradient": npix * 16},
+            "coordinate_fd": {"render_ms_8_views": t_render * 1e3, "param_gradients_per_s": fd_rate,
+                              "renders_per_gradient": 2 * int(n_params),
+                              "ms_per_gradient": 2 * n_params * t_render * 1e3},
+            "adjoint_over_fd": adj_rate / fd_rate,
+            "fit": {"iterations": fit_iters, "seconds": fit_s, "optimizer": "Adam lr 0.03, decorrelated replay",
+                    "roughness_init": [float(x) for x in mats0[rough_ids, 4]], "loss_first": losses[0], "loss_last": losses[-1],
+                    "map_rmse_init": map_rmse0, "map_rmse_final": map_rmse1, "holdout_mse_init": hold0,
+                    "holdout_mse_final": hold1, "roughness_gt": [float(x) for x in gt_rough],
+                    "roughness_final": [float(x) for x in fit.roughness]},
+            "clocks": clocks,
+            "e2e": {"value": n_params / t_e2e, "unit": "parameter-gradients/s",
+                    "h2d_bytes_per_step": int(sum(t.numel() * 4 for t in host_t)),
+                    "d2h_bytes_per_step": int(host_g.numel() * 4),
+                    "call": "ohao_pt_adjoint (targets from pinned host memory, gradients back to host)"}}
+    print(json.dumps(line), flush=True)
+    pt.close()
+
+
 def main():
     args = parse()
     if args.impl == "reference":
         run_reference(args)
     elif args.workload == "instanced":
         run_instanced(args)
+    elif args.workload == "studio":
+        run_studio(args)
     else:
         run_ours(args)
 

@@ -97,6 +97,11 @@ typedef struct ohao_pt_view {
 #define OHAO_PT_FLAG_FIREFLY_CLAMP (1u << 2)
 #define OHAO_PT_FLAG_ENV_FIXED_V (1u << 8)   /* not reference: un-mirrored env lookup */
 #define OHAO_PT_FLAG_PROFILE (1u << 16)      /* record per-kernel CUDA-event times */
+/* ohao_pt_adjoint: replay the gradient with fresh samples (sample indices
+ * from sample_index_base + spp) instead of the rendered ones, so that it
+ * estimates the gradient of the loss of the expected image; with the same
+ * samples it would also differentiate the image's noise. */
+#define OHAO_PT_FLAG_ADJOINT_DECORRELATE (1u << 17)
 
 #define OHAO_PT_MODE_AUTO 0u
 #define OHAO_PT_MODE_WAVEFRONT 1u

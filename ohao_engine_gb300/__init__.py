@@ -30,6 +30,7 @@ SAMPLER_PCG, SAMPLER_SOBOL = 0, 1
 FLAG_FIREFLY_CLAMP = 1 << 2
 FLAG_ENV_FIXED_V = 1 << 8
 FLAG_PROFILE = 1 << 16
+FLAG_ADJOINT_DECORRELATE = 1 << 17
 MODE_AUTO, MODE_WAVEFRONT, MODE_PERSISTENT = 0, 1, 2
 
 EXPORTED_SYMBOLS = [

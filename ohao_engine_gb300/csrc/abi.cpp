@@ -775,7 +775,9 @@ ohao_status ohao_pt_adjoint(ohao_pt_ctx* ctx, const ohao_pt_view* views, uint32_
     if (s != OHAO_OK) return fail(ctx, s, err);
     if (loss) *loss = l;
     std::vector<const float*> cgrads(grads.begin(), grads.end());
-    return run_backward(ctx, rvs, cgrads.data(), st, d_grad_albedo_map, d_grad_roughness, cs);
+    ohao_pt_settings replay = *st;
+    if (st->flags & OHAO_PT_FLAG_ADJOINT_DECORRELATE) replay.sample_index_base = st->sample_index_base + st->spp;
+    return run_backward(ctx, rvs, cgrads.data(), &replay, d_grad_albedo_map, d_grad_roughness, cs);
 }
 
 ohao_status ohao_pt_get_profile(const ohao_pt_ctx* ctx, ohao_pt_profile* out) {

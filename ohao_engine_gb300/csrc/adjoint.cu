@@ -8,19 +8,24 @@
 //   * the linear tile albedo map read through diffuse texture slot 0
 //     (bilinear, ohao/render/diff/diff_map.hpp:40-67), and
 //   * each material's roughness (matColors[3*id+1].x).
-// Sampling is detached: random decisions, sampled directions, the
-// Russian-roulette probability and the lobe-selection divisor keep their
-// primal values (their expectation does not depend on the parameters), while
-// albedo factors, BRDF values and MIS weights are differentiated. Per chain
-//   R = sum_j T_j * G_j,   T_{j+1} = T_j * a_j / p_j,
+// The result estimates the derivative of the expected image. Each path keeps
+// its primal decisions and directions; albedo factors, BRDF values and MIS
+// weights are differentiated (pathwise part), and where the reference's
+// estimator is not importance-weighted by the density it samples from, the
+// score of that density is added: the roughness-scaled specular jitter, the
+// lobe choice where its divisor is clamped or forced, and the
+// Russian-roulette divisor where it exceeds the survival probability
+// (p = maxc(T) > 1, which makes 1/p a value of the throughput). Per chain
+//   R = sum_j T_j * G_j,   T_{j+1} = (T_j / p_j) * a_j,
 // where G_j is the light added at vertex j (emission, light NEE, env NEE, or
 // the environment seen by a ray that missed) and a_j the lobe factor. Each
 // vertex's G_j, a_j and outgoing MIS pdf are evaluated with 4-wide forward
 // duals over its local parameters (albedo r, g, b, roughness); a reverse
-// sweep over a per-thread record of the chain's vertices supplies
-// U_{j+1} = sum_{k>j} (prod a/p) G_k for the a_j terms. Nothing is stored
-// between kernels: memory traffic is the replayed traversal plus the
-// gradient scatter, which goes through a block-shared copy of the map.
+// sweep over a per-thread record of the chain's vertices carries
+// lambda_j = d loss / d T_j and the suffix value that multiplies the scores.
+// Nothing is stored between kernels: memory traffic is the replayed
+// traversal plus the gradient scatter, which goes through a block-shared copy
+// of the map.
 #include "pt_path.cuh"
 
 #include <algorithm>
@@ -261,23 +266,78 @@ struct VRec {
     float a[3];     // lobe factor (value)
     float da;       // d a_c / d albedo_c (the same for all channels)
     float dl[4];    // d loss / d local parameters
-    float invp;     // 1 / Russian-roulette probability applied here
+    float S[4];     // d log (probability of this vertex's sampling decisions) / d local parameters
+    float invp;     // 1 / Russian-roulette divisor applied here
     int has_a;
+    int cmax;       // >= 0: the divisor is maxc(T) > 1, a value of the throughput (channel of the max)
     Prov pv;
 };
+
+// Score of the reference's specular jitter (pt_raygen.rgen:516-525): the
+// direction w = normalize(R + r h), h cosine-distributed around R, has the
+// solid-angle density q(w | r) = (s c - 1) s^2 / (pi r^2 sqrt(c^2 - 1 + r^2))
+// with c = w.R and s = c + sqrt(c^2 - 1 + r^2). Its derivative in r at fixed
+// w, written with t = h.R, is
+//   d log q / d r = (1 - t^2) / (t (t + r)^2) + 2 / (t + r) - 2 / r.
+// The sampling weight of the lobe does not contain q, so the expectation
+// depends on r through it; the derivative of the expectation adds
+// (radiance after the sample) * this score (score-function estimator on the
+// jittered direction, also when the fallback direction replaced it).
+__device__ __forceinline__ float jitter_score(V3 refl, V3 h, float rough) {
+    const double t = fmax(static_cast<double>(dot(h, refl)), 1e-12);
+    const double r = rough;
+    const double tr = t + r;
+    return static_cast<float>((1.0 - t * t) / (t * tr * tr) + 2.0 / tr - 2.0 / r);
+}
+
+// spec_dir with the jitter score; same draws and same result.
+__device__ V3 spec_dir_score(Rng& rng, uint32_t& dim, V3 inDir, V3 N, float rough, float& score) {
+    V3 refl = reflect(inDir, N);
+    score = 0.0f;
+    if (rough > 0.01f) {
+        const float j0 = rng.s1(dim), j1 = rng.s1(dim + 1);
+        dim += 2;
+        const V3 h = cos_hemi(refl, j0, j1);
+        score = jitter_score(refl, h, rough);
+        const V3 jit = h * rough;
+        refl = normalize(refl + jit);
+        if (dot(refl, N) < 0.0f) {
+            const float f0 = rng.s1(dim), f1 = rng.s1(dim + 1);
+            dim += 2;
+            refl = cos_hemi(N, f0, f1);
+        }
+    }
+    return refl;
+}
+
+// lambda[c] * d g_c / d theta, accumulated
+__device__ __forceinline__ void add_lam(float dl[4], const float lam[3], const D3& g) {
+#pragma unroll
+    for (int i = 0; i < 4; ++i) dl[i] += lam[0] * g.x.d[i] + lam[1] * g.y.d[i] + lam[2] * g.z.d[i];
+}
 
 __device__ __forceinline__ void add_dl(float dl[4], const float delta[3], const float T[3], const D3& g) {
 #pragma unroll
     for (int i = 0; i < 4; ++i) dl[i] += delta[0] * T[0] * g.x.d[i] + delta[1] * T[1] * g.y.d[i] + delta[2] * T[2] * g.z.d[i];
 }
 
+struct ChainOut {
+    float lam[3];   // d loss / d (throughput at the chain's first vertex)
+    float value;    // the chain's contribution to the loss's linearisation, sum_k delta . (T_k G_k)
+};
+
 // Replays one chain (stage B when specChain, stage C otherwise) from its
-// first outgoing ray, accumulating gradients of its vertices; returns U_1,
-// the chain's radiance per unit throughput at its first vertex. prev_dl is
-// the gradient slot of the vertex the chain leaves from, which owns lastPdf.
-__device__ V3 replay_chain(const DScene& sc, const PathParams& pp, Rng& rng, uint32_t& dim, bool specChain, V3 ro,
-                           V3 rd, V3 thr, D4 lastPdf, bool lastDelta, const float delta[3], float* prev_dl, VRec* rec,
-                           const Sink& sk, int& err) {
+// first outgoing ray and accumulates the gradients of its vertices. prev_dl
+// is the gradient slot of the vertex the chain leaves from, which owns
+// lastPdf. Reverse sweep with lambda_j = d loss / d T_j:
+//   lambda_j = delta G_j + J_j^T (a_j * lambda_{j+1}),
+// J_j = d (T_j / p_j) / d T_j: diagonal 1/p_j while the Russian-roulette
+// divisor is the survival probability (p_j <= 1), plus the rank-one term of
+// p_j = maxc(T_j) when p_j > 1 (the divisor is then a value, not a
+// probability).
+__device__ ChainOut replay_chain(const DScene& sc, const PathParams& pp, Rng& rng, uint32_t& dim, bool specChain, V3 ro,
+                                 V3 rd, V3 thr, D4 lastPdf, bool lastDelta, const float delta[3], float* prev_dl,
+                                 VRec* rec, const Sink& sk, int& err) {
     int nrec = 0;
     float* last_dl = prev_dl;
     for (uint32_t bounce = 1; bounce <= pp.max_bounces && nrec < kMaxRec; ++bounce) {
@@ -286,8 +346,10 @@ __device__ V3 replay_chain(const DScene& sc, const PathParams& pp, Rng& rng, uin
         VRec& R = rec[nrec];
         R.T[0] = thr.x; R.T[1] = thr.y; R.T[2] = thr.z;
         R.has_a = 0;
+        R.cmax = -1;
         R.invp = 1.0f;
         R.dl[0] = R.dl[1] = R.dl[2] = R.dl[3] = 0.0f;
+        R.S[0] = R.S[1] = R.S[2] = R.S[3] = 0.0f;
         R.pv.flags = 0;
         if (h.prim == 0xFFFFFFFFu) {
             Surf ms;
@@ -310,11 +372,12 @@ __device__ V3 replay_chain(const DScene& sc, const PathParams& pp, Rng& rng, uin
         R.G[0] = G.x.v; R.G[1] = G.y.v; R.G[2] = G.z.v;
         nrec++;
         last_dl = R.dl;
-        if (bounce > 1) {   // Russian roulette with the primal probability
+        if (bounce > 1) {   // Russian roulette (survival probability min(p, 1), divisor p)
             const float p = maxc(thr);
             const float rr = rng.s1(dim);
             dim += 1;
             if (p < 0.01f || rr > p) break;
+            if (p > 1.0f) R.cmax = (thr.x >= thr.y && thr.x >= thr.z) ? 0 : (thr.y >= thr.z ? 1 : 2);
             thr = thr / p;
             R.invp = 1.0f / p;
         }
@@ -329,9 +392,26 @@ __device__ V3 replay_chain(const DScene& sc, const PathParams& pp, Rng& rng, uin
         dim += 1;
         const D4 spd = spec_prob(lm, rd, s.N);
         float fa, fb;   // a_c = fa * albedo_c + fb
+        // Lobe choice: probability P_b, divisor max(P, 0.01). Where they differ
+        // (clamped divisor, or the specular lobe forced below roughness 0.05)
+        // the expectation keeps d log P_b - d log div_b as a score.
+        if (bR < 0.05f) {
+            if (sp > 0.01f)
+#pragma unroll
+                for (int i = 0; i < 4; ++i) R.S[i] -= spd.d[i] / spd.v;
+        } else if (choice < sp) {
+            if (sp < 0.01f)
+#pragma unroll
+                for (int i = 0; i < 4; ++i) R.S[i] += spd.d[i] / spd.v;
+        } else if (1.0f - sp < 0.01f) {
+#pragma unroll
+            for (int i = 0; i < 4; ++i) R.S[i] -= spd.d[i] / (1.0f - spd.v);
+        }
         if (choice < sp || bR < 0.05f) {
             const V3 inDir = rd;
-            rd = spec_dir(rng, dim, rd, s.N, bR);
+            float js;
+            rd = spec_dir_score(rng, dim, rd, s.N, bR, js);
+            if (R.pv.flags & 2u) R.S[3] += js;
             ro = s.pos + s.N * 0.01f;
             const float div = gmaxf(sp, 0.01f);
             if (specChain) {
@@ -370,22 +450,40 @@ __device__ V3 replay_chain(const DScene& sc, const PathParams& pp, Rng& rng, uin
         R.a[2] = fa * s.albedo.z + fb;
         R.da = fa;
     }
-    // reverse sweep: U_j = G_j + a_j / p_j * U_{j+1}
-    float U[3] = {0.f, 0.f, 0.f};
+    // reverse sweep over lambda (d loss / d T) and the suffix value V
+    ChainOut out;
+    float lam[3] = {0.f, 0.f, 0.f};
+    float V = 0.0f;
     for (int j = nrec - 1; j >= 0; --j) {
         VRec& R = rec[j];
+        float nl[3] = {0.f, 0.f, 0.f};
         if (R.has_a) {
+            float mu[3];   // d loss / d (T_j / p_j)
 #pragma unroll
-            for (int c = 0; c < 3; ++c) R.dl[c] += R.invp * delta[c] * R.T[c] * U[c] * R.da;
+            for (int c = 0; c < 3; ++c) {
+                mu[c] = R.a[c] * lam[c];
+                R.dl[c] += R.T[c] * R.invp * lam[c] * R.da;   // through a_c(albedo_c)
+            }
 #pragma unroll
-            for (int c = 0; c < 3; ++c) U[c] = R.G[c] + R.a[c] * R.invp * U[c];
-        } else {
+            for (int i = 0; i < 4; ++i) R.dl[i] += V * R.S[i];   // sampling scores times what follows
 #pragma unroll
-            for (int c = 0; c < 3; ++c) U[c] = R.G[c];
+            for (int c = 0; c < 3; ++c) nl[c] = mu[c] * R.invp;
+            if (R.cmax >= 0) {
+                const float tm = R.T[0] * mu[0] + R.T[1] * mu[1] + R.T[2] * mu[2];
+                nl[R.cmax] -= tm * R.invp * R.invp;
+            }
+        }
+#pragma unroll
+        for (int c = 0; c < 3; ++c) {
+            nl[c] += delta[c] * R.G[c];
+            V += delta[c] * R.T[c] * R.G[c];
+            lam[c] = nl[c];
         }
     }
     for (int j = 0; j < nrec; ++j) scatter(sk, rec[j].pv, rec[j].dl);
-    return v3(U[0], U[1], U[2]);
+    out.lam[0] = lam[0]; out.lam[1] = lam[1]; out.lam[2] = lam[2];
+    out.value = V;
+    return out;
 }
 
 struct AdjParams {
@@ -456,23 +554,23 @@ __global__ void __launch_bounds__(128) k_adjoint(DScene sc, AdjParams ap, const 
         // stage A: light NEE and env NEE at throughput 1
         add_dl(dl0, delta, one, nee_d(sc, pp, rng, dim, s0, rayDir, m0, true, err));
         // stage B: specular chain from vertex 0
-        const V3 sd = spec_dir(rng, dim, rayDir, s0.N, s0.rough);
+        float js0;
+        const V3 sd = spec_dir_score(rng, dim, rayDir, s0.N, s0.rough, js0);
         const D3 tB = dvmix(d3c(v3s(1.0f)), m0.alb, s0.metal);
         const bool deltaB = s0.rough < 0.05f;
         const D4 pdfB = deltaB ? dc(1.0f) : spec_pdf(pp, m0, s0.N, rayDir, sd, true);
-        const V3 UB = replay_chain(sc, pp, rng, dim, true, s0.pos + s0.N * 0.01f, sd,
-                                   vmix(v3s(1.0f), s0.albedo, s0.metal), pdfB, deltaB, delta, dl0, rec, sk, err);
-        const float ub[3] = {UB.x, UB.y, UB.z};
-        add_dl(dl0, delta, ub, tB);
+        const ChainOut cb = replay_chain(sc, pp, rng, dim, true, s0.pos + s0.N * 0.01f, sd,
+                                         vmix(v3s(1.0f), s0.albedo, s0.metal), pdfB, deltaB, delta, dl0, rec, sk, err);
+        add_lam(dl0, cb.lam, tB);
+        if (p0.flags & 2u) dl0[3] += cb.value * js0;
         // stage C: diffuse chain from vertex 0
         const float d0 = rng.s1(dim), d1 = rng.s1(dim + 1);
         dim += 2;
         const V3 dd = cos_hemi(s0.N, d0, d1);
         const D4 pdfC = dc(gmaxf(dot(dd, s0.N), 0.0f) / kPI);
-        const V3 UC = replay_chain(sc, pp, rng, dim, false, s0.pos + s0.N * 0.01f, dd, s0.albedo, pdfC, false, delta,
-                                   dl0, rec, sk, err);
-        const float uc[3] = {UC.x, UC.y, UC.z};
-        add_dl(dl0, delta, uc, m0.alb);
+        const ChainOut cc = replay_chain(sc, pp, rng, dim, false, s0.pos + s0.N * 0.01f, dd, s0.albedo, pdfC, false,
+                                         delta, dl0, rec, sk, err);
+        add_lam(dl0, cc.lam, m0.alb);
         scatter(sk, p0, dl0);
     }
     __syncthreads();

@@ -243,6 +243,61 @@ void orc_detached_paths(const Scene* s, const float* inv_view, const float* inv_
     }
 }
 
+// Analytic FP64 gradient of the detached estimator (DetachedPathT<Dd>) for
+// up to kGradSlots selected parameters: grad[j] = sum over pixels p and
+// channels c of dLdI[p*3+c] * d(mean of the p's spp paths)_c / d theta_j,
+// theta = roughness of materials rough_ids[0..n_rough) then map entries
+// (texel*3 + channel) map_ids[0..n_map). Sampling with the scene's
+// parameters; values too (theta_e == theta_s). with_score adds the score
+// terms of the sampling decisions (the derivative of the expectation);
+// without them it is the derivative of the function that the finite
+// differences of orc_detached_paths see.
+int orc_detached_grad(const Scene* s, const float* inv_view, const float* inv_proj, uint32_t width, uint32_t height,
+                      const AbiSettings* as, uint32_t sample_base, uint32_t spp, const double* dLdI,
+                      const int32_t* rough_ids, uint32_t n_rough, const int32_t* map_ids, uint32_t n_map,
+                      int with_score, double* grad_out, int nthreads) {
+    if (n_rough + n_map > static_cast<uint32_t>(kGradSlots)) return -1;
+    View vw;
+    std::memcpy(vw.inv_view, inv_view, 64);
+    std::memcpy(vw.inv_proj, inv_proj, 64);
+    vw.width = width; vw.height = height;
+    Settings st = to_settings(as);
+    const size_t nmat = s->mats.size() / 12;
+    std::vector<int32_t> rslot(nmat, -1), mslot(s->albedo_map.size(), -1);
+    for (uint32_t j = 0; j < n_rough; ++j) rslot[static_cast<size_t>(rough_ids[j])] = static_cast<int32_t>(j);
+    for (uint32_t j = 0; j < n_map; ++j) mslot[static_cast<size_t>(map_ids[j])] = static_cast<int32_t>(n_rough + j);
+    const uint32_t np = width * height;
+    const int64_t total = static_cast<int64_t>(np) * spp;
+    const uint32_t nparam = n_rough + n_map;
+    std::vector<double> acc(nparam, 0.0);
+#ifdef _OPENMP
+    if (nthreads > 0) omp_set_num_threads(nthreads);
+#pragma omp parallel
+#endif
+    {
+        std::vector<double> loc(nparam, 0.0);
+#ifdef _OPENMP
+#pragma omp for schedule(dynamic, 16)
+#endif
+        for (int64_t k = 0; k < total; ++k) {
+            const uint32_t smp = static_cast<uint32_t>(k / np), p = static_cast<uint32_t>(k % np);
+            DetachedPathT<Dd> dp(*s, st, s->mats.data(), s->albedo_map.empty() ? nullptr : s->albedo_map.data());
+            dp.rough_slot = rslot.data();
+            dp.map_slot = mslot.empty() ? nullptr : mslot.data();
+            dp.with_score = with_score != 0;
+            const V3<Dd> r = dp.path(vw, p % width, p / width, sample_base + smp);
+            const double* g = dLdI + static_cast<size_t>(p) * 3;
+            for (uint32_t j = 0; j < nparam; ++j) loc[j] += (g[0] * r.x.d[j] + g[1] * r.y.d[j] + g[2] * r.z.d[j]) / spp;
+        }
+#ifdef _OPENMP
+#pragma omp critical
+#endif
+        for (uint32_t j = 0; j < nparam; ++j) acc[j] += loc[j];
+    }
+    for (uint32_t j = 0; j < nparam; ++j) grad_out[j] = acc[j];
+    return 0;
+}
+
 // Progressive own-pixel accumulation of per-path radiance in sample order
 // (pt_raygen.rgen:1144-1186 with reprojection off): accum is RGBA32F
 // (mean, count) per pixel, updated in place; history = frames already in it.

@@ -59,6 +59,8 @@ def lib():
         L.orc_render_paths.argtypes = [vp, vp, vp, u32, u32, vp, u32, u32, vp, u32, vp, i32, i32, vp]
         L.orc_accumulate.argtypes = [vp, u32, u32, vp, u32]
         L.orc_detached_paths.argtypes = [vp, vp, vp, u32, u32, vp, u32, u32, vp, u32, vp, vp, vp, i32]
+        L.orc_detached_grad.argtypes = [vp, vp, vp, u32, u32, vp, u32, u32, vp, vp, u32, vp, u32, i32, vp, i32]
+        L.orc_detached_grad.restype = i32
         L.orc_env_cdf_build.argtypes = [vp, i32, i32, vp, vp, vp]
         L.orc_sobol_sample1d.argtypes = [u32, u32]
         L.orc_sobol_sample1d.restype = f32
@@ -190,6 +192,29 @@ class OracleScene:
         out = np.zeros((spp, npix, 3), np.float64)
         lib().orc_detached_paths(self.h, _p(view.inv_view), _p(view.inv_proj), view.width, view.height, _p(st),
                                  sample_base, spp, _p(pix), npix, _p(mats), _p(amap), _p(out), nthreads)
+        return out
+
+    def detached_grad(self, view, settings: dict, sample_base: int, spp: int, dLdI, rough_ids=(), map_ids=(),
+                      with_score: bool = True, nthreads: int = 0):
+        """Analytic FP64 gradient (forward-mode duals) of sum_p dLdI_p . I_p,
+        I_p the mean of the pixel's detached paths, w.r.t. the roughness of
+        materials ``rough_ids`` then the map entries ``map_ids`` (texel*3+c);
+        at most 40 parameters. with_score adds the sampling-score terms (the
+        device adjoint's full estimator); without, it is the derivative of
+        :meth:`detached_paths`."""
+        st = np.zeros(1, SETTINGS_DTYPE)
+        for k in SETTINGS_DTYPE.names:
+            st[k] = settings.get(k, 0)
+        g = np.ascontiguousarray(dLdI, np.float64).reshape(-1, 3)
+        assert g.shape[0] == view.width * view.height
+        r = np.ascontiguousarray(rough_ids, np.int32)
+        m = np.ascontiguousarray(map_ids, np.int32)
+        out = np.zeros(r.size + m.size, np.float64)
+        rc = lib().orc_detached_grad(self.h, _p(view.inv_view), _p(view.inv_proj), view.width, view.height, _p(st),
+                                     sample_base, spp, _p(g), _p(r), r.size, _p(m), m.size, int(with_score), _p(out),
+                                     nthreads)
+        if rc != 0:
+            raise ValueError("detached_grad: too many parameters")
         return out
 
 
