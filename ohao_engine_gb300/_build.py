@@ -24,8 +24,8 @@ NVCC_FLAGS = ["-O3", "-lineinfo", "-std=c++20", "-fmad=false", "--extended-lambd
               "-Xcompiler", "-ffp-contract=off", "-Xptxas", "-warn-spills"]
 CXX_FLAGS = ["-O2", "-std=c++20", "-fPIC", "-ffp-contract=off", "-Wall"]
 
-CU_SOURCES = ["bvh_build.cu", "scene_kernels.cu", "wavefront.cu", "adjoint.cu"]
-CPP_SOURCES = ["abi.cpp"]
+CU_SOURCES = ["bvh_build.cu", "scene_kernels.cu", "wavefront.cu", "adjoint.cu", "dn_kernels.cu"]
+CPP_SOURCES = ["abi.cpp", "dn_net.cpp"]
 
 
 def _cuda_home() -> str:
@@ -51,7 +51,7 @@ def _newer(target: str, deps) -> bool:
 
 def _headers():
     return [os.path.join(CSRC, f) for f in os.listdir(CSRC) if f.endswith((".cuh", ".hpp", ".h"))] + [
-        os.path.join(PKG, "..", "include", "ohao_pt.h")]
+        os.path.join(PKG, "..", "include", "ohao_pt.h"), os.path.join(PKG, "..", "include", "ohao_dn.h")]
 
 
 def _compile(src: str, verbose: bool) -> str:

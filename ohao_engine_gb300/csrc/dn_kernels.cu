@@ -1,0 +1,590 @@
+// dn_kernels.cu -- kernels of the BF16 U-Net denoiser on tcgen05 tensor cores.
+//
+// Every 3x3 convolution (forward, data gradient, weight gradient) is one
+// implicit GEMM on tcgen05.mma: the CTA's 128 threads gather the operand
+// tiles from NHWC activations straight into shared memory in the canonical
+// no-swizzle layout (zero padding, nearest 2x upsampling and the skip
+// concatenation are folded into the gather), one thread issues the MMAs into
+// an FP32 accumulator in tensor memory, two shared-memory stages overlap the
+// gather of chunk k+1 with the MMAs of chunk k (tcgen05.commit -> mbarrier),
+// and the epilogue reads the accumulator with tcgen05.ld and applies bias,
+// ReLU and the BF16 store (forward), the scatter into the input gradients
+// (data gradient), or FP32 atomics into the weight gradient.
+//
+// Shapes: activations [pixels][C8] BF16 with C8 = round_up(C, 8); gradients
+// [pixels][C8] FP32. Weights W [cout_n][k_pad] BF16, k = tap*cin8 + ci
+// (tap = 3*dy + dx), and the transposed copy Wt [cin_n][k2_pad],
+// k2 = tap*cout8 + co, for the data gradient.
+#include <cuda_bf16.h>
+
+#include <algorithm>
+
+#include "dn_types.hpp"
+#include "umma.cuh"
+
+namespace ohao {
+namespace dn {
+
+namespace {
+
+constexpr int kThreads = 128;
+constexpr int kBM = 128;     // rows of the accumulator (TMEM lanes)
+constexpr int kBK = 64;      // K elements per stage (8 core-matrix columns)
+constexpr int kStages = 2;
+
+__device__ __forceinline__ uint4 pack8(const float (&f)[8]) {
+    uint4 u;
+    __nv_bfloat162 h0 = __floats2bfloat162_rn(f[0], f[1]);
+    __nv_bfloat162 h1 = __floats2bfloat162_rn(f[2], f[3]);
+    __nv_bfloat162 h2 = __floats2bfloat162_rn(f[4], f[5]);
+    __nv_bfloat162 h3 = __floats2bfloat162_rn(f[6], f[7]);
+    u.x = *reinterpret_cast<uint32_t*>(&h0);
+    u.y = *reinterpret_cast<uint32_t*>(&h1);
+    u.z = *reinterpret_cast<uint32_t*>(&h2);
+    u.w = *reinterpret_cast<uint32_t*>(&h3);
+    return u;
+}
+__device__ __forceinline__ void unpack8(uint4 u, float (&f)[8]) {
+    const __nv_bfloat162* h = reinterpret_cast<const __nv_bfloat162*>(&u);
+#pragma unroll
+    for (int i = 0; i < 4; ++i) {
+        const float2 t = __bfloat1622float2(h[i]);
+        f[2 * i] = t.x;
+        f[2 * i + 1] = t.y;
+    }
+}
+
+// Pixel p of the flattened [n][h][w] grid shifted by tap; false outside.
+__device__ __forceinline__ bool tap_pixel(const Geo& g, int64_t p, int tap, int sign, int64_t& q, int& qy, int& qx) {
+    const int x = static_cast<int>(p % g.w);
+    const int64_t t = p / g.w;
+    const int y = static_cast<int>(t % g.h);
+    const int64_t n = t / g.h;
+    qy = y + sign * (tap / 3 - 1);
+    qx = x + sign * (tap % 3 - 1);
+    if (qy < 0 || qy >= g.h || qx < 0 || qx >= g.w) return false;
+    q = (n * g.h + qy) * g.w + qx;
+    return true;
+}
+
+// 8 input channels [c0, c0+8) of the (possibly upsampled + concatenated)
+// convolution input at pixel q (row qy, column qx of the full-res grid).
+__device__ __forceinline__ uint4 load_input8(const ConvArgs& a, int64_t q, int qy, int qx, int c0) {
+    if (c0 < a.c0) {
+        if (a.up0) {   // nearest 2x upsample of a half-resolution source
+            const int64_t n = q / (static_cast<int64_t>(a.g.h) * a.g.w);
+            const int64_t lq = (n * (a.g.h / 2) + qy / 2) * (a.g.w / 2) + qx / 2;
+            return *reinterpret_cast<const uint4*>(a.x0 + lq * a.c0s + c0);
+        }
+        return *reinterpret_cast<const uint4*>(a.x0 + q * a.c0s + c0);
+    }
+    if (c0 - a.c0 < a.c1) return *reinterpret_cast<const uint4*>(a.x1 + q * a.c1s + (c0 - a.c0));
+    return make_uint4(0, 0, 0, 0);
+}
+
+// 8 channels of dZ = dY * relu'(Y) at pixel q, as BF16.
+__device__ __forceinline__ uint4 load_dz8(const ConvArgs& a, int64_t q, int c0) {
+    if (c0 >= a.cout8) return make_uint4(0, 0, 0, 0);
+    const float4* gp = reinterpret_cast<const float4*>(a.dy + q * a.cout8 + c0);
+    const float4 g0 = gp[0], g1 = gp[1];
+    float f[8] = {g0.x, g0.y, g0.z, g0.w, g1.x, g1.y, g1.z, g1.w};
+    if (a.relu) {
+        float yv[8];
+        unpack8(*reinterpret_cast<const uint4*>(a.y + q * a.cout8 + c0), yv);
+#pragma unroll
+        for (int i = 0; i < 8; ++i)
+            if (!(yv[i] > 0.0f)) f[i] = 0.0f;
+    }
+    return pack8(f);
+}
+
+struct Smem {
+    uint64_t bar[kStages];
+    uint64_t done;
+    uint32_t tmem;
+};
+
+// Fills stage buffers for K chunk kc. A: kBM rows; B: bn rows.
+template <int kMode>
+__device__ __forceinline__ void gather(const ConvArgs& a, int64_t mtile, int ntile, int kc, uint8_t* sa, uint8_t* sb,
+                                       int bn) {
+    const int t = threadIdx.x;
+    if constexpr (kMode == kFwd || kMode == kDgrad) {
+        // A, K-major: offset(row m, vector kb) = ((m/8)*8 + kb)*128 + (m%8)*16 = L*16
+        const int vec_per_tap = (kMode == kFwd ? a.cin8 : a.cout8) / 8;
+        const int kvec_total = 9 * vec_per_tap;
+#pragma unroll 2
+        for (int it = 0; it < (kBM * 8) / kThreads; ++it) {
+            const int L = it * kThreads + t;
+            const int r = L & 7, kb = (L >> 3) & 7, mb = L >> 6;
+            const int m = mb * 8 + r;
+            const int kv = kc * 8 + kb;
+            const int64_t p = mtile * kBM + m;
+            uint4 v = make_uint4(0, 0, 0, 0);
+            if (p < a.g.npix && kv < kvec_total) {
+                const int tap = kv / vec_per_tap, c0 = (kv % vec_per_tap) * 8;
+                int64_t q;
+                int qy, qx;
+                if (kMode == kFwd) {
+                    if (tap_pixel(a.g, p, tap, 1, q, qy, qx)) v = load_input8(a, q, qy, qx, c0);
+                } else {
+                    if (tap_pixel(a.g, p, tap, -1, q, qy, qx)) v = load_dz8(a, q, c0);
+                }
+            }
+            *reinterpret_cast<uint4*>(sa + L * 16) = v;
+        }
+        // B, K-major weights: row n, vector kb
+        const __nv_bfloat16* wsrc = (kMode == kFwd) ? a.w : a.wt;
+        const int kpad = (kMode == kFwd) ? a.k_pad : a.k2_pad;
+        for (int L = t; L < bn * 8; L += kThreads) {
+            const int r = L & 7, kb = (L >> 3) & 7, nb = L >> 6;
+            const int n = nb * 8 + r;
+            const uint4 v = *reinterpret_cast<const uint4*>(wsrc + static_cast<int64_t>(n) * kpad + kc * kBK + kb * 8);
+            *reinterpret_cast<uint4*>(sb + L * 16) = v;
+        }
+    } else {
+        // weight gradient: K = pixels. A (MN-major): row k = pixel, 16 B = 8 output channels.
+        // offset(mn_blk, k_blk) = (k_blk*16 + mn_blk)*128 + (k%8)*16 = L*16
+        const int64_t kbase = mtile * static_cast<int64_t>(kBK);
+#pragma unroll 2
+        for (int it = 0; it < (kBM * 8) / kThreads; ++it) {
+            const int L = it * kThreads + t;
+            const int r = L & 7, mnb = (L >> 3) & 15, kb = L >> 7;
+            const int64_t p = kbase + kb * 8 + r;
+            uint4 v = make_uint4(0, 0, 0, 0);
+            if (p < a.g.npix) v = load_dz8(a, p, mnb * 8);
+            *reinterpret_cast<uint4*>(sa + L * 16) = v;
+        }
+        // B (MN-major): row k = pixel, 16 B = 8 consecutive features (tap, ci..ci+7)
+        const int nb_count = bn / 8;
+        for (int L = t; L < bn * 8; L += kThreads) {
+            const int r = L & 7, nb = (L >> 3) % nb_count, kb = (L >> 3) / nb_count;
+            const int64_t p = kbase + kb * 8 + r;
+            const int f = ntile * a.bn + nb * 8;
+            uint4 v = make_uint4(0, 0, 0, 0);
+            if (p < a.g.npix && f < 9 * a.cin8) {
+                const int tap = f / a.cin8, c0 = f % a.cin8;
+                int64_t q;
+                int qy, qx;
+                if (tap_pixel(a.g, p, tap, 1, q, qy, qx)) v = load_input8(a, q, qy, qx, c0);
+            }
+            *reinterpret_cast<uint4*>(sb + L * 16) = v;
+        }
+    }
+}
+
+template <int kMode>
+__global__ void __launch_bounds__(kThreads) k_conv(ConvArgs a, int* err_flag) {
+    extern __shared__ __align__(1024) uint8_t dsm[];
+    __shared__ Smem ss;
+    const int bn = a.bn;
+    const uint32_t a_bytes = kBM * kBK * 2, b_bytes = static_cast<uint32_t>(bn) * kBK * 2;
+    uint8_t* stage_a[kStages];
+    uint8_t* stage_b[kStages];
+    for (int s = 0; s < kStages; ++s) {
+        stage_a[s] = dsm + s * (a_bytes + b_bytes);
+        stage_b[s] = stage_a[s] + a_bytes;
+    }
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    uint32_t ncols = 32;
+    while (ncols < static_cast<uint32_t>(bn)) ncols <<= 1;
+    if (threadIdx.x == 0) {
+        for (int s = 0; s < kStages; ++s) umma::mbar_init(&ss.bar[s], 1);
+        umma::mbar_init(&ss.done, 1);
+        umma::mbar_fence_init();
+    }
+    if (warp == 0) umma::tmem_alloc(&ss.tmem, ncols);
+    umma::tc_fence_before();
+    __syncthreads();
+    umma::tc_fence_after();
+    const uint32_t tmem = ss.tmem;
+
+    // tiles: fwd/dgrad -> blockIdx.x = pixel tile, blockIdx.y = N tile
+    //        wgrad     -> blockIdx.x = N tile, blockIdx.y = pixel split
+    int64_t mtile;
+    int ntile, kchunks;
+    int64_t wg_first = 0, wg_last = 0;
+    if constexpr (kMode == kWgrad) {
+        ntile = blockIdx.x;
+        const int64_t nchunks_total = (a.g.npix + kBK - 1) / kBK;
+        const int64_t per = (nchunks_total + gridDim.y - 1) / gridDim.y;
+        wg_first = blockIdx.y * per;
+        wg_last = wg_first + per < nchunks_total ? wg_first + per : nchunks_total;
+        kchunks = wg_last > wg_first ? static_cast<int>(wg_last - wg_first) : 0;
+        mtile = wg_first;
+    } else {
+        mtile = blockIdx.x;
+        ntile = blockIdx.y;
+        kchunks = (kMode == kFwd ? a.k_pad : a.k2_pad) / kBK;
+    }
+    const uint32_t idesc = umma::idesc_bf16(kBM, static_cast<uint32_t>(bn), kMode == kWgrad, kMode == kWgrad);
+    bool ok = true;
+    for (int kc = 0; kc < kchunks && ok; ++kc) {
+        const int s = kc % kStages;
+        if (kc >= kStages) ok = umma::mbar_wait(&ss.bar[s], ((kc / kStages) - 1) & 1);
+        if (!__syncthreads_and(ok)) {
+            ok = false;
+            break;
+        }
+        if constexpr (kMode == kWgrad) gather<kMode>(a, wg_first + kc, ntile, kc, stage_a[s], stage_b[s], bn);
+        else gather<kMode>(a, mtile, ntile, kc, stage_a[s], stage_b[s], bn);
+        umma::fence_async_smem();
+        __syncthreads();
+        if (threadIdx.x == 0) {
+            umma::tc_fence_after();
+            const uint32_t sa = umma::smem_u32(stage_a[s]), sb = umma::smem_u32(stage_b[s]);
+#pragma unroll
+            for (int i = 0; i < kBK / 16; ++i) {
+                uint64_t da, db;
+                if constexpr (kMode == kWgrad) {
+                    // MN-major, no swizzle: SBO = stride between 8-element M/N groups (128 B),
+                    // LBO = stride between 8-row K groups
+                    da = umma::smem_desc(sa + i * 2 * 2048, 2048, 128);
+                    db = umma::smem_desc(sb + i * 2 * (bn / 8) * 128, (bn / 8) * 128, 128);
+                } else {
+                    // K-major: LBO = 128 (next 8 K), SBO = 1024 (next 8 rows)
+                    da = umma::smem_desc(sa + i * 256, 128, 1024);
+                    db = umma::smem_desc(sb + i * 256, 128, 1024);
+                }
+                umma::mma_bf16(tmem, da, db, idesc, kc > 0 || i > 0);
+            }
+            umma::mma_commit(&ss.bar[s]);
+        }
+    }
+    // drain: the last commit covers every MMA issued before it
+    if (threadIdx.x == 0) umma::mma_commit(&ss.done);
+    bool drained = umma::mbar_wait(&ss.done, 0);
+    if (!ok || !drained) {
+        if (threadIdx.x == 0) atomicOr(err_flag, 2);
+    }
+    umma::tc_fence_after();
+    const bool good = __syncthreads_and(ok && drained);
+    if (good && kchunks > 0) {
+        const int row = warp * 32 + lane;
+        const uint32_t trow = tmem + (static_cast<uint32_t>(warp * 32) << 16);
+        if constexpr (kMode == kFwd) {
+            const int64_t p = mtile * kBM + row;
+            for (int c = 0; c < bn; c += 8) {
+                float v[8];
+                umma::tmem_ld8(trow + c, v);
+                const int co = ntile * a.bn + c;
+                if (p < a.g.npix && co < a.cout8) {
+#pragma unroll
+                    for (int i = 0; i < 8; ++i) {
+                        v[i] += (co + i < a.cout) ? a.bias[co + i] : 0.0f;
+                        if (a.relu) v[i] = fmaxf(v[i], 0.0f);
+                        if (co + i >= a.cout) v[i] = 0.0f;
+                    }
+                    if (a.yf) {
+                        float4* o = reinterpret_cast<float4*>(a.yf + p * a.cout8 + co);
+                        o[0] = make_float4(v[0], v[1], v[2], v[3]);
+                        o[1] = make_float4(v[4], v[5], v[6], v[7]);
+                    } else {
+                        *reinterpret_cast<uint4*>(a.yout + p * a.cout8 + co) = pack8(v);
+                    }
+                }
+            }
+        } else if constexpr (kMode == kDgrad) {
+            // tcgen05.ld is warp-collective (.sync.aligned): every lane loads,
+            // the row test comes after
+            const int64_t p = mtile * kBM + row;
+            const bool live = p < a.g.npix;
+            const int64_t pc = live ? p : 0;
+            const int x = static_cast<int>(pc % a.g.w);
+            const int64_t tt = pc / a.g.w;
+            const int y = static_cast<int>(tt % a.g.h);
+            const int64_t n = tt / a.g.h;
+            for (int c = 0; c < bn; c += 8) {
+                float v[8];
+                umma::tmem_ld8(trow + c, v);
+                const int ci = ntile * a.bn + c;
+                if (live) {
+                    if (ci < a.c0) {
+                        if (a.up0) {
+                            const int64_t lq = (n * (a.g.h / 2) + y / 2) * (a.g.w / 2) + x / 2;
+                            float* d = a.dx0 + lq * a.c0s + ci;
+#pragma unroll
+                            for (int i = 0; i < 8; ++i) atomicAdd(d + i, v[i]);
+                        } else {
+                            float* d = a.dx0 + p * a.c0s + ci;
+#pragma unroll
+                            for (int i = 0; i < 8; ++i) d[i] += v[i];
+                        }
+                    } else if (ci - a.c0 < a.c1) {
+                        float* d = a.dx1 + p * a.c1s + (ci - a.c0);
+#pragma unroll
+                        for (int i = 0; i < 8; ++i) d[i] += v[i];
+                    }
+                }
+            }
+        } else {
+            // weight gradient: row = output channel, columns = features
+            // (warp-collective load first, row test after)
+            for (int c = 0; c < bn; c += 8) {
+                float v[8];
+                umma::tmem_ld8(trow + c, v);
+                const int f = ntile * a.bn + c;
+                if (row < a.cout) {
+#pragma unroll
+                    for (int i = 0; i < 8; ++i)
+                        if (f + i < 9 * a.cin8 && v[i] != 0.0f)
+                            atomicAdd(a.dw + static_cast<int64_t>(row) * a.k_pad + f + i, v[i]);
+                }
+            }
+        }
+    }
+    umma::tc_fence_before();
+    __syncthreads();
+    if (warp == 0) umma::tmem_dealloc(tmem, ncols);
+}
+
+// ---- elementwise kernels ----
+__global__ void k_pool_fwd(const __nv_bfloat16* __restrict__ x, __nv_bfloat16* __restrict__ y, Geo lo, int c8) {
+    const int64_t total = lo.npix * (c8 / 8);
+    for (int64_t i = blockIdx.x * static_cast<int64_t>(blockDim.x) + threadIdx.x; i < total;
+         i += static_cast<int64_t>(gridDim.x) * blockDim.x) {
+        const int cv = static_cast<int>(i % (c8 / 8));
+        const int64_t p = i / (c8 / 8);
+        const int lx = static_cast<int>(p % lo.w);
+        const int64_t t = p / lo.w;
+        const int ly = static_cast<int>(t % lo.h);
+        const int64_t n = t / lo.h;
+        const int W = lo.w * 2, H = lo.h * 2;
+        float m[8];
+        for (int j = 0; j < 8; ++j) m[j] = -3.0e38f;
+        for (int dy = 0; dy < 2; ++dy)
+            for (int dx = 0; dx < 2; ++dx) {
+                const int64_t q = (n * H + ly * 2 + dy) * W + lx * 2 + dx;
+                float f[8];
+                unpack8(*reinterpret_cast<const uint4*>(x + q * c8 + cv * 8), f);
+                for (int j = 0; j < 8; ++j) m[j] = fmaxf(m[j], f[j]);
+            }
+        *reinterpret_cast<uint4*>(y + p * c8 + cv * 8) = pack8(m);
+    }
+}
+
+// d x[argmax of each 2x2 window] += d y (first maximum in dy, dx order)
+__global__ void k_pool_bwd(const __nv_bfloat16* __restrict__ x, const float* __restrict__ dy, float* __restrict__ dx,
+                           Geo lo, int c8) {
+    const int64_t total = lo.npix * c8;
+    for (int64_t i = blockIdx.x * static_cast<int64_t>(blockDim.x) + threadIdx.x; i < total;
+         i += static_cast<int64_t>(gridDim.x) * blockDim.x) {
+        const int c = static_cast<int>(i % c8);
+        const int64_t p = i / c8;
+        const int lx = static_cast<int>(p % lo.w);
+        const int64_t t = p / lo.w;
+        const int ly = static_cast<int>(t % lo.h);
+        const int64_t n = t / lo.h;
+        const int W = lo.w * 2, H = lo.h * 2;
+        float best = -3.0e38f;
+        int64_t bq = 0;
+        for (int ddy = 0; ddy < 2; ++ddy)
+            for (int ddx = 0; ddx < 2; ++ddx) {
+                const int64_t q = (n * H + ly * 2 + ddy) * W + lx * 2 + ddx;
+                const float v = __bfloat162float(x[q * c8 + c]);
+                if (v > best) { best = v; bq = q; }
+            }
+        dx[bq * c8 + c] += dy[p * c8 + c];
+    }
+}
+
+// features: log1p(radiance), albedo, normal (encoded 0..1), 1/(1+depth) on hits
+__global__ void k_pack(const float4* __restrict__ rad, const float* __restrict__ aov, __nv_bfloat16* __restrict__ x,
+                       int64_t npix_img, int w, int h, int wp, int hp, int64_t img_offset) {
+    const int64_t total = static_cast<int64_t>(wp) * hp;
+    for (int64_t i = blockIdx.x * static_cast<int64_t>(blockDim.x) + threadIdx.x; i < total;
+         i += static_cast<int64_t>(gridDim.x) * blockDim.x) {
+        const int px = static_cast<int>(i % wp), py = static_cast<int>(i / wp);
+        float f[16];
+        for (int j = 0; j < 16; ++j) f[j] = 0.0f;
+        if (px < w && py < h) {
+            const int64_t s = static_cast<int64_t>(py) * w + px;
+            const float4 r = rad[s];
+            f[0] = log1pf(fmaxf(r.x, 0.0f));
+            f[1] = log1pf(fmaxf(r.y, 0.0f));
+            f[2] = log1pf(fmaxf(r.z, 0.0f));
+            const float* a = aov + s * 8;
+            f[3] = a[0]; f[4] = a[1]; f[5] = a[2];
+            f[6] = a[3]; f[7] = a[4]; f[8] = a[5];
+            f[9] = a[7] > 0.5f ? 1.0f / (1.0f + fmaxf(a[6], 0.0f)) : 0.0f;
+        }
+        float lo8[8], hi8[8];
+        for (int j = 0; j < 8; ++j) { lo8[j] = f[j]; hi8[j] = f[8 + j]; }
+        uint4* o = reinterpret_cast<uint4*>(x + (img_offset + i) * 16);
+        o[0] = pack8(lo8);
+        o[1] = pack8(hi8);
+    }
+    (void)npix_img;
+}
+
+// out: [pixels][8] FP32 log1p radiance -> RGBA32F linear (crop from the padded grid)
+__global__ void k_unpack(const float* __restrict__ y, float4* __restrict__ out, int w, int h, int wp,
+                         int64_t img_offset) {
+    const int64_t total = static_cast<int64_t>(w) * h;
+    for (int64_t i = blockIdx.x * static_cast<int64_t>(blockDim.x) + threadIdx.x; i < total;
+         i += static_cast<int64_t>(gridDim.x) * blockDim.x) {
+        const int px = static_cast<int>(i % w), py = static_cast<int>(i / w);
+        const float* s = y + (img_offset + static_cast<int64_t>(py) * wp + px) * 8;
+        out[i] = make_float4(expm1f(fmaxf(s[0], 0.0f)), expm1f(fmaxf(s[1], 0.0f)), expm1f(fmaxf(s[2], 0.0f)), 1.0f);
+    }
+}
+
+// L1 between the prediction (log1p space) and log1p(target); d out = sign / count.
+__global__ void k_l1(const float* __restrict__ y, const float4* __restrict__ tgt, float* __restrict__ dy, int w, int h,
+                     int wp, int64_t img_offset, float inv_count, double* __restrict__ loss) {
+    double part = 0.0;
+    const int64_t total = static_cast<int64_t>(w) * h;
+    for (int64_t i = blockIdx.x * static_cast<int64_t>(blockDim.x) + threadIdx.x; i < total;
+         i += static_cast<int64_t>(gridDim.x) * blockDim.x) {
+        const int px = static_cast<int>(i % w), py = static_cast<int>(i / w);
+        const int64_t q = img_offset + static_cast<int64_t>(py) * wp + px;
+        const float4 t = tgt[i];
+        const float tv[3] = {log1pf(fmaxf(t.x, 0.0f)), log1pf(fmaxf(t.y, 0.0f)), log1pf(fmaxf(t.z, 0.0f))};
+        for (int c = 0; c < 3; ++c) {
+            const float d = y[q * 8 + c] - tv[c];
+            part += fabs(static_cast<double>(d));
+            dy[q * 8 + c] = (d > 0.0f ? 1.0f : (d < 0.0f ? -1.0f : 0.0f)) * inv_count;
+        }
+    }
+    for (int off = 16; off > 0; off >>= 1) part += __shfl_down_sync(0xFFFFFFFFu, part, off);
+    if ((threadIdx.x & 31) == 0) atomicAdd(loss, part * inv_count);
+}
+
+// bias gradient: db[co] += sum over pixels of dZ
+__global__ void k_bias_grad(const float* __restrict__ dy, const __nv_bfloat16* __restrict__ y, int relu, Geo g,
+                            int cout, int cout8, float* __restrict__ db) {
+    const int co = blockIdx.y;
+    float s = 0.0f;
+    for (int64_t p = blockIdx.x * static_cast<int64_t>(blockDim.x) + threadIdx.x; p < g.npix;
+         p += static_cast<int64_t>(gridDim.x) * blockDim.x) {
+        float v = dy[p * cout8 + co];
+        if (relu && !(__bfloat162float(y[p * cout8 + co]) > 0.0f)) v = 0.0f;
+        s += v;
+    }
+    for (int off = 16; off > 0; off >>= 1) s += __shfl_down_sync(0xFFFFFFFFu, s, off);
+    if ((threadIdx.x & 31) == 0 && co < cout) atomicAdd(db + co, s);
+}
+
+// Adam (ohao/inverse/optimizer.hpp:26-39 update rule) on FP32 master weights;
+// refreshes the BF16 copy W [cout_n][k_pad] and its transpose Wt [cin_n][k2_pad].
+__global__ void k_adam_w(float* __restrict__ w32, const float* __restrict__ g, float* __restrict__ m,
+                         float* __restrict__ v, __nv_bfloat16* __restrict__ w16, __nv_bfloat16* __restrict__ wt16,
+                         LayerShape L, float lr, float b1, float b2, float eps, float c1, float c2) {
+    const int64_t total = static_cast<int64_t>(L.cout) * 9 * L.cin8;
+    for (int64_t i = blockIdx.x * static_cast<int64_t>(blockDim.x) + threadIdx.x; i < total;
+         i += static_cast<int64_t>(gridDim.x) * blockDim.x) {
+        const int co = static_cast<int>(i / (9 * L.cin8));
+        const int f = static_cast<int>(i % (9 * L.cin8));
+        const int tap = f / L.cin8, ci = f % L.cin8;
+        const int64_t wi = static_cast<int64_t>(co) * L.k_pad + f;
+        float wv = w32[wi];
+        if (ci < L.cin) {
+            const float gv = g[wi];
+            const float mv = b1 * m[wi] + (1.0f - b1) * gv;
+            const float vv = b2 * v[wi] + (1.0f - b2) * gv * gv;
+            m[wi] = mv;
+            v[wi] = vv;
+            wv -= lr * (mv / c1) / (sqrtf(vv / c2) + eps);
+            w32[wi] = wv;
+        }
+        const __nv_bfloat16 b = __float2bfloat16_rn(ci < L.cin ? wv : 0.0f);
+        w16[wi] = b;
+        wt16[static_cast<int64_t>(ci) * L.k2_pad + tap * L.cout8 + co] = b;
+    }
+}
+
+__global__ void k_refresh(const float* __restrict__ w32, __nv_bfloat16* __restrict__ w16,
+                          __nv_bfloat16* __restrict__ wt16, LayerShape L) {
+    const int64_t total = static_cast<int64_t>(L.cout) * 9 * L.cin8;
+    for (int64_t i = blockIdx.x * static_cast<int64_t>(blockDim.x) + threadIdx.x; i < total;
+         i += static_cast<int64_t>(gridDim.x) * blockDim.x) {
+        const int co = static_cast<int>(i / (9 * L.cin8));
+        const int f = static_cast<int>(i % (9 * L.cin8));
+        const int tap = f / L.cin8, ci = f % L.cin8;
+        const int64_t wi = static_cast<int64_t>(co) * L.k_pad + f;
+        const __nv_bfloat16 b = __float2bfloat16_rn(ci < L.cin ? w32[wi] : 0.0f);
+        w16[wi] = b;
+        wt16[static_cast<int64_t>(ci) * L.k2_pad + tap * L.cout8 + co] = b;
+    }
+}
+
+__global__ void k_adam_b(float* __restrict__ b32, const float* __restrict__ g, float* __restrict__ m,
+                         float* __restrict__ v, int n, float lr, float b1, float b2, float eps, float c1, float c2) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const float gv = g[i];
+    const float mv = b1 * m[i] + (1.0f - b1) * gv;
+    const float vv = b2 * v[i] + (1.0f - b2) * gv * gv;
+    m[i] = mv;
+    v[i] = vv;
+    b32[i] -= lr * (mv / c1) / (sqrtf(vv / c2) + eps);
+}
+
+int grid_for(int64_t n, int block) {
+    return static_cast<int>(std::max<int64_t>(1, std::min<int64_t>((n + block - 1) / block, 152 * 16)));
+}
+
+}  // namespace
+
+size_t conv_smem_bytes(int bn) {
+    return static_cast<size_t>(kStages) * (kBM * kBK * 2 + bn * kBK * 2) + 1024;
+}
+
+cudaError_t launch_conv(int mode, const ConvArgs& a, int wgrad_splits, int* err_flag, cudaStream_t st) {
+    const size_t smem = conv_smem_bytes(a.bn);
+    if (mode == kFwd) {
+        cudaFuncSetAttribute(k_conv<kFwd>, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(smem));
+        const dim3 grid(static_cast<unsigned>((a.g.npix + kBM - 1) / kBM), static_cast<unsigned>(a.n_tiles));
+        k_conv<kFwd><<<grid, kThreads, smem, st>>>(a, err_flag);
+    } else if (mode == kDgrad) {
+        cudaFuncSetAttribute(k_conv<kDgrad>, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(smem));
+        const dim3 grid(static_cast<unsigned>((a.g.npix + kBM - 1) / kBM), static_cast<unsigned>(a.n_tiles));
+        k_conv<kDgrad><<<grid, kThreads, smem, st>>>(a, err_flag);
+    } else {
+        cudaFuncSetAttribute(k_conv<kWgrad>, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(smem));
+        const dim3 grid(static_cast<unsigned>(a.n_tiles), static_cast<unsigned>(std::max(1, wgrad_splits)));
+        k_conv<kWgrad><<<grid, kThreads, smem, st>>>(a, err_flag);
+    }
+    return cudaGetLastError();
+}
+
+void launch_pool_fwd(const __nv_bfloat16* x, __nv_bfloat16* y, const Geo& lo, int c8, cudaStream_t st) {
+    k_pool_fwd<<<grid_for(lo.npix * (c8 / 8), 256), 256, 0, st>>>(x, y, lo, c8);
+}
+void launch_pool_bwd(const __nv_bfloat16* x, const float* dy, float* dx, const Geo& lo, int c8, cudaStream_t st) {
+    k_pool_bwd<<<grid_for(lo.npix * c8, 256), 256, 0, st>>>(x, dy, dx, lo, c8);
+}
+void launch_pack(const float* rad, const float* aov, __nv_bfloat16* x, int w, int h, int wp, int hp, int64_t img_off,
+                 cudaStream_t st) {
+    k_pack<<<grid_for(static_cast<int64_t>(wp) * hp, 256), 256, 0, st>>>(
+        reinterpret_cast<const float4*>(rad), aov, x, static_cast<int64_t>(w) * h, w, h, wp, hp, img_off);
+}
+void launch_unpack(const float* y, float* out, int w, int h, int wp, int64_t img_off, cudaStream_t st) {
+    k_unpack<<<grid_for(static_cast<int64_t>(w) * h, 256), 256, 0, st>>>(y, reinterpret_cast<float4*>(out), w, h, wp,
+                                                                           img_off);
+}
+void launch_l1(const float* y, const float* tgt, float* dy, int w, int h, int wp, int64_t img_off, float inv_count,
+               double* loss, cudaStream_t st) {
+    k_l1<<<grid_for(static_cast<int64_t>(w) * h, 256), 256, 0, st>>>(y, reinterpret_cast<const float4*>(tgt), dy, w, h,
+                                                                        wp, img_off, inv_count, loss);
+}
+void launch_bias_grad(const float* dy, const __nv_bfloat16* y, bool relu, const Geo& g, int cout, int cout8, float* db,
+                      cudaStream_t st) {
+    const dim3 grid(static_cast<unsigned>(std::min<int64_t>(64, (g.npix + 255) / 256)), static_cast<unsigned>(cout));
+    k_bias_grad<<<grid, 256, 0, st>>>(dy, y, relu ? 1 : 0, g, cout, cout8, db);
+}
+void launch_refresh(const LayerShape& L, const float* w32, __nv_bfloat16* w16, __nv_bfloat16* wt16, cudaStream_t st) {
+    k_refresh<<<grid_for(static_cast<int64_t>(L.cout) * 9 * L.cin8, 256), 256, 0, st>>>(w32, w16, wt16, L);
+}
+void launch_adam(const LayerShape& L, float* w32, const float* gw, float* mw, float* vw, __nv_bfloat16* w16,
+                 __nv_bfloat16* wt16, float* b32, const float* gb, float* mb, float* vb, float lr, int t,
+                 cudaStream_t st) {
+    const float b1 = 0.9f, b2 = 0.999f, eps = 1e-8f;
+    const float c1 = 1.0f - powf(b1, static_cast<float>(t)), c2 = 1.0f - powf(b2, static_cast<float>(t));
+    k_adam_w<<<grid_for(static_cast<int64_t>(L.cout) * 9 * L.cin8, 256), 256, 0, st>>>(w32, gw, mw, vw, w16, wt16, L,
+                                                                                     lr, b1, b2, eps, c1, c2);
+    k_adam_b<<<(L.cout + 127) / 128, 128, 0, st>>>(b32, gb, mb, vb, L.cout, lr, b1, b2, eps, c1, c2);
+}
+
+}  // namespace dn
+}  // namespace ohao
