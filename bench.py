@@ -557,7 +557,7 @@ def run_studio(args, fit_iters=80):
     pt.close()
 
 
-def run_denoise(args, n_scenes=50, iters=3000, crop=128, batch=8):
+def run_denoise(args, n_scenes=50, iters=10000, crop=128, batch=8, variants=6):
     """Learned denoiser: the U-Net (tcgen05 BF16 convolutions, FP32
     accumulation) is trained on this GPU by the library's own kernels on
     1-spp / 1024-spp pairs of 256x256 renders of n_scenes seeded scenes of
@@ -581,7 +581,7 @@ def run_denoise(args, n_scenes=50, iters=3000, crop=128, batch=8):
         pt = og.PathTracer()
         pt.load_scene(sd)
         pairs = [render_pair(pt, sd.views[0], side, side, 1, 1024 if k == 0 else 1, seed_base=4096 * k)
-                 for k in range(4)]
+                 for k in range(variants)]
         ref = pairs[0][2]
         data.append(([p[0] for p in pairs], [p[1] for p in pairs], ref))
         pt.close()
@@ -599,7 +599,7 @@ def run_denoise(args, n_scenes=50, iters=3000, crop=128, batch=8):
         xs, aovs, ts = [], [], []
         for _ in range(batch):
             s = int(rng.integers(n_scenes))
-            k = int(rng.integers(4))
+            k = int(rng.integers(variants))
             y0, x0 = (int(v) for v in rng.integers(0, side - crop + 1, 2) // 16 * 16)
             xs.append(crop_of(data[s][0][k], 4, y0, x0))
             aovs.append(crop_of(data[s][1][k], 8, y0, x0))
@@ -665,8 +665,9 @@ def run_denoise(args, n_scenes=50, iters=3000, crop=128, batch=8):
             "ms_per_step": render_ms + infer_ms, "higher_is_better": False, "scaling": "weak", "vs_baseline": None,
             "dtype": "bf16 (FP32 accumulation)", "data": "synthetic (seeded)",
             "config": {"workload": "U-Net 32/48/64/96/128, 10-ch input; trained on "
-                                   f"{n_scenes} scenes x 256^2 (1 spp x4 vs 1024 spp), {iters} Adam steps of "
-                                   f"{batch}x{crop}^2 crops, L1 on log radiance; judged on sphere_1m 1920x1080"},
+                                   f"{n_scenes} scenes x 256^2 (1 spp x{variants} vs 1024 spp), {iters} Adam steps "
+                                   f"of {batch}x{crop}^2 crops, L1 on log radiance + L1 after the display "
+                                   "transform; judged on sphere_1m 1920x1080"},
             "denoised": {"rmse": den_rmse, "render_1spp_ms": render_ms, "infer_ms": infer_ms,
                          "total_ms": render_ms + infer_ms},
             "plain": plain, "plain_spp_matched": matched,

@@ -15,7 +15,8 @@
  * ohao_pt_view.aov layout: first-hit albedo.rgb, normal*0.5+0.5, view depth,
  * hit flag). Network input channels: log(1 + radiance).rgb, albedo.rgb,
  * encoded normal, 1 / (1 + depth) on hits. Output: log(1 + radiance),
- * returned as linear RGBA32F. Loss: L1 in log(1 + radiance).
+ * returned as linear RGBA32F. Loss: L1 in log(1 + radiance) plus L1 after
+ * the reference's display transform.
  *
  * Status codes and ohao_stream are those of ohao_pt.h. A context is
  * externally synchronised. No counterpart calls in the reference beyond the
@@ -56,8 +57,10 @@ ohao_status ohao_dn_infer(ohao_dn_ctx* ctx, const float* const* d_radiance, cons
                           uint32_t n_images, uint32_t width, uint32_t height, float* const* d_out,
                           ohao_stream stream);
 
-/* One Adam step (beta1 0.9, beta2 0.999, eps 1e-8) of the L1 loss between
- * the network output and log(1 + d_target) (device RGBA32F) over a batch;
+/* One Adam step (beta1 0.9, beta2 0.999, eps 1e-8) of the loss between the
+ * network output y and the reference d_target (device RGBA32F) over a batch:
+ * per channel |y - log(1 + t)| + |D(exp(y) - 1) - D(t)|, D the display
+ * transform pow(ACES(x / 2), 1/2.2) of pt_raygen.rgen:1263-1264, averaged.
  * *loss (host) receives the batch loss before the step. width and height
  * must be multiples of 16. */
 ohao_status ohao_dn_train_step(ohao_dn_ctx* ctx, const float* const* d_radiance, const float* const* d_aov,

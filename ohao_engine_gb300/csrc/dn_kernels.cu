@@ -429,7 +429,28 @@ __global__ void k_unpack(const float* __restrict__ y, float4* __restrict__ out, 
     }
 }
 
-// L1 between the prediction (log1p space) and log1p(target); d out = sign / count.
+// The reference's display transform pow(ACES(x / 2), 1/2.2) with
+// ACES(u) = clamp(u (2.51 u + 0.03) / (u (2.43 u + 0.59) + 0.14), 0, 1)
+// (pt_raygen.rgen:99-102, 1263-1264) and its derivative in x (the slope at
+// black is bounded by evaluating it at ACES >= 1e-3).
+__device__ __forceinline__ float display_tf(float x, float& slope) {
+    const float u = 0.5f * fmaxf(x, 0.0f);
+    const float num = u * (2.51f * u + 0.03f), den = u * (2.43f * u + 0.59f) + 0.14f;
+    const float a = num / den;
+    if (a >= 1.0f) {
+        slope = 0.0f;
+        return 1.0f;
+    }
+    const float da = ((5.02f * u + 0.03f) * den - num * (4.86f * u + 0.59f)) / (den * den) * 0.5f;
+    const float ac = fmaxf(a, 1e-3f);
+    slope = (1.0f / 2.2f) * powf(ac, 1.0f / 2.2f) / ac * da;
+    return powf(fmaxf(a, 0.0f), 1.0f / 2.2f);
+}
+
+// Loss per channel: |y - log1p(t)| + kDisplayWeight |D(expm1(y)) - D(t)|
+// (y = prediction in log1p space, D = display transform); d out = its
+// (sub)gradient / count.
+constexpr float kDisplayWeight = 1.0f;
 __global__ void k_l1(const float* __restrict__ y, const float4* __restrict__ tgt, float* __restrict__ dy, int w, int h,
                      int wp, int64_t img_offset, float inv_count, double* __restrict__ loss) {
     double part = 0.0;
@@ -439,11 +460,18 @@ __global__ void k_l1(const float* __restrict__ y, const float4* __restrict__ tgt
         const int px = static_cast<int>(i % w), py = static_cast<int>(i / w);
         const int64_t q = img_offset + static_cast<int64_t>(py) * wp + px;
         const float4 t = tgt[i];
-        const float tv[3] = {log1pf(fmaxf(t.x, 0.0f)), log1pf(fmaxf(t.y, 0.0f)), log1pf(fmaxf(t.z, 0.0f))};
+        const float tl[3] = {fmaxf(t.x, 0.0f), fmaxf(t.y, 0.0f), fmaxf(t.z, 0.0f)};
         for (int c = 0; c < 3; ++c) {
-            const float d = y[q * 8 + c] - tv[c];
-            part += fabs(static_cast<double>(d));
-            dy[q * 8 + c] = (d > 0.0f ? 1.0f : (d < 0.0f ? -1.0f : 0.0f)) * inv_count;
+            const float yv = y[q * 8 + c];
+            const float d = yv - log1pf(tl[c]);
+            float s_unused, slope;
+            const float dt = display_tf(tl[c], s_unused);
+            const float x = yv > 0.0f ? expm1f(yv) : 0.0f;
+            const float dd = display_tf(x, slope) - dt;
+            part += fabs(static_cast<double>(d)) + kDisplayWeight * fabs(static_cast<double>(dd));
+            const float g_log = d > 0.0f ? 1.0f : (d < 0.0f ? -1.0f : 0.0f);
+            const float g_disp = yv > 0.0f ? (dd > 0.0f ? 1.0f : (dd < 0.0f ? -1.0f : 0.0f)) * slope * (x + 1.0f) : 0.0f;
+            dy[q * 8 + c] = (g_log + kDisplayWeight * g_disp) * inv_count;
         }
     }
     for (int off = 16; off > 0; off >>= 1) part += __shfl_down_sync(0xFFFFFFFFu, part, off);

@@ -178,14 +178,34 @@ def forward(x, params):
     return T
 
 
+DISPLAY_WEIGHT = 1.0
+
+
+def display_tf(x):
+    """pow(ACES(x / 2), 1/2.2) and its slope (evaluated at ACES >= 1e-3)."""
+    u = 0.5 * np.maximum(x, 0.0)
+    num = u * (2.51 * u + 0.03)
+    den = u * (2.43 * u + 0.59) + 0.14
+    a = num / den
+    da = ((5.02 * u + 0.03) * den - num * (4.86 * u + 0.59)) / (den * den) * 0.5
+    ac = np.maximum(a, 1e-3)
+    slope = np.where(a >= 1.0, 0.0, (1.0 / 2.2) * ac ** (1.0 / 2.2) / ac * da)
+    return np.where(a >= 1.0, 1.0, np.maximum(a, 0.0) ** (1.0 / 2.2)), slope
+
+
 def l1_loss_grad(out, target_lin):
-    """L1 between out[..., :3] (log1p space) and log1p(target); d out."""
-    t = np.log1p(np.maximum(target_lin, 0.0))
-    d = out[..., :3] - t
+    """|out - log1p(t)| + DISPLAY_WEIGHT |D(expm1(out)) - D(t)| per channel
+    (out in log1p space, D the display transform), mean and d out."""
+    tl = np.maximum(target_lin, 0.0)
+    y = out[..., :3]
+    d = y - np.log1p(tl)
+    x = np.where(y > 0, np.expm1(np.maximum(y, 0.0)), 0.0)
+    dx, slope = display_tf(x)
+    dd = dx - display_tf(tl)[0]
     cnt = d.size
     g = np.zeros_like(out)
-    g[..., :3] = np.sign(d) / cnt
-    return np.abs(d).sum() / cnt, g
+    g[..., :3] = (np.sign(d) + DISPLAY_WEIGHT * np.where(y > 0, np.sign(dd) * slope * (x + 1.0), 0.0)) / cnt
+    return (np.abs(d).sum() + DISPLAY_WEIGHT * np.abs(dd).sum()) / cnt, g
 
 
 def backward(T, params, d_out):
