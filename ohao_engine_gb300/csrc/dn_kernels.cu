@@ -54,31 +54,36 @@ __device__ __forceinline__ void unpack8(uint4 u, float (&f)[8]) {
     }
 }
 
-// Pixel p of the flattened [n][h][w] grid shifted by tap; false outside.
-__device__ __forceinline__ bool tap_pixel(const Geo& g, int64_t p, int tap, int sign, int64_t& q, int& qy, int& qx) {
-    const int x = static_cast<int>(p % g.w);
-    const int64_t t = p / g.w;
-    const int y = static_cast<int>(t % g.h);
-    const int64_t n = t / g.h;
-    qy = y + sign * (tap / 3 - 1);
-    qx = x + sign * (tap % 3 - 1);
-    if (qy < 0 || qy >= g.h || qx < 0 || qx >= g.w) return false;
-    q = (n * g.h + qy) * g.w + qx;
-    return true;
+// Pixel coordinates of the flattened [n][h][w] grid (pixel counts < 2^31).
+struct Pix {
+    int x, y, n;   // n < 0: outside the grid
+};
+__device__ __forceinline__ Pix pix_of(const Geo& g, int p) {
+    Pix r;
+    if (p >= g.npix) {
+        r.x = r.y = 0;
+        r.n = -1;
+        return r;
+    }
+    r.x = p % g.w;
+    const int t = p / g.w;
+    r.y = t % g.h;
+    r.n = t / g.h;
+    return r;
 }
 
 // 8 input channels [c0, c0+8) of the (possibly upsampled + concatenated)
-// convolution input at pixel q (row qy, column qx of the full-res grid).
-__device__ __forceinline__ uint4 load_input8(const ConvArgs& a, int64_t q, int qy, int qx, int c0) {
+// convolution input at pixel (n, qy, qx) = flat index q of the full-res grid.
+__device__ __forceinline__ uint4 load_input8(const ConvArgs& a, int q, int n, int qy, int qx, int c0) {
     if (c0 < a.c0) {
         if (a.up0) {   // nearest 2x upsample of a half-resolution source
-            const int64_t n = q / (static_cast<int64_t>(a.g.h) * a.g.w);
-            const int64_t lq = (n * (a.g.h / 2) + qy / 2) * (a.g.w / 2) + qx / 2;
-            return *reinterpret_cast<const uint4*>(a.x0 + lq * a.c0s + c0);
+            const int lq = (n * (a.g.h >> 1) + (qy >> 1)) * (a.g.w >> 1) + (qx >> 1);
+            return *reinterpret_cast<const uint4*>(a.x0 + static_cast<int64_t>(lq) * a.c0s + c0);
         }
-        return *reinterpret_cast<const uint4*>(a.x0 + q * a.c0s + c0);
+        return *reinterpret_cast<const uint4*>(a.x0 + static_cast<int64_t>(q) * a.c0s + c0);
     }
-    if (c0 - a.c0 < a.c1) return *reinterpret_cast<const uint4*>(a.x1 + q * a.c1s + (c0 - a.c0));
+    if (c0 - a.c0 < a.c1)
+        return *reinterpret_cast<const uint4*>(a.x1 + static_cast<int64_t>(q) * a.c1s + (c0 - a.c0));
     return make_uint4(0, 0, 0, 0);
 }
 
@@ -104,35 +109,39 @@ struct Smem {
     uint32_t tmem;
 };
 
+constexpr int kRowsPerThread = (kBM * 8) / kThreads;   // 8
+
 // Fills stage buffers for K chunk kc. A: kBM rows; B: bn rows.
+// Forward / data gradient: thread t always fills the rows
+// m = (2 it + t/64) * 8 + t%8 (it = 0..7) at vector t/8 % 8 of the chunk, so
+// their pixel coordinates (rows[]) are computed once per tile. Weight
+// gradient: px[] holds the coordinates of the chunk's 64 pixels.
 template <int kMode>
-__device__ __forceinline__ void gather(const ConvArgs& a, int64_t mtile, int ntile, int kc, uint8_t* sa, uint8_t* sb,
-                                       int bn) {
+__device__ __forceinline__ void gather(const ConvArgs& a, const Pix (&rows)[kRowsPerThread], const Pix* px, int ntile,
+                                       int kc, int64_t kbase, uint8_t* sa, uint8_t* sb, int bn) {
     const int t = threadIdx.x;
     if constexpr (kMode == kFwd || kMode == kDgrad) {
         // A, K-major: offset(row m, vector kb) = ((m/8)*8 + kb)*128 + (m%8)*16 = L*16
-        const int vec_per_tap = (kMode == kFwd ? a.cin8 : a.cout8) / 8;
-        const int kvec_total = 9 * vec_per_tap;
-#pragma unroll 2
-        for (int it = 0; it < (kBM * 8) / kThreads; ++it) {
-            const int L = it * kThreads + t;
-            const int r = L & 7, kb = (L >> 3) & 7, mb = L >> 6;
-            const int m = mb * 8 + r;
-            const int kv = kc * 8 + kb;
-            const int64_t p = mtile * kBM + m;
-            uint4 v = make_uint4(0, 0, 0, 0);
-            if (p < a.g.npix && kv < kvec_total) {
-                const int tap = kv / vec_per_tap, c0 = (kv % vec_per_tap) * 8;
-                int64_t q;
-                int qy, qx;
-                if (kMode == kFwd) {
-                    if (tap_pixel(a.g, p, tap, 1, q, qy, qx)) v = load_input8(a, q, qy, qx, c0);
-                } else {
-                    if (tap_pixel(a.g, p, tap, -1, q, qy, qx)) v = load_dz8(a, q, c0);
-                }
+        const int vpt = (kMode == kFwd ? a.cin8 : a.cout8) >> 3;
+        const int kv = kc * 8 + ((t >> 3) & 7);
+        const bool kvalid = kv < 9 * vpt;
+        const int tap = kvalid ? kv / vpt : 0;
+        const int c0 = kvalid ? (kv - tap * vpt) * 8 : 0;
+        const int sgn = kMode == kFwd ? 1 : -1;
+        const int ty = sgn * (tap / 3 - 1), tx = sgn * (tap % 3 - 1);
+        uint4 v[kRowsPerThread];
+#pragma unroll
+        for (int it = 0; it < kRowsPerThread; ++it) {
+            v[it] = make_uint4(0, 0, 0, 0);
+            const int qy = rows[it].y + ty, qx = rows[it].x + tx;
+            if (kvalid && rows[it].n >= 0 && qy >= 0 && qy < a.g.h && qx >= 0 && qx < a.g.w) {
+                const int q = (rows[it].n * a.g.h + qy) * a.g.w + qx;
+                if constexpr (kMode == kFwd) v[it] = load_input8(a, q, rows[it].n, qy, qx, c0);
+                else v[it] = load_dz8(a, q, c0);
             }
-            *reinterpret_cast<uint4*>(sa + L * 16) = v;
         }
+#pragma unroll
+        for (int it = 0; it < kRowsPerThread; ++it) *reinterpret_cast<uint4*>(sa + (it * kThreads + t) * 16) = v[it];
         // B, K-major weights: row n, vector kb
         const __nv_bfloat16* wsrc = (kMode == kFwd) ? a.w : a.wt;
         const int kpad = (kMode == kFwd) ? a.k_pad : a.k2_pad;
@@ -144,31 +153,32 @@ __device__ __forceinline__ void gather(const ConvArgs& a, int64_t mtile, int nti
         }
     } else {
         // weight gradient: K = pixels. A (MN-major): row k = pixel, 16 B = 8 output channels.
-        // offset(mn_blk, k_blk) = (k_blk*16 + mn_blk)*128 + (k%8)*16 = L*16
-        const int64_t kbase = mtile * static_cast<int64_t>(kBK);
-#pragma unroll 2
-        for (int it = 0; it < (kBM * 8) / kThreads; ++it) {
-            const int L = it * kThreads + t;
-            const int r = L & 7, mnb = (L >> 3) & 15, kb = L >> 7;
-            const int64_t p = kbase + kb * 8 + r;
-            uint4 v = make_uint4(0, 0, 0, 0);
-            if (p < a.g.npix) v = load_dz8(a, p, mnb * 8);
-            *reinterpret_cast<uint4*>(sa + L * 16) = v;
+        // offset(mn_blk, k_blk) = (k_blk*16 + mn_blk)*128 + (k%8)*16 = L*16; thread t
+        // always loads channels ((t/8) % 16) * 8 of pixel kbase + 8 it + t%8.
+        uint4 v[kRowsPerThread];
+        const int c0a = ((t >> 3) & 15) * 8;
+#pragma unroll
+        for (int it = 0; it < kRowsPerThread; ++it) {
+            const int64_t p = kbase + it * 8 + (t & 7);
+            v[it] = p < a.g.npix ? load_dz8(a, p, c0a) : make_uint4(0, 0, 0, 0);
         }
+#pragma unroll
+        for (int it = 0; it < kRowsPerThread; ++it) *reinterpret_cast<uint4*>(sa + (it * kThreads + t) * 16) = v[it];
         // B (MN-major): row k = pixel, 16 B = 8 consecutive features (tap, ci..ci+7)
         const int nb_count = bn / 8;
         for (int L = t; L < bn * 8; L += kThreads) {
-            const int r = L & 7, nb = (L >> 3) % nb_count, kb = (L >> 3) / nb_count;
-            const int64_t p = kbase + kb * 8 + r;
+            const int k = L >> 3;
+            const int nb = k % nb_count, kb = k / nb_count;
+            const Pix pp = px[kb * 8 + (L & 7)];
             const int f = ntile * a.bn + nb * 8;
-            uint4 v = make_uint4(0, 0, 0, 0);
-            if (p < a.g.npix && f < 9 * a.cin8) {
-                const int tap = f / a.cin8, c0 = f % a.cin8;
-                int64_t q;
-                int qy, qx;
-                if (tap_pixel(a.g, p, tap, 1, q, qy, qx)) v = load_input8(a, q, qy, qx, c0);
+            uint4 w = make_uint4(0, 0, 0, 0);
+            if (pp.n >= 0 && f < 9 * a.cin8) {
+                const int tap = f / a.cin8, c0 = f - tap * a.cin8;
+                const int qy = pp.y + tap / 3 - 1, qx = pp.x + tap % 3 - 1;
+                if (qy >= 0 && qy < a.g.h && qx >= 0 && qx < a.g.w)
+                    w = load_input8(a, (pp.n * a.g.h + qy) * a.g.w + qx, pp.n, qy, qx, c0);
             }
-            *reinterpret_cast<uint4*>(sb + L * 16) = v;
+            *reinterpret_cast<uint4*>(sb + L * 16) = w;
         }
     }
 }
@@ -218,16 +228,26 @@ __global__ void __launch_bounds__(kThreads) k_conv(ConvArgs a, int* err_flag) {
         kchunks = (kMode == kFwd ? a.k_pad : a.k2_pad) / kBK;
     }
     const uint32_t idesc = umma::idesc_bf16(kBM, static_cast<uint32_t>(bn), kMode == kWgrad, kMode == kWgrad);
+    // per-thread pixel rows (forward / data gradient) or the chunk's pixels (weight gradient)
+    Pix rows[kRowsPerThread];
+    __shared__ Pix s_px[kBK];
+    if constexpr (kMode != kWgrad) {
+#pragma unroll
+        for (int it = 0; it < kRowsPerThread; ++it)
+            rows[it] = pix_of(a.g, static_cast<int>(mtile * kBM) + (2 * it + (threadIdx.x >> 6)) * 8 + (threadIdx.x & 7));
+    }
     bool ok = true;
     for (int kc = 0; kc < kchunks && ok; ++kc) {
         const int s = kc % kStages;
         if (kc >= kStages) ok = umma::mbar_wait(&ss.bar[s], ((kc / kStages) - 1) & 1);
+        if constexpr (kMode == kWgrad) {
+            if (threadIdx.x < kBK) s_px[threadIdx.x] = pix_of(a.g, static_cast<int>((wg_first + kc) * kBK) + threadIdx.x);
+        }
         if (!__syncthreads_and(ok)) {
             ok = false;
             break;
         }
-        if constexpr (kMode == kWgrad) gather<kMode>(a, wg_first + kc, ntile, kc, stage_a[s], stage_b[s], bn);
-        else gather<kMode>(a, mtile, ntile, kc, stage_a[s], stage_b[s], bn);
+        gather<kMode>(a, rows, s_px, ntile, kc, (wg_first + kc) * kBK, stage_a[s], stage_b[s], bn);
         umma::fence_async_smem();
         __syncthreads();
         if (threadIdx.x == 0) {

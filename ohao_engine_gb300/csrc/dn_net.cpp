@@ -359,7 +359,7 @@ ohao_status pack_inputs(ohao_dn_ctx* ctx, const float* const* rad, const float* 
 extern "C" {
 
 ohao_status ohao_dn_create(const ohao_dn_desc* desc, ohao_dn_ctx** out) {
-    if (!desc || !out || desc->max_pixels == 0) return OHAO_ERR_INVALID_ARG;
+    if (!desc || !out || desc->max_pixels == 0 || desc->max_pixels >= (1ull << 31)) return OHAO_ERR_INVALID_ARG;
     *out = nullptr;
     int ndev = 0;
     if (cudaGetDeviceCount(&ndev) != cudaSuccess || desc->device < 0 || desc->device >= ndev)
