@@ -40,7 +40,7 @@ UNIT = "Msamples/s"
 def parse():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
-    ap.add_argument("--steps", type=int, default=10)
+    ap.add_argument("--steps", type=int, default=200)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--workload", default="sphere_1m", choices=["sphere_1m", "cornell", "instanced", "studio", "denoise"])
@@ -85,7 +85,7 @@ class ClockSampler:
             os.close(fd)
             self.f = open(self.path, "w")
             self.proc = subprocess.Popen(["nvidia-smi", f"--query-gpu={self.FIELDS}", "--format=csv,noheader,nounits",
-                                          "-i", str(self.dev), "-lms", "200"], stdout=self.f, stderr=subprocess.DEVNULL)
+                                          "-i", str(self.dev), "-lms", "50"], stdout=self.f, stderr=subprocess.DEVNULL)
         except Exception:
             self.proc = None
 
@@ -140,15 +140,17 @@ def cpu_baseline(sd, spp_step, target_s, full_step_samples):
     t0 = time.time()
     orc.render_paths(v, st, 0, spp_step, pixels=pix)
     dt0 = max(time.time() - t0, 1e-3)
-    n1 = int(min(npix, max(n0, n0 * target_s / dt0)))
+    want = n0 * target_s / dt0                      # paths (at spp_step per pixel) for ~target_s
+    n1 = int(min(npix, max(n0, want)))
+    spp = spp_step * max(1, int(round(want / n1)))  # whole frame not enough: more samples per pixel
     pix = np.sort(rng.choice(npix, n1, replace=False)).astype(np.uint32)
     t0 = time.time()
-    orc.render_paths(v, st, 0, spp_step, pixels=pix)
+    orc.render_paths(v, st, 0, spp, pixels=pix)
     dt = time.time() - t0
-    samples = n1 * spp_step
+    samples = n1 * spp
     return {"value": samples / dt / 1e6, "unit": UNIT, "cores": int(pyoracle.lib().orc_num_threads()),
             "kind": "port",
-            "sample": f"{n1} seeded random pixels x {spp_step} spp of the same frame ({samples} paths, "
+            "sample": f"{n1} seeded random pixels x {spp} spp of the same frame ({samples} paths, "
                       f"{dt:.1f} s; host BVH build {build_s:.1f} s excluded); full step = {full_step_samples} paths"}
 
 
@@ -169,8 +171,8 @@ def run_reference(args):
     t0 = time.time()
     orc.render_paths(v, st, 0, spp_step, pixels=pix)
     dt0 = max(time.time() - t0, 1e-3)
-    per_step_s = 3.0
-    n = int(min(npix, max(n0, n0 * per_step_s / dt0)))
+    per_step_s = min(3.0, 60.0 / (args.steps + args.warmup))   # the whole run stays near a minute
+    n = int(min(npix, max(256, n0 * per_step_s / dt0)))
     times = []
     for k in range(args.warmup + args.steps):
         pix = np.sort(rng.choice(npix, n, replace=False)).astype(np.uint32)
