@@ -240,7 +240,10 @@ OHAO_D void xform_dir(const float m[12], V3 d, V3& o) {
 }
 
 // Scene-level closest hit (flat or two-level). tmax <= tmin means no hit.
-template <bool kStats>
+// kLevels: 0 = decided by the scene at run time, 1 = flat BVH only,
+// 2 = two-level only (kernels specialised per scene kind keep the flat
+// traversal at its own register count).
+template <bool kStats, int kLevels = 0>
 OHAO_D Hit scene_closest(const DScene& sc, V3 o, V3 d, float tmin, float tmax, TravCount& cnt, int& err) {
     Hit best;
     best.t = 0.0f; best.u = 0.0f; best.v = 0.0f;
@@ -249,102 +252,258 @@ OHAO_D Hit scene_closest(const DScene& sc, V3 o, V3 d, float tmin, float tmax, T
     uint32_t st_node[kStackSize];
     float st_t[kStackSize];
     const RayPre r = ray_pre(o, d);
-    if (!sc.two_level) {
+    if (kLevels == 1 || (kLevels == 0 && !sc.two_level)) {
         bvh_closest<kStats>(sc.nodes, sc.tris, r, tmin, tmax, best, 0xFFFFFFFFu, st_node, st_t, 0, cnt, err);
         return best;
     }
+    // Two-level: one loop whose every iteration visits one node (TLAS or
+    // BLAS) or enters one instance, so the lanes of a warp stay on the same
+    // code whatever level each ray is in. Order of visits per ray: at a TLAS
+    // node, its hit instance leaves in slot order (each BLAS fully), then the
+    // nearest internal child, then the stack -- the order of a nested
+    // TLAS-then-BLAS traversal, hence the same hits and visit counts.
     int sp = 0;
+    bool in_blas = false;
+    RayPre ra = r;                          // the ray of the current level (object space inside a BLAS)
+    const uint4* bnodes = sc.nodes;
+    const float4* btris = nullptr;
+    uint32_t inst = 0u;
+    int base = 0;                           // stack base of the current BLAS
     uint32_t cur = 0u;
     float cur_tn = -INFINITY;
+    bool have_node = true;
+    bool resume = false;                    // TLAS child to continue with after the pending instances
+    uint32_t res_cur = 0u;
+    float res_tn = 0.0f;
+    uint4 pq = make_uint4(0, 0, 0, 0);      // pending instance leaves: the TLAS node's (child, leaf, meta, meta)
+    uint32_t plm = 0u, pidx = 0u;
     while (true) {
-        const float tb = best.prim != 0xFFFFFFFFu ? best.t : tmax;
-        if (cur_tn <= tb + tb * kTravRelSlack) {
-            const NodeRec n = load_node(sc.nodes, cur);
-            if (kStats) cnt.nodes++;
-            float tn[8];
-            const uint32_t hit = node_test(n, r, tmin, tb, tn);
-            const uint32_t imask = n.q0.w >> 24;
-            uint32_t lm = hit & ~imask;
-            while (lm) {
-                const int i = __ffs(lm) - 1;
-                lm &= lm - 1;
-                const uint32_t meta = byte_of(n.q1.z, n.q1.w, i);
-                const uint32_t c = meta >> 5, off = meta & 31u;
-                for (uint32_t q = 0; q < c; ++q) {
-                    const uint32_t ii = __ldg(sc.tlas_inst + n.q1.y + off + q);
-                    const DInst& in = sc.inst[ii];
-                    const DBlas bl = sc.blas[in.blas];
-                    V3 oo, od;
-                    xform_point(in.w2o, o, oo);
-                    xform_dir(in.w2o, d, od);
-                    const RayPre ro = ray_pre(oo, od);
-                    bvh_closest<kStats>(sc.blas_nodes + static_cast<size_t>(bl.node_off) * 5,
-                                        sc.blas_tris + static_cast<size_t>(bl.tri_off) * 3, ro, tmin, tmax, best, ii,
-                                        st_node, st_t, sp, cnt, err);
-                    if (err) return best;
+        if (have_node) {
+            const float tb = best.prim != 0xFFFFFFFFu ? best.t : tmax;
+            bool desc = false;
+            bool leaves = false;
+            if (cur_tn <= tb + tb * kTravRelSlack) {
+                const NodeRec n = load_node(in_blas ? bnodes : sc.nodes, cur);
+                if (kStats) cnt.nodes++;
+                float tn[8];
+                const uint32_t hit = node_test(n, ra, tmin, tb, tn);
+                const uint32_t imask = n.q0.w >> 24;
+                uint32_t lm = hit & ~imask;
+                if (in_blas) {
+                    while (lm) {
+                        const int i = __ffs(lm) - 1;
+                        lm &= lm - 1;
+                        const uint32_t meta = byte_of(n.q1.z, n.q1.w, i);
+                        const uint32_t c = meta >> 5, off = meta & 31u;
+                        for (uint32_t q = 0; q < c; ++q) {
+                            const float4* tp = btris + static_cast<size_t>(n.q1.y + off + q) * 3;
+                            const float4 v0 = __ldg(tp), v1 = __ldg(tp + 1), v2 = __ldg(tp + 2);
+                            if (kStats) cnt.tris++;
+                            float t, u, v;
+                            if (!tri_intersect(ra, v0, v1, v2, tmin, tmax, t, u, v)) continue;
+                            const uint32_t prim = __float_as_uint(v0.w);
+                            if (best.prim == 0xFFFFFFFFu || t < best.t ||
+                                (t == best.t && key_less(inst, prim, best.inst, best.prim))) {
+                                best.t = t; best.u = u; best.v = v; best.inst = inst; best.prim = prim;
+                            }
+                        }
+                    }
+                } else if (lm) {
+                    pq = n.q1;
+                    plm = lm;
+                    pidx = 0u;
+                    leaves = true;
+                }
+                const uint32_t rem = hit & imask;
+                if (rem) {
+                    if (!order_children(rem, tn, n, st_node, st_t, sp, cur, cur_tn)) { err = 1; return best; }
+                    desc = true;
                 }
             }
-            const uint32_t rem = hit & imask;
-            if (rem) {
-                if (!order_children(rem, tn, n, st_node, st_t, sp, cur, cur_tn)) { err = 1; return best; }
+            if (leaves) {
+                resume = desc;
+                res_cur = cur;
+                res_tn = cur_tn;
+                have_node = false;
+            } else if (!desc) {
+                have_node = false;
+            }
+            if (have_node) continue;
+        }
+        if (in_blas) {
+            if (sp > base) {
+                sp--;
+                cur = st_node[sp];
+                cur_tn = st_t[sp];
+                have_node = true;
                 continue;
             }
+            in_blas = false;
+            ra = r;
+        }
+        if (plm) {   // enter the next pending instance
+            const int i = __ffs(plm) - 1;
+            const uint32_t meta = byte_of(pq.z, pq.w, i);
+            const uint32_t c = meta >> 5, off = meta & 31u;
+            if (pidx >= c) {
+                plm &= plm - 1;
+                pidx = 0u;
+                continue;
+            }
+            const uint32_t ii = __ldg(sc.tlas_inst + pq.y + off + pidx);
+            if (++pidx == c) {
+                plm &= plm - 1;
+                pidx = 0u;
+            }
+            const DInst& in = sc.inst[ii];
+            const DBlas bl = sc.blas[in.blas];
+            V3 oo, od;
+            xform_point(in.w2o, o, oo);
+            xform_dir(in.w2o, d, od);
+            ra = ray_pre(oo, od);
+            bnodes = sc.blas_nodes + static_cast<size_t>(bl.node_off) * 5;
+            btris = sc.blas_tris + static_cast<size_t>(bl.tri_off) * 3;
+            inst = ii;
+            base = sp;
+            if (base >= kStackSize) { err = 1; return best; }
+            cur = 0u;
+            cur_tn = -INFINITY;
+            in_blas = true;
+            have_node = true;
+            continue;
+        }
+        if (resume) {
+            resume = false;
+            cur = res_cur;
+            cur_tn = res_tn;
+            have_node = true;
+            continue;
         }
         if (sp == 0) return best;
         sp--;
         cur = st_node[sp];
         cur_tn = st_t[sp];
+        have_node = true;
     }
 }
 
-template <bool kStats>
+template <bool kStats, int kLevels = 0>
 OHAO_D bool scene_occluded(const DScene& sc, V3 o, V3 d, float tmin, float tmax, TravCount& cnt, int& err) {
     if (!(tmax > tmin) || sc.nnodes == 0) return false;
     uint32_t st_node[kStackSize];
     const RayPre r = ray_pre(o, d);
-    if (!sc.two_level) return bvh_any<kStats>(sc.nodes, sc.tris, r, tmin, tmax, st_node, 0, cnt, err);
+    if (kLevels == 1 || (kLevels == 0 && !sc.two_level))
+        return bvh_any<kStats>(sc.nodes, sc.tris, r, tmin, tmax, st_node, 0, cnt, err);
+    // Two-level, as one loop (see scene_closest): at a TLAS node the internal
+    // children but the last (slot order) are pushed, its instance leaves are
+    // entered in slot order, then the last internal child is visited.
     int sp = 0;
+    bool in_blas = false;
+    RayPre ra = r;
+    const uint4* bnodes = sc.nodes;
+    const float4* btris = nullptr;
+    int base = 0;
     uint32_t cur = 0u;
+    bool have_node = true;
+    bool resume = false;
+    uint32_t res_cur = 0u;
+    uint4 pq = make_uint4(0, 0, 0, 0);
+    uint32_t plm = 0u, pidx = 0u;
     while (true) {
-        const NodeRec n = load_node(sc.nodes, cur);
-        if (kStats) cnt.nodes++;
-        float tn[8];
-        uint32_t m = node_test(n, r, tmin, tmax, tn);
-        const uint32_t imask = n.q0.w >> 24;
-        bool have = false;
-        uint32_t next = 0u;
-        while (m) {
-            const int i = __ffs(m) - 1;
-            m &= m - 1;
-            const uint32_t meta = byte_of(n.q1.z, n.q1.w, i);
-            if ((imask >> i) & 1u) {
-                if (have) {
-                    if (sp >= kStackSize) { err = 1; return false; }
-                    st_node[sp++] = next;
-                }
-                next = n.q1.x + (meta & 7u);
-                have = true;
-                continue;
+        if (have_node) {
+            const NodeRec n = load_node(in_blas ? bnodes : sc.nodes, cur);
+            if (kStats) cnt.nodes++;
+            float tn[8];
+            uint32_t m = node_test(n, ra, tmin, tmax, tn);
+            const uint32_t imask = n.q0.w >> 24;
+            bool have = false;
+            uint32_t next = 0u;
+            if (!in_blas) {
+                plm = m & ~imask;
+                pq = n.q1;
+                pidx = 0u;
+                m &= imask;
             }
-            const uint32_t c = meta >> 5, off = meta & 31u;
-            for (uint32_t q = 0; q < c; ++q) {
-                const uint32_t ii = __ldg(sc.tlas_inst + n.q1.y + off + q);
-                const DInst& in = sc.inst[ii];
-                const DBlas bl = sc.blas[in.blas];
-                V3 oo, od;
-                xform_point(in.w2o, o, oo);
-                xform_dir(in.w2o, d, od);
-                const RayPre ro = ray_pre(oo, od);
-                if (bvh_any<kStats>(sc.blas_nodes + static_cast<size_t>(bl.node_off) * 5,
-                                    sc.blas_tris + static_cast<size_t>(bl.tri_off) * 3, ro, tmin, tmax, st_node, sp, cnt,
-                                    err))
-                    return true;
-                if (err) return false;
+            while (m) {
+                const int i = __ffs(m) - 1;
+                m &= m - 1;
+                const uint32_t meta = byte_of(n.q1.z, n.q1.w, i);
+                if ((imask >> i) & 1u) {
+                    if (have) {
+                        if (sp >= kStackSize) { err = 1; return false; }
+                        st_node[sp++] = next;
+                    }
+                    next = n.q1.x + (meta & 7u);
+                    have = true;
+                    continue;
+                }
+                const uint32_t c = meta >> 5, off = meta & 31u;
+                for (uint32_t q = 0; q < c; ++q) {
+                    const float4* tp = btris + static_cast<size_t>(n.q1.y + off + q) * 3;
+                    const float4 v0 = __ldg(tp), v1 = __ldg(tp + 1), v2 = __ldg(tp + 2);
+                    if (kStats) cnt.tris++;
+                    float t, u, v;
+                    if (tri_intersect(ra, v0, v1, v2, tmin, tmax, t, u, v)) return true;
+                }
+            }
+            if (!in_blas && plm) {
+                resume = have;
+                res_cur = next;
+                have_node = false;
+            } else if (have) {
+                cur = next;
+                continue;
+            } else {
+                have_node = false;
             }
         }
-        if (have) { cur = next; continue; }
+        if (in_blas) {
+            if (sp > base) {
+                cur = st_node[--sp];
+                have_node = true;
+                continue;
+            }
+            in_blas = false;
+            ra = r;
+        }
+        if (plm) {   // enter the next pending instance
+            const int i = __ffs(plm) - 1;
+            const uint32_t meta = byte_of(pq.z, pq.w, i);
+            const uint32_t c = meta >> 5, off = meta & 31u;
+            if (pidx >= c) {
+                plm &= plm - 1;
+                pidx = 0u;
+                continue;
+            }
+            const uint32_t ii = __ldg(sc.tlas_inst + pq.y + off + pidx);
+            if (++pidx == c) {
+                plm &= plm - 1;
+                pidx = 0u;
+            }
+            const DInst& in = sc.inst[ii];
+            const DBlas bl = sc.blas[in.blas];
+            V3 oo, od;
+            xform_point(in.w2o, o, oo);
+            xform_dir(in.w2o, d, od);
+            ra = ray_pre(oo, od);
+            bnodes = sc.blas_nodes + static_cast<size_t>(bl.node_off) * 5;
+            btris = sc.blas_tris + static_cast<size_t>(bl.tri_off) * 3;
+            base = sp;
+            if (base >= kStackSize) { err = 1; return false; }
+            cur = 0u;
+            in_blas = true;
+            have_node = true;
+            continue;
+        }
+        if (resume) {
+            resume = false;
+            cur = res_cur;
+            have_node = true;
+            continue;
+        }
         if (sp == 0) return false;
         cur = st_node[--sp];
+        have_node = true;
     }
 }
 

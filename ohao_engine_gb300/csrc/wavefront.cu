@@ -152,7 +152,8 @@ __global__ void k_generate(ViewParams vp, PathParams pp, uint32_t w0, uint32_t n
 }
 
 // stats (profiling only): [0] rays, [1] nodes, [2] triangles
-template <bool kStats>
+// kLevels: 1 = flat BVH, 2 = two-level (one kernel per scene kind).
+template <bool kStats, int kLevels>
 __global__ void __launch_bounds__(128) k_extend(DScene sc, Soa s, int cur, int* err, unsigned long long* stats) {
     const uint32_t count = s.counts[cur];
     const uint32_t* q = s.q_ray[cur];
@@ -162,7 +163,7 @@ __global__ void __launch_bounds__(128) k_extend(DScene sc, Soa s, int cur, int* 
     for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < count; i += gridDim.x * blockDim.x) {
         const uint32_t p = q[i];
         const float4 ro = s.ro[p], rd = s.rd[p];
-        const Hit h = scene_closest<kStats>(sc, ld3(ro), ld3(rd), 0.001f, 10000.0f, tc, e);
+        const Hit h = scene_closest<kStats, kLevels>(sc, ld3(ro), ld3(rd), 0.001f, 10000.0f, tc, e);
         s.hit[p] = make_float4(h.t, h.u, h.v, __uint_as_float(h.prim));
         s.hit_inst[p] = h.inst;
         nr++;
@@ -360,7 +361,7 @@ __global__ void __launch_bounds__(128) k_regen(PathParams pp, const LaunchBlock*
 }
 
 // stats (profiling only): [3] shadow rays, [4] nodes, [5] triangles
-template <bool kStats>
+template <bool kStats, int kLevels>
 __global__ void __launch_bounds__(128) k_shadow(DScene sc, Soa s, int* err, unsigned long long* stats) {
     const uint32_t count = s.counts[2];
     int e = 0;
@@ -374,12 +375,12 @@ __global__ void __launch_bounds__(128) k_shadow(DScene sc, Soa s, int* err, unsi
         if (f & kFlagShL) {
             const float4 d = s.shL[p];
             nr++;
-            if (!scene_occluded<kStats>(sc, org, ld3(d), 0.001f, d.w, tc, e)) rad = rad + ld3(s.shLc[p]);
+            if (!scene_occluded<kStats, kLevels>(sc, org, ld3(d), 0.001f, d.w, tc, e)) rad = rad + ld3(s.shLc[p]);
         }
         if (f & kFlagShE) {
             const float4 d = s.shE[p];
             nr++;
-            if (!scene_occluded<kStats>(sc, org, ld3(d), 0.001f, d.w, tc, e)) rad = rad + ld3(s.shEc[p]);
+            if (!scene_occluded<kStats, kLevels>(sc, org, ld3(d), 0.001f, d.w, tc, e)) rad = rad + ld3(s.shEc[p]);
         }
         s.rad[p] = f4(rad, 0.0f);
         s.flags[p] = f & ~(kFlagShL | kFlagShE);
@@ -501,7 +502,8 @@ Soa carve_soa(void* base, uint32_t cap) {
 }
 
 int g_num_sms = 0;
-int g_blocks_extend = 0, g_blocks_shade = 0, g_blocks_shadow = 0, g_blocks_trace = 0;
+int g_blocks_extend[2] = {0, 0}, g_blocks_shadow[2] = {0, 0};   // [flat, two-level]
+int g_blocks_shade = 0, g_blocks_trace = 0;
 
 void init_launch_shapes() {
     if (g_num_sms) return;
@@ -510,14 +512,40 @@ void init_launch_shapes() {
     cudaDeviceGetAttribute(&g_num_sms, cudaDevAttrMultiProcessorCount, dev);
     if (g_num_sms <= 0) g_num_sms = 152;
     int b = 0;
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, k_extend<false>, 128, 0);
-    g_blocks_extend = std::max(1, b) * g_num_sms;
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, k_extend<false, 1>, 128, 0);
+    g_blocks_extend[0] = std::max(1, b) * g_num_sms;
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, k_extend<false, 2>, 128, 0);
+    g_blocks_extend[1] = std::max(1, b) * g_num_sms;
     cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, k_shade<false>, 128, 0);
     g_blocks_shade = std::max(1, b) * g_num_sms;
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, k_shadow<false>, 128, 0);
-    g_blocks_shadow = std::max(1, b) * g_num_sms;
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, k_shadow<false, 1>, 128, 0);
+    g_blocks_shadow[0] = std::max(1, b) * g_num_sms;
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, k_shadow<false, 2>, 128, 0);
+    g_blocks_shadow[1] = std::max(1, b) * g_num_sms;
     cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, k_trace, 128, 0);
     g_blocks_trace = std::max(1, b) * g_num_sms;
+}
+
+// closest-hit / any-hit kernels specialised for the scene kind
+void launch_extend(const DScene& sc, const Soa& s, int cur, int* d_err, unsigned long long* stats, cudaStream_t st) {
+    const int two = sc.two_level ? 1 : 0;
+    if (stats) {
+        if (two) k_extend<true, 2><<<g_blocks_extend[1], 128, 0, st>>>(sc, s, cur, d_err, stats);
+        else k_extend<true, 1><<<g_blocks_extend[0], 128, 0, st>>>(sc, s, cur, d_err, stats);
+    } else {
+        if (two) k_extend<false, 2><<<g_blocks_extend[1], 128, 0, st>>>(sc, s, cur, d_err, nullptr);
+        else k_extend<false, 1><<<g_blocks_extend[0], 128, 0, st>>>(sc, s, cur, d_err, nullptr);
+    }
+}
+void launch_shadow(const DScene& sc, const Soa& s, int* d_err, unsigned long long* stats, cudaStream_t st) {
+    const int two = sc.two_level ? 1 : 0;
+    if (stats) {
+        if (two) k_shadow<true, 2><<<g_blocks_shadow[1], 128, 0, st>>>(sc, s, d_err, stats);
+        else k_shadow<true, 1><<<g_blocks_shadow[0], 128, 0, st>>>(sc, s, d_err, stats);
+    } else {
+        if (two) k_shadow<false, 2><<<g_blocks_shadow[1], 128, 0, st>>>(sc, s, d_err, nullptr);
+        else k_shadow<false, 1><<<g_blocks_shadow[0], 128, 0, st>>>(sc, s, d_err, nullptr);
+    }
 }
 
 struct EvTimer {
@@ -597,8 +625,7 @@ ohao_status wavefront_render(const DScene& sc, const RenderView& view, const Pat
         int cur = 0;
         for (uint32_t it = 0; it < niters; ++it) {
             tm.begin(0, a);
-            if (profile) k_extend<true><<<g_blocks_extend, 128, 0, st>>>(sc, s, cur, d_err, dstats);
-            else k_extend<false><<<g_blocks_extend, 128, 0, st>>>(sc, s, cur, d_err, nullptr);
+            launch_extend(sc, s, cur, d_err, profile ? dstats : nullptr, st);
             tm.end(0, a);
             cudaMemsetAsync(s.counts + (cur ^ 1), 0, 4, st);
             cudaMemsetAsync(s.counts + 2, 0, 4, st);
@@ -607,8 +634,7 @@ ohao_status wavefront_render(const DScene& sc, const RenderView& view, const Pat
                                                            view.aov, spp - 1, nullptr);
             tm.end(1, a);
             tm.begin(2, a);
-            if (profile) k_shadow<true><<<g_blocks_shadow, 128, 0, st>>>(sc, s, d_err, dstats);
-            else k_shadow<false><<<g_blocks_shadow, 128, 0, st>>>(sc, s, d_err, nullptr);
+            launch_shadow(sc, s, d_err, profile ? dstats : nullptr, st);
             tm.end(2, a);
             cur ^= 1;
         }
@@ -779,11 +805,11 @@ void enqueue_chunk(const DScene& sc, const PathParams& pp, const LaunchBlock* lb
             rsort::sort_pairs(s.skA, s.svA, s.skB, s.svB, s.shist, s.counts + cur, cap, 24, st);
             k_copy_queue<<<g_blocks_shade, 128, 0, st>>>(s, cur);
         }
-        k_extend<false><<<g_blocks_extend, 128, 0, st>>>(sc, s, cur, d_err, nullptr);
+        launch_extend(sc, s, cur, d_err, nullptr, st);
         cudaMemsetAsync(s.counts + (cur ^ 1), 0, 4, st);
         cudaMemsetAsync(s.counts + 2, 0, 8, st);   // shadow and done counts
         k_shade<true><<<g_blocks_shade, 128, 0, st>>>(sc, pp, ViewParams{}, 0u, 1u, s, cur, nullptr, 0u, lb);
-        k_shadow<false><<<g_blocks_shadow, 128, 0, st>>>(sc, s, d_err, nullptr);
+        launch_shadow(sc, s, d_err, nullptr, st);
     }
 }
 
