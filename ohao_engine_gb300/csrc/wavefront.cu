@@ -265,9 +265,11 @@ __global__ void k_ray_keys(const LaunchBlock* lb, Soa s, int cur) {
         const uint32_t p = q[i];
         const float4 o = s.ro[p], d = s.rd[p];
         const uint32_t oct = (d.x < 0.0f ? 4u : 0u) | (d.y < 0.0f ? 2u : 0u) | (d.z < 0.0f ? 1u : 0u);
-        const float fx = (o.x - lb->box_lo[0]) * lb->box_scale[0];
-        const float fy = (o.y - lb->box_lo[1]) * lb->box_scale[1];
-        const float fz = (o.z - lb->box_lo[2]) * lb->box_scale[2];
+        // a point 1/8 of the scene box along the ray: groups primary rays of
+        // one camera by image region and secondary rays by origin and direction
+        const float fx = (o.x - lb->box_lo[0]) * lb->box_scale[0] + d.x * 16.0f;
+        const float fy = (o.y - lb->box_lo[1]) * lb->box_scale[1] + d.y * 16.0f;
+        const float fz = (o.z - lb->box_lo[2]) * lb->box_scale[2] + d.z * 16.0f;
         const uint32_t ix = static_cast<uint32_t>(fminf(fmaxf(fx, 0.0f), 127.0f));
         const uint32_t iy = static_cast<uint32_t>(fminf(fmaxf(fy, 0.0f), 127.0f));
         const uint32_t iz = static_cast<uint32_t>(fminf(fmaxf(fz, 0.0f), 127.0f));
