@@ -197,6 +197,12 @@ ohao_status ohao_pt_autotune(ohao_pt_ctx* ctx, const ohao_pt_view* views, uint32
                              const ohao_pt_settings* settings, float* best_ms, ohao_stream stream);
 /* Name of the persistent launch shape in use ("default" before autotune). */
 const char* ohao_pt_launch_config(const ohao_pt_ctx* ctx);
+/* Name of compiled launch shape `index` (NULL past the last), and selection
+ * of one by name for later renders of this context (OHAO_ERR_INVALID_ARG for
+ * an unknown name). All shapes give bit-identical images. No counterpart in
+ * the reference. */
+const char* ohao_pt_launch_config_at(uint32_t index);
+ohao_status ohao_pt_set_launch_config(ohao_pt_ctx* ctx, const char* name);
 
 /* ---- Gradients (path replay) ----
  * Replace the inverse lab's coordinate finite differences over the tile

@@ -39,7 +39,8 @@ EXPORTED_SYMBOLS = [
     "ohao_pt_set_materials", "ohao_pt_update_materials", "ohao_pt_set_lights", "ohao_pt_set_env",
     "ohao_pt_set_albedo_map", "ohao_env_cdf_build", "ohao_pt_render", "ohao_pt_render_host",
     "ohao_pt_get_profile", "ohao_pt_trace", "ohao_pt_bvh_info", "ohao_pt_bvh_download", "ohao_bvh_build_noalloc",
-    "ohao_pt_autotune", "ohao_pt_launch_config", "ohao_pt_backward", "ohao_pt_adjoint",
+    "ohao_pt_autotune", "ohao_pt_launch_config", "ohao_pt_launch_config_at", "ohao_pt_set_launch_config",
+    "ohao_pt_backward", "ohao_pt_adjoint",
 ]
 
 
@@ -114,6 +115,8 @@ def load_library(path: str | None = None):
         "ohao_bvh_build_noalloc": ([vp, u32, vp, vp, vp, C.POINTER(u32), C.POINTER(u32), vp], i32),
         "ohao_pt_autotune": ([vp, C.POINTER(View), u32, C.POINTER(Settings), C.POINTER(f32), vp], i32),
         "ohao_pt_launch_config": ([vp], C.c_char_p),
+        "ohao_pt_launch_config_at": ([u32], C.c_char_p),
+        "ohao_pt_set_launch_config": ([vp, C.c_char_p], i32),
         "ohao_pt_backward": ([vp, C.POINTER(View), u32, C.POINTER(Settings), C.POINTER(vp), vp, vp, vp], i32),
         "ohao_pt_adjoint": ([vp, C.POINTER(View), u32, C.POINTER(Settings), C.POINTER(vp), vp, vp,
                                    C.POINTER(f32), vp], i32),
@@ -328,6 +331,20 @@ class PathTracer:
     @property
     def launch_config(self) -> str:
         return self._L.ohao_pt_launch_config(self.h).decode()
+
+    @launch_config.setter
+    def launch_config(self, name: str) -> None:
+        self._ck(self._L.ohao_pt_set_launch_config(self.h, name.encode()), "set_launch_config")
+
+    def launch_configs(self) -> list:
+        """Names of the compiled persistent launch shapes."""
+        out, i = [], 0
+        while True:
+            n = self._L.ohao_pt_launch_config_at(i)
+            if n is None:
+                return out
+            out.append(n.decode())
+            i += 1
 
     def profile(self) -> Profile:
         p = Profile()

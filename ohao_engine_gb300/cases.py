@@ -4,6 +4,8 @@ profiler captures (one process, one GPU, a few GB at most):
     python -m ohao_engine_gb300.cases denoise_infer   # U-Net inference at 1920x1080 (13 calls)
     python -m ohao_engine_gb300.cases adjoint         # ohao_pt_adjoint, studio scene, 1 view 256^2, 4 spp (2 calls)
     python -m ohao_engine_gb300.cases instanced_view  # one 512^2 view of the instanced scene, 4 spp (3 calls)
+    python -m ohao_engine_gb300.cases instanced_pool [launch shape]
+                                              # 4 views 384^2 of the instanced scene, persistent pool (2 calls)
 
 Each prints one line with its CUDA-event time per call.
 """
@@ -72,7 +74,22 @@ def instanced_view():
     print(f"instanced one 512^2 view x 4 spp: {ms:.3f} ms per call")
 
 
-CASES = {"denoise_infer": denoise_infer, "adjoint": adjoint, "instanced_view": instanced_view}
+def instanced_pool():
+    import torch
+    import ohao_engine_gb300 as og
+    from . import scenes
+    sd = scenes.instanced(n_views=4, side_range=(384, 384))
+    pt = og.PathTracer()
+    pt.load_scene(sd)
+    pt.launch_config = sys.argv[2] if len(sys.argv) > 2 else "pool_2M_unsorted_fetch4_chunk8"
+    accs = [torch.zeros((v.width * v.height, 4), device="cuda") for v in sd.views]
+    s = og.make_settings(spp=4, max_bounces=4, mode=og.MODE_PERSISTENT)
+    ms = _timed(lambda: pt.render([og.make_view(v, accum=a) for v, a in zip(sd.views, accs)], s), 2)
+    print(f"instanced 4 views 384^2 x 4 spp, {pt.launch_config}: {ms:.3f} ms per call")
+
+
+CASES = {"denoise_infer": denoise_infer, "adjoint": adjoint, "instanced_view": instanced_view,
+         "instanced_pool": instanced_pool}
 
 if __name__ == "__main__":
     import ohao_engine_gb300 as og

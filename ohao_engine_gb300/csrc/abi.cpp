@@ -659,6 +659,17 @@ const char* ohao_pt_launch_config(const ohao_pt_ctx* ctx) {
     return ctx && ctx->persistent ? ohao::persistent_variant_name(ctx->persistent) : "default";
 }
 
+const char* ohao_pt_launch_config_at(uint32_t index) { return ohao::persistent_variant_at(index); }
+
+ohao_status ohao_pt_set_launch_config(ohao_pt_ctx* ctx, const char* name) {
+    if (!ctx || !name) return OHAO_ERR_INVALID_ARG;
+    ohao_status s = ensure_persistent(ctx);
+    if (s != OHAO_OK) return s;
+    if (!ohao::persistent_select(ctx->persistent, name))
+        return fail(ctx, OHAO_ERR_INVALID_ARG, std::string("set_launch_config: unknown launch shape ") + name);
+    return OHAO_OK;
+}
+
 ohao_status ohao_pt_render(ohao_pt_ctx* ctx, const ohao_pt_view* views, uint32_t n_views,
                            const ohao_pt_settings* st, ohao_stream stream) {
     ohao_status s = validate_render(ctx, views, n_views, st);

@@ -191,7 +191,6 @@ __device__ D4 spec_pdf(const PathParams& pp, const LocalMat& lm, V3 N, V3 inDir,
 
 // Light NEE and env NEE at a vertex (primal draws and visibility, dual
 // values), without throughput.
-template <int kLv>
 __device__ D3 nee_d(const DScene& sc, const PathParams& pp, Rng& rng, uint32_t& dim, const Surf& s, V3 inDir,
                     const LocalMat& lm, bool bounce0, int& err) {
     D3 g = d3c(v3s(0.0f));
@@ -199,14 +198,14 @@ __device__ D3 nee_d(const DScene& sc, const PathParams& pp, Rng& rng, uint32_t& 
     const V3 org = s.pos + s.N * 0.01f;
     if (sc.nlights > 0) {
         const LightSample ls = sample_light(sc, rng, dim, s.pos, s.N);
-        if (ls.valid && !scene_occluded<false, kLv>(sc, org, ls.L, 0.001f, ls.shadowDist, tc, err)) {
+        if (ls.valid && !scene_occluded<false>(sc, org, ls.L, 0.001f, ls.shadowDist, tc, err)) {
             const BrdfD b = brdf_d(pp, lm, s.N, inDir, ls.L, ls.NdotL, bounce0, 3.14159f, 3.14159f);
             g = g + dmul(b.f, ls.Le) * (ls.NdotL * ls.weight * ls.n);
         }
     }
     if (sc.has_cdf) {
         const EnvSample es = sample_env_nee(sc, pp, rng, dim, s.N);
-        if (es.valid && !scene_occluded<false, kLv>(sc, org, es.dir, 0.001f, 10000.0f, tc, err)) {
+        if (es.valid && !scene_occluded<false>(sc, org, es.dir, 0.001f, 10000.0f, tc, err)) {
             const BrdfD b = brdf_d(pp, lm, s.N, inDir, es.dir, es.NdotL, bounce0, kPI, kPI);
             const D4 sp = spec_prob(lm, inDir, s.N);
             const D4 pdfS = (b.D * b.NdotH) * (1.0f / (4.0f * b.VdotH + 1e-4f));
@@ -336,7 +335,6 @@ struct ChainOut {
 // divisor is the survival probability (p_j <= 1), plus the rank-one term of
 // p_j = maxc(T_j) when p_j > 1 (the divisor is then a value, not a
 // probability).
-template <int kLv>
 __device__ ChainOut replay_chain(const DScene& sc, const PathParams& pp, Rng& rng, uint32_t& dim, bool specChain, V3 ro,
                                  V3 rd, V3 thr, D4 lastPdf, bool lastDelta, const float delta[3], float* prev_dl,
                                  VRec* rec, const Sink& sk, int& err) {
@@ -344,7 +342,7 @@ __device__ ChainOut replay_chain(const DScene& sc, const PathParams& pp, Rng& rn
     float* last_dl = prev_dl;
     for (uint32_t bounce = 1; bounce <= pp.max_bounces && nrec < kMaxRec; ++bounce) {
         TravCount tc{0, 0};
-        const Hit h = scene_closest<false, kLv>(sc, ro, rd, 0.001f, 10000.0f, tc, err);
+        const Hit h = scene_closest<false>(sc, ro, rd, 0.001f, 10000.0f, tc, err);
         VRec& R = rec[nrec];
         R.T[0] = thr.x; R.T[1] = thr.y; R.T[2] = thr.z;
         R.has_a = 0;
@@ -369,7 +367,7 @@ __device__ ChainOut replay_chain(const DScene& sc, const PathParams& pp, Rng& rn
         LocalMat lm;
         local_mat(sc, s, lm, R.pv);
         D3 G = d3c(length(s.color) > 0.001f ? s.color : v3s(0.0f));
-        G = G + nee_d<kLv>(sc, pp, rng, dim, s, rd, lm, false, err);
+        G = G + nee_d(sc, pp, rng, dim, s, rd, lm, false, err);
         add_dl(R.dl, delta, R.T, G);
         R.G[0] = G.x.v; R.G[1] = G.y.v; R.G[2] = G.z.v;
         nrec++;
@@ -506,7 +504,7 @@ struct AdjView {
 };
 
 // One thread per path (global pixel, sample), grid-stride.
-template <bool kSharedMap, int kLv>
+template <bool kSharedMap>
 __global__ void __launch_bounds__(128) k_adjoint(DScene sc, AdjParams ap, const AdjView* __restrict__ views,
                                                  float* __restrict__ grad_map, float* __restrict__ grad_rough,
                                                  int* err_flag) {
@@ -543,7 +541,7 @@ __global__ void __launch_bounds__(128) k_adjoint(DScene sc, AdjParams ap, const 
         Rng rng = make_rng(pp, px, py, sidx, ps.rng);
         uint32_t dim = ps.dim;
         TravCount tc{0, 0};
-        const Hit h = scene_closest<false, kLv>(sc, ps.ro, ps.rd, 0.001f, 10000.0f, tc, err);
+        const Hit h = scene_closest<false>(sc, ps.ro, ps.rd, 0.001f, 10000.0f, tc, err);
         if (h.prim == 0xFFFFFFFFu) continue;   // primary miss: no parameter dependence
         Surf s0;
         hit_shade(sc, ps.ro, ps.rd, h, s0);
@@ -554,14 +552,14 @@ __global__ void __launch_bounds__(128) k_adjoint(DScene sc, AdjParams ap, const 
         const float one[3] = {1.0f, 1.0f, 1.0f};
         float dl0[4] = {0.f, 0.f, 0.f, 0.f};
         // stage A: light NEE and env NEE at throughput 1
-        add_dl(dl0, delta, one, nee_d<kLv>(sc, pp, rng, dim, s0, rayDir, m0, true, err));
+        add_dl(dl0, delta, one, nee_d(sc, pp, rng, dim, s0, rayDir, m0, true, err));
         // stage B: specular chain from vertex 0
         float js0;
         const V3 sd = spec_dir_score(rng, dim, rayDir, s0.N, s0.rough, js0);
         const D3 tB = dvmix(d3c(v3s(1.0f)), m0.alb, s0.metal);
         const bool deltaB = s0.rough < 0.05f;
         const D4 pdfB = deltaB ? dc(1.0f) : spec_pdf(pp, m0, s0.N, rayDir, sd, true);
-        const ChainOut cb = replay_chain<kLv>(sc, pp, rng, dim, true, s0.pos + s0.N * 0.01f, sd,
+        const ChainOut cb = replay_chain(sc, pp, rng, dim, true, s0.pos + s0.N * 0.01f, sd,
                                          vmix(v3s(1.0f), s0.albedo, s0.metal), pdfB, deltaB, delta, dl0, rec, sk, err);
         add_lam(dl0, cb.lam, tB);
         if (p0.flags & 2u) dl0[3] += cb.value * js0;
@@ -570,7 +568,7 @@ __global__ void __launch_bounds__(128) k_adjoint(DScene sc, AdjParams ap, const 
         dim += 2;
         const V3 dd = cos_hemi(s0.N, d0, d1);
         const D4 pdfC = dc(gmaxf(dot(dd, s0.N), 0.0f) / kPI);
-        const ChainOut cc = replay_chain<kLv>(sc, pp, rng, dim, false, s0.pos + s0.N * 0.01f, dd, s0.albedo, pdfC, false,
+        const ChainOut cc = replay_chain(sc, pp, rng, dim, false, s0.pos + s0.N * 0.01f, dd, s0.albedo, pdfC, false,
                                          delta, dl0, rec, sk, err);
         add_lam(dl0, cc.lam, m0.alb);
         scatter(sk, p0, dl0);
@@ -677,22 +675,18 @@ ohao_status adjoint_backward(const DScene& sc, const RenderView* views, const fl
     const size_t smem_shared = kSharedRough * sizeof(float) + map_n * sizeof(float);
     const bool shared_map = map_n > 0 && smem_shared <= 96 * 1024;
     const uint64_t paths = total * spp;
-    const unsigned grid = static_cast<unsigned>(
-        std::max<uint64_t>(1, std::min<uint64_t>((paths + 127) / 128, static_cast<uint64_t>(sms) * 4)));
-    // specialised per scene kind (flat BVH or two-level) and map placement
+    // One traversal for both scene kinds (decided per ray at run time): the
+    // scene-kind-specialised kernels measured slower, their larger inlined
+    // code costing more in instruction fetch than the branch saves. Grid:
+    // 32 blocks per SM over a grid-stride path loop, enough small blocks for
+    // the uneven path lengths to balance across SMs.
     float* gm = map_n ? grad_map : nullptr;
-    const size_t smem_small = kSharedRough * sizeof(float);
-    if (shared_map && !sc.two_level) {
-        cudaFuncSetAttribute(k_adjoint<true, 1>, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(smem_shared));
-        k_adjoint<true, 1><<<grid, 128, smem_shared, st>>>(sc, ap, dviews, grad_map, grad_rough, d_err);
-    } else if (shared_map) {
-        cudaFuncSetAttribute(k_adjoint<true, 2>, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(smem_shared));
-        k_adjoint<true, 2><<<grid, 128, smem_shared, st>>>(sc, ap, dviews, grad_map, grad_rough, d_err);
-    } else if (!sc.two_level) {
-        k_adjoint<false, 1><<<grid, 128, smem_small, st>>>(sc, ap, dviews, gm, grad_rough, d_err);
-    } else {
-        k_adjoint<false, 2><<<grid, 128, smem_small, st>>>(sc, ap, dviews, gm, grad_rough, d_err);
-    }
+    auto fn = shared_map ? k_adjoint<true> : k_adjoint<false>;
+    const size_t smem = shared_map ? smem_shared : kSharedRough * sizeof(float);
+    if (shared_map) cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(smem));
+    const unsigned grid = static_cast<unsigned>(
+        std::max<uint64_t>(1, std::min<uint64_t>((paths + 127) / 128, static_cast<uint64_t>(sms) * 32)));
+    fn<<<grid, 128, smem, st>>>(sc, ap, dviews, gm, grad_rough, d_err);
     const cudaError_t e = cudaStreamSynchronize(st);   // also keeps hv alive until the copy has read it
     if (e != cudaSuccess) {
         err = std::string("backward: ") + cudaGetErrorString(e);

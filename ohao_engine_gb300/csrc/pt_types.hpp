@@ -97,6 +97,8 @@ PersistentState* persistent_create();
 void persistent_destroy(PersistentState* s);
 uint32_t persistent_max_views();
 const char* persistent_variant_name(const PersistentState* s);
+const char* persistent_variant_at(uint32_t i);                        // nullptr past the last
+bool persistent_select(PersistentState* s, const char* name);         // false: unknown name
 // scene_box: 6 floats (lo.xyz, hi.xyz) bounding the scene, for ray reordering
 ohao_status persistent_render(PersistentState* s, const DScene& sc, const RenderView* views, uint32_t n,
                               const PathParams& pp, uint32_t spp, const float* scene_box, cudaStream_t st, int* d_err,

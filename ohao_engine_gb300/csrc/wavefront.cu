@@ -14,6 +14,7 @@
 // Every kernel is a grid-stride loop over a device-side count, so the launch
 // sequence is fixed and does not read counts back to the host.
 #include "pt_path.cuh"
+#include "pt_fetch.cuh"
 #include "radix_sort.cuh"
 
 #include <algorithm>
@@ -395,6 +396,123 @@ __global__ void __launch_bounds__(128) k_shadow(DScene sc, Soa s, int* err, unsi
     }
 }
 
+// Pool extend / shadow for two-level scenes with persistent warps. A lane
+// whose ray finished takes the next one from the queue while the other lanes
+// carry on: once at least `refill` lanes of a warp are idle, one atomic on the
+// queue's fetch counter claims rays for all of them. A warp therefore does
+// not wait for its longest ray before taking more work -- in instanced scenes
+// per-ray step counts vary by orders of magnitude. Results equal those of
+// k_extend / k_shadow (see pt_fetch.cuh); the shadow rays of one path run in
+// one lane, light ray first, so their contributions add in the same order.
+constexpr int kCtrExtendFetch = 5, kCtrShadowFetch = 6;   // fetch counters in Soa::counts
+
+struct WarpFetch {
+    bool drained = false;
+    // Claims up to one queue index per idle lane; returns this lane's index
+    // (>= count: none). Call with the whole warp.
+    __device__ __forceinline__ uint32_t claim(bool idle_lane, uint32_t* ctr, uint32_t count, int refill) {
+        const uint32_t idle = __ballot_sync(0xFFFFFFFFu, idle_lane);
+        const uint32_t nidle = __popc(idle);
+        if (drained || static_cast<int>(nidle) < refill) return 0xFFFFFFFFu;
+        const uint32_t lane = threadIdx.x & 31u;
+        uint32_t b = 0u;
+        if (lane == 0u) b = atomicAdd(ctr, nidle);
+        b = __shfl_sync(0xFFFFFFFFu, b, 0);
+        if (b >= count || count - b <= nidle) drained = true;
+        if (!idle_lane) return 0xFFFFFFFFu;
+        const uint32_t i = b + __popc(idle & ((1u << lane) - 1u));
+        return i < count ? i : 0xFFFFFFFFu;
+    }
+};
+
+__global__ void __launch_bounds__(128) k_extend_fetch(DScene sc, Soa s, int cur, int refill, int* err) {
+    const uint32_t count = s.counts[cur];
+    const uint32_t* q = s.q_ray[cur];
+    uint32_t st_node[kStackSize];
+    float st_t[kStackSize];
+    Walk2 w;
+    RayPre r;
+    uint32_t p = 0u;
+    bool active = false;
+    WarpFetch wf;
+    int e = 0;
+    while (true) {
+        const uint32_t i = wf.claim(!active, s.counts + kCtrExtendFetch, count, refill);
+        if (i != 0xFFFFFFFFu) {
+            p = q[i];
+            r = ray_pre(ld3(s.ro[p]), ld3(s.rd[p]));
+            walk2_begin(w, r);
+            active = true;
+        }
+        if (__ballot_sync(0xFFFFFFFFu, active) == 0u) {
+            if (wf.drained) break;
+            continue;
+        }
+        if (active && walk2_step(sc, w, r, 0.001f, 10000.0f, st_node, st_t, e)) {
+            s.hit[p] = make_float4(w.best.t, w.best.u, w.best.v, __uint_as_float(w.best.prim));
+            s.hit_inst[p] = w.best.inst;
+            active = false;
+        }
+    }
+    if (e) atomicOr(err, 1);
+}
+
+// Starts shadow ray `which` (0 light, 1 environment) of path p; a ray with
+// tmax <= tmin is unoccluded without a walk (as in scene_occluded).
+__device__ __forceinline__ void start_shadow(const Soa& s, uint32_t p, int which, Probe2& w, RayPre& r) {
+    const float4 d = which == 0 ? s.shL[p] : s.shE[p];
+    r = ray_pre(ld3(s.sh_org[p]), ld3(d));
+    probe2_begin(w, r);
+    if (!(d.w > 0.001f)) w.have_node = false;   // the next step ends the walk unoccluded
+}
+
+__global__ void __launch_bounds__(128) k_shadow_fetch(DScene sc, Soa s, int refill, int* err) {
+    const uint32_t count = s.counts[2];
+    uint32_t st_node[kStackSize];
+    Probe2 w;
+    RayPre r;
+    float tmax = 0.0f;
+    uint32_t p = 0u, f = 0u;
+    int which = 0;
+    bool visL = false;
+    bool active = false;
+    WarpFetch wf;
+    int e = 0;
+    while (true) {
+        const uint32_t i = wf.claim(!active, s.counts + kCtrShadowFetch, count, refill);
+        if (i != 0xFFFFFFFFu) {
+            p = s.q_sh[i];
+            f = s.flags[p];
+            which = (f & kFlagShL) ? 0 : 1;
+            start_shadow(s, p, which, w, r);
+            tmax = which == 0 ? s.shL[p].w : s.shE[p].w;
+            visL = false;
+            active = true;
+        }
+        if (__ballot_sync(0xFFFFFFFFu, active) == 0u) {
+            if (wf.drained) break;
+            continue;
+        }
+        if (active && probe2_step(sc, w, r, 0.001f, tmax, st_node, e)) {
+            if (which == 0) visL = !w.hit;
+            if (which == 0 && (f & kFlagShE)) {
+                which = 1;
+                start_shadow(s, p, 1, w, r);
+                tmax = s.shE[p].w;
+            } else {
+                const bool visE = which == 1 && !w.hit;
+                V3 rad = ld3(s.rad[p]);
+                if (visL) rad = rad + ld3(s.shLc[p]);
+                if (visE) rad = rad + ld3(s.shEc[p]);
+                s.rad[p] = f4(rad, 0.0f);
+                s.flags[p] = f & ~(kFlagShL | kFlagShE);
+                active = false;
+            }
+        }
+    }
+    if (e) atomicOr(err, 1);
+}
+
 __global__ void k_finalize(PathParams pp, uint32_t w0, uint32_t n, uint32_t npix, Soa s, float* accum,
                            uint32_t history, float* path_out) {
     for (uint32_t p = blockIdx.x * blockDim.x + threadIdx.x; p < npix; p += gridDim.x * blockDim.x) {
@@ -506,6 +624,7 @@ Soa carve_soa(void* base, uint32_t cap) {
 int g_num_sms = 0;
 int g_blocks_extend[2] = {0, 0}, g_blocks_shadow[2] = {0, 0};   // [flat, two-level]
 int g_blocks_shade = 0, g_blocks_trace = 0;
+int g_blocks_fetch[2] = {0, 0};   // persistent-warp extend, shadow: one full residency
 
 void init_launch_shapes() {
     if (g_num_sms) return;
@@ -526,6 +645,10 @@ void init_launch_shapes() {
     g_blocks_shadow[1] = std::max(1, b) * g_num_sms;
     cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, k_trace, 128, 0);
     g_blocks_trace = std::max(1, b) * g_num_sms;
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, k_extend_fetch, 128, 0);
+    g_blocks_fetch[0] = std::max(1, b) * g_num_sms;
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, k_shadow_fetch, 128, 0);
+    g_blocks_fetch[1] = std::max(1, b) * g_num_sms;
 }
 
 // closest-hit / any-hit kernels specialised for the scene kind
@@ -701,12 +824,14 @@ constexpr int kChunk = 8;                       // iterations per graph replay (
 struct PoolVariant {
     uint32_t cap;
     bool reorder;
+    int refill;          // two-level scenes: persistent-warp traversal refilled at >= refill idle lanes (0: off)
     const char* name;
 };
 const PoolVariant kPool[] = {
-    {1u << 20, true, "pool_1M_sorted_chunk8"},  {1u << 21, true, "pool_2M_sorted_chunk8"},
-    {1u << 22, true, "pool_4M_sorted_chunk8"},  {1u << 21, false, "pool_2M_unsorted_chunk8"},
-    {1u << 22, false, "pool_4M_unsorted_chunk8"},
+    {1u << 20, true, 0, "pool_1M_sorted_chunk8"},          {1u << 21, true, 0, "pool_2M_sorted_chunk8"},
+    {1u << 22, true, 0, "pool_4M_sorted_chunk8"},          {1u << 21, false, 0, "pool_2M_unsorted_chunk8"},
+    {1u << 22, false, 0, "pool_4M_unsorted_chunk8"},       {1u << 21, true, 4, "pool_2M_sorted_fetch4_chunk8"},
+    {1u << 22, false, 4, "pool_4M_unsorted_fetch4_chunk8"}, {1u << 22, false, 8, "pool_4M_unsorted_fetch8_chunk8"},
 };
 constexpr int kNumPool = sizeof(kPool) / sizeof(kPool[0]);
 constexpr int kDefaultPool = 1;
@@ -755,6 +880,18 @@ const char* persistent_variant_name(const PersistentState* s) {
     return s && s->variant >= 0 ? kPool[s->variant].name : "default";
 }
 
+const char* persistent_variant_at(uint32_t i) { return i < static_cast<uint32_t>(kNumPool) ? kPool[i].name : nullptr; }
+
+bool persistent_select(PersistentState* s, const char* name) {
+    for (int v = 0; v < kNumPool; ++v) {
+        if (std::strcmp(kPool[v].name, name) == 0) {
+            s->variant = v;
+            return true;
+        }
+    }
+    return false;
+}
+
 namespace {
 
 ohao_status stage_views(PersistentState* s, const RenderView* views, uint32_t n, uint32_t spp, const float* box,
@@ -798,20 +935,30 @@ ohao_status stage_views(PersistentState* s, const RenderView* views, uint32_t n,
 }
 
 void enqueue_chunk(const DScene& sc, const PathParams& pp, const LaunchBlock* lb, const Soa& s, uint32_t cap,
-                   bool reorder, int* d_err, cudaStream_t st) {
+                   const PoolVariant& pv, int* d_err, cudaStream_t st) {
+    const bool fetch = pv.refill > 0 && sc.two_level && sc.nnodes > 0;
     for (int it = 0; it < kChunk; ++it) {
         const int cur = it & 1;
         k_regen<<<g_blocks_shade, 128, 0, st>>>(pp, lb, s, cur);
-        if (reorder) {
+        if (pv.reorder) {
             k_ray_keys<<<g_blocks_shade, 128, 0, st>>>(lb, s, cur);
             rsort::sort_pairs(s.skA, s.svA, s.skB, s.svB, s.shist, s.counts + cur, cap, 24, st);
             k_copy_queue<<<g_blocks_shade, 128, 0, st>>>(s, cur);
         }
-        launch_extend(sc, s, cur, d_err, nullptr, st);
+        if (fetch) {
+            cudaMemsetAsync(s.counts + kCtrExtendFetch, 0, 8, st);   // both fetch counters
+            k_extend_fetch<<<g_blocks_fetch[0], 128, 0, st>>>(sc, s, cur, pv.refill, d_err);
+        } else {
+            launch_extend(sc, s, cur, d_err, nullptr, st);
+        }
         cudaMemsetAsync(s.counts + (cur ^ 1), 0, 4, st);
         cudaMemsetAsync(s.counts + 2, 0, 8, st);   // shadow and done counts
         k_shade<true><<<g_blocks_shade, 128, 0, st>>>(sc, pp, ViewParams{}, 0u, 1u, s, cur, nullptr, 0u, lb);
-        launch_shadow(sc, s, d_err, nullptr, st);
+        if (fetch) {
+            k_shadow_fetch<<<g_blocks_fetch[1], 128, 0, st>>>(sc, s, pv.refill, d_err);
+        } else {
+            launch_shadow(sc, s, d_err, nullptr, st);
+        }
     }
 }
 
@@ -819,7 +966,6 @@ ohao_status run_pool(PersistentState* s, int variant, const DScene& sc, const Pa
                      int* d_err, bool use_graph, std::string& err) {
     init_launch_shapes();
     const uint32_t cap = kPool[variant].cap;
-    const bool reorder = kPool[variant].reorder;
     const size_t need = wavefront_scratch_bytes(cap);
     if (s->pool_bytes < need) {
         if (s->graph) { cudaGraphExecDestroy(s->graph); s->graph = nullptr; }
@@ -847,7 +993,7 @@ ohao_status run_pool(PersistentState* s, int variant, const DScene& sc, const Pa
             }
             cudaGraph_t g = nullptr;
             cudaStreamBeginCapture(cap_st, cudaStreamCaptureModeThreadLocal);
-            enqueue_chunk(sc, pp, s->d_lb, soa, cap, reorder, d_err, cap_st);
+            enqueue_chunk(sc, pp, s->d_lb, soa, cap, kPool[variant], d_err, cap_st);
             cudaError_t e = cudaStreamEndCapture(cap_st, &g);
             if (e == cudaSuccess) e = cudaGraphInstantiate(&s->graph, g, 0);
             if (g) cudaGraphDestroy(g);
@@ -872,7 +1018,7 @@ ohao_status run_pool(PersistentState* s, int variant, const DScene& sc, const Pa
             const cudaError_t e = cudaGraphLaunch(s->graph, st);
             if (e != cudaSuccess) { err = std::string("persistent graph launch: ") + cudaGetErrorString(e); return OHAO_ERR_CUDA; }
         } else {
-            enqueue_chunk(sc, pp, s->d_lb, soa, cap, reorder, d_err, st);
+            enqueue_chunk(sc, pp, s->d_lb, soa, cap, kPool[variant], d_err, st);
         }
         cudaMemcpyAsync(s->h_counts, soa.counts, 5 * sizeof(uint32_t), cudaMemcpyDeviceToHost, st);
         const cudaError_t e = cudaStreamSynchronize(st);
@@ -922,6 +1068,7 @@ ohao_status persistent_autotune(PersistentState* s, const DScene& sc, const Rend
     cudaEventCreate(&e0);
     cudaEventCreate(&e1);
     for (int v = 0; v < kNumPool; ++v) {
+        if (kPool[v].refill > 0 && !(sc.two_level && sc.nnodes > 0)) continue;   // same kernels as its plain twin
         cudaEventRecord(e0, st);
         r = run_pool(s, v, sc, pp, st, d_err, false, err);
         cudaEventRecord(e1, st);

@@ -239,3 +239,25 @@ def test_persistent_multiview_matches_wavefront_and_oracle(gpu_lib, oracle, two_
     torch.cuda.synchronize()
     for k in range(len(sd.views)):
         assert np.array_equal(accs[k].cpu().numpy(), outs[og.MODE_WAVEFRONT][0][k])
+    # every compiled launch shape (pool size, ray reordering, persistent-warp
+    # traversal) gives the same accumulators and per-path radiance
+    names = pt.launch_configs()
+    assert len(names) >= 5 and any("fetch" in n for n in names)
+    with pytest.raises(og.OhaoError):
+        pt.launch_config = "no_such_shape"
+    for name in names:
+        pt.launch_config = name
+        assert pt.launch_config == name
+        accs, paths, views = [], [], []
+        for v in sd.views:
+            npix = v.width * v.height
+            accs.append(torch.full((npix, 4), 7.0, dtype=torch.float32, device="cuda"))
+            paths.append(torch.zeros((spp, npix, 4), dtype=torch.float32, device="cuda"))
+            views.append(og.make_view(v, accum=accs[-1], history=0, path_radiance=paths[-1]))
+        pt.render(views, og.make_settings(spp=spp, max_bounces=4, sampler=1, sample_index_base=5,
+                                          mode=og.MODE_PERSISTENT))
+        torch.cuda.synchronize()
+        for k in range(len(sd.views)):
+            assert np.array_equal(accs[k].cpu().numpy(), outs[og.MODE_WAVEFRONT][0][k]), f"{name} accum view {k}"
+            assert np.array_equal(paths[k].cpu().numpy()[:, :, :3], outs[og.MODE_WAVEFRONT][1][k]), \
+                f"{name} paths view {k}"
