@@ -81,7 +81,7 @@ def instanced_pool():
     sd = scenes.instanced(n_views=4, side_range=(384, 384))
     pt = og.PathTracer()
     pt.load_scene(sd)
-    pt.launch_config = sys.argv[2] if len(sys.argv) > 2 else "pool_2M_unsorted_fetch4_chunk8"
+    pt.launch_config = sys.argv[2] if len(sys.argv) > 2 else "pool_4M_unsorted_fetch4_chunk8"
     accs = [torch.zeros((v.width * v.height, 4), device="cuda") for v in sd.views]
     s = og.make_settings(spp=4, max_bounces=4, mode=og.MODE_PERSISTENT)
     ms = _timed(lambda: pt.render([og.make_view(v, accum=a) for v, a in zip(sd.views, accs)], s), 2)

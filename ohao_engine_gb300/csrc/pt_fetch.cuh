@@ -1,5 +1,5 @@
-// pt_fetch.cuh -- two-level traversal as resumable state machines, for
-// persistent warps that refill finished lanes from a ray queue.
+// pt_fetch.cuh -- BVH traversal (flat or two-level) as resumable state
+// machines, for persistent warps that refill finished lanes from a ray queue.
 //
 // One *_step call does one unit of work of the traversal of scene_closest /
 // scene_occluded -- a node test, ONE triangle test, an instance entry or a
@@ -22,8 +22,9 @@ namespace ohao {
 
 constexpr uint32_t kNoHit = 0xFFFFFFFFu;
 
-// closest-hit state of one ray in a two-level scene
-struct Walk2 {
+// closest-hit state of one ray. kLevels 1: flat BVH (walked as one BLAS
+// whose triangle records carry their instance), 2: two-level.
+struct Walk {
     RayPre ra;                   // ray of the current level (object space inside a BLAS)
     Hit best;
     const uint4* bnodes;
@@ -36,7 +37,8 @@ struct Walk2 {
     bool in_blas, have_node, resume;
 };
 
-OHAO_D void walk2_begin(Walk2& w, const RayPre& r) {
+template <int kLevels>
+OHAO_D void walk_begin(const DScene& sc, Walk& w, const RayPre& r) {
     w.ra = r;
     w.best.t = 0.0f; w.best.u = 0.0f; w.best.v = 0.0f;
     w.best.inst = kNoHit; w.best.prim = kNoHit;
@@ -48,6 +50,11 @@ OHAO_D void walk2_begin(Walk2& w, const RayPre& r) {
     w.cur_tn = -INFINITY; w.res_tn = 0.0f;
     w.sp = 0; w.base = 0;
     w.in_blas = false; w.have_node = true; w.resume = false;
+    if (kLevels == 1) {
+        w.in_blas = true;
+        w.bnodes = sc.nodes;
+        w.btris = sc.tris;
+    }
 }
 
 // Enters the next pending instance leaf of w.pq/w.plm (or skips an empty
@@ -83,8 +90,9 @@ OHAO_D void enter_instance(const DScene& sc, const RayPre& r, const uint4& pq, u
 // One step of the closest-hit walk; true when the ray is finished (w.best
 // holds its hit). r: the world-space ray. Stack overflow sets err and ends
 // the walk.
-OHAO_D bool walk2_step(const DScene& sc, Walk2& w, const RayPre& r, float tmin, float tmax, uint32_t* st_node,
-                       float* st_t, int& err) {
+template <int kLevels>
+OHAO_D bool walk_step(const DScene& sc, Walk& w, const RayPre& r, float tmin, float tmax, uint32_t* st_node,
+                      float* st_t, int& err) {
     if (w.tlm) {   // one pending triangle
         const int i = __ffs(w.tlm) - 1;
         const uint32_t meta = byte_of(w.tmz, w.tmw, i);
@@ -95,9 +103,10 @@ OHAO_D bool walk2_step(const DScene& sc, Walk2& w, const RayPre& r, float tmin, 
             float t, u, v;
             if (tri_intersect(w.ra, v0, v1, v2, tmin, tmax, t, u, v)) {
                 const uint32_t prim = __float_as_uint(v0.w);
+                const uint32_t inst = kLevels == 1 ? __float_as_uint(v1.w) : w.inst;
                 if (w.best.prim == kNoHit || t < w.best.t ||
-                    (t == w.best.t && key_less(w.inst, prim, w.best.inst, w.best.prim))) {
-                    w.best.t = t; w.best.u = u; w.best.v = v; w.best.inst = w.inst; w.best.prim = prim;
+                    (t == w.best.t && key_less(inst, prim, w.best.inst, w.best.prim))) {
+                    w.best.t = t; w.best.u = u; w.best.v = v; w.best.inst = inst; w.best.prim = prim;
                 }
             }
         }
@@ -117,7 +126,7 @@ OHAO_D bool walk2_step(const DScene& sc, Walk2& w, const RayPre& r, float tmin, 
             const uint32_t hit = node_test(n, w.ra, tmin, tb, tn);
             const uint32_t imask = n.q0.w >> 24;
             const uint32_t lm = hit & ~imask;
-            if (w.in_blas) {   // its triangle leaves, one triangle per step, before the next node
+            if (kLevels == 1 || w.in_blas) {   // its triangle leaves, one triangle per step, before the next node
                 w.tbase = n.q1.y;
                 w.tmz = n.q1.z;
                 w.tmw = n.q1.w;
@@ -153,6 +162,7 @@ OHAO_D bool walk2_step(const DScene& sc, Walk2& w, const RayPre& r, float tmin, 
             w.have_node = true;
             return false;
         }
+        if (kLevels == 1) return true;
         w.in_blas = false;
         w.ra = r;
     }
@@ -184,8 +194,8 @@ OHAO_D bool walk2_step(const DScene& sc, Walk2& w, const RayPre& r, float tmin, 
     return false;
 }
 
-// any-hit state of one ray in a two-level scene
-struct Probe2 {
+// any-hit state of one ray (kLevels as for Walk)
+struct Probe {
     RayPre ra;
     const uint4* bnodes;
     const float4* btris;
@@ -196,7 +206,8 @@ struct Probe2 {
     bool in_blas, have_node, resume, hit;
 };
 
-OHAO_D void probe2_begin(Probe2& w, const RayPre& r) {
+template <int kLevels>
+OHAO_D void probe_begin(const DScene& sc, Probe& w, const RayPre& r) {
     w.ra = r;
     w.bnodes = nullptr;
     w.btris = nullptr;
@@ -205,11 +216,17 @@ OHAO_D void probe2_begin(Probe2& w, const RayPre& r) {
     w.tbase = 0u; w.tmz = 0u; w.tmw = 0u; w.tlm = 0u; w.tq = 0u;
     w.sp = 0; w.base = 0;
     w.in_blas = false; w.have_node = true; w.resume = false; w.hit = false;
+    if (kLevels == 1) {
+        w.in_blas = true;
+        w.bnodes = sc.nodes;
+        w.btris = sc.tris;
+    }
 }
 
 // One step of the any-hit walk; true when finished (w.hit: occluded).
-OHAO_D bool probe2_step(const DScene& sc, Probe2& w, const RayPre& r, float tmin, float tmax, uint32_t* st_node,
-                        int& err) {
+template <int kLevels>
+OHAO_D bool probe_step(const DScene& sc, Probe& w, const RayPre& r, float tmin, float tmax, uint32_t* st_node,
+                       int& err) {
     if (w.tlm) {   // one pending triangle
         const int i = __ffs(w.tlm) - 1;
         const uint32_t meta = byte_of(w.tmz, w.tmw, i);
@@ -236,7 +253,7 @@ OHAO_D bool probe2_step(const DScene& sc, Probe2& w, const RayPre& r, float tmin
         const uint32_t imask = n.q0.w >> 24;
         bool have = false;
         uint32_t next = 0u;
-        if (!w.in_blas) {
+        if (kLevels == 2 && !w.in_blas) {
             w.plm = m & ~imask;
             w.pq = n.q1;
             w.pidx = 0u;
@@ -258,7 +275,7 @@ OHAO_D bool probe2_step(const DScene& sc, Probe2& w, const RayPre& r, float tmin
             next = n.q1.x + (byte_of(n.q1.z, n.q1.w, i) & 7u);
             have = true;
         }
-        if (!w.in_blas && w.plm) {
+        if (kLevels == 2 && !w.in_blas && w.plm) {
             w.resume = have;
             w.res_cur = next;
             w.have_node = false;
@@ -276,6 +293,7 @@ OHAO_D bool probe2_step(const DScene& sc, Probe2& w, const RayPre& r, float tmin
             w.have_node = true;
             return false;
         }
+        if (kLevels == 1) return true;
         w.in_blas = false;
         w.ra = r;
     }

@@ -396,7 +396,7 @@ __global__ void __launch_bounds__(128) k_shadow(DScene sc, Soa s, int* err, unsi
     }
 }
 
-// Pool extend / shadow for two-level scenes with persistent warps. A lane
+// Pool extend / shadow with persistent warps (flat or two-level scenes). A lane
 // whose ray finished takes the next one from the queue while the other lanes
 // carry on: once at least `refill` lanes of a warp are idle, one atomic on the
 // queue's fetch counter claims rays for all of them. A warp therefore does
@@ -425,12 +425,13 @@ struct WarpFetch {
     }
 };
 
+template <int kLevels>
 __global__ void __launch_bounds__(128) k_extend_fetch(DScene sc, Soa s, int cur, int refill, int* err) {
     const uint32_t count = s.counts[cur];
     const uint32_t* q = s.q_ray[cur];
     uint32_t st_node[kStackSize];
     float st_t[kStackSize];
-    Walk2 w;
+    Walk w;
     RayPre r;
     uint32_t p = 0u;
     bool active = false;
@@ -441,14 +442,14 @@ __global__ void __launch_bounds__(128) k_extend_fetch(DScene sc, Soa s, int cur,
         if (i != 0xFFFFFFFFu) {
             p = q[i];
             r = ray_pre(ld3(s.ro[p]), ld3(s.rd[p]));
-            walk2_begin(w, r);
+            walk_begin<kLevels>(sc, w, r);
             active = true;
         }
         if (__ballot_sync(0xFFFFFFFFu, active) == 0u) {
             if (wf.drained) break;
             continue;
         }
-        if (active && walk2_step(sc, w, r, 0.001f, 10000.0f, st_node, st_t, e)) {
+        if (active && walk_step<kLevels>(sc, w, r, 0.001f, 10000.0f, st_node, st_t, e)) {
             s.hit[p] = make_float4(w.best.t, w.best.u, w.best.v, __uint_as_float(w.best.prim));
             s.hit_inst[p] = w.best.inst;
             active = false;
@@ -459,17 +460,20 @@ __global__ void __launch_bounds__(128) k_extend_fetch(DScene sc, Soa s, int cur,
 
 // Starts shadow ray `which` (0 light, 1 environment) of path p; a ray with
 // tmax <= tmin is unoccluded without a walk (as in scene_occluded).
-__device__ __forceinline__ void start_shadow(const Soa& s, uint32_t p, int which, Probe2& w, RayPre& r) {
+template <int kLevels>
+__device__ __forceinline__ void start_shadow(const DScene& sc, const Soa& s, uint32_t p, int which, Probe& w,
+                                             RayPre& r) {
     const float4 d = which == 0 ? s.shL[p] : s.shE[p];
     r = ray_pre(ld3(s.sh_org[p]), ld3(d));
-    probe2_begin(w, r);
+    probe_begin<kLevels>(sc, w, r);
     if (!(d.w > 0.001f)) w.have_node = false;   // the next step ends the walk unoccluded
 }
 
+template <int kLevels>
 __global__ void __launch_bounds__(128) k_shadow_fetch(DScene sc, Soa s, int refill, int* err) {
     const uint32_t count = s.counts[2];
     uint32_t st_node[kStackSize];
-    Probe2 w;
+    Probe w;
     RayPre r;
     float tmax = 0.0f;
     uint32_t p = 0u, f = 0u;
@@ -484,7 +488,7 @@ __global__ void __launch_bounds__(128) k_shadow_fetch(DScene sc, Soa s, int refi
             p = s.q_sh[i];
             f = s.flags[p];
             which = (f & kFlagShL) ? 0 : 1;
-            start_shadow(s, p, which, w, r);
+            start_shadow<kLevels>(sc, s, p, which, w, r);
             tmax = which == 0 ? s.shL[p].w : s.shE[p].w;
             visL = false;
             active = true;
@@ -493,11 +497,11 @@ __global__ void __launch_bounds__(128) k_shadow_fetch(DScene sc, Soa s, int refi
             if (wf.drained) break;
             continue;
         }
-        if (active && probe2_step(sc, w, r, 0.001f, tmax, st_node, e)) {
+        if (active && probe_step<kLevels>(sc, w, r, 0.001f, tmax, st_node, e)) {
             if (which == 0) visL = !w.hit;
             if (which == 0 && (f & kFlagShE)) {
                 which = 1;
-                start_shadow(s, p, 1, w, r);
+                start_shadow<kLevels>(sc, s, p, 1, w, r);
                 tmax = s.shE[p].w;
             } else {
                 const bool visE = which == 1 && !w.hit;
@@ -624,7 +628,7 @@ Soa carve_soa(void* base, uint32_t cap) {
 int g_num_sms = 0;
 int g_blocks_extend[2] = {0, 0}, g_blocks_shadow[2] = {0, 0};   // [flat, two-level]
 int g_blocks_shade = 0, g_blocks_trace = 0;
-int g_blocks_fetch[2] = {0, 0};   // persistent-warp extend, shadow: one full residency
+int g_blocks_fetch[4] = {0, 0, 0, 0};   // persistent-warp extend [flat, two-level], shadow [flat, two-level]
 
 void init_launch_shapes() {
     if (g_num_sms) return;
@@ -645,10 +649,14 @@ void init_launch_shapes() {
     g_blocks_shadow[1] = std::max(1, b) * g_num_sms;
     cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, k_trace, 128, 0);
     g_blocks_trace = std::max(1, b) * g_num_sms;
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, k_extend_fetch, 128, 0);
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, k_extend_fetch<1>, 128, 0);
     g_blocks_fetch[0] = std::max(1, b) * g_num_sms;
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, k_shadow_fetch, 128, 0);
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, k_extend_fetch<2>, 128, 0);
     g_blocks_fetch[1] = std::max(1, b) * g_num_sms;
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, k_shadow_fetch<1>, 128, 0);
+    g_blocks_fetch[2] = std::max(1, b) * g_num_sms;
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, k_shadow_fetch<2>, 128, 0);
+    g_blocks_fetch[3] = std::max(1, b) * g_num_sms;
 }
 
 // closest-hit / any-hit kernels specialised for the scene kind
@@ -824,7 +832,7 @@ constexpr int kChunk = 8;                       // iterations per graph replay (
 struct PoolVariant {
     uint32_t cap;
     bool reorder;
-    int refill;          // two-level scenes: persistent-warp traversal refilled at >= refill idle lanes (0: off)
+    int refill;          // persistent-warp traversal refilled at >= refill idle lanes (0: one ray per thread)
     const char* name;
 };
 const PoolVariant kPool[] = {
@@ -936,7 +944,7 @@ ohao_status stage_views(PersistentState* s, const RenderView* views, uint32_t n,
 
 void enqueue_chunk(const DScene& sc, const PathParams& pp, const LaunchBlock* lb, const Soa& s, uint32_t cap,
                    const PoolVariant& pv, int* d_err, cudaStream_t st) {
-    const bool fetch = pv.refill > 0 && sc.two_level && sc.nnodes > 0;
+    const bool fetch = pv.refill > 0 && sc.nnodes > 0;
     for (int it = 0; it < kChunk; ++it) {
         const int cur = it & 1;
         k_regen<<<g_blocks_shade, 128, 0, st>>>(pp, lb, s, cur);
@@ -947,7 +955,8 @@ void enqueue_chunk(const DScene& sc, const PathParams& pp, const LaunchBlock* lb
         }
         if (fetch) {
             cudaMemsetAsync(s.counts + kCtrExtendFetch, 0, 8, st);   // both fetch counters
-            k_extend_fetch<<<g_blocks_fetch[0], 128, 0, st>>>(sc, s, cur, pv.refill, d_err);
+            if (sc.two_level) k_extend_fetch<2><<<g_blocks_fetch[1], 128, 0, st>>>(sc, s, cur, pv.refill, d_err);
+            else k_extend_fetch<1><<<g_blocks_fetch[0], 128, 0, st>>>(sc, s, cur, pv.refill, d_err);
         } else {
             launch_extend(sc, s, cur, d_err, nullptr, st);
         }
@@ -955,7 +964,8 @@ void enqueue_chunk(const DScene& sc, const PathParams& pp, const LaunchBlock* lb
         cudaMemsetAsync(s.counts + 2, 0, 8, st);   // shadow and done counts
         k_shade<true><<<g_blocks_shade, 128, 0, st>>>(sc, pp, ViewParams{}, 0u, 1u, s, cur, nullptr, 0u, lb);
         if (fetch) {
-            k_shadow_fetch<<<g_blocks_fetch[1], 128, 0, st>>>(sc, s, pv.refill, d_err);
+            if (sc.two_level) k_shadow_fetch<2><<<g_blocks_fetch[3], 128, 0, st>>>(sc, s, pv.refill, d_err);
+            else k_shadow_fetch<1><<<g_blocks_fetch[2], 128, 0, st>>>(sc, s, pv.refill, d_err);
         } else {
             launch_shadow(sc, s, d_err, nullptr, st);
         }
@@ -1068,7 +1078,6 @@ ohao_status persistent_autotune(PersistentState* s, const DScene& sc, const Rend
     cudaEventCreate(&e0);
     cudaEventCreate(&e1);
     for (int v = 0; v < kNumPool; ++v) {
-        if (kPool[v].refill > 0 && !(sc.two_level && sc.nnodes > 0)) continue;   // same kernels as its plain twin
         cudaEventRecord(e0, st);
         r = run_pool(s, v, sc, pp, st, d_err, false, err);
         cudaEventRecord(e1, st);
