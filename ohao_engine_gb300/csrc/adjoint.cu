@@ -189,23 +189,49 @@ __device__ D4 spec_pdf(const PathParams& pp, const LocalMat& lm, V3 N, V3 inDir,
     return (Ds * NdotHs) * (1.0f / (4.0f * VdotHs + 1e-4f));
 }
 
+// Traversal entry points of the adjoint. It traces from several places (the
+// primary hit, two replayed chains, light and environment shadow rays);
+// inlined at each, the kernel's code outgrew the instruction cache (warps
+// mostly stalled on instruction fetch). Out of line there is one copy of each
+// traversal, behind an interface of a few registers.
+struct AdjHit {
+    Hit h;
+    int err;
+};
+__device__ __noinline__ AdjHit adj_closest(const DScene* sc, V3 o, V3 d) {
+    TravCount tc{0, 0};
+    int e = 0;
+    const Hit h = scene_closest<false>(*sc, o, d, 0.001f, 10000.0f, tc, e);
+    return AdjHit{h, e};
+}
+// bit 0: occluded, bit 1: traversal error
+__device__ __noinline__ int adj_occluded(const DScene* sc, V3 o, V3 d, float tmax) {
+    TravCount tc{0, 0};
+    int e = 0;
+    const bool occ = scene_occluded<false>(*sc, o, d, 0.001f, tmax, tc, e);
+    return (occ ? 1 : 0) | (e ? 2 : 0);
+}
+
 // Light NEE and env NEE at a vertex (primal draws and visibility, dual
 // values), without throughput.
 __device__ D3 nee_d(const DScene& sc, const PathParams& pp, Rng& rng, uint32_t& dim, const Surf& s, V3 inDir,
                     const LocalMat& lm, bool bounce0, int& err) {
     D3 g = d3c(v3s(0.0f));
-    TravCount tc{0, 0};
     const V3 org = s.pos + s.N * 0.01f;
     if (sc.nlights > 0) {
         const LightSample ls = sample_light(sc, rng, dim, s.pos, s.N);
-        if (ls.valid && !scene_occluded<false>(sc, org, ls.L, 0.001f, ls.shadowDist, tc, err)) {
+        const int oc = ls.valid ? adj_occluded(&sc, org, ls.L, ls.shadowDist) : 1;
+        if (oc & 2) err = 1;
+        if (!(oc & 1)) {
             const BrdfD b = brdf_d(pp, lm, s.N, inDir, ls.L, ls.NdotL, bounce0, 3.14159f, 3.14159f);
             g = g + dmul(b.f, ls.Le) * (ls.NdotL * ls.weight * ls.n);
         }
     }
     if (sc.has_cdf) {
         const EnvSample es = sample_env_nee(sc, pp, rng, dim, s.N);
-        if (es.valid && !scene_occluded<false>(sc, org, es.dir, 0.001f, 10000.0f, tc, err)) {
+        const int oc = es.valid ? adj_occluded(&sc, org, es.dir, 10000.0f) : 1;
+        if (oc & 2) err = 1;
+        if (!(oc & 1)) {
             const BrdfD b = brdf_d(pp, lm, s.N, inDir, es.dir, es.NdotL, bounce0, kPI, kPI);
             const D4 sp = spec_prob(lm, inDir, s.N);
             const D4 pdfS = (b.D * b.NdotH) * (1.0f / (4.0f * b.VdotH + 1e-4f));
@@ -341,8 +367,9 @@ __device__ ChainOut replay_chain(const DScene& sc, const PathParams& pp, Rng& rn
     int nrec = 0;
     float* last_dl = prev_dl;
     for (uint32_t bounce = 1; bounce <= pp.max_bounces && nrec < kMaxRec; ++bounce) {
-        TravCount tc{0, 0};
-        const Hit h = scene_closest<false>(sc, ro, rd, 0.001f, 10000.0f, tc, err);
+        const AdjHit ah = adj_closest(&sc, ro, rd);
+        if (ah.err) err = 1;
+        const Hit h = ah.h;
         VRec& R = rec[nrec];
         R.T[0] = thr.x; R.T[1] = thr.y; R.T[2] = thr.z;
         R.has_a = 0;
@@ -505,7 +532,8 @@ struct AdjView {
 
 // One thread per path (global pixel, sample), grid-stride.
 template <bool kSharedMap>
-__global__ void __launch_bounds__(128) k_adjoint(DScene sc, AdjParams ap, const AdjView* __restrict__ views,
+__global__ void __launch_bounds__(128) k_adjoint(const __grid_constant__ DScene sc, AdjParams ap,
+                                                 const AdjView* __restrict__ views,
                                                  float* __restrict__ grad_map, float* __restrict__ grad_rough,
                                                  int* err_flag) {
     extern __shared__ float smem[];
@@ -540,8 +568,9 @@ __global__ void __launch_bounds__(128) k_adjoint(DScene sc, AdjParams ap, const 
         path_start(vp, pp, px, py, sidx, ps);
         Rng rng = make_rng(pp, px, py, sidx, ps.rng);
         uint32_t dim = ps.dim;
-        TravCount tc{0, 0};
-        const Hit h = scene_closest<false>(sc, ps.ro, ps.rd, 0.001f, 10000.0f, tc, err);
+        const AdjHit ah = adj_closest(&sc, ps.ro, ps.rd);
+        if (ah.err) err = 1;
+        const Hit h = ah.h;
         if (h.prim == 0xFFFFFFFFu) continue;   // primary miss: no parameter dependence
         Surf s0;
         hit_shade(sc, ps.ro, ps.rd, h, s0);
