@@ -604,9 +604,9 @@ def run_denoise(args, n_scenes=50, iters=10000, crop=128, batch=8, variants=6):
             k = int(rng.integers(variants))
             y0, x0 = (int(v) for v in rng.integers(0, side - crop + 1, 2) // 16 * 16)
             xs.append(crop_of(data[s][0][k], 4, y0, x0))
-            aovs.append(crop_of(data[s][1][k], 8, y0, x0))
+            aovs.append(crop_of(data[s][1][k], og.AOV_FLOATS, y0, x0))
             ts.append(crop_of(data[s][2], 4, y0, x0))
-        lr = 2e-3 * (0.1 ** (it / iters))
+        lr = 2e-3 * min(1.0, (it + 1) / 200.0) * (0.1 ** (it / iters))   # 200-step warm-up, then decay
         losses.append(dn.train_step(xs, aovs, ts, crop, crop, lr))
     torch.cuda.synchronize()
     train_s = time.time() - t0
@@ -646,7 +646,7 @@ def run_denoise(args, n_scenes=50, iters=10000, crop=128, batch=8, variants=6):
                                      og.make_settings(spp=spp, max_bounces=4, sample_index_base=0)))
         plain[str(spp)] = {"rmse": rmse(acc), "ms": ms}
     noisy = torch.zeros((npix, 4), dtype=torch.float32, device="cuda")
-    aov = torch.zeros((npix, 8), dtype=torch.float32, device="cuda")
+    aov = torch.zeros((npix, og.AOV_FLOATS), dtype=torch.float32, device="cuda")
     out = torch.zeros((npix, 4), dtype=torch.float32, device="cuda")
     render_ms = timed(lambda: pt.render([og.make_view(v, accum=noisy, aov=aov)],
                                         og.make_settings(spp=1, max_bounces=4, sample_index_base=0)))
@@ -654,7 +654,7 @@ def run_denoise(args, n_scenes=50, iters=10000, crop=128, batch=8, variants=6):
     den_rmse = rmse(out)
     matched = max([int(s) for s, r in plain.items() if r["rmse"] >= den_rmse], default=0)
     flops = 2.0 * 9 * sum(ci * co * (1920 * 1088) / 4 ** lv for ci, co, lv in (
-        (10, 32, 0), (32, 32, 0), (32, 48, 1), (48, 48, 1), (48, 64, 2), (64, 64, 2), (64, 96, 3), (96, 96, 3),
+        (12, 32, 0), (32, 32, 0), (32, 48, 1), (48, 48, 1), (48, 64, 2), (64, 64, 2), (64, 96, 3), (96, 96, 3),
         (96, 128, 4), (128, 128, 4), (224, 96, 3), (96, 96, 3), (160, 64, 2), (64, 64, 2), (112, 48, 1), (48, 48, 1),
         (80, 32, 0), (32, 32, 0), (32, 3, 0)))
     peak = None
@@ -666,9 +666,10 @@ def run_denoise(args, n_scenes=50, iters=10000, crop=128, batch=8, variants=6):
             "value": den_rmse, "unit": "RMSE (display-transformed)", "n_gpus": 1, "steps": 1, "warmup": 0,
             "ms_per_step": render_ms + infer_ms, "higher_is_better": False, "scaling": "weak", "vs_baseline": None,
             "dtype": "bf16 (FP32 accumulation)", "data": "synthetic (seeded)",
-            "config": {"workload": "U-Net 32/48/64/96/128, 10-ch input; trained on "
+            "config": {"workload": "U-Net 32/48/64/96/128, 12-ch input (albedo-demodulated radiance, albedo, normal, "
+                                   "inverse depth, roughness, metallic); trained on "
                                    f"{n_scenes} scenes x 256^2 (1 spp x{variants} vs 1024 spp), {iters} Adam steps "
-                                   f"of {batch}x{crop}^2 crops, L1 on log radiance + L1 after the display "
+                                   f"of {batch}x{crop}^2 crops, L1 on log demodulated radiance + L1 after the display "
                                    "transform; judged on sphere_1m 1920x1080"},
             "denoised": {"rmse": den_rmse, "render_1spp_ms": render_ms, "infer_ms": infer_ms,
                          "total_ms": render_ms + infer_ms},

@@ -11,12 +11,13 @@
  * on the GPU by the same library from pairs the path tracer renders.
  *
  * Inputs per image: the path tracer's accumulator (device RGBA32F, the
- * ohao_pt_view.accum layout) and its AOV image (device [h*w][8] floats, the
- * ohao_pt_view.aov layout: first-hit albedo.rgb, normal*0.5+0.5, view depth,
- * hit flag). Network input channels: log(1 + radiance).rgb, albedo.rgb,
- * encoded normal, 1 / (1 + depth) on hits. Output: log(1 + radiance),
- * returned as linear RGBA32F. Loss: L1 in log(1 + radiance) plus L1 after
- * the reference's display transform.
+ * ohao_pt_view.accum layout) and its AOV image (device
+ * [h*w][OHAO_PT_AOV_FLOATS] floats, the ohao_pt_view.aov layout). Network
+ * input channels: log(1 + radiance / m).rgb with m = albedo + 0.04 on hits
+ * and 1 elsewhere (albedo demodulation), albedo.rgb, encoded normal,
+ * 1 / (1 + depth) on hits, roughness, metallic. Output: log(1 + radiance / m),
+ * returned remodulated as linear RGBA32F. Loss: L1 in that log space plus
+ * L1 after the reference's display transform.
  *
  * Status codes and ohao_stream are those of ohao_pt.h. A context is
  * externally synchronised. No counterpart calls in the reference beyond the

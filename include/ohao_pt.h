@@ -70,14 +70,17 @@ typedef struct ohao_pt_instance {
     uint32_t sbt_offset;       /* unused (one hit group) */
 } ohao_pt_instance;
 
+#define OHAO_PT_AOV_FLOATS 12
+
 /* One camera view. Matrices are column-major (glm) like the reference push
  * constants (pt_raygen.rgen:41-49). accum is a device RGBA32F image of
  * width*height texels holding (mean radiance, sample count); history is the
  * number of frames already in it (0 overwrites), the reference's
  * historyFrameCount. path_radiance (device, optional) receives every path's
  * radiance as [spp][height*width][4] floats. aov (device, optional) receives
- * the last sample's first-hit albedo.rgb, normal*0.5+0.5, view depth and a
- * hit flag as [height*width][8] floats. */
+ * the last sample's first-hit record as [height*width][OHAO_PT_AOV_FLOATS]
+ * floats: albedo.rgb, normal*0.5+0.5, view depth, hit flag, roughness,
+ * metallic, 0, 0 (background pixels: environment colour, 0, 1e30, 0, 0, 0). */
 typedef struct ohao_pt_view {
     float inv_view[16];
     float inv_proj[16];

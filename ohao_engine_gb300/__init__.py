@@ -32,6 +32,7 @@ FLAG_ENV_FIXED_V = 1 << 8
 FLAG_PROFILE = 1 << 16
 FLAG_ADJOINT_DECORRELATE = 1 << 17
 MODE_AUTO, MODE_WAVEFRONT, MODE_PERSISTENT = 0, 1, 2
+AOV_FLOATS = 12   # OHAO_PT_AOV_FLOATS: first-hit record per pixel (ohao_pt_view.aov)
 
 EXPORTED_SYMBOLS = [
     "ohao_pt_create", "ohao_pt_destroy", "ohao_pt_last_error", "ohao_pt_version", "ohao_pt_set_geometry",

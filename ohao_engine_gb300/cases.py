@@ -33,7 +33,7 @@ def denoise_infer():
     w, h = 1920, 1080
     rng = np.random.default_rng(0)
     rad = torch.from_numpy(rng.exponential(0.5, (w * h, 4)).astype(np.float32)).cuda()
-    aov = torch.from_numpy(rng.random((w * h, 8)).astype(np.float32)).cuda()
+    aov = torch.from_numpy(rng.random((w * h, 12)).astype(np.float32)).cuda()
     out = torch.zeros((w * h, 4), dtype=torch.float32, device="cuda")
     dn = Denoiser(max_pixels=1920 * 1088, seed=1)
     for _ in range(3):

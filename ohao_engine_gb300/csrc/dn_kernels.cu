@@ -409,6 +409,18 @@ __global__ void k_pool_bwd(const __nv_bfloat16* __restrict__ x, const float* __r
 }
 
 // features: log1p(radiance), albedo, normal (encoded 0..1), 1/(1+depth) on hits
+// Albedo demodulation of the radiance channels: the network sees and predicts
+// log1p(radiance / m), m = first-hit albedo + kDemodEps at surface hits and 1
+// on background pixels, so surface texture passes through the AOV instead of
+// being rebuilt from noise; the output is remodulated by the same m.
+constexpr float kDemodEps = 0.04f;
+// Output cap in log1p space (radiance ~1e13): keeps expm1 finite while the
+// first optimiser steps move the output far from the data.
+constexpr float kMaxLog = 30.0f;
+__device__ __forceinline__ float demod_of(const float* a, int c) {
+    return a[7] > 0.5f ? fmaxf(a[c], 0.0f) + kDemodEps : 1.0f;
+}
+
 __global__ void k_pack(const float4* __restrict__ rad, const float* __restrict__ aov, __nv_bfloat16* __restrict__ x,
                        int64_t npix_img, int w, int h, int wp, int hp, int64_t img_offset) {
     const int64_t total = static_cast<int64_t>(wp) * hp;
@@ -420,13 +432,15 @@ __global__ void k_pack(const float4* __restrict__ rad, const float* __restrict__
         if (px < w && py < h) {
             const int64_t s = static_cast<int64_t>(py) * w + px;
             const float4 r = rad[s];
-            f[0] = log1pf(fmaxf(r.x, 0.0f));
-            f[1] = log1pf(fmaxf(r.y, 0.0f));
-            f[2] = log1pf(fmaxf(r.z, 0.0f));
-            const float* a = aov + s * 8;
+            const float* a = aov + s * OHAO_PT_AOV_FLOATS;
+            f[0] = log1pf(fmaxf(r.x, 0.0f) / demod_of(a, 0));
+            f[1] = log1pf(fmaxf(r.y, 0.0f) / demod_of(a, 1));
+            f[2] = log1pf(fmaxf(r.z, 0.0f) / demod_of(a, 2));
             f[3] = a[0]; f[4] = a[1]; f[5] = a[2];
             f[6] = a[3]; f[7] = a[4]; f[8] = a[5];
             f[9] = a[7] > 0.5f ? 1.0f / (1.0f + fmaxf(a[6], 0.0f)) : 0.0f;
+            f[10] = a[8];
+            f[11] = a[9];
         }
         float lo8[8], hi8[8];
         for (int j = 0; j < 8; ++j) { lo8[j] = f[j]; hi8[j] = f[8 + j]; }
@@ -437,15 +451,19 @@ __global__ void k_pack(const float4* __restrict__ rad, const float* __restrict__
     (void)npix_img;
 }
 
-// out: [pixels][8] FP32 log1p radiance -> RGBA32F linear (crop from the padded grid)
-__global__ void k_unpack(const float* __restrict__ y, float4* __restrict__ out, int w, int h, int wp,
-                         int64_t img_offset) {
+// out: [pixels][8] FP32 log1p demodulated radiance -> RGBA32F linear
+// radiance (crop from the padded grid)
+__global__ void k_unpack(const float* __restrict__ y, const float* __restrict__ aov, float4* __restrict__ out, int w,
+                         int h, int wp, int64_t img_offset) {
     const int64_t total = static_cast<int64_t>(w) * h;
     for (int64_t i = blockIdx.x * static_cast<int64_t>(blockDim.x) + threadIdx.x; i < total;
          i += static_cast<int64_t>(gridDim.x) * blockDim.x) {
         const int px = static_cast<int>(i % w), py = static_cast<int>(i / w);
         const float* s = y + (img_offset + static_cast<int64_t>(py) * wp + px) * 8;
-        out[i] = make_float4(expm1f(fmaxf(s[0], 0.0f)), expm1f(fmaxf(s[1], 0.0f)), expm1f(fmaxf(s[2], 0.0f)), 1.0f);
+        const float* a = aov + i * OHAO_PT_AOV_FLOATS;
+        out[i] = make_float4(expm1f(fminf(fmaxf(s[0], 0.0f), kMaxLog)) * demod_of(a, 0),
+                             expm1f(fminf(fmaxf(s[1], 0.0f), kMaxLog)) * demod_of(a, 1),
+                             expm1f(fminf(fmaxf(s[2], 0.0f), kMaxLog)) * demod_of(a, 2), 1.0f);
     }
 }
 
@@ -467,12 +485,13 @@ __device__ __forceinline__ float display_tf(float x, float& slope) {
     return powf(fmaxf(a, 0.0f), 1.0f / 2.2f);
 }
 
-// Loss per channel: |y - log1p(t)| + kDisplayWeight |D(expm1(y)) - D(t)|
-// (y = prediction in log1p space, D = display transform); d out = its
-// (sub)gradient / count.
+// Loss per channel: |y - log1p(t / m)| + kDisplayWeight |D(m expm1(y')) - D(t)|
+// (y = prediction in demodulated log1p space, y' = min(y, kMaxLog), m its
+// albedo modulation, D = display transform); d out = its (sub)gradient / count.
 constexpr float kDisplayWeight = 1.0f;
-__global__ void k_l1(const float* __restrict__ y, const float4* __restrict__ tgt, float* __restrict__ dy, int w, int h,
-                     int wp, int64_t img_offset, float inv_count, double* __restrict__ loss) {
+__global__ void k_l1(const float* __restrict__ y, const float4* __restrict__ tgt, const float* __restrict__ aov,
+                     float* __restrict__ dy, int w, int h, int wp, int64_t img_offset, float inv_count,
+                     double* __restrict__ loss) {
     double part = 0.0;
     const int64_t total = static_cast<int64_t>(w) * h;
     for (int64_t i = blockIdx.x * static_cast<int64_t>(blockDim.x) + threadIdx.x; i < total;
@@ -481,16 +500,20 @@ __global__ void k_l1(const float* __restrict__ y, const float4* __restrict__ tgt
         const int64_t q = img_offset + static_cast<int64_t>(py) * wp + px;
         const float4 t = tgt[i];
         const float tl[3] = {fmaxf(t.x, 0.0f), fmaxf(t.y, 0.0f), fmaxf(t.z, 0.0f)};
+        const float* a = aov + i * OHAO_PT_AOV_FLOATS;
         for (int c = 0; c < 3; ++c) {
+            const float m = demod_of(a, c);
             const float yv = y[q * 8 + c];
-            const float d = yv - log1pf(tl[c]);
+            const float d = yv - log1pf(tl[c] / m);
             float s_unused, slope;
             const float dt = display_tf(tl[c], s_unused);
-            const float x = yv > 0.0f ? expm1f(yv) : 0.0f;
-            const float dd = display_tf(x, slope) - dt;
+            const bool live = yv > 0.0f && yv < kMaxLog;
+            const float e = yv > 0.0f ? expm1f(fminf(yv, kMaxLog)) : 0.0f;
+            const float dd = display_tf(e * m, slope) - dt;
             part += fabs(static_cast<double>(d)) + kDisplayWeight * fabs(static_cast<double>(dd));
             const float g_log = d > 0.0f ? 1.0f : (d < 0.0f ? -1.0f : 0.0f);
-            const float g_disp = yv > 0.0f ? (dd > 0.0f ? 1.0f : (dd < 0.0f ? -1.0f : 0.0f)) * slope * (x + 1.0f) : 0.0f;
+            const float g_disp =
+                live ? (dd > 0.0f ? 1.0f : (dd < 0.0f ? -1.0f : 0.0f)) * slope * m * (e + 1.0f) : 0.0f;
             dy[q * 8 + c] = (g_log + kDisplayWeight * g_disp) * inv_count;
         }
     }
@@ -607,14 +630,15 @@ void launch_pack(const float* rad, const float* aov, __nv_bfloat16* x, int w, in
     k_pack<<<grid_for(static_cast<int64_t>(wp) * hp, 256), 256, 0, st>>>(
         reinterpret_cast<const float4*>(rad), aov, x, static_cast<int64_t>(w) * h, w, h, wp, hp, img_off);
 }
-void launch_unpack(const float* y, float* out, int w, int h, int wp, int64_t img_off, cudaStream_t st) {
-    k_unpack<<<grid_for(static_cast<int64_t>(w) * h, 256), 256, 0, st>>>(y, reinterpret_cast<float4*>(out), w, h, wp,
-                                                                           img_off);
+void launch_unpack(const float* y, const float* aov, float* out, int w, int h, int wp, int64_t img_off,
+                   cudaStream_t st) {
+    k_unpack<<<grid_for(static_cast<int64_t>(w) * h, 256), 256, 0, st>>>(y, aov, reinterpret_cast<float4*>(out), w,
+                                                                           h, wp, img_off);
 }
-void launch_l1(const float* y, const float* tgt, float* dy, int w, int h, int wp, int64_t img_off, float inv_count,
-               double* loss, cudaStream_t st) {
-    k_l1<<<grid_for(static_cast<int64_t>(w) * h, 256), 256, 0, st>>>(y, reinterpret_cast<const float4*>(tgt), dy, w, h,
-                                                                        wp, img_off, inv_count, loss);
+void launch_l1(const float* y, const float* tgt, const float* aov, float* dy, int w, int h, int wp, int64_t img_off,
+               float inv_count, double* loss, cudaStream_t st) {
+    k_l1<<<grid_for(static_cast<int64_t>(w) * h, 256), 256, 0, st>>>(y, reinterpret_cast<const float4*>(tgt), aov, dy,
+                                                                        w, h, wp, img_off, inv_count, loss);
 }
 void launch_bias_grad(const float* dy, const __nv_bfloat16* y, bool relu, const Geo& g, int cout, int cout8, float* db,
                       cudaStream_t st) {

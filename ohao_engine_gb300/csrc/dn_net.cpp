@@ -64,6 +64,9 @@ struct Op {
 };
 
 constexpr int kChannels[5] = {32, 48, 64, 96, 128};
+// input channels used: log1p demodulated radiance (3), albedo (3), normal (3),
+// inverse depth, roughness, metallic
+constexpr int kInputChannels = 12;
 constexpr int kWgradBN = 256;  // N tile of the weight-gradient GEMM (features per CTA)
 
 // Deterministic normal draws (PCG32 + Box-Muller), identical on every host.
@@ -158,7 +161,7 @@ void build_graph(ohao_dn_ctx* c) {
     int cur = x;
     int skip[4];
     for (int l = 0; l < 5; ++l) {
-        const int a = add_conv(c, cur, -1, false, kChannels[l], true, l == 0 ? 10 : -1);
+        const int a = add_conv(c, cur, -1, false, kChannels[l], true, l == 0 ? kInputChannels : -1);
         const int e = add_conv(c, a, -1, false, kChannels[l], true);
         if (l < 4) {
             skip[l] = e;
@@ -470,7 +473,7 @@ ohao_status ohao_dn_infer(ohao_dn_ctx* ctx, const float* const* d_radiance, cons
     if ((s = forward(ctx, g0, st)) != OHAO_OK) return s;
     for (uint32_t i = 0; i < n_images; ++i) {
         if (!d_out[i]) return fail(ctx, OHAO_ERR_INVALID_ARG, "infer: null output image");
-        launch_unpack(ctx->T[ctx->out_tensor].act.as<float>(), d_out[i], static_cast<int>(width),
+        launch_unpack(ctx->T[ctx->out_tensor].act.as<float>(), d_aov[i], d_out[i], static_cast<int>(width),
                       static_cast<int>(height), g0.w, static_cast<int64_t>(i) * g0.w * g0.h, st);
     }
     DN_CK(cudaGetLastError(), "infer launch");
@@ -501,7 +504,7 @@ ohao_status ohao_dn_train_step(ohao_dn_ctx* ctx, const float* const* d_radiance,
     Tensor& to = ctx->T[ctx->out_tensor];
     for (uint32_t i = 0; i < n_images; ++i) {
         if (!d_target[i]) return fail(ctx, OHAO_ERR_INVALID_ARG, "train_step: null target");
-        launch_l1(to.act.as<float>(), d_target[i], to.grad.as<float>(), static_cast<int>(width),
+        launch_l1(to.act.as<float>(), d_target[i], d_aov[i], to.grad.as<float>(), static_cast<int>(width),
                   static_cast<int>(height), g0.w, static_cast<int64_t>(i) * g0.w * g0.h, inv,
                   ctx->loss_acc.as<double>(), st);
     }

@@ -6,6 +6,8 @@
 #include <cstddef>
 #include <cstdint>
 
+#include "../../include/ohao_pt.h"
+
 namespace ohao {
 namespace dn {
 
@@ -63,9 +65,10 @@ void launch_pool_fwd(const __nv_bfloat16* x, __nv_bfloat16* y, const Geo& lo, in
 void launch_pool_bwd(const __nv_bfloat16* x, const float* dy, float* dx, const Geo& lo, int c8, cudaStream_t st);
 void launch_pack(const float* rad, const float* aov, __nv_bfloat16* x, int w, int h, int wp, int hp, int64_t img_off,
                  cudaStream_t st);
-void launch_unpack(const float* y, float* out, int w, int h, int wp, int64_t img_off, cudaStream_t st);
-void launch_l1(const float* y, const float* tgt, float* dy, int w, int h, int wp, int64_t img_off, float inv_count,
-               double* loss, cudaStream_t st);
+void launch_unpack(const float* y, const float* aov, float* out, int w, int h, int wp, int64_t img_off,
+                   cudaStream_t st);
+void launch_l1(const float* y, const float* tgt, const float* aov, float* dy, int w, int h, int wp, int64_t img_off,
+               float inv_count, double* loss, cudaStream_t st);
 void launch_bias_grad(const float* dy, const __nv_bfloat16* y, bool relu, const Geo& g, int cout, int cout8, float* db,
                       cudaStream_t st);
 void launch_refresh(const LayerShape& L, const float* w32, __nv_bfloat16* w16, __nv_bfloat16* wt16, cudaStream_t st);

@@ -600,7 +600,7 @@ OHAO_D void path_start(const ViewParams& vw, const PathParams& pp, uint32_t px, 
 
 struct AovOut {
     V3 albedo, normal;
-    float depth, hit;
+    float depth, hit, rough, metal;
 };
 
 // Starts the diffuse chain from the stored first hit (pt_raygen.rgen:836-853).
@@ -642,11 +642,15 @@ OHAO_D bool path_step(const DScene& sc, const PathParams& pp, const ViewParams& 
                 const V3 fz = v3(iv[8], iv[9], iv[10]);
                 aov->depth = dot(s.pos - c, fz) * -1.0f;
                 aov->hit = 1.0f;
+                aov->rough = s.rough;
+                aov->metal = s.metal;
             } else {
                 aov->albedo = s.color;
                 aov->normal = v3s(0.0f);
                 aov->depth = 1e30f;
                 aov->hit = 0.0f;
+                aov->rough = 0.0f;
+                aov->metal = 0.0f;
             }
         }
         if (!s.hit) {

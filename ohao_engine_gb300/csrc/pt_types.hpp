@@ -72,7 +72,7 @@ struct RenderView {
     float* accum;        // device RGBA32F
     uint32_t history;
     float* path_out;     // device [spp][npix][4] or null
-    float* aov;          // device [npix][8] or null
+    float* aov;          // device [npix][OHAO_PT_AOV_FLOATS] or null
 };
 
 struct ProfileAcc {

@@ -1,7 +1,8 @@
 // wavefront.cu -- wavefront path integrator and the batch trace call.
 //
 // One wave holds up to `capacity` paths, numbered sample-major
-// (slot = k*npix + pixel - wave_begin), in structure-of-arrays state. Each of
+// (slot = k*npix + rank - wave_begin, rank = the pixel's place in 8x4-tile
+// order, see rank_pixel), in structure-of-arrays state. Each of
 // the 1 + 2*max_bounces iterations runs:
 //   extend  closest-hit traversal for the ray queue;
 //   shade   closest-hit/miss shading and the estimator step; emits the next
@@ -125,6 +126,31 @@ __device__ __forceinline__ void load_state(const Soa& s, uint32_t p, PathState& 
     ps.fhAlb = ld3(s.fhA[p]);
 }
 
+// Pixel of work rank j in a w x h view. Waves and the pool's work queue take
+// pixels in rank order; ranks run over 8x4 tiles in row-major tile order (a
+// warp's 32 consecutive paths cover one tile, so its primary rays and first
+// hits are compact), then the pixels right of and below the whole tiles, row
+// by row. Every output is written at the pixel's own index py * w + px.
+__device__ __forceinline__ void rank_pixel(uint32_t j, uint32_t w, uint32_t h, uint32_t& px, uint32_t& py) {
+    const uint32_t tw = w / 8u, th = h / 4u, nt = tw * th * 32u;
+    if (j < nt) {
+        const uint32_t t = j >> 5, r = j & 31u;
+        px = (t % tw) * 8u + (r & 7u);
+        py = (t / tw) * 4u + (r >> 3);
+        return;
+    }
+    j -= nt;
+    const uint32_t rw = w - tw * 8u, rh = th * 4u;
+    if (j < rw * rh) {
+        px = tw * 8u + j % rw;
+        py = j / rw;
+        return;
+    }
+    j -= rw * rh;
+    px = j % w;
+    py = rh + j / w;
+}
+
 // warp-aggregated queue append; returns the slot or ~0u
 __device__ __forceinline__ uint32_t warp_push(uint32_t* counter, bool pred) {
     const unsigned act = __activemask();
@@ -145,7 +171,8 @@ __global__ void k_generate(ViewParams vp, PathParams pp, uint32_t w0, uint32_t n
     if (i >= n) return;
     const uint32_t lin = w0 + i;
     const uint32_t k = lin / npix, p = lin - k * npix;
-    const uint32_t px = p % vp.width, py = p / vp.width;
+    uint32_t px, py;
+    rank_pixel(p, vp.width, vp.height, px, py);
     PathState ps;
     path_start(vp, pp, px, py, pp.sample_base + k, ps);
     store_state(s, i, ps, 0u);
@@ -207,7 +234,9 @@ __global__ void __launch_bounds__(128) k_shade(DScene sc, PathParams pp, ViewPar
             aov = aov_plain;
         }
         const ViewParams& vp = *vpp;
-        const uint32_t px = pix % vp.width, py = pix / vp.width;
+        uint32_t px, py;
+        rank_pixel(pix, vp.width, vp.height, px, py);
+        pix = py * vp.width + px;
         PathState ps;
         load_state(s, p, ps);
         const float4 hv = s.hit[p];
@@ -233,10 +262,10 @@ __global__ void __launch_bounds__(128) k_shade(DScene sc, PathParams pp, ViewPar
         }
         store_state(s, p, ps, extra);
         if (want_aov) {
-            float* a = aov + static_cast<size_t>(pix) * 8;
-            a[0] = ao.albedo.x; a[1] = ao.albedo.y; a[2] = ao.albedo.z;
-            a[3] = ao.normal.x; a[4] = ao.normal.y; a[5] = ao.normal.z;
-            a[6] = ao.depth; a[7] = ao.hit;
+            float4* a = reinterpret_cast<float4*>(aov + static_cast<size_t>(pix) * OHAO_PT_AOV_FLOATS);
+            a[0] = make_float4(ao.albedo.x, ao.albedo.y, ao.albedo.z, ao.normal.x);
+            a[1] = make_float4(ao.normal.y, ao.normal.z, ao.depth, ao.hit);
+            a[2] = make_float4(ao.rough, ao.metal, 0.0f, 0.0f);
         }
         const uint32_t slot = warp_push(s.counts + (cur ^ 1), more);
         if (slot != 0xFFFFFFFFu) qn[slot] = p;
@@ -316,7 +345,9 @@ __global__ void __launch_bounds__(128) k_regen(PathParams pp, const LaunchBlock*
         bool start = false;
         if (g != kIdle) {
             const PView& pv = lb->views[find_view(lb, g)];
-            const uint32_t pix = g - pv.pix_begin;
+            uint32_t px, py;
+            rank_pixel(g - pv.pix_begin, pv.vp.width, pv.vp.height, px, py);
+            const uint32_t pix = py * pv.vp.width + px;
             const V3 L = firefly(pp, ld3(s.rad[p]));
             if (pv.path_out)
                 reinterpret_cast<float4*>(pv.path_out)[static_cast<size_t>(k) * pv.npix + pix] = f4(L, 0.0f);
@@ -342,15 +373,18 @@ __global__ void __launch_bounds__(128) k_regen(PathParams pp, const LaunchBlock*
             g = claim;
             k = 0;
             const PView& pv = lb->views[find_view(lb, g)];
-            const uint32_t pix = g - pv.pix_begin;
-            acc = pv.history > 0 ? reinterpret_cast<const float4*>(pv.accum)[pix] : make_float4(0.f, 0.f, 0.f, 0.f);
+            uint32_t px, py;
+            rank_pixel(g - pv.pix_begin, pv.vp.width, pv.vp.height, px, py);
+            acc = pv.history > 0 ? reinterpret_cast<const float4*>(pv.accum)[py * pv.vp.width + px]
+                                 : make_float4(0.f, 0.f, 0.f, 0.f);
             start = true;
         }
         if (start) {
             const PView& pv = lb->views[find_view(lb, g)];
-            const uint32_t pix = g - pv.pix_begin;
+            uint32_t px, py;
+            rank_pixel(g - pv.pix_begin, pv.vp.width, pv.vp.height, px, py);
             PathState ps;
-            path_start(pv.vp, pp, pix % pv.vp.width, pix / pv.vp.width, pp.sample_base + k, ps);
+            path_start(pv.vp, pp, px, py, pp.sample_base + k, ps);
             store_state(s, p, ps, 0u);
         } else {
             g = kIdle;
@@ -517,18 +551,23 @@ __global__ void __launch_bounds__(128) k_shadow_fetch(DScene sc, Soa s, int refi
     if (e) atomicOr(err, 1);
 }
 
-__global__ void k_finalize(PathParams pp, uint32_t w0, uint32_t n, uint32_t npix, Soa s, float* accum,
-                           uint32_t history, float* path_out) {
+// p: the pixel's work rank (slots are rank-major); outputs at its index.
+__global__ void k_finalize(PathParams pp, uint32_t w0, uint32_t n, uint32_t width, uint32_t height, Soa s,
+                           float* accum, uint32_t history, float* path_out) {
+    const uint32_t npix = width * height;
     for (uint32_t p = blockIdx.x * blockDim.x + threadIdx.x; p < npix; p += gridDim.x * blockDim.x) {
         const uint64_t lo = w0, hi = static_cast<uint64_t>(w0) + n;   // [lo, hi)
         uint64_t k0 = (lo > p) ? (lo - p + npix - 1) / npix : 0;
         if (k0 * npix + p >= hi) continue;
         const uint64_t k1 = (hi - 1 - p) / npix;
-        float4 acc = reinterpret_cast<float4*>(accum)[p];
+        uint32_t px, py;
+        rank_pixel(p, width, height, px, py);
+        const uint32_t pidx = py * width + px;
+        float4 acc = reinterpret_cast<float4*>(accum)[pidx];
         for (uint64_t k = k0; k <= k1; ++k) {
             const uint32_t slot = static_cast<uint32_t>(k * npix + p - lo);
             const V3 L = firefly(pp, ld3(s.rad[slot]));
-            if (path_out) reinterpret_cast<float4*>(path_out)[k * npix + p] = f4(L, 0.0f);
+            if (path_out) reinterpret_cast<float4*>(path_out)[k * npix + pidx] = f4(L, 0.0f);
             if (history + k == 0) {
                 acc = make_float4(L.x, L.y, L.z, 1.0f);
             } else {
@@ -539,7 +578,7 @@ __global__ void k_finalize(PathParams pp, uint32_t w0, uint32_t n, uint32_t npix
                 acc.w = cnt;
             }
         }
-        reinterpret_cast<float4*>(accum)[p] = acc;
+        reinterpret_cast<float4*>(accum)[pidx] = acc;
     }
 }
 
@@ -773,7 +812,7 @@ ohao_status wavefront_render(const DScene& sc, const RenderView& view, const Pat
         }
         tm.begin(3, a);
         k_finalize<<<std::max(1u, std::min(4096u, (npix + 255) / 256)), 256, 0, st>>>(
-            pp, static_cast<uint32_t>(w0), n, npix, s, view.accum, view.history, view.path_out);
+            pp, static_cast<uint32_t>(w0), n, view.vp.width, view.vp.height, s, view.accum, view.history, view.path_out);
         tm.end(3, a);
     }
     const cudaError_t e = cudaGetLastError();

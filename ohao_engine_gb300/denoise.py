@@ -12,7 +12,7 @@ import ctypes as C
 
 import numpy as np
 
-from . import OhaoError, OK, _ptr, load_library, make_settings, make_view
+from . import AOV_FLOATS, OhaoError, OK, _ptr, load_library, make_settings, make_view
 
 EXPORTED_SYMBOLS = [
     "ohao_dn_create", "ohao_dn_destroy", "ohao_dn_last_error", "ohao_dn_param_count", "ohao_dn_get_params",
@@ -58,7 +58,7 @@ def _ptrs(items):
 
 class Denoiser:
     """One network on one GPU. Inputs are device tensors: radiance RGBA32F
-    [h*w, 4] (an accumulator), AOV [h*w, 8] (ohao_pt_view.aov)."""
+    [h*w, 4] (an accumulator), AOV [h*w, 12] (ohao_pt_view.aov)."""
 
     def __init__(self, max_pixels: int, device: int = 0, seed: int = 1):
         self._L = _bind(load_library())
@@ -161,7 +161,7 @@ def render_pair(pt, view, width, height, spp_noisy, spp_ref, seed_base, max_boun
     import torch
     npix = width * height
     noisy = torch.zeros((npix, 4), dtype=torch.float32, device="cuda")
-    aov = torch.zeros((npix, 8), dtype=torch.float32, device="cuda")
+    aov = torch.zeros((npix, AOV_FLOATS), dtype=torch.float32, device="cuda")
     ref = torch.zeros((npix, 4), dtype=torch.float32, device="cuda")
     pt.render([make_view(view, accum=noisy, aov=aov)],
               make_settings(spp=spp_noisy, max_bounces=max_bounces, sample_index_base=seed_base))

@@ -51,7 +51,7 @@ def layer_specs():
 
     cur, skips = 0, []
     for l in range(5):
-        a = conv(f"e{l}a", cur, None, False, CHANNELS[l], cin_used=10 if l == 0 else None)
+        a = conv(f"e{l}a", cur, None, False, CHANNELS[l], cin_used=12 if l == 0 else None)
         e = conv(f"e{l}", a, None, False, CHANNELS[l])
         if l < 4:
             skips.append(e)
@@ -193,19 +193,38 @@ def display_tf(x):
     return np.where(a >= 1.0, 1.0, np.maximum(a, 0.0) ** (1.0 / 2.2)), slope
 
 
-def l1_loss_grad(out, target_lin):
-    """|out - log1p(t)| + DISPLAY_WEIGHT |D(expm1(out)) - D(t)| per channel
-    (out in log1p space, D the display transform), mean and d out."""
+DEMOD_EPS = 0.04
+Y_MAX = 30.0   # output cap in log1p space
+
+
+def demod(aov):
+    """Albedo modulation m per pixel and channel: first-hit albedo + DEMOD_EPS
+    on surface hits, 1 on background pixels."""
+    hit = aov[..., 7:8] > 0.5
+    return np.where(hit, np.maximum(aov[..., 0:3], 0.0) + DEMOD_EPS, 1.0)
+
+
+def l1_loss_grad(out, target_lin, aov):
+    """|out - log1p(t / m)| + DISPLAY_WEIGHT |D(m expm1(min(out, Y_MAX))) - D(t)|
+    per channel (out in demodulated log1p space, m = demod(aov), D the
+    display transform), mean and d out."""
     tl = np.maximum(target_lin, 0.0)
+    m = demod(aov)
     y = out[..., :3]
-    d = y - np.log1p(tl)
-    x = np.where(y > 0, np.expm1(np.maximum(y, 0.0)), 0.0)
-    dx, slope = display_tf(x)
+    d = y - np.log1p(tl / m)
+    e = np.where(y > 0, np.expm1(np.clip(y, 0.0, Y_MAX)), 0.0)
+    dx, slope = display_tf(e * m)
     dd = dx - display_tf(tl)[0]
     cnt = d.size
     g = np.zeros_like(out)
-    g[..., :3] = (np.sign(d) + DISPLAY_WEIGHT * np.where(y > 0, np.sign(dd) * slope * (x + 1.0), 0.0)) / cnt
+    live = (y > 0) & (y < Y_MAX)
+    g[..., :3] = (np.sign(d) + DISPLAY_WEIGHT * np.where(live, np.sign(dd) * slope * m * (e + 1.0), 0.0)) / cnt
     return (np.abs(d).sum() + DISPLAY_WEIGHT * np.abs(dd).sum()) / cnt, g
+
+
+def unpack(out, aov):
+    """Linear radiance from the network output and the AOV image."""
+    return np.expm1(np.clip(out[..., :3], 0.0, Y_MAX)) * demod(aov)
 
 
 def backward(T, params, d_out):
@@ -244,10 +263,11 @@ def backward(T, params, d_out):
 
 
 def pack(rad, aov):
-    """Network input [h, w, 16] from RGBA radiance and the 8-float AOV image."""
+    """Network input [h, w, 16] from RGBA radiance and the 12-float AOV image."""
     h, w = rad.shape[:2]
     x = np.zeros((h, w, 16))
-    x[..., 0:3] = np.log1p(np.maximum(rad[..., :3], 0.0))
+    x[..., 0:3] = np.log1p(np.maximum(rad[..., :3], 0.0) / demod(aov))
     x[..., 3:9] = aov[..., 0:6]
     x[..., 9] = np.where(aov[..., 7] > 0.5, 1.0 / (1.0 + np.maximum(aov[..., 6], 0.0)), 0.0)
+    x[..., 10:12] = aov[..., 8:10]
     return bf16(x)

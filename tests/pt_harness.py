@@ -41,7 +41,7 @@ def render_paths_gpu(og, pt, view, spp, settings_kw, history=0, accum=None, aov=
     npix = view.width * view.height
     acc = torch.zeros((npix, 4), dtype=torch.float32, device="cuda") if accum is None else accum
     paths = torch.zeros((spp, npix, 4), dtype=torch.float32, device="cuda")
-    aovt = torch.zeros((npix, 8), dtype=torch.float32, device="cuda") if aov else None
+    aovt = torch.zeros((npix, og.AOV_FLOATS), dtype=torch.float32, device="cuda") if aov else None
     v = og.make_view(view, accum=acc, history=history, path_radiance=paths, aov=aovt)
     s = og.make_settings(spp=spp, **settings_kw)
     pt.render([v], s)

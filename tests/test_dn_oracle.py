@@ -37,3 +37,36 @@ def test_oracle_backward_matches_finite_differences():
             assert abs(fd - an) <= 1e-5 * max(abs(an), 1e-3), (li, kind, idx, fd, an)
     finally:
         R.ROUND = True
+
+
+def test_oracle_loss_gradient_and_demodulation():
+    """The training loss's gradient in the network's output (demodulated
+    log1p radiance) against central differences, and pack/unpack as inverse
+    albedo modulations."""
+    rng = np.random.default_rng(1)
+    h, w = 6, 5
+    aov = rng.random((1, h, w, 12))
+    aov[..., 7] = (rng.random((1, h, w)) < 0.7).astype(np.float64)
+    tgt = rng.exponential(0.6, (1, h, w, 3))
+    out = np.zeros((1, h, w, 8))
+    out[..., :3] = rng.uniform(0.05, 1.5, (1, h, w, 3))
+    l0, g = R.l1_loss_grad(out, tgt, aov)
+    for idx in [(0, 1, 2, 0), (0, 3, 4, 1), (0, 5, 0, 2), (0, 2, 2, 1)]:
+        e = 1e-7
+        op, om = out.copy(), out.copy()
+        op[idx] += e
+        om[idx] -= e
+        fd = (R.l1_loss_grad(op, tgt, aov)[0] - R.l1_loss_grad(om, tgt, aov)[0]) / (2 * e)
+        assert abs(fd - g[idx]) <= 1e-4 * abs(g[idx]) + 1e-9, (idx, fd, g[idx])
+    rad = np.zeros((h, w, 4))
+    rad[..., :3] = rng.exponential(0.6, (h, w, 3))
+    m = R.demod(aov[0])
+    assert np.all(m[aov[0, ..., 7] <= 0.5] == 1.0)
+    R.ROUND = False
+    try:
+        x = R.pack(rad, aov[0])
+        y = np.zeros((h, w, 8))
+        y[..., :3] = x[..., :3]
+        assert np.allclose(R.unpack(y, aov[0]), rad[..., :3], rtol=1e-12, atol=1e-12)
+    finally:
+        R.ROUND = True

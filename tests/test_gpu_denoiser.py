@@ -16,7 +16,7 @@ def _inputs(rng, n, h, w):
         r = np.zeros((h * w, 4), np.float32)
         r[:, :3] = rng.exponential(0.6, (h * w, 3)) * (rng.random((h * w, 1)) < 0.9)
         r[rng.random(h * w) < 0.02, :3] *= 40.0
-        a = rng.random((h * w, 8)).astype(np.float32)
+        a = rng.random((h * w, 12)).astype(np.float32)
         a[:, 6] *= 8.0
         a[:, 7] = (rng.random(h * w) < 0.85).astype(np.float32)
         t = np.zeros((h * w, 4), np.float32)
@@ -57,12 +57,13 @@ def test_pack_and_loss(trained_step):
     dn, (n, h, w), rad, aov, tgt, loss = trained_step
     specs, tensors, T, G = _device_state(dn, n, h, w)
     for i in range(n):
-        x = R.pack(rad[i].cpu().numpy().reshape(h, w, 4), aov[i].cpu().numpy().reshape(h, w, 8))
+        x = R.pack(rad[i].cpu().numpy().reshape(h, w, 4), aov[i].cpu().numpy().reshape(h, w, 12))
         # log1pf vs log1p may round to the other side of a BF16 boundary
         assert np.max(np.abs(T[0][i] - x)) <= np.max(np.abs(x)) * 2 ** -7
     out = T[-1]
     tg = np.stack([t.cpu().numpy().reshape(h, w, 4) for t in tgt])
-    l_ref, g_ref = R.l1_loss_grad(out, tg[..., :3])
+    av = np.stack([a.cpu().numpy().reshape(h, w, 12) for a in aov])
+    l_ref, g_ref = R.l1_loss_grad(out, tg[..., :3], av)
     assert abs(loss - l_ref) <= 1e-5 * l_ref
     # FP32 transcendental functions on the device: compare away from the
     # L1 kinks, within float rounding
@@ -145,7 +146,8 @@ def test_network_end_to_end(trained_step):
     Tr = R.forward(T[0], params)
     assert _rel(T[-1][..., :3], Tr[-1][..., :3]) < 1e-2
     tg = np.stack([t.cpu().numpy().reshape(h, w, 4) for t in tgt])
-    l_ref, g_out = R.l1_loss_grad(Tr[-1], tg[..., :3])
+    av = np.stack([a.cpu().numpy().reshape(h, w, 12) for a in aov])
+    l_ref, g_out = R.l1_loss_grad(Tr[-1], tg[..., :3], av)
     assert abs(loss - l_ref) <= 1e-2 * l_ref
     # backpropagate the device's own d loss / d output: the L1 sign flips
     # wherever the two outputs straddle the target, which is not under test

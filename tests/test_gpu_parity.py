@@ -142,14 +142,21 @@ def test_aov_first_hit(gpu_lib, oracle):
     sd = scenes.cornell(20, 20, 1)
     pt = gpu_tracer(gpu_lib, sd)
     _, _, aov = render_paths_gpu(gpu_lib, pt, sd.views[0], 1, dict(max_bounces=1), aov=True)
-    a = aov.cpu().numpy().reshape(20, 20, 8)
-    centre = a[5:15, 5:15].reshape(-1, 8)
+    a = aov.cpu().numpy().reshape(20, 20, 12)
+    centre = a[5:15, 5:15].reshape(-1, 12)
     assert np.all(centre[:, 7] == 1.0)      # the centre of the frame sees the box interior
-    hit = a.reshape(-1, 8)[a.reshape(-1, 8)[:, 7] == 1.0]
+    flat = a.reshape(-1, 12)
+    hit = flat[flat[:, 7] == 1.0]
     assert np.all((hit[:, 0:3] >= 0) & (hit[:, 0:3] <= 1))
     n = hit[:, 3:6] * 2.0 - 1.0
     assert np.allclose(np.linalg.norm(n, axis=1), 1.0, atol=1e-5)
     assert np.all(hit[:, 6] > 0)
+    # roughness and metallic of the hit material (the Cornell box: rough dielectrics)
+    mats = sd.materials
+    assert np.all((hit[:, 8] >= 0) & (hit[:, 8] <= 1)) and np.all(np.isin(hit[:, 9], mats[:, 5]))
+    assert np.all(np.isin(hit[:, 8], mats[:, 4]))
+    miss = flat[flat[:, 7] == 0.0]
+    assert np.all(miss[:, 8:12] == 0.0) and np.all(hit[:, 10:12] == 0.0)
 
 
 def test_errors_are_status_codes(gpu_lib):
