@@ -358,6 +358,154 @@ __global__ void __launch_bounds__(kThreads) k_conv(ConvArgs a, int* err_flag) {
     if (warp == 0) umma::tmem_dealloc(tmem, ncols);
 }
 
+// Forward convolution on rows of at least kHaloMinW pixels (single-source
+// inputs, see launch_conv). A CTA's 128
+// output pixels are x0 .. x0+127 of one image row; their 3 x 130-pixel
+// neighbourhood is loaded once into shared memory, channel-blocked as
+// [row 0..2][channel block][x 0..129][8 channels] (16 B per entry), and the
+// A operand of every tap is a descriptor into it: a core matrix is 8
+// consecutive x (16 B apart), the next 8 output pixels start 128 B on (SBO)
+// and the next 8 channels kHaloX * 16 B on (LBO); tap (dy, dx) starts at row
+// dy, x offset dx. Each input pixel is read 3 times per row of tiles instead
+// of once per tap and channel chunk. Weights stream through two stages in
+// 64-wide K chunks as in k_conv; a K step of 16 never crosses a tap because
+// cin8 is a multiple of 16 on this path.
+constexpr int kHaloX = kBM + 2;
+constexpr int kHaloMinW = 96;
+
+size_t halo_bytes(int cin8) { return static_cast<size_t>(3) * (cin8 / 8) * kHaloX * 16; }
+
+__global__ void __launch_bounds__(kThreads) k_conv_halo(ConvArgs a, int* err_flag) {
+    extern __shared__ __align__(1024) uint8_t dsm[];
+    __shared__ Smem ss;
+    const int bn = a.bn;
+    const int cb_count = a.cin8 / 8;
+    const uint32_t hbytes = static_cast<uint32_t>(3 * cb_count * kHaloX * 16);
+    const uint32_t b_off = (hbytes + 1023u) & ~1023u;
+    const uint32_t b_bytes = static_cast<uint32_t>(bn) * kBK * 2;
+    uint8_t* halo = dsm;
+    uint8_t* stage_b[kStages];
+    for (int s = 0; s < kStages; ++s) stage_b[s] = dsm + b_off + s * b_bytes;
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    uint32_t ncols = 32;
+    while (ncols < static_cast<uint32_t>(bn)) ncols <<= 1;
+    if (threadIdx.x == 0) {
+        for (int s = 0; s < kStages; ++s) umma::mbar_init(&ss.bar[s], 1);
+        umma::mbar_init(&ss.done, 1);
+        umma::mbar_fence_init();
+    }
+    if (warp == 0) umma::tmem_alloc(&ss.tmem, ncols);
+    umma::tc_fence_before();
+    __syncthreads();
+    umma::tc_fence_after();
+    const uint32_t tmem = ss.tmem;
+
+    // tile -> (image n, row y, first column x0)
+    const int xtiles = (a.g.w + kBM - 1) / kBM;
+    const int x0 = static_cast<int>(blockIdx.x % xtiles) * kBM;
+    const int ny = static_cast<int>(blockIdx.x / xtiles);
+    const int y = ny % a.g.h, n = ny / a.g.h;
+    // the neighbourhood, zero outside the image (padding 1); 8 independent
+    // 16-byte loads in flight per thread before their shared-memory stores
+    const int items = 3 * kHaloX * cb_count;
+    constexpr int kBatch = 8;
+    for (int base = 0; base < items; base += kThreads * kBatch) {
+        uint4 v[kBatch];
+        uint32_t dst[kBatch];
+#pragma unroll
+        for (int u = 0; u < kBatch; ++u) {
+            const int i = base + u * kThreads + static_cast<int>(threadIdx.x);
+            v[u] = make_uint4(0, 0, 0, 0);
+            dst[u] = 0xFFFFFFFFu;
+            if (i < items) {
+                const int cb = i % cb_count, rj = i / cb_count;
+                const int j = rj % kHaloX, r = rj / kHaloX;
+                const int qy = y - 1 + r, qx = x0 - 1 + j;
+                dst[u] = static_cast<uint32_t>(((r * cb_count + cb) * kHaloX + j) * 16);
+                if (qy >= 0 && qy < a.g.h && qx >= 0 && qx < a.g.w)
+                    v[u] = load_input8(a, (n * a.g.h + qy) * a.g.w + qx, n, qy, qx, cb * 8);
+            }
+        }
+#pragma unroll
+        for (int u = 0; u < kBatch; ++u)
+            if (dst[u] != 0xFFFFFFFFu) *reinterpret_cast<uint4*>(halo + dst[u]) = v[u];
+    }
+    const uint32_t idesc = umma::idesc_bf16(kBM, static_cast<uint32_t>(bn), false, false);
+    const uint32_t hbase = umma::smem_u32(halo);
+    const int kchunks = a.k_pad / kBK;
+    const int kreal = 9 * a.cin8;
+    bool ok = true;
+    for (int kc = 0; kc < kchunks && ok; ++kc) {
+        const int s = kc % kStages;
+        if (kc >= kStages) ok = umma::mbar_wait(&ss.bar[s], ((kc / kStages) - 1) & 1);
+        if (!__syncthreads_and(ok)) {
+            ok = false;
+            break;
+        }
+        uint8_t* sb = stage_b[s];
+        for (int L = threadIdx.x; L < bn * 8; L += kThreads) {
+            const int r = L & 7, kb = (L >> 3) & 7, nb = L >> 6;
+            const uint4 v =
+                *reinterpret_cast<const uint4*>(a.w + static_cast<int64_t>(nb * 8 + r) * a.k_pad + kc * kBK + kb * 8);
+            *reinterpret_cast<uint4*>(sb + L * 16) = v;
+        }
+        umma::fence_async_smem();   // also publishes the neighbourhood before the first MMA
+        __syncthreads();
+        if (threadIdx.x == 0) {
+            umma::tc_fence_after();
+            const uint32_t sbu = umma::smem_u32(sb);
+#pragma unroll
+            for (int i = 0; i < kBK / 16; ++i) {
+                const int k0 = kc * kBK + i * 16;
+                if (k0 >= kreal) break;   // zero-padded tail of K
+                const int tap = k0 / a.cin8, cb = (k0 - tap * a.cin8) >> 3;
+                const int dy = tap / 3, dx = tap % 3;
+                const uint64_t da =
+                    umma::smem_desc(hbase + static_cast<uint32_t>(((dy * cb_count + cb) * kHaloX + dx) * 16),
+                                    kHaloX * 16, 128);
+                const uint64_t db = umma::smem_desc(sbu + i * 256, 128, 1024);
+                umma::mma_bf16(tmem, da, db, idesc, k0 > 0);
+            }
+            umma::mma_commit(&ss.bar[s]);
+        }
+    }
+    if (threadIdx.x == 0) umma::mma_commit(&ss.done);
+    const bool drained = umma::mbar_wait(&ss.done, 0);
+    if (!ok || !drained) {
+        if (threadIdx.x == 0) atomicOr(err_flag, 2);
+    }
+    umma::tc_fence_after();
+    const bool good = __syncthreads_and(ok && drained);
+    if (good && kchunks > 0) {
+        const int row = warp * 32 + lane;
+        const uint32_t trow = tmem + (static_cast<uint32_t>(warp * 32) << 16);
+        const bool live = x0 + row < a.g.w;
+        const int64_t p = (static_cast<int64_t>(n) * a.g.h + y) * a.g.w + x0 + row;
+        for (int c = 0; c < bn; c += 8) {
+            float v[8];
+            umma::tmem_ld8(trow + c, v);   // warp-collective: every lane loads, the row test comes after
+            if (live && c < a.cout8) {
+#pragma unroll
+                for (int i = 0; i < 8; ++i) {
+                    v[i] += (c + i < a.cout) ? a.bias[c + i] : 0.0f;
+                    if (a.relu) v[i] = fmaxf(v[i], 0.0f);
+                    if (c + i >= a.cout) v[i] = 0.0f;
+                }
+                if (a.yf) {
+                    float4* o = reinterpret_cast<float4*>(a.yf + p * a.cout8 + c);
+                    o[0] = make_float4(v[0], v[1], v[2], v[3]);
+                    o[1] = make_float4(v[4], v[5], v[6], v[7]);
+                } else {
+                    *reinterpret_cast<uint4*>(a.yout + p * a.cout8 + c) = pack8(v);
+                }
+            }
+        }
+    }
+    umma::tc_fence_before();
+    __syncthreads();
+    if (warp == 0) umma::tmem_dealloc(tmem, ncols);
+}
+
 // ---- elementwise kernels ----
 __global__ void k_pool_fwd(const __nv_bfloat16* __restrict__ x, __nv_bfloat16* __restrict__ y, Geo lo, int c8) {
     const int64_t total = lo.npix * (c8 / 8);
@@ -601,9 +749,23 @@ size_t conv_smem_bytes(int bn) {
     return static_cast<size_t>(kStages) * (kBM * kBK * 2 + bn * kBK * 2) + 1024;
 }
 
+size_t conv_halo_smem_bytes(int cin8, int bn) {
+    return ((halo_bytes(cin8) + 1023) & ~static_cast<size_t>(1023)) + static_cast<size_t>(kStages) * bn * kBK * 2 + 1024;
+}
+
 cudaError_t launch_conv(int mode, const ConvArgs& a, int wgrad_splits, int* err_flag, cudaStream_t st) {
     const size_t smem = conv_smem_bytes(a.bn);
-    if (mode == kFwd) {
+    const size_t hsmem = conv_halo_smem_bytes(a.cin8, a.bn);
+    // the neighbourhood kernel for wide rows of single-source inputs; the
+    // upsample + skip-concatenation layers stay on the gather (measured: their
+    // large neighbourhoods leave one or two CTAs per SM and the two sources
+    // split the fill's warps)
+    if (mode == kFwd && a.g.w >= kHaloMinW && a.c1 == 0 && a.cin8 % 16 == 0 && a.n_tiles == 1 &&
+        hsmem <= 227 * 1024) {
+        cudaFuncSetAttribute(k_conv_halo, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(hsmem));
+        const int64_t tiles = static_cast<int64_t>(a.g.n) * a.g.h * ((a.g.w + kBM - 1) / kBM);
+        k_conv_halo<<<static_cast<unsigned>(tiles), kThreads, hsmem, st>>>(a, err_flag);
+    } else if (mode == kFwd) {
         cudaFuncSetAttribute(k_conv<kFwd>, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(smem));
         const dim3 grid(static_cast<unsigned>((a.g.npix + kBM - 1) / kBM), static_cast<unsigned>(a.n_tiles));
         k_conv<kFwd><<<grid, kThreads, smem, st>>>(a, err_flag);

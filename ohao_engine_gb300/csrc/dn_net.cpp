@@ -372,6 +372,15 @@ ohao_status ohao_dn_create(const ohao_dn_desc* desc, ohao_dn_ctx** out) {
     ctx->device = desc->device;
     ctx->max_pixels = (desc->max_pixels + 255) / 256 * 256;
     build_graph(ctx);
+    // every GEMM must fit the kernels' tcgen05.mma shapes: M = 128 and N in
+    // [16, 256] a multiple of 16 (forward: N = output channels; data gradient:
+    // N = input channels; weight gradient: M = output channels)
+    for (const Layer& l : ctx->L) {
+        if (l.s.cout_n > 256 || l.s.cin_n > 256 || l.s.cout > 128) {
+            delete ctx;
+            return OHAO_ERR_UNSUPPORTED;
+        }
+    }
     ohao_status s = alloc_params(ctx);
     if (s == OHAO_OK) s = alloc_acts(ctx, false);
     if (s == OHAO_OK && (ctx->err_flag.alloc(4) != cudaSuccess || ctx->loss_acc.alloc(8) != cudaSuccess))

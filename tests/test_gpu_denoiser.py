@@ -41,10 +41,12 @@ def _rel(a, b):
     return np.linalg.norm(a - b) / max(np.linalg.norm(b), 1e-30)
 
 
-@pytest.fixture(scope="module")
-def trained_step(gpu_lib):
+# "wide": rows of >= 96 pixels run the forward convolutions of the first two
+# levels on the shared-memory neighbourhood kernel, the others on the gather
+@pytest.fixture(scope="module", params=[(2, 32, 48), (1, 16, 256)], ids=["narrow", "wide"])
+def trained_step(gpu_lib, request):
     from ohao_engine_gb300.denoise import Denoiser
-    n, h, w = 2, 32, 48
+    n, h, w = request.param
     rng = np.random.default_rng(5)
     dn = Denoiser(max_pixels=n * h * w, seed=3)
     rad, aov, tgt = _inputs(rng, n, h, w)
