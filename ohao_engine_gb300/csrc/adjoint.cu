@@ -582,24 +582,34 @@ __global__ void __launch_bounds__(128) k_adjoint(const __grid_constant__ DScene 
         float dl0[4] = {0.f, 0.f, 0.f, 0.f};
         // stage A: light NEE and env NEE at throughput 1
         add_dl(dl0, delta, one, nee_d(sc, pp, rng, dim, s0, rayDir, m0, true, err));
-        // stage B: specular chain from vertex 0
-        float js0;
-        const V3 sd = spec_dir_score(rng, dim, rayDir, s0.N, s0.rough, js0);
+        // stage B (specular chain) then stage C (diffuse chain) from vertex 0,
+        // through one copy of the replay (a loop, not unrolled: inlined twice
+        // the kernel's code outgrows the instruction cache)
         const D3 tB = dvmix(d3c(v3s(1.0f)), m0.alb, s0.metal);
-        const bool deltaB = s0.rough < 0.05f;
-        const D4 pdfB = deltaB ? dc(1.0f) : spec_pdf(pp, m0, s0.N, rayDir, sd, true);
-        const ChainOut cb = replay_chain(sc, pp, rng, dim, true, s0.pos + s0.N * 0.01f, sd,
-                                         vmix(v3s(1.0f), s0.albedo, s0.metal), pdfB, deltaB, delta, dl0, rec, sk, err);
-        add_lam(dl0, cb.lam, tB);
-        if (p0.flags & 2u) dl0[3] += cb.value * js0;
-        // stage C: diffuse chain from vertex 0
-        const float d0 = rng.s1(dim), d1 = rng.s1(dim + 1);
-        dim += 2;
-        const V3 dd = cos_hemi(s0.N, d0, d1);
-        const D4 pdfC = dc(gmaxf(dot(dd, s0.N), 0.0f) / kPI);
-        const ChainOut cc = replay_chain(sc, pp, rng, dim, false, s0.pos + s0.N * 0.01f, dd, s0.albedo, pdfC, false,
-                                         delta, dl0, rec, sk, err);
-        add_lam(dl0, cc.lam, m0.alb);
+#pragma unroll 1
+        for (int chain = 0; chain < 2; ++chain) {
+            const bool spec = chain == 0;
+            V3 dir, thr0;
+            D4 pdf0;
+            bool delta0 = false;
+            float js0 = 0.0f;
+            if (spec) {
+                dir = spec_dir_score(rng, dim, rayDir, s0.N, s0.rough, js0);
+                delta0 = s0.rough < 0.05f;
+                pdf0 = delta0 ? dc(1.0f) : spec_pdf(pp, m0, s0.N, rayDir, dir, true);
+                thr0 = vmix(v3s(1.0f), s0.albedo, s0.metal);
+            } else {
+                const float d0 = rng.s1(dim), d1 = rng.s1(dim + 1);
+                dim += 2;
+                dir = cos_hemi(s0.N, d0, d1);
+                pdf0 = dc(gmaxf(dot(dir, s0.N), 0.0f) / kPI);
+                thr0 = s0.albedo;
+            }
+            const ChainOut co = replay_chain(sc, pp, rng, dim, spec, s0.pos + s0.N * 0.01f, dir, thr0, pdf0, delta0,
+                                             delta, dl0, rec, sk, err);
+            add_lam(dl0, co.lam, spec ? tB : m0.alb);
+            if (spec && (p0.flags & 2u)) dl0[3] += co.value * js0;
+        }
         scatter(sk, p0, dl0);
     }
     __syncthreads();
