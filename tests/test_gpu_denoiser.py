@@ -41,9 +41,10 @@ def _rel(a, b):
     return np.linalg.norm(a - b) / max(np.linalg.norm(b), 1e-30)
 
 
-# "wide": rows of >= 96 pixels run the forward convolutions of the first two
-# levels on the shared-memory neighbourhood kernel, the others on the gather
-@pytest.fixture(scope="module", params=[(2, 32, 48), (1, 16, 256)], ids=["narrow", "wide"])
+# "wide": rows of >= 96 pixels (levels 0-2 here) run the single-source
+# forward convolutions on the shared-memory neighbourhood kernel, the
+# concatenation layers and narrow levels on the gather
+@pytest.fixture(scope="module", params=[(2, 32, 48), (1, 16, 512)], ids=["narrow", "wide"])
 def trained_step(gpu_lib, request):
     from ohao_engine_gb300.denoise import Denoiser
     n, h, w = request.param
