@@ -268,3 +268,35 @@ def test_persistent_multiview_matches_wavefront_and_oracle(gpu_lib, oracle, two_
             assert np.array_equal(accs[k].cpu().numpy(), outs[og.MODE_WAVEFRONT][0][k]), f"{name} accum view {k}"
             assert np.array_equal(paths[k].cpu().numpy()[:, :, :3], outs[og.MODE_WAVEFRONT][1][k]), \
                 f"{name} paths view {k}"
+
+
+@pytest.mark.parametrize("two_level", [False, True])
+def test_degenerate_view_sizes(gpu_lib, oracle, two_level):
+    """Views of 1x1, 3x2, 7x5, 9x4 and 1x37 pixels (no whole 8x4 work tile,
+    or tiles plus ragged remainders) through the per-view wavefront and the
+    persistent pool in every launch shape: per-path radiance against the
+    oracle, accumulators bit-identical across forms."""
+    import torch
+    og = gpu_lib
+    sd = small_instanced(side=8) if two_level else small_env_scene(freq=8)
+    fl = 1 if two_level else 0
+    sizes = [(1, 1), (3, 2), (7, 5), (9, 4), (1, 37)]
+    sd.views = [scenes.look_at_view((0.0, 0.6, 3.2) if not two_level else (60.0, 10.0, 40.0),
+                                    (0, -0.1, 0) if not two_level else (0, 0, 0), width=w, height=h)
+                for w, h in sizes]
+    pt = gpu_tracer(og, sd, flatten_limit=fl)
+    orc = oracle.OracleScene(sd, flatten_limit=fl if fl else 1 << 25)
+    spp = 3
+    ref = {}
+    for k, v in enumerate(sd.views):
+        g, acc, _ = render_paths_gpu(og, pt, v, spp, dict(max_bounces=4, sampler=1, sample_index_base=2))
+        assert_paths_match(g, orc.render_paths(v, dict(max_bounces=4, sampler=1), 2, spp), f"view {sizes[k]}")
+        ref[k] = acc.cpu().numpy()
+    for name in pt.launch_configs():
+        pt.launch_config = name
+        accs = [torch.zeros((v.width * v.height, 4), dtype=torch.float32, device="cuda") for v in sd.views]
+        pt.render([og.make_view(v, accum=a) for v, a in zip(sd.views, accs)],
+                  og.make_settings(spp=spp, max_bounces=4, sampler=1, sample_index_base=2, mode=og.MODE_PERSISTENT))
+        torch.cuda.synchronize()
+        for k in range(len(sd.views)):
+            assert np.array_equal(accs[k].cpu().numpy(), ref[k]), f"{name} view {sizes[k]}"
