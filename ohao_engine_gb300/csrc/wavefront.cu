@@ -96,7 +96,12 @@ constexpr uint32_t kFlagDelta = 1u << 10, kFlagShL = 1u << 11, kFlagShE = 1u << 
 
 __device__ __forceinline__ float4 f4(V3 v, float w) { return make_float4(v.x, v.y, v.z, w); }
 
-__device__ __forceinline__ void store_state(const Soa& s, uint32_t p, const PathState& ps, uint32_t extra_flags) {
+// The first-hit record (fhP, fhN, fhAlb) is written by the primary step and
+// read only while the specular chain runs (the diffuse chain starts from it),
+// so it moves through memory only then: with_first_hit on the store after a
+// primary step, and on the load when the path is in its specular chain.
+__device__ __forceinline__ void store_state(const Soa& s, uint32_t p, const PathState& ps, uint32_t extra_flags,
+                                            bool with_first_hit) {
     s.rng[p] = ps.rng;
     s.dim[p] = ps.dim;
     s.flags[p] = ps.phase | (ps.bounce << 2) | (ps.delta ? kFlagDelta : 0u) | extra_flags;
@@ -104,9 +109,11 @@ __device__ __forceinline__ void store_state(const Soa& s, uint32_t p, const Path
     s.rd[p] = f4(ps.rd, ps.last_pdf);
     s.thr[p] = f4(ps.thr, 0.0f);
     s.rad[p] = f4(ps.rad, 0.0f);
-    s.fhP[p] = f4(ps.fhP, 0.0f);
-    s.fhN[p] = f4(ps.fhN, 0.0f);
-    s.fhA[p] = f4(ps.fhAlb, 0.0f);
+    if (with_first_hit) {
+        s.fhP[p] = f4(ps.fhP, 0.0f);
+        s.fhN[p] = f4(ps.fhN, 0.0f);
+        s.fhA[p] = f4(ps.fhAlb, 0.0f);
+    }
 }
 __device__ __forceinline__ void load_state(const Soa& s, uint32_t p, PathState& ps) {
     ps.rng = s.rng[p];
@@ -121,9 +128,13 @@ __device__ __forceinline__ void load_state(const Soa& s, uint32_t p, PathState& 
     ps.last_pdf = rd.w;
     ps.thr = ld3(s.thr[p]);
     ps.rad = ld3(s.rad[p]);
-    ps.fhP = ld3(s.fhP[p]);
-    ps.fhN = ld3(s.fhN[p]);
-    ps.fhAlb = ld3(s.fhA[p]);
+    if (ps.phase == kPhaseSpec) {
+        ps.fhP = ld3(s.fhP[p]);
+        ps.fhN = ld3(s.fhN[p]);
+        ps.fhAlb = ld3(s.fhA[p]);
+    } else {
+        ps.fhP = ps.fhN = ps.fhAlb = v3s(0.0f);
+    }
 }
 
 // Pixel of work rank j in a w x h view. Waves and the pool's work queue take
@@ -175,7 +186,7 @@ __global__ void k_generate(ViewParams vp, PathParams pp, uint32_t w0, uint32_t n
     rank_pixel(p, vp.width, vp.height, px, py);
     PathState ps;
     path_start(vp, pp, px, py, pp.sample_base + k, ps);
-    store_state(s, i, ps, 0u);
+    store_state(s, i, ps, 0u, false);
     s.q_ray[0][i] = i;
 }
 
@@ -260,7 +271,7 @@ __global__ void __launch_bounds__(128) k_shade(DScene sc, PathParams pp, ViewPar
             s.shEc[p] = f4(qE.contrib, 0.0f);
             s.sh_org[p] = f4(qE.org, 0.0f);
         }
-        store_state(s, p, ps, extra);
+        store_state(s, p, ps, extra, primary && ps.phase == kPhaseSpec);
         if (want_aov) {
             float4* a = reinterpret_cast<float4*>(aov + static_cast<size_t>(pix) * OHAO_PT_AOV_FLOATS);
             a[0] = make_float4(ao.albedo.x, ao.albedo.y, ao.albedo.z, ao.normal.x);
@@ -385,7 +396,7 @@ __global__ void __launch_bounds__(128) k_regen(PathParams pp, const LaunchBlock*
             rank_pixel(g - pv.pix_begin, pv.vp.width, pv.vp.height, px, py);
             PathState ps;
             path_start(pv.vp, pp, px, py, pp.sample_base + k, ps);
-            store_state(s, p, ps, 0u);
+            store_state(s, p, ps, 0u, false);
         } else {
             g = kIdle;
         }
