@@ -218,8 +218,12 @@ __global__ void __launch_bounds__(128) k_extend(DScene sc, Soa s, int cur, int* 
 // kPool: slot -> (pixel, sample) comes from the pool arrays and the view
 // table; finished paths are queued for regeneration. Otherwise a slot is
 // the sample-major index inside the wave [w0, w0 + n) of one view.
+// Registers capped for 8 resident blocks per SM: the step is latency-bound
+// (scene and state loads, 21% of issue slots at 128 registers and 4 blocks),
+// and 32 warps hide more of it than the spills cost (sphere_1m: 376 -> 402
+// Msamples/s; 10 or 12 blocks gain under 1% more).
 template <bool kPool>
-__global__ void __launch_bounds__(128) k_shade(DScene sc, PathParams pp, ViewParams vp_plain, uint32_t w0,
+__global__ void __launch_bounds__(128, 8) k_shade(DScene sc, PathParams pp, ViewParams vp_plain, uint32_t w0,
                                                uint32_t npix_plain, Soa s, int cur, float* aov_plain, uint32_t aov_k,
                                                const LaunchBlock* lb) {
     const uint32_t count = s.counts[cur];
