@@ -16,7 +16,11 @@
 // nearest internal child is visited next and the others are pushed far to
 // near (ties: lower slot pushed first). Popped entries whose entry distance
 // exceeds the best hit (with a 2^-14 relative slack) are skipped. Any-hit
-// queries push internal children in slot order and return at the first hit.
+// queries return at the first hit; in a flat BVH they test a node's leaves,
+// then continue with the nearest internal child (others pushed far to near,
+// so nearby occluders are found sooner; the host oracle walks in slot order
+// -- the answer is the same boolean either way); the two-level any-hit
+// keeps slot order.
 // The stack holds 64 (node, t_near) entries in local memory; overflow sets
 // the error flag instead of faulting.
 #pragma once
@@ -196,23 +200,13 @@ OHAO_D bool bvh_any(const uint4* __restrict__ nodes, const float4* __restrict__ 
         const NodeRec n = load_node(nodes, cur);
         if (kStats) cnt.nodes++;
         float tn[8];
-        uint32_t m = node_test(n, r, tmin, tmax, tn);
+        const uint32_t m = node_test(n, r, tmin, tmax, tn);
         const uint32_t imask = n.q0.w >> 24;
-        bool have = false;
-        uint32_t next = 0u;
-        while (m) {
-            const int i = __ffs(m) - 1;
-            m &= m - 1;
+        uint32_t lm = m & ~imask;
+        while (lm) {
+            const int i = __ffs(lm) - 1;
+            lm &= lm - 1;
             const uint32_t meta = byte_of(n.q1.z, n.q1.w, i);
-            if ((imask >> i) & 1u) {
-                if (have) {
-                    if (sp >= kStackSize) { err = 1; return false; }
-                    st_node[sp++] = next;
-                }
-                next = n.q1.x + (meta & 7u);
-                have = true;
-                continue;
-            }
             const uint32_t c = meta >> 5, off = meta & 31u;
             for (uint32_t q = 0; q < c; ++q) {
                 const float4* tp = tris + static_cast<size_t>(n.q1.y + off + q) * 3;
@@ -222,7 +216,21 @@ OHAO_D bool bvh_any(const uint4* __restrict__ nodes, const float4* __restrict__ 
                 if (tri_intersect(r, v0, v1, v2, tmin, tmax, t, u, v)) return true;
             }
         }
-        if (have) { cur = next; continue; }
+        uint32_t rem = m & imask;
+        if (rem) {   // nearest internal child next, the others pushed far to near
+            while (__popc(rem) > 1) {
+                float bt = 0.0f;
+                int bi = -1;
+#pragma unroll
+                for (int i = 0; i < 8; ++i)
+                    if (((rem >> i) & 1u) && (bi < 0 || tn[i] > bt)) { bt = tn[i]; bi = i; }
+                if (sp >= kStackSize) { err = 1; return false; }
+                st_node[sp++] = n.q1.x + (byte_of(n.q1.z, n.q1.w, bi) & 7u);
+                rem &= ~(1u << bi);
+            }
+            cur = n.q1.x + (byte_of(n.q1.z, n.q1.w, __ffs(rem) - 1) & 7u);
+            continue;
+        }
         if (sp == stack_base) return false;
         cur = st_node[--sp];
     }
