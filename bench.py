@@ -199,13 +199,9 @@ def run_reference(args):
 
 def run_ours(args):
     import torch
-    world = int(os.environ.get("WORLD_SIZE", "1"))
-    rank = int(os.environ.get("RANK", "0"))
-    local = int(os.environ.get("LOCAL_RANK", "0"))
-    dist = None
-    if world > 1:
-        import torch.distributed as dist
-        dist.init_process_group("nccl")
+    from ohao_engine_gb300 import replicas
+    ranks = replicas.init("nccl")
+    world, rank, local = ranks.world, ranks.rank, ranks.local
     torch.cuda.set_device(local)
     import ohao_engine_gb300 as og
     from ohao_engine_gb300 import _build
@@ -237,8 +233,7 @@ def run_ours(args):
     clk = ClockSampler(local)
     clk.start()
     times = []
-    if dist:
-        dist.barrier()
+    replicas.barrier(ranks)
     torch.cuda.synchronize()
     for k in range(args.steps):
         flush.zero_()
@@ -250,16 +245,10 @@ def run_ours(args):
         e1.synchronize()
         times.append(e0.elapsed_time(e1))
     torch.cuda.synchronize()
-    if dist:
-        dist.barrier()
+    replicas.barrier(ranks)
     clocks = clk.stop()
-    total_ms = float(sum(times))
-    if dist:
-        t = torch.tensor([total_ms], device="cuda")
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        total_ms = float(t.item())
-    samples_all = npix * spp_step * args.steps * world
-    value = samples_all / (total_ms / 1e3) / 1e6
+    total_ms = replicas.max_over_ranks(ranks, float(sum(times)))
+    value = replicas.whole_job_rate(npix * spp_step * args.steps, ranks, total_ms / 1e3) / 1e6
 
     # profiled pass: per-kernel CUDA events + traversal visit counters
     prof_ms = []
@@ -311,12 +300,8 @@ def run_ours(args):
         t0 = time.perf_counter()
         pt.render_host([og.make_view(v, history=1 + k * spp_step)], s, [hnp])
         e2e_times.append(time.perf_counter() - t0)
-    e2e_total = sum(e2e_times)
-    if dist:
-        t = torch.tensor([e2e_total], device="cuda")
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        e2e_total = float(t.item())
-    e2e = {"value": npix * spp_step * args.steps * world / e2e_total / 1e6, "unit": UNIT,
+    e2e_value = replicas.whole_job_rate(npix * spp_step * args.steps, ranks, sum(e2e_times)) / 1e6
+    e2e = {"value": e2e_value, "unit": UNIT,
            "h2d_bytes_per_step": npix * 16, "d2h_bytes_per_step": npix * 16,
            "call": "ohao_pt_render_host (pinned host accumulator in and out)"}
 
@@ -335,8 +320,7 @@ def run_ours(args):
                 "roofline": roofline, "cpu_baseline": cpu}
         print(json.dumps(line), flush=True)
     pt.close()
-    if dist:
-        dist.destroy_process_group()
+    replicas.finish(ranks)
 
 
 def run_instanced(args):
