@@ -140,28 +140,6 @@ void instance_matrices(const float x[12], float w2o[12], float nrm[9]) {
         for (int k = 0; k < 3; ++k) nrm[r * 3 + k] = static_cast<float>(inv[k * 3 + r]);
 }
 
-void xform_point(const float m[12], const float p[3], float o[3]) {
-    for (int r = 0; r < 3; ++r) o[r] = ((m[r * 4 + 0] * p[0] + m[r * 4 + 1] * p[1]) + m[r * 4 + 2] * p[2]) + m[r * 4 + 3];
-}
-
-// World box of an instance: the 8 transformed corners of the BLAS box, padded
-// by 2^-20 of the coordinate magnitude so that rounding in the transform
-// cannot exclude geometry.
-void instance_world_box(const ohao_pt_instance& in, const float ob[6], float wb[6]) {
-    for (int a = 0; a < 3; ++a) { wb[a] = INFINITY; wb[3 + a] = -INFINITY; }
-    if (!(ob[0] <= ob[3])) return;
-    for (int c = 0; c < 8; ++c) {
-        const float p[3] = {(c & 1) ? ob[3] : ob[0], (c & 2) ? ob[4] : ob[1], (c & 4) ? ob[5] : ob[2]};
-        float w[3];
-        xform_point(in.transform, p, w);
-        for (int a = 0; a < 3; ++a) { wb[a] = std::min(wb[a], w[a]); wb[3 + a] = std::max(wb[3 + a], w[a]); }
-    }
-    for (int a = 0; a < 3; ++a) {
-        const float pad = (std::fabs(wb[a]) + std::fabs(wb[3 + a])) * 0x1p-20f;
-        wb[a] = wb[a] - pad;
-        wb[3 + a] = wb[3 + a] + pad;
-    }
-}
 
 ohao_status build_one(ohao_pt_ctx* ctx, const float* d_boxes, uint32_t n, BvhDev& out, cudaStream_t st) {
     std::string err;
@@ -431,24 +409,25 @@ ohao_status ohao_pt_build(ohao_pt_ctx* ctx, ohao_stream stream) {
                                    static_cast<size_t>(bv.nprims) * 48, cudaMemcpyDeviceToDevice, st), "build");
         }
         if ((s = upload(ctx, ctx->blas_desc, desc.data(), desc.size() * sizeof(ohao::DBlas), "build")) != OHAO_OK) return s;
-        // TLAS over visible instances' world boxes
-        std::vector<float> ib;
-        std::vector<uint32_t> ids;
+        // TLAS over visible instances' world boxes: min/max of every
+        // transformed vertex of the instance's BLAS, on the device
+        std::vector<float> xf;
+        std::vector<uint32_t> span, ids;
         for (uint32_t i = 0; i < ninst; ++i) {
             const auto& in = ctx->instances[i];
             if (!(in.mask & 0xFFu) || ctx->blas_bvh[in.blas].nprims == 0) continue;
-            float wb[6];
-            const BvhDev& bv = ctx->blas_bvh[in.blas];
-            float ob[6];
-            if (bv.nprims) std::memcpy(ob, bv.root_box, 24);
-            else { ob[0] = ob[1] = ob[2] = INFINITY; ob[3] = ob[4] = ob[5] = -INFINITY; }
-            instance_world_box(in, ob, wb);
-            ib.insert(ib.end(), wb, wb + 6);
+            xf.insert(xf.end(), in.transform, in.transform + 12);
+            span.push_back(desc[in.blas].tri_off);
+            span.push_back(desc[in.blas].ntris);
             ids.push_back(i);
         }
-        DevBuf dib;
-        if ((s = upload(ctx, dib, ib.data(), ib.size() * 4, "build")) != OHAO_OK) return s;
         const uint32_t ni = static_cast<uint32_t>(ids.size());
+        DevBuf dxf, dspan, dib;
+        if ((s = upload(ctx, dxf, xf.data(), xf.size() * 4, "build")) != OHAO_OK) return s;
+        if ((s = upload(ctx, dspan, span.data(), span.size() * 4, "build")) != OHAO_OK) return s;
+        CK(dib.ensure(static_cast<size_t>(std::max(ni, 1u)) * 24), "build");
+        ohao::launch_instance_boxes(dxf.as<float>(), dspan.as<uint32_t>(), ctx->blas_tris_all.as<float4>(), ni,
+                                    dib.as<float>(), st);
         if ((s = build_one(ctx, dib.as<float>(), ni, ctx->flat, st)) != OHAO_OK) return s;
         std::vector<uint32_t> order(ni);
         if (ni) CK(cudaMemcpy(order.data(), ctx->flat.prims.p, static_cast<size_t>(ni) * 4, cudaMemcpyDeviceToHost), "build");

@@ -37,6 +37,11 @@ void launch_flat_triangles(const float* pos, const uint32_t* indices, const uint
 void launch_blas_triangles(const float* pos, const uint32_t* indices, uint32_t first_index, uint32_t ntris,
                            float* tri_verts, uint32_t* tri_inst, uint32_t* tri_prim, float* boxes, cudaStream_t st);
 // Record gather: recs[j] = (v0, prim; v1, inst; v2, ref = order[j]).
+// World boxes of n instances from their object-to-world transforms (12
+// floats each) and the (first record, count) span of their BLAS's triangle
+// records (48 B each, object space).
+void launch_instance_boxes(const float* o2w, const uint32_t* span, const float4* recs, uint32_t n, float* boxes,
+                           cudaStream_t st);
 void launch_gather_records(const float* tri_verts, const uint32_t* tri_inst, const uint32_t* tri_prim,
                            const uint32_t* order, uint32_t n, float4* recs, cudaStream_t st);
 

@@ -7,6 +7,8 @@
 // (rt_acceleration_structure.cpp:205-300). Boxes are per-triangle min/max.
 #include "bvh_internal.hpp"
 
+#include <algorithm>
+
 namespace ohao {
 
 namespace {
@@ -83,7 +85,66 @@ __global__ void k_gather(const float* __restrict__ tv, const uint32_t* __restric
     recs[static_cast<size_t>(j) * 3 + 2] = make_float4(v[6], v[7], v[8], __uint_as_float(b));
 }
 
+// World box of instance i: min/max of its object-to-world transform applied
+// to every vertex of every triangle record of its BLAS (the same rounding as
+// the host: x' = ((m0*x + m1*y) + m2*z) + m3 per row), padded by 2^-20 of the
+// coordinate magnitude. Exact for the instance's geometry, where the 8
+// transformed corners of the BLAS box overestimate a rotated instance by up
+// to sqrt(3) per axis. One block per instance.
+__global__ void k_instance_boxes(const float* __restrict__ o2w, const uint2* __restrict__ span,
+                                 const float4* __restrict__ recs, uint32_t n, float* __restrict__ boxes) {
+    __shared__ float red[6][32];
+    for (uint32_t i = blockIdx.x; i < n; i += gridDim.x) {
+        float m[12];
+#pragma unroll
+        for (int k = 0; k < 12; ++k) m[k] = o2w[static_cast<size_t>(i) * 12 + k];
+        float v[6] = {INFINITY, INFINITY, INFINITY, -INFINITY, -INFINITY, -INFINITY};
+        const uint2 sp = span[i];
+        for (uint32_t t = threadIdx.x; t < sp.y; t += blockDim.x) {
+            const float4* r = recs + (static_cast<size_t>(sp.x) + t) * 3;
+#pragma unroll
+            for (int q = 0; q < 3; ++q) {
+                const float4 p = r[q];
+#pragma unroll
+                for (int a = 0; a < 3; ++a) {
+                    const float w = ((m[a * 4] * p.x + m[a * 4 + 1] * p.y) + m[a * 4 + 2] * p.z) + m[a * 4 + 3];
+                    v[a] = fminf(v[a], w);
+                    v[3 + a] = fmaxf(v[3 + a], w);
+                }
+            }
+        }
+#pragma unroll
+        for (int k = 0; k < 6; ++k)
+            for (int off = 16; off > 0; off >>= 1) {
+                const float o = __shfl_down_sync(0xFFFFFFFFu, v[k], off);
+                v[k] = k < 3 ? fminf(v[k], o) : fmaxf(v[k], o);
+            }
+        const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+        if (lane == 0)
+            for (int k = 0; k < 6; ++k) red[k][warp] = v[k];
+        __syncthreads();
+        if (threadIdx.x == 0) {
+            const int nw = static_cast<int>(blockDim.x >> 5);
+            for (int w = 1; w < nw; ++w)
+                for (int k = 0; k < 6; ++k) v[k] = k < 3 ? fminf(v[k], red[k][w]) : fmaxf(v[k], red[k][w]);
+            for (int a = 0; a < 3; ++a) {
+                const float pad = (fabsf(v[a]) + fabsf(v[3 + a])) * 0x1p-20f;
+                boxes[static_cast<size_t>(i) * 6 + a] = v[a] - pad;
+                boxes[static_cast<size_t>(i) * 6 + 3 + a] = v[3 + a] + pad;
+            }
+        }
+        __syncthreads();
+    }
+}
+
 }  // namespace
+
+void launch_instance_boxes(const float* o2w, const uint32_t* span, const float4* recs, uint32_t n, float* boxes,
+                           cudaStream_t st) {
+    if (n == 0) return;
+    k_instance_boxes<<<std::min<uint32_t>(n, 65535u), 256, 0, st>>>(o2w, reinterpret_cast<const uint2*>(span), recs,
+                                                                    n, boxes);
+}
 
 void launch_flat_triangles(const float* pos, const uint32_t* indices, const uint32_t* inst_first_index,
                            const uint32_t* inst_tri_offset, const float* inst_o2w, uint32_t n_inst, uint32_t total,

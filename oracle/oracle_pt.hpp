@@ -193,7 +193,7 @@ struct Scene {
             for (uint32_t ii = 0; ii < instances.size(); ++ii) {
                 const Instance& in = instances[ii];
                 if (!(in.mask & 0xFFu) || blases[in.blas].tris.empty()) continue;
-                iboxes.push_back(instance_world_box(in, blases[in.blas].box));
+                iboxes.push_back(instance_world_box(in, blases[in.blas].tris));
                 ids.push_back(ii);
             }
             tlas = WideBuilder(iboxes).build();
@@ -202,14 +202,20 @@ struct Scene {
         }
     }
 
-    static Box instance_world_box(const Instance& in, const Box& ob) {
+    // World box of an instance: min/max of its transform applied to every
+    // vertex of its BLAS's triangle records, padded by 2^-20 of the
+    // coordinate magnitude so that rounding in the transform cannot exclude
+    // geometry.
+    static Box instance_world_box(const Instance& in, const std::vector<TriRec>& tris) {
         Box wb = box_empty();
-        if (!(ob.lo[0] <= ob.hi[0])) return wb;
-        for (int c = 0; c < 8; ++c) {
-            float p[3] = {(c & 1) ? ob.hi[0] : ob.lo[0], (c & 2) ? ob.hi[1] : ob.lo[1], (c & 4) ? ob.hi[2] : ob.lo[2]};
-            float w[3];
-            affine_xform_point(in.xform, p, w);
-            for (int a = 0; a < 3; ++a) { wb.lo[a] = std::min(wb.lo[a], w[a]); wb.hi[a] = std::max(wb.hi[a], w[a]); }
+        if (tris.empty()) return wb;
+        for (const TriRec& r : tris) {
+            const float* vs[3] = {r.v0, r.v1, r.v2};
+            for (int k = 0; k < 3; ++k) {
+                float w[3];
+                affine_xform_point(in.xform, vs[k], w);
+                for (int a = 0; a < 3; ++a) { wb.lo[a] = std::min(wb.lo[a], w[a]); wb.hi[a] = std::max(wb.hi[a], w[a]); }
+            }
         }
         for (int a = 0; a < 3; ++a) {
             float pad = (std::fabs(wb.lo[a]) + std::fabs(wb.hi[a])) * 0x1p-20f;
