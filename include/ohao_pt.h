@@ -99,6 +99,12 @@ typedef struct ohao_pt_view {
 /* flag bits keep the reference's PT_FLAG values (pt_raygen.rgen:56-60) */
 #define OHAO_PT_FLAG_FIREFLY_CLAMP (1u << 2)
 #define OHAO_PT_FLAG_ENV_FIXED_V (1u << 8)   /* not reference: un-mirrored env lookup */
+/* Not the offline reference estimator: the first specular bounce (stage B)
+ * draws the half-vector from the GGX distribution of visible normals with
+ * weight F * G2/G1 (pt_raygen_realtime.rgen:723-800, ggx_aniso.glsl:56-133)
+ * instead of the roughness-scaled cosine jitter; not differentiated by
+ * ohao_pt_backward / ohao_pt_adjoint. */
+#define OHAO_PT_FLAG_GGX_VNDF (1u << 9)
 #define OHAO_PT_FLAG_PROFILE (1u << 16)      /* record per-kernel CUDA-event times */
 /* ohao_pt_adjoint: replay the gradient with fresh samples (sample indices
  * from sample_index_base + spp) instead of the rendered ones, so that it

@@ -29,6 +29,7 @@ STATUS_NAMES = {0: "OK", -1: "INVALID_ARG", -2: "OOM", -3: "CUDA_ERROR", -4: "TI
 SAMPLER_PCG, SAMPLER_SOBOL = 0, 1
 FLAG_FIREFLY_CLAMP = 1 << 2
 FLAG_ENV_FIXED_V = 1 << 8
+FLAG_GGX_VNDF = 1 << 9        # VNDF sampling of the first specular bounce (not the offline estimator)
 FLAG_PROFILE = 1 << 16
 FLAG_ADJOINT_DECORRELATE = 1 << 17
 MODE_AUTO, MODE_WAVEFRONT, MODE_PERSISTENT = 0, 1, 2

@@ -697,6 +697,8 @@ static ohao_status validate_backward(ohao_pt_ctx* ctx, const ohao_pt_view* views
         return fail(ctx, OHAO_ERR_INVALID_ARG, "backward: the firefly clamp is not differentiable; clear the flag");
     if (st->max_bounces > ohao::adjoint_max_bounces())
         return fail(ctx, OHAO_ERR_INVALID_ARG, "backward: max_bounces above 16");
+    if (st->flags & OHAO_PT_FLAG_GGX_VNDF)
+        return fail(ctx, OHAO_ERR_INVALID_ARG, "backward: the replay differentiates the offline estimator; clear GGX_VNDF");
     return OHAO_OK;
 }
 

@@ -42,6 +42,7 @@ __constant__ uint32_t c_sobol_dirs[128] = {
 constexpr uint32_t kSamplerPCG = 0, kSamplerSobol = 1;
 constexpr uint32_t kFlagFirefly = 1u << 2;
 constexpr uint32_t kFlagEnvFixedV = 1u << 8;
+constexpr uint32_t kFlagVndf = 1u << 9;
 
 // ---------------------------------------------------------------------------
 // samplers (sampler_pcg.glsl:9-29, sampler_sobol.glsl:13-82)
@@ -278,6 +279,40 @@ OHAO_D V3 cos_hemi(V3 N, float u0, float u1) {
     sincos_f(phi, &sp, &cp);
     return normalize(T * r * cp + B * r * sp + N * sqrtf(gmaxf(0.0f, 1.0f - r * r)));
 }
+// GGX visible-normal sampling and its Smith terms (ggx_aniso.glsl:56-133,
+// Heitz 2018), alpha = roughness^2; inversesqrt as 1 / sqrt.
+OHAO_D float ggx_d_iso(float NdotH, float alpha) {
+    const float a2 = alpha * alpha;
+    const float denom = NdotH * NdotH * (a2 - 1.0f) + 1.0f;
+    return a2 / (3.14159265f * denom * denom + 1e-8f);
+}
+OHAO_D float smith_lambda(float c, float alpha) {
+    const float c2 = c * c;
+    const float tan2 = gmaxf(0.0f, 1.0f - c2) / gmaxf(c2, 1e-8f);
+    return 0.5f * (-1.0f + sqrtf(1.0f + alpha * alpha * tan2));
+}
+OHAO_D float smith_g1(float c, float alpha) { return 1.0f / (1.0f + smith_lambda(c, alpha)); }
+OHAO_D float smith_g2_over_g1(float NdotV, float NdotL, float alpha) {
+    const float lv = smith_lambda(NdotV, alpha), ll = smith_lambda(NdotL, alpha);
+    return (1.0f + lv) / (1.0f + lv + ll + 1e-8f);
+}
+OHAO_D V3 sample_vndf(V3 Ve, float ax, float ay, float u0, float u1) {
+    const V3 Vh = normalize(v3(ax * Ve.x, ay * Ve.y, Ve.z));
+    const float lensq = Vh.x * Vh.x + Vh.y * Vh.y;
+    const V3 T1 = lensq > 0.0f ? v3(-Vh.y, Vh.x, 0.0f) * (1.0f / sqrtf(lensq)) : v3(1.0f, 0.0f, 0.0f);
+    const V3 T2 = cross(Vh, T1);
+    const float r = sqrtf(u0);
+    const float phi = 2.0f * 3.14159265f * u1;
+    float sp, cp;
+    sincos_f(phi, &sp, &cp);
+    const float t1 = r * cp;
+    float t2 = r * sp;
+    const float s = 0.5f * (1.0f + Vh.z);
+    t2 = (1.0f - s) * sqrtf(gmaxf(0.0f, 1.0f - t1 * t1)) + s * t2;
+    const V3 Nh = T1 * t1 + T2 * t2 + Vh * sqrtf(gmaxf(0.0f, 1.0f - t1 * t1 - t2 * t2));
+    return normalize(v3(ax * Nh.x, ay * Nh.y, gmaxf(0.0f, Nh.z)));
+}
+
 // ggx_aniso.glsl:31-55
 OHAO_D float ggxD(const PathParams& pp, V3 N, V3 H, float NdotH, float rough) {
     const float an = pp.aniso;
@@ -668,18 +703,57 @@ OHAO_D bool path_step(const DScene& sc, const PathParams& pp, const ViewParams& 
         if (sc.has_cdf) nee_env(sc, pp, rng, dim, P, N, ps.rd, alb, rough, metal, F0, nullptr, qE);
         // stage B init (505-543)
         const V3 inDir = ps.rd;
-        const V3 sd = spec_dir(rng, dim, inDir, N, rough);
-        ps.thr = vmix(v3s(1.0f), alb, metal);
-        if (rough < 0.05f) {
-            ps.last_pdf = 1.0f;
-            ps.delta = true;
+        V3 sd;
+        if (pp.flags & kFlagVndf) {
+            // VNDF mode (pt_raygen_realtime.rgen:723-800)
+            const V3 V = normalize(-inDir);
+            const float NdotV = gmaxf(dot(N, V), 1e-4f);
+            const float alpha = rough * rough;
+            if (rough < 0.02f) {
+                sd = reflect(inDir, N);
+                ps.thr = F0 + (1.0f - F0) * pow5f(1.0f - NdotV);
+                ps.last_pdf = 1.0f;
+                ps.delta = true;
+            } else {
+                const V3 up = fabsf(N.y) < 0.999f ? v3(0.0f, 1.0f, 0.0f) : v3(1.0f, 0.0f, 0.0f);
+                const V3 T = normalize(cross(up, N));
+                const V3 B = cross(N, T);
+                const V3 Vloc = v3(dot(V, T), dot(V, B), dot(V, N));
+                const float u0 = rng.s1(dim), u1 = rng.s1(dim + 1);
+                dim += 2;
+                const V3 Hloc = sample_vndf(Vloc, alpha, alpha, u0, u1);
+                V3 H = normalize(T * Hloc.x + B * Hloc.y + N * Hloc.z);
+                V3 refl = reflect(-V, H);
+                if (dot(refl, N) <= 0.0f) {
+                    refl = reflect(inDir, N);
+                    H = N;
+                }
+                refl = normalize(refl);
+                sd = refl;
+                const float NdotL = gmaxf(dot(N, refl), 1e-4f);
+                const float NdotH = gmaxf(dot(N, H), 1e-4f);
+                const float VdotH = gmaxf(dot(V, H), 1e-4f);
+                const V3 F = F0 + (1.0f - F0) * pow5f(1.0f - VdotH);
+                ps.thr = F * smith_g2_over_g1(NdotV, NdotL, alpha);
+                const float D = ggx_d_iso(NdotH, alpha);
+                const float G1V = smith_g1(NdotV, alpha);
+                ps.last_pdf = G1V * D / (4.0f * NdotV) + 1e-6f;
+                ps.delta = false;
+            }
         } else {
-            const V3 Hs = normalize(-inDir + sd);
-            const float NdotHs = gmaxf(dot(N, Hs), 0.001f);
-            const float VdotHs = gmaxf(dot(-inDir, Hs), 0.001f);
-            const float Ds = ggxD(pp, N, Hs, NdotHs, rough);
-            ps.last_pdf = Ds * NdotHs / (4.0f * VdotHs + 1e-4f);
-            ps.delta = false;
+            sd = spec_dir(rng, dim, inDir, N, rough);
+            ps.thr = vmix(v3s(1.0f), alb, metal);
+            if (rough < 0.05f) {
+                ps.last_pdf = 1.0f;
+                ps.delta = true;
+            } else {
+                const V3 Hs = normalize(-inDir + sd);
+                const float NdotHs = gmaxf(dot(N, Hs), 0.001f);
+                const float VdotHs = gmaxf(dot(-inDir, Hs), 0.001f);
+                const float Ds = ggxD(pp, N, Hs, NdotHs, rough);
+                ps.last_pdf = Ds * NdotHs / (4.0f * VdotHs + 1e-4f);
+                ps.delta = false;
+            }
         }
         ps.fhP = P;
         ps.fhN = N;

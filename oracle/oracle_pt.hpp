@@ -32,6 +32,7 @@ namespace orc {
 
 constexpr uint32_t kFlagFireflyClamp = 1u << 2;   // pt_raygen.rgen:58
 constexpr uint32_t kFlagEnvFixedV = 1u << 8;      // "fixed" env lookup mode (not reference)
+constexpr uint32_t kFlagVndf = 1u << 9;           // VNDF stage-B sampling (pt_raygen_realtime.rgen:723-800)
 constexpr uint32_t kSamplerPCG = 0, kSamplerSobol = 1;
 constexpr uint32_t kNoTex = 0xFFFFFFFFu;
 
@@ -842,6 +843,38 @@ struct PathTracer {
         return out;
     }
 
+    // GGX visible-normal sampling and its Smith terms (ggx_aniso.glsl:56-133,
+    // Heitz 2018), alpha = roughness^2; inversesqrt as 1 / sqrt.
+    static R ggx_d_iso(R NdotH, R alpha) {
+        R a2 = alpha * alpha;
+        R denom = NdotH * NdotH * (a2 - R(1)) + R(1);
+        return a2 / (R(3.14159265f) * denom * denom + R(1e-8f));
+    }
+    static R smith_lambda(R c, R alpha) {
+        R c2 = c * c;
+        R tan2 = gmax(R(0), R(1) - c2) / gmax(c2, R(1e-8f));
+        return R(0.5f) * (R(-1) + m_sqrt(R(1) + alpha * alpha * tan2));
+    }
+    static R smith_g1(R c, R alpha) { return R(1) / (R(1) + smith_lambda(c, alpha)); }
+    static R smith_g2_over_g1(R NdotV, R NdotL, R alpha) {
+        R lv = smith_lambda(NdotV, alpha), ll = smith_lambda(NdotL, alpha);
+        return (R(1) + lv) / (R(1) + lv + ll + R(1e-8f));
+    }
+    static V3<R> sample_vndf(V3<R> Ve, R ax, R ay, R u0, R u1) {
+        V3<R> Vh = normalize(V3<R>(ax * Ve.x, ay * Ve.y, Ve.z));
+        R lensq = Vh.x * Vh.x + Vh.y * Vh.y;
+        V3<R> T1 = lensq > R(0) ? V3<R>(-Vh.y, Vh.x, R(0)) * (R(1) / m_sqrt(lensq)) : V3<R>(R(1), R(0), R(0));
+        V3<R> T2 = cross(Vh, T1);
+        R r = m_sqrt(u0);
+        R phi = R(2.0f) * R(3.14159265f) * u1;
+        R t1 = r * m_cos(phi);
+        R t2 = r * m_sin(phi);
+        R s = R(0.5f) * (R(1) + Vh.z);
+        t2 = (R(1) - s) * m_sqrt(gmax(R(0), R(1) - t1 * t1)) + s * t2;
+        V3<R> Nh = T1 * t1 + T2 * t2 + Vh * m_sqrt(gmax(R(0), R(1) - t1 * t1 - t2 * t2));
+        return normalize(V3<R>(ax * Nh.x, ay * Nh.y, gmax(R(0), Nh.z)));
+    }
+
     // Specular-lobe "jitter" sample (pt_raygen.rgen:516-525, 784-793).
     V3<R> spec_dir(Sampler& smp, uint32_t& dim, V3<R> inDir, V3<R> N, R rough) const {
         V3<R> refl = reflect(inDir, N);
@@ -994,17 +1027,50 @@ struct PathTracer {
                 sp = gmix(sp, R(1), metal);
                 (void)sp;
                 V3<R> inDir = rayDir;
-                specDir = spec_dir(smp, dim, rayDir, N, rough);
-                specThr = vmix(V3<R>(R(1)), alb, metal);
-                if (rough < R(0.05f)) {
-                    specPdf = R(1); specDelta = true;
+                if (st.flags & kFlagVndf) {
+                    // VNDF mode (pt_raygen_realtime.rgen:723-800)
+                    V3<R> V = normalize(-inDir);
+                    R NdotV = gmax(dot(N, V), R(1e-4f));
+                    R alpha = rough * rough;
+                    if (rough < R(0.02f)) {
+                        specDir = reflect(inDir, N);
+                        specThr = F0 + (R(1) - F0) * pow5(R(1) - NdotV);
+                        specPdf = R(1); specDelta = true;
+                    } else {
+                        V3<R> up = std::fabs(N.y) < R(0.999f) ? V3<R>(R(0), R(1), R(0)) : V3<R>(R(1), R(0), R(0));
+                        V3<R> T = normalize(cross(up, N));
+                        V3<R> B = cross(N, T);
+                        V3<R> Vloc(dot(V, T), dot(V, B), dot(V, N));
+                        R u0 = R(smp.s1(dim)), u1 = R(smp.s1(dim + 1)); dim += 2;
+                        V3<R> Hloc = sample_vndf(Vloc, alpha, alpha, u0, u1);
+                        V3<R> H = normalize(T * Hloc.x + B * Hloc.y + N * Hloc.z);
+                        V3<R> refl = reflect(-V, H);
+                        if (dot(refl, N) <= R(0)) { refl = reflect(inDir, N); H = N; }
+                        refl = normalize(refl);
+                        specDir = refl;
+                        R NdotL = gmax(dot(N, refl), R(1e-4f));
+                        R NdotH = gmax(dot(N, H), R(1e-4f));
+                        R VdotH = gmax(dot(V, H), R(1e-4f));
+                        V3<R> F = F0 + (R(1) - F0) * pow5(R(1) - VdotH);
+                        specThr = F * smith_g2_over_g1(NdotV, NdotL, alpha);
+                        R D = ggx_d_iso(NdotH, alpha);
+                        R G1V = smith_g1(NdotV, alpha);
+                        specPdf = G1V * D / (R(4) * NdotV) + R(1e-6f);
+                        specDelta = false;
+                    }
                 } else {
-                    V3<R> Hs = normalize(-inDir + specDir);
-                    R NdotHs = gmax(dot(N, Hs), R(0.001f));
-                    R VdotHs = gmax(dot(-inDir, Hs), R(0.001f));
-                    R Ds = ggxD(N, Hs, NdotHs, rough);
-                    specPdf = Ds * NdotHs / (R(4) * VdotHs + R(1e-4f));
-                    specDelta = false;
+                    specDir = spec_dir(smp, dim, rayDir, N, rough);
+                    specThr = vmix(V3<R>(R(1)), alb, metal);
+                    if (rough < R(0.05f)) {
+                        specPdf = R(1); specDelta = true;
+                    } else {
+                        V3<R> Hs = normalize(-inDir + specDir);
+                        R NdotHs = gmax(dot(N, Hs), R(0.001f));
+                        R VdotHs = gmax(dot(-inDir, Hs), R(0.001f));
+                        R Ds = ggxD(N, Hs, NdotHs, rough);
+                        specPdf = Ds * NdotHs / (R(4) * VdotHs + R(1e-4f));
+                        specDelta = false;
+                    }
                 }
             }
             chain(smp, dim, true, P + N * R(0.01f), specDir, specThr, specPdf, specDelta, radiance, ts);

@@ -169,7 +169,8 @@ def test_backward_rejects_firefly_clamp_and_deep_paths(gpu_lib):
     pt = H.gpu_tracer(og, sd)
     view = sd.views[0]
     g = torch.zeros((view.width * view.height, 4), dtype=torch.float32, device="cuda")
-    for kw in (dict(flags=og.FLAG_FIREFLY_CLAMP, clamp_luminance=4.0), dict(max_bounces=17)):
+    for kw in (dict(flags=og.FLAG_FIREFLY_CLAMP, clamp_luminance=4.0), dict(max_bounces=17),
+               dict(flags=og.FLAG_GGX_VNDF)):
         with pytest.raises(og.OhaoError):
             pt.backward([og.make_view(view)], og.make_settings(spp=1, **kw), [g])
 

@@ -101,6 +101,24 @@ def test_render_env_paths(gpu_lib, oracle, sampler):
     assert np.array_equal(acc.cpu().numpy(), oracle.accumulate(o))
 
 
+@pytest.mark.parametrize("sampler", [0, 1])
+def test_render_vndf_mode_paths(gpu_lib, oracle, sampler):
+    """The VNDF stage-B estimator mode (OHAO_PT_FLAG_GGX_VNDF) per path
+    against the oracle, on a scene with smooth and rough metals and
+    dielectrics under an environment with a sun."""
+    sd = small_env_scene(freq=16)
+    pt = gpu_tracer(gpu_lib, sd)
+    orc = oracle.OracleScene(sd)
+    v = sd.views[0]
+    fl = gpu_lib.FLAG_GGX_VNDF
+    g, acc, _ = render_paths_gpu(gpu_lib, pt, v, 3, dict(max_bounces=4, sampler=sampler, flags=fl))
+    o = orc.render_paths(v, dict(max_bounces=4, sampler=sampler, flags=fl), 0, 3)
+    assert_paths_match(g, o, "vndf")
+    assert np.array_equal(acc.cpu().numpy(), oracle.accumulate(o))
+    plain = orc.render_paths(v, dict(max_bounces=4, sampler=sampler), 0, 3)
+    assert not np.array_equal(plain, o)   # the flag changes the estimator
+
+
 def test_render_two_level_paths(gpu_lib, oracle):
     sd = small_instanced(side=24)
     pt = gpu_tracer(gpu_lib, sd, flatten_limit=1)

@@ -134,6 +134,33 @@ def test_fp32_fp64_integrator_agree_cornell(oracle):
     assert abs(p32.mean() - p64.mean()) / p64.mean() < 1e-3
 
 
+def test_fp32_fp64_agree_vndf_mode(oracle):
+    """The VNDF stage-B mode in FP32 and FP64 on a scene of smooth and rough
+    metals and dielectrics; the flag changes the estimator."""
+    pos, nrm, uv, idx = scenes.displaced_sphere(8, seed=2)
+    b = scenes._Builder()
+    rng = np.random.default_rng(3)
+    nt = idx.shape[0]
+    mats = scenes._random_materials(rng, nt + 1)
+    mats[nt] = scenes.material((0.5, 0.5, 0.5), rough=0.3)
+    b.add(pos, nrm, uv, idx, np.arange(nt, dtype=np.uint32))
+    scenes._ground(b, -1.05, 6.0, nt)
+    P, N, U, I, M = b.arrays()
+    env = scenes.sky_env(64, 32, seed=2, peak=50.0, radius_deg=3.0)
+    view = scenes.look_at_view((0, 0.6, 3.2), (0, -0.1, 0), width=24, height=16)
+    sd = scenes.SceneData("vndf", P, N, U, I, M, mats, np.zeros((0, 20), np.float32), env, 1.0, [(0, I.size)],
+                          scenes.identity_instance(1), [view], spp=4, max_bounces=3)
+    sc = oracle.OracleScene(sd)
+    st = dict(max_bounces=3, sampler=1, flags=1 << 9)
+    p32 = sc.render_paths(view, st, 0, 4)
+    p64 = sc.render_paths(view, st, 0, 4, fp64=True)
+    assert np.isfinite(p32).all() and (p32 >= 0).all()
+    rel = np.abs(p32 - p64) / np.maximum(np.abs(p64), 1e-3)
+    assert np.mean(rel < 1e-3) > 0.98
+    assert abs(p32.mean() - p64.mean()) / p64.mean() < 2e-3
+    assert not np.array_equal(p32, sc.render_paths(view, dict(max_bounces=3, sampler=1), 0, 4))
+
+
 @pytest.mark.parametrize("sampler", [0, 1])
 def test_oracle_render_env_scene(oracle, sampler):
     pos, nrm, uv, idx = scenes.displaced_sphere(8, seed=1)
