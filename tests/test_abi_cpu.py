@@ -72,3 +72,27 @@ def test_no_device_reports_status(og):
         pytest.skip("a CUDA device is present")
     with pytest.raises(og.OhaoError):
         og.PathTracer()
+
+
+def test_no_device_reports_status_denoiser(og):
+    import torch
+    if torch.cuda.is_available():
+        pytest.skip("a CUDA device is present")
+    from ohao_engine_gb300.denoise import Denoiser
+    with pytest.raises(og.OhaoError):
+        Denoiser(max_pixels=1024, seed=1)
+
+
+def test_launch_shapes_listed_without_device(og):
+    """The persistent launch shapes are a host table: listed without a GPU,
+    each name unique, the persistent-warp traversal among them."""
+    L = og.load_library()
+    names, i = [], 0
+    while True:
+        n = L.ohao_pt_launch_config_at(i)
+        if n is None:
+            break
+        names.append(n.decode())
+        i += 1
+    assert len(names) == len(set(names)) >= 5
+    assert any("fetch" in n for n in names) and any("sorted" in n for n in names)
