@@ -75,8 +75,6 @@ struct ohao_pt_ctx {
     DevBuf pos, normals, uvs, indices, mat_ids, mats, lights, env, marg, cond, albedo_map;
     uint32_t nverts = 0, ntris = 0, nmats = 0, nlights = 0;
     uint32_t max_mat_id = 0;              // largest per-triangle material id
-    std::vector<float> host_pos;          // packed, for host-side instance boxes
-    std::vector<uint32_t> host_indices;
     uint32_t env_w = 0, env_h = 0;
     bool has_env = false, has_cdf = false;
     float env_intensity = 1.0f;
@@ -258,14 +256,18 @@ ohao_status ohao_pt_set_geometry(ohao_pt_ctx* ctx, const float* pos, uint32_t po
         return fail(ctx, OHAO_ERR_INVALID_ARG, "set_geometry: null array or stride < 12");
     for (size_t i = 0; i < static_cast<size_t>(ntris) * 3; ++i)
         if (indices[i] >= nverts) return fail(ctx, OHAO_ERR_INVALID_ARG, "set_geometry: index out of range");
-    ctx->host_pos.resize(static_cast<size_t>(nverts) * 3);
+    // a failed upload below leaves buffers reallocated or released: nothing
+    // renders from them until the next successful set_geometry + build
+    ctx->built = false;
+    ctx->nverts = ctx->ntris = 0;
+    // positions are stored packed (12 B per vertex) whatever the caller's stride
+    std::vector<float> packed(static_cast<size_t>(nverts) * 3);
     const auto* pb = reinterpret_cast<const uint8_t*>(pos);
-    for (uint32_t i = 0; i < nverts; ++i) std::memcpy(&ctx->host_pos[3 * static_cast<size_t>(i)], pb + static_cast<size_t>(i) * pos_stride_bytes, 12);
-    ctx->host_indices.assign(indices, indices + static_cast<size_t>(ntris) * 3);
+    for (uint32_t i = 0; i < nverts; ++i) std::memcpy(&packed[3 * static_cast<size_t>(i)], pb + static_cast<size_t>(i) * pos_stride_bytes, 12);
     std::vector<float> uvz;
     if (!uv2) uvz.assign(static_cast<size_t>(nverts) * 2, 0.0f);
     ohao_status s;
-    if ((s = upload(ctx, ctx->pos, ctx->host_pos.data(), ctx->host_pos.size() * 4, "positions")) != OHAO_OK) return s;
+    if ((s = upload(ctx, ctx->pos, packed.data(), packed.size() * 4, "positions")) != OHAO_OK) return s;
     if ((s = upload(ctx, ctx->normals, normal4, static_cast<size_t>(nverts) * 16, "normals")) != OHAO_OK) return s;
     if ((s = upload(ctx, ctx->uvs, uv2 ? uv2 : uvz.data(), static_cast<size_t>(nverts) * 8, "uvs")) != OHAO_OK) return s;
     if ((s = upload(ctx, ctx->indices, indices, static_cast<size_t>(ntris) * 12, "indices")) != OHAO_OK) return s;
@@ -304,6 +306,7 @@ ohao_status ohao_pt_build(ohao_pt_ctx* ctx, ohao_stream stream) {
     if (!ctx) return OHAO_ERR_INVALID_ARG;
     cudaStream_t st = reinterpret_cast<cudaStream_t>(stream);
     CK(cudaSetDevice(ctx->device), "set device");
+    ctx->built = false;   // a build that fails part way leaves no usable structure
     const uint32_t ninst = static_cast<uint32_t>(ctx->instances.size());
     // per-instance device records
     std::vector<ohao::DInst> di(std::max(ninst, 1u));
@@ -451,7 +454,7 @@ ohao_status ohao_pt_set_materials(ohao_pt_ctx* ctx, const float* m, uint32_t n) 
             return fail(ctx, OHAO_ERR_UNSUPPORTED, "set_materials: bindless textures are not supported (only diffuse slot 0 = tile albedo map)");
     }
     ohao_status s = upload(ctx, ctx->mats, m, static_cast<size_t>(n) * 48, "materials");
-    if (s == OHAO_OK) ctx->nmats = n;
+    ctx->nmats = s == OHAO_OK ? n : 0;   // a failed upload may have released the table
     return s;
 }
 
@@ -466,7 +469,7 @@ ohao_status ohao_pt_set_lights(ohao_pt_ctx* ctx, const ohao_gpu_light* l, uint32
     if (!ctx || (n && !l)) return OHAO_ERR_INVALID_ARG;
     if (n > 64) return fail(ctx, OHAO_ERR_INVALID_ARG, "set_lights: at most 64 lights (MAX_GPU_LIGHTS)");
     ohao_status s = upload(ctx, ctx->lights, l, static_cast<size_t>(n) * 80, "lights");
-    if (s == OHAO_OK) ctx->nlights = n;
+    ctx->nlights = s == OHAO_OK ? n : 0;
     return s;
 }
 
@@ -479,12 +482,14 @@ ohao_status ohao_pt_set_env(ohao_pt_ctx* ctx, const float* rgba, uint32_t w, uin
         ctx->env_w = ctx->env_h = 0;
         return OHAO_OK;
     }
+    ctx->has_env = ctx->has_cdf = false;   // until every upload below has succeeded
+    ctx->env_w = ctx->env_h = 0;
     ohao_status s = upload(ctx, ctx->env, rgba, static_cast<size_t>(w) * h * 16, "env");
     if (s != OHAO_OK) return s;
-    ctx->has_cdf = marg && cond;
-    if (ctx->has_cdf) {
+    if (marg && cond) {
         if ((s = upload(ctx, ctx->marg, marg, static_cast<size_t>(h) * 4, "env marginal")) != OHAO_OK) return s;
         if ((s = upload(ctx, ctx->cond, cond, static_cast<size_t>(w) * h * 4, "env conditional")) != OHAO_OK) return s;
+        ctx->has_cdf = true;
     }
     ctx->has_env = true;
     ctx->env_w = w;
@@ -497,7 +502,8 @@ ohao_status ohao_pt_set_albedo_map(ohao_pt_ctx* ctx, const float* rgb, uint32_t 
     if (!ctx) return OHAO_ERR_INVALID_ARG;
     if (!rgb || !w || !h) { ctx->map_w = ctx->map_h = 0; return OHAO_OK; }
     ohao_status s = upload(ctx, ctx->albedo_map, rgb, static_cast<size_t>(w) * h * 12, "albedo map");
-    if (s == OHAO_OK) { ctx->map_w = w; ctx->map_h = h; }
+    ctx->map_w = s == OHAO_OK ? w : 0;
+    ctx->map_h = s == OHAO_OK ? h : 0;
     return s;
 }
 
