@@ -307,6 +307,10 @@ ohao_status ohao_pt_build(ohao_pt_ctx* ctx, ohao_stream stream) {
     cudaStream_t st = reinterpret_cast<cudaStream_t>(stream);
     CK(cudaSetDevice(ctx->device), "set device");
     ctx->built = false;   // a build that fails part way leaves no usable structure
+    // BLAS ranges were checked when created; geometry set since may be smaller
+    for (const auto& b : ctx->blas)
+        if (static_cast<uint64_t>(b.first_index) + b.index_count > static_cast<uint64_t>(ctx->ntris) * 3)
+            return fail(ctx, OHAO_ERR_INVALID_ARG, "build: a BLAS index range lies outside the current geometry");
     const uint32_t ninst = static_cast<uint32_t>(ctx->instances.size());
     // per-instance device records
     std::vector<ohao::DInst> di(std::max(ninst, 1u));

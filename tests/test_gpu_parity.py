@@ -194,6 +194,35 @@ def test_errors_are_status_codes(gpu_lib):
     assert e.value.status == -6
 
 
+def test_build_rechecks_blas_ranges(gpu_lib):
+    """A BLAS created over the old geometry that a smaller new geometry no
+    longer covers: the build reports it instead of reading past the index
+    buffer, nothing renders from that state, and restoring the geometry
+    builds again."""
+    og = gpu_lib
+    sd = scenes.cornell(8, 8, 1)
+    idx = np.asarray(sd.indices, np.uint32)
+    mids = np.asarray(sd.mat_ids, np.uint32)
+    pt = og.PathTracer()
+    pt.set_geometry(sd.pos, sd.normals, sd.uvs, idx, mids)
+    b = pt.create_blas(54, 54)                       # the second half of the 36 triangles
+    inst = scenes.identity_instance(1)
+    inst["blas"] = b
+    pt.set_instances(inst)
+    pt.set_materials(sd.materials)
+    pt.build()
+    pt.set_geometry(sd.pos, sd.normals, sd.uvs, idx[:54], mids[:18])
+    with pytest.raises(og.OhaoError) as e:
+        pt.build()
+    assert e.value.status == -1
+    with pytest.raises(og.OhaoError) as e:
+        pt.render([og.make_view(sd.views[0])], og.make_settings())
+    assert e.value.status == -5
+    pt.set_geometry(sd.pos, sd.normals, sd.uvs, idx, mids)
+    pt.build()
+    pt.close()
+
+
 def test_full_size_sphere_properties(gpu_lib, oracle):
     """1,003,522-triangle scene: bit-exact BVH, hits on 100k rays, per-path
     radiance on a seeded pixel subset of a 1920x1080 frame."""
