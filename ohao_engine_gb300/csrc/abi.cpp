@@ -446,8 +446,9 @@ ohao_status ohao_pt_build(ohao_pt_ctx* ctx, ohao_stream stream) {
     return OHAO_OK;
 }
 
-ohao_status ohao_pt_set_materials(ohao_pt_ctx* ctx, const float* m, uint32_t n) {
-    if (!ctx || (n && !m)) return OHAO_ERR_INVALID_ARG;
+// Texture slots of a 48-byte material record (layout_meta.hpp:20-58): only
+// "none" (0xFFFFFFFF) is accepted, and diffuse slot 0 = the tile albedo map.
+static bool material_textures_supported(const float* m, uint32_t n) {
     for (uint32_t i = 0; i < n; ++i) {
         uint32_t tex[4];
         std::memcpy(&tex[0], m + 12 * static_cast<size_t>(i) + 3, 4);   // diffuse
@@ -455,8 +456,15 @@ ohao_status ohao_pt_set_materials(ohao_pt_ctx* ctx, const float* m, uint32_t n) 
         std::memcpy(&tex[2], m + 12 * static_cast<size_t>(i) + 7, 4);   // emissive
         std::memcpy(&tex[3], m + 12 * static_cast<size_t>(i) + 8, 4);   // rough/metal
         if ((tex[0] != 0xFFFFFFFFu && tex[0] != 0u) || tex[1] != 0xFFFFFFFFu || tex[2] != 0xFFFFFFFFu || tex[3] != 0xFFFFFFFFu)
-            return fail(ctx, OHAO_ERR_UNSUPPORTED, "set_materials: bindless textures are not supported (only diffuse slot 0 = tile albedo map)");
+            return false;
     }
+    return true;
+}
+
+ohao_status ohao_pt_set_materials(ohao_pt_ctx* ctx, const float* m, uint32_t n) {
+    if (!ctx || (n && !m)) return OHAO_ERR_INVALID_ARG;
+    if (!material_textures_supported(m, n))
+        return fail(ctx, OHAO_ERR_UNSUPPORTED, "set_materials: bindless textures are not supported (only diffuse slot 0 = tile albedo map)");
     ohao_status s = upload(ctx, ctx->mats, m, static_cast<size_t>(n) * 48, "materials");
     ctx->nmats = s == OHAO_OK ? n : 0;   // a failed upload may have released the table
     return s;
@@ -465,6 +473,8 @@ ohao_status ohao_pt_set_materials(ohao_pt_ctx* ctx, const float* m, uint32_t n) 
 ohao_status ohao_pt_update_materials(ohao_pt_ctx* ctx, const float* m, uint32_t first, uint32_t n) {
     if (!ctx || (n && !m)) return OHAO_ERR_INVALID_ARG;
     if (static_cast<uint64_t>(first) + n > ctx->nmats) return fail(ctx, OHAO_ERR_INVALID_ARG, "update_materials: range outside the table");
+    if (!material_textures_supported(m, n))
+        return fail(ctx, OHAO_ERR_UNSUPPORTED, "update_materials: bindless textures are not supported (only diffuse slot 0 = tile albedo map)");
     if (n) CK(cudaMemcpy(ctx->mats.as<char>() + static_cast<size_t>(first) * 48, m, static_cast<size_t>(n) * 48, cudaMemcpyHostToDevice), "materials");
     return OHAO_OK;
 }

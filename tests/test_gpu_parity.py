@@ -192,6 +192,13 @@ def test_errors_are_status_codes(gpu_lib):
     with pytest.raises(og.OhaoError) as e:
         pt.set_materials(bad)
     assert e.value.status == -6
+    pt.set_materials(sd.materials)
+    with pytest.raises(og.OhaoError) as e:
+        pt.update_materials(bad[:1])
+    assert e.value.status == -6
+    with pytest.raises(og.OhaoError) as e:
+        pt.update_materials(sd.materials[:1], first=sd.materials.shape[0])
+    assert e.value.status == -1
 
 
 def test_build_rechecks_blas_ranges(gpu_lib):
