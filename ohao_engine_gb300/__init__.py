@@ -168,15 +168,61 @@ class EnvCDF:
         return self.width > 0 and self.height > 0 and self.marginal.size > 0
 
 
+def _buffer(a, elems: int, what: str, host: bool = False, floats: bool = True):
+    """Pointer value of a buffer that the kernels (or, with ``host``, the
+    library's copies) use without bounds checks: a contiguous array or tensor
+    of 4-byte elements (float32 unless ``floats`` is False), at least
+    ``elems`` long, on a CUDA device (in host memory with ``host``). A wrong
+    buffer raises ValueError here instead of faulting the device; raw integer
+    pointers pass unchecked."""
+    if a is None:
+        return None
+    if isinstance(a, np.ndarray):
+        if not host:
+            raise ValueError(f"{what}: a host array where a CUDA device buffer is needed")
+        ok = (a.flags.c_contiguous and a.flags.writeable and a.itemsize == 4
+              and (a.dtype == np.float32 or not floats) and a.size >= elems)
+        if not ok:
+            raise ValueError(f"{what}: needs a writable C-contiguous float32 array of at least {elems} elements "
+                             f"(got {a.shape} {a.dtype})")
+        return a.ctypes.data
+    if hasattr(a, "data_ptr"):
+        ok = (a.element_size() == 4 and (a.is_floating_point() or not floats) and a.is_contiguous()
+              and a.numel() >= elems)
+        if not ok:
+            raise ValueError(f"{what}: needs a contiguous {'float32' if floats else '4-byte'} tensor of at least "
+                             f"{elems} elements (got {tuple(a.shape)} {a.dtype})")
+        if bool(a.is_cuda) == host:
+            raise ValueError(f"{what}: needs a {'host' if host else 'CUDA device'} tensor (got one on {a.device})")
+        return a.data_ptr()
+    return int(a)
+
+
 def make_view(view, accum=None, history: int = 0, path_radiance=None, aov=None) -> View:
+    """One ``ohao_pt_view``. accum: RGBA32F per pixel; path_radiance: RGBA32F
+    per sample and pixel ([spp][pixel][4], for up to as many samples per call
+    as it holds); aov: AOV_FLOATS per pixel; all on the device."""
     v = View()
     v.inv_view[:] = [float(x) for x in np.asarray(view.inv_view, np.float32)]
     v.inv_proj[:] = [float(x) for x in np.asarray(view.inv_proj, np.float32)]
     v.width, v.height, v.history = int(view.width), int(view.height), int(history)
-    v.accum = _ptr(accum).value if accum is not None else None
-    v.path_radiance = _ptr(path_radiance).value if path_radiance is not None else None
-    v.aov = _ptr(aov).value if aov is not None else None
+    npix = v.width * v.height
+    v.accum = _buffer(accum, npix * 4, "accum")
+    v.path_radiance = _buffer(path_radiance, npix * 4, "path_radiance")
+    v.aov = _buffer(aov, npix * AOV_FLOATS, "aov")
+    if path_radiance is not None and hasattr(path_radiance, "numel") and npix:
+        v._path_samples = path_radiance.numel() // (npix * 4)
     return v
+
+
+def _view_array(views, settings: "Settings"):
+    """ctypes array of the views, after checking that every per-sample
+    radiance buffer holds the call's samples."""
+    for v in views:
+        ns = getattr(v, "_path_samples", None)
+        if ns is not None and settings.spp > ns:
+            raise ValueError(f"path_radiance holds {ns} samples per pixel, the call renders {settings.spp}")
+    return (View * len(views))(*views)
 
 
 def make_settings(spp=1, max_bounces=4, sample_index_base=0, sampler=SAMPLER_PCG, flags=0, clamp_luminance=0.0,
@@ -201,6 +247,8 @@ class PathTracer:
         self.h = h
         self.device = device
         self._keep = {}
+        self._nmats = 0        # material table size (gradient buffer bounds)
+        self._map_floats = 0   # tile albedo map floats (gradient buffer bounds)
 
     def close(self):
         if getattr(self, "h", None):
@@ -248,6 +296,7 @@ class PathTracer:
     def set_materials(self, mats):
         m = np.ascontiguousarray(mats, np.float32).reshape(-1, 12)
         self._ck(self._L.ohao_pt_set_materials(self.h, _ptr(m), m.shape[0]), "set_materials")
+        self._nmats = m.shape[0]
 
     def update_materials(self, mats, first: int = 0):
         m = np.ascontiguousarray(mats, np.float32).reshape(-1, 12)
@@ -273,6 +322,7 @@ class PathTracer:
     def set_albedo_map(self, rgb):
         m = np.ascontiguousarray(rgb, np.float32)
         self._ck(self._L.ohao_pt_set_albedo_map(self.h, _ptr(m), m.shape[1], m.shape[0]), "set_albedo_map")
+        self._map_floats = m.shape[0] * m.shape[1] * 3
 
     def load_scene(self, sd, build: bool = True):
         """Upload a :class:`scenes.SceneData` and build its BVH."""
@@ -292,18 +342,21 @@ class PathTracer:
 
     # -- render --------------------------------------------------------------
     def render(self, views, settings: Settings, stream=None):
-        arr = (View * len(views))(*views)
+        arr = _view_array(views, settings)
         self._ck(self._L.ohao_pt_render(self.h, arr, len(views), C.byref(settings),
                                         _ptr(stream) if stream is not None else None), "render")
 
     def render_host(self, views, settings: Settings, host_accum, stream=None):
-        arr = (View * len(views))(*views)
-        ptrs = (C.c_void_p * len(views))(*[_ptr(a).value for a in host_accum])
+        arr = _view_array(views, settings)
+        if len(host_accum) != len(views):
+            raise ValueError("render_host: one host accumulator per view")
+        ptrs = (C.c_void_p * len(views))(*[_buffer(a, v.width * v.height * 4, "host_accum", host=True)
+                                           for a, v in zip(host_accum, views)])
         self._ck(self._L.ohao_pt_render_host(self.h, arr, len(views), C.byref(settings), ptrs,
                                              _ptr(stream) if stream is not None else None), "render_host")
 
     def autotune(self, views, settings: Settings, stream=None) -> float:
-        arr = (View * len(views))(*views)
+        arr = _view_array(views, settings)
         ms = C.c_float()
         self._ck(self._L.ohao_pt_autotune(self.h, arr, len(views), C.byref(settings), C.byref(ms),
                                           _ptr(stream) if stream is not None else None), "autotune")
@@ -313,22 +366,32 @@ class PathTracer:
     def backward(self, views, settings: Settings, grad_images, grad_map=None, grad_rough=None, stream=None):
         """d loss / d (albedo map, roughness) from per-view d loss / d image
         (device RGBA32F); writes the device buffers grad_map / grad_rough."""
-        arr = (View * len(views))(*views)
-        ptrs = (C.c_void_p * len(views))(*[_ptr(g).value for g in grad_images])
-        self._ck(self._L.ohao_pt_backward(self.h, arr, len(views), C.byref(settings), ptrs, _ptr(grad_map),
-                                          _ptr(grad_rough), _ptr(stream) if stream is not None else None),
-                 "backward")
+        arr = _view_array(views, settings)
+        ptrs = self._image_ptrs(views, grad_images, "grad_images")
+        gm, gr = self._grad_ptrs(grad_map, grad_rough)
+        self._ck(self._L.ohao_pt_backward(self.h, arr, len(views), C.byref(settings), ptrs, gm, gr,
+                                          _ptr(stream) if stream is not None else None), "backward")
 
     def adjoint(self, views, settings: Settings, targets, grad_map=None, grad_rough=None, stream=None) -> float:
         """Renders the views (history 0), returns the multi-view RGB MSE against
         the device RGBA32F targets and writes its gradients."""
-        arr = (View * len(views))(*views)
-        ptrs = (C.c_void_p * len(views))(*[_ptr(t).value for t in targets])
+        arr = _view_array(views, settings)
+        ptrs = self._image_ptrs(views, targets, "targets")
+        gm, gr = self._grad_ptrs(grad_map, grad_rough)
         loss = C.c_float()
-        self._ck(self._L.ohao_pt_adjoint(self.h, arr, len(views), C.byref(settings), ptrs, _ptr(grad_map),
-                                               _ptr(grad_rough), C.byref(loss),
-                                               _ptr(stream) if stream is not None else None), "adjoint")
+        self._ck(self._L.ohao_pt_adjoint(self.h, arr, len(views), C.byref(settings), ptrs, gm, gr, C.byref(loss),
+                                         _ptr(stream) if stream is not None else None), "adjoint")
         return loss.value
+
+    @staticmethod
+    def _image_ptrs(views, images, what):
+        if len(images) != len(views):
+            raise ValueError(f"{what}: one RGBA32F image per view")
+        return (C.c_void_p * len(views))(*[_buffer(g, v.width * v.height * 4, what) for g, v in zip(images, views)])
+
+    def _grad_ptrs(self, grad_map, grad_rough):
+        return (_buffer(grad_map, self._map_floats, "grad_map"),
+                _buffer(grad_rough, self._nmats, "grad_rough"))
 
     @property
     def launch_config(self) -> str:
@@ -354,7 +417,10 @@ class PathTracer:
         return p
 
     def trace(self, rays_dev, n: int, hits_dev, any_hit: bool = False, stats_dev=None, stream=None):
-        self._ck(self._L.ohao_pt_trace(self.h, _ptr(rays_dev), n, _ptr(hits_dev), int(any_hit), _ptr(stats_dev),
+        rays = _buffer(rays_dev, 8 * n, "rays")
+        hits = _buffer(hits_dev, 5 * n, "hits", floats=False)
+        stats = _buffer(stats_dev, 2 * n, "stats", floats=False)
+        self._ck(self._L.ohao_pt_trace(self.h, rays, n, hits, int(any_hit), stats,
                                        _ptr(stream) if stream is not None else None), "trace")
 
     def bvh(self, which: int = -1):

@@ -96,3 +96,46 @@ def test_launch_shapes_listed_without_device(og):
         i += 1
     assert len(names) == len(set(names)) >= 5
     assert any("fetch" in n for n in names) and any("sorted" in n for n in names)
+
+
+def test_buffer_checks_before_any_device_call(og):
+    """Buffers the kernels write unchecked are checked in the Python layer:
+    host arrays, wrong dtypes, short or strided tensors and host tensors
+    where a device buffer is needed raise ValueError; raw pointers pass."""
+    import torch
+    from ohao_engine_gb300 import scenes
+    v = scenes.look_at_view((0, 0, 3), (0, 0, 0), width=8, height=4)
+    npix = 32
+    bad = [np.zeros((npix, 4), np.float32),                       # host array
+           torch.zeros((npix, 4), dtype=torch.float64),             # dtype
+           torch.zeros((npix - 1, 4), dtype=torch.float32),         # too short
+           torch.zeros((npix, 8), dtype=torch.float32)[:, :4],      # strided
+           torch.zeros((npix, 4), dtype=torch.float32)]             # on the host
+    for b in bad:
+        with pytest.raises(ValueError):
+            og.make_view(v, accum=b)
+    with pytest.raises(ValueError):
+        og.make_view(v, aov=torch.zeros((npix, og.AOV_FLOATS - 1)))
+    assert og.make_view(v, accum=0x7f0000000000).accum == 0x7f0000000000
+    # host buffers (render_host): writable C-contiguous float32 arrays
+    ok = np.zeros((npix, 4), np.float32)
+    assert og._buffer(ok, npix * 4, "host_accum", host=True) == ok.ctypes.data
+    ro = np.zeros((npix, 4), np.float32)
+    ro.flags.writeable = False
+    for b in (np.zeros((npix, 4)), ro, np.zeros((npix, 3), np.float32)):
+        with pytest.raises(ValueError):
+            og._buffer(b, npix * 4, "host_accum", host=True)
+    # 4-byte integer buffers (trace hits) where floats are not required
+    with pytest.raises(ValueError):
+        og._buffer(torch.zeros(10, dtype=torch.int32), 10, "hits")
+    with pytest.raises(ValueError, match="CUDA device"):
+        og._buffer(torch.zeros(10, dtype=torch.int32), 10, "hits", floats=False)
+
+
+def test_path_radiance_must_hold_the_call_samples(og):
+    from ohao_engine_gb300 import scenes
+    v = og.make_view(scenes.look_at_view((0, 0, 3), (0, 0, 0), width=8, height=4))
+    v._path_samples = 2
+    assert len(og._view_array([v], og.make_settings(spp=2))) == 1
+    with pytest.raises(ValueError):
+        og._view_array([v], og.make_settings(spp=3))
