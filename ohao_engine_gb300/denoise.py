@@ -12,7 +12,7 @@ import ctypes as C
 
 import numpy as np
 
-from . import AOV_FLOATS, OhaoError, OK, _ptr, load_library, make_settings, make_view
+from . import AOV_FLOATS, OhaoError, OK, _buffer, _ptr, load_library, make_settings, make_view
 
 EXPORTED_SYMBOLS = [
     "ohao_dn_create", "ohao_dn_destroy", "ohao_dn_last_error", "ohao_dn_param_count", "ohao_dn_get_params",
@@ -52,8 +52,12 @@ def _bind(L):
     return L
 
 
-def _ptrs(items):
-    return (C.c_void_p * len(items))(*[_ptr(t).value for t in items])
+def _frames(items, n: int, elems: int, what: str):
+    """Pointer array of n device buffers of at least ``elems`` floats each
+    (checked: the kernels read and write them without bounds)."""
+    if len(items) != n:
+        raise ValueError(f"{what}: {n} buffers expected, got {len(items)}")
+    return (C.c_void_p * n)(*[_buffer(t, elems, what) for t in items])
 
 
 class Denoiser:
@@ -110,13 +114,18 @@ class Denoiser:
         self._ck(self._L.ohao_dn_load(self.h, path.encode()), "load")
 
     def infer(self, radiance, aov, out, width: int, height: int, stream=None):
-        n = len(radiance)
-        self._ck(self._L.ohao_dn_infer(self.h, _ptrs(radiance), _ptrs(aov), n, width, height, _ptrs(out),
+        n, npix = len(radiance), width * height
+        self._ck(self._L.ohao_dn_infer(self.h, _frames(radiance, n, npix * 4, "radiance"),
+                                       _frames(aov, n, npix * AOV_FLOATS, "aov"), n, width, height,
+                                       _frames(out, n, npix * 4, "out"),
                                        _ptr(stream) if stream is not None else None), "infer")
 
     def train_step(self, radiance, aov, target, width: int, height: int, lr: float, stream=None) -> float:
         loss = C.c_float()
-        self._ck(self._L.ohao_dn_train_step(self.h, _ptrs(radiance), _ptrs(aov), _ptrs(target), len(radiance),
+        n, npix = len(radiance), width * height
+        self._ck(self._L.ohao_dn_train_step(self.h, _frames(radiance, n, npix * 4, "radiance"),
+                                            _frames(aov, n, npix * AOV_FLOATS, "aov"),
+                                            _frames(target, n, npix * 4, "target"), n,
                                             width, height, lr, C.byref(loss),
                                             _ptr(stream) if stream is not None else None), "train_step")
         return loss.value

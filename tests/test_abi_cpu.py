@@ -139,3 +139,13 @@ def test_path_radiance_must_hold_the_call_samples(og):
     assert len(og._view_array([v], og.make_settings(spp=2))) == 1
     with pytest.raises(ValueError):
         og._view_array([v], og.make_settings(spp=3))
+
+
+def test_denoiser_frame_checks(og):
+    import torch
+    from ohao_engine_gb300 import denoise
+    with pytest.raises(ValueError, match="2 buffers expected"):
+        denoise._frames([torch.zeros(8)], 2, 8, "aov")
+    with pytest.raises(ValueError):
+        denoise._frames([torch.zeros(7)], 1, 8, "aov")
+    assert list(denoise._frames([0x1000, 0x2000], 2, 8, "out")) == [0x1000, 0x2000]
