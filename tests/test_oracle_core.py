@@ -179,3 +179,35 @@ def test_oracle_render_env_scene(oracle, sampler):
     sc = oracle.OracleScene(sd)
     p = sc.render_paths(view, dict(max_bounces=4, sampler=sampler), 0, 2)
     assert np.isfinite(p).all() and p.mean() > 0.05
+
+
+def _empty_scene(env):
+    v = scenes.look_at_view((0.0, 0.0, 3.0), (0.0, 0.0, 0.0), width=8, height=4)
+    return scenes.SceneData("empty", np.zeros((0, 3), np.float32), np.zeros((0, 4), np.float32),
+                            np.zeros((0, 2), np.float32), np.zeros(0, np.uint32), np.zeros(0, np.uint32),
+                            scenes.material((0.5, 0.5, 0.5))[None], np.zeros((0, 20), np.float32), env, 1.0,
+                            [(0, 0)], scenes.identity_instance(1), [v])
+
+
+@pytest.mark.parametrize("kind", ["no_triangles", "all_masked"])
+def test_scene_without_visible_geometry(oracle, kind):
+    """No triangles, or every instance masked out: every ray misses and every
+    path is the environment seen by its camera ray (the sky is 0.5 away from
+    the sun)."""
+    env = scenes.sky_env(64, 32, seed=1)
+    if kind == "no_triangles":
+        sd = _empty_scene(env)
+    else:
+        sd = scenes.cornell(8, 4, 1)
+        sd.env, sd.env_intensity = env, 1.0
+        sd.lights = np.zeros((0, 20), np.float32)
+        sd.instances = sd.instances.copy()
+        sd.instances["mask"] = 0
+    orc = oracle.OracleScene(sd)
+    rng = np.random.default_rng(2)
+    rays = random_rays(rng, 256, -1.0, 1.0)
+    for mode in (0, 1, 2):
+        h = orc.trace(rays, mode)
+        assert np.all(h[:, 3:5] == 0xFFFFFFFF), f"mode {mode}: a hit in a scene without geometry"
+    p = orc.render_paths(sd.views[0], dict(max_bounces=4, sampler=0), 0, 2)
+    assert p.shape == (2, 32, 3) and np.all(p == np.float32(0.5))
