@@ -361,7 +361,7 @@ ohao_status ohao_pt_build(ohao_pt_ctx* ctx, ohao_stream stream) {
                                     dto.as<uint32_t>(), do2w.as<float>(), static_cast<uint32_t>(vis.size()), n,
                                     tv.as<float>(), tinst.as<uint32_t>(), tprim.as<uint32_t>(), boxes.as<float>(), st);
         // map the visible-instance index back to the instance id
-        if (vis.size() != ninst) {
+        if (vis.size() != ninst && n) {
             std::vector<uint32_t> h_inst(n);
             CK(cudaMemcpyAsync(h_inst.data(), tinst.p, static_cast<size_t>(n) * 4, cudaMemcpyDeviceToHost, st), "build");
             CK(cudaStreamSynchronize(st), "build");
