@@ -1,0 +1,121 @@
+"""Compiles the reference's GLSL helper includes as C++ -- TEST INFRASTRUCTURE ONLY.
+
+The path's shaders run only through Vulkan ray tracing, which neither this
+machine nor the GPU host can bring up. Their plain helper functions (PCG
+sampler, balance heuristic, GGX D / Smith / VNDF sampling, metal-rough
+unpack, environment CDF search and pdf) are ordinary scalar code, so they are
+compiled here, from the reference tree where it lies, as C++ with the GLSL
+subset of ``glsl_shim.hpp`` and ``-fsingle-precision-constant`` (GLSL float
+literals are single precision). The only change to their text is GLSL's
+``out T name`` parameter qualifier, written as the C++ reference ``T& name``
+(the same copy-out result when arguments do not alias). The source text is
+passed to the compiler on standard input; only the library
+``oracle/_ref/libohao_glsl.so`` is written. The pin tests compare it with
+the oracle's restatement bit for bit, and ``tests/golden/make_golden.py``
+records its outputs as fixtures for machines without the reference tree.
+"""
+from __future__ import annotations
+
+import os
+import re
+import subprocess
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+REF_ROOT = "/root/reference"
+LIB_PATH = os.path.join(HERE, "_ref", "libohao_glsl.so")
+
+GLSL_FILES = [
+    "shaders/includes/rt/sampler_pcg.glsl",
+    "shaders/includes/rt/mis.glsl",
+    "shaders/includes/material/ggx_aniso.glsl",
+    "shaders/rt/includes/pbr_unpack.glsl",
+    "shaders/includes/rt/env_sampling.glsl",
+]
+
+_OUT_PARAM = re.compile(r"\bout\s+(\w+)\s+(\w+)")
+
+
+def translation_unit(ref_root: str = REF_ROOT) -> str:
+    parts = ['#include "glsl_shim.hpp"', "namespace glsl {"]
+    for rel in GLSL_FILES:
+        with open(os.path.join(ref_root, rel)) as f:
+            text = f.read()
+        parts.append(f'#line 1 "{rel}"')
+        parts.append(_OUT_PARAM.sub(r"\1& \2", text))
+    parts.append("}  // namespace glsl")
+    parts.append('#include "glsl_ref_api.inc"')
+    return "\n".join(parts) + "\n"
+
+
+def available(ref_root: str = REF_ROOT) -> bool:
+    return all(os.path.exists(os.path.join(ref_root, rel)) for rel in GLSL_FILES)
+
+
+def build(ref_root: str = REF_ROOT) -> str:
+    os.makedirs(os.path.dirname(LIB_PATH), exist_ok=True)
+    cmd = ["g++", "-std=c++20", "-O2", "-fPIC", "-shared", "-ffp-contract=off", "-fsingle-precision-constant",
+           "-Wall", "-Wno-unused-variable", "-Wno-unused-but-set-variable", "-I", HERE, "-x", "c++", "-",
+           "-o", LIB_PATH]
+    subprocess.run(cmd, input=translation_unit(ref_root), text=True, check=True)
+    return LIB_PATH
+
+
+# ---- record layouts and input generators shared by the fixtures and tests ----
+# (inputs, outputs) floats per record; function ids as in glsl_ref_api.inc
+HELPER_IO = {0: (3, 10), 1: (2, 1), 2: (10, 1), 3: (2, 1), 4: (2, 1), 5: (2, 1), 6: (3, 1), 7: (7, 3), 8: (3, 2)}
+HELPER_NAMES = {0: "pcg_stream", 1: "mis_balance", 2: "ggx_d_aniso_or_iso", 3: "ggx_d_iso", 4: "smith_lambda",
+                5: "smith_g1", 6: "smith_g2_over_g1", 7: "sample_ggx_vndf", 8: "unpack_hit_pbr"}
+ENV_IO = {0: (1, 1), 1: (2, 1), 2: (2, 4), 3: (3, 1)}
+ENV_NAMES = {0: "search_marginal", 1: "search_conditional", 2: "sample_env_map", 3: "pdf_env_map"}
+
+
+def _unit(rng, n):
+    import numpy as np
+    v = rng.normal(size=(n, 3))
+    return v / np.linalg.norm(v, axis=1, keepdims=True)
+
+
+def helper_records(fn: int, n: int, rng):
+    """n input records of helper ``fn``, float32 [n, inputs]: the ranges the
+    integrator feeds them plus the branch edges (anisotropy at and around its
+    0.001 switch, signed-roughness payloads, zero pdfs)."""
+    import numpy as np
+    if fn == 0:
+        x = np.stack([rng.integers(0, 4096, n), rng.integers(0, 4096, n), rng.integers(0, 1 << 20, n)], 1)
+    elif fn == 1:
+        x = rng.exponential(1.0, (n, 2)) * (rng.random((n, 2)) < 0.9)
+    elif fn == 2:
+        N, H = _unit(rng, n), _unit(rng, n)
+        ndh = np.abs((N * H).sum(1, keepdims=True))
+        x = np.concatenate([N, H, ndh, rng.uniform(0, 1, (n, 1)),
+                            rng.choice([0.0, 0.0005, 0.001, 0.3, 0.9, 1.0], (n, 1)), rng.uniform(-3, 3, (n, 1))], 1)
+    elif fn in (3, 4, 5):
+        x = np.stack([rng.uniform(-1, 1, n), rng.uniform(0, 1, n)], 1)
+    elif fn == 6:
+        x = rng.uniform(0, 1, (n, 3))
+    elif fn == 7:
+        ve = _unit(rng, n)
+        ve[:, 2] = np.abs(ve[:, 2]) + 1e-3
+        ve /= np.linalg.norm(ve, axis=1, keepdims=True)
+        x = np.concatenate([ve, rng.uniform(0.001, 1, (n, 2)), rng.random((n, 2))], 1)
+    else:
+        x = np.concatenate([rng.uniform(-12, 12, (n, 1)), rng.choice([0.0, 5e-5, 0.5, 1.0, 1.5, -0.2], (n, 1)),
+                            rng.random((n, 1))], 1)
+    return np.ascontiguousarray(x, np.float32)
+
+
+def env_records(fn: int, n: int, rng, w: int, h: int):
+    import numpy as np
+    if fn == 0:
+        x = rng.random((n, 1))
+    elif fn == 1:
+        x = np.stack([rng.integers(0, h, n), rng.random(n)], 1)
+    elif fn == 2:
+        x = rng.random((n, 2))
+    else:
+        x = _unit(rng, n)
+    return np.ascontiguousarray(x, np.float32)
+
+
+if __name__ == "__main__":
+    print(build())

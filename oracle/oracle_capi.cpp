@@ -369,6 +369,85 @@ void orc_math(int op, const float* in, uint32_t n, float* out) {
         }
     }
 }
+// The oracle's restatement of the reference's GLSL helpers, record for
+// record as gref_helper / gref_env in glsl_ref_api.inc (same function ids
+// and layouts), for the pin tests.
+int orc_glsl_helper(int fn, const float* in, uint32_t n, float* out) {
+    static constexpr int kIn[9] = {3, 2, 10, 2, 2, 2, 3, 7, 3};
+    static constexpr int kOut[9] = {10, 1, 1, 1, 1, 1, 1, 3, 2};
+    using PT = PathTracer<float>;
+    using V = V3<float>;
+    if (fn < 0 || fn > 8) return -1;
+    for (uint32_t i = 0; i < n; ++i) {
+        const float* a = in + static_cast<size_t>(i) * kIn[fn];
+        float* o = out + static_cast<size_t>(i) * kOut[fn];
+        switch (fn) {
+            case 0: {
+                Sampler s;
+                s.init(kSamplerPCG, uint32_t(a[0]), uint32_t(a[1]), uint32_t(a[2]));
+                for (uint32_t d = 0; d < 10; ++d) o[d] = s.s1(d);
+                break;
+            }
+            case 1: o[0] = PT::mis(a[0], a[1]); break;
+            case 2: {
+                Scene sc;
+                Settings st;
+                st.aniso = a[8];
+                st.aniso_rot = a[9];
+                PT pt(sc, st);
+                o[0] = pt.ggxD(V(a[0], a[1], a[2]), V(a[3], a[4], a[5]), a[6], a[7]);
+                break;
+            }
+            case 3: o[0] = PT::ggx_d_iso(a[0], a[1]); break;
+            case 4: o[0] = PT::smith_lambda(a[0], a[1]); break;
+            case 5: o[0] = PT::smith_g1(a[0], a[1]); break;
+            case 6: o[0] = PT::smith_g2_over_g1(a[0], a[1], a[2]); break;
+            case 7: {
+                const V h = PT::sample_vndf(V(a[0], a[1], a[2]), a[3], a[4], a[5], a[6]);
+                o[0] = h.x;
+                o[1] = h.y;
+                o[2] = h.z;
+                break;
+            }
+            default: PT::unpack_hit_pbr(V(a[0], a[1], a[2]), o[0], o[1]); break;
+        }
+    }
+    return 0;
+}
+int orc_glsl_env(int fn, const float* marg, const float* cond, uint32_t w, uint32_t h, const float* in, uint32_t n,
+                 float* out) {
+    static constexpr int kIn[4] = {1, 2, 2, 3};
+    static constexpr int kOut[4] = {1, 1, 4, 1};
+    if (fn < 0 || fn > 3 || !marg || !cond || w == 0 || h == 0) return -1;
+    Scene sc;
+    sc.env_w = w;
+    sc.env_h = h;
+    sc.marg.assign(marg, marg + h);
+    sc.cond.assign(cond, cond + static_cast<size_t>(w) * h);
+    sc.has_env = sc.has_cdf = true;
+    Settings st;
+    PathTracer<float> pt(sc, st);
+    for (uint32_t i = 0; i < n; ++i) {
+        const float* a = in + static_cast<size_t>(i) * kIn[fn];
+        float* o = out + static_cast<size_t>(i) * kOut[fn];
+        switch (fn) {
+            case 0: o[0] = float(pt.search_marg(a[0])); break;
+            case 1: o[0] = float(pt.search_cond(uint32_t(a[0]) * w, a[1])); break;
+            case 2: {
+                V3<float> dir;
+                float pdf;
+                pt.sample_env(a[0], a[1], dir, pdf);
+                o[0] = dir.x;
+                o[1] = dir.y;
+                o[2] = dir.z;
+                o[3] = pdf;
+                break;
+            }
+            default: o[0] = pt.pdf_env(V3<float>(a[0], a[1], a[2])); break;
+        }
+    }
+    return 0;
+}
 int orc_num_threads() {
 #ifdef _OPENMP
     return omp_get_max_threads();

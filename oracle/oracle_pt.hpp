@@ -596,16 +596,19 @@ struct PathTracer {
         rough = gmax(rough, R(0.04f));
         s.color = V3<R>(R(m[9]), R(m[10]), R(m[11]));
         // payload.attenuation = (roughness, clamp(metallic,0,1), curv) then
-        // unpackHitPbr (pbr_unpack.glsl:8-20)
-        R ax = rough, ay = gclamp(metal, R(0), R(1));
+        // unpackHitPbr
         R rr, mm;
-        if (ax < R(0) && ay < R(1e-4f)) {
-            rr = -ax; if (rr >= R(10)) rr = rr - R(10); rr = gmax(rr, R(0.01f)); mm = R(1);
-        } else {
-            rr = std::fabs(ax); if (rr >= R(10)) rr = rr - R(10); rr = gmax(rr, R(0.01f)); mm = gclamp(ay, R(0), R(1));
-        }
+        unpack_hit_pbr(V3<R>(rough, gclamp(metal, R(0), R(1)), R(0)), rr, mm);
         s.rough = rr;
         s.metal = mm;
+    }
+    // unpackHitPbr (pbr_unpack.glsl:8-20)
+    static void unpack_hit_pbr(V3<R> att, R& rr, R& mm) {
+        if (att.x < R(0) && att.y < R(1e-4f)) {
+            rr = -att.x; if (rr >= R(10)) rr = rr - R(10); rr = gmax(rr, R(0.01f)); mm = R(1);
+        } else {
+            rr = std::fabs(att.x); if (rr >= R(10)) rr = rr - R(10); rr = gmax(rr, R(0.01f)); mm = gclamp(att.y, R(0), R(1));
+        }
     }
 
     void trace(V3<R> o, V3<R> d, Surf<R>& s, TravStats* ts) const {

@@ -16,6 +16,7 @@ import numpy as np
 HERE = os.path.dirname(os.path.abspath(__file__))
 LIB_PATH = os.path.join(HERE, "_build", "liboracle.so")
 REF_PATH = os.path.join(HERE, "_ref", "libohao_ref.so")
+GLSL_PATH = os.path.join(HERE, "_ref", "libohao_glsl.so")
 REF_ROOT = "/root/reference"
 
 _lib = None
@@ -27,6 +28,9 @@ def build(ref: bool | None = None) -> None:
         ref = os.path.isdir(os.path.join(REF_ROOT, "ohao"))
     if ref:
         subprocess.run(["make", "-s", "-C", HERE, "ref", f"REF_ROOT={REF_ROOT}"], check=True)
+        import glsl_pin
+        if glsl_pin.available(REF_ROOT):
+            glsl_pin.build(REF_ROOT)
 
 
 def _p(a):
@@ -69,6 +73,10 @@ def lib():
         L.orc_sampler_stream.argtypes = [u32, u32, u32, u32, u32, vp]
         L.orc_math.argtypes = [i32, vp, u32, vp]
         L.orc_num_threads.restype = i32
+        L.orc_glsl_helper.argtypes = [i32, vp, u32, vp]
+        L.orc_glsl_helper.restype = i32
+        L.orc_glsl_env.argtypes = [i32, vp, vp, u32, u32, vp, u32, vp]
+        L.orc_glsl_env.restype = i32
         _lib = L
     return _lib
 
@@ -85,6 +93,36 @@ def ref_lib():
     L.ref_owen_scramble.restype = C.c_uint32
     L.ref_sobol_dirs.restype = C.POINTER(C.c_uint32)
     return L
+
+
+def glsl_lib():
+    """The reference's GLSL helper includes compiled as C++ (glsl_pin.py; only
+    where the reference tree exists)."""
+    if not os.path.exists(GLSL_PATH):
+        return None
+    L = C.CDLL(GLSL_PATH)
+    L.gref_helper.argtypes = [C.c_int, C.c_void_p, C.c_uint32, C.c_void_p]
+    L.gref_helper.restype = C.c_int
+    L.gref_env.argtypes = [C.c_int, C.c_void_p, C.c_void_p, C.c_uint32, C.c_uint32, C.c_void_p, C.c_uint32, C.c_void_p]
+    L.gref_env.restype = C.c_int
+    return L
+
+
+def glsl_eval(lib_, prefix: str, fn: int, x: np.ndarray, n_out: int, env=None) -> np.ndarray:
+    """Runs helper (env=None) or env function ``fn`` of the oracle
+    (prefix "orc_glsl_") or of the compiled reference GLSL ("gref_") on the
+    records x; env = (marg, cond, w, h)."""
+    x = np.ascontiguousarray(x, np.float32)
+    out = np.zeros((x.shape[0], n_out), np.float32)
+    if env is None:
+        st = getattr(lib_, prefix + "helper")(fn, _p(x), x.shape[0], _p(out))
+    else:
+        m, c, w, h = env
+        m = np.ascontiguousarray(m, np.float32)
+        c = np.ascontiguousarray(c, np.float32)
+        st = getattr(lib_, prefix + "env")(fn, _p(m), _p(c), w, h, _p(x), x.shape[0], _p(out))
+    assert st == 0, f"{prefix} fn {fn}: status {st}"
+    return out
 
 
 def env_cdf(env: np.ndarray):

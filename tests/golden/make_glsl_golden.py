@@ -1,0 +1,59 @@
+"""Regenerate tests/golden/glsl_kats.json from the reference's own shader text.
+
+Compiles the reference's GLSL helper includes as C++ where they lie in the
+reference tree (oracle/glsl_pin.py) and records their outputs on seeded
+inputs: 64 records per helper, and the environment-CDF functions over the
+CDFs of a seeded 32x16 map. Run in a container that has the reference
+checkout:
+
+    python tests/golden/make_glsl_golden.py
+"""
+import json
+import os
+import sys
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+ROOT = os.path.dirname(os.path.dirname(HERE))
+sys.path.insert(0, os.path.join(ROOT, "oracle"))
+import glsl_pin  # noqa: E402
+import pyoracle  # noqa: E402
+
+N = 64
+ENV_W, ENV_H = 32, 16
+
+
+def bits(a):
+    return np.ascontiguousarray(a, np.float32).view(np.uint32).reshape(-1).tolist()
+
+
+def main():
+    pyoracle.build(ref=True)
+    G = pyoracle.glsl_lib()
+    assert G is not None, "GLSL helpers not built (needs the reference checkout)"
+    rng = np.random.default_rng(2024)
+    out = {"generator": "tests/golden/make_glsl_golden.py",
+           "source": "reference shader includes " + ", ".join(glsl_pin.GLSL_FILES) + ", compiled as C++",
+           "helpers": {}, "env": {}}
+    for fn, (nin, nout) in glsl_pin.HELPER_IO.items():
+        x = glsl_pin.helper_records(fn, N, rng)
+        y = pyoracle.glsl_eval(G, "gref_", fn, x, nout)
+        out["helpers"][glsl_pin.HELPER_NAMES[fn]] = {"fn": fn, "in_bits": bits(x), "out_bits": bits(y)}
+    env = rng.uniform(0, 4, (ENV_H, ENV_W, 4)).astype(np.float32)
+    env[3] = 0.0
+    env[9, 20, :3] = 200.0
+    marg, cond, _ = pyoracle.env_cdf(env)
+    out["env_cdf"] = {"w": ENV_W, "h": ENV_H, "marg_bits": bits(marg), "cond_bits": bits(cond)}
+    for fn, (nin, nout) in glsl_pin.ENV_IO.items():
+        x = glsl_pin.env_records(fn, N, rng, ENV_W, ENV_H)
+        y = pyoracle.glsl_eval(G, "gref_", fn, x, nout, env=(marg, cond, ENV_W, ENV_H))
+        out["env"][glsl_pin.ENV_NAMES[fn]] = {"fn": fn, "in_bits": bits(x), "out_bits": bits(y)}
+    path = os.path.join(HERE, "glsl_kats.json")
+    with open(path, "w") as f:
+        json.dump(out, f)
+    print("wrote", path)
+
+
+if __name__ == "__main__":
+    main()
