@@ -36,7 +36,8 @@ _OUT_PARAM = re.compile(r"\bout\s+(\w+)\s+(\w+)")
 
 
 def translation_unit(ref_root: str = REF_ROOT) -> str:
-    parts = ['#include "glsl_shim.hpp"', "namespace glsl {"]
+    parts = ['#include "glsl_shim.hpp"', "namespace glsl {",
+             "inline FloatBuffer envMarg{nullptr}, envCond{nullptr};   // env_sampling.glsl's CDF buffers"]
     for rel in GLSL_FILES:
         with open(os.path.join(ref_root, rel)) as f:
             text = f.read()
@@ -54,6 +55,7 @@ def available(ref_root: str = REF_ROOT) -> bool:
 def build(ref_root: str = REF_ROOT) -> str:
     os.makedirs(os.path.dirname(LIB_PATH), exist_ok=True)
     cmd = ["g++", "-std=c++20", "-O2", "-fPIC", "-shared", "-ffp-contract=off", "-fsingle-precision-constant",
+           "-fno-strict-aliasing",
            "-Wall", "-Wno-unused-variable", "-Wno-unused-but-set-variable", "-I", HERE, "-x", "c++", "-",
            "-o", LIB_PATH]
     subprocess.run(cmd, input=translation_unit(ref_root), text=True, check=True)
@@ -117,5 +119,86 @@ def env_records(fn: int, n: int, rng, w: int, h: int):
     return np.ascontiguousarray(x, np.float32)
 
 
+# ---- the path-tracing shaders themselves (raygen, closest hit, miss) ----
+PT_LIB_PATH = os.path.join(HERE, "_ref", "libohao_glslpt.so")
+PT_SHADERS = [("rgen", "shaders/rt/pt_raygen.rgen"), ("rchit", "shaders/rt/pt_closesthit.rchit"),
+              ("rmiss", "shaders/rt/pt_miss.rmiss")]
+
+_COMMENTS = re.compile(r"//[^\n]*|/\*.*?\*/", re.S)
+_INOUT_PARAM = re.compile(r"\b(?:out|inout)\s+(\w+)\s+(\w+)")
+_SPEC_CONST = re.compile(r"layout\s*\(\s*constant_id\s*=\s*\d+\s*\)\s*const\s+")
+_UNSIZED = re.compile(r"(\w+)\s+(\w+)\s*\[\s*\]\s*;")
+_ARRAY_CTOR = re.compile(r"=\s*\w+\s*\[\s*\d*\s*\]\s*\(")
+_DEFINE = re.compile(r"^\s*#\s*define\s+(\w+)", re.M)
+
+
+def _expand(path: str, ref_root: str) -> str:
+    """The shader with its #include files inlined (resolved against the
+    including file's folder, then shaders/), #version / #extension dropped."""
+    out = []
+    with open(path) as f:
+        for line in f.read().splitlines():
+            m = re.match(r'\s*#\s*include\s+"([^"]+)"', line)
+            if m:
+                cands = [os.path.join(os.path.dirname(path), m.group(1)), os.path.join(ref_root, "shaders", m.group(1))]
+                out.append(_expand(next(c for c in cands if os.path.exists(c)), ref_root))
+            elif not re.match(r"\s*#\s*(version|extension)\b", line):
+                out.append(line)
+    return "\n".join(out)
+
+
+def _array_ctors(text: str) -> str:
+    """`= T[N](a, b, ...)` array constructors -> `= {a, b, ...}`."""
+    while True:
+        m = _ARRAY_CTOR.search(text)
+        if not m:
+            return text
+        depth, i = 1, m.end()
+        while depth:
+            depth += {"(": 1, ")": -1}.get(text[i], 0)
+            i += 1
+        text = text[:m.start()] + "= {" + text[m.end():i - 1] + "}" + text[i:]
+
+
+def shader_text(rel: str, ref_root: str = REF_ROOT) -> str:
+    """GLSL -> C++ for one shader: comments removed, `out`/`inout T x` ->
+    `T& x`, specialization constants as plain globals, unsized buffer arrays
+    as pointers, array constructors as brace lists. Nothing else changes."""
+    text = _COMMENTS.sub(lambda m: "\n" * m.group(0).count("\n"), _expand(os.path.join(ref_root, rel), ref_root))
+    text = _INOUT_PARAM.sub(r"\1& \2", text)
+    text = _SPEC_CONST.sub("", text)
+    text = _UNSIZED.sub(r"\1* \2;", text)
+    return _array_ctors(text)
+
+
+def pt_translation_unit(ref_root: str = REF_ROOT) -> str:
+    parts = ['#include "glsl_rt.hpp"']
+    for ns, rel in PT_SHADERS:
+        text = shader_text(rel, ref_root)
+        parts += [f"namespace {ns} {{", "using namespace glsl;", f'#line 1 "{rel}"', text, f"}}  // namespace {ns}"]
+        parts += [f"#undef {name}" for name in sorted(set(_DEFINE.findall(text)))]
+    parts.append('#include "glsl_pt_api.inc"')
+    return "\n".join(parts) + "\n"
+
+
+def pt_available(ref_root: str = REF_ROOT) -> bool:
+    return all(os.path.exists(os.path.join(ref_root, rel)) for _, rel in PT_SHADERS)
+
+
+def build_pt(ref_root: str = REF_ROOT) -> str:
+    """libohao_glslpt.so: the shaders (GLSL float semantics) + the host side
+    over the oracle's scene (glsl_pt_host.cpp, ordinary flags)."""
+    os.makedirs(os.path.dirname(PT_LIB_PATH), exist_ok=True)
+    obj = os.path.join(os.path.dirname(PT_LIB_PATH), "glslpt_shaders.o")
+    subprocess.run(["g++", "-std=c++20", "-O2", "-fPIC", "-c", "-ffp-contract=off", "-fsingle-precision-constant",
+                    "-fno-strict-aliasing", "-w", "-I", HERE, "-x", "c++", "-", "-o", obj],
+                   input=pt_translation_unit(ref_root), text=True, check=True)
+    subprocess.run(["g++", "-std=c++20", "-O2", "-fPIC", "-shared", "-ffp-contract=off", "-I", HERE,
+                    os.path.join(HERE, "glsl_pt_host.cpp"), obj, "-o", PT_LIB_PATH], check=True)
+    os.remove(obj)
+    return PT_LIB_PATH
+
+
 if __name__ == "__main__":
     print(build())
+    print(build_pt())

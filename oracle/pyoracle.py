@@ -17,6 +17,7 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 LIB_PATH = os.path.join(HERE, "_build", "liboracle.so")
 REF_PATH = os.path.join(HERE, "_ref", "libohao_ref.so")
 GLSL_PATH = os.path.join(HERE, "_ref", "libohao_glsl.so")
+GLSL_PT_PATH = os.path.join(HERE, "_ref", "libohao_glslpt.so")
 REF_ROOT = "/root/reference"
 
 _lib = None
@@ -31,6 +32,8 @@ def build(ref: bool | None = None) -> None:
         import glsl_pin
         if glsl_pin.available(REF_ROOT):
             glsl_pin.build(REF_ROOT)
+        if glsl_pin.pt_available(REF_ROOT):
+            glsl_pin.build_pt(REF_ROOT)
 
 
 def _p(a):
@@ -106,6 +109,33 @@ def glsl_lib():
     L.gref_env.argtypes = [C.c_int, C.c_void_p, C.c_void_p, C.c_uint32, C.c_uint32, C.c_void_p, C.c_uint32, C.c_void_p]
     L.gref_env.restype = C.c_int
     return L
+
+
+def glsl_pt_lib():
+    """The reference's raygen / closest-hit / miss shaders compiled as C++
+    over the oracle's scenes (glsl_pin.py; only where the reference tree
+    exists)."""
+    if not os.path.exists(GLSL_PT_PATH):
+        return None
+    L = C.CDLL(GLSL_PT_PATH)
+    vp, u32 = C.c_void_p, C.c_uint32
+    L.gpt_render_paths.argtypes = [vp, vp, vp, u32, u32, vp, u32, u32, vp, u32, vp]
+    return L
+
+
+def shader_paths(glsl_lib_, scene: "OracleScene", view, settings: dict, sample_base: int, spp: int,
+                 pixels=None) -> np.ndarray:
+    """Per-path radiance [spp, npix, 3] from the reference's shaders, traced
+    through the oracle's BVH; the layout of OracleScene.render_paths."""
+    st = np.zeros(1, SETTINGS_DTYPE)
+    for k in SETTINGS_DTYPE.names:
+        st[k] = settings.get(k, 0)
+    pix = None if pixels is None else np.ascontiguousarray(pixels, np.uint32)
+    npix = view.width * view.height if pix is None else pix.size
+    out = np.zeros((spp, npix, 3), np.float32)
+    glsl_lib_.gpt_render_paths(scene.h, _p(view.inv_view), _p(view.inv_proj), view.width, view.height, _p(st),
+                               sample_base, spp, _p(pix), npix, _p(out))
+    return out
 
 
 def glsl_eval(lib_, prefix: str, fn: int, x: np.ndarray, n_out: int, env=None) -> np.ndarray:

@@ -2,9 +2,11 @@
 
 Compiles the reference's GLSL helper includes as C++ where they lie in the
 reference tree (oracle/glsl_pin.py) and records their outputs on seeded
-inputs: 64 records per helper, and the environment-CDF functions over the
-CDFs of a seeded 32x16 map. Run in a container that has the reference
-checkout:
+inputs: 64 records per helper, the environment-CDF functions over the CDFs
+of a seeded 32x16 map, and the per-path radiance of the raygen, closest-hit
+and miss shaders (traced through the oracle's BVH) on the seeded scenes of
+tests/pin_cases.py, 96 pixels of the first view each. Run in a container
+that has the reference checkout:
 
     python tests/golden/make_glsl_golden.py
 """
@@ -17,6 +19,8 @@ import numpy as np
 HERE = os.path.dirname(os.path.abspath(__file__))
 ROOT = os.path.dirname(os.path.dirname(HERE))
 sys.path.insert(0, os.path.join(ROOT, "oracle"))
+sys.path.insert(0, os.path.dirname(HERE))
+sys.path.insert(0, ROOT)
 import glsl_pin  # noqa: E402
 import pyoracle  # noqa: E402
 
@@ -49,6 +53,17 @@ def main():
         x = glsl_pin.env_records(fn, N, rng, ENV_W, ENV_H)
         y = pyoracle.glsl_eval(G, "gref_", fn, x, nout, env=(marg, cond, ENV_W, ENV_H))
         out["env"][glsl_pin.ENV_NAMES[fn]] = {"fn": fn, "in_bits": bits(x), "out_bits": bits(y)}
+    import pin_cases
+    P = pyoracle.glsl_pt_lib()
+    assert P is not None, "path-tracing shaders not built (needs the reference checkout)"
+    out["paths"] = {}
+    for name, (make, settings, flatten_limit) in pin_cases.CASES.items():
+        sd = make()
+        scene = pyoracle.OracleScene(sd, flatten_limit=flatten_limit)
+        v = sd.views[0]
+        pix = np.sort(np.random.default_rng(len(name)).choice(v.width * v.height, 96, replace=False)).astype(np.uint32)
+        y = pyoracle.shader_paths(P, scene, v, settings, pin_cases.SAMPLE_BASE, pin_cases.SPP, pix)
+        out["paths"][name] = {"pixels": pix.tolist(), "out_bits": bits(y)}
     path = os.path.join(HERE, "glsl_kats.json")
     with open(path, "w") as f:
         json.dump(out, f)
