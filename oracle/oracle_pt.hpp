@@ -22,7 +22,9 @@
 //   * texture filtering is restated in float (the reference uses the
 //     hardware sampler, LINEAR/REPEAT, LOD 0).
 // Traversal is float in both instantiations; the integrator arithmetic runs
-// in Real.
+// in Real. The float instantiation is checked bit for bit against the
+// reference's own shader files compiled as C++ (glsl_pin.py), on scenes
+// outside the deviations above.
 #pragma once
 #include "oracle_bvh.hpp"
 #include <vector>
