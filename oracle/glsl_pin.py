@@ -120,9 +120,15 @@ def env_records(fn: int, n: int, rng, w: int, h: int):
 
 
 # ---- the path-tracing shaders themselves (raygen, closest hit, miss) ----
-PT_LIB_PATH = os.path.join(HERE, "_ref", "libohao_glslpt.so")
-PT_SHADERS = [("rgen", "shaders/rt/pt_raygen.rgen"), ("rchit", "shaders/rt/pt_closesthit.rchit"),
-              ("rmiss", "shaders/rt/pt_miss.rmiss")]
+# raygen variants: the path tracer's default raygen, and the offline
+# profile's (the same estimator with its analytic-light products regrouped
+# and optional subsurface terms, off unless push constant tuning.w > 0)
+PT_RAYGENS = {"base": "shaders/rt/pt_raygen.rgen", "offline": "shaders/rt/pt_raygen_offline.rgen"}
+PT_HIT_MISS = [("rchit", "shaders/rt/pt_closesthit.rchit"), ("rmiss", "shaders/rt/pt_miss.rmiss")]
+
+
+def pt_lib_path(variant: str = "base") -> str:
+    return os.path.join(HERE, "_ref", "libohao_glslpt.so" if variant == "base" else f"libohao_glslpt_{variant}.so")
 
 _COMMENTS = re.compile(r"//[^\n]*|/\*.*?\*/", re.S)
 _INOUT_PARAM = re.compile(r"\b(?:out|inout)\s+(\w+)\s+(\w+)")
@@ -171,9 +177,9 @@ def shader_text(rel: str, ref_root: str = REF_ROOT) -> str:
     return _array_ctors(text)
 
 
-def pt_translation_unit(ref_root: str = REF_ROOT) -> str:
+def pt_translation_unit(ref_root: str = REF_ROOT, variant: str = "base") -> str:
     parts = ['#include "glsl_rt.hpp"']
-    for ns, rel in PT_SHADERS:
+    for ns, rel in [("rgen", PT_RAYGENS[variant])] + PT_HIT_MISS:
         text = shader_text(rel, ref_root)
         parts += [f"namespace {ns} {{", "using namespace glsl;", f'#line 1 "{rel}"', text, f"}}  // namespace {ns}"]
         parts += [f"#undef {name}" for name in sorted(set(_DEFINE.findall(text)))]
@@ -182,21 +188,27 @@ def pt_translation_unit(ref_root: str = REF_ROOT) -> str:
 
 
 def pt_available(ref_root: str = REF_ROOT) -> bool:
-    return all(os.path.exists(os.path.join(ref_root, rel)) for _, rel in PT_SHADERS)
+    rels = list(PT_RAYGENS.values()) + [rel for _, rel in PT_HIT_MISS]
+    return all(os.path.exists(os.path.join(ref_root, rel)) for rel in rels)
 
 
-def build_pt(ref_root: str = REF_ROOT) -> str:
-    """libohao_glslpt.so: the shaders (GLSL float semantics) + the host side
-    over the oracle's scene (glsl_pt_host.cpp, ordinary flags)."""
-    os.makedirs(os.path.dirname(PT_LIB_PATH), exist_ok=True)
-    obj = os.path.join(os.path.dirname(PT_LIB_PATH), "glslpt_shaders.o")
-    subprocess.run(["g++", "-std=c++20", "-O2", "-fPIC", "-c", "-ffp-contract=off", "-fsingle-precision-constant",
-                    "-fno-strict-aliasing", "-w", "-I", HERE, "-x", "c++", "-", "-o", obj],
-                   input=pt_translation_unit(ref_root), text=True, check=True)
-    subprocess.run(["g++", "-std=c++20", "-O2", "-fPIC", "-shared", "-ffp-contract=off", "-I", HERE,
-                    os.path.join(HERE, "glsl_pt_host.cpp"), obj, "-o", PT_LIB_PATH], check=True)
-    os.remove(obj)
-    return PT_LIB_PATH
+def build_pt(ref_root: str = REF_ROOT) -> list:
+    """libohao_glslpt[_offline].so: a raygen variant with the closest-hit and
+    miss shaders (GLSL float semantics) + the host side over the oracle's
+    scene (glsl_pt_host.cpp, ordinary flags)."""
+    paths = []
+    for variant in PT_RAYGENS:
+        out = pt_lib_path(variant)
+        os.makedirs(os.path.dirname(out), exist_ok=True)
+        obj = out[:-3] + ".o"
+        subprocess.run(["g++", "-std=c++20", "-O2", "-fPIC", "-c", "-ffp-contract=off",
+                        "-fsingle-precision-constant", "-fno-strict-aliasing", "-w", "-I", HERE, "-x", "c++", "-",
+                        "-o", obj], input=pt_translation_unit(ref_root, variant), text=True, check=True)
+        subprocess.run(["g++", "-std=c++20", "-O2", "-fPIC", "-shared", "-ffp-contract=off", "-I", HERE,
+                        os.path.join(HERE, "glsl_pt_host.cpp"), obj, "-o", out], check=True)
+        os.remove(obj)
+        paths.append(out)
+    return paths
 
 
 if __name__ == "__main__":

@@ -315,6 +315,11 @@ inline vec4 mix(const vec4& x, const vec4& y, float a) { return x * (1.0f - a) +
 inline vec3 mix(const vec3& x, const vec3& y, const vec3& a) {
     return {mix(x.x, y.x, a.x), mix(x.y, y.y, a.y), mix(x.z, y.z, a.z)};
 }
+// smoothstep as the GLSL specification writes it: t * t * (3 - 2 t)
+inline float smoothstep(float e0, float e1, float x) {
+    const float t = clamp((x - e0) / (e1 - e0), 0.0f, 1.0f);
+    return t * t * (3.0f - 2.0f * t);
+}
 inline float pow(float x, float y) {
     if (y == 5.0f) return orc::pow5(x);
     return std::pow(x, y);

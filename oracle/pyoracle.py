@@ -17,7 +17,6 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 LIB_PATH = os.path.join(HERE, "_build", "liboracle.so")
 REF_PATH = os.path.join(HERE, "_ref", "libohao_ref.so")
 GLSL_PATH = os.path.join(HERE, "_ref", "libohao_glsl.so")
-GLSL_PT_PATH = os.path.join(HERE, "_ref", "libohao_glslpt.so")
 REF_ROOT = "/root/reference"
 
 _lib = None
@@ -111,13 +110,16 @@ def glsl_lib():
     return L
 
 
-def glsl_pt_lib():
-    """The reference's raygen / closest-hit / miss shaders compiled as C++
-    over the oracle's scenes (glsl_pin.py; only where the reference tree
+def glsl_pt_lib(variant: str = "base"):
+    """The reference's raygen ("base": pt_raygen.rgen, "offline":
+    pt_raygen_offline.rgen) with its closest-hit and miss shaders compiled as
+    C++ over the oracle's scenes (glsl_pin.py; only where the reference tree
     exists)."""
-    if not os.path.exists(GLSL_PT_PATH):
+    import glsl_pin
+    path = glsl_pin.pt_lib_path(variant)
+    if not os.path.exists(path):
         return None
-    L = C.CDLL(GLSL_PT_PATH)
+    L = C.CDLL(path)
     vp, u32 = C.c_void_p, C.c_uint32
     L.gpt_render_paths.argtypes = [vp, vp, vp, u32, u32, vp, u32, u32, vp, u32, vp]
     return L

@@ -54,16 +54,18 @@ def main():
         y = pyoracle.glsl_eval(G, "gref_", fn, x, nout, env=(marg, cond, ENV_W, ENV_H))
         out["env"][glsl_pin.ENV_NAMES[fn]] = {"fn": fn, "in_bits": bits(x), "out_bits": bits(y)}
     import pin_cases
-    P = pyoracle.glsl_pt_lib()
-    assert P is not None, "path-tracing shaders not built (needs the reference checkout)"
-    out["paths"] = {}
-    for name, (make, settings, flatten_limit) in pin_cases.CASES.items():
-        sd = make()
-        scene = pyoracle.OracleScene(sd, flatten_limit=flatten_limit)
-        v = sd.views[0]
-        pix = np.sort(np.random.default_rng(len(name)).choice(v.width * v.height, 96, replace=False)).astype(np.uint32)
-        y = pyoracle.shader_paths(P, scene, v, settings, pin_cases.SAMPLE_BASE, pin_cases.SPP, pix)
-        out["paths"][name] = {"pixels": pix.tolist(), "out_bits": bits(y)}
+    for key, variant in (("paths", "base"), ("paths_offline", "offline")):
+        P = pyoracle.glsl_pt_lib(variant)
+        assert P is not None, "path-tracing shaders not built (needs the reference checkout)"
+        out[key] = {}
+        for name, (make, settings, flatten_limit) in pin_cases.CASES.items():
+            sd = make()
+            scene = pyoracle.OracleScene(sd, flatten_limit=flatten_limit)
+            v = sd.views[0]
+            pix = np.sort(np.random.default_rng(len(name)).choice(v.width * v.height, 96, replace=False))
+            pix = pix.astype(np.uint32)
+            y = pyoracle.shader_paths(P, scene, v, settings, pin_cases.SAMPLE_BASE, pin_cases.SPP, pix)
+            out[key][name] = {"pixels": pix.tolist(), "out_bits": bits(y)}
     path = os.path.join(HERE, "glsl_kats.json")
     with open(path, "w") as f:
         json.dump(out, f)

@@ -238,3 +238,44 @@ def test_integrator_matches_reference_shaders_live(oracle):
             b = oracle.shader_paths(P, scene, v, settings, 0, 2)
             bad = (a.view(np.uint32) != b.view(np.uint32)).any(-1)
             assert not bad.any(), f"{name}: {bad.sum()} of {bad.size} paths differ from the reference shaders"
+
+
+OFFLINE_RTOL = 1e-6   # the offline raygen regroups the analytic-light NEE products
+
+
+def _offline_check(name, sd, got, want):
+    if sd.lights.shape[0] == 0:
+        assert np.array_equal(got.view(np.uint32), want.view(np.uint32)), f"{name}: offline raygen, no lights"
+    else:
+        rel = np.abs(got - want) / np.maximum(np.maximum(np.abs(got), np.abs(want)), 1e-3)
+        assert rel.max() <= OFFLINE_RTOL, f"{name}: offline raygen differs by {rel.max():.3g} relative"
+
+
+def test_integrator_within_offline_raygen_golden(oracle):
+    """Against the offline profile's raygen (pt_raygen_offline.rgen, the
+    subsurface terms off): bit-identical without analytic lights, within
+    1e-6 relative with them (its light NEE multiplies the same factors in
+    another grouping)."""
+    import pin_cases
+    for name, (make, settings, flatten_limit) in pin_cases.CASES.items():
+        rec = GLSL_KATS["paths_offline"][name]
+        sd = make()
+        scene = oracle.OracleScene(sd, flatten_limit=flatten_limit)
+        got = scene.render_paths(sd.views[0], settings, pin_cases.SAMPLE_BASE, pin_cases.SPP, pixels=rec["pixels"])
+        _offline_check(name, sd, got, _u32(rec["out_bits"]).view(np.float32).reshape(got.shape))
+
+
+def test_integrator_within_offline_raygen_live(oracle):
+    import glsl_pin
+    import pin_cases
+    P = oracle.glsl_pt_lib("offline")
+    if P is None and glsl_pin.pt_available():
+        glsl_pin.build_pt()
+        P = oracle.glsl_pt_lib("offline")
+    if P is None:
+        pytest.skip("reference shaders not available here")
+    for name, (make, settings, flatten_limit) in pin_cases.CASES.items():
+        sd = make()
+        scene = oracle.OracleScene(sd, flatten_limit=flatten_limit)
+        v = sd.views[0]
+        _offline_check(name, sd, scene.render_paths(v, settings, 0, 2), oracle.shader_paths(P, scene, v, settings, 0, 2))
