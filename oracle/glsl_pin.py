@@ -1,18 +1,30 @@
-"""Compiles the reference's GLSL helper includes as C++ -- TEST INFRASTRUCTURE ONLY.
+"""Compiles the reference's path-tracing shaders as C++ -- TEST INFRASTRUCTURE ONLY.
 
 The path's shaders run only through Vulkan ray tracing, which neither this
-machine nor the GPU host can bring up. Their plain helper functions (PCG
-sampler, balance heuristic, GGX D / Smith / VNDF sampling, metal-rough
-unpack, environment CDF search and pdf) are ordinary scalar code, so they are
-compiled here, from the reference tree where it lies, as C++ with the GLSL
-subset of ``glsl_shim.hpp`` and ``-fsingle-precision-constant`` (GLSL float
-literals are single precision). The only change to their text is GLSL's
-``out T name`` parameter qualifier, written as the C++ reference ``T& name``
-(the same copy-out result when arguments do not alias). The source text is
-passed to the compiler on standard input; only the library
-``oracle/_ref/libohao_glsl.so`` is written. The pin tests compare it with
-the oracle's restatement bit for bit, and ``tests/golden/make_golden.py``
-records its outputs as fixtures for machines without the reference tree.
+machine nor the GPU host can bring up. Their arithmetic is ordinary scalar
+GLSL, so it is compiled here, from the reference tree where it lies, as C++
+against the GLSL subset of ``glsl_shim.hpp`` (and the ray-tracing built-ins
+of ``glsl_rt.hpp``) with ``-fsingle-precision-constant`` (GLSL float
+literals are single precision). Two libraries come out of it:
+
+* ``oracle/_ref/libohao_glsl.so``: the helper includes (PCG sampler, balance
+  heuristic, GGX D / Smith / VNDF sampling, metal-rough unpack, environment
+  CDF search and pdf) behind ``glsl_ref_api.inc``;
+* ``oracle/_ref/libohao_glslpt[_offline].so``: a raygen (the default one or
+  the offline profile's) with the closest-hit and miss shaders and every
+  file they include, behind ``glsl_pt_api.inc``; ``traceRayEXT`` runs the
+  oracle's traversal (``glsl_pt_host.cpp``).
+
+The text changes are mechanical and listed in ``shader_text``: GLSL's
+``out`` / ``inout T name`` parameters written as C++ references ``T& name``
+(the same copy-out result when arguments do not alias), comments and
+``#version`` / ``#extension`` lines dropped, includes inlined, the
+specialization constant made a settable global, unsized buffer arrays as
+pointers, array constructors as brace lists. The source text goes to the
+compiler on standard input; only the libraries are written. The pin tests
+compare them with the oracle bit for bit, and
+``tests/golden/make_glsl_golden.py`` records their outputs as fixtures for
+machines without the reference tree.
 """
 from __future__ import annotations
 
