@@ -53,6 +53,10 @@ def _instanced():
     return sd
 
 
+def _bench_sphere():
+    return scenes.sphere_1m()   # the default benchmark frame: 1,003,522 triangles, 1920x1080, sky + sun
+
+
 # name -> (scene maker, oracle settings, flatten limit)
 CASES = {
     "env_pcg": (lambda: _env_lit(False), dict(max_bounces=4, sampler=0), 1 << 25),
@@ -63,5 +67,7 @@ CASES = {
     "cornell_area_pcg": (lambda: _cornell_lit(1), dict(max_bounces=4, sampler=0), 1 << 25),
     "cornell_4_types_sobol": (lambda: _cornell_lit(4), dict(max_bounces=3, sampler=1), 1 << 25),
     "instanced_two_level": (_instanced, dict(max_bounces=4, sampler=0), 1000),
+    "sphere_1m_1080p": (_bench_sphere, dict(max_bounces=4, sampler=0), 1 << 25),
 }
+LIVE_PIXELS = 4096   # live comparisons sample at most this many pixels of a view
 SAMPLE_BASE, SPP = 3, 2

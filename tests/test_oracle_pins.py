@@ -204,8 +204,8 @@ def test_integrator_matches_reference_shaders_golden(oracle):
     recorded output of the reference's own path-tracing shaders compiled as
     C++ and traced through the oracle's BVH, on every pin scene: env-lit with
     PCG and Sobol, anisotropic GGX, the firefly clamp, depth 0 and 2, all four
-    analytic light types, and two-level instancing with rotated, scaled
-    instances."""
+    analytic light types, two-level instancing with rotated, scaled
+    instances, and the default benchmark frame (1M triangles, 1080p)."""
     import pin_cases
     assert set(GLSL_KATS["paths"]) == set(pin_cases.CASES)
     for name, (make, settings, flatten_limit) in pin_cases.CASES.items():
@@ -234,10 +234,19 @@ def test_integrator_matches_reference_shaders_live(oracle):
         sd = make()
         scene = oracle.OracleScene(sd, flatten_limit=flatten_limit)
         for v in sd.views[:2]:
-            a = scene.render_paths(v, settings, 0, 2)
-            b = oracle.shader_paths(P, scene, v, settings, 0, 2)
+            pix = _live_pixels(v)
+            a = scene.render_paths(v, settings, 0, 2, pixels=pix)
+            b = oracle.shader_paths(P, scene, v, settings, 0, 2, pix)
             bad = (a.view(np.uint32) != b.view(np.uint32)).any(-1)
             assert not bad.any(), f"{name}: {bad.sum()} of {bad.size} paths differ from the reference shaders"
+
+
+def _live_pixels(v):
+    import pin_cases
+    n = v.width * v.height
+    if n <= pin_cases.LIVE_PIXELS:
+        return None
+    return np.sort(np.random.default_rng(n).choice(n, pin_cases.LIVE_PIXELS, replace=False)).astype(np.uint32)
 
 
 OFFLINE_RTOL = 1e-6   # the offline raygen regroups the analytic-light NEE products
@@ -278,4 +287,6 @@ def test_integrator_within_offline_raygen_live(oracle):
         sd = make()
         scene = oracle.OracleScene(sd, flatten_limit=flatten_limit)
         v = sd.views[0]
-        _offline_check(name, sd, scene.render_paths(v, settings, 0, 2), oracle.shader_paths(P, scene, v, settings, 0, 2))
+        pix = _live_pixels(v)
+        _offline_check(name, sd, scene.render_paths(v, settings, 0, 2, pixels=pix),
+                       oracle.shader_paths(P, scene, v, settings, 0, 2, pix))
