@@ -6,7 +6,6 @@ on fixed inputs. Run in a container that has the reference checkout:
 
     python tests/golden/make_golden.py
 """
-import ctypes as C
 import json
 import os
 import sys
