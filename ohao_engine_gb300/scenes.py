@@ -10,6 +10,9 @@ ranges and 64-byte instance records.
 Workloads (all seeds fixed):
 
 * ``cornell``     -- Cornell box, 36 triangles, one area light, 256x256.
+* ``cornell_example`` -- the reference example's Cornell box (five walls,
+  two primitive spheres, twelve sphere lights) at 1920x1080, the scene of
+  its golden image; a parity case, not a benchmark workload.
 * ``sphere_1m``   -- geodesic sphere of frequency 224 (1,003,520 triangles)
   displaced by 5% value noise plus a 2-triangle ground plane, per-triangle
   GGX materials, 1024x512 sky + sun environment, 1920x1080.
@@ -434,3 +437,147 @@ def studio(freq=100, seed=1, side=512, n_train=8, n_holdout=2, map_size=64, albe
 
 
 WORKLOADS = {"cornell": cornell, "sphere_1m": sphere_1m, "instanced": instanced, "studio": studio}
+
+
+def _f32(x):
+    return np.float32(x)
+
+
+def _glm_sphere_mesh(radius=0.5, sectors=32, stacks=16):
+    """The primitive sphere of ``ComponentFactory::generateSphereMesh``
+    (``scene/component/component_factory.cpp:347-395``): a UV sphere of
+    radius 0.5, 32 sectors x 16 stacks, angles and products in float32,
+    sin/cos of the float angle evaluated in double and rounded (the C
+    library's double sin/cos), unit normals = the unscaled positions."""
+    pi = _f32(math.pi)
+    pos, nrm, uv = [], [], []
+    for i in range(stacks + 1):
+        phi = _f32(_f32(pi * _f32(i)) / _f32(stacks))
+        sp, cp = _f32(math.sin(float(phi))), _f32(math.cos(float(phi)))
+        for j in range(sectors + 1):
+            theta = _f32(_f32(_f32(2.0) * pi * _f32(j)) / _f32(sectors))
+            st, ct = _f32(math.sin(float(theta))), _f32(math.cos(float(theta)))
+            x, y, z = _f32(ct * sp), cp, _f32(st * sp)
+            r = _f32(radius)
+            pos.append((x * r, y * r, z * r))
+            nrm.append((x, y, z))
+            uv.append((_f32(j) / _f32(sectors), _f32(i) / _f32(stacks)))
+    idx = []
+    for i in range(stacks):
+        for j in range(sectors):
+            first = i * (sectors + 1) + j
+            second = first + sectors + 1
+            idx.append((first, second, first + 1))
+            idx.append((second, second + 1, first + 1))
+    return (np.array(pos, np.float32), np.array(nrm, np.float32), np.array(uv, np.float32), idx)
+
+
+def _glm_look_at_inverse(eye, yaw_deg, pitch_deg):
+    """Inverse view matrix (column-major) of OHAO's camera
+    (``render/camera/camera.cpp:25-42``: front from yaw/pitch, right/up by
+    cross products, ``glm::lookAt``), built in float32 and inverted in double."""
+    rad = _f32(0.017453292519943295)
+    yaw, pitch = _f32(_f32(yaw_deg) * rad), _f32(_f32(pitch_deg) * rad)
+    cy, sy = _f32(math.cos(float(yaw))), _f32(math.sin(float(yaw)))
+    cpi, spi = _f32(math.cos(float(pitch))), _f32(math.sin(float(pitch)))
+    front = np.array([cy * cpi, spi, sy * cpi], np.float32)
+
+    def normalize(v):
+        return (v * _f32(1.0 / math.sqrt(float(np.dot(v, v))))).astype(np.float32)
+
+    front = normalize(front)
+    right = normalize(np.cross(front, np.array([0, 1, 0], np.float32)).astype(np.float32))
+    up = normalize(np.cross(right, front).astype(np.float32))
+    eye = np.asarray(eye, np.float32)
+    f = normalize((eye + front).astype(np.float32) - eye)
+    s = normalize(np.cross(f, up).astype(np.float32))
+    u = np.cross(s, f).astype(np.float32)
+    view = np.eye(4)
+    view[0, :3], view[1, :3], view[2, :3] = s, u, -f
+    view[0, 3], view[1, 3], view[2, 3] = -np.dot(s, eye), -np.dot(u, eye), np.dot(f, eye)
+    return np.linalg.inv(view.astype(np.float32).astype(np.float64)).T.reshape(-1).astype(np.float32)
+
+
+# light colours and positions of the reference example's 12 sphere lights
+_EXAMPLE_LIGHT_COLORS = [(1.0, 0.3, 0.2), (0.2, 1.0, 0.3), (0.3, 0.4, 1.0), (1.0, 0.9, 0.3), (1.0, 0.5, 0.0),
+                         (0.8, 0.2, 1.0), (0.0, 1.0, 1.0), (1.0, 0.0, 0.5), (1.0, 1.0, 1.0), (0.5, 1.0, 0.5),
+                         (1.0, 0.7, 0.5), (0.5, 0.7, 1.0)]
+_EXAMPLE_LIGHT_POS = [(-3, 4, -3), (0, 4, -3), (3, 4, -3), (-3, 4, 0), (0, 4, 0), (3, 4, 0),
+                      (-3, 4, 3), (0, 4, 3), (3, 4, 3), (-4, 0, 0), (4, 0, 0), (0, 0, -4)]
+# Upload order of the 12 lights. The engine walks its actor table, an
+# std::unordered_map keyed by sequential actor ids (the root actor is 1, the
+# five walls 2-6, the two spheres 7-8, the lights 9-20); libstdc++ iterates
+# those 20 keys as 20, 19, ..., 14, 1, 2, ..., 13, so the light records go
+# out as lights 11..5 followed by lights 0..4.
+EXAMPLE_LIGHT_ORDER = (11, 10, 9, 8, 7, 6, 5, 0, 1, 2, 3, 4)
+
+
+def cornell_example(width=1920, height=1080, spp=16, light_order=EXAMPLE_LIGHT_ORDER) -> SceneData:
+    """The reference's ``examples/cornell_box.cpp`` scene as its renderer
+    uploads it, the scene of its golden image ``tests/golden/cornell_box.png``:
+    five 10x10 walls (white 0.73, red, green; roughness 0.95), a metal sphere
+    (radius 1 at (-2, -3, 0), roughness 0.05) and a dielectric one (radius 0.9
+    at (2.5, -3.2, 1.5), roughness 0.02), both the 32x16 primitive UV sphere
+    as instances of their own BLAS; twelve coloured sphere lights (intensity
+    5, radius 0.3); no environment (misses are black); camera at (0, 0, 13),
+    yaw -90, 38 degree vertical field of view. Actors are packed in the
+    engine's order (walls Back, Left, Right, Floor, Ceiling, then the two
+    spheres), one BLAS and one material per actor, instance custom index =
+    the actor's first global triangle (``gpu/vulkan/rt_build.cpp:825-900``,
+    ``scene_upload.cpp:20-80``)."""
+    S = 5.0
+    white, red, green = (0.73, 0.73, 0.73), (0.65, 0.05, 0.05), (0.12, 0.45, 0.15)
+    LBB, RBB, LTB, RTB = (-S, -S, -S), (S, -S, -S), (-S, S, -S), (S, S, -S)
+    LBF, RBF, LTF, RTF = (-S, -S, S), (S, -S, S), (-S, S, S), (S, S, S)
+    walls = [((LBB, RBB, RTB, LTB), (0, 0, 1), white), ((LBB, LTB, LTF, LBF), (1, 0, 0), red),
+             ((RBB, RBF, RTF, RTB), (-1, 0, 0), green), ((LBB, LBF, RBF, RBB), (0, 1, 0), white),
+             ((LTB, RTB, RTF, LTF), (0, -1, 0), white)]
+    b = _Builder()
+    blas, mats, xforms = [], [], []
+    ident = np.array([1, 0, 0, 0, 0, 1, 0, 0, 0, 0, 1, 0], np.float32)
+    for k, (quad, n, col) in enumerate(walls):
+        pos = np.array(quad, np.float32)
+        uv = np.zeros((4, 2), np.float32)
+        blas.append(b.add(pos, np.tile(np.array(n, np.float32), (4, 1)), uv, [[0, 1, 2], [0, 2, 3]], k))
+        mats.append(material(col, rough=0.95))
+        xforms.append(ident)
+    spos, snrm, suv, sidx = _glm_sphere_mesh()
+    spheres = [((-2.0, -S + 2.0, 0.0), 2.0, (0.95, 0.93, 0.88), 0.05, 1.0),
+               ((2.5, -S + 1.8, 1.5), 1.8, (0.9, 0.95, 1.0), 0.02, 0.0)]
+    for k, (c, scale, col, rough, metal) in enumerate(spheres):
+        blas.append(b.add(spos, snrm, suv, sidx, len(walls) + k))
+        mats.append(material(col, rough=rough, metal=metal))
+        c = np.array(c, np.float32)
+        sc = _f32(scale)
+        xforms.append(np.array([sc, 0, 0, c[0], 0, sc, 0, c[1], 0, 0, sc, c[2]], np.float32))
+    pos, nrm, uv, idx, mid = b.arrays()
+    inst = np.zeros(len(blas), INSTANCE_DTYPE)
+    tri0 = 0
+    for k, (first, count) in enumerate(blas):
+        inst[k]["blas"] = k
+        inst[k]["xform"] = xforms[k]
+        inst[k]["custom_index"] = tri0
+        inst[k]["mask"] = 0xFF
+        tri0 += count // 3
+    lights = []
+    for i in light_order:
+        L = np.zeros(20, np.float32)
+        L[0:3] = _EXAMPLE_LIGHT_POS[i]
+        L[3] = 0.0
+        L[4:7] = _EXAMPLE_LIGHT_COLORS[i]
+        L[7] = 5.0
+        L[8:11] = (-0.3, -1.0, -0.2) / np.float32(np.linalg.norm((-0.3, -1.0, -0.2)))
+        L[11] = 0.3
+        lights.append(L)
+    inv_view = _glm_look_at_inverse((0.0, 0.0, 13.0), -90.0, 0.0)
+    t = np.float32(math.tan(float(_f32(_f32(38.0) * _f32(0.017453292519943295)) / _f32(2.0))))
+    # inverse of glm::perspective(fov, aspect, 0.1, 1000) (OpenGL depth range),
+    # column-major; the raygen reads only |[1][1]| = tan(fov / 2)
+    inv_proj = np.zeros(16, np.float32)
+    aspect = _f32(_f32(width) / _f32(height))
+    inv_proj[0] = _f32(1.0) / _f32(_f32(1.0) / _f32(aspect * t))
+    inv_proj[5] = _f32(1.0) / _f32(_f32(1.0) / t)
+    inv_proj[11], inv_proj[14], inv_proj[15] = -4.9995, -1.0, 5.0005
+    view = View(inv_view, inv_proj, int(width), int(height))
+    return SceneData("cornell_example", pos, nrm, uv, idx, mid, np.stack(mats), np.stack(lights), None, 1.0,
+                     blas, inst, [view], spp=spp, max_bounces=4)
