@@ -19,9 +19,10 @@ rays, geometry, the Sobol streams and light selection follow the reference's
 GPU render. What does not agree: radiance. The golden's 8-bit values are
 about 0.7 times the oracle's (about 0.6 times in radiance), with a slight
 colour shift, and no single scale of the light intensity brings the pixels
-together (the closest leaves a mean difference of 3 LSB). The reference's own shaders, compiled
-as C++ over the same scene, give the oracle's radiance, not the golden's
-(within 3.2e-7 relative on 4,096 pixels x 4 samples). The checkout has no
+together (the closest leaves a mean difference of 3 LSB). The reference's
+own shaders, compiled as C++ over the same scene, give the oracle's
+radiance, not the golden's (within 3.2e-7 relative on 4,096 pixels x 4
+samples; the last test here checks 1,024 pixels). The checkout has no
 history to show which engine revision wrote the golden. Parity at this level
 is therefore partial; the tolerance of ``tests/golden/manifest.json``
 (max 4 LSB, at most 1% of pixels differing) is not met.
@@ -138,3 +139,27 @@ def test_noise_correlation_discriminates(oracle, band_sobol):
     assert noise_correlation(render_band(oracle, scenes.cornell_example(), sampler=0), BAND["band"]) < 0.3
     ratio = BAND["band"].reshape(-1, 3).mean(axis=0) / band_sobol.reshape(-1, 3).mean(axis=0)
     assert np.all(ratio < 0.8), f"golden / oracle mean 8-bit value {ratio}"
+
+
+def test_example_scene_radiance_equals_reference_shaders(oracle):
+    """Where the reference tree exists: on this scene the reference's offline
+    raygen, closest-hit and miss shaders compiled as C++ give the oracle's
+    per-path radiance (within the 1e-6 relative that the offline raygen's
+    regrouped light-sampling products allow), so the radiance gap to the
+    golden image is not in the restatement of those shaders."""
+    import glsl_pin
+    lib = oracle.glsl_pt_lib("offline")
+    if lib is None and glsl_pin.pt_available():
+        glsl_pin.build_pt()
+        lib = oracle.glsl_pt_lib("offline")
+    if lib is None:
+        pytest.skip("reference shaders not available here")
+    sd = scenes.cornell_example()
+    v = sd.views[0]
+    scene = oracle.OracleScene(sd)
+    pix = np.sort(np.random.default_rng(7).choice(v.width * v.height, 1024, replace=False)).astype(np.uint32)
+    settings = dict(max_bounces=4, sampler=1)
+    got = scene.render_paths(v, settings, 0, 2, pixels=pix)
+    want = oracle.shader_paths(lib, scene, v, settings, 0, 2, pix)
+    rel = np.abs(got - want) / np.maximum(np.maximum(np.abs(got), np.abs(want)), 1e-3)
+    assert rel.max() <= 1e-6, f"oracle vs the reference's offline shaders: {rel.max():.3g} relative"
