@@ -46,6 +46,9 @@ def parse():
     ap.add_argument("--workload", default="sphere_1m", choices=["sphere_1m", "cornell", "instanced", "studio", "denoise"])
     ap.add_argument("--cpu-seconds", type=float, default=12.0)
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--case", default=None, choices=sorted(CASES),
+                    help="run one small profiling case instead of the benchmark (one process, a few GB at most)")
+    ap.add_argument("--case-arg", default=None, help="launch shape name for --case instanced_pool")
     return ap.parse_args()
 
 
@@ -668,9 +671,106 @@ def run_denoise(args, n_scenes=50, iters=10000, crop=128, batch=8, variants=6):
     pt.close()
 
 
+# ---------------------------------------------------------------------------
+# Small profiling cases (bench.py --case NAME): self-contained runs of one
+# GPU path for ncu captures, each printing its CUDA-event time per call.
+# ---------------------------------------------------------------------------
+def _timed_calls(fn, reps):
+    import torch
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record()
+    for _ in range(reps):
+        fn()
+    e1.record()
+    e1.synchronize()
+    return e0.elapsed_time(e1) / reps
+
+
+def case_denoise_infer(arg):
+    """U-Net inference at 1920x1080 on seeded inputs (3 + 10 calls)."""
+    import torch
+    from ohao_engine_gb300.denoise import Denoiser
+    w, h = 1920, 1080
+    rng = np.random.default_rng(0)
+    rad = torch.from_numpy(rng.exponential(0.5, (w * h, 4)).astype(np.float32)).cuda()
+    aov = torch.from_numpy(rng.random((w * h, 12)).astype(np.float32)).cuda()
+    out = torch.zeros((w * h, 4), dtype=torch.float32, device="cuda")
+    dn = Denoiser(max_pixels=1920 * 1088, seed=1)
+    for _ in range(3):
+        dn.infer([rad], [aov], [out], w, h)
+    ms = _timed_calls(lambda: dn.infer([rad], [aov], [out], w, h), 10)
+    print(f"denoise_infer 1920x1080: {ms:.3f} ms per call")
+
+
+def case_adjoint(arg):
+    """ohao_pt_adjoint on the studio scene, one 256^2 view, 4 spp (2 calls)."""
+    import torch
+    import ohao_engine_gb300 as og
+    from ohao_engine_gb300 import scenes
+    sd = scenes.studio(n_train=1, n_holdout=0, side=256)
+    pt = og.PathTracer()
+    pt.load_scene(sd)
+    v = sd.views[0]
+    npix = v.width * v.height
+    tgt = torch.full((npix, 4), 0.3, device="cuda")
+    acc = torch.zeros((npix, 4), device="cuda")
+    gm = torch.zeros(sd.albedo_map.size, device="cuda")
+    gr = torch.zeros(sd.materials.shape[0], device="cuda")
+    s = og.make_settings(spp=4, max_bounces=3, flags=og.FLAG_ADJOINT_DECORRELATE)
+    ms = _timed_calls(lambda: pt.adjoint([og.make_view(v, accum=acc)], s, [tgt], gm, gr), 2)
+    print(f"adjoint studio 256^2 x 4 spp: {ms:.3f} ms per call")
+
+
+def case_instanced_view(arg):
+    """One 512^2 view of the instanced scene, 4 spp, per-view wavefront (3 calls)."""
+    import torch
+    import ohao_engine_gb300 as og
+    from ohao_engine_gb300 import scenes
+    sd = scenes.instanced(n_views=1, side_range=(512, 512))
+    pt = og.PathTracer()
+    pt.load_scene(sd)
+    v = sd.views[0]
+    acc = torch.zeros((v.width * v.height, 4), device="cuda")
+    s = og.make_settings(spp=4, max_bounces=4, mode=og.MODE_WAVEFRONT)
+    ms = _timed_calls(lambda: pt.render([og.make_view(v, accum=acc)], s), 3)
+    print(f"instanced one 512^2 view x 4 spp: {ms:.3f} ms per call")
+
+
+def case_instanced_pool(arg):
+    """Four 384^2 views of the instanced scene, 4 spp, persistent pool (2 calls)."""
+    import torch
+    import ohao_engine_gb300 as og
+    from ohao_engine_gb300 import scenes
+    sd = scenes.instanced(n_views=4, side_range=(384, 384))
+    pt = og.PathTracer()
+    pt.load_scene(sd)
+    pt.launch_config = arg or "pool_4M_unsorted_fetch4_chunk8"
+    accs = [torch.zeros((v.width * v.height, 4), device="cuda") for v in sd.views]
+    s = og.make_settings(spp=4, max_bounces=4, mode=og.MODE_PERSISTENT)
+    ms = _timed_calls(lambda: pt.render([og.make_view(v, accum=a) for v, a in zip(sd.views, accs)], s), 2)
+    print(f"instanced 4 views 384^2 x 4 spp, {pt.launch_config}: {ms:.3f} ms per call")
+
+
+CASES = {"denoise_infer": case_denoise_infer, "adjoint": case_adjoint, "instanced_view": case_instanced_view,
+         "instanced_pool": case_instanced_pool}
+
+
+def run_case(args):
+    import torch
+    import ohao_engine_gb300 as og
+    from ohao_engine_gb300 import _build
+    torch.cuda.set_device(0)
+    if not os.path.exists(og.LIB_PATH):
+        _build.build()
+    og.load_library()
+    CASES[args.case](args.case_arg)
+
+
 def main():
     args = parse()
-    if args.impl == "reference":
+    if args.case:
+        run_case(args)
+    elif args.impl == "reference":
         run_reference(args)
     elif args.workload == "instanced":
         run_instanced(args)

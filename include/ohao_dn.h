@@ -44,6 +44,14 @@ ohao_status ohao_dn_create(const ohao_dn_desc* desc, ohao_dn_ctx** out);
 void ohao_dn_destroy(ohao_dn_ctx* ctx);
 const char* ohao_dn_last_error(const ohao_dn_ctx* ctx);
 
+/* Check of the tensor-core pipeline's bounded waits (no counterpart in the
+ * reference): one kernel waits spin_limit polls (1..65536) on an mbarrier
+ * whose phase never completes -- no MMA is issued and no tensor memory is
+ * held -- and records the timeout as every convolution kernel does. Returns
+ * OHAO_ERR_TIMEOUT, the status a convolution reports when one of its waits
+ * gives up; the context stays usable. */
+ohao_status ohao_dn_wait_selftest(ohao_dn_ctx* ctx, uint32_t spin_limit, ohao_stream stream);
+
 /* Parameters as FP32 host arrays, layer by layer: W[cout][3][3][cin] then
  * bias[cout]. */
 uint64_t ohao_dn_param_count(const ohao_dn_ctx* ctx);

@@ -129,7 +129,11 @@ typedef struct ohao_pt_settings {
     float aniso_strength;      /* jitter.z */
     float aniso_rotation;      /* jitter.w */
     uint32_t mode;             /* OHAO_PT_MODE_* */
-    uint32_t reserved[7];
+    /* Traversal stack entries per ray (0 = all 64). A smaller limit makes
+     * deep traversals stop with OHAO_ERR_DEVICE_CHECK instead of finishing;
+     * it exists to exercise that check. Not the reference's. */
+    uint32_t trace_stack_limit;
+    uint32_t reserved[6];
 } ohao_pt_settings;
 
 /* Per-kernel timings of the last profiled render/trace (CUDA events on the
@@ -276,19 +280,21 @@ ohao_status ohao_pt_bvh_download(ohao_pt_ctx* ctx, int32_t which, void* nodes, v
  * No counterpart in the reference (its BVH builds happen inside the Vulkan
  * driver). For callers that cannot call cudaMalloc: a host application that
  * gives the renderer a fixed memory budget and owns the rest of the GPU, or a
- * per-frame rebuild of a small animated mesh (createBLASFromPositions,
- * rt_acceleration_structure.cpp:322-400) where an allocation would
- * synchronise the device. Builds the same 8-wide BVH as ohao_pt_build over n
- * primitive boxes (device, 6 floats lo.xyz hi.xyz each), n <= 65536:
- * d_nodes (device) receives up to n ohao_bvh8_node records, d_prim_order
- * (device, n uint32) the box index of each leaf slot, d_root_box (device) 6
- * floats; *out_nnodes / *out_height are written on the host. Larger n returns
- * OHAO_ERR_TOO_LARGE. The build scratch is one fixed array in device memory
+ * per-frame rebuild of a small animated mesh where an allocation would
+ * synchronise the device and stall the engine's other streams. Builds the
+ * same 8-wide BVH as ohao_pt_build over n primitive boxes (device, 6 floats
+ * lo.xyz hi.xyz each), n <= 65536: d_nodes (device) receives up to n
+ * ohao_bvh8_node records, d_prim_order (device, n uint32) the box index of
+ * each leaf slot, d_root_box (device) 6 floats; *out_nnodes / *out_height
+ * are written on the host. Larger n returns OHAO_ERR_TOO_LARGE before the
+ * device is touched. The build scratch is one fixed array in device memory
  * (about 9.2 MB per GPU that loads the library, held until exit) shared by
  * every call: calls that overlap on the GPU (other threads or streams) race
  * on it and must be serialised by the caller. The first call on a device
- * resolves the array's device address and should come before any stream
- * capture. Synchronous with respect to `stream`. */
+ * resolves the array's device address (cached per device ordinal; a
+ * cudaDeviceReset of that device invalidates it, so the library is not used
+ * on a device after a reset) and should come before any stream capture.
+ * Every call blocks the host until its build on `stream` has finished. */
 #define OHAO_BVH_NOALLOC_MAX_PRIMS 65536u
 ohao_status ohao_bvh_build_noalloc(const float* d_boxes, uint32_t n, void* d_nodes, uint32_t* d_prim_order,
                                    float* d_root_box, uint32_t* out_nnodes, uint32_t* out_height, ohao_stream stream);

@@ -122,6 +122,16 @@ ohao_status upload(ohao_pt_ctx* ctx, DevBuf& b, const void* src, size_t bytes, c
     return OHAO_OK;
 }
 
+// True when the row-major 3x4 transform is finite and its 3x3 part has a
+// non-zero, finite determinant (computed in double, as instance_matrices does).
+bool instance_invertible(const float x[12]) {
+    for (int k = 0; k < 12; ++k)
+        if (!std::isfinite(x[k])) return false;
+    const double a = x[0], b = x[1], c = x[2], d = x[4], e = x[5], f = x[6], g = x[8], h = x[9], i = x[10];
+    const double det = a * (e * i - f * h) - b * (d * i - f * g) + c * (d * h - e * g);
+    return det != 0.0 && std::isfinite(det);
+}
+
 void instance_matrices(const float x[12], float w2o[12], float nrm[9]) {
     const double a = x[0], b = x[1], c = x[2], d = x[4], e = x[5], f = x[6], g = x[8], h = x[9], i = x[10];
     const double A = e * i - f * h, B = -(d * i - f * g), C = d * h - e * g;
@@ -196,6 +206,7 @@ ohao::DScene make_scene(const ohao_pt_ctx* c) {
     s.albedo_map = c->albedo_map.as<float>();
     s.map_w = c->map_w;
     s.map_h = c->map_h;
+    s.stack_limit = 0;
     return s;
 }
 
@@ -311,21 +322,27 @@ ohao_status ohao_pt_build(ohao_pt_ctx* ctx, ohao_stream stream) {
     for (const auto& b : ctx->blas)
         if (static_cast<uint64_t>(b.first_index) + b.index_count > static_cast<uint64_t>(ctx->ntris) * 3)
             return fail(ctx, OHAO_ERR_INVALID_ARG, "build: a BLAS index range lies outside the current geometry");
-    const uint32_t ninst = static_cast<uint32_t>(ctx->instances.size());
+    // An instance whose 3x3 part is singular (zero scale, often used to hide
+    // an instance) or not finite has no world-to-object transform: it is
+    // treated as masked out, in the flat and the two-level build alike.
+    std::vector<ohao_pt_instance> insts = ctx->instances;
+    for (auto& in : insts)
+        if (!instance_invertible(in.transform)) in.mask = 0;
+    const uint32_t ninst = static_cast<uint32_t>(insts.size());
     // per-instance device records
     std::vector<ohao::DInst> di(std::max(ninst, 1u));
     for (uint32_t i = 0; i < ninst; ++i) {
-        instance_matrices(ctx->instances[i].transform, di[i].w2o, di[i].nrm);
-        di[i].custom = ctx->instances[i].custom_index;
-        di[i].blas = ctx->instances[i].blas;
-        di[i].mask = ctx->instances[i].mask;
+        instance_matrices(insts[i].transform, di[i].w2o, di[i].nrm);
+        di[i].custom = insts[i].custom_index;
+        di[i].blas = insts[i].blas;
+        di[i].mask = insts[i].mask;
     }
     ohao_status s = upload(ctx, ctx->inst_dev, di.data(), di.size() * sizeof(ohao::DInst), "instances");
     if (s != OHAO_OK) return s;
     uint64_t total = 0;
-    for (const auto& in : ctx->instances)
+    for (const auto& in : insts)
         if (in.mask & 0xFFu) total += ctx->blas[in.blas].index_count / 3;
-    for (const auto& in : ctx->instances) {
+    for (const auto& in : insts) {
         const uint64_t last = static_cast<uint64_t>(in.custom_index & 0xFFFFFFu) + ctx->blas[in.blas].index_count / 3;
         if ((in.mask & 0xFFu) && last > ctx->ntris)
             return fail(ctx, OHAO_ERR_INVALID_ARG, "build: custom_index + primitive id exceeds the global triangle count");
@@ -341,7 +358,7 @@ ohao_status ohao_pt_build(ohao_pt_ctx* ctx, ohao_stream stream) {
         std::vector<float> o2w;
         uint32_t acc = 0;
         for (uint32_t i = 0; i < ninst; ++i) {
-            const auto& in = ctx->instances[i];
+            const auto& in = insts[i];
             if (!(in.mask & 0xFFu)) continue;
             vis.push_back(i);
             first_index.push_back(ctx->blas[in.blas].first_index);
@@ -421,7 +438,7 @@ ohao_status ohao_pt_build(ohao_pt_ctx* ctx, ohao_stream stream) {
         std::vector<float> xf;
         std::vector<uint32_t> span, ids;
         for (uint32_t i = 0; i < ninst; ++i) {
-            const auto& in = ctx->instances[i];
+            const auto& in = insts[i];
             if (!(in.mask & 0xFFu) || ctx->blas_bvh[in.blas].nprims == 0) continue;
             xf.insert(xf.end(), in.transform, in.transform + 12);
             span.push_back(desc[in.blas].tri_off);
@@ -597,6 +614,7 @@ static ohao_status render_views(ohao_pt_ctx* ctx, const ohao_pt_view* views, uin
     const bool profile = (st->flags & OHAO_PT_FLAG_PROFILE) != 0;
     ohao::ProfileAcc acc;
     ohao::DScene sc = make_scene(ctx);
+    sc.stack_limit = st->trace_stack_limit;
     ohao::PathParams pp{st->max_bounces, st->sampler, st->flags, st->clamp_luminance, st->aniso_strength,
                         st->aniso_rotation, st->sample_index_base};
     const std::vector<ohao::RenderView> rvs = to_render_views(views, n_views, dev_accum);
@@ -729,7 +747,9 @@ static ohao_status run_backward(ohao_pt_ctx* ctx, const std::vector<ohao::Render
     const uint32_t n = static_cast<uint32_t>(rvs.size());
     CK(ctx->adj_scratch.ensure(ohao::adjoint_scratch_bytes(n)), "backward scratch");
     std::string err;
-    const ohao_status s = ohao::adjoint_backward(make_scene(ctx), rvs.data(), grads, n, pp, st->spp, ctx->nmats,
+    ohao::DScene sc = make_scene(ctx);
+    sc.stack_limit = st->trace_stack_limit;
+    const ohao_status s = ohao::adjoint_backward(sc, rvs.data(), grads, n, pp, st->spp, ctx->nmats,
                                                  ctx->adj_scratch.p, ctx->adj_scratch.n, d_grad_map, d_grad_rough, cs,
                                                  ctx->err_flag.as<int>(), err);
     if (s != OHAO_OK) return fail(ctx, s, err);

@@ -663,6 +663,3 @@ extern "C" ohao_status ohao_bvh_build_noalloc(const float* d_boxes, uint32_t n, 
     *out_height = info.height;
     return OHAO_OK;
 }
-
-namespace ohao {
-}  // namespace ohao

@@ -353,6 +353,10 @@ __global__ void __launch_bounds__(kThreads) k_conv(ConvArgs a, int* err_flag) {
             }
         }
     }
+    // A CTA must not exit holding tensor memory, so the columns are freed even
+    // after a wait gave up; MMAs still in flight then may write columns that
+    // are no longer this CTA's. The host reports OHAO_ERR_TIMEOUT and the
+    // denoiser context is to be destroyed and re-created after it.
     umma::tc_fence_before();
     __syncthreads();
     if (warp == 0) umma::tmem_dealloc(tmem, ncols);
@@ -739,6 +743,20 @@ __global__ void k_adam_b(float* __restrict__ b32, const float* __restrict__ g, f
     b32[i] -= lr * (mv / c1) / (sqrtf(vv / c2) + eps);
 }
 
+// Exercises the bounded wait of the tensor-core pipeline: thread 0 waits
+// with `limit` polls on an mbarrier whose phase never completes (no MMA and
+// no arrival is ever issued, no tensor memory is held), records the timeout
+// in err_flag exactly as k_conv does, and returns.
+__global__ void k_wait_probe(uint32_t limit, int* err_flag) {
+    __shared__ uint64_t bar;
+    if (threadIdx.x == 0) {
+        umma::mbar_init(&bar, 1);
+        umma::mbar_fence_init();
+    }
+    __syncthreads();
+    if (threadIdx.x == 0 && !umma::mbar_wait(&bar, 0, limit)) atomicOr(err_flag, 2);
+}
+
 int grid_for(int64_t n, int block) {
     return static_cast<int>(std::max<int64_t>(1, std::min<int64_t>((n + block - 1) / block, 152 * 16)));
 }
@@ -781,6 +799,10 @@ cudaError_t launch_conv(int mode, const ConvArgs& a, int wgrad_splits, int* err_
     return cudaGetLastError();
 }
 
+cudaError_t launch_wait_probe(uint32_t limit, int* err_flag, cudaStream_t st) {
+    k_wait_probe<<<1, 32, 0, st>>>(limit, err_flag);
+    return cudaGetLastError();
+}
 void launch_pool_fwd(const __nv_bfloat16* x, __nv_bfloat16* y, const Geo& lo, int c8, cudaStream_t st) {
     k_pool_fwd<<<grid_for(lo.npix * (c8 / 8), 256), 256, 0, st>>>(x, y, lo, c8);
 }

@@ -413,6 +413,14 @@ void ohao_dn_destroy(ohao_dn_ctx* ctx) {
 
 const char* ohao_dn_last_error(const ohao_dn_ctx* ctx) { return ctx ? ctx->last_error.c_str() : "null context"; }
 
+ohao_status ohao_dn_wait_selftest(ohao_dn_ctx* ctx, uint32_t spin_limit, ohao_stream stream) {
+    if (!ctx || spin_limit == 0 || spin_limit > (1u << 16)) return fail(ctx, OHAO_ERR_INVALID_ARG, "wait_selftest: limit");
+    cudaStream_t st = reinterpret_cast<cudaStream_t>(stream);
+    DN_CK(cudaSetDevice(ctx->device), "set device");
+    DN_CK(launch_wait_probe(spin_limit, ctx->err_flag.as<int>(), st), "wait probe");
+    return check_flag(ctx, st);
+}
+
 uint64_t ohao_dn_param_count(const ohao_dn_ctx* ctx) { return ctx ? count_params(ctx) : 0; }
 
 ohao_status ohao_dn_get_params(ohao_dn_ctx* ctx, float* host, uint64_t n) {

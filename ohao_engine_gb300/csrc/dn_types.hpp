@@ -60,6 +60,7 @@ struct ConvArgs {
 };
 
 size_t conv_smem_bytes(int bn);
+cudaError_t launch_wait_probe(uint32_t limit, int* err_flag, cudaStream_t st);
 cudaError_t launch_conv(int mode, const ConvArgs& a, int wgrad_splits, int* err_flag, cudaStream_t st);
 void launch_pool_fwd(const __nv_bfloat16* x, __nv_bfloat16* y, const Geo& lo, int c8, cudaStream_t st);
 void launch_pool_bwd(const __nv_bfloat16* x, const float* dy, float* dx, const Geo& lo, int c8, cudaStream_t st);

@@ -140,7 +140,10 @@ OHAO_D bool walk_step(const DScene& sc, Walk& w, const RayPre& r, float tmin, fl
             }
             const uint32_t rem = hit & imask;
             if (rem) {
-                if (!order_children(rem, tn, n, st_node, st_t, w.sp, w.cur, w.cur_tn)) { err = 1; return true; }
+                if (!order_children(rem, tn, n, st_node, st_t, w.sp, w.cur, w.cur_tn, stack_limit(sc))) {
+                    err = 1;
+                    return true;
+                }
                 desc = true;
             }
         }
@@ -171,7 +174,7 @@ OHAO_D bool walk_step(const DScene& sc, Walk& w, const RayPre& r, float tmin, fl
         enter_instance(sc, r, w.pq, w.plm, w.pidx, w.ra, w.bnodes, w.btris, w.inst, entered);
         if (entered) {
             w.base = w.sp;
-            if (w.base >= kStackSize) { err = 1; return true; }
+            if (w.base >= stack_limit(sc)) { err = 1; return true; }
             w.cur = 0u;
             w.cur_tn = -INFINITY;
             w.in_blas = true;
@@ -269,7 +272,7 @@ OHAO_D bool probe_step(const DScene& sc, Probe& w, const RayPre& r, float tmin, 
             const int i = __ffs(m) - 1;
             m &= m - 1;
             if (have) {
-                if (w.sp >= kStackSize) { err = 1; return true; }
+                if (w.sp >= stack_limit(sc)) { err = 1; return true; }
                 st_node[w.sp++] = next;
             }
             next = n.q1.x + (byte_of(n.q1.z, n.q1.w, i) & 7u);
@@ -302,7 +305,7 @@ OHAO_D bool probe_step(const DScene& sc, Probe& w, const RayPre& r, float tmin, 
         enter_instance(sc, r, w.pq, w.plm, w.pidx, w.ra, w.bnodes, w.btris, w.inst, entered);
         if (entered) {
             w.base = w.sp;
-            if (w.base >= kStackSize) { err = 1; return true; }
+            if (w.base >= stack_limit(sc)) { err = 1; return true; }
             w.cur = 0u;
             w.in_blas = true;
             w.have_node = true;

@@ -21,8 +21,9 @@
 // so nearby occluders are found sooner; the host oracle walks in slot order
 // -- the answer is the same boolean either way); the two-level any-hit
 // keeps slot order.
-// The stack holds 64 (node, t_near) entries in local memory; overflow sets
-// the error flag instead of faulting.
+// The stack holds 64 (node, t_near) entries in local memory (fewer when the
+// scene's stack_limit says so); overflow sets the error flag instead of
+// faulting or writing past the stack.
 #pragma once
 
 namespace ohao {
@@ -30,6 +31,14 @@ namespace ohao {
 constexpr float kTravRelSlack = 0x1p-14f;
 constexpr float kTravAbsScale = 0x1p-21f;
 constexpr int kStackSize = 64;
+
+// Stack entries a ray may use: the scene's limit (a smaller one makes deep
+// traversals report the overflow error; used to test that check), at most
+// kStackSize.
+OHAO_D int stack_limit(const DScene& sc) {
+    return (sc.stack_limit > 0u && sc.stack_limit < static_cast<uint32_t>(kStackSize)) ? static_cast<int>(sc.stack_limit)
+                                                                                       : kStackSize;
+}
 
 struct Hit {
     float t, u, v;
@@ -120,14 +129,14 @@ OHAO_D float pick8(const float v[8], int i) {
 // ties: lower slot first) and returns the nearest in (cur, cur_tn).
 // Returns false on stack overflow.
 OHAO_D bool order_children(uint32_t rem, const float tn[8], const NodeRec& n, uint32_t* st_node, float* st_t, int& sp,
-                           uint32_t& cur, float& cur_tn) {
+                           uint32_t& cur, float& cur_tn, int lim) {
     while (__popc(rem) > 1) {
         float bt = 0.0f;
         int bi = -1;
 #pragma unroll
         for (int i = 0; i < 8; ++i)
             if (((rem >> i) & 1u) && (bi < 0 || tn[i] > bt)) { bt = tn[i]; bi = i; }
-        if (sp >= kStackSize) return false;
+        if (sp >= lim) return false;
         st_node[sp] = n.q1.x + (byte_of(n.q1.z, n.q1.w, bi) & 7u);
         st_t[sp] = bt;
         sp++;
@@ -143,8 +152,8 @@ OHAO_D bool order_children(uint32_t rem, const float tn[8], const NodeRec& n, ui
 template <bool kStats>
 OHAO_D void bvh_closest(const uint4* __restrict__ nodes, const float4* __restrict__ tris, const RayPre& r,
                         float tmin, float tmax, Hit& best, uint32_t inst_override, uint32_t* st_node, float* st_t,
-                        int stack_base, TravCount& cnt, int& err) {
-    if (stack_base >= kStackSize) { err = 1; return; }
+                        int stack_base, int lim, TravCount& cnt, int& err) {
+    if (stack_base >= lim) { err = 1; return; }
     int sp = stack_base;
     uint32_t cur = 0u;
     float cur_tn = -INFINITY;
@@ -178,7 +187,7 @@ OHAO_D void bvh_closest(const uint4* __restrict__ nodes, const float4* __restric
             }
             const uint32_t rem = hit & imask;
             if (rem) {
-                if (!order_children(rem, tn, n, st_node, st_t, sp, cur, cur_tn)) { err = 1; return; }
+                if (!order_children(rem, tn, n, st_node, st_t, sp, cur, cur_tn, lim)) { err = 1; return; }
                 continue;
             }
         }
@@ -192,8 +201,8 @@ OHAO_D void bvh_closest(const uint4* __restrict__ nodes, const float4* __restric
 // Any hit in one BVH.
 template <bool kStats>
 OHAO_D bool bvh_any(const uint4* __restrict__ nodes, const float4* __restrict__ tris, const RayPre& r, float tmin,
-                    float tmax, uint32_t* st_node, int stack_base, TravCount& cnt, int& err) {
-    if (stack_base >= kStackSize) { err = 1; return false; }
+                    float tmax, uint32_t* st_node, int stack_base, int lim, TravCount& cnt, int& err) {
+    if (stack_base >= lim) { err = 1; return false; }
     int sp = stack_base;
     uint32_t cur = 0u;
     while (true) {
@@ -224,7 +233,7 @@ OHAO_D bool bvh_any(const uint4* __restrict__ nodes, const float4* __restrict__ 
 #pragma unroll
                 for (int i = 0; i < 8; ++i)
                     if (((rem >> i) & 1u) && (bi < 0 || tn[i] > bt)) { bt = tn[i]; bi = i; }
-                if (sp >= kStackSize) { err = 1; return false; }
+                if (sp >= lim) { err = 1; return false; }
                 st_node[sp++] = n.q1.x + (byte_of(n.q1.z, n.q1.w, bi) & 7u);
                 rem &= ~(1u << bi);
             }
@@ -261,7 +270,8 @@ OHAO_D Hit scene_closest(const DScene& sc, V3 o, V3 d, float tmin, float tmax, T
     float st_t[kStackSize];
     const RayPre r = ray_pre(o, d);
     if (kLevels == 1 || (kLevels == 0 && !sc.two_level)) {
-        bvh_closest<kStats>(sc.nodes, sc.tris, r, tmin, tmax, best, 0xFFFFFFFFu, st_node, st_t, 0, cnt, err);
+        bvh_closest<kStats>(sc.nodes, sc.tris, r, tmin, tmax, best, 0xFFFFFFFFu, st_node, st_t, 0, stack_limit(sc), cnt,
+                            err);
         return best;
     }
     // Two-level: one loop whose every iteration visits one node (TLAS or
@@ -324,7 +334,10 @@ OHAO_D Hit scene_closest(const DScene& sc, V3 o, V3 d, float tmin, float tmax, T
                 }
                 const uint32_t rem = hit & imask;
                 if (rem) {
-                    if (!order_children(rem, tn, n, st_node, st_t, sp, cur, cur_tn)) { err = 1; return best; }
+                    if (!order_children(rem, tn, n, st_node, st_t, sp, cur, cur_tn, stack_limit(sc))) {
+                        err = 1;
+                        return best;
+                    }
                     desc = true;
                 }
             }
@@ -373,7 +386,7 @@ OHAO_D Hit scene_closest(const DScene& sc, V3 o, V3 d, float tmin, float tmax, T
             btris = sc.blas_tris + static_cast<size_t>(bl.tri_off) * 3;
             inst = ii;
             base = sp;
-            if (base >= kStackSize) { err = 1; return best; }
+            if (base >= stack_limit(sc)) { err = 1; return best; }
             cur = 0u;
             cur_tn = -INFINITY;
             in_blas = true;
@@ -401,7 +414,7 @@ OHAO_D bool scene_occluded(const DScene& sc, V3 o, V3 d, float tmin, float tmax,
     uint32_t st_node[kStackSize];
     const RayPre r = ray_pre(o, d);
     if (kLevels == 1 || (kLevels == 0 && !sc.two_level))
-        return bvh_any<kStats>(sc.nodes, sc.tris, r, tmin, tmax, st_node, 0, cnt, err);
+        return bvh_any<kStats>(sc.nodes, sc.tris, r, tmin, tmax, st_node, 0, stack_limit(sc), cnt, err);
     // Two-level, as one loop (see scene_closest): at a TLAS node the internal
     // children but the last (slot order) are pushed, its instance leaves are
     // entered in slot order, then the last internal child is visited.
@@ -438,7 +451,7 @@ OHAO_D bool scene_occluded(const DScene& sc, V3 o, V3 d, float tmin, float tmax,
                 const uint32_t meta = byte_of(n.q1.z, n.q1.w, i);
                 if ((imask >> i) & 1u) {
                     if (have) {
-                        if (sp >= kStackSize) { err = 1; return false; }
+                        if (sp >= stack_limit(sc)) { err = 1; return false; }
                         st_node[sp++] = next;
                     }
                     next = n.q1.x + (meta & 7u);
@@ -497,7 +510,7 @@ OHAO_D bool scene_occluded(const DScene& sc, V3 o, V3 d, float tmin, float tmax,
             bnodes = sc.blas_nodes + static_cast<size_t>(bl.node_off) * 5;
             btris = sc.blas_tris + static_cast<size_t>(bl.tri_off) * 3;
             base = sp;
-            if (base >= kStackSize) { err = 1; return false; }
+            if (base >= stack_limit(sc)) { err = 1; return false; }
             cur = 0u;
             in_blas = true;
             have_node = true;

@@ -50,6 +50,7 @@ struct DScene {
     int has_env, has_cdf;
     const float* albedo_map;
     uint32_t map_w, map_h;
+    uint32_t stack_limit;   // traversal stack entries per ray; 0 or >= 64 = all 64
 };
 
 struct PathParams {

@@ -17,7 +17,7 @@ from . import AOV_FLOATS, OhaoError, OK, _buffer, _ptr, load_library, make_setti
 EXPORTED_SYMBOLS = [
     "ohao_dn_create", "ohao_dn_destroy", "ohao_dn_last_error", "ohao_dn_param_count", "ohao_dn_get_params",
     "ohao_dn_set_params", "ohao_dn_save", "ohao_dn_load", "ohao_dn_infer", "ohao_dn_train_step",
-    "ohao_dn_get_grads", "ohao_dn_tensor",
+    "ohao_dn_get_grads", "ohao_dn_tensor", "ohao_dn_wait_selftest",
 ]
 
 
@@ -43,6 +43,7 @@ def _bind(L):
                                 C.POINTER(f32), vp], i32),
         "ohao_dn_get_grads": ([vp, vp, u64], i32),
         "ohao_dn_tensor": ([vp, i32, i32, vp, u64, C.POINTER(u32), C.POINTER(u64)], i32),
+        "ohao_dn_wait_selftest": ([vp, u32, vp], i32),
     }
     for name, (args, res) in sigs.items():
         fn = getattr(L, name)
@@ -129,6 +130,11 @@ class Denoiser:
                                             width, height, lr, C.byref(loss),
                                             _ptr(stream) if stream is not None else None), "train_step")
         return loss.value
+
+    def wait_selftest(self, spin_limit: int = 1024, stream=None) -> int:
+        """Status of ohao_dn_wait_selftest: a bounded tensor-core pipeline
+        wait that is made to run out (OHAO_ERR_TIMEOUT, -4, expected)."""
+        return int(self._L.ohao_dn_wait_selftest(self.h, spin_limit, _ptr(stream) if stream is not None else None))
 
     def tensor(self, index: int, grad: bool = False) -> np.ndarray:
         ch, px = C.c_uint32(), C.c_uint64()

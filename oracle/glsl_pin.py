@@ -33,7 +33,7 @@ import re
 import subprocess
 
 HERE = os.path.dirname(os.path.abspath(__file__))
-REF_ROOT = "/root/reference"
+REF_ROOT = os.environ.get("OHAO_REFERENCE_ROOT", "/root/reference")   # the reference checkout, where present
 LIB_PATH = os.path.join(HERE, "_ref", "libohao_glsl.so")
 
 GLSL_FILES = [

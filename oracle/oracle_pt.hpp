@@ -80,6 +80,17 @@ inline void affine_xform_dir(const float m[12], const float d[3], float out[3]) 
     for (int r = 0; r < 3; ++r) out[r] = (m[r * 4 + 0] * d[0] + m[r * 4 + 1] * d[1]) + m[r * 4 + 2] * d[2];
 }
 
+// An instance transform is usable when it is finite and its 3x3 part has a
+// non-zero, finite determinant (double); the build treats any other instance
+// as masked out (ohao_pt_build does the same).
+inline bool instance_invertible(const float x[12]) {
+    for (int k = 0; k < 12; ++k)
+        if (!std::isfinite(x[k])) return false;
+    const double a = x[0], b = x[1], c = x[2], d = x[4], e = x[5], f = x[6], g = x[8], h = x[9], i = x[10];
+    const double det = a * (e * i - f * h) - b * (d * i - f * g) + c * (d * h - e * g);
+    return det != 0.0 && std::isfinite(det);
+}
+
 // Inverse of a row-major 3x4 affine transform and the normal matrix
 // transpose(inverse(M3)), computed in double by cofactors, rounded to float.
 inline void instance_matrices(const float x[12], float w2o[12], float nrm[9]) {
@@ -144,7 +155,10 @@ struct Scene {
     // ohao_pt_build: flat BVH over world-space triangles when the instanced
     // triangle count is <= flatten_limit, two-level TLAS/BLAS otherwise.
     void build(uint64_t flatten_limit, int force_mode) {
-        for (auto& in : instances) instance_matrices(in.xform, in.w2o, in.nrm);
+        for (auto& in : instances) {
+            if (!instance_invertible(in.xform)) in.mask = 0;
+            instance_matrices(in.xform, in.w2o, in.nrm);
+        }
         uint64_t total = 0;
         for (auto& in : instances)
             if (in.mask & 0xFFu) total += blases[in.blas].index_count / 3;

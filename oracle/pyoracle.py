@@ -17,7 +17,7 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 LIB_PATH = os.path.join(HERE, "_build", "liboracle.so")
 REF_PATH = os.path.join(HERE, "_ref", "libohao_ref.so")
 GLSL_PATH = os.path.join(HERE, "_ref", "libohao_glsl.so")
-REF_ROOT = "/root/reference"
+REF_ROOT = os.environ.get("OHAO_REFERENCE_ROOT", "/root/reference")   # the reference checkout, where present
 
 _lib = None
 

@@ -18,7 +18,7 @@ import zlib
 import numpy as np
 
 HERE = os.path.dirname(os.path.abspath(__file__))
-REF_PNG = "/root/reference/tests/golden/cornell_box.png"
+REF_PNG = os.path.join(os.environ.get("OHAO_REFERENCE_ROOT", "/root/reference"), "tests/golden/cornell_box.png")
 OUT = os.path.join(HERE, "cornell_example_band.npz")
 ROWS = (100, 140)
 

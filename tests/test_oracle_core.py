@@ -211,3 +211,27 @@ def test_scene_without_visible_geometry(oracle, kind):
         assert np.all(h[:, 3:5] == 0xFFFFFFFF), f"mode {mode}: a hit in a scene without geometry"
     p = orc.render_paths(sd.views[0], dict(max_bounces=4, sampler=0), 0, 2)
     assert p.shape == (2, 32, 3) and np.all(p == np.float32(0.5))
+
+
+@pytest.mark.parametrize("flatten_limit", [1 << 25, 1])
+def test_zero_scale_instance_equals_masked(oracle, flatten_limit):
+    """A singular instance transform (zero scale) has no inverse; the build
+    treats the instance as masked out, flat and two-level alike."""
+    from pt_harness import small_instanced
+    sd = small_instanced(side=8)
+    sd.instances = sd.instances.copy()
+    x = sd.instances[5]["xform"].reshape(3, 4).copy()
+    x[:, :3] = 0.0
+    sd.instances[5]["xform"] = x.reshape(-1)
+    m = small_instanced(side=8)
+    m.instances = m.instances.copy()
+    m.instances["mask"][5] = 0
+    a = oracle.OracleScene(sd, flatten_limit=flatten_limit)
+    b = oracle.OracleScene(m, flatten_limit=flatten_limit)
+    rng = np.random.default_rng(3)
+    rays = random_rays(rng, 4000, -60, 60)
+    ha = a.trace(rays, 0)
+    assert np.array_equal(ha, b.trace(rays, 0))
+    assert np.all(np.isfinite(ha[:, 0].view(np.float32)))
+    assert np.array_equal(a.render_paths(sd.views[0], dict(max_bounces=3), 0, 1),
+                          b.render_paths(m.views[0], dict(max_bounces=3), 0, 1))

@@ -66,6 +66,36 @@ def test_noalloc_matches_regular_build_call_after_call(gpu_lib):
         assert np.array_equal(root, np.concatenate([boxes[:, :3].min(0), boxes[:, 3:].max(0)]))
 
 
+def triangle_soup(n, seed):
+    """n seeded random small triangles in a unit cube: a scene with exactly n
+    primitives, for builds at the fixed capacity of the scratch array."""
+    rng = np.random.default_rng(seed)
+    c = rng.uniform(-1.0, 1.0, (n, 1, 3))
+    pos = (c + rng.normal(scale=0.01, size=(n, 3, 3))).reshape(-1, 3).astype(np.float32)
+    nrm = np.zeros((pos.shape[0], 4), np.float32)
+    nrm[:, 1] = 1.0
+    uv = np.zeros((pos.shape[0], 2), np.float32)
+    idx = np.arange(3 * n, dtype=np.uint32)
+    mats = np.stack([scenes.material((0.5, 0.5, 0.5))])
+    return scenes.SceneData("soup", pos, nrm, uv, idx, np.zeros(n, np.uint32), mats, np.zeros((0, 20), np.float32),
+                            None, 1.0, [(0, idx.size)], scenes.identity_instance(1))
+
+
+@pytest.mark.parametrize("n", [65536, 65535])
+def test_noalloc_at_capacity(gpu_lib, n):
+    """Builds at and one below OHAO_BVH_NOALLOC_MAX_PRIMS, where the scratch
+    layout uses all of its per-primitive share, twice in a row."""
+    og = gpu_lib
+    sd = triangle_soup(n, seed=n)
+    boxes = scene_boxes(sd)
+    ref_nodes, ref_order, ref_h = regular_build(og, sd)
+    for _ in range(2):
+        nodes, order, h, _ = noalloc_build(og, boxes)
+        assert h == ref_h
+        assert np.array_equal(nodes, ref_nodes), "node bytes differ from ohao_pt_build at capacity"
+        assert np.array_equal(order, ref_order), "leaf order differs from ohao_pt_build at capacity"
+
+
 def test_noalloc_rejects_oversize(gpu_lib):
     fn = gpu_lib.load_library().ohao_bvh_build_noalloc
     nn, hh = C.c_uint32(), C.c_uint32()
