@@ -46,6 +46,8 @@ def parse():
     ap.add_argument("--workload", default="sphere_1m", choices=["sphere_1m", "cornell", "instanced", "studio", "denoise"])
     ap.add_argument("--cpu-seconds", type=float, default=12.0)
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-gates", action="store_true",
+                    help="skip the gates (configs 3-5 and the FP64 comparisons) after the headline")
     ap.add_argument("--case", default=None, choices=sorted(CASES),
                     help="run one small profiling case instead of the benchmark (one process, a few GB at most)")
     ap.add_argument("--case-arg", default=None, help="launch shape name for --case instanced_pool")
@@ -200,6 +202,331 @@ def run_reference(args):
     print(json.dumps(line), flush=True)
 
 
+# ---------------------------------------------------------------------------
+# Gates: the rest of the metric, measured in the default run after the
+# headline (configs 3-5 and the FP64 comparison of every config). Each gate
+# is CUDA-event timed on the render stream with its own clock record; all of
+# them together stay within a few minutes on one GB300.
+# ---------------------------------------------------------------------------
+def _events():
+    import torch
+    return torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+
+
+def _time_steps(fn, warmup, steps, flush):
+    """CUDA-event milliseconds of each of `steps` calls of fn(k) after
+    `warmup` untimed calls; L2 flushed before every timed call."""
+    import torch
+    for k in range(warmup):
+        fn(k)
+    torch.cuda.synchronize()
+    times = []
+    for k in range(steps):
+        flush.zero_()
+        e0, e1 = _events()
+        e0.record()
+        fn(warmup + k)
+        e1.record()
+        e1.synchronize()
+        times.append(e0.elapsed_time(e1))
+    return times
+
+
+def gate_batched(flush, warmup=3, steps=3):
+    """Config 3: the 64-view instanced set through the per-view wavefront
+    (plain) and the persistent multi-view pool (batched, launch shape chosen
+    by the autotuner on the same views); equal RMSE is shown by equal
+    images (bit identity of the two forms' accumulators)."""
+    import torch
+    import ohao_engine_gb300 as og
+    from ohao_engine_gb300 import scenes
+    t0 = time.time()
+    sd = scenes.instanced()
+    gen_s = time.time() - t0
+    pt = og.PathTracer()
+    t0 = time.time()
+    pt.load_scene(sd)
+    torch.cuda.synchronize()
+    build_s = time.time() - t0
+    spp = sd.spp
+    accs = [torch.zeros((v.width * v.height, 4), dtype=torch.float32, device="cuda") for v in sd.views]
+    total_px = sum(v.width * v.height for v in sd.views)
+
+    def views_for(k):
+        return [og.make_view(v, accum=a, history=k * spp) for v, a in zip(sd.views, accs)]
+
+    def settings(k, mode):
+        return og.make_settings(spp=spp, max_bounces=sd.max_bounces, sample_index_base=k * spp, mode=mode)
+
+    t0 = time.time()
+    tune_ms = pt.autotune(views_for(0), settings(0, og.MODE_PERSISTENT))
+    tune_s = time.time() - t0
+    out = {"workload": "instanced: 10,000 instances of 5 displaced geodesic spheres (362,500 base tris, two-level), "
+                       f"64 views log-uniform 256..1024 ({total_px} pixels), {spp} spp, depth 4, PCG",
+           "scene_gen_s": gen_s, "upload_and_build_s": build_s, "autotune_s": tune_s,
+           "launch_config": pt.launch_config, "autotune_best_ms": tune_ms, "warmup": warmup, "steps": steps}
+    for name, mode in (("plain", og.MODE_WAVEFRONT), ("batched", og.MODE_PERSISTENT)):
+        clk = ClockSampler(0)
+        clk.start()
+        times = _time_steps(lambda k: pt.render(views_for(k), settings(k, mode)), warmup, steps, flush)
+        out[name] = {"msamples_per_s": total_px * spp * steps / (sum(times) / 1e3) / 1e6,
+                     "ms_per_step": sum(times) / steps, "clocks": clk.stop()}
+    out["batched_over_plain"] = out["batched"]["msamples_per_s"] / out["plain"]["msamples_per_s"]
+    pt.render(views_for(0), settings(0, og.MODE_WAVEFRONT))
+    a_plain = [a.clone() for a in accs]
+    pt.render(views_for(0), settings(0, og.MODE_PERSISTENT))
+    out["bit_identical"] = bool(all(torch.equal(x, y) for x, y in zip(a_plain, accs)))
+    pt.close()
+    return out, sd
+
+
+def gate_adjoint(flush, warmup=3, steps=3):
+    """Config 4: one full gradient of the multi-view L2 loss (64x64x3 tile
+    albedo map + 4 roughness regions, 8 views of 512^2, 16 spp, depth 3)
+    through ohao_pt_adjoint, against coordinate finite differences (two
+    renders of the 8 views per parameter, the reference fitter's method)
+    timed with the same renderer."""
+    import torch
+    import ohao_engine_gb300 as og
+    from ohao_engine_gb300 import scenes
+    from ohao_engine_gb300.fit import AdjointFit
+    sd = scenes.studio()
+    train = sd.views[:8]
+    pt = og.PathTracer()
+    pt.load_scene(sd)
+    tgt = [torch.zeros((v.width * v.height, 4), dtype=torch.float32, device="cuda") for v in train]
+    pt.render([og.make_view(v, accum=a) for v, a in zip(train, tgt)],
+              og.make_settings(spp=256, max_bounces=3, sample_index_base=1 << 20))
+    rng = np.random.default_rng(2)
+    init_map = np.clip(sd.albedo_map + rng.uniform(-0.4, 0.4, sd.albedo_map.shape), 0, 1).astype(np.float32)
+    rough_ids = np.arange(4)
+    mats0 = sd.materials.copy()
+    mats0[rough_ids, 4] = np.clip(mats0[rough_ids, 4] + rng.uniform(-0.2, 0.2, 4), 0.05, 1.0).astype(np.float32)
+    fit = AdjointFit(pt, mats0, init_map, train, tgt, spp=16, max_bounces=3, rough_ids=rough_ids, lr=0.03)
+    n_params = int(fit.theta.size)
+    npix = sum(v.width * v.height for v in train)
+    acc = [torch.zeros((v.width * v.height, 4), dtype=torch.float32, device="cuda") for v in train]
+    st16 = og.make_settings(spp=16, max_bounces=3, sample_index_base=0)
+    clk = ClockSampler(0)
+    clk.start()
+    g_times = _time_steps(lambda k: pt.adjoint([og.make_view(v, accum=a) for v, a in zip(train, fit.accums)],
+                                               fit.settings(k * 16), fit.targets, fit.gmap, fit.grough),
+                          warmup, steps, flush)
+    r_times = _time_steps(lambda k: pt.render([og.make_view(v, accum=a) for v, a in zip(train, acc)], st16),
+                          warmup, steps, flush)
+    clocks = clk.stop()
+    t_grad = sum(g_times) / steps / 1e3
+    t_render = sum(r_times) / steps / 1e3
+    adj_rate = n_params / t_grad
+    fd_rate = 1.0 / (2.0 * t_render)
+    pt.close()
+    return {"workload": f"studio: displaced sphere + plane ({sd.ntris} tris), 64x64x3 tile albedo map + 4 roughness "
+                        "regions, 8 views 512x512, 16 spp, depth 3, PCG; targets 256 spp",
+            "params": n_params, "paths_per_gradient": npix * 16, "warmup": warmup, "steps": steps,
+            "adjoint_ms_per_gradient": t_grad * 1e3, "adjoint_param_gradients_per_s": adj_rate,
+            "render_ms_8_views": t_render * 1e3, "coordinate_fd_param_gradients_per_s": fd_rate,
+            "coordinate_fd_ms_per_gradient": 2 * n_params * t_render * 1e3,
+            "adjoint_over_coordinate_fd": adj_rate / fd_rate, "clocks": clocks}, sd
+
+
+def gate_denoiser(flush, n_scenes=20, iters=3000, crop=128, batch=8, variants=6, ref_spp=4096):
+    """Config 5: the U-Net trained here by the library's own tcgen05
+    kernels (bounded: n_scenes scenes x variants 1-spp renders against a
+    1024-spp target, `iters` Adam steps), then judged on the 1920x1080
+    headline frame against a ref_spp render: RMSE after the reference's
+    display transform of the denoised 1-spp image and of plain accumulation,
+    with CUDA-event wall time of each."""
+    import torch
+    import ohao_engine_gb300 as og
+    from ohao_engine_gb300 import scenes
+    from ohao_engine_gb300.denoise import Denoiser, render_pair, tonemap, training_scene
+    t0 = time.time()
+    side = 256
+    data = []
+    for seed in range(1, n_scenes + 1):
+        sd = training_scene(seed, side=side, freq=64)
+        pt = og.PathTracer()
+        pt.load_scene(sd)
+        pairs = [render_pair(pt, sd.views[0], side, side, 1, 1024 if k == 0 else 1, seed_base=4096 * k)
+                 for k in range(variants)]
+        data.append(([p[0] for p in pairs], [p[1] for p in pairs], pairs[0][2]))
+        pt.close()
+    torch.cuda.synchronize()
+    data_s = time.time() - t0
+    dn = Denoiser(max_pixels=max(batch * crop * crop, 1920 * 1088), seed=1)
+    rng = np.random.default_rng(0)
+
+    def crop_of(t, ch, y0, x0):
+        return t.view(side, side, ch)[y0:y0 + crop, x0:x0 + crop].contiguous().view(-1, ch)
+
+    losses = []
+    t0 = time.time()
+    for it in range(iters):
+        xs, aovs, ts = [], [], []
+        for _ in range(batch):
+            s = int(rng.integers(n_scenes))
+            k = int(rng.integers(variants))
+            y0, x0 = (int(v) for v in rng.integers(0, side - crop + 1, 2) // 16 * 16)
+            xs.append(crop_of(data[s][0][k], 4, y0, x0))
+            aovs.append(crop_of(data[s][1][k], og.AOV_FLOATS, y0, x0))
+            ts.append(crop_of(data[s][2], 4, y0, x0))
+        lr = 2e-3 * min(1.0, (it + 1) / 200.0) * (0.1 ** (it / iters))
+        losses.append(dn.train_step(xs, aovs, ts, crop, crop, lr))
+    torch.cuda.synchronize()
+    train_s = time.time() - t0
+    del data
+    sd = scenes.sphere_1m()
+    pt = og.PathTracer()
+    pt.load_scene(sd)
+    v = sd.views[0]
+    npix = v.width * v.height
+    ref = torch.zeros((npix, 4), dtype=torch.float32, device="cuda")
+    t0 = time.time()
+    for k in range(ref_spp // 256):
+        pt.render([og.make_view(v, accum=ref, history=k * 256)],
+                  og.make_settings(spp=256, max_bounces=4, sample_index_base=(1 << 24) + k * 256))
+    torch.cuda.synchronize()
+    ref_s = time.time() - t0
+    ref_ldr = tonemap(ref.cpu().numpy()[:, :3])
+
+    def rmse(t):
+        return float(np.sqrt(((tonemap(t.cpu().numpy()[:, :3]) - ref_ldr) ** 2).mean()))
+
+    clk = ClockSampler(0)
+    clk.start()
+    plain = {}
+    acc = torch.zeros((npix, 4), dtype=torch.float32, device="cuda")
+    for spp in (1, 4, 16, 64):
+        ms = min(_time_steps(lambda k: pt.render([og.make_view(v, accum=acc)],
+                                                 og.make_settings(spp=spp, max_bounces=4, sample_index_base=0)),
+                             1, 3, flush))
+        plain[str(spp)] = {"rmse": rmse(acc), "ms": ms}
+    noisy = torch.zeros((npix, 4), dtype=torch.float32, device="cuda")
+    aov = torch.zeros((npix, og.AOV_FLOATS), dtype=torch.float32, device="cuda")
+    out = torch.zeros((npix, 4), dtype=torch.float32, device="cuda")
+    render_ms = min(_time_steps(lambda k: pt.render([og.make_view(v, accum=noisy, aov=aov)],
+                                                    og.make_settings(spp=1, max_bounces=4, sample_index_base=0)),
+                                1, 3, flush))
+    infer_ms = min(_time_steps(lambda k: dn.infer([noisy], [aov], [out], v.width, v.height), 2, 5, flush))
+    clocks = clk.stop()
+    den = rmse(out)
+    matched = max([int(s) for s, r in plain.items() if r["rmse"] >= den], default=0)
+    flops = 2.0 * 9 * sum(ci * co * (1920 * 1088) / 4 ** lv for ci, co, lv in (
+        (12, 32, 0), (32, 32, 0), (32, 48, 1), (48, 48, 1), (48, 64, 2), (64, 64, 2), (64, 96, 3), (96, 96, 3),
+        (96, 128, 4), (128, 128, 4), (224, 96, 3), (96, 96, 3), (160, 64, 2), (64, 64, 2), (112, 48, 1), (48, 48, 1),
+        (80, 32, 0), (32, 32, 0), (32, 3, 0)))
+    pk = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    peak = float(json.load(open(pk)).get("bf16_tflops", 0)) if os.path.exists(pk) else 1900.0
+    dn.close()
+    res = {"workload": "U-Net 32/48/64/96/128 (BF16 tcgen05, FP32 accumulation) trained here: "
+                       f"{n_scenes} scenes x 256^2 ({variants} x 1 spp vs 1024 spp), {iters} Adam steps of "
+                       f"{batch}x{crop}^2 crops; judged on sphere_1m 1920x1080 against {ref_spp} spp",
+           "training": {"data_s": data_s, "train_s": train_s, "iters": iters,
+                        "loss_first100": float(np.mean(losses[:100])), "loss_last100": float(np.mean(losses[-100:]))},
+           "reference_render_s": ref_s,
+           "denoised": {"rmse": den, "render_1spp_ms": render_ms, "infer_ms": infer_ms,
+                        "total_ms": render_ms + infer_ms},
+           "plain": plain, "plain_spp_matched": matched,
+           "meets_64spp": bool(den <= plain["64"]["rmse"] and render_ms + infer_ms < plain["64"]["ms"]),
+           "infer_tflops": flops / (infer_ms / 1e3) / 1e12, "infer_frac_of_bf16_peak": flops / (infer_ms / 1e3) / 1e12 / peak,
+           "clocks": clocks}
+    return res, pt, sd, ref
+
+
+def fp64_compare(og, pt, orc, view, spp, sample_base, pixels, settings):
+    """GPU FP32 image (spp samples per pixel, progressive mean) against the
+    FP64 host render of the same samples on `pixels`: relative RMSE of the
+    per-pixel means, and the relative Monte-Carlo standard error of those
+    means (the noise level the difference is to be read against)."""
+    import torch
+    npix = view.width * view.height
+    acc = torch.zeros((npix, 4), dtype=torch.float32, device="cuda")
+    pt.render([og.make_view(view, accum=acc)], og.make_settings(spp=spp, sample_index_base=sample_base, **settings))
+    g = acc.cpu().numpy()[pixels, :3].astype(np.float64)
+    t0 = time.time()
+    p64 = orc.render_paths(view, dict(settings, sampler=settings.get("sampler", 0)), sample_base, spp, pixels=pixels,
+                           fp64=True)
+    host_s = time.time() - t0
+    m64 = p64.mean(axis=0)
+    scale = float(np.sqrt((m64 ** 2).mean())) or 1.0
+    rel = float(np.sqrt(((g - m64) ** 2).mean())) / scale
+    se = float(np.sqrt((p64.var(axis=0, ddof=1) / spp).mean())) / scale if spp > 1 else None
+    return {"pixels": int(pixels.size), "spp": spp, "rel_rmse_vs_fp64": rel, "rel_mc_stderr": se,
+            "max_abs_diff": float(np.abs(g - m64).max()), "host_fp64_s": host_s}
+
+
+def gate_fp64(headline_sd, instanced_sd, studio_sd, dn_pt, dn_sd, dn_ref):
+    """Converged-image comparison against an FP64 host render for every
+    config: the GPU's FP32 image and the host oracle instantiated in double,
+    on the same samples (same PCG streams), over seeded pixel subsets."""
+    import pyoracle
+    import ohao_engine_gb300 as og
+    from ohao_engine_gb300 import scenes
+    pyoracle.build(ref=False)
+    out = {}
+    rng = np.random.default_rng(99)
+
+    def subset(v, n):
+        npx = v.width * v.height
+        return np.sort(rng.choice(npx, min(n, npx), replace=False)).astype(np.uint32)
+
+    sd = scenes.cornell(256, 256, 16)
+    pt = og.PathTracer()
+    pt.load_scene(sd)
+    v = sd.views[0]
+    out["config1_cornell"] = fp64_compare(og, pt, pyoracle.OracleScene(sd), v, 16, 0,
+                                          np.arange(v.width * v.height, dtype=np.uint32), dict(max_bounces=4))
+    pt.close()
+    sd = headline_sd
+    pt = og.PathTracer()
+    pt.load_scene(sd)
+    v = sd.views[0]
+    out["config2_sphere_1m"] = fp64_compare(og, pt, pyoracle.OracleScene(sd), v, 64, 0, subset(v, 8192),
+                                            dict(max_bounces=4))
+    pt.close()
+    sd = instanced_sd
+    pt = og.PathTracer()
+    pt.load_scene(sd)
+    v = max(sd.views, key=lambda x: x.width * x.height)
+    out["config3_instanced"] = fp64_compare(og, pt, pyoracle.OracleScene(sd), v, 16, 0, subset(v, 4096),
+                                            dict(max_bounces=4))
+    pt.close()
+    sd = studio_sd
+    pt = og.PathTracer()
+    pt.load_scene(sd)
+    v = sd.views[0]
+    out["config4_studio"] = fp64_compare(og, pt, pyoracle.OracleScene(sd), v, 16, 0, subset(v, 8192),
+                                         dict(max_bounces=3))
+    pt.close()
+    # config 5: the judge's 4096-spp reference frame against FP64 on the same samples
+    v = dn_sd.views[0]
+    pix = subset(v, 512)
+    orc = pyoracle.OracleScene(dn_sd)
+    t0 = time.time()
+    p64 = np.zeros((len(pix), 3))
+    for k in range(16):
+        p64 += orc.render_paths(v, dict(max_bounces=4), (1 << 24) + k * 256, 256, pixels=pix, fp64=True).sum(axis=0)
+    m64 = p64 / 4096.0
+    g = dn_ref.cpu().numpy()[pix, :3].astype(np.float64)
+    scale = float(np.sqrt((m64 ** 2).mean())) or 1.0
+    out["config5_reference_frame"] = {"pixels": int(pix.size), "spp": 4096,
+                                      "rel_rmse_vs_fp64": float(np.sqrt(((g - m64) ** 2).mean())) / scale,
+                                      "max_abs_diff": float(np.abs(g - m64).max()), "host_fp64_s": time.time() - t0}
+    dn_pt.close()
+    return out
+
+
+def run_gates(headline_sd, flush):
+    res = {}
+    t0 = time.time()
+    res["config3_batched"], inst_sd = gate_batched(flush)
+    res["config4_adjoint"], studio_sd = gate_adjoint(flush)
+    res["config5_denoiser"], dn_pt, dn_sd, dn_ref = gate_denoiser(flush)
+    res["fp64_rmse"] = gate_fp64(headline_sd, inst_sd, studio_sd, dn_pt, dn_sd, dn_ref)
+    res["wall_s"] = time.time() - t0
+    return res
+
+
 def run_ours(args):
     import torch
     from ohao_engine_gb300 import replicas
@@ -308,6 +635,9 @@ def run_ours(args):
            "h2d_bytes_per_step": npix * 16, "d2h_bytes_per_step": npix * 16,
            "call": "ohao_pt_render_host (pinned host accumulator in and out)"}
 
+    gates = None
+    if rank == 0 and world == 1 and not args.no_gates and args.workload == "sphere_1m":
+        gates = run_gates(sd, flush)
     cpu = None
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
         cpu = cpu_baseline(sd, spp_step, args.cpu_seconds, npix * spp_step)
@@ -321,6 +651,8 @@ def run_ours(args):
                            "rays_per_step": {"closest": rays_c / len(prof_ms), "shadow": rays_s / len(prof_ms)}},
                 "clocks": clocks, "e2e": e2e, "gpu_launches": int(round(launches_per_step * args.steps)),
                 "roofline": roofline, "cpu_baseline": cpu}
+        if gates is not None:
+            line["gates"] = gates
         print(json.dumps(line), flush=True)
     pt.close()
     replicas.finish(ranks)

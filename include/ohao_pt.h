@@ -91,6 +91,13 @@ typedef struct ohao_pt_view {
     float* accum;
     float* path_radiance;
     float* aov;
+    /* Optional display image, RGBA8 width*height*4 bytes: the reference's
+     * outputImage (pt_raygen.rgen:1262-1269), pow(ACES(accum * 0.5), 1/2.2)
+     * per channel rounded to nearest, alpha 255, written from the
+     * accumulator after the call's samples. Device memory for
+     * ohao_pt_render; host memory for ohao_pt_render_host (the readback of
+     * VulkanRenderer::getPixels, render_dispatch.cpp:170-186). */
+    uint8_t* display;
 } ohao_pt_view;
 
 #define OHAO_SAMPLER_PCG 0u
@@ -161,6 +168,15 @@ const char* ohao_pt_version(void);
 ohao_status ohao_pt_set_geometry(ohao_pt_ctx* ctx, const float* pos, uint32_t pos_stride_bytes, uint32_t nverts,
                                  const float* normal4, const float* uv2, const uint32_t* indices, uint32_t ntris,
                                  const uint32_t* mat_ids);
+/* The same upload from device memory, ordered on `stream` (the device
+ * buffers the reference's RT scene packer fills, rt_build.cpp:27-186, bound
+ * without a host round trip). uv2 may be NULL. The index and material-id
+ * checks run on the device; the call returns when the copies and checks on
+ * `stream` have finished, so the caller may reuse its buffers afterwards. */
+ohao_status ohao_pt_set_geometry_device(ohao_pt_ctx* ctx, const float* d_pos, uint32_t pos_stride_bytes,
+                                        uint32_t nverts, const float* d_normal4, const float* d_uv2,
+                                        const uint32_t* d_indices, uint32_t ntris, const uint32_t* d_mat_ids,
+                                        ohao_stream stream);
 /* RTAccelerationStructure::createBLAS (rt_acceleration_structure.cpp:205-300):
  * one triangle geometry over indices [first_index, first_index+index_count). */
 ohao_status ohao_pt_create_blas(ohao_pt_ctx* ctx, uint32_t first_index, uint32_t index_count, uint32_t* out_blas);
@@ -202,6 +218,10 @@ ohao_status ohao_pt_render(ohao_pt_ctx* ctx, const ohao_pt_view* views, uint32_t
 ohao_status ohao_pt_render_host(ohao_pt_ctx* ctx, const ohao_pt_view* views, uint32_t n_views,
                                 const ohao_pt_settings* settings, float* const* host_accum, ohao_stream stream);
 ohao_status ohao_pt_get_profile(const ohao_pt_ctx* ctx, ohao_pt_profile* out);
+/* The display transform alone (the tonemap + gamma tail of
+ * pt_raygen.rgen:1262-1269) over npix device RGBA32F texels into device
+ * RGBA8: for an accumulator written elsewhere, or a denoised image. */
+ohao_status ohao_pt_display(const float* d_rgba32f, uint32_t npix, uint8_t* d_rgba8, ohao_stream stream);
 /* Times the compiled launch shapes of the persistent multi-view kernel
  * (block size, blocks per SM, pixels per work-queue claim) on these views
  * and keeps the fastest for later renders of this context. The views'

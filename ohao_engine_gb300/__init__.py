@@ -42,7 +42,7 @@ EXPORTED_SYMBOLS = [
     "ohao_pt_set_albedo_map", "ohao_env_cdf_build", "ohao_pt_render", "ohao_pt_render_host",
     "ohao_pt_get_profile", "ohao_pt_trace", "ohao_pt_bvh_info", "ohao_pt_bvh_download", "ohao_bvh_build_noalloc",
     "ohao_pt_autotune", "ohao_pt_launch_config", "ohao_pt_launch_config_at", "ohao_pt_set_launch_config",
-    "ohao_pt_backward", "ohao_pt_adjoint",
+    "ohao_pt_backward", "ohao_pt_adjoint", "ohao_pt_display", "ohao_pt_set_geometry_device",
 ]
 
 
@@ -60,7 +60,8 @@ class View(C.Structure):
     """ohao_pt_view"""
     _fields_ = [("inv_view", C.c_float * 16), ("inv_proj", C.c_float * 16), ("width", C.c_uint32),
                 ("height", C.c_uint32), ("history", C.c_uint32), ("reserved", C.c_uint32),
-                ("accum", C.c_void_p), ("path_radiance", C.c_void_p), ("aov", C.c_void_p)]
+                ("accum", C.c_void_p), ("path_radiance", C.c_void_p), ("aov", C.c_void_p),
+                ("display", C.c_void_p)]
 
 
 class Settings(C.Structure):
@@ -122,6 +123,8 @@ def load_library(path: str | None = None):
         "ohao_pt_backward": ([vp, C.POINTER(View), u32, C.POINTER(Settings), C.POINTER(vp), vp, vp, vp], i32),
         "ohao_pt_adjoint": ([vp, C.POINTER(View), u32, C.POINTER(Settings), C.POINTER(vp), vp, vp,
                                    C.POINTER(f32), vp], i32),
+        "ohao_pt_display": ([vp, u32, vp, vp], i32),
+        "ohao_pt_set_geometry_device": ([vp, vp, u32, u32, vp, vp, vp, u32, vp, vp], i32),
     }
     for name, (args, res) in sigs.items():
         fn = getattr(L, name)
@@ -198,10 +201,42 @@ def _buffer(a, elems: int, what: str, host: bool = False, floats: bool = True):
     return int(a)
 
 
-def make_view(view, accum=None, history: int = 0, path_radiance=None, aov=None) -> View:
+def _bytes(a, nbytes: int, what: str, host: bool):
+    """Pointer value of a uint8 buffer of at least nbytes (device memory, or
+    host memory with ``host``); a wrong buffer raises ValueError."""
+    if a is None:
+        return None
+    if isinstance(a, np.ndarray):
+        if not host:
+            raise ValueError(f"{what}: a host array where a CUDA device buffer is needed")
+        if not (a.flags.c_contiguous and a.flags.writeable and a.dtype == np.uint8 and a.size >= nbytes):
+            raise ValueError(f"{what}: needs a writable C-contiguous uint8 array of at least {nbytes} bytes")
+        return a.ctypes.data
+    if hasattr(a, "data_ptr"):
+        if not (a.element_size() == 1 and a.is_contiguous() and a.numel() >= nbytes):
+            raise ValueError(f"{what}: needs a contiguous uint8 tensor of at least {nbytes} bytes")
+        if bool(a.is_cuda) == host:
+            raise ValueError(f"{what}: needs a {'host' if host else 'CUDA device'} tensor (got one on {a.device})")
+        return a.data_ptr()
+    return int(a)
+
+
+def display(rgba32f, npix: int, out_rgba8, stream=None):
+    """ohao_pt_display: RGBA8 display image of npix device RGBA32F texels."""
+    st = load_library().ohao_pt_display(_ptr(_buffer(rgba32f, npix * 4, "rgba32f")), npix,
+                                        _ptr(_bytes(out_rgba8, npix * 4, "rgba8", False)),
+                                        _ptr(stream) if stream is not None else None)
+    if st != OK:
+        raise OhaoError(st, "ohao_pt_display failed")
+
+
+def make_view(view, accum=None, history: int = 0, path_radiance=None, aov=None, display=None,
+              display_host: bool = False) -> View:
     """One ``ohao_pt_view``. accum: RGBA32F per pixel; path_radiance: RGBA32F
     per sample and pixel ([spp][pixel][4], for up to as many samples per call
-    as it holds); aov: AOV_FLOATS per pixel; all on the device."""
+    as it holds); aov: AOV_FLOATS per pixel; all on the device. display:
+    RGBA8 per pixel (uint8, 4 per pixel), on the device, or in host memory
+    with display_host for render_host."""
     v = View()
     v.inv_view[:] = [float(x) for x in np.asarray(view.inv_view, np.float32)]
     v.inv_proj[:] = [float(x) for x in np.asarray(view.inv_proj, np.float32)]
@@ -210,6 +245,7 @@ def make_view(view, accum=None, history: int = 0, path_radiance=None, aov=None) 
     v.accum = _buffer(accum, npix * 4, "accum")
     v.path_radiance = _buffer(path_radiance, npix * 4, "path_radiance")
     v.aov = _buffer(aov, npix * AOV_FLOATS, "aov")
+    v.display = _bytes(display, npix * 4, "display", display_host)
     if path_radiance is not None and hasattr(path_radiance, "numel") and npix:
         v._path_samples = path_radiance.numel() // (npix * 4)
     return v
@@ -277,6 +313,21 @@ class PathTracer:
         nverts = pos.size * 4 // pos_stride_bytes
         self._ck(self._L.ohao_pt_set_geometry(self.h, _ptr(pos), pos_stride_bytes, nverts, _ptr(nrm), _ptr(uv),
                                               _ptr(idx), idx.size // 3, _ptr(mid)), "set_geometry")
+
+    def set_geometry_device(self, pos, normals, uvs, indices, mat_ids, nverts: int, ntris: int,
+                            pos_stride_bytes: int = 12, stream=None):
+        """ohao_pt_set_geometry_device: the geometry from CUDA tensors
+        (positions at pos_stride_bytes, float4 normals, float2 UVs or None,
+        uint32 indices and material ids), ordered on `stream`."""
+        pf = pos_stride_bytes // 4
+        p = _buffer(pos, max(nverts - 1, 0) * pf + 3 if nverts else 0, "pos")
+        n = _buffer(normals, nverts * 4, "normals")
+        u = _buffer(uvs, nverts * 2, "uvs")
+        i = _buffer(indices, ntris * 3, "indices", floats=False)
+        m = _buffer(mat_ids, ntris, "mat_ids", floats=False)
+        self._ck(self._L.ohao_pt_set_geometry_device(self.h, p, pos_stride_bytes, nverts, n, u, i, ntris, m,
+                                                     _ptr(stream) if stream is not None else None),
+                 "set_geometry_device")
 
     def create_blas(self, first_index: int, index_count: int) -> int:
         out = C.c_uint32()

@@ -89,12 +89,13 @@ struct ohao_pt_ctx {
     // scratch
     DevBuf scratch, build_scratch, err_flag;
     DevBuf adj_scratch, adj_grads;        // backward: view table, loss cell; per-pixel loss gradients
-    std::vector<DevBuf*> host_accum_bufs;
+    std::vector<DevBuf*> host_accum_bufs, host_display_bufs;
     ohao_pt_profile profile{};
     ohao::PersistentState* persistent = nullptr;
     ~ohao_pt_ctx() {
         if (persistent) ohao::persistent_destroy(persistent);
         for (auto* b : host_accum_bufs) delete b;
+        for (auto* b : host_display_bufs) delete b;
     }
 };
 
@@ -288,6 +289,51 @@ ohao_status ohao_pt_set_geometry(ohao_pt_ctx* ctx, const float* pos, uint32_t po
     ctx->nverts = nverts;
     ctx->ntris = ntris;
     ctx->built = false;
+    return OHAO_OK;
+}
+
+ohao_status ohao_pt_set_geometry_device(ohao_pt_ctx* ctx, const float* d_pos, uint32_t pos_stride_bytes,
+                                        uint32_t nverts, const float* d_normal4, const float* d_uv2,
+                                        const uint32_t* d_indices, uint32_t ntris, const uint32_t* d_mat_ids,
+                                        ohao_stream stream) {
+    if (!ctx) return OHAO_ERR_INVALID_ARG;
+    if ((nverts && (!d_pos || !d_normal4)) || (ntris && (!d_indices || !d_mat_ids)) || pos_stride_bytes < 12 ||
+        pos_stride_bytes % 4 != 0)
+        return fail(ctx, OHAO_ERR_INVALID_ARG, "set_geometry_device: null array or stride < 12 (or not 4-byte aligned)");
+    cudaStream_t st = reinterpret_cast<cudaStream_t>(stream);
+    CK(cudaSetDevice(ctx->device), "set device");
+    ctx->built = false;
+    ctx->nverts = ctx->ntris = 0;
+    const size_t nv = nverts, nt = ntris;
+    CK(ctx->pos.ensure(nv * 12), "positions");
+    CK(ctx->normals.ensure(nv * 16), "normals");
+    CK(ctx->uvs.ensure(nv * 8), "uvs");
+    CK(ctx->indices.ensure(nt * 12), "indices");
+    CK(ctx->mat_ids.ensure(nt * 4), "material ids");
+    if (nv) {
+        // positions packed to 12 B per vertex whatever the caller's stride
+        CK(cudaMemcpy2DAsync(ctx->pos.p, 12, d_pos, pos_stride_bytes, 12, nv, cudaMemcpyDeviceToDevice, st), "positions");
+        CK(cudaMemcpyAsync(ctx->normals.p, d_normal4, nv * 16, cudaMemcpyDeviceToDevice, st), "normals");
+        if (d_uv2) CK(cudaMemcpyAsync(ctx->uvs.p, d_uv2, nv * 8, cudaMemcpyDeviceToDevice, st), "uvs");
+        else CK(cudaMemsetAsync(ctx->uvs.p, 0, nv * 8, st), "uvs");
+    }
+    uint32_t maxes[2] = {0, 0};
+    if (nt) {
+        CK(cudaMemcpyAsync(ctx->indices.p, d_indices, nt * 12, cudaMemcpyDeviceToDevice, st), "indices");
+        CK(cudaMemcpyAsync(ctx->mat_ids.p, d_mat_ids, nt * 4, cudaMemcpyDeviceToDevice, st), "material ids");
+        DevBuf m;
+        CK(m.ensure(8), "range check");
+        CK(cudaMemsetAsync(m.p, 0, 8, st), "range check");
+        ohao::launch_max_u32(ctx->indices.as<uint32_t>(), nt * 3, m.as<uint32_t>(), st);
+        ohao::launch_max_u32(ctx->mat_ids.as<uint32_t>(), nt, m.as<uint32_t>() + 1, st);
+        CK(cudaGetLastError(), "range check");
+        CK(cudaMemcpyAsync(maxes, m.p, 8, cudaMemcpyDeviceToHost, st), "range check");
+    }
+    CK(cudaStreamSynchronize(st), "set_geometry_device");
+    if (nt && maxes[0] >= nverts) return fail(ctx, OHAO_ERR_INVALID_ARG, "set_geometry_device: index out of range");
+    ctx->max_mat_id = maxes[1];
+    ctx->nverts = nverts;
+    ctx->ntris = ntris;
     return OHAO_OK;
 }
 
@@ -699,6 +745,9 @@ ohao_status ohao_pt_render(ohao_pt_ctx* ctx, const ohao_pt_view* views, uint32_t
     cudaStream_t cs = reinterpret_cast<cudaStream_t>(stream);
     CK(cudaSetDevice(ctx->device), "set device");
     if ((s = render_views(ctx, views, n_views, st, acc.data(), cs)) != OHAO_OK) return s;
+    for (uint32_t v = 0; v < n_views; ++v)
+        if (views[v].display)
+            CK(ohao::launch_display(acc[v], views[v].width * views[v].height, views[v].display, cs), "display");
     return check_device_error(ctx, cs);
 }
 
@@ -721,8 +770,16 @@ ohao_status ohao_pt_render_host(ohao_pt_ctx* ctx, const ohao_pt_view* views, uin
     }
     if ((s = render_views(ctx, views, n_views, st, acc.data(), cs)) != OHAO_OK) return s;
     for (uint32_t v = 0; v < n_views; ++v) {
-        const size_t bytes = static_cast<size_t>(views[v].width) * views[v].height * 16;
-        CK(cudaMemcpyAsync(host_accum[v], acc[v], bytes, cudaMemcpyDeviceToHost, cs), "accum download");
+        const size_t npix = static_cast<size_t>(views[v].width) * views[v].height;
+        CK(cudaMemcpyAsync(host_accum[v], acc[v], npix * 16, cudaMemcpyDeviceToHost, cs), "accum download");
+        if (views[v].display) {   // host RGBA8 readback of the display image
+            while (ctx->host_display_bufs.size() <= v) ctx->host_display_bufs.push_back(new DevBuf());
+            CK(ctx->host_display_bufs[v]->ensure(npix * 4), "display image");
+            CK(ohao::launch_display(acc[v], static_cast<uint32_t>(npix), ctx->host_display_bufs[v]->as<uint8_t>(), cs),
+               "display");
+            CK(cudaMemcpyAsync(views[v].display, ctx->host_display_bufs[v]->p, npix * 4, cudaMemcpyDeviceToHost, cs),
+               "display download");
+        }
     }
     return check_device_error(ctx, cs);
 }
@@ -810,6 +867,12 @@ ohao_status ohao_pt_adjoint(ohao_pt_ctx* ctx, const ohao_pt_view* views, uint32_
     ohao_pt_settings replay = *st;
     if (st->flags & OHAO_PT_FLAG_ADJOINT_DECORRELATE) replay.sample_index_base = st->sample_index_base + st->spp;
     return run_backward(ctx, rvs, cgrads.data(), &replay, d_grad_albedo_map, d_grad_roughness, cs);
+}
+
+ohao_status ohao_pt_display(const float* d_rgba32f, uint32_t npix, uint8_t* d_rgba8, ohao_stream stream) {
+    if (npix && (!d_rgba32f || !d_rgba8)) return OHAO_ERR_INVALID_ARG;
+    const cudaError_t e = ohao::launch_display(d_rgba32f, npix, d_rgba8, reinterpret_cast<cudaStream_t>(stream));
+    return e == cudaSuccess ? OHAO_OK : OHAO_ERR_CUDA;
 }
 
 ohao_status ohao_pt_get_profile(const ohao_pt_ctx* ctx, ohao_pt_profile* out) {

@@ -29,6 +29,8 @@ ohao_status bvh_build(const float* d_boxes, uint32_t n, void* d_scratch, size_t 
 
 // Triangle gather kernels (scene_kernels.cu).
 // Flat: world-space triangles of all visible instances, instance-major.
+// *out = max(*out, max of a[0..n)); the caller zeroes *out first.
+void launch_max_u32(const uint32_t* a, size_t n, uint32_t* out, cudaStream_t st);
 void launch_flat_triangles(const float* pos, const uint32_t* indices, const uint32_t* inst_first_index,
                            const uint32_t* inst_tri_offset, const float* inst_o2w, uint32_t n_inst, uint32_t total,
                            float* tri_verts /*9 per tri*/, uint32_t* tri_inst, uint32_t* tri_prim, float* boxes,

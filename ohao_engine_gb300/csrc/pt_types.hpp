@@ -83,6 +83,9 @@ struct ProfileAcc {
     uint64_t nodes_closest = 0, tris_closest = 0, nodes_shadow = 0, tris_shadow = 0;
 };
 
+// display.cu: RGBA8 display image of npix RGBA32F texels
+cudaError_t launch_display(const float* accum, uint32_t npix, uint8_t* rgba8, cudaStream_t st);
+
 // wavefront.cu
 size_t wavefront_scratch_bytes(uint32_t capacity);
 uint32_t wavefront_default_capacity();

@@ -137,7 +137,28 @@ __global__ void k_instance_boxes(const float* __restrict__ o2w, const uint2* __r
     }
 }
 
+// Largest value of a uint32 array (atomicMax into *out, which the caller
+// zeroes): the index and material-id range checks of a device-side
+// geometry upload.
+__global__ void k_max_u32(const uint32_t* __restrict__ a, size_t n, uint32_t* __restrict__ out) {
+    uint32_t m = 0;
+    for (size_t i = blockIdx.x * static_cast<size_t>(blockDim.x) + threadIdx.x; i < n;
+         i += static_cast<size_t>(gridDim.x) * blockDim.x)
+        m = a[i] > m ? a[i] : m;
+    for (int off = 16; off > 0; off >>= 1) {
+        const uint32_t o = __shfl_down_sync(0xFFFFFFFFu, m, off);
+        m = o > m ? o : m;
+    }
+    if ((threadIdx.x & 31) == 0 && m) atomicMax(out, m);
+}
+
 }  // namespace
+
+void launch_max_u32(const uint32_t* a, size_t n, uint32_t* out, cudaStream_t st) {
+    if (n == 0) return;
+    const size_t want = (n + 255) / 256;
+    k_max_u32<<<static_cast<unsigned>(std::min<size_t>(want, 152 * 8)), 256, 0, st>>>(a, n, out);
+}
 
 void launch_instance_boxes(const float* o2w, const uint32_t* span, const float4* recs, uint32_t n, float* boxes,
                            cudaStream_t st) {

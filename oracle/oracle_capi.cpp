@@ -448,6 +448,28 @@ int orc_glsl_env(int fn, const float* marg, const float* cond, uint32_t w, uint3
     }
     return 0;
 }
+// The reference's display transform to RGBA8 (pt_raygen.rgen:99-102,
+// 1262-1269): per channel pow(ACES(x * 0.5), 1/2.2) stored to UNORM8 with
+// round to nearest, alpha 255. The byte is the number of thresholds
+// ((k + 0.5) / 255)^2.2 (k = 0..254, double pow rounded to float) that
+// ACES(x * 0.5) reaches, which is that rounding without a float pow.
+void orc_display_rgba8(const float* rgba, uint64_t npix, uint8_t* out) {
+    float thr[255];
+    for (int k = 0; k < 255; ++k) thr[k] = static_cast<float>(std::pow((k + 0.5) / 255.0, 2.2));
+    for (uint64_t i = 0; i < npix; ++i) {
+        for (int c = 0; c < 3; ++c) {
+            const float x = rgba[4 * i + c] * 0.5f;
+            const float y = (x * (2.51f * x + 0.03f)) / (x * (2.43f * x + 0.59f) + 0.14f);
+            const float cl = std::min(std::max(y, 0.0f), 1.0f);
+            const float v = (y != y) ? 0.0f : cl;   // NaN -> 0
+            int b = 0;
+            while (b < 255 && v >= thr[b]) ++b;
+            out[4 * i + c] = static_cast<uint8_t>(b);
+        }
+        out[4 * i + 3] = 255;
+    }
+}
+
 int orc_num_threads() {
 #ifdef _OPENMP
     return omp_get_max_threads();

@@ -75,6 +75,7 @@ def lib():
         L.orc_sampler_stream.argtypes = [u32, u32, u32, u32, u32, vp]
         L.orc_math.argtypes = [i32, vp, u32, vp]
         L.orc_num_threads.restype = i32
+        L.orc_display_rgba8.argtypes = [vp, u64, vp]
         L.orc_glsl_helper.argtypes = [i32, vp, u32, vp]
         L.orc_glsl_helper.restype = i32
         L.orc_glsl_env.argtypes = [i32, vp, vp, u32, u32, vp, u32, vp]
@@ -286,6 +287,15 @@ class OracleScene:
         if rc != 0:
             raise ValueError("detached_grad: too many parameters")
         return out
+
+
+def display_rgba8(rgba: np.ndarray) -> np.ndarray:
+    """RGBA8 display image of RGBA32F texels (n, 4): the reference's
+    pow(ACES(x * 0.5), 1/2.2) to UNORM8, alpha 255."""
+    a = np.ascontiguousarray(rgba, np.float32).reshape(-1, 4)
+    out = np.zeros((a.shape[0], 4), np.uint8)
+    lib().orc_display_rgba8(_p(a), a.shape[0], _p(out))
+    return out
 
 
 def accumulate(paths: np.ndarray, accum: np.ndarray | None = None, history: int = 0):

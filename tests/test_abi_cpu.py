@@ -44,7 +44,7 @@ def test_exports_every_declared_symbol(og):
 
 def test_struct_sizes_match_header(og):
     import ctypes as C
-    assert C.sizeof(og.View) == 16 * 4 * 2 + 16 + 3 * 8
+    assert C.sizeof(og.View) == 16 * 4 * 2 + 16 + 4 * 8
     assert C.sizeof(og.Settings) == 64
     from ohao_engine_gb300 import scenes
     assert scenes.INSTANCE_DTYPE.itemsize == 64

@@ -194,3 +194,47 @@ def test_denoiser_wait_timeout_is_a_status(gpu_lib):
     torch.cuda.synchronize()
     assert torch.isfinite(out).all()
     dn.close()
+
+
+@pytest.mark.parametrize("stride", [12, 100])
+def test_device_geometry_upload(gpu_lib, stride):
+    """ohao_pt_set_geometry_device (device buffers, a stream, OHAO's 100-byte
+    Vertex stride) builds the same BVH and renders the same image as the
+    host-array upload; an out-of-range index is rejected on the device."""
+    import torch
+    og = gpu_lib
+    sd = small_instanced(side=16)
+    ref = gpu_tracer(og, sd)
+    v = sd.views[0]
+    npix = v.width * v.height
+    acc_ref = torch.zeros((npix, 4), dtype=torch.float32, device="cuda")
+    ref.render([og.make_view(v, accum=acc_ref)], og.make_settings(spp=2, max_bounces=4))
+    nv, nt = sd.pos.shape[0], sd.ntris
+    packed = np.zeros((nv, stride // 4), np.float32)
+    packed[:, :3] = sd.pos
+    packed[:, 3:] = 7.0   # other vertex attributes the stride skips
+    stream = torch.cuda.Stream()
+    d = [torch.from_numpy(np.ascontiguousarray(a)).cuda() for a in
+         (packed, sd.normals, sd.uvs, sd.indices.astype(np.int32), sd.mat_ids.astype(np.int32))]
+    pt = og.PathTracer()
+    pt.set_geometry_device(d[0], d[1], d[2], d[3], d[4], nv, nt, pos_stride_bytes=stride, stream=stream.cuda_stream)
+    for fi, ic in sd.blas:
+        pt.create_blas(fi, ic)
+    pt.set_instances(sd.instances)
+    pt.set_materials(sd.materials)
+    pt.set_env(sd.env, intensity=sd.env_intensity)
+    pt.build()
+    for which in (-1,):
+        a, b = pt.bvh(which), ref.bvh(which)
+        assert np.array_equal(a[0], b[0]) and np.array_equal(a[1], b[1])
+    acc = torch.zeros_like(acc_ref)
+    pt.render([og.make_view(v, accum=acc)], og.make_settings(spp=2, max_bounces=4))
+    torch.cuda.synchronize()
+    assert torch.equal(acc, acc_ref)
+    bad = d[3].clone()
+    bad[5] = nv
+    with pytest.raises(og.OhaoError) as e:
+        pt.set_geometry_device(d[0], d[1], d[2], bad, d[4], nv, nt, pos_stride_bytes=stride)
+    assert e.value.status == -1
+    pt.close()
+    ref.close()
