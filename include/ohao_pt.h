@@ -118,6 +118,12 @@ typedef struct ohao_pt_view {
  * estimates the gradient of the loss of the expected image; with the same
  * samples it would also differentiate the image's noise. */
 #define OHAO_PT_FLAG_ADJOINT_DECORRELATE (1u << 17)
+/* ohao_pt_adjoint: the loss of the reference's inverse lab, mseRGB on
+ * display images (ohao/inverse/image_loss.hpp:59-80): d_targets hold display
+ * values in [0, 1] (an RGBA8 capture / 255) and the render passes through
+ * the display transform pow(ACES(x / 2), 1/2.2) in float -- before the 8-bit
+ * rounding, whose derivative is zero almost everywhere. */
+#define OHAO_PT_FLAG_ADJOINT_LDR_LOSS (1u << 18)
 
 #define OHAO_PT_MODE_AUTO 0u
 #define OHAO_PT_MODE_WAVEFRONT 1u
@@ -263,6 +269,18 @@ ohao_status ohao_pt_adjoint(ohao_pt_ctx* ctx, const ohao_pt_view* views, uint32_
                                   const ohao_pt_settings* settings, const float* const* d_targets,
                                   float* d_grad_albedo_map, float* d_grad_roughness, float* loss,
                                   ohao_stream stream);
+
+/* Host-buffer variant (the inverse lab keeps its images and parameters in
+ * host memory): views' device pointers are ignored; host_targets[v] (RGBA32F
+ * width*height, display values in [0, 1] with OHAO_PT_FLAG_ADJOINT_LDR_LOSS)
+ * are uploaded, the renders accumulate in library-owned device images, and
+ * the gradients land in host_grad_albedo_map (map_h*map_w*3 floats) and
+ * host_grad_roughness (one float per material); either may be NULL. Returns
+ * when the host buffers hold the results. */
+ohao_status ohao_pt_adjoint_host(ohao_pt_ctx* ctx, const ohao_pt_view* views, uint32_t n_views,
+                                 const ohao_pt_settings* settings, const float* const* host_targets,
+                                 float* host_grad_albedo_map, float* host_grad_roughness, float* loss,
+                                 ohao_stream stream);
 
 /* ---- traceRayEXT as a batch call ----
  * rays: device, n x 8 floats (origin.xyz, tmin, dir.xyz, tmax).

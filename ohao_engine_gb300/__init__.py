@@ -32,6 +32,7 @@ FLAG_ENV_FIXED_V = 1 << 8
 FLAG_GGX_VNDF = 1 << 9        # VNDF sampling of the first specular bounce (not the offline estimator)
 FLAG_PROFILE = 1 << 16
 FLAG_ADJOINT_DECORRELATE = 1 << 17
+FLAG_ADJOINT_LDR_LOSS = 1 << 18   # loss on display values (the reference's mseRGB), targets in [0, 1]
 MODE_AUTO, MODE_WAVEFRONT, MODE_PERSISTENT = 0, 1, 2
 AOV_FLOATS = 12   # OHAO_PT_AOV_FLOATS: first-hit record per pixel (ohao_pt_view.aov)
 
@@ -43,6 +44,7 @@ EXPORTED_SYMBOLS = [
     "ohao_pt_get_profile", "ohao_pt_trace", "ohao_pt_bvh_info", "ohao_pt_bvh_download", "ohao_bvh_build_noalloc",
     "ohao_pt_autotune", "ohao_pt_launch_config", "ohao_pt_launch_config_at", "ohao_pt_set_launch_config",
     "ohao_pt_backward", "ohao_pt_adjoint", "ohao_pt_display", "ohao_pt_set_geometry_device",
+    "ohao_pt_adjoint_host",
 ]
 
 
@@ -124,6 +126,8 @@ def load_library(path: str | None = None):
         "ohao_pt_adjoint": ([vp, C.POINTER(View), u32, C.POINTER(Settings), C.POINTER(vp), vp, vp,
                                    C.POINTER(f32), vp], i32),
         "ohao_pt_display": ([vp, u32, vp, vp], i32),
+        "ohao_pt_adjoint_host": ([vp, C.POINTER(View), u32, C.POINTER(Settings), C.POINTER(vp), vp, vp,
+                                  C.POINTER(f32), vp], i32),
         "ohao_pt_set_geometry_device": ([vp, vp, u32, u32, vp, vp, vp, u32, vp, vp], i32),
     }
     for name, (args, res) in sigs.items():
@@ -433,6 +437,20 @@ class PathTracer:
         loss = C.c_float()
         self._ck(self._L.ohao_pt_adjoint(self.h, arr, len(views), C.byref(settings), ptrs, gm, gr, C.byref(loss),
                                          _ptr(stream) if stream is not None else None), "adjoint")
+        return loss.value
+
+    def adjoint_host(self, views, settings: Settings, host_targets, grad_map=None, grad_rough=None) -> float:
+        """ohao_pt_adjoint_host: targets and gradients in host (numpy) memory."""
+        arr = _view_array(views, settings)
+        if len(host_targets) != len(views):
+            raise ValueError("adjoint_host: one host target per view")
+        tp = (C.c_void_p * len(views))(*[_buffer(t, v.width * v.height * 4, "host_targets", host=True)
+                                         for t, v in zip(host_targets, views)])
+        gm = _buffer(grad_map, self._map_floats, "grad_map", host=True)
+        gr = _buffer(grad_rough, self._nmats, "grad_rough", host=True)
+        loss = C.c_float()
+        self._ck(self._L.ohao_pt_adjoint_host(self.h, arr, len(views), C.byref(settings), tp, gm, gr, C.byref(loss),
+                                              None), "adjoint_host")
         return loss.value
 
     @staticmethod

@@ -89,13 +89,15 @@ struct ohao_pt_ctx {
     // scratch
     DevBuf scratch, build_scratch, err_flag;
     DevBuf adj_scratch, adj_grads;        // backward: view table, loss cell; per-pixel loss gradients
-    std::vector<DevBuf*> host_accum_bufs, host_display_bufs;
+    std::vector<DevBuf*> host_accum_bufs, host_display_bufs, host_target_bufs;
+    DevBuf host_grad_bufs[2];             // ohao_pt_adjoint_host: map and roughness gradients
     ohao_pt_profile profile{};
     ohao::PersistentState* persistent = nullptr;
     ~ohao_pt_ctx() {
         if (persistent) ohao::persistent_destroy(persistent);
         for (auto* b : host_accum_bufs) delete b;
         for (auto* b : host_display_bufs) delete b;
+        for (auto* b : host_target_bufs) delete b;
     }
 };
 
@@ -859,14 +861,59 @@ ohao_status ohao_pt_adjoint(ohao_pt_ctx* ctx, const ohao_pt_view* views, uint32_
     const std::vector<ohao::RenderView> rvs = to_render_views(fresh.data(), n_views, acc.data());
     std::string err;
     float l = 0.0f;
-    s = ohao::adjoint_mse(rvs.data(), d_targets, n_views, ctx->adj_scratch.p, ctx->adj_scratch.n, grads.data(), &l, cs,
-                          err);
+    s = ohao::adjoint_mse(rvs.data(), d_targets, n_views, (st->flags & OHAO_PT_FLAG_ADJOINT_LDR_LOSS) != 0,
+                          ctx->adj_scratch.p, ctx->adj_scratch.n, grads.data(), &l, cs, err);
     if (s != OHAO_OK) return fail(ctx, s, err);
     if (loss) *loss = l;
     std::vector<const float*> cgrads(grads.begin(), grads.end());
     ohao_pt_settings replay = *st;
     if (st->flags & OHAO_PT_FLAG_ADJOINT_DECORRELATE) replay.sample_index_base = st->sample_index_base + st->spp;
     return run_backward(ctx, rvs, cgrads.data(), &replay, d_grad_albedo_map, d_grad_roughness, cs);
+}
+
+ohao_status ohao_pt_adjoint_host(ohao_pt_ctx* ctx, const ohao_pt_view* views, uint32_t n_views,
+                                 const ohao_pt_settings* st, const float* const* host_targets,
+                                 float* host_grad_albedo_map, float* host_grad_roughness, float* loss,
+                                 ohao_stream stream) {
+    if (!ctx || !views || !host_targets || n_views == 0) return fail(ctx, OHAO_ERR_INVALID_ARG, "adjoint_host: null argument");
+    cudaStream_t cs = reinterpret_cast<cudaStream_t>(stream);
+    CK(cudaSetDevice(ctx->device), "set device");
+    while (ctx->host_accum_bufs.size() < n_views) ctx->host_accum_bufs.push_back(new DevBuf());
+    while (ctx->host_target_bufs.size() < n_views) ctx->host_target_bufs.push_back(new DevBuf());
+    std::vector<ohao_pt_view> dv(views, views + n_views);
+    std::vector<const float*> tgt(n_views);
+    for (uint32_t v = 0; v < n_views; ++v) {
+        if (!host_targets[v]) return fail(ctx, OHAO_ERR_INVALID_ARG, "adjoint_host: null target");
+        const size_t bytes = static_cast<size_t>(views[v].width) * views[v].height * 16;
+        CK(ctx->host_accum_bufs[v]->ensure(bytes), "adjoint_host accum");
+        CK(ctx->host_target_bufs[v]->ensure(bytes), "adjoint_host target");
+        CK(cudaMemcpyAsync(ctx->host_target_bufs[v]->p, host_targets[v], bytes, cudaMemcpyHostToDevice, cs),
+           "target upload");
+        dv[v].accum = ctx->host_accum_bufs[v]->as<float>();
+        dv[v].path_radiance = nullptr;
+        dv[v].aov = nullptr;
+        dv[v].display = nullptr;
+        tgt[v] = ctx->host_target_bufs[v]->as<float>();
+    }
+    const size_t map_floats = static_cast<size_t>(ctx->map_w) * ctx->map_h * 3;
+    float* gm = nullptr;
+    float* gr = nullptr;
+    if (host_grad_albedo_map && map_floats) {
+        CK(ctx->host_grad_bufs[0].ensure(map_floats * 4), "gradient buffer");
+        gm = ctx->host_grad_bufs[0].as<float>();
+    }
+    if (host_grad_roughness && ctx->nmats) {
+        CK(ctx->host_grad_bufs[1].ensure(static_cast<size_t>(ctx->nmats) * 4), "gradient buffer");
+        gr = ctx->host_grad_bufs[1].as<float>();
+    }
+    const ohao_status s = ohao_pt_adjoint(ctx, dv.data(), n_views, st, tgt.data(), gm, gr, loss, stream);
+    if (s != OHAO_OK) return s;
+    if (gm) CK(cudaMemcpyAsync(host_grad_albedo_map, gm, map_floats * 4, cudaMemcpyDeviceToHost, cs), "gradient download");
+    if (gr)
+        CK(cudaMemcpyAsync(host_grad_roughness, gr, static_cast<size_t>(ctx->nmats) * 4, cudaMemcpyDeviceToHost, cs),
+           "gradient download");
+    CK(cudaStreamSynchronize(cs), "adjoint_host");
+    return OHAO_OK;
 }
 
 ohao_status ohao_pt_display(const float* d_rgba32f, uint32_t npix, uint8_t* d_rgba8, ohao_stream stream) {

@@ -624,14 +624,44 @@ __global__ void __launch_bounds__(128) k_adjoint(const __grid_constant__ DScene 
 
 // Per-view MSE over RGB and its gradient: loss += scale * sum (I - T)^2,
 // grad = 2 scale (I - T), scale = 1 / (n_views * npix * 3).
+// Display transform of the reference, D(x) = pow(ACES(x / 2), 1/2.2)
+// (pt_raygen.rgen:99-102, 1263-1264), in float before the 8-bit rounding,
+// and its derivative (zero where ACES clamps).
+__device__ __forceinline__ void display_and_slope(float x, float& d, float& slope) {
+    const float u = 0.5f * x;
+    const float num = u * (2.51f * u + 0.03f), den = u * (2.43f * u + 0.59f) + 0.14f;
+    const float a = num / den;
+    if (!(a > 0.0f)) { d = 0.0f; slope = 0.0f; return; }
+    if (a >= 1.0f) { d = 1.0f; slope = 0.0f; return; }
+    d = powf(a, 1.0f / 2.2f);
+    const float da_du = ((5.02f * u + 0.03f) * den - num * (4.86f * u + 0.59f)) / (den * den);
+    slope = (1.0f / 2.2f) * (d / a) * da_du * 0.5f;
+}
+
+// Per-pixel loss gradient and loss sum of one view. Linear: RGB squared error
+// of the radiance against the target radiance. Display (ldr): RGB squared
+// error of D(radiance) against the target's display values in [0, 1] (an
+// RGBA8 target / 255), the mseRGB of the reference's inverse lab.
 __global__ void k_mse_grad(const float4* __restrict__ img, const float4* __restrict__ target, uint32_t npix,
-                           float scale, float4* __restrict__ grad, double* __restrict__ loss_sum) {
+                           float scale, int ldr, float4* __restrict__ grad, double* __restrict__ loss_sum) {
     double part = 0.0;
     for (uint32_t p = blockIdx.x * blockDim.x + threadIdx.x; p < npix; p += gridDim.x * blockDim.x) {
         const float4 a = img[p], t = target[p];
-        const float ex = a.x - t.x, ey = a.y - t.y, ez = a.z - t.z;
+        float ex, ey, ez;
+        float4 g;
+        if (ldr) {
+            float dx, dy, dz, sx, sy, sz;
+            display_and_slope(a.x, dx, sx);
+            display_and_slope(a.y, dy, sy);
+            display_and_slope(a.z, dz, sz);
+            ex = dx - t.x; ey = dy - t.y; ez = dz - t.z;
+            g = make_float4(2.0f * scale * ex * sx, 2.0f * scale * ey * sy, 2.0f * scale * ez * sz, 0.0f);
+        } else {
+            ex = a.x - t.x; ey = a.y - t.y; ez = a.z - t.z;
+            g = make_float4(2.0f * scale * ex, 2.0f * scale * ey, 2.0f * scale * ez, 0.0f);
+        }
         part += static_cast<double>(ex) * ex + static_cast<double>(ey) * ey + static_cast<double>(ez) * ez;
-        grad[p] = make_float4(2.0f * scale * ex, 2.0f * scale * ey, 2.0f * scale * ez, 0.0f);
+        grad[p] = g;
     }
     for (int off = 16; off > 0; off >>= 1) part += __shfl_down_sync(0xFFFFFFFFu, part, off);
     if ((threadIdx.x & 31) == 0) atomicAdd(loss_sum, part * static_cast<double>(scale));
@@ -645,7 +675,7 @@ uint32_t adjoint_max_bounces() { return static_cast<uint32_t>(kMaxRec); }
 
 size_t adjoint_scratch_bytes(uint32_t nviews) { return round256(nviews * sizeof(AdjView)) + 256; }
 
-ohao_status adjoint_mse(const RenderView* views, const float* const* targets, uint32_t nviews, void* scratch,
+ohao_status adjoint_mse(const RenderView* views, const float* const* targets, uint32_t nviews, bool ldr, void* scratch,
                         size_t scratch_bytes, float* const* grads_out, float* loss_out, cudaStream_t st,
                         std::string& err) {
     if (scratch_bytes < adjoint_scratch_bytes(nviews)) {
@@ -662,7 +692,7 @@ ohao_status adjoint_mse(const RenderView* views, const float* const* targets, ui
         const float scale = static_cast<float>(1.0 / (static_cast<double>(nviews) * npix * 3.0));
         k_mse_grad<<<std::max(1u, std::min(1024u, (npix + 255) / 256)), 256, 0, st>>>(
             reinterpret_cast<const float4*>(views[v].accum), reinterpret_cast<const float4*>(targets[v]), npix, scale,
-            reinterpret_cast<float4*>(grads_out[v]), dloss);
+            ldr ? 1 : 0, reinterpret_cast<float4*>(grads_out[v]), dloss);
     }
     double lsum = 0.0;
     cudaMemcpyAsync(&lsum, dloss, sizeof(double), cudaMemcpyDeviceToHost, st);

@@ -115,8 +115,10 @@ ohao_status persistent_autotune(PersistentState* s, const DScene& sc, const Rend
 uint32_t adjoint_max_bounces();
 size_t adjoint_scratch_bytes(uint32_t nviews);
 // Mean over views of the per-view RGB MSE between views[v].accum and
-// targets[v]; writes d loss / d pixel into grads_out[v] (device RGBA32F).
-ohao_status adjoint_mse(const RenderView* views, const float* const* targets, uint32_t nviews, void* scratch,
+// targets[v] (with ldr: between the display transform of views[v].accum and
+// display-space targets); writes d loss / d pixel into grads_out[v] (device
+// RGBA32F).
+ohao_status adjoint_mse(const RenderView* views, const float* const* targets, uint32_t nviews, bool ldr, void* scratch,
                         size_t scratch_bytes, float* const* grads_out, float* loss_out, cudaStream_t st,
                         std::string& err);
 // Path-replay gradient: grads[v] = d loss / d pixel of views[v]'s image (the
