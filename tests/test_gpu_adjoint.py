@@ -205,3 +205,54 @@ def test_adjoint_decorrelated_replay(gpu_lib, oracle):
     g64 = o.detached_grad(v, ost, spp, spp, dLdI, [0, 1, 2, 3], map_ids, with_score=True)
     dev = np.concatenate([grough.cpu().numpy()[:4], g[map_ids]]).astype(np.float64)
     assert np.allclose(dev, g64, rtol=1e-3, atol=1e-6 * np.abs(g64).max()), (dev, g64)
+
+
+@pytest.mark.gpu
+def test_display_space_loss_equals_chain_rule(gpu_lib):
+    """OHAO_PT_FLAG_ADJOINT_LDR_LOSS (the lab's mseRGB on display values):
+    loss and gradients equal ohao_pt_backward fed with dL/dI of the same loss
+    computed here in float64 from the rendered image (chain rule through
+    pow(ACES(x / 2), 1/2.2)), and the host-buffer call gives the same."""
+    import torch
+    og = gpu_lib
+    sd = scenes.studio(freq=20, side=40)
+    pt = H.gpu_tracer(og, sd)
+    view = sd.views[0]
+    npix = view.width * view.height
+    st = og.make_settings(spp=2, max_bounces=3, flags=og.FLAG_ADJOINT_LDR_LOSS)
+    rng = np.random.default_rng(3)
+    tgt_np = rng.uniform(0.05, 0.95, (npix, 4)).astype(np.float32)
+    target = torch.from_numpy(tgt_np).cuda()
+    acc = torch.zeros((npix, 4), dtype=torch.float32, device="cuda")
+    gmap = torch.zeros(sd.albedo_map.size, dtype=torch.float32, device="cuda")
+    grough = torch.zeros(sd.materials.shape[0], dtype=torch.float32, device="cuda")
+    loss = pt.adjoint([og.make_view(view, accum=acc)], st, [target], gmap, grough)
+    torch.cuda.synchronize()
+    I = acc.cpu().numpy()[:, :3].astype(np.float64)
+    u = 0.5 * I
+    num, den = u * (2.51 * u + 0.03), u * (2.43 * u + 0.59) + 0.14
+    a = num / den
+    inside = (a > 0) & (a < 1)
+    D = np.where(a >= 1, 1.0, np.where(inside, np.clip(a, 1e-30, 1) ** (1 / 2.2), 0.0))
+    slope = np.where(inside, (1 / 2.2) * D / np.clip(a, 1e-30, 1)
+                     * ((5.02 * u + 0.03) * den - num * (4.86 * u + 0.59)) / den ** 2 * 0.5, 0.0)
+    E = D - tgt_np[:, :3]
+    ref_loss = (E ** 2).sum() / (npix * 3)
+    assert abs(loss - ref_loss) <= 1e-4 * ref_loss
+    dLdI = np.zeros((npix, 4), np.float32)
+    dLdI[:, :3] = 2.0 * E * slope / (npix * 3)
+    gm2 = torch.zeros_like(gmap)
+    gr2 = torch.zeros_like(grough)
+    plain = og.make_settings(spp=2, max_bounces=3)
+    pt.backward([og.make_view(view)], plain, [torch.from_numpy(dLdI).cuda()], gm2, gr2)
+    torch.cuda.synchronize()
+    g1 = np.concatenate([gmap.cpu().numpy(), grough.cpu().numpy()])
+    g2 = np.concatenate([gm2.cpu().numpy(), gr2.cpu().numpy()])
+    scale = np.abs(g2).max()
+    assert scale > 0 and np.abs(g1 - g2).max() <= 1e-3 * scale
+    hm = np.zeros(sd.albedo_map.size, np.float32)
+    hr = np.zeros(sd.materials.shape[0], np.float32)
+    hl = pt.adjoint_host([og.make_view(view)], st, [tgt_np], hm, hr)
+    assert abs(hl - loss) <= 1e-6 * loss   # same render; sums in another atomic order
+    assert np.abs(np.concatenate([hm, hr]) - g1).max() <= 1e-5 * scale
+    pt.close()
