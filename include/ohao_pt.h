@@ -106,6 +106,10 @@ typedef struct ohao_pt_view {
 /* flag bits keep the reference's PT_FLAG values (pt_raygen.rgen:56-60) */
 #define OHAO_PT_FLAG_FIREFLY_CLAMP (1u << 2)
 #define OHAO_PT_FLAG_ENV_FIXED_V (1u << 8)   /* not reference: un-mirrored env lookup */
+/* Rays without gl_RayFlagsOpaqueEXT: triangles of OHAO_BLAS_FLAG_NO_OPAQUE
+ * BLASes take the alpha test of pt_anyhit.rahit:17-50 (closest-hit and
+ * shadow rays alike). Off by default, as in the reference. */
+#define OHAO_PT_FLAG_ALPHA_TEST (1u << 10)
 /* Not the offline reference estimator: the first specular bounce (stage B)
  * draws the half-vector from the GGX distribution of visible normals with
  * weight F * G2/G1 (pt_raygen_realtime.rgen:723-800, ggx_aniso.glsl:56-133)
@@ -186,16 +190,42 @@ ohao_status ohao_pt_set_geometry_device(ohao_pt_ctx* ctx, const float* d_pos, ui
 /* RTAccelerationStructure::createBLAS (rt_acceleration_structure.cpp:205-300):
  * one triangle geometry over indices [first_index, first_index+index_count). */
 ohao_status ohao_pt_create_blas(ohao_pt_ctx* ctx, uint32_t first_index, uint32_t index_count, uint32_t* out_blas);
+/* Geometry flags of a BLAS. The reference builds every BLAS with
+ * VK_GEOMETRY_OPAQUE_BIT_KHR (rt_acceleration_structure.cpp:227,342) and
+ * traces every ray with gl_RayFlagsOpaqueEXT, so its any-hit shader never
+ * runs; OHAO_BLAS_FLAG_NO_OPAQUE marks a BLAS whose triangles take the
+ * alpha test of pt_anyhit.rahit:17-50 (a hit whose diffuse texture alpha at
+ * the hit's UV is below 0.5 is ignored) for rays traced with
+ * OHAO_PT_FLAG_ALPHA_TEST. Applies from the next ohao_pt_build. */
+#define OHAO_BLAS_FLAG_NO_OPAQUE 1u
+ohao_status ohao_pt_set_blas_flags(ohao_pt_ctx* ctx, uint32_t blas, uint32_t flags);
 /* clearInstances + addInstance (rt_acceleration_structure.hpp:90-97). */
 ohao_status ohao_pt_set_instances(ohao_pt_ctx* ctx, const ohao_pt_instance* inst, uint32_t n);
 /* buildTLAS + the BLAS builds (rt_acceleration_structure.cpp:419-530): LBVH
  * on the device; synchronous with respect to `stream`. */
 ohao_status ohao_pt_build(ohao_pt_ctx* ctx, ohao_stream stream);
 int32_t ohao_pt_is_two_level(const ohao_pt_ctx* ctx);
-/* Material table, 3 x vec4 per material (layout_meta.hpp:20-58). Slot 2 .yzw
- * (unused by the reference) carries emissive RGB. Texture indices other than
- * 0xFFFFFFFF are unsupported except diffuse index 0 = the tile albedo map. */
+/* Material table, 3 x vec4 per material (layout_meta.hpp:20-58): diffuse,
+ * normal, emissive and roughness-metal texture indices into the bindless
+ * texture array of ohao_pt_set_textures (0xFFFFFFFF = none), sampled as
+ * pt_closesthit.rchit:108-157 does (sRGB decode pow(c, 2.2) of diffuse and
+ * emissive, tangent-space normal map in the Frisvad basis, G = roughness and
+ * B = metallic factors). Diffuse index 0 reads the tile albedo map instead
+ * when one is set (ohao_pt_set_albedo_map; linear RGB, no alpha). Slot 2
+ * .yzw (unused by the reference) carries emissive RGB added to the texture's.
+ * Every index a render needs must name a texture by then
+ * (OHAO_ERR_INVALID_ARG otherwise). */
 ohao_status ohao_pt_set_materials(ohao_pt_ctx* ctx, const float* vec4x3, uint32_t n);
+/* The bindless texture array (BindlessTextureManager's sampler2D
+ * textures[], pt_closesthit.rchit:35): RGBA8 UNORM images sampled LINEAR /
+ * REPEAT at LOD 0 with texel centres at (i + 0.5) / size, restated in float.
+ * Replaces the whole array; at most 65536 textures. */
+typedef struct ohao_pt_texture {
+    const uint8_t* rgba8;      /* host, width*height*4 bytes, row 0 at v = 0 */
+    uint32_t width;
+    uint32_t height;
+} ohao_pt_texture;
+ohao_status ohao_pt_set_textures(ohao_pt_ctx* ctx, const ohao_pt_texture* textures, uint32_t n);
 /* updateRTMaterialParams (rt_build.cpp:313-389): rewrite records in place. */
 ohao_status ohao_pt_update_materials(ohao_pt_ctx* ctx, const float* vec4x3, uint32_t first, uint32_t n);
 /* Light SSBO (light_upload.cpp:153-300), at most 64 lights. */
@@ -285,9 +315,10 @@ ohao_status ohao_pt_adjoint_host(ohao_pt_ctx* ctx, const ohao_pt_view* views, ui
 /* ---- traceRayEXT as a batch call ----
  * rays: device, n x 8 floats (origin.xyz, tmin, dir.xyz, tmax).
  * hits: device, n x 5 uint32 (t bits, u bits, v bits, instance, primitive);
- * a miss has instance = primitive = 0xFFFFFFFF. any_hit != 0 writes 1/0 in
- * hits[5i] (occluded). stats (device, optional): n x 2 uint32 nodes/triangles
- * visited. */
+ * a miss has instance = primitive = 0xFFFFFFFF. any_hit bit 0 set writes 1/0
+ * in hits[5i] (occluded); bit 1 set traces non-opaque rays (the alpha test
+ * of OHAO_PT_FLAG_ALPHA_TEST). stats (device, optional): n x 2 uint32
+ * nodes/triangles visited. */
 ohao_status ohao_pt_trace(ohao_pt_ctx* ctx, const float* rays, uint32_t n, uint32_t* hits, int32_t any_hit,
                           uint32_t* stats, ohao_stream stream);
 

@@ -29,6 +29,8 @@ STATUS_NAMES = {0: "OK", -1: "INVALID_ARG", -2: "OOM", -3: "CUDA_ERROR", -4: "TI
 SAMPLER_PCG, SAMPLER_SOBOL = 0, 1
 FLAG_FIREFLY_CLAMP = 1 << 2
 FLAG_ENV_FIXED_V = 1 << 8
+FLAG_ALPHA_TEST = 1 << 10     # non-opaque rays: alpha test on OHAO_BLAS_FLAG_NO_OPAQUE geometry
+BLAS_FLAG_NO_OPAQUE = 1
 FLAG_GGX_VNDF = 1 << 9        # VNDF sampling of the first specular bounce (not the offline estimator)
 FLAG_PROFILE = 1 << 16
 FLAG_ADJOINT_DECORRELATE = 1 << 17
@@ -44,7 +46,7 @@ EXPORTED_SYMBOLS = [
     "ohao_pt_get_profile", "ohao_pt_trace", "ohao_pt_bvh_info", "ohao_pt_bvh_download", "ohao_bvh_build_noalloc",
     "ohao_pt_autotune", "ohao_pt_launch_config", "ohao_pt_launch_config_at", "ohao_pt_set_launch_config",
     "ohao_pt_backward", "ohao_pt_adjoint", "ohao_pt_display", "ohao_pt_set_geometry_device",
-    "ohao_pt_adjoint_host",
+    "ohao_pt_adjoint_host", "ohao_pt_set_textures", "ohao_pt_set_blas_flags",
 ]
 
 
@@ -72,6 +74,11 @@ class Settings(C.Structure):
                 ("sampler", C.c_uint32), ("flags", C.c_uint32), ("clamp_luminance", C.c_float),
                 ("aniso_strength", C.c_float), ("aniso_rotation", C.c_float), ("mode", C.c_uint32),
                 ("trace_stack_limit", C.c_uint32), ("reserved", C.c_uint32 * 6)]
+
+
+class Texture(C.Structure):
+    """ohao_pt_texture"""
+    _fields_ = [("rgba8", C.c_void_p), ("width", C.c_uint32), ("height", C.c_uint32)]
 
 
 class Profile(C.Structure):
@@ -126,6 +133,8 @@ def load_library(path: str | None = None):
         "ohao_pt_adjoint": ([vp, C.POINTER(View), u32, C.POINTER(Settings), C.POINTER(vp), vp, vp,
                                    C.POINTER(f32), vp], i32),
         "ohao_pt_display": ([vp, u32, vp, vp], i32),
+        "ohao_pt_set_textures": ([vp, vp, u32], i32),
+        "ohao_pt_set_blas_flags": ([vp, u32, u32], i32),
         "ohao_pt_adjoint_host": ([vp, C.POINTER(View), u32, C.POINTER(Settings), C.POINTER(vp), vp, vp,
                                   C.POINTER(f32), vp], i32),
         "ohao_pt_set_geometry_device": ([vp, vp, u32, u32, vp, vp, vp, u32, vp, vp], i32),
@@ -362,6 +371,18 @@ class PathTracer:
         l = np.ascontiguousarray(lights, np.float32).reshape(-1, 20)
         self._ck(self._L.ohao_pt_set_lights(self.h, _ptr(l), l.shape[0]), "set_lights")
 
+    def set_textures(self, textures):
+        """Bindless RGBA8 textures, each a (h, w, 4) uint8 array."""
+        arrs = [np.ascontiguousarray(t, np.uint8) for t in textures]
+        for a in arrs:
+            if a.ndim != 3 or a.shape[2] != 4:
+                raise ValueError("set_textures: each texture is a (height, width, 4) uint8 array")
+        tex = (Texture * max(len(arrs), 1))(*[Texture(a.ctypes.data, a.shape[1], a.shape[0]) for a in arrs])
+        self._ck(self._L.ohao_pt_set_textures(self.h, tex, len(arrs)), "set_textures")
+
+    def set_blas_flags(self, blas: int, flags: int):
+        self._ck(self._L.ohao_pt_set_blas_flags(self.h, blas, flags), "set_blas_flags")
+
     def set_env(self, rgba, cdf: EnvCDF | None = None, intensity: float = 1.0, importance_sampling: bool = True):
         if rgba is None:
             self._ck(self._L.ohao_pt_set_env(self.h, None, 0, 0, None, None, 0.0, 0.0), "set_env")
@@ -383,8 +404,12 @@ class PathTracer:
     def load_scene(self, sd, build: bool = True):
         """Upload a :class:`scenes.SceneData` and build its BVH."""
         self.set_geometry(sd.pos, sd.normals, sd.uvs, sd.indices, sd.mat_ids)
-        for fi, ic in sd.blas:
-            self.create_blas(fi, ic)
+        for k, (fi, ic) in enumerate(sd.blas):
+            b = self.create_blas(fi, ic)
+            if sd.blas_flags:
+                self.set_blas_flags(b, int(sd.blas_flags[k]))
+        if sd.textures:
+            self.set_textures(sd.textures)
         self.set_instances(sd.instances)
         self.set_materials(sd.materials)
         if sd.lights is not None and len(sd.lights):
@@ -486,11 +511,12 @@ class PathTracer:
         self._ck(self._L.ohao_pt_get_profile(self.h, C.byref(p)), "get_profile")
         return p
 
-    def trace(self, rays_dev, n: int, hits_dev, any_hit: bool = False, stats_dev=None, stream=None):
+    def trace(self, rays_dev, n: int, hits_dev, any_hit: bool = False, stats_dev=None, stream=None,
+              alpha: bool = False):
         rays = _buffer(rays_dev, 8 * n, "rays")
         hits = _buffer(hits_dev, 5 * n, "hits", floats=False)
         stats = _buffer(stats_dev, 2 * n, "stats", floats=False)
-        self._ck(self._L.ohao_pt_trace(self.h, rays, n, hits, int(any_hit), stats,
+        self._ck(self._L.ohao_pt_trace(self.h, rays, n, hits, int(any_hit) | (2 if alpha else 0), stats,
                                        _ptr(stream) if stream is not None else None), "trace")
 
     def bvh(self, which: int = -1):

@@ -63,6 +63,7 @@ struct BvhDev {
 
 struct BlasDesc {
     uint32_t first_index, index_count;
+    uint32_t flags = 0;        // OHAO_BLAS_FLAG_*
 };
 
 }  // namespace
@@ -79,6 +80,12 @@ struct ohao_pt_ctx {
     bool has_env = false, has_cdf = false;
     float env_intensity = 1.0f;
     uint32_t map_w = 0, map_h = 0;
+    // bindless textures: RGBA8 texels of every texture back to back, and per
+    // texture (first texel, width, height, 0)
+    DevBuf tex_texels, tex_info;
+    uint32_t ntex = 0;
+    // material texture indices the renders need (from the host copy of the table)
+    std::vector<float> mats_host;
     // acceleration structure
     std::vector<BlasDesc> blas;
     std::vector<ohao_pt_instance> instances;
@@ -210,6 +217,10 @@ ohao::DScene make_scene(const ohao_pt_ctx* c) {
     s.map_w = c->map_w;
     s.map_h = c->map_h;
     s.stack_limit = 0;
+    s.tex = c->tex_texels.as<uchar4>();
+    s.tex_info = c->tex_info.as<uint4>();
+    s.ntex = c->ntex;
+    s.alpha_test = 0;
     return s;
 }
 
@@ -344,7 +355,7 @@ ohao_status ohao_pt_create_blas(ohao_pt_ctx* ctx, uint32_t first_index, uint32_t
     *out_blas = 0xFFFFFFFFu;   // INVALID_BLAS
     if (index_count % 3 != 0 || static_cast<uint64_t>(first_index) + index_count > static_cast<uint64_t>(ctx->ntris) * 3)
         return fail(ctx, OHAO_ERR_INVALID_ARG, "create_blas: index range outside the geometry");
-    ctx->blas.push_back({first_index, index_count});
+    ctx->blas.push_back({first_index, index_count, 0u});
     *out_blas = static_cast<uint32_t>(ctx->blas.size() - 1);
     ctx->built = false;
     return OHAO_OK;
@@ -383,7 +394,8 @@ ohao_status ohao_pt_build(ohao_pt_ctx* ctx, ohao_stream stream) {
         instance_matrices(insts[i].transform, di[i].w2o, di[i].nrm);
         di[i].custom = insts[i].custom_index;
         di[i].blas = insts[i].blas;
-        di[i].mask = insts[i].mask;
+        di[i].mask = insts[i].mask & 0xFFu;
+        if (ctx->blas[insts[i].blas].flags & OHAO_BLAS_FLAG_NO_OPAQUE) di[i].mask |= ohao::kInstNoOpaque;
     }
     ohao_status s = upload(ctx, ctx->inst_dev, di.data(), di.size() * sizeof(ohao::DInst), "instances");
     if (s != OHAO_OK) return s;
@@ -511,36 +523,100 @@ ohao_status ohao_pt_build(ohao_pt_ctx* ctx, ohao_stream stream) {
     return OHAO_OK;
 }
 
-// Texture slots of a 48-byte material record (layout_meta.hpp:20-58): only
-// "none" (0xFFFFFFFF) is accepted, and diffuse slot 0 = the tile albedo map.
-static bool material_textures_supported(const float* m, uint32_t n) {
-    for (uint32_t i = 0; i < n; ++i) {
-        uint32_t tex[4];
-        std::memcpy(&tex[0], m + 12 * static_cast<size_t>(i) + 3, 4);   // diffuse
-        std::memcpy(&tex[1], m + 12 * static_cast<size_t>(i) + 6, 4);   // normal
-        std::memcpy(&tex[2], m + 12 * static_cast<size_t>(i) + 7, 4);   // emissive
-        std::memcpy(&tex[3], m + 12 * static_cast<size_t>(i) + 8, 4);   // rough/metal
-        if ((tex[0] != 0xFFFFFFFFu && tex[0] != 0u) || tex[1] != 0xFFFFFFFFu || tex[2] != 0xFFFFFFFFu || tex[3] != 0xFFFFFFFFu)
-            return false;
-    }
+// Texture slots of a 48-byte material record (layout_meta.hpp:20-58):
+// diffuse [3], normal [6], emissive [7], roughness-metal [8].
+constexpr uint32_t kNoTex = 0xFFFFFFFFu;
+constexpr uint32_t kMaxTextures = 65536u;
+static bool material_indices_valid(const float* m, uint32_t n) {
+    for (uint32_t i = 0; i < n; ++i)
+        for (int slot : {3, 6, 7, 8}) {
+            uint32_t t;
+            std::memcpy(&t, m + 12 * static_cast<size_t>(i) + slot, 4);
+            if (t != kNoTex && t >= kMaxTextures) return false;
+        }
     return true;
+}
+
+// Whether every texture index of the material table names a texture (or,
+// for diffuse index 0, the tile albedo map when one is set).
+static bool material_textures_bound(const ohao_pt_ctx* ctx) {
+    const size_t n = ctx->mats_host.size() / 12;
+    for (size_t i = 0; i < n; ++i)
+        for (int slot : {3, 6, 7, 8}) {
+            uint32_t t;
+            std::memcpy(&t, ctx->mats_host.data() + 12 * i + slot, 4);
+            if (t == kNoTex) continue;
+            if (slot == 3 && t == 0u && ctx->map_w > 0) continue;
+            if (t >= ctx->ntex) return false;
+        }
+    return true;
+}
+
+// Whether any material uses a bindless texture (the tile albedo map aside).
+static bool material_uses_textures(const ohao_pt_ctx* ctx) {
+    const size_t n = ctx->mats_host.size() / 12;
+    for (size_t i = 0; i < n; ++i)
+        for (int slot : {3, 6, 7, 8}) {
+            uint32_t t;
+            std::memcpy(&t, ctx->mats_host.data() + 12 * i + slot, 4);
+            if (t == kNoTex || (slot == 3 && t == 0u && ctx->map_w > 0)) continue;
+            return true;
+        }
+    return false;
 }
 
 ohao_status ohao_pt_set_materials(ohao_pt_ctx* ctx, const float* m, uint32_t n) {
     if (!ctx || (n && !m)) return OHAO_ERR_INVALID_ARG;
-    if (!material_textures_supported(m, n))
-        return fail(ctx, OHAO_ERR_UNSUPPORTED, "set_materials: bindless textures are not supported (only diffuse slot 0 = tile albedo map)");
+    if (!material_indices_valid(m, n))
+        return fail(ctx, OHAO_ERR_INVALID_ARG, "set_materials: a texture index is neither 0xFFFFFFFF nor below 65536");
     ohao_status s = upload(ctx, ctx->mats, m, static_cast<size_t>(n) * 48, "materials");
     ctx->nmats = s == OHAO_OK ? n : 0;   // a failed upload may have released the table
+    if (s == OHAO_OK) ctx->mats_host.assign(m, m + static_cast<size_t>(n) * 12);
+    else ctx->mats_host.clear();
     return s;
 }
 
 ohao_status ohao_pt_update_materials(ohao_pt_ctx* ctx, const float* m, uint32_t first, uint32_t n) {
     if (!ctx || (n && !m)) return OHAO_ERR_INVALID_ARG;
     if (static_cast<uint64_t>(first) + n > ctx->nmats) return fail(ctx, OHAO_ERR_INVALID_ARG, "update_materials: range outside the table");
-    if (!material_textures_supported(m, n))
-        return fail(ctx, OHAO_ERR_UNSUPPORTED, "update_materials: bindless textures are not supported (only diffuse slot 0 = tile albedo map)");
+    if (!material_indices_valid(m, n))
+        return fail(ctx, OHAO_ERR_INVALID_ARG, "update_materials: a texture index is neither 0xFFFFFFFF nor below 65536");
     if (n) CK(cudaMemcpy(ctx->mats.as<char>() + static_cast<size_t>(first) * 48, m, static_cast<size_t>(n) * 48, cudaMemcpyHostToDevice), "materials");
+    std::copy(m, m + static_cast<size_t>(n) * 12, ctx->mats_host.begin() + static_cast<size_t>(first) * 12);
+    return OHAO_OK;
+}
+
+ohao_status ohao_pt_set_textures(ohao_pt_ctx* ctx, const ohao_pt_texture* tex, uint32_t n) {
+    if (!ctx || (n && !tex)) return OHAO_ERR_INVALID_ARG;
+    if (n > kMaxTextures) return fail(ctx, OHAO_ERR_INVALID_ARG, "set_textures: more than 65536 textures");
+    uint64_t total = 0;
+    std::vector<uint32_t> info(static_cast<size_t>(std::max(n, 1u)) * 4, 0u);
+    for (uint32_t i = 0; i < n; ++i) {
+        if (!tex[i].rgba8 || tex[i].width == 0 || tex[i].height == 0 || tex[i].width > 65536u || tex[i].height > 65536u)
+            return fail(ctx, OHAO_ERR_INVALID_ARG, "set_textures: null texels or a size outside [1, 65536]");
+        info[4 * i] = static_cast<uint32_t>(total);
+        info[4 * i + 1] = tex[i].width;
+        info[4 * i + 2] = tex[i].height;
+        total += static_cast<uint64_t>(tex[i].width) * tex[i].height;
+        if (total >= (1ull << 32)) return fail(ctx, OHAO_ERR_INVALID_ARG, "set_textures: more than 2^32 texels");
+    }
+    ctx->ntex = 0;   // until every upload below has succeeded
+    CK(ctx->tex_texels.ensure(std::max<uint64_t>(total, 1) * 4), "textures");
+    for (uint32_t i = 0; i < n; ++i)
+        CK(cudaMemcpy(ctx->tex_texels.as<uint8_t>() + static_cast<size_t>(info[4 * i]) * 4, tex[i].rgba8,
+                      static_cast<size_t>(tex[i].width) * tex[i].height * 4, cudaMemcpyHostToDevice), "textures");
+    ohao_status s = upload(ctx, ctx->tex_info, info.data(), info.size() * 4, "texture table");
+    if (s != OHAO_OK) return s;
+    ctx->ntex = n;
+    return OHAO_OK;
+}
+
+ohao_status ohao_pt_set_blas_flags(ohao_pt_ctx* ctx, uint32_t blas, uint32_t flags) {
+    if (!ctx) return OHAO_ERR_INVALID_ARG;
+    if (blas >= ctx->blas.size()) return fail(ctx, OHAO_ERR_INVALID_ARG, "set_blas_flags: unknown BLAS handle");
+    if (flags & ~OHAO_BLAS_FLAG_NO_OPAQUE) return fail(ctx, OHAO_ERR_INVALID_ARG, "set_blas_flags: unknown flag");
+    ctx->blas[blas].flags = flags;
+    ctx->built = false;
     return OHAO_OK;
 }
 
@@ -621,6 +697,8 @@ static ohao_status validate_render(ohao_pt_ctx* ctx, const ohao_pt_view* views, 
     if (!ctx->built) return fail(ctx, OHAO_ERR_NOT_BUILT, "render before ohao_pt_build");
     if (ctx->ntris && ctx->max_mat_id >= ctx->nmats)
         return fail(ctx, OHAO_ERR_INVALID_ARG, "render: a triangle's material id is outside the material table");
+    if (!material_textures_bound(ctx))
+        return fail(ctx, OHAO_ERR_INVALID_ARG, "render: a material's texture index names no texture");
     if (st->spp == 0) return fail(ctx, OHAO_ERR_INVALID_ARG, "render: spp must be >= 1");
     if (st->max_bounces > 64) return fail(ctx, OHAO_ERR_INVALID_ARG, "render: max_bounces > 64");
     if (st->sampler > 1) return fail(ctx, OHAO_ERR_INVALID_ARG, "render: unknown sampler");
@@ -629,6 +707,12 @@ static ohao_status validate_render(ohao_pt_ctx* ctx, const ohao_pt_view* views, 
         if (views[v].width == 0 || views[v].height == 0 || static_cast<uint64_t>(views[v].width) * views[v].height > (1ull << 31))
             return fail(ctx, OHAO_ERR_INVALID_ARG, "render: bad view size");
     return OHAO_OK;
+}
+
+static bool any_non_opaque(const ohao_pt_ctx* ctx) {
+    for (const auto& b : ctx->blas)
+        if (b.flags & OHAO_BLAS_FLAG_NO_OPAQUE) return true;
+    return false;
 }
 
 static std::vector<ohao::RenderView> to_render_views(const ohao_pt_view* views, uint32_t n, float* const* dev_accum) {
@@ -663,6 +747,7 @@ static ohao_status render_views(ohao_pt_ctx* ctx, const ohao_pt_view* views, uin
     ohao::ProfileAcc acc;
     ohao::DScene sc = make_scene(ctx);
     sc.stack_limit = st->trace_stack_limit;
+    sc.alpha_test = (st->flags & OHAO_PT_FLAG_ALPHA_TEST) && any_non_opaque(ctx) ? 1u : 0u;
     ohao::PathParams pp{st->max_bounces, st->sampler, st->flags, st->clamp_luminance, st->aniso_strength,
                         st->aniso_rotation, st->sample_index_base};
     const std::vector<ohao::RenderView> rvs = to_render_views(views, n_views, dev_accum);
@@ -796,6 +881,9 @@ static ohao_status validate_backward(ohao_pt_ctx* ctx, const ohao_pt_view* views
         return fail(ctx, OHAO_ERR_INVALID_ARG, "backward: max_bounces above 16");
     if (st->flags & OHAO_PT_FLAG_GGX_VNDF)
         return fail(ctx, OHAO_ERR_INVALID_ARG, "backward: the replay differentiates the offline estimator; clear GGX_VNDF");
+    if ((st->flags & OHAO_PT_FLAG_ALPHA_TEST) || material_uses_textures(ctx))
+        return fail(ctx, OHAO_ERR_UNSUPPORTED,
+                    "backward: bindless textures and the alpha test are not differentiated (the tile albedo map is)");
     return OHAO_OK;
 }
 
@@ -935,7 +1023,11 @@ ohao_status ohao_pt_trace(ohao_pt_ctx* ctx, const float* rays, uint32_t n, uint3
     cudaStream_t cs = reinterpret_cast<cudaStream_t>(stream);
     CK(cudaSetDevice(ctx->device), "set device");
     std::string err;
-    const ohao_status s = ohao::trace_rays(make_scene(ctx), rays, n, hits, any_hit, stats, cs, ctx->err_flag.as<int>(), err);
+    ohao::DScene sc = make_scene(ctx);
+    sc.alpha_test = (any_hit & 2) && any_non_opaque(ctx) ? 1u : 0u;
+    if ((any_hit & 2) && !material_textures_bound(ctx))
+        return fail(ctx, OHAO_ERR_INVALID_ARG, "trace: a material's texture index names no texture");
+    const ohao_status s = ohao::trace_rays(sc, rays, n, hits, any_hit & 1, stats, cs, ctx->err_flag.as<int>(), err);
     if (s != OHAO_OK) return fail(ctx, s, err);
     return check_device_error(ctx, cs);
 }

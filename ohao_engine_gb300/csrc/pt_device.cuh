@@ -84,6 +84,57 @@ OHAO_D float atan2_f(float y, float x) {
 OHAO_D float asin_f(float x) { return atan2_f(x, sqrtf((1.0f - x) * (1.0f + x))); }
 OHAO_D float acos_f(float x) { return atan2_f(sqrtf((1.0f - x) * (1.0f + x)), x); }
 
+// pow(x, y) for x >= 0 as exp2(y * log2(x)), both defined here (GLSL leaves
+// pow's precision to the implementation): log2 by the atanh series of
+// s = (m - 1)/(m + 1) for x = m 2^e, m in [sqrt(1/2), sqrt(2)) (Abramowitz &
+// Stegun 4.1.27, to s^11); exp2 by reduction to |f| <= 1/2 and the Taylor
+// series of e^(f ln 2) to degree 9, scaled by 2^n from the exponent bits
+// (below 2^-126 flushed to 0). The host oracle evaluates the same steps.
+constexpr float kLn2F = 0x1.62e430p-1f;
+constexpr float kLog2eF = 0x1.715476p+0f;
+OHAO_D float log2_def(float x) {
+    int e = 0;
+    if (x < 0x1p-126f) { x = x * 0x1p23f; e = -23; }
+    const uint32_t b = __float_as_uint(x);
+    e += static_cast<int>((b >> 23) & 0xFFu) - 127;
+    float m = __uint_as_float((b & 0x7FFFFFu) | 0x3F800000u);
+    if (m > 0x1.6a09e6p+0f) { m = m * 0.5f; e += 1; }
+    const float s = (m - 1.0f) / (m + 1.0f);
+    const float s2 = s * s;
+    float p = 1.0f / 11.0f;
+    p = fmaf(p, s2, 1.0f / 9.0f);
+    p = fmaf(p, s2, 1.0f / 7.0f);
+    p = fmaf(p, s2, 1.0f / 5.0f);
+    p = fmaf(p, s2, 1.0f / 3.0f);
+    const float lnm = 2.0f * fmaf(s2 * s, p, s);
+    return fmaf(lnm, kLog2eF, static_cast<float>(e));
+}
+OHAO_D float exp2_def(float y) {
+    if (!(y >= -126.0f)) return y != y ? y : 0.0f;
+    if (y > 127.0f) return INFINITY;
+    const float n = rintf(y);
+    const float z = (y - n) * kLn2F;
+    float p = 1.0f / 362880.0f;
+    p = fmaf(p, z, 1.0f / 40320.0f);
+    p = fmaf(p, z, 1.0f / 5040.0f);
+    p = fmaf(p, z, 1.0f / 720.0f);
+    p = fmaf(p, z, 1.0f / 120.0f);
+    p = fmaf(p, z, 1.0f / 24.0f);
+    p = fmaf(p, z, 1.0f / 6.0f);
+    p = fmaf(p, z, 0.5f);
+    p = fmaf(p, z, 1.0f);
+    p = fmaf(p, z, 1.0f);
+    return p * __uint_as_float(static_cast<uint32_t>(static_cast<int>(n) + 127) << 23);
+}
+OHAO_D float pow5f(float x);
+OHAO_D float pow_def(float x, float y) {
+    if (y == 5.0f) return pow5f(x);
+    if (x == 0.0f) return y > 0.0f ? 0.0f : (y == 0.0f ? 1.0f : INFINITY);
+    if (x == 1.0f || y == 0.0f) return 1.0f;
+    if (!(x > 0.0f)) return NAN;
+    return exp2_def(y * log2_def(x));
+}
+
 OHAO_D float gmaxf(float a, float b) { return a > b ? a : b; }
 OHAO_D float gminf(float a, float b) { return a < b ? a : b; }
 OHAO_D float gclampf(float x, float lo, float hi) { return gminf(gmaxf(x, lo), hi); }
@@ -194,6 +245,62 @@ OHAO_D bool tri_intersect(const RayPre& r, float4 v0, float4 v1, float4 v2, floa
     return true;
 }
 
+// ---------------------------------------------------------------------------
+// bindless textures: RGBA8 UNORM texel c read as c / 255, sampled LINEAR /
+// REPEAT at LOD 0 with texel centres at (i + 0.5) / size (the hardware
+// sampler of the reference's texture array, restated in float)
+// ---------------------------------------------------------------------------
+OHAO_D int wrap_texel(long long i, int n) {
+    const long long m = i % n;
+    return static_cast<int>(m < 0 ? m + n : m);
+}
+OHAO_D float4 unorm4(uchar4 c) {
+    return make_float4(static_cast<float>(c.x) / 255.0f, static_cast<float>(c.y) / 255.0f,
+                       static_cast<float>(c.z) / 255.0f, static_cast<float>(c.w) / 255.0f);
+}
+OHAO_D float4 tex_sample(const DScene& sc, uint32_t idx, float u, float v) {
+    const uint4 ti = __ldg(sc.tex_info + idx);
+    const int W = static_cast<int>(ti.y), H = static_cast<int>(ti.z);
+    const float x = u * static_cast<float>(W) - 0.5f;
+    const float y = v * static_cast<float>(H) - 0.5f;
+    const float fx0 = floorf(x), fy0 = floorf(y);
+    const float fx = x - fx0, fy = y - fy0;
+    const long long ix = static_cast<long long>(fx0), iy = static_cast<long long>(fy0);
+    const int x0 = wrap_texel(ix, W), x1 = wrap_texel(ix + 1, W), y0 = wrap_texel(iy, H), y1 = wrap_texel(iy + 1, H);
+    const uchar4* t = sc.tex + ti.x;
+    const float4 t00 = unorm4(t[static_cast<size_t>(y0) * W + x0]), t10 = unorm4(t[static_cast<size_t>(y0) * W + x1]);
+    const float4 t01 = unorm4(t[static_cast<size_t>(y1) * W + x0]), t11 = unorm4(t[static_cast<size_t>(y1) * W + x1]);
+    float4 r;
+    const float top_x = t00.x * (1.0f - fx) + t10.x * fx, bot_x = t01.x * (1.0f - fx) + t11.x * fx;
+    const float top_y = t00.y * (1.0f - fx) + t10.y * fx, bot_y = t01.y * (1.0f - fx) + t11.y * fx;
+    const float top_z = t00.z * (1.0f - fx) + t10.z * fx, bot_z = t01.z * (1.0f - fx) + t11.z * fx;
+    const float top_w = t00.w * (1.0f - fx) + t10.w * fx, bot_w = t01.w * (1.0f - fx) + t11.w * fx;
+    r.x = top_x * (1.0f - fy) + bot_x * fy;
+    r.y = top_y * (1.0f - fy) + bot_y * fy;
+    r.z = top_z * (1.0f - fy) + bot_z * fy;
+    r.w = top_w * (1.0f - fy) + bot_w * fy;
+    return r;
+}
+
+// pt_anyhit.rahit:17-50 for rays traced without gl_RayFlagsOpaqueEXT: a
+// candidate hit on a non-opaque instance whose material's diffuse texture
+// has alpha < 0.5 at the hit's UV is ignored. Opaque instances, materials
+// without a diffuse texture and the tile albedo map (no alpha) accept.
+OHAO_D bool alpha_accept(const DScene& sc, uint32_t inst, uint32_t prim, float u, float v) {
+    const DInst& in = sc.inst[inst];
+    if (!(__ldg(&in.mask) & kInstNoOpaque)) return true;
+    const uint32_t gtri = (__ldg(&in.custom) & 0xFFFFFFu) + prim;
+    const uint32_t mid = __ldg(sc.mat_ids + gtri);
+    const uint32_t dtex = __float_as_uint(__ldg(&sc.mats[mid * 3].w));
+    if (dtex == 0xFFFFFFFFu || (dtex == 0u && sc.map_w > 0)) return true;
+    const uint32_t i0 = __ldg(sc.indices + gtri * 3), i1 = __ldg(sc.indices + gtri * 3 + 1),
+                   i2 = __ldg(sc.indices + gtri * 3 + 2);
+    const float2 uv0 = __ldg(sc.uvs + i0), uv1 = __ldg(sc.uvs + i1), uv2 = __ldg(sc.uvs + i2);
+    const float w = 1.0f - u - v;
+    const float tu = w * uv0.x + u * uv1.x + v * uv2.x;
+    const float tv = w * uv0.y + u * uv1.y + v * uv2.y;
+    return !(tex_sample(sc, dtex, tu, tv).w < 0.5f);
+}
 
 }  // namespace ohao
 

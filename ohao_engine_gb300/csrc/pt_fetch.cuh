@@ -101,9 +101,10 @@ OHAO_D bool walk_step(const DScene& sc, Walk& w, const RayPre& r, float tmin, fl
             const float4* tp = w.btris + static_cast<size_t>(w.tbase + off + w.tq) * 3;
             const float4 v0 = __ldg(tp), v1 = __ldg(tp + 1), v2 = __ldg(tp + 2);
             float t, u, v;
-            if (tri_intersect(w.ra, v0, v1, v2, tmin, tmax, t, u, v)) {
-                const uint32_t prim = __float_as_uint(v0.w);
-                const uint32_t inst = kLevels == 1 ? __float_as_uint(v1.w) : w.inst;
+            const bool h = tri_intersect(w.ra, v0, v1, v2, tmin, tmax, t, u, v);
+            const uint32_t prim = __float_as_uint(v0.w);
+            const uint32_t inst = kLevels == 1 ? __float_as_uint(v1.w) : w.inst;
+            if (h && (!sc.alpha_test || alpha_accept(sc, inst, prim, u, v))) {
                 if (w.best.prim == kNoHit || t < w.best.t ||
                     (t == w.best.t && key_less(inst, prim, w.best.inst, w.best.prim))) {
                     w.best.t = t; w.best.u = u; w.best.v = v; w.best.inst = inst; w.best.prim = prim;
@@ -238,7 +239,9 @@ OHAO_D bool probe_step(const DScene& sc, Probe& w, const RayPre& r, float tmin, 
             const float4* tp = w.btris + static_cast<size_t>(w.tbase + off + w.tq) * 3;
             const float4 v0 = __ldg(tp), v1 = __ldg(tp + 1), v2 = __ldg(tp + 2);
             float t, u, v;
-            if (tri_intersect(w.ra, v0, v1, v2, tmin, tmax, t, u, v)) {
+            if (tri_intersect(w.ra, v0, v1, v2, tmin, tmax, t, u, v) &&
+                (!sc.alpha_test ||
+                 alpha_accept(sc, kLevels == 1 ? __float_as_uint(v1.w) : w.inst, __float_as_uint(v0.w), u, v))) {
                 w.hit = true;
                 return true;
             }

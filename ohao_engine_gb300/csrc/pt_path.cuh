@@ -247,14 +247,59 @@ OHAO_D void hit_shade(const DScene& sc, V3 o, V3 d, const Hit& h, Surf& s) {
     const uint32_t mid = __ldg(sc.mat_ids + gtri);
     s.matid = mid;
     const float4 m0 = __ldg(sc.mats + mid * 3), m1 = __ldg(sc.mats + mid * 3 + 1), m2 = __ldg(sc.mats + mid * 3 + 2);
+    const uint32_t dtex = __float_as_uint(m0.w), ntex = __float_as_uint(m1.z), etex = __float_as_uint(m1.w),
+                   rmtex = __float_as_uint(m2.x);
+    constexpr uint32_t kNone = 0xFFFFFFFFu;
+    // albedo: base colour times the sRGB-decoded diffuse texture
+    // (pt_closesthit.rchit:108-113); diffuse index 0 is the tile albedo map
+    // when one is set (linear, diff_map.hpp:40-67)
     V3 alb = v3(m0.x, m0.y, m0.z);
-    if (__float_as_uint(m0.w) == 0u && sc.map_w > 0) alb = alb * albedo_map_sample(sc.albedo_map, sc.map_w, sc.map_h, s.tu, s.tv);
+    if (dtex != kNone) {
+        if (dtex == 0u && sc.map_w > 0) {
+            alb = alb * albedo_map_sample(sc.albedo_map, sc.map_w, sc.map_h, s.tu, s.tv);
+        } else {
+            const float4 c = tex_sample(sc, dtex, s.tu, s.tv);
+            alb = alb * v3(pow_def(c.x, 2.2f), pow_def(c.y, 2.2f), pow_def(c.z, 2.2f));
+        }
+    }
+    // tangent-space normal map in the Frisvad basis of the shading normal
+    // (pt_closesthit.rchit:116-133)
+    if (ntex != kNone) {
+        const float4 c = tex_sample(sc, ntex, s.tu, s.tv);
+        const V3 mapN = normalize(v3(c.x * 2.0f - 1.0f, c.y * 2.0f - 1.0f, c.z * 2.0f - 1.0f));
+        V3 T, B;
+        if (wn.z < -0.9999f) {
+            T = v3(0.0f, -1.0f, 0.0f);
+            B = v3(-1.0f, 0.0f, 0.0f);
+        } else {
+            const float a = 1.0f / (1.0f + wn.z);
+            const float d = -wn.x * wn.y * a;
+            T = v3(1.0f - wn.x * wn.x * a, d, -wn.x);
+            B = v3(d, 1.0f - wn.y * wn.y * a, -wn.y);
+        }
+        wn = normalize(T * mapN.x + B * mapN.y + wn * mapN.z);
+    }
     s.N = wn;
     s.albedo = alb;
-    const float rough = gmaxf(m1.x, 0.04f);
-    s.color = v3(m2.y, m2.z, m2.w);
+    // roughness / metallic factors from the ORM texture's G and B
+    // (pt_closesthit.rchit:139-148)
+    float rough = m1.x, metal = m1.y;
+    if (rmtex != kNone) {
+        const float4 c = tex_sample(sc, rmtex, s.tu, s.tv);
+        rough = rough * c.y;
+        metal = metal * c.z;
+    }
+    rough = gmaxf(rough, 0.04f);
+    // emission: the sRGB-decoded emissive texture (pt_closesthit.rchit:150-156)
+    // plus the material's slot-2 emission (not the reference's)
+    V3 emis = v3s(0.0f);
+    if (etex != kNone) {
+        const float4 c = tex_sample(sc, etex, s.tu, s.tv);
+        emis = v3(pow_def(c.x, 2.2f), pow_def(c.y, 2.2f), pow_def(c.z, 2.2f));
+    }
+    s.color = emis + v3(m2.y, m2.z, m2.w);
     // payload.attenuation = (rough, clamp(metal,0,1), curv) -> unpackHitPbr
-    const float ax = rough, ay = gclampf(m1.y, 0.0f, 1.0f);
+    const float ax = rough, ay = gclampf(metal, 0.0f, 1.0f);
     float rr, mm;
     if (ax < 0.0f && ay < 1e-4f) {
         rr = -ax; if (rr >= 10.0f) rr = rr - 10.0f; rr = gmaxf(rr, 0.01f); mm = 1.0f;

@@ -150,9 +150,9 @@ OHAO_D bool order_children(uint32_t rem, const float tn[8], const NodeRec& n, ui
 
 // Closest hit in one BVH (flat, or a BLAS inside instance inst_override).
 template <bool kStats>
-OHAO_D void bvh_closest(const uint4* __restrict__ nodes, const float4* __restrict__ tris, const RayPre& r,
-                        float tmin, float tmax, Hit& best, uint32_t inst_override, uint32_t* st_node, float* st_t,
-                        int stack_base, int lim, TravCount& cnt, int& err) {
+OHAO_D void bvh_closest(const DScene& sc, const uint4* __restrict__ nodes, const float4* __restrict__ tris,
+                        const RayPre& r, float tmin, float tmax, Hit& best, uint32_t inst_override, uint32_t* st_node,
+                        float* st_t, int stack_base, int lim, TravCount& cnt, int& err) {
     if (stack_base >= lim) { err = 1; return; }
     int sp = stack_base;
     uint32_t cur = 0u;
@@ -179,6 +179,7 @@ OHAO_D void bvh_closest(const uint4* __restrict__ nodes, const float4* __restric
                     if (!tri_intersect(r, v0, v1, v2, tmin, tmax, t, u, v)) continue;
                     const uint32_t prim = __float_as_uint(v0.w);
                     const uint32_t inst = (inst_override != 0xFFFFFFFFu) ? inst_override : __float_as_uint(v1.w);
+                    if (sc.alpha_test && !alpha_accept(sc, inst, prim, u, v)) continue;
                     if (best.prim == 0xFFFFFFFFu || t < best.t ||
                         (t == best.t && key_less(inst, prim, best.inst, best.prim))) {
                         best.t = t; best.u = u; best.v = v; best.inst = inst; best.prim = prim;
@@ -200,8 +201,8 @@ OHAO_D void bvh_closest(const uint4* __restrict__ nodes, const float4* __restric
 
 // Any hit in one BVH.
 template <bool kStats>
-OHAO_D bool bvh_any(const uint4* __restrict__ nodes, const float4* __restrict__ tris, const RayPre& r, float tmin,
-                    float tmax, uint32_t* st_node, int stack_base, int lim, TravCount& cnt, int& err) {
+OHAO_D bool bvh_any(const DScene& sc, const uint4* __restrict__ nodes, const float4* __restrict__ tris, const RayPre& r,
+                    float tmin, float tmax, uint32_t* st_node, int stack_base, int lim, TravCount& cnt, int& err) {
     if (stack_base >= lim) { err = 1; return false; }
     int sp = stack_base;
     uint32_t cur = 0u;
@@ -222,7 +223,9 @@ OHAO_D bool bvh_any(const uint4* __restrict__ nodes, const float4* __restrict__ 
                 const float4 v0 = __ldg(tp), v1 = __ldg(tp + 1), v2 = __ldg(tp + 2);
                 if (kStats) cnt.tris++;
                 float t, u, v;
-                if (tri_intersect(r, v0, v1, v2, tmin, tmax, t, u, v)) return true;
+                if (tri_intersect(r, v0, v1, v2, tmin, tmax, t, u, v) &&
+                    (!sc.alpha_test || alpha_accept(sc, __float_as_uint(v1.w), __float_as_uint(v0.w), u, v)))
+                    return true;
             }
         }
         uint32_t rem = m & imask;
@@ -270,8 +273,8 @@ OHAO_D Hit scene_closest(const DScene& sc, V3 o, V3 d, float tmin, float tmax, T
     float st_t[kStackSize];
     const RayPre r = ray_pre(o, d);
     if (kLevels == 1 || (kLevels == 0 && !sc.two_level)) {
-        bvh_closest<kStats>(sc.nodes, sc.tris, r, tmin, tmax, best, 0xFFFFFFFFu, st_node, st_t, 0, stack_limit(sc), cnt,
-                            err);
+        bvh_closest<kStats>(sc, sc.nodes, sc.tris, r, tmin, tmax, best, 0xFFFFFFFFu, st_node, st_t, 0, stack_limit(sc),
+                            cnt, err);
         return best;
     }
     // Two-level: one loop whose every iteration visits one node (TLAS or
@@ -320,6 +323,7 @@ OHAO_D Hit scene_closest(const DScene& sc, V3 o, V3 d, float tmin, float tmax, T
                             float t, u, v;
                             if (!tri_intersect(ra, v0, v1, v2, tmin, tmax, t, u, v)) continue;
                             const uint32_t prim = __float_as_uint(v0.w);
+                            if (sc.alpha_test && !alpha_accept(sc, inst, prim, u, v)) continue;
                             if (best.prim == 0xFFFFFFFFu || t < best.t ||
                                 (t == best.t && key_less(inst, prim, best.inst, best.prim))) {
                                 best.t = t; best.u = u; best.v = v; best.inst = inst; best.prim = prim;
@@ -414,7 +418,7 @@ OHAO_D bool scene_occluded(const DScene& sc, V3 o, V3 d, float tmin, float tmax,
     uint32_t st_node[kStackSize];
     const RayPre r = ray_pre(o, d);
     if (kLevels == 1 || (kLevels == 0 && !sc.two_level))
-        return bvh_any<kStats>(sc.nodes, sc.tris, r, tmin, tmax, st_node, 0, stack_limit(sc), cnt, err);
+        return bvh_any<kStats>(sc, sc.nodes, sc.tris, r, tmin, tmax, st_node, 0, stack_limit(sc), cnt, err);
     // Two-level, as one loop (see scene_closest): at a TLAS node the internal
     // children but the last (slot order) are pushed, its instance leaves are
     // entered in slot order, then the last internal child is visited.
@@ -423,6 +427,7 @@ OHAO_D bool scene_occluded(const DScene& sc, V3 o, V3 d, float tmin, float tmax,
     RayPre ra = r;
     const uint4* bnodes = sc.nodes;
     const float4* btris = nullptr;
+    uint32_t inst = 0u;                     // instance of the current BLAS
     int base = 0;
     uint32_t cur = 0u;
     bool have_node = true;
@@ -464,7 +469,9 @@ OHAO_D bool scene_occluded(const DScene& sc, V3 o, V3 d, float tmin, float tmax,
                     const float4 v0 = __ldg(tp), v1 = __ldg(tp + 1), v2 = __ldg(tp + 2);
                     if (kStats) cnt.tris++;
                     float t, u, v;
-                    if (tri_intersect(ra, v0, v1, v2, tmin, tmax, t, u, v)) return true;
+                    if (tri_intersect(ra, v0, v1, v2, tmin, tmax, t, u, v) &&
+                        (!sc.alpha_test || alpha_accept(sc, inst, __float_as_uint(v0.w), u, v)))
+                        return true;
                 }
             }
             if (!in_blas && plm) {
@@ -507,6 +514,7 @@ OHAO_D bool scene_occluded(const DScene& sc, V3 o, V3 d, float tmin, float tmax,
             xform_point(in.w2o, o, oo);
             xform_dir(in.w2o, d, od);
             ra = ray_pre(oo, od);
+            inst = ii;
             bnodes = sc.blas_nodes + static_cast<size_t>(bl.node_off) * 5;
             btris = sc.blas_tris + static_cast<size_t>(bl.tri_off) * 3;
             base = sp;

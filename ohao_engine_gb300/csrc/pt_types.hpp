@@ -10,6 +10,8 @@
 
 namespace ohao {
 
+constexpr uint32_t kInstNoOpaque = 1u << 8;   // DInst::mask: the BLAS takes the alpha test
+
 struct DInst {          // per instance, 96 bytes
     float w2o[12];      // world-to-object 3x4, row-major
     float nrm[9];       // transpose(inverse(mat3(object-to-world))), row-major
@@ -51,6 +53,11 @@ struct DScene {
     const float* albedo_map;
     uint32_t map_w, map_h;
     uint32_t stack_limit;   // traversal stack entries per ray; 0 or >= 64 = all 64
+    // bindless textures (RGBA8 UNORM) and their (first texel, width, height, 0)
+    const uchar4* tex;
+    const uint4* tex_info;
+    uint32_t ntex;
+    uint32_t alpha_test;    // non-opaque rays: alpha-test kInstNoOpaque instances
 };
 
 struct PathParams {

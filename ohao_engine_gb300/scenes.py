@@ -61,6 +61,8 @@ class SceneData:
     albedo_map: np.ndarray | None = None   # (h,w,3) f32
     spp: int = 1
     max_bounces: int = 4
+    textures: list | None = None           # bindless RGBA8 textures, each (h,w,4) u8
+    blas_flags: list | None = None         # per BLAS: OHAO_BLAS_FLAG_* (1 = non-opaque, alpha-tested)
 
     @property
     def ntris(self) -> int:
@@ -434,6 +436,84 @@ def studio(freq=100, seed=1, side=512, n_train=8, n_holdout=2, map_size=64, albe
     return SceneData("studio", P, N, U, I, M, np.stack(mats), np.zeros((0, 20), np.float32), env, 1.0,
                      [(0, I.size)], identity_instance(1), views, albedo_map=np.asarray(albedo_map, np.float32),
                      spp=16, max_bounces=3)
+
+
+def material_tex(albedo, rough=1.0, metal=0.0, diffuse_tex=NO_TEX, normal_tex=NO_TEX, emissive_tex=NO_TEX,
+                 rough_metal_tex=NO_TEX, emissive=(0.0, 0.0, 0.0)):
+    """A 48-byte material record with every bindless texture slot
+    (layout_meta.hpp:32-56): diffuse [3], normal [6], emissive [7],
+    roughness-metal [8]."""
+    m = material(albedo, rough=rough, metal=metal, emissive=emissive, diffuse_tex=diffuse_tex)
+    m[6:7] = np.array([normal_tex], np.uint32).view(np.float32)
+    m[7:8] = np.array([emissive_tex], np.uint32).view(np.float32)
+    m[8:9] = np.array([rough_metal_tex], np.uint32).view(np.float32)
+    return m
+
+
+def _textures(rng, size=64):
+    """Seeded RGBA8 textures: 0 checker albedo, 1 bump normal map, 2 ORM
+    (R ao, G roughness, B metallic), 3 noise albedo, 4 emissive pattern, 5
+    albedo with an alpha cut-out (alpha 0, 255 and a soft edge band)."""
+    y, x = np.meshgrid(np.arange(size), np.arange(size), indexing="ij")
+    u, v = (x + 0.5) / size, (y + 0.5) / size
+    tex = []
+    chk = ((x // 8 + y // 8) % 2).astype(np.float64)
+    a = np.stack([0.2 + 0.7 * chk, 0.3 + 0.5 * (1 - chk), 0.6 * np.ones_like(chk), np.ones_like(chk)], -1)
+    tex.append(a)
+    h = 0.5 * np.sin(2 * math.pi * 3 * u) * np.cos(2 * math.pi * 2 * v)
+    nx, ny = -np.gradient(h, axis=1) * 4, -np.gradient(h, axis=0) * 4
+    n = np.stack([nx, ny, np.ones_like(nx)], -1)
+    n /= np.linalg.norm(n, axis=-1, keepdims=True)
+    tex.append(np.concatenate([n * 0.5 + 0.5, np.ones_like(nx)[..., None]], -1))
+    tex.append(np.stack([0.8 + 0.2 * rng.random((size, size)), 0.2 + 0.8 * rng.random((size, size)),
+                         (rng.random((size, size)) > 0.5).astype(np.float64), np.ones((size, size))], -1))
+    tex.append(np.concatenate([rng.random((size, size, 3)), np.ones((size, size, 1))], -1))
+    e = ((np.sin(2 * math.pi * 4 * u) > 0.3) & (np.cos(2 * math.pi * 4 * v) > 0.0)).astype(np.float64)
+    tex.append(np.stack([e, 0.8 * e, 0.3 * e, np.ones_like(e)], -1))
+    r = np.hypot(u - 0.5, v - 0.5)
+    alpha = np.clip((0.42 - r) / 0.04, 0.0, 1.0) * ((x // 6 + y // 6) % 3 != 0)
+    tex.append(np.stack([0.3 + 0.2 * u, 0.6 * np.ones_like(u), 0.2 + 0.3 * v, alpha], -1))
+    return [np.clip(np.rint(t * 255.0), 0, 255).astype(np.uint8) for t in tex]
+
+
+def textured(width=48, height=32, seed=3, freq=12) -> SceneData:
+    """Bindless-texture scene: a tiled floor (checker albedo, normal map,
+    ORM), a displaced sphere (noise albedo, ORM, metallic), an emissive
+    texture panel, and a curtain of alpha cut-out leaves in a non-opaque
+    BLAS, under a sky with a sun and one sphere light."""
+    rng = np.random.default_rng(seed)
+    texs = _textures(rng)
+    b = _Builder()
+    mats = [material_tex((1.0, 1.0, 1.0), rough=0.9, diffuse_tex=0, normal_tex=1, rough_metal_tex=2),
+            material_tex((0.9, 0.9, 0.9), rough=0.7, metal=1.0, diffuse_tex=3, rough_metal_tex=2),
+            material_tex((0.0, 0.0, 0.0), rough=1.0, emissive_tex=4),
+            material_tex((1.0, 1.0, 1.0), rough=0.8, diffuse_tex=5, normal_tex=1)]
+    half = 3.0
+    pos = np.array([(-half, -1.0, -half), (-half, -1.0, half), (half, -1.0, half), (half, -1.0, -half)], np.float64)
+    b.add(pos, np.tile([0.0, 1.0, 0.0], (4, 1)), np.array([[0, 0], [0, 3], [3, 3], [3, 0]], np.float64),
+          [[0, 1, 2], [0, 2, 3]], 0)
+    sp, sn, su, si = displaced_sphere(freq, seed, amp=0.05, radius=0.7, center=(0.3, -0.25, 0.0))
+    b.add(sp, sn, su * 2.0, si, 1)
+    b.quad((-1.6, -0.6, -1.2), (-1.6, -0.6, -0.4), (-1.6, 0.4, -0.4), (-1.6, 0.4, -1.2), (1, 0, 0), 2)
+    opaque_count = b.ntri * 3
+    for k in range(5):     # leaves: the non-opaque BLAS
+        x0 = -1.2 + 0.55 * k
+        z0 = 0.9 + 0.15 * math.sin(k)
+        b.quad((x0, -0.9, z0), (x0 + 0.5, -0.9, z0 + 0.1), (x0 + 0.5, 0.2, z0 + 0.1), (x0, 0.2, z0),
+               (-0.2, 0.0, 1.0), 3)
+    P, N, U, I, M = b.arrays()
+    env = sky_env(64, 32, seed=seed, peak=300.0, radius_deg=4.0)
+    light = np.zeros(20, np.float32)
+    light[0:4] = (1.2, 1.5, 1.5, 0.0)         # sphere light
+    light[4:8] = (1.0, 0.9, 0.8, 6.0)
+    light[11] = 0.15
+    inst = identity_instance(2)
+    inst[1]["blas"] = 1
+    inst[1]["custom_index"] = opaque_count // 3
+    view = look_at_view((0.6, 0.9, 3.6), (0.0, -0.4, 0.0), fov_y_deg=45.0, width=width, height=height)
+    return SceneData("textured", P, N, U, I, M, np.stack(mats), light[None, :], env, 1.0,
+                     [(0, opaque_count), (opaque_count, I.size - opaque_count)], inst, [view], spp=4, max_bounces=4,
+                     textures=texs, blas_flags=[0, 1])
 
 
 WORKLOADS = {"cornell": cornell, "sphere_1m": sphere_1m, "instanced": instanced, "studio": studio}

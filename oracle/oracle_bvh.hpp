@@ -492,6 +492,13 @@ inline NodeHits node_test(const WideNode& n, const RayPre& r, float tmin, float 
     return h;
 }
 
+// Optional test of a candidate hit (an any-hit shader): false ignores it.
+struct HitFilter {
+    const void* ctx = nullptr;
+    bool (*accept)(const void* ctx, uint32_t inst, uint32_t prim, float u, float v) = nullptr;
+    bool operator()(uint32_t inst, uint32_t prim, float u, float v) const { return accept(ctx, inst, prim, u, v); }
+};
+
 struct BvhView {
     const WideNode* nodes = nullptr;
     const TriRec* tris = nullptr;
@@ -508,7 +515,7 @@ inline float cull_limit(const HitRec& best, float tmax) {
 }
 
 inline void bvh_closest(const BvhView& bvh, const RayPre& r, float tmin, float tmax, HitRec& best,
-                        uint32_t inst_override, TravStats* st) {
+                        uint32_t inst_override, TravStats* st, const HitFilter* filter = nullptr) {
     if (bvh.empty()) return;
     std::vector<std::pair<uint32_t, float>> stack;
     stack.reserve(64);
@@ -529,6 +536,7 @@ inline void bvh_closest(const BvhView& bvh, const RayPre& r, float tmin, float t
                 float t, u, v;
                 if (!tri_intersect(r, tr.v0, tr.v1, tr.v2, tmin, tmax, t, u, v)) continue;
                 uint32_t inst = (inst_override != 0xFFFFFFFFu) ? inst_override : tr.inst;
+                if (filter && !(*filter)(inst, tr.prim, u, v)) continue;
                 if (!best.hit() || t < best.t || (t == best.t && key_less(inst, tr.prim, best.inst, best.prim))) {
                     best.t = t; best.u = u; best.v = v; best.inst = inst; best.prim = tr.prim;
                 }
@@ -547,7 +555,8 @@ inline void bvh_closest(const BvhView& bvh, const RayPre& r, float tmin, float t
     }
 }
 
-inline bool bvh_any(const BvhView& bvh, const RayPre& r, float tmin, float tmax, TravStats* st) {
+inline bool bvh_any(const BvhView& bvh, const RayPre& r, float tmin, float tmax, TravStats* st,
+                    const HitFilter* filter = nullptr, uint32_t inst_override = 0xFFFFFFFFu) {
     if (bvh.empty()) return false;
     std::vector<uint32_t> stack;
     stack.reserve(64);
@@ -566,7 +575,9 @@ inline bool bvh_any(const BvhView& bvh, const RayPre& r, float tmin, float tmax,
                 const TriRec& tr = bvh.tris[n.tri_base + off + q];
                 if (st) st->tris++;
                 float t, u, v;
-                if (tri_intersect(r, tr.v0, tr.v1, tr.v2, tmin, tmax, t, u, v)) return true;
+                if (!tri_intersect(r, tr.v0, tr.v1, tr.v2, tmin, tmax, t, u, v)) continue;
+                if (!filter || (*filter)(inst_override != 0xFFFFFFFFu ? inst_override : tr.inst, tr.prim, u, v))
+                    return true;
             }
         }
     }

@@ -86,6 +86,17 @@ void orc_scene_set_albedo_map(Scene* s, const float* map, uint32_t w, uint32_t h
     s->map_w = w; s->map_h = h;
     s->albedo_map.assign(map, map + static_cast<size_t>(w) * h * 3);
 }
+// n RGBA8 textures: texels back to back, sizes as (width, height) pairs
+void orc_scene_set_textures(Scene* s, const uint8_t* texels, const uint32_t* sizes, uint32_t n) {
+    s->tex_info.clear();
+    size_t off = 0;
+    for (uint32_t i = 0; i < n; ++i) {
+        s->tex_info.push_back({off, static_cast<int>(sizes[2 * i]), static_cast<int>(sizes[2 * i + 1])});
+        off += static_cast<size_t>(sizes[2 * i]) * sizes[2 * i + 1];
+    }
+    s->tex_texels.assign(texels, texels + off * 4);
+}
+void orc_scene_set_blas_flags(Scene* s, uint32_t blas, uint32_t flags) { s->blases[blas].no_opaque = (flags & 1u) != 0; }
 uint32_t orc_scene_add_blas(Scene* s, uint32_t first_index, uint32_t index_count) {
     Blas b;
     b.first_index = first_index;
@@ -148,11 +159,14 @@ void orc_trace(const Scene* s, const float* rays, uint32_t n, uint32_t* hits, in
         const float* r = rays + i * 8;
         TravStats st;
         uint32_t* h = hits + i * 5;
-        if (mode == 1) {
-            bool occ = s->occluded(r, r + 4, r[3], r[7], &st);
+        const bool alpha = (mode & 4) != 0;   // non-opaque rays (alpha test)
+        const int kind = mode & 3;
+        if (kind == 1) {
+            bool occ = s->occluded(r, r + 4, r[3], r[7], &st, alpha);
             h[0] = occ ? 1u : 0u; h[1] = h[2] = 0; h[3] = h[4] = 0xFFFFFFFFu;
         } else {
-            HitRec hr = (mode == 2) ? s->closest_brute(r, r + 4, r[3], r[7]) : s->closest(r, r + 4, r[3], r[7], &st);
+            HitRec hr = (kind == 2) ? s->closest_brute(r, r + 4, r[3], r[7], alpha)
+                                    : s->closest(r, r + 4, r[3], r[7], &st, alpha);
             h[0] = f2u(hr.t); h[1] = f2u(hr.u); h[2] = f2u(hr.v); h[3] = hr.inst; h[4] = hr.prim;
             if (!hr.hit()) { h[0] = h[1] = h[2] = 0; h[3] = h[4] = 0xFFFFFFFFu; }
         }
@@ -468,6 +482,10 @@ void orc_display_rgba8(const float* rgba, uint64_t npix, uint8_t* out) {
         }
         out[4 * i + 3] = 255;
     }
+}
+
+void orc_pow_def(const float* x, uint64_t n, float y, float* out) {
+    for (uint64_t i = 0; i < n; ++i) out[i] = pow_def(x[i], y);
 }
 
 int orc_num_threads() {

@@ -106,6 +106,61 @@ inline float atan2_f(float y, float x) {
 inline float asin_f(float x) { return atan2_f(x, std::sqrt((1.0f - x) * (1.0f + x))); }
 inline float acos_f(float x) { return atan2_f(std::sqrt((1.0f - x) * (1.0f + x)), x); }
 
+// GLSL pow(x, 5.0) as used by the Schlick terms: ((x*x)*(x*x))*x.
+template <class T> inline T pow5(T x) { T x2 = x * x; T x4 = x2 * x2; return x4 * x; }
+
+// pow(x, y) for x >= 0 as exp2(y * log2(x)), each defined here (GLSL leaves
+// pow's precision to exp2 and log2 of the implementation):
+//   log2(x): x = m 2^e with m in [sqrt(1/2), sqrt(2)); ln m = 2 atanh(s),
+//            s = (m - 1) / (m + 1), by the atanh series to s^11 (|s| < 0.172;
+//            Abramowitz & Stegun 4.1.27); log2 x = e + ln m / ln 2.
+//   exp2(y): y = n + f, n = rint(y), |f| <= 1/2; 2^f = e^(f ln 2) by its
+//            Taylor series to degree 9; times 2^n built from the exponent
+//            bits (results below 2^-126 flush to 0).
+constexpr float kLn2F = 0x1.62e430p-1f;
+constexpr float kLog2eF = 0x1.715476p+0f;
+inline float log2_def(float x) {
+    int e = 0;
+    if (x < 0x1p-126f) { x = x * 0x1p23f; e = -23; }
+    const uint32_t b = f2u(x);
+    e += static_cast<int>((b >> 23) & 0xFFu) - 127;
+    float m = u2f((b & 0x7FFFFFu) | 0x3F800000u);
+    if (m > 0x1.6a09e6p+0f) { m = m * 0.5f; e += 1; }
+    const float s = (m - 1.0f) / (m + 1.0f);
+    const float s2 = s * s;
+    float p = 1.0f / 11.0f;
+    p = fma_(p, s2, 1.0f / 9.0f);
+    p = fma_(p, s2, 1.0f / 7.0f);
+    p = fma_(p, s2, 1.0f / 5.0f);
+    p = fma_(p, s2, 1.0f / 3.0f);
+    const float lnm = 2.0f * fma_(s2 * s, p, s);
+    return fma_(lnm, kLog2eF, static_cast<float>(e));
+}
+inline float exp2_def(float y) {
+    if (!(y >= -126.0f)) return y != y ? y : 0.0f;
+    if (y > 127.0f) return INFINITY;
+    const float n = std::rint(y);
+    const float z = (y - n) * kLn2F;
+    float p = 1.0f / 362880.0f;
+    p = fma_(p, z, 1.0f / 40320.0f);
+    p = fma_(p, z, 1.0f / 5040.0f);
+    p = fma_(p, z, 1.0f / 720.0f);
+    p = fma_(p, z, 1.0f / 120.0f);
+    p = fma_(p, z, 1.0f / 24.0f);
+    p = fma_(p, z, 1.0f / 6.0f);
+    p = fma_(p, z, 0.5f);
+    p = fma_(p, z, 1.0f);
+    p = fma_(p, z, 1.0f);
+    return p * u2f(static_cast<uint32_t>(static_cast<int>(n) + 127) << 23);
+}
+inline float pow_def(float x, float y) {
+    if (y == 5.0f) return pow5(x);
+    if (x == 0.0f) return y > 0.0f ? 0.0f : (y == 0.0f ? 1.0f : INFINITY);
+    if (x == 1.0f || y == 0.0f) return 1.0f;
+    if (!(x > 0.0f)) return NAN;
+    return exp2_def(y * log2_def(x));
+}
+
 // ---- Real-dispatched scalar functions ----
 inline float m_sin(float x) { return sin_f(x); }
 inline float m_cos(float x) { return cos_f(x); }
@@ -119,9 +174,9 @@ inline double m_atan2(double y, double x) { return std::atan2(y, x); }
 inline double m_asin(double x) { return std::asin(x); }
 inline double m_acos(double x) { return std::acos(x); }
 inline double m_sqrt(double x) { return std::sqrt(x); }
+inline float m_pow(float x, float y) { return pow_def(x, y); }
+inline double m_pow(double x, double y) { return y == 5.0 ? (x * x) * (x * x) * x : std::pow(x, y); }
 
-// GLSL pow(x, 5.0) as used by the Schlick terms: ((x*x)*(x*x))*x.
-template <class T> inline T pow5(T x) { T x2 = x * x; T x4 = x2 * x2; return x4 * x; }
 // GLSL min/max/clamp (IEEE fmin/fmax semantics for non-NaN inputs).
 template <class T> inline T gmax(T a, T b) { return a > b ? a : b; }
 template <class T> inline T gmin(T a, T b) { return a < b ? a : b; }

@@ -35,6 +35,7 @@ namespace orc {
 constexpr uint32_t kFlagFireflyClamp = 1u << 2;   // pt_raygen.rgen:58
 constexpr uint32_t kFlagEnvFixedV = 1u << 8;      // "fixed" env lookup mode (not reference)
 constexpr uint32_t kFlagVndf = 1u << 9;           // VNDF stage-B sampling (pt_raygen_realtime.rgen:723-800)
+constexpr uint32_t kFlagAlphaTest = 1u << 10;     // rays without gl_RayFlagsOpaqueEXT (pt_anyhit.rahit runs)
 constexpr uint32_t kSamplerPCG = 0, kSamplerSobol = 1;
 constexpr uint32_t kNoTex = 0xFFFFFFFFu;
 
@@ -53,6 +54,7 @@ struct Instance {
 
 struct Blas {
     uint32_t first_index = 0, index_count = 0;
+    bool no_opaque = false;   // OHAO_BLAS_FLAG_NO_OPAQUE: takes the alpha test
     WideBVH bvh;
     std::vector<TriRec> tris;
     Box box = box_empty();
@@ -127,6 +129,55 @@ struct Scene {
     // tile albedo map (texture slot 0)
     std::vector<float> albedo_map;  // w*h*3
     uint32_t map_w = 0, map_h = 0;
+    // bindless textures: RGBA8 UNORM texels back to back, per texture (first texel, w, h)
+    std::vector<uint8_t> tex_texels;
+    struct TexInfo { size_t off; int w, h; };
+    std::vector<TexInfo> tex_info;
+
+    // Texel c read as c / 255, sampled LINEAR / REPEAT at LOD 0 with texel
+    // centres at (i + 0.5) / size; the four channels in float.
+    void tex_sample(uint32_t idx, float u, float v, float out[4]) const {
+        const TexInfo& ti = tex_info[idx];
+        const int W = ti.w, H = ti.h;
+        const float x = u * float(W) - 0.5f;
+        const float y = v * float(H) - 0.5f;
+        const float fx0 = std::floor(x), fy0 = std::floor(y);
+        const float fx = x - fx0, fy = y - fy0;
+        auto wrap = [](long long i, int n) { long long m = i % n; return static_cast<int>(m < 0 ? m + n : m); };
+        const long long ix = static_cast<long long>(fx0), iy = static_cast<long long>(fy0);
+        const int x0 = wrap(ix, W), x1 = wrap(ix + 1, W), y0 = wrap(iy, H), y1 = wrap(iy + 1, H);
+        auto tx = [&](int xx, int yy, int c) {
+            return float(tex_texels[ti.off * 4 + (static_cast<size_t>(yy) * W + xx) * 4 + c]) / 255.0f;
+        };
+        for (int c = 0; c < 4; ++c) {
+            const float top = tx(x0, y0, c) * (1.0f - fx) + tx(x1, y0, c) * fx;
+            const float bot = tx(x0, y1, c) * (1.0f - fx) + tx(x1, y1, c) * fx;
+            out[c] = top * (1.0f - fy) + bot * fy;
+        }
+    }
+
+    // pt_anyhit.rahit:17-50 for a candidate hit of a non-opaque ray: false
+    // (ignore) when the instance's BLAS is non-opaque and the material's
+    // diffuse texture has alpha < 0.5 at the hit's UV.
+    bool alpha_accept(uint32_t inst, uint32_t prim, float u, float v) const {
+        const Instance& in = instances[inst];
+        if (!blases[in.blas].no_opaque) return true;
+        const uint32_t gtri = (in.custom & 0xFFFFFFu) + prim;
+        const uint32_t mid = mat_ids[gtri];
+        const uint32_t dtex = f2u(mats[static_cast<size_t>(mid) * 12 + 3]);
+        if (dtex == kNoTex || (dtex == 0u && map_w > 0)) return true;
+        const uint32_t i0 = indices[gtri * 3 + 0], i1 = indices[gtri * 3 + 1], i2 = indices[gtri * 3 + 2];
+        const float w = 1.0f - u - v;
+        const float tu = w * uvs[2 * i0] + u * uvs[2 * i1] + v * uvs[2 * i2];
+        const float tv = w * uvs[2 * i0 + 1] + u * uvs[2 * i1 + 1] + v * uvs[2 * i2 + 1];
+        float c[4];
+        tex_sample(dtex, tu, tv, c);
+        return !(c[3] < 0.5f);
+    }
+    static bool alpha_accept_cb(const void* self, uint32_t inst, uint32_t prim, float u, float v) {
+        return static_cast<const Scene*>(self)->alpha_accept(inst, prim, u, v);
+    }
+    HitFilter alpha_filter() const { return HitFilter{this, &Scene::alpha_accept_cb}; }
     // acceleration structure
     std::vector<Instance> instances;
     std::vector<Blas> blases;
@@ -243,13 +294,17 @@ struct Scene {
     }
 
     // traceRayEXT(gl_RayFlagsOpaqueEXT) closest hit.
-    HitRec closest(const float o[3], const float d[3], float tmin, float tmax, TravStats* st = nullptr) const {
+    // alpha: a ray without gl_RayFlagsOpaqueEXT (the alpha test applies).
+    HitRec closest(const float o[3], const float d[3], float tmin, float tmax, TravStats* st = nullptr,
+                   bool alpha = false) const {
         HitRec best;
         if (!(tmax > tmin)) return best;
+        const HitFilter af = alpha_filter();
+        const HitFilter* filter = alpha ? &af : nullptr;
         if (!two_level) {
             RayPre r = ray_pre(o, d);
             BvhView v{flat.nodes.data(), flat_tris.data(), static_cast<uint32_t>(flat.nodes.size())};
-            bvh_closest(v, r, tmin, tmax, best, 0xFFFFFFFFu, st);
+            bvh_closest(v, r, tmin, tmax, best, 0xFFFFFFFFu, st, filter);
             return best;
         }
         RayPre r = ray_pre(o, d);
@@ -276,7 +331,7 @@ struct Scene {
                     affine_xform_dir(in.w2o, d, od);
                     RayPre ro = ray_pre(oo, od);
                     BvhView v{bl.bvh.nodes.data(), bl.tris.data(), static_cast<uint32_t>(bl.bvh.nodes.size())};
-                    bvh_closest(v, ro, tmin, tmax, best, ii, st);
+                    bvh_closest(v, ro, tmin, tmax, best, ii, st, filter);
                 }
             }
             uint32_t ids[8]; float tns[8]; int cnt = 0;
@@ -294,12 +349,15 @@ struct Scene {
     }
 
     // traceRayEXT(TerminateOnFirstHit|Opaque|SkipClosestHit): occluded?
-    bool occluded(const float o[3], const float d[3], float tmin, float tmax, TravStats* st = nullptr) const {
+    bool occluded(const float o[3], const float d[3], float tmin, float tmax, TravStats* st = nullptr,
+                  bool alpha = false) const {
         if (!(tmax > tmin)) return false;
         RayPre r = ray_pre(o, d);
+        const HitFilter af = alpha_filter();
+        const HitFilter* filter = alpha ? &af : nullptr;
         if (!two_level) {
             BvhView v{flat.nodes.data(), flat_tris.data(), static_cast<uint32_t>(flat.nodes.size())};
-            return bvh_any(v, r, tmin, tmax, st);
+            return bvh_any(v, r, tmin, tmax, st, filter);
         }
         if (tlas.nodes.empty()) return false;
         std::vector<uint32_t> stack{0u};
@@ -323,7 +381,7 @@ struct Scene {
                     affine_xform_dir(in.w2o, d, od);
                     RayPre ro = ray_pre(oo, od);
                     BvhView v{bl.bvh.nodes.data(), bl.tris.data(), static_cast<uint32_t>(bl.bvh.nodes.size())};
-                    if (bvh_any(v, ro, tmin, tmax, st)) return true;
+                    if (bvh_any(v, ro, tmin, tmax, st, filter, ii)) return true;
                 }
             }
         }
@@ -331,7 +389,7 @@ struct Scene {
     }
 
     // Brute-force ground truth over every visible instance triangle.
-    HitRec closest_brute(const float o[3], const float d[3], float tmin, float tmax) const {
+    HitRec closest_brute(const float o[3], const float d[3], float tmin, float tmax, bool alpha = false) const {
         HitRec best;
         if (!(tmax > tmin)) return best;
         for (uint32_t ii = 0; ii < instances.size(); ++ii) {
@@ -356,6 +414,7 @@ struct Scene {
                 bool h = obj ? tri_intersect(r, v[0], v[1], v[2], tmin, tmax, t, u, vv)
                              : tri_intersect(r, w[0], w[1], w[2], tmin, tmax, t, u, vv);
                 if (!h) continue;
+                if (alpha && !alpha_accept(ii, p, u, vv)) continue;
                 if (!best.hit() || t < best.t || (t == best.t && key_less(ii, p, best.inst, best.prim))) {
                     best.t = t; best.u = u; best.v = vv; best.inst = ii; best.prim = p;
                 }
@@ -603,14 +662,62 @@ struct PathTracer {
         uint32_t mid = sc.mat_ids[gtri];
         s.matid = mid;
         const float* m = &sc.mats[static_cast<size_t>(mid) * 12];
+        const uint32_t diffTex = f2u(m[3]), normTex = f2u(m[6]), emisTex = f2u(m[7]), rmTex = f2u(m[8]);
+        // bindless texture sample at the hit's UV (texture coordinates in float)
+        auto tex = [&](uint32_t idx, R out[4]) {
+            float c[4];
+            sc.tex_sample(idx, static_cast<float>(tu), static_cast<float>(tv), c);
+            for (int k = 0; k < 4; ++k) out[k] = R(c[k]);
+        };
+        // albedo x sRGB-decoded diffuse texture (pt_closesthit.rchit:108-113);
+        // diffuse index 0 = the tile albedo map when one is set
         V3<R> alb{R(m[0]), R(m[1]), R(m[2])};
-        uint32_t diffTex = f2u(m[3]);
-        if (diffTex == 0u && sc.map_w > 0) alb = alb * albedo_map_sample(tu, tv);
+        if (diffTex != kNoTex) {
+            if (diffTex == 0u && sc.map_w > 0) {
+                alb = alb * albedo_map_sample(tu, tv);
+            } else {
+                R c[4];
+                tex(diffTex, c);
+                alb = alb * V3<R>(m_pow(c[0], R(2.2f)), m_pow(c[1], R(2.2f)), m_pow(c[2], R(2.2f)));
+            }
+        }
+        // normal map in the Frisvad basis (pt_closesthit.rchit:116-133)
+        if (normTex != kNoTex) {
+            R c[4];
+            tex(normTex, c);
+            V3<R> mapN = normalize(V3<R>(c[0] * R(2) - R(1), c[1] * R(2) - R(1), c[2] * R(2) - R(1)));
+            V3<R> T, B;
+            if (wn.z < R(-0.9999f)) {
+                T = V3<R>(R(0), R(-1), R(0));
+                B = V3<R>(R(-1), R(0), R(0));
+            } else {
+                R a = R(1) / (R(1) + wn.z);
+                R dd = -wn.x * wn.y * a;
+                T = V3<R>(R(1) - wn.x * wn.x * a, dd, -wn.x);
+                B = V3<R>(dd, R(1) - wn.y * wn.y * a, -wn.y);
+            }
+            wn = normalize(T * mapN.x + B * mapN.y + wn * mapN.z);
+        }
         s.N = wn;
         s.albedo = alb;
+        // roughness / metallic x ORM texture G / B (pt_closesthit.rchit:139-148)
         R rough = R(m[4]), metal = R(m[5]);
+        if (rmTex != kNoTex) {
+            R c[4];
+            tex(rmTex, c);
+            rough = rough * c[1];
+            metal = metal * c[2];
+        }
         rough = gmax(rough, R(0.04f));
-        s.color = V3<R>(R(m[9]), R(m[10]), R(m[11]));
+        // sRGB-decoded emissive texture (pt_closesthit.rchit:150-156) plus the
+        // slot-2 emission of this ABI
+        V3<R> emis(R(0));
+        if (emisTex != kNoTex) {
+            R c[4];
+            tex(emisTex, c);
+            emis = V3<R>(m_pow(c[0], R(2.2f)), m_pow(c[1], R(2.2f)), m_pow(c[2], R(2.2f)));
+        }
+        s.color = emis + V3<R>(R(m[9]), R(m[10]), R(m[11]));
         // payload.attenuation = (roughness, clamp(metallic,0,1), curv) then
         // unpackHitPbr
         R rr, mm;
@@ -629,14 +736,14 @@ struct PathTracer {
 
     void trace(V3<R> o, V3<R> d, Surf<R>& s, TravStats* ts) const {
         float of[3] = {float(o.x), float(o.y), float(o.z)}, df[3] = {float(d.x), float(d.y), float(d.z)};
-        HitRec h = sc.closest(of, df, 0.001f, 10000.0f, ts);
+        HitRec h = sc.closest(of, df, 0.001f, 10000.0f, ts, (st.flags & kFlagAlphaTest) != 0u);
         if (h.hit()) closest_hit(of, df, h, s);
         else miss(d, s);
     }
     // Shadow query; on a miss the miss shader runs (payload.color = env).
     bool shadow(V3<R> o, V3<R> d, R tmax, Surf<R>& s, TravStats* ts) const {
         float of[3] = {float(o.x), float(o.y), float(o.z)}, df[3] = {float(d.x), float(d.y), float(d.z)};
-        bool occ = sc.occluded(of, df, 0.001f, float(tmax), ts);
+        bool occ = sc.occluded(of, df, 0.001f, float(tmax), ts, (st.flags & kFlagAlphaTest) != 0u);
         if (!occ) miss(d, s);
         return !occ;
     }

@@ -53,6 +53,8 @@ def lib():
         L.orc_scene_set_lights.argtypes = [vp, vp, u32]
         L.orc_scene_set_env.argtypes = [vp, vp, u32, u32, vp, vp, f32, f32]
         L.orc_scene_set_albedo_map.argtypes = [vp, vp, u32, u32]
+        L.orc_scene_set_textures.argtypes = [vp, vp, vp, u32]
+        L.orc_scene_set_blas_flags.argtypes = [vp, u32, u32]
         L.orc_scene_add_blas.argtypes = [vp, u32, u32]
         L.orc_scene_add_blas.restype = u32
         L.orc_scene_set_instances.argtypes = [vp, vp, u32]
@@ -76,6 +78,7 @@ def lib():
         L.orc_math.argtypes = [i32, vp, u32, vp]
         L.orc_num_threads.restype = i32
         L.orc_display_rgba8.argtypes = [vp, u64, vp]
+        L.orc_pow_def.argtypes = [vp, u64, f32, vp]
         L.orc_glsl_helper.argtypes = [i32, vp, u32, vp]
         L.orc_glsl_helper.restype = i32
         L.orc_glsl_env.argtypes = [i32, vp, vp, u32, u32, vp, u32, vp]
@@ -197,8 +200,16 @@ class OracleScene:
                                 sd.env_intensity)
         if sd.albedo_map is not None:
             self.set_albedo_map(sd.albedo_map)
-        for fi, ic in sd.blas:
+        if getattr(sd, "textures", None):
+            texels = np.ascontiguousarray(np.concatenate([np.asarray(t, np.uint8).reshape(-1) for t in sd.textures]))
+            sizes = np.array([[t.shape[1], t.shape[0]] for t in sd.textures], np.uint32)
+            self._keep.append(texels)
+            L.orc_scene_set_textures(self.h, _p(texels), _p(sizes), len(sd.textures))
+        for k, (fi, ic) in enumerate(sd.blas):
             L.orc_scene_add_blas(self.h, fi, ic)
+            flags = getattr(sd, "blas_flags", None)
+            if flags:
+                L.orc_scene_set_blas_flags(self.h, k, int(flags[k]))
         inst = np.ascontiguousarray(sd.instances)
         L.orc_scene_set_instances(self.h, _p(inst), inst.size)
         L.orc_scene_build(self.h, flatten_limit, force_mode)
@@ -226,7 +237,10 @@ class OracleScene:
         lib().orc_bvh_copy(self.h, which, _p(nodes), _p(prims))
         return nodes, prims, hh.value
 
-    def trace(self, rays: np.ndarray, mode: int = 0, stats: bool = False, nthreads: int = 0):
+    def trace(self, rays: np.ndarray, mode: int = 0, stats: bool = False, nthreads: int = 0, alpha: bool = False):
+        """mode 0 closest hit, 1 any hit, 2 brute-force closest hit; alpha:
+        non-opaque rays (the any-hit alpha test)."""
+        mode = mode | (4 if alpha else 0)
         rays = np.ascontiguousarray(rays, np.float32)
         n = rays.shape[0]
         hits = np.zeros((n, 5), np.uint32)
@@ -287,6 +301,14 @@ class OracleScene:
         if rc != 0:
             raise ValueError("detached_grad: too many parameters")
         return out
+
+
+def pow_def(x: np.ndarray, y: float) -> np.ndarray:
+    """The pow(x, y) definition that the oracle and the kernels share."""
+    a = np.ascontiguousarray(x, np.float32)
+    out = np.zeros_like(a)
+    lib().orc_pow_def(_p(a), a.size, float(y), _p(out))
+    return out
 
 
 def display_rgba8(rgba: np.ndarray) -> np.ndarray:

@@ -235,3 +235,30 @@ def test_zero_scale_instance_equals_masked(oracle, flatten_limit):
     assert np.all(np.isfinite(ha[:, 0].view(np.float32)))
     assert np.array_equal(a.render_paths(sd.views[0], dict(max_bounces=3), 0, 1),
                           b.render_paths(m.views[0], dict(max_bounces=3), 0, 1))
+
+
+def test_pow_definition_accuracy(oracle):
+    """The pow shared by the oracle and the kernels (exp2(y log2 x), both
+    defined from their series) against float64 pow: within 1e-5 relative
+    (float exp2 of a float exponent of magnitude up to ~44 here; GLSL allows
+    pow the error of exp2(y * log2(x)), several ulp)."""
+    import ctypes as C
+    rng = np.random.default_rng(8)
+    x = np.exp(rng.uniform(np.log(1e-6), 0.0, 200000)).astype(np.float32)
+    for y in (2.2, 1.0 / 2.2, 0.7, 3.0):
+        got = oracle.pow_def(x, np.float32(y))
+        ref = x.astype(np.float64) ** np.float64(np.float32(y))
+        rel = np.abs(got - ref) / ref
+        assert rel.max() < 1e-5, (y, rel.max())
+    assert oracle.pow_def(np.array([0.0, 1.0], np.float32), np.float32(2.2)).tolist() == [0.0, 1.0]
+
+
+def test_alpha_test_bvh_equals_brute_force(oracle):
+    sd = scenes.textured()
+    for fl in (1 << 25, 1):
+        orc = oracle.OracleScene(sd, flatten_limit=fl)
+        rng = np.random.default_rng(5)
+        rays = random_rays(rng, 6000, -1.5, 1.5)
+        for alpha in (False, True):
+            assert np.array_equal(orc.trace(rays, 0, alpha=alpha), orc.trace(rays, 2, alpha=alpha))
+        assert not np.array_equal(orc.trace(rays, 0), orc.trace(rays, 0, alpha=True))
