@@ -11,9 +11,10 @@ literals are single precision). Two libraries come out of it:
   heuristic, GGX D / Smith / VNDF sampling, metal-rough unpack, environment
   CDF search and pdf) behind ``glsl_ref_api.inc``;
 * ``oracle/_ref/libohao_glslpt[_offline].so``: a raygen (the default one or
-  the offline profile's) with the closest-hit and miss shaders and every
-  file they include, behind ``glsl_pt_api.inc``; ``traceRayEXT`` runs the
-  oracle's traversal (``glsl_pt_host.cpp``).
+  the offline profile's) with the closest-hit, miss and any-hit (alpha test)
+  shaders and every file they include, behind ``glsl_pt_api.inc``;
+  ``traceRayEXT`` runs the oracle's traversal (``glsl_pt_host.cpp``); the
+  any-hit shader is driven on its own for candidate hits.
 
 The text changes are mechanical and listed in ``shader_text``: GLSL's
 ``out`` / ``inout T name`` parameters written as C++ references ``T& name``
@@ -136,7 +137,8 @@ def env_records(fn: int, n: int, rng, w: int, h: int):
 # profile's (the same estimator with its analytic-light products regrouped
 # and optional subsurface terms, off unless push constant tuning.w > 0)
 PT_RAYGENS = {"base": "shaders/rt/pt_raygen.rgen", "offline": "shaders/rt/pt_raygen_offline.rgen"}
-PT_HIT_MISS = [("rchit", "shaders/rt/pt_closesthit.rchit"), ("rmiss", "shaders/rt/pt_miss.rmiss")]
+PT_HIT_MISS = [("rchit", "shaders/rt/pt_closesthit.rchit"), ("rmiss", "shaders/rt/pt_miss.rmiss"),
+               ("rahit", "shaders/rt/pt_anyhit.rahit")]
 
 
 def pt_lib_path(variant: str = "base") -> str:

@@ -41,6 +41,10 @@ typedef struct GptScene {
     int32_t has_cdf;
     const void* trace_ctx;
     GptTraceFn trace;
+    // bindless textures as RGBA32F texels (the UNORM8 texels c / 255)
+    const float* const* tex_rgba;
+    const uint32_t* tex_sizes;   // (width, height) per texture
+    uint32_t ntex;
 } GptScene;
 
 typedef struct GptCamera {
@@ -58,6 +62,11 @@ typedef struct GptSettings {
 // path's radiance, count 1).
 void gpt_shade_pixel(const GptScene* scene, const GptCamera* cam, const GptSettings* st, uint32_t px, uint32_t py,
                      uint32_t sample, float rgba[4]);
+
+// The any-hit shader on one candidate hit (instance custom index, primitive
+// index, barycentrics): 1 when it accepts the hit, 0 when it executes
+// ignoreIntersectionEXT.
+int32_t gpt_anyhit_accept(const GptScene* scene, int32_t custom_index, int32_t primitive, float u, float v);
 
 #ifdef __cplusplus
 }

@@ -22,6 +22,10 @@ inline float gl_HitTEXT;
 inline int gl_InstanceCustomIndexEXT, gl_PrimitiveID;
 inline mat4x3 gl_ObjectToWorldEXT;
 
+// ignoreIntersectionEXT (an any-hit shader's jump statement): the pin driver
+// reads the flag after the any-hit shader returns.
+inline bool gl_IgnoreIntersection = false;
+
 // Defined by the pin driver: traverses the oracle's BVH and runs the
 // closest-hit or miss shader on the caller's payload (location 0).
 void traceRayEXT(const accelerationStructureEXT& as, uint flags, uint mask, uint sbt_offset, uint sbt_stride,
@@ -38,3 +42,8 @@ void traceRayEXT(const accelerationStructureEXT& as, uint flags, uint mask, uint
 #define rayPayloadEXT
 #define rayPayloadInEXT
 #define hitAttributeEXT
+#define ignoreIntersectionEXT          \
+    {                                  \
+        glsl::gl_IgnoreIntersection = true; \
+        return;                        \
+    }

@@ -320,10 +320,10 @@ inline float smoothstep(float e0, float e1, float x) {
     const float t = clamp((x - e0) / (e1 - e0), 0.0f, 1.0f);
     return t * t * (3.0f - 2.0f * t);
 }
-inline float pow(float x, float y) {
-    if (y == 5.0f) return orc::pow5(x);
-    return std::pow(x, y);
-}
+// GLSL leaves pow's precision to exp2(y * log2(x)) of the implementation:
+// the oracle's definition (pow5 for the Schlick exponent, else exp2 / log2
+// from their series).
+inline float pow(float x, float y) { return orc::pow_def(x, y); }
 inline vec3 pow(const vec3& x, const vec3& y) { return {pow(x.x, y.x), pow(x.y, y.y), pow(x.z, y.z)}; }
 inline vec3 reflect(const vec3& i, const vec3& n) { float d = 2.0f * dot(n, i); return i - n * d; }
 inline float radians(float deg) { return deg * 0.017453292f; }
@@ -372,7 +372,10 @@ inline vec4 texture(const sampler2D& s, const vec2& uv) {
     };
     const vec3 top = tex(x0, y0) * (1.0f - fx) + tex(x1, y0) * fx;
     const vec3 bot = tex(x0, y1) * (1.0f - fx) + tex(x1, y1) * fx;
-    return vec4(top * (1.0f - fy) + bot * fy, 1.0f);
+    auto alpha = [&](int xx, int yy) { return s.rgba[(static_cast<size_t>(yy) * W + xx) * 4 + 3]; };
+    const float atop = alpha(x0, y0) * (1.0f - fx) + alpha(x1, y0) * fx;
+    const float abot = alpha(x0, y1) * (1.0f - fx) + alpha(x1, y1) * fx;
+    return vec4(top * (1.0f - fy) + bot * fy, atop * (1.0f - fy) + abot * fy);
 }
 
 }  // namespace glsl

@@ -96,6 +96,11 @@ void orc_scene_set_textures(Scene* s, const uint8_t* texels, const uint32_t* siz
     }
     s->tex_texels.assign(texels, texels + off * 4);
 }
+// pt_anyhit.rahit's alpha test on n candidate hits (instance, primitive, u, v)
+void orc_alpha_accept(const Scene* s, const uint32_t* inst, const uint32_t* prim, const float* uv, uint32_t n,
+                      uint32_t* out) {
+    for (uint32_t i = 0; i < n; ++i) out[i] = s->alpha_accept(inst[i], prim[i], uv[2 * i], uv[2 * i + 1]) ? 1u : 0u;
+}
 void orc_scene_set_blas_flags(Scene* s, uint32_t blas, uint32_t flags) { s->blases[blas].no_opaque = (flags & 1u) != 0; }
 uint32_t orc_scene_add_blas(Scene* s, uint32_t first_index, uint32_t index_count) {
     Blas b;

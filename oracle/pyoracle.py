@@ -55,6 +55,7 @@ def lib():
         L.orc_scene_set_albedo_map.argtypes = [vp, vp, u32, u32]
         L.orc_scene_set_textures.argtypes = [vp, vp, vp, u32]
         L.orc_scene_set_blas_flags.argtypes = [vp, u32, u32]
+        L.orc_alpha_accept.argtypes = [vp, vp, vp, vp, u32, vp]
         L.orc_scene_add_blas.argtypes = [vp, u32, u32]
         L.orc_scene_add_blas.restype = u32
         L.orc_scene_set_instances.argtypes = [vp, vp, u32]
@@ -126,6 +127,7 @@ def glsl_pt_lib(variant: str = "base"):
     L = C.CDLL(path)
     vp, u32 = C.c_void_p, C.c_uint32
     L.gpt_render_paths.argtypes = [vp, vp, vp, u32, u32, vp, u32, u32, vp, u32, vp]
+    L.gpt_anyhit.argtypes = [vp, vp, vp, vp, u32, vp]
     return L
 
 
@@ -141,6 +143,17 @@ def shader_paths(glsl_lib_, scene: "OracleScene", view, settings: dict, sample_b
     out = np.zeros((spp, npix, 3), np.float32)
     glsl_lib_.gpt_render_paths(scene.h, _p(view.inv_view), _p(view.inv_proj), view.width, view.height, _p(st),
                                sample_base, spp, _p(pix), npix, _p(out))
+    return out
+
+
+def shader_anyhit(glsl_pt_lib_, scene: "OracleScene", inst, prim, uv) -> np.ndarray:
+    """The reference's any-hit shader (pt_anyhit.rahit, compiled as C++) on
+    candidate hits: 1 accepted, 0 ignored."""
+    inst = np.ascontiguousarray(inst, np.uint32)
+    prim = np.ascontiguousarray(prim, np.uint32)
+    uv = np.ascontiguousarray(uv, np.float32)
+    out = np.zeros(inst.size, np.uint32)
+    glsl_pt_lib_.gpt_anyhit(scene.h, _p(inst), _p(prim), _p(uv), inst.size, _p(out))
     return out
 
 
@@ -247,6 +260,15 @@ class OracleScene:
         st = np.zeros((n, 2), np.uint32) if stats else None
         lib().orc_trace(self.h, _p(rays), n, _p(hits), mode, _p(st), nthreads)
         return (hits, st) if stats else hits
+
+    def alpha_accept(self, inst, prim, uv) -> np.ndarray:
+        """The oracle's any-hit alpha test on candidate hits (uint32 0/1)."""
+        inst = np.ascontiguousarray(inst, np.uint32)
+        prim = np.ascontiguousarray(prim, np.uint32)
+        uv = np.ascontiguousarray(uv, np.float32)
+        out = np.zeros(inst.size, np.uint32)
+        lib().orc_alpha_accept(self.h, _p(inst), _p(prim), _p(uv), inst.size, _p(out))
+        return out
 
     def render_paths(self, view, settings: dict, sample_base: int, spp: int, pixels=None, fp64=False,
                      nthreads: int = 0, stats: bool = False):

@@ -5,7 +5,9 @@ reference tree (oracle/glsl_pin.py) and records their outputs on seeded
 inputs: 64 records per helper, the environment-CDF functions over the CDFs
 of a seeded 32x16 map, and the per-path radiance of the raygen, closest-hit
 and miss shaders (traced through the oracle's BVH) on the seeded scenes of
-tests/pin_cases.py, 96 pixels of the first view each. Run in a container
+tests/pin_cases.py, 96 pixels of the first view each, and the any-hit
+shader's accept / ignore decision on 2,048 seeded candidate hits of the
+textured scene. Run in a container
 that has the reference checkout:
 
     python tests/golden/make_glsl_golden.py
@@ -30,6 +32,19 @@ ENV_W, ENV_H = 32, 16
 
 def bits(a):
     return np.ascontiguousarray(a, np.float32).view(np.uint32).reshape(-1).tolist()
+
+
+def anyhit_candidates(n=2048, seed=77):
+    """Seeded candidate hits (instance, primitive, barycentrics) of the
+    textured pin scene: three quarters on the alpha-tested leaves (instance
+    1, 10 triangles), the rest on the opaque geometry (instance 0)."""
+    rng = np.random.default_rng(seed)
+    inst = (rng.random(n) < 0.75).astype(np.uint32)
+    prim = np.where(inst == 1, rng.integers(0, 10, n), rng.integers(0, 2884, n)).astype(np.uint32)
+    uv = rng.random((n, 2))
+    flip = uv.sum(1) > 1.0
+    uv[flip] = 1.0 - uv[flip]
+    return inst, prim, np.ascontiguousarray(uv, np.float32)
 
 
 def main():
@@ -66,6 +81,14 @@ def main():
             pix = pix.astype(np.uint32)
             y = pyoracle.shader_paths(P, scene, v, settings, pin_cases.SAMPLE_BASE, pin_cases.SPP, pix)
             out[key][name] = {"pixels": pix.tolist(), "out_bits": bits(y)}
+    # the any-hit shader (alpha test) on candidate hits of the textured scene's
+    # non-opaque leaves and its opaque geometry
+    import pin_cases
+    P = pyoracle.glsl_pt_lib("base")
+    inst, prim, uv = anyhit_candidates()
+    scene = pyoracle.OracleScene(pin_cases.CASES["textured_pcg"][0]())
+    out["anyhit"] = {"inst": inst.tolist(), "prim": prim.tolist(), "uv_bits": bits(uv),
+                     "accept": pyoracle.shader_anyhit(P, scene, inst, prim, uv).tolist()}
     path = os.path.join(HERE, "glsl_kats.json")
     with open(path, "w") as f:
         json.dump(out, f)

@@ -1,9 +1,12 @@
 """Seeded scenes and settings on which the oracle's integrator is compared
 with the reference's own path-tracing shaders (raygen, closest hit, miss)
 compiled as C++ (oracle/glsl_pin.py). The reference shades emission only
-from emissive textures, which the C ABI does not take, so these scenes carry
-no emissive materials; light comes from the environment and from analytic
-lights of all four GPULight types."""
+from emissive textures, so these scenes carry no slot-2 emission; light
+comes from the environment, from analytic lights of all four GPULight types
+and, in the textured scene, from an emissive texture. Its bindless diffuse,
+normal, roughness-metal and emissive textures go through the reference's
+closest-hit shader; the reference traces every ray opaque, so the alpha
+test is pinned on its own (pt_anyhit.rahit, tests/test_oracle_pins.py)."""
 from __future__ import annotations
 
 import numpy as np
@@ -68,6 +71,8 @@ CASES = {
     "cornell_4_types_sobol": (lambda: _cornell_lit(4), dict(max_bounces=3, sampler=1), 1 << 25),
     "instanced_two_level": (_instanced, dict(max_bounces=4, sampler=0), 1000),
     "sphere_1m_1080p": (_bench_sphere, dict(max_bounces=4, sampler=0), 1 << 25),
+    "textured_pcg": (lambda: scenes.textured(), dict(max_bounces=4, sampler=0), 1 << 25),
+    "textured_sobol_two_level": (lambda: scenes.textured(), dict(max_bounces=3, sampler=1), 1),
 }
 LIVE_PIXELS = 4096   # live comparisons sample at most this many pixels of a view
 SAMPLE_BASE, SPP = 3, 2

@@ -178,6 +178,7 @@ def test_aov_first_hit(gpu_lib, oracle):
 
 
 def test_errors_are_status_codes(gpu_lib):
+    import torch
     og = gpu_lib
     pt = og.PathTracer()
     sd = scenes.cornell(8, 8, 1)
@@ -188,16 +189,27 @@ def test_errors_are_status_codes(gpu_lib):
     with pytest.raises(og.OhaoError):
         pt.create_blas(0, 10 ** 6)
     bad = sd.materials.copy()
-    bad[0, 6:7] = np.array([3], np.uint32).view(np.float32)
+    bad[0, 6:7] = np.array([70000], np.uint32).view(np.float32)   # beyond the 65536 texture slots
     with pytest.raises(og.OhaoError) as e:
         pt.set_materials(bad)
-    assert e.value.status == -6
+    assert e.value.status == -1
     pt.set_materials(sd.materials)
     with pytest.raises(og.OhaoError) as e:
         pt.update_materials(bad[:1])
-    assert e.value.status == -6
+    assert e.value.status == -1
     with pytest.raises(og.OhaoError) as e:
         pt.update_materials(sd.materials[:1], first=sd.materials.shape[0])
+    assert e.value.status == -1
+    # a texture index that names no texture: accepted in the table, refused by a render
+    missing = sd.materials.copy()
+    missing[0, 6:7] = np.array([3], np.uint32).view(np.float32)
+    pt.set_materials(missing)
+    for fi, ic in sd.blas:
+        pt.create_blas(fi, ic)
+    pt.set_instances(sd.instances)
+    pt.build()
+    with pytest.raises(og.OhaoError) as e:
+        pt.render([og.make_view(sd.views[0], accum=torch.zeros((64, 4), device="cuda"))], og.make_settings())
     assert e.value.status == -1
 
 

@@ -241,6 +241,44 @@ def test_integrator_matches_reference_shaders_live(oracle):
             assert not bad.any(), f"{name}: {bad.sum()} of {bad.size} paths differ from the reference shaders"
 
 
+def test_alpha_test_matches_reference_anyhit_golden(oracle):
+    """The oracle's alpha test (and so the kernels', which equal it on the
+    GPU) against the recorded decisions of the reference's any-hit shader
+    (pt_anyhit.rahit compiled as C++) on candidate hits of the textured pin
+    scene; some hits are ignored, some accepted."""
+    import pin_cases
+    rec = GLSL_KATS["anyhit"]
+    inst, prim = _u32(rec["inst"]), _u32(rec["prim"])
+    uv = _u32(rec["uv_bits"]).view(np.float32).reshape(-1, 2)
+    scene = oracle.OracleScene(pin_cases.CASES["textured_pcg"][0]())
+    got = scene.alpha_accept(inst, prim, uv)
+    want = np.asarray(rec["accept"], np.uint32)
+    assert np.array_equal(got, want)
+    leaves = inst == 1
+    assert 0.1 < want[leaves].mean() < 0.9 and want[~leaves].all()
+
+
+def test_alpha_test_matches_reference_anyhit_live(oracle):
+    import glsl_pin
+    import pin_cases
+    P = oracle.glsl_pt_lib()
+    if P is None and glsl_pin.pt_available():
+        glsl_pin.build_pt()
+        P = oracle.glsl_pt_lib()
+    if P is None:
+        pytest.skip("reference shaders not available here")
+    scene = oracle.OracleScene(pin_cases.CASES["textured_pcg"][0]())
+    rng = np.random.default_rng(5)
+    n = 50000
+    inst = np.ones(n, np.uint32)
+    prim = rng.integers(0, 10, n).astype(np.uint32)
+    uv = rng.random((n, 2))
+    flip = uv.sum(1) > 1.0
+    uv[flip] = 1.0 - uv[flip]
+    uv = uv.astype(np.float32)
+    assert np.array_equal(scene.alpha_accept(inst, prim, uv), oracle.shader_anyhit(P, scene, inst, prim, uv))
+
+
 def _live_pixels(v):
     import pin_cases
     n = v.width * v.height
