@@ -1083,7 +1083,38 @@ def case_instanced_pool(arg):
     print(f"instanced 4 views 384^2 x 4 spp, {pt.launch_config}: {ms:.3f} ms per call")
 
 
-CASES = {"denoise_infer": case_denoise_infer, "adjoint": case_adjoint, "instanced_view": case_instanced_view,
+def case_traversal_shapes(arg):
+    """Per-view wavefront on sphere_1m (1920x1080, 1 spp, depth 4) in each
+    traversal shape: one ray per thread, or persistent warps refilled at
+    1/2/4/8/16 idle lanes; CUDA-event ms per frame (3 warm-up, 20 timed,
+    L2 flushed), and the images' bit identity."""
+    import torch
+    import ohao_engine_gb300 as og
+    from ohao_engine_gb300 import scenes
+    sd = scenes.sphere_1m() if arg != "instanced" else scenes.instanced(n_views=1, side_range=(1024, 1024))
+    pt = og.PathTracer()
+    pt.load_scene(sd)
+    v = sd.views[0]
+    npix = v.width * v.height
+    acc = torch.zeros((npix, 4), dtype=torch.float32, device="cuda")
+    flush = torch.empty(64 * 1024 * 1024, dtype=torch.float32, device="cuda")
+    ref = None
+    for refill in (33, 1, 2, 4, 8, 16):
+        st = og.make_settings(spp=1, max_bounces=4, wavefront_refill=refill)
+        times = _time_steps(lambda k: pt.render([og.make_view(v, accum=acc)], st), 3, 20, flush)
+        same = True
+        if ref is None:
+            ref = acc.clone()
+        else:
+            same = bool(torch.equal(acc, ref))
+        pt.render([og.make_view(v, accum=acc)], og.make_settings(spp=1, max_bounces=4, wavefront_refill=refill,
+                                                                 flags=og.FLAG_PROFILE))
+        p = pt.profile()
+        print(f"refill {refill:2d}: {sum(times) / len(times):.3f} ms/frame  extend {p.extend_ms:.3f} ms "
+              f"shadow {p.shadow_ms:.3f} ms shade {p.shade_ms:.3f} ms  identical={same}")
+
+
+CASES = {"traversal_shapes": case_traversal_shapes, "denoise_infer": case_denoise_infer, "adjoint": case_adjoint, "instanced_view": case_instanced_view,
          "instanced_pool": case_instanced_pool}
 
 

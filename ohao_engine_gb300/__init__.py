@@ -73,7 +73,7 @@ class Settings(C.Structure):
     _fields_ = [("spp", C.c_uint32), ("max_bounces", C.c_uint32), ("sample_index_base", C.c_uint32),
                 ("sampler", C.c_uint32), ("flags", C.c_uint32), ("clamp_luminance", C.c_float),
                 ("aniso_strength", C.c_float), ("aniso_rotation", C.c_float), ("mode", C.c_uint32),
-                ("trace_stack_limit", C.c_uint32), ("reserved", C.c_uint32 * 6)]
+                ("trace_stack_limit", C.c_uint32), ("wavefront_refill", C.c_uint32), ("reserved", C.c_uint32 * 5)]
 
 
 class Texture(C.Structure):
@@ -275,9 +275,11 @@ def _view_array(views, settings: "Settings"):
 
 
 def make_settings(spp=1, max_bounces=4, sample_index_base=0, sampler=SAMPLER_PCG, flags=0, clamp_luminance=0.0,
-                  aniso_strength=0.0, aniso_rotation=0.0, mode=MODE_AUTO, trace_stack_limit=0) -> Settings:
+                  aniso_strength=0.0, aniso_rotation=0.0, mode=MODE_AUTO, trace_stack_limit=0,
+                  wavefront_refill=0) -> Settings:
     s = Settings()
     s.trace_stack_limit = trace_stack_limit
+    s.wavefront_refill = wavefront_refill
     s.spp, s.max_bounces, s.sample_index_base, s.sampler = spp, max_bounces, sample_index_base, sampler
     s.flags, s.clamp_luminance, s.aniso_strength, s.aniso_rotation, s.mode = (flags, clamp_luminance,
                                                                              aniso_strength, aniso_rotation, mode)

@@ -84,8 +84,12 @@ struct ohao_pt_ctx {
     // texture (first texel, width, height, 0)
     DevBuf tex_texels, tex_info;
     uint32_t ntex = 0;
-    // material texture indices the renders need (from the host copy of the table)
+    // material texture indices the renders need, from the host copy of the
+    // table, summarised when the table changes: the largest bindless index
+    // other than diffuse 0 (or -1), whether diffuse index 0 occurs
     std::vector<float> mats_host;
+    int64_t mat_max_tex = -1;
+    bool mat_uses_diffuse0 = false;
     // acceleration structure
     std::vector<BlasDesc> blas;
     std::vector<ohao_pt_instance> instances;
@@ -537,32 +541,35 @@ static bool material_indices_valid(const float* m, uint32_t n) {
     return true;
 }
 
-// Whether every texture index of the material table names a texture (or,
-// for diffuse index 0, the tile albedo map when one is set).
-static bool material_textures_bound(const ohao_pt_ctx* ctx) {
+// Re-summarises the texture indices of the host copy of the material table
+// (called when the table changes, so renders check two numbers).
+static void summarise_material_textures(ohao_pt_ctx* ctx) {
+    ctx->mat_max_tex = -1;
+    ctx->mat_uses_diffuse0 = false;
     const size_t n = ctx->mats_host.size() / 12;
     for (size_t i = 0; i < n; ++i)
         for (int slot : {3, 6, 7, 8}) {
             uint32_t t;
             std::memcpy(&t, ctx->mats_host.data() + 12 * i + slot, 4);
             if (t == kNoTex) continue;
-            if (slot == 3 && t == 0u && ctx->map_w > 0) continue;
-            if (t >= ctx->ntex) return false;
+            if (slot == 3 && t == 0u) {
+                ctx->mat_uses_diffuse0 = true;
+                continue;
+            }
+            ctx->mat_max_tex = std::max<int64_t>(ctx->mat_max_tex, t);
         }
-    return true;
+}
+
+// Whether every texture index of the material table names a texture (or,
+// for diffuse index 0, the tile albedo map when one is set).
+static bool material_textures_bound(const ohao_pt_ctx* ctx) {
+    if (ctx->mat_max_tex >= static_cast<int64_t>(ctx->ntex)) return false;
+    return !ctx->mat_uses_diffuse0 || ctx->map_w > 0 || ctx->ntex > 0;
 }
 
 // Whether any material uses a bindless texture (the tile albedo map aside).
 static bool material_uses_textures(const ohao_pt_ctx* ctx) {
-    const size_t n = ctx->mats_host.size() / 12;
-    for (size_t i = 0; i < n; ++i)
-        for (int slot : {3, 6, 7, 8}) {
-            uint32_t t;
-            std::memcpy(&t, ctx->mats_host.data() + 12 * i + slot, 4);
-            if (t == kNoTex || (slot == 3 && t == 0u && ctx->map_w > 0)) continue;
-            return true;
-        }
-    return false;
+    return ctx->mat_max_tex >= 0 || (ctx->mat_uses_diffuse0 && ctx->map_w == 0);
 }
 
 ohao_status ohao_pt_set_materials(ohao_pt_ctx* ctx, const float* m, uint32_t n) {
@@ -573,6 +580,7 @@ ohao_status ohao_pt_set_materials(ohao_pt_ctx* ctx, const float* m, uint32_t n) 
     ctx->nmats = s == OHAO_OK ? n : 0;   // a failed upload may have released the table
     if (s == OHAO_OK) ctx->mats_host.assign(m, m + static_cast<size_t>(n) * 12);
     else ctx->mats_host.clear();
+    summarise_material_textures(ctx);
     return s;
 }
 
@@ -583,6 +591,7 @@ ohao_status ohao_pt_update_materials(ohao_pt_ctx* ctx, const float* m, uint32_t 
         return fail(ctx, OHAO_ERR_INVALID_ARG, "update_materials: a texture index is neither 0xFFFFFFFF nor below 65536");
     if (n) CK(cudaMemcpy(ctx->mats.as<char>() + static_cast<size_t>(first) * 48, m, static_cast<size_t>(n) * 48, cudaMemcpyHostToDevice), "materials");
     std::copy(m, m + static_cast<size_t>(n) * 12, ctx->mats_host.begin() + static_cast<size_t>(first) * 12);
+    summarise_material_textures(ctx);
     return OHAO_OK;
 }
 
@@ -703,10 +712,19 @@ static ohao_status validate_render(ohao_pt_ctx* ctx, const ohao_pt_view* views, 
     if (st->max_bounces > 64) return fail(ctx, OHAO_ERR_INVALID_ARG, "render: max_bounces > 64");
     if (st->sampler > 1) return fail(ctx, OHAO_ERR_INVALID_ARG, "render: unknown sampler");
     if (st->mode > OHAO_PT_MODE_PERSISTENT) return fail(ctx, OHAO_ERR_INVALID_ARG, "render: unknown mode");
+    if (st->wavefront_refill > 33u) return fail(ctx, OHAO_ERR_INVALID_ARG, "render: wavefront_refill above 33");
     for (uint32_t v = 0; v < n_views; ++v)
         if (views[v].width == 0 || views[v].height == 0 || static_cast<uint64_t>(views[v].width) * views[v].height > (1ull << 31))
             return fail(ctx, OHAO_ERR_INVALID_ARG, "render: bad view size");
     return OHAO_OK;
+}
+
+// Traversal shape of the per-view wavefront (settings.wavefront_refill; 0 =
+// the default below, 33 = one ray per thread).
+static uint32_t wavefront_refill(const ohao_pt_settings* st) {
+    constexpr uint32_t kDefaultRefill = 0u;
+    if (st->wavefront_refill == 0u) return kDefaultRefill;
+    return st->wavefront_refill >= 33u ? 0u : st->wavefront_refill;
 }
 
 static bool any_non_opaque(const ohao_pt_ctx* ctx) {
@@ -749,7 +767,7 @@ static ohao_status render_views(ohao_pt_ctx* ctx, const ohao_pt_view* views, uin
     sc.stack_limit = st->trace_stack_limit;
     sc.alpha_test = (st->flags & OHAO_PT_FLAG_ALPHA_TEST) && any_non_opaque(ctx) ? 1u : 0u;
     ohao::PathParams pp{st->max_bounces, st->sampler, st->flags, st->clamp_luminance, st->aniso_strength,
-                        st->aniso_rotation, st->sample_index_base};
+                        st->aniso_rotation, st->sample_index_base, wavefront_refill(st)};
     const std::vector<ohao::RenderView> rvs = to_render_views(views, n_views, dev_accum);
     if (use_persistent(st, n_views)) {
         ohao_status s = ensure_persistent(ctx);
@@ -796,7 +814,7 @@ ohao_status ohao_pt_autotune(ohao_pt_ctx* ctx, const ohao_pt_view* views, uint32
     if ((s = ensure_persistent(ctx)) != OHAO_OK) return s;
     cudaStream_t cs = reinterpret_cast<cudaStream_t>(stream);
     ohao::PathParams pp{st->max_bounces, st->sampler, st->flags, st->clamp_luminance, st->aniso_strength,
-                        st->aniso_rotation, st->sample_index_base};
+                        st->aniso_rotation, st->sample_index_base, wavefront_refill(st)};
     const std::vector<ohao::RenderView> rvs = to_render_views(views, n_views, acc.data());
     std::string err;
     s = ohao::persistent_autotune(ctx->persistent, make_scene(ctx), rvs.data(), n_views, pp, st->spp,
@@ -890,7 +908,7 @@ static ohao_status validate_backward(ohao_pt_ctx* ctx, const ohao_pt_view* views
 static ohao_status run_backward(ohao_pt_ctx* ctx, const std::vector<ohao::RenderView>& rvs, const float* const* grads,
                                 const ohao_pt_settings* st, float* d_grad_map, float* d_grad_rough, cudaStream_t cs) {
     ohao::PathParams pp{st->max_bounces, st->sampler, st->flags, st->clamp_luminance, st->aniso_strength,
-                        st->aniso_rotation, st->sample_index_base};
+                        st->aniso_rotation, st->sample_index_base, wavefront_refill(st)};
     const uint32_t n = static_cast<uint32_t>(rvs.size());
     CK(ctx->adj_scratch.ensure(ohao::adjoint_scratch_bytes(n)), "backward scratch");
     std::string err;

@@ -90,9 +90,9 @@ OHAO_D void enter_instance(const DScene& sc, const RayPre& r, const uint4& pq, u
 // One step of the closest-hit walk; true when the ray is finished (w.best
 // holds its hit). r: the world-space ray. Stack overflow sets err and ends
 // the walk.
-template <int kLevels>
+template <int kLevels, bool kStats = false>
 OHAO_D bool walk_step(const DScene& sc, Walk& w, const RayPre& r, float tmin, float tmax, uint32_t* st_node,
-                      float* st_t, int& err) {
+                      float* st_t, int& err, TravCount* cnt = nullptr) {
     if (w.tlm) {   // one pending triangle
         const int i = __ffs(w.tlm) - 1;
         const uint32_t meta = byte_of(w.tmz, w.tmw, i);
@@ -100,6 +100,7 @@ OHAO_D bool walk_step(const DScene& sc, Walk& w, const RayPre& r, float tmin, fl
         if (w.tq < c) {
             const float4* tp = w.btris + static_cast<size_t>(w.tbase + off + w.tq) * 3;
             const float4 v0 = __ldg(tp), v1 = __ldg(tp + 1), v2 = __ldg(tp + 2);
+            if (kStats) cnt->tris++;
             float t, u, v;
             const bool h = tri_intersect(w.ra, v0, v1, v2, tmin, tmax, t, u, v);
             const uint32_t prim = __float_as_uint(v0.w);
@@ -123,6 +124,7 @@ OHAO_D bool walk_step(const DScene& sc, Walk& w, const RayPre& r, float tmin, fl
         bool leaves = false;
         if (w.cur_tn <= tb + tb * kTravRelSlack) {
             const NodeRec n = load_node(w.in_blas ? w.bnodes : sc.nodes, w.cur);
+            if (kStats) cnt->nodes++;
             float tn[8];
             const uint32_t hit = node_test(n, w.ra, tmin, tb, tn);
             const uint32_t imask = n.q0.w >> 24;
@@ -228,9 +230,9 @@ OHAO_D void probe_begin(const DScene& sc, Probe& w, const RayPre& r) {
 }
 
 // One step of the any-hit walk; true when finished (w.hit: occluded).
-template <int kLevels>
+template <int kLevels, bool kStats = false>
 OHAO_D bool probe_step(const DScene& sc, Probe& w, const RayPre& r, float tmin, float tmax, uint32_t* st_node,
-                       int& err) {
+                       int& err, TravCount* cnt = nullptr) {
     if (w.tlm) {   // one pending triangle
         const int i = __ffs(w.tlm) - 1;
         const uint32_t meta = byte_of(w.tmz, w.tmw, i);
@@ -238,6 +240,7 @@ OHAO_D bool probe_step(const DScene& sc, Probe& w, const RayPre& r, float tmin, 
         if (w.tq < c) {
             const float4* tp = w.btris + static_cast<size_t>(w.tbase + off + w.tq) * 3;
             const float4 v0 = __ldg(tp), v1 = __ldg(tp + 1), v2 = __ldg(tp + 2);
+            if (kStats) cnt->tris++;
             float t, u, v;
             if (tri_intersect(w.ra, v0, v1, v2, tmin, tmax, t, u, v) &&
                 (!sc.alpha_test ||
@@ -254,6 +257,7 @@ OHAO_D bool probe_step(const DScene& sc, Probe& w, const RayPre& r, float tmin, 
     }
     if (w.have_node) {
         const NodeRec n = load_node(w.in_blas ? w.bnodes : sc.nodes, w.cur);
+        if (kStats) cnt->nodes++;
         float tn[8];
         uint32_t m = node_test(n, w.ra, tmin, tmax, tn);
         const uint32_t imask = n.q0.w >> 24;

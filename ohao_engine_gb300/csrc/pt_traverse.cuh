@@ -73,6 +73,19 @@ OHAO_D uint32_t byte_of(uint32_t lo4, uint32_t hi4, int i) {
     return (w >> ((i & 3) * 8)) & 0xFFu;
 }
 
+// three-input min / max of sm_100+ (one instruction each; NaN operands are
+// ignored, as by fmaxf / fminf)
+OHAO_D float max3f(float a, float b, float c) {
+    float d;
+    asm("max.f32 %0, %1, %2, %3;" : "=f"(d) : "f"(a), "f"(b), "f"(c));
+    return d;
+}
+OHAO_D float min3f(float a, float b, float c) {
+    float d;
+    asm("min.f32 %0, %1, %2, %3;" : "=f"(d) : "f"(a), "f"(b), "f"(c));
+    return d;
+}
+
 // exact uint8 -> float: bits (0x4B000000 | b) encode 2^23 + b
 OHAO_D float u8f(uint32_t word, int b) {
     return __uint_as_float(__byte_perm(word, 0x4B000000u, 0x7440u | static_cast<uint32_t>(b))) - 8388608.0f;
@@ -109,11 +122,12 @@ OHAO_D uint32_t node_test(const NodeRec& n, const RayPre& r, float tmin, float t
         const float qnx = u8f(i < 4 ? nx0 : nx1, b), qfx = u8f(i < 4 ? fx0 : fx1, b);
         const float qny = u8f(i < 4 ? ny0 : ny1, b), qfy = u8f(i < 4 ? fy0 : fy1, b);
         const float qnz = u8f(i < 4 ? nz0 : nz1, b), qfz = u8f(i < 4 ? fz0 : fz1, b);
-        const float t0 = fmaxf(fmaxf(fmaf(qnx, a[0], bn[0]), fmaf(qny, a[1], bn[1])), fmaf(qnz, a[2], bn[2]));
-        const float t1 = fminf(fminf(fmaf(qfx, a[0], bf[0]), fmaf(qfy, a[1], bf[1])), fmaf(qfz, a[2], bf[2]));
+        const float t0 = max3f(fmaf(qnx, a[0], bn[0]), fmaf(qny, a[1], bn[1]), fmaf(qnz, a[2], bn[2]));
+        const float t1 = min3f(fmaf(qfx, a[0], bf[0]), fmaf(qfy, a[1], bf[1]), fmaf(qfz, a[2], bf[2]));
         tn[i] = t0;
         const uint32_t meta = byte_of(n.q1.z, n.q1.w, i);
-        if (meta != 0u && t0 <= t1 && t0 <= tlimit && t1 >= tmin) hit |= 1u << i;
+        // t0 <= t1, t0 <= tlimit and t1 >= tmin at once (tmin <= tlimit always)
+        if (meta != 0u && fmaxf(t0, tmin) <= fminf(t1, tlimit)) hit |= 1u << i;
     }
     return hit;
 }

@@ -67,6 +67,7 @@ struct PathParams {
     float clamp_lum;
     float aniso, aniso_rot;
     uint32_t sample_base;
+    uint32_t refill;        // per-view wavefront traversal: 0 one ray per thread, 1..32 persistent warps
 };
 
 struct ViewParams {

@@ -479,8 +479,9 @@ struct WarpFetch {
     }
 };
 
-template <int kLevels>
-__global__ void __launch_bounds__(128) k_extend_fetch(DScene sc, Soa s, int cur, int refill, int* err) {
+template <bool kStats, int kLevels>
+__global__ void __launch_bounds__(128) k_extend_fetch(DScene sc, Soa s, int cur, int refill, int* err,
+                                                      unsigned long long* stats) {
     const uint32_t count = s.counts[cur];
     const uint32_t* q = s.q_ray[cur];
     uint32_t st_node[kStackSize];
@@ -491,6 +492,8 @@ __global__ void __launch_bounds__(128) k_extend_fetch(DScene sc, Soa s, int cur,
     bool active = false;
     WarpFetch wf;
     int e = 0;
+    TravCount tc{0, 0};
+    uint32_t nr = 0;
     while (true) {
         const uint32_t i = wf.claim(!active, s.counts + kCtrExtendFetch, count, refill);
         if (i != 0xFFFFFFFFu) {
@@ -498,18 +501,20 @@ __global__ void __launch_bounds__(128) k_extend_fetch(DScene sc, Soa s, int cur,
             r = ray_pre(ld3(s.ro[p]), ld3(s.rd[p]));
             walk_begin<kLevels>(sc, w, r);
             active = true;
+            nr++;
         }
         if (__ballot_sync(0xFFFFFFFFu, active) == 0u) {
             if (wf.drained) break;
             continue;
         }
-        if (active && walk_step<kLevels>(sc, w, r, 0.001f, 10000.0f, st_node, st_t, e)) {
+        if (active && walk_step<kLevels, kStats>(sc, w, r, 0.001f, 10000.0f, st_node, st_t, e, &tc)) {
             s.hit[p] = make_float4(w.best.t, w.best.u, w.best.v, __uint_as_float(w.best.prim));
             s.hit_inst[p] = w.best.inst;
             active = false;
         }
     }
     if (e) atomicOr(err, 1);
+    if (kStats) add_stats(stats + 0, nr, tc);
 }
 
 // Starts shadow ray `which` (0 light, 1 environment) of path p; a ray with
@@ -523,8 +528,9 @@ __device__ __forceinline__ void start_shadow(const DScene& sc, const Soa& s, uin
     if (!(d.w > 0.001f)) w.have_node = false;   // the next step ends the walk unoccluded
 }
 
-template <int kLevels>
-__global__ void __launch_bounds__(128) k_shadow_fetch(DScene sc, Soa s, int refill, int* err) {
+template <bool kStats, int kLevels>
+__global__ void __launch_bounds__(128) k_shadow_fetch(DScene sc, Soa s, int refill, int* err,
+                                                      unsigned long long* stats) {
     const uint32_t count = s.counts[2];
     uint32_t st_node[kStackSize];
     Probe w;
@@ -536,6 +542,8 @@ __global__ void __launch_bounds__(128) k_shadow_fetch(DScene sc, Soa s, int refi
     bool active = false;
     WarpFetch wf;
     int e = 0;
+    TravCount tc{0, 0};
+    uint32_t nr = 0;
     while (true) {
         const uint32_t i = wf.claim(!active, s.counts + kCtrShadowFetch, count, refill);
         if (i != 0xFFFFFFFFu) {
@@ -546,17 +554,19 @@ __global__ void __launch_bounds__(128) k_shadow_fetch(DScene sc, Soa s, int refi
             tmax = which == 0 ? s.shL[p].w : s.shE[p].w;
             visL = false;
             active = true;
+            nr++;
         }
         if (__ballot_sync(0xFFFFFFFFu, active) == 0u) {
             if (wf.drained) break;
             continue;
         }
-        if (active && probe_step<kLevels>(sc, w, r, 0.001f, tmax, st_node, e)) {
+        if (active && probe_step<kLevels, kStats>(sc, w, r, 0.001f, tmax, st_node, e, &tc)) {
             if (which == 0) visL = !w.hit;
             if (which == 0 && (f & kFlagShE)) {
                 which = 1;
                 start_shadow<kLevels>(sc, s, p, 1, w, r);
                 tmax = s.shE[p].w;
+                nr++;
             } else {
                 const bool visE = which == 1 && !w.hit;
                 V3 rad = ld3(s.rad[p]);
@@ -569,6 +579,7 @@ __global__ void __launch_bounds__(128) k_shadow_fetch(DScene sc, Soa s, int refi
         }
     }
     if (e) atomicOr(err, 1);
+    if (kStats) add_stats(stats + 3, nr, tc);
 }
 
 // p: the pixel's work rank (slots are rank-major); outputs at its index.
@@ -716,14 +727,39 @@ void init_launch_shapes() {
         g_blocks_extend[k] *= kTraversalWaves;
         g_blocks_shadow[k] *= kTraversalWaves;
     }
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, k_extend_fetch<1>, 128, 0);
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, k_extend_fetch<false, 1>, 128, 0);
     g_blocks_fetch[0] = std::max(1, b) * g_num_sms;
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, k_extend_fetch<2>, 128, 0);
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, k_extend_fetch<false, 2>, 128, 0);
     g_blocks_fetch[1] = std::max(1, b) * g_num_sms;
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, k_shadow_fetch<1>, 128, 0);
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, k_shadow_fetch<false, 1>, 128, 0);
     g_blocks_fetch[2] = std::max(1, b) * g_num_sms;
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, k_shadow_fetch<2>, 128, 0);
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, k_shadow_fetch<false, 2>, 128, 0);
     g_blocks_fetch[3] = std::max(1, b) * g_num_sms;
+}
+
+// persistent-warp closest-hit / any-hit kernels for the scene kind (the
+// caller zeroes the fetch counter first)
+void launch_extend_fetch(const DScene& sc, const Soa& s, int cur, int refill, int* d_err, unsigned long long* stats,
+                         cudaStream_t st) {
+    const int two = sc.two_level ? 1 : 0;
+    if (stats) {
+        if (two) k_extend_fetch<true, 2><<<g_blocks_fetch[1], 128, 0, st>>>(sc, s, cur, refill, d_err, stats);
+        else k_extend_fetch<true, 1><<<g_blocks_fetch[0], 128, 0, st>>>(sc, s, cur, refill, d_err, stats);
+    } else {
+        if (two) k_extend_fetch<false, 2><<<g_blocks_fetch[1], 128, 0, st>>>(sc, s, cur, refill, d_err, nullptr);
+        else k_extend_fetch<false, 1><<<g_blocks_fetch[0], 128, 0, st>>>(sc, s, cur, refill, d_err, nullptr);
+    }
+}
+void launch_shadow_fetch(const DScene& sc, const Soa& s, int refill, int* d_err, unsigned long long* stats,
+                         cudaStream_t st) {
+    const int two = sc.two_level ? 1 : 0;
+    if (stats) {
+        if (two) k_shadow_fetch<true, 2><<<g_blocks_fetch[3], 128, 0, st>>>(sc, s, refill, d_err, stats);
+        else k_shadow_fetch<true, 1><<<g_blocks_fetch[2], 128, 0, st>>>(sc, s, refill, d_err, stats);
+    } else {
+        if (two) k_shadow_fetch<false, 2><<<g_blocks_fetch[3], 128, 0, st>>>(sc, s, refill, d_err, nullptr);
+        else k_shadow_fetch<false, 1><<<g_blocks_fetch[2], 128, 0, st>>>(sc, s, refill, d_err, nullptr);
+    }
 }
 
 // closest-hit / any-hit kernels specialised for the scene kind
@@ -823,9 +859,12 @@ ohao_status wavefront_render(const DScene& sc, const RenderView& view, const Pat
         k_generate<<<(n + 255) / 256, 256, 0, st>>>(view.vp, pp, static_cast<uint32_t>(w0), n, npix, s);
         tm.end(3, a);
         int cur = 0;
+        const bool fetch = pp.refill > 0 && sc.nnodes > 0;
         for (uint32_t it = 0; it < niters; ++it) {
+            if (fetch) cudaMemsetAsync(s.counts + kCtrExtendFetch, 0, 8, st);   // both fetch counters
             tm.begin(0, a);
-            launch_extend(sc, s, cur, d_err, profile ? dstats : nullptr, st);
+            if (fetch) launch_extend_fetch(sc, s, cur, static_cast<int>(pp.refill), d_err, profile ? dstats : nullptr, st);
+            else launch_extend(sc, s, cur, d_err, profile ? dstats : nullptr, st);
             tm.end(0, a);
             cudaMemsetAsync(s.counts + (cur ^ 1), 0, 4, st);
             cudaMemsetAsync(s.counts + 2, 0, 4, st);
@@ -834,7 +873,8 @@ ohao_status wavefront_render(const DScene& sc, const RenderView& view, const Pat
                                                            view.aov, spp - 1, nullptr);
             tm.end(1, a);
             tm.begin(2, a);
-            launch_shadow(sc, s, d_err, profile ? dstats : nullptr, st);
+            if (fetch) launch_shadow_fetch(sc, s, static_cast<int>(pp.refill), d_err, profile ? dstats : nullptr, st);
+            else launch_shadow(sc, s, d_err, profile ? dstats : nullptr, st);
             tm.end(2, a);
             cur ^= 1;
         }
@@ -1022,8 +1062,7 @@ void enqueue_chunk(const DScene& sc, const PathParams& pp, const LaunchBlock* lb
         }
         if (fetch) {
             cudaMemsetAsync(s.counts + kCtrExtendFetch, 0, 8, st);   // both fetch counters
-            if (sc.two_level) k_extend_fetch<2><<<g_blocks_fetch[1], 128, 0, st>>>(sc, s, cur, pv.refill, d_err);
-            else k_extend_fetch<1><<<g_blocks_fetch[0], 128, 0, st>>>(sc, s, cur, pv.refill, d_err);
+            launch_extend_fetch(sc, s, cur, pv.refill, d_err, nullptr, st);
         } else {
             launch_extend(sc, s, cur, d_err, nullptr, st);
         }
@@ -1031,8 +1070,7 @@ void enqueue_chunk(const DScene& sc, const PathParams& pp, const LaunchBlock* lb
         cudaMemsetAsync(s.counts + 2, 0, 8, st);   // shadow and done counts
         k_shade<true><<<g_blocks_shade, 128, 0, st>>>(sc, pp, ViewParams{}, 0u, 1u, s, cur, nullptr, 0u, lb);
         if (fetch) {
-            if (sc.two_level) k_shadow_fetch<2><<<g_blocks_fetch[3], 128, 0, st>>>(sc, s, pv.refill, d_err);
-            else k_shadow_fetch<1><<<g_blocks_fetch[2], 128, 0, st>>>(sc, s, pv.refill, d_err);
+            launch_shadow_fetch(sc, s, pv.refill, d_err, nullptr, st);
         } else {
             launch_shadow(sc, s, d_err, nullptr, st);
         }

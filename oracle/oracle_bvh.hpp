@@ -487,7 +487,8 @@ inline NodeHits node_test(const WideNode& n, const RayPre& r, float tmin, float 
             tf = (k == 0) ? vf : std::fmin(tf, vf);
         }
         h.tnear[i] = tn;
-        if (n.meta[i] != 0 && tn <= tf && tn <= tlimit && tf >= tmin) h.mask |= 1u << i;
+        // tn <= tf, tn <= tlimit and tf >= tmin in one comparison (tmin <= tlimit)
+        if (n.meta[i] != 0 && std::fmax(tn, tmin) <= std::fmin(tf, tlimit)) h.mask |= 1u << i;
     }
     return h;
 }
