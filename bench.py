@@ -122,12 +122,32 @@ class ClockSampler:
                 "reasons": sorted(reasons), "samples": len(sm)}
 
 
+TRAVERSAL_SOURCES = ["pt_device.cuh", "pt_traverse.cuh", "pt_fetch.cuh", "wavefront.cu", "pt_types.hpp"]
+
+
+def traversal_source_sha():
+    """sha256 of the sources k_extend is compiled from: a committed DRAM
+    traffic figure is used only while it was captured from these sources."""
+    import hashlib
+    h = hashlib.sha256()
+    for f in TRAVERSAL_SOURCES:
+        with open(os.path.join(ROOT, "ohao_engine_gb300", "csrc", f), "rb") as fh:
+            h.update(fh.read())
+    return h.hexdigest()
+
+
 def traffic_from_profiles(kernel, workload_name):
+    """DRAM bytes per launch of the kernel from the committed ncu capture
+    (profiles/<kernel>_<workload>.json), or None with the reason when the
+    capture does not match the current traversal sources."""
     p = os.path.join(ROOT, "profiles", f"{kernel}_{workload_name}.json")
-    if os.path.exists(p):
-        d = json.load(open(p))
-        return d.get("dram_bytes_per_launch"), d.get("note")
-    return None, None
+    if not os.path.exists(p):
+        return None, "no ncu capture committed for this kernel and workload"
+    d = json.load(open(p))
+    if d.get("source_sha256") != traversal_source_sha():
+        return None, (f"the committed capture ({os.path.basename(p)}) was taken from other traversal sources than "
+                      "these; re-capture with the command in profiles/ to fill traffic")
+    return d.get("dram_bytes_per_launch"), d.get("note")
 
 
 def cpu_baseline(sd, spp_step, target_s, full_step_samples):
@@ -1099,8 +1119,9 @@ def case_traversal_shapes(arg):
     acc = torch.zeros((npix, 4), dtype=torch.float32, device="cuda")
     flush = torch.empty(64 * 1024 * 1024, dtype=torch.float32, device="cuda")
     ref = None
-    for refill in (33, 1, 2, 4, 8, 16):
-        st = og.make_settings(spp=1, max_bounces=4, wavefront_refill=refill)
+    for refill, flags in ((33, 0), (33, og.FLAG_SORT_MATERIAL), (1, 0), (4, 0), (8, 0), (16, 0),
+                          (8, og.FLAG_SORT_MATERIAL)):
+        st = og.make_settings(spp=1, max_bounces=4, wavefront_refill=refill, flags=flags)
         times = _time_steps(lambda k: pt.render([og.make_view(v, accum=acc)], st), 3, 20, flush)
         same = True
         if ref is None:
@@ -1108,10 +1129,11 @@ def case_traversal_shapes(arg):
         else:
             same = bool(torch.equal(acc, ref))
         pt.render([og.make_view(v, accum=acc)], og.make_settings(spp=1, max_bounces=4, wavefront_refill=refill,
-                                                                 flags=og.FLAG_PROFILE))
+                                                                 flags=og.FLAG_PROFILE | flags))
         p = pt.profile()
-        print(f"refill {refill:2d}: {sum(times) / len(times):.3f} ms/frame  extend {p.extend_ms:.3f} ms "
-              f"shadow {p.shadow_ms:.3f} ms shade {p.shade_ms:.3f} ms  identical={same}")
+        print(f"refill {refill:2d} sort {int(flags != 0)}: {sum(times) / len(times):.3f} ms/frame  extend "
+              f"{p.extend_ms:.3f} ms shadow {p.shadow_ms:.3f} ms shade {p.shade_ms:.3f} ms other {p.other_ms:.3f} ms  "
+              f"identical={same}")
 
 
 CASES = {"traversal_shapes": case_traversal_shapes, "denoise_infer": case_denoise_infer, "adjoint": case_adjoint, "instanced_view": case_instanced_view,

@@ -186,6 +186,15 @@ ohao_status build_one(ohao_pt_ctx* ctx, const float* d_boxes, uint32_t n, BvhDev
     return OHAO_OK;
 }
 
+constexpr uint32_t kStackEntries = 64;   // the traversal stack of every ray (pt_traverse.cuh kStackSize)
+
+// The per-ray stack limit of a render: settings.trace_stack_limit in
+// [1, 64], 0 = all 64.
+uint32_t stack_limit_of(const ohao_pt_settings* st) {
+    return (st->trace_stack_limit == 0u || st->trace_stack_limit > kStackEntries) ? kStackEntries
+                                                                                  : st->trace_stack_limit;
+}
+
 ohao::DScene make_scene(const ohao_pt_ctx* c) {
     ohao::DScene s{};
     s.nodes = c->flat.nodes.as<uint4>();
@@ -220,7 +229,7 @@ ohao::DScene make_scene(const ohao_pt_ctx* c) {
     s.albedo_map = c->albedo_map.as<float>();
     s.map_w = c->map_w;
     s.map_h = c->map_h;
-    s.stack_limit = 0;
+    s.stack_limit = kStackEntries;
     s.tex = c->tex_texels.as<uchar4>();
     s.tex_info = c->tex_info.as<uint4>();
     s.ntex = c->ntex;
@@ -234,6 +243,8 @@ ohao_status check_device_error(ohao_pt_ctx* ctx, cudaStream_t st) {
     CK(cudaStreamSynchronize(st), "stream sync");
     if (flag) {
         cudaMemsetAsync(ctx->err_flag.p, 0, sizeof(int), st);
+        if (flag & 4)   // the persistent pool's device loop gave up
+            return fail(ctx, OHAO_ERR_TIMEOUT, "persistent render: the work queue did not drain within the chunk bound");
         return fail(ctx, OHAO_ERR_DEVICE_CHECK, "traversal stack limit exceeded on the device");
     }
     return OHAO_OK;
@@ -764,7 +775,7 @@ static ohao_status render_views(ohao_pt_ctx* ctx, const ohao_pt_view* views, uin
     const bool profile = (st->flags & OHAO_PT_FLAG_PROFILE) != 0;
     ohao::ProfileAcc acc;
     ohao::DScene sc = make_scene(ctx);
-    sc.stack_limit = st->trace_stack_limit;
+    sc.stack_limit = stack_limit_of(st);
     sc.alpha_test = (st->flags & OHAO_PT_FLAG_ALPHA_TEST) && any_non_opaque(ctx) ? 1u : 0u;
     ohao::PathParams pp{st->max_bounces, st->sampler, st->flags, st->clamp_luminance, st->aniso_strength,
                         st->aniso_rotation, st->sample_index_base, wavefront_refill(st)};
@@ -913,7 +924,7 @@ static ohao_status run_backward(ohao_pt_ctx* ctx, const std::vector<ohao::Render
     CK(ctx->adj_scratch.ensure(ohao::adjoint_scratch_bytes(n)), "backward scratch");
     std::string err;
     ohao::DScene sc = make_scene(ctx);
-    sc.stack_limit = st->trace_stack_limit;
+    sc.stack_limit = stack_limit_of(st);
     const ohao_status s = ohao::adjoint_backward(sc, rvs.data(), grads, n, pp, st->spp, ctx->nmats,
                                                  ctx->adj_scratch.p, ctx->adj_scratch.n, d_grad_map, d_grad_rough, cs,
                                                  ctx->err_flag.as<int>(), err);

@@ -286,6 +286,8 @@ OHAO_D float4 tex_sample(const DScene& sc, uint32_t idx, float u, float v) {
 // candidate hit on a non-opaque instance whose material's diffuse texture
 // has alpha < 0.5 at the hit's UV is ignored. Opaque instances, materials
 // without a diffuse texture and the tile albedo map (no alpha) accept.
+// Out of line: it runs only for candidate hits of non-opaque geometry, and
+// inlined into the traversal loops it would raise their register count.
 OHAO_D bool alpha_accept(const DScene& sc, uint32_t inst, uint32_t prim, float u, float v) {
     const DInst& in = sc.inst[inst];
     if (!(__ldg(&in.mask) & kInstNoOpaque)) return true;

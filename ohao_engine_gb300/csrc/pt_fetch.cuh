@@ -90,7 +90,7 @@ OHAO_D void enter_instance(const DScene& sc, const RayPre& r, const uint4& pq, u
 // One step of the closest-hit walk; true when the ray is finished (w.best
 // holds its hit). r: the world-space ray. Stack overflow sets err and ends
 // the walk.
-template <int kLevels, bool kStats = false>
+template <int kLevels, bool kStats = false, bool kAlpha = false>
 OHAO_D bool walk_step(const DScene& sc, Walk& w, const RayPre& r, float tmin, float tmax, uint32_t* st_node,
                       float* st_t, int& err, TravCount* cnt = nullptr) {
     if (w.tlm) {   // one pending triangle
@@ -105,7 +105,7 @@ OHAO_D bool walk_step(const DScene& sc, Walk& w, const RayPre& r, float tmin, fl
             const bool h = tri_intersect(w.ra, v0, v1, v2, tmin, tmax, t, u, v);
             const uint32_t prim = __float_as_uint(v0.w);
             const uint32_t inst = kLevels == 1 ? __float_as_uint(v1.w) : w.inst;
-            if (h && (!sc.alpha_test || alpha_accept(sc, inst, prim, u, v))) {
+            if (h && (!kAlpha || !sc.alpha_test || alpha_accept(sc, inst, prim, u, v))) {
                 if (w.best.prim == kNoHit || t < w.best.t ||
                     (t == w.best.t && key_less(inst, prim, w.best.inst, w.best.prim))) {
                     w.best.t = t; w.best.u = u; w.best.v = v; w.best.inst = inst; w.best.prim = prim;
@@ -230,7 +230,7 @@ OHAO_D void probe_begin(const DScene& sc, Probe& w, const RayPre& r) {
 }
 
 // One step of the any-hit walk; true when finished (w.hit: occluded).
-template <int kLevels, bool kStats = false>
+template <int kLevels, bool kStats = false, bool kAlpha = false>
 OHAO_D bool probe_step(const DScene& sc, Probe& w, const RayPre& r, float tmin, float tmax, uint32_t* st_node,
                        int& err, TravCount* cnt = nullptr) {
     if (w.tlm) {   // one pending triangle
@@ -243,7 +243,7 @@ OHAO_D bool probe_step(const DScene& sc, Probe& w, const RayPre& r, float tmin, 
             if (kStats) cnt->tris++;
             float t, u, v;
             if (tri_intersect(w.ra, v0, v1, v2, tmin, tmax, t, u, v) &&
-                (!sc.alpha_test ||
+                (!kAlpha || !sc.alpha_test ||
                  alpha_accept(sc, kLevels == 1 ? __float_as_uint(v1.w) : w.inst, __float_as_uint(v0.w), u, v))) {
                 w.hit = true;
                 return true;

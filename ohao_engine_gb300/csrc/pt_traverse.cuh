@@ -32,13 +32,11 @@ constexpr float kTravRelSlack = 0x1p-14f;
 constexpr float kTravAbsScale = 0x1p-21f;
 constexpr int kStackSize = 64;
 
-// Stack entries a ray may use: the scene's limit (a smaller one makes deep
-// traversals report the overflow error; used to test that check), at most
-// kStackSize.
-OHAO_D int stack_limit(const DScene& sc) {
-    return (sc.stack_limit > 0u && sc.stack_limit < static_cast<uint32_t>(kStackSize)) ? static_cast<int>(sc.stack_limit)
-                                                                                       : kStackSize;
-}
+// Stack entries a ray may use: the scene's limit, which the host sets in
+// [1, kStackSize] (a smaller one makes deep traversals report the overflow
+// error; used to test that check). Read from the kernel parameters at each
+// use, so it costs no register.
+OHAO_D int stack_limit(const DScene& sc) { return static_cast<int>(sc.stack_limit); }
 
 struct Hit {
     float t, u, v;
@@ -163,7 +161,7 @@ OHAO_D bool order_children(uint32_t rem, const float tn[8], const NodeRec& n, ui
 }
 
 // Closest hit in one BVH (flat, or a BLAS inside instance inst_override).
-template <bool kStats>
+template <bool kStats, bool kAlpha = false>
 OHAO_D void bvh_closest(const DScene& sc, const uint4* __restrict__ nodes, const float4* __restrict__ tris,
                         const RayPre& r, float tmin, float tmax, Hit& best, uint32_t inst_override, uint32_t* st_node,
                         float* st_t, int stack_base, int lim, TravCount& cnt, int& err) {
@@ -193,7 +191,7 @@ OHAO_D void bvh_closest(const DScene& sc, const uint4* __restrict__ nodes, const
                     if (!tri_intersect(r, v0, v1, v2, tmin, tmax, t, u, v)) continue;
                     const uint32_t prim = __float_as_uint(v0.w);
                     const uint32_t inst = (inst_override != 0xFFFFFFFFu) ? inst_override : __float_as_uint(v1.w);
-                    if (sc.alpha_test && !alpha_accept(sc, inst, prim, u, v)) continue;
+                    if (kAlpha && sc.alpha_test && !alpha_accept(sc, inst, prim, u, v)) continue;
                     if (best.prim == 0xFFFFFFFFu || t < best.t ||
                         (t == best.t && key_less(inst, prim, best.inst, best.prim))) {
                         best.t = t; best.u = u; best.v = v; best.inst = inst; best.prim = prim;
@@ -214,7 +212,7 @@ OHAO_D void bvh_closest(const DScene& sc, const uint4* __restrict__ nodes, const
 }
 
 // Any hit in one BVH.
-template <bool kStats>
+template <bool kStats, bool kAlpha = false>
 OHAO_D bool bvh_any(const DScene& sc, const uint4* __restrict__ nodes, const float4* __restrict__ tris, const RayPre& r,
                     float tmin, float tmax, uint32_t* st_node, int stack_base, int lim, TravCount& cnt, int& err) {
     if (stack_base >= lim) { err = 1; return false; }
@@ -238,7 +236,7 @@ OHAO_D bool bvh_any(const DScene& sc, const uint4* __restrict__ nodes, const flo
                 if (kStats) cnt.tris++;
                 float t, u, v;
                 if (tri_intersect(r, v0, v1, v2, tmin, tmax, t, u, v) &&
-                    (!sc.alpha_test || alpha_accept(sc, __float_as_uint(v1.w), __float_as_uint(v0.w), u, v)))
+                    (!kAlpha || !sc.alpha_test || alpha_accept(sc, __float_as_uint(v1.w), __float_as_uint(v0.w), u, v)))
                     return true;
             }
         }
@@ -277,7 +275,9 @@ OHAO_D void xform_dir(const float m[12], V3 d, V3& o) {
 // kLevels: 0 = decided by the scene at run time, 1 = flat BVH only,
 // 2 = two-level only (kernels specialised per scene kind keep the flat
 // traversal at its own register count).
-template <bool kStats, int kLevels = 0>
+// kAlpha: rays without gl_RayFlagsOpaqueEXT are possible (the alpha test
+// of non-opaque instances is compiled in; it runs when sc.alpha_test).
+template <bool kStats, int kLevels = 0, bool kAlpha = false>
 OHAO_D Hit scene_closest(const DScene& sc, V3 o, V3 d, float tmin, float tmax, TravCount& cnt, int& err) {
     Hit best;
     best.t = 0.0f; best.u = 0.0f; best.v = 0.0f;
@@ -287,7 +287,7 @@ OHAO_D Hit scene_closest(const DScene& sc, V3 o, V3 d, float tmin, float tmax, T
     float st_t[kStackSize];
     const RayPre r = ray_pre(o, d);
     if (kLevels == 1 || (kLevels == 0 && !sc.two_level)) {
-        bvh_closest<kStats>(sc, sc.nodes, sc.tris, r, tmin, tmax, best, 0xFFFFFFFFu, st_node, st_t, 0, stack_limit(sc),
+        bvh_closest<kStats, kAlpha>(sc, sc.nodes, sc.tris, r, tmin, tmax, best, 0xFFFFFFFFu, st_node, st_t, 0, stack_limit(sc),
                             cnt, err);
         return best;
     }
@@ -337,7 +337,7 @@ OHAO_D Hit scene_closest(const DScene& sc, V3 o, V3 d, float tmin, float tmax, T
                             float t, u, v;
                             if (!tri_intersect(ra, v0, v1, v2, tmin, tmax, t, u, v)) continue;
                             const uint32_t prim = __float_as_uint(v0.w);
-                            if (sc.alpha_test && !alpha_accept(sc, inst, prim, u, v)) continue;
+                            if (kAlpha && sc.alpha_test && !alpha_accept(sc, inst, prim, u, v)) continue;
                             if (best.prim == 0xFFFFFFFFu || t < best.t ||
                                 (t == best.t && key_less(inst, prim, best.inst, best.prim))) {
                                 best.t = t; best.u = u; best.v = v; best.inst = inst; best.prim = prim;
@@ -426,13 +426,13 @@ OHAO_D Hit scene_closest(const DScene& sc, V3 o, V3 d, float tmin, float tmax, T
     }
 }
 
-template <bool kStats, int kLevels = 0>
+template <bool kStats, int kLevels = 0, bool kAlpha = false>
 OHAO_D bool scene_occluded(const DScene& sc, V3 o, V3 d, float tmin, float tmax, TravCount& cnt, int& err) {
     if (!(tmax > tmin) || sc.nnodes == 0) return false;
     uint32_t st_node[kStackSize];
     const RayPre r = ray_pre(o, d);
     if (kLevels == 1 || (kLevels == 0 && !sc.two_level))
-        return bvh_any<kStats>(sc, sc.nodes, sc.tris, r, tmin, tmax, st_node, 0, stack_limit(sc), cnt, err);
+        return bvh_any<kStats, kAlpha>(sc, sc.nodes, sc.tris, r, tmin, tmax, st_node, 0, stack_limit(sc), cnt, err);
     // Two-level, as one loop (see scene_closest): at a TLAS node the internal
     // children but the last (slot order) are pushed, its instance leaves are
     // entered in slot order, then the last internal child is visited.
@@ -484,7 +484,7 @@ OHAO_D bool scene_occluded(const DScene& sc, V3 o, V3 d, float tmin, float tmax,
                     if (kStats) cnt.tris++;
                     float t, u, v;
                     if (tri_intersect(ra, v0, v1, v2, tmin, tmax, t, u, v) &&
-                        (!sc.alpha_test || alpha_accept(sc, inst, __float_as_uint(v0.w), u, v)))
+                        (!kAlpha || !sc.alpha_test || alpha_accept(sc, inst, __float_as_uint(v0.w), u, v)))
                         return true;
                 }
             }

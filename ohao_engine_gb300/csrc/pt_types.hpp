@@ -52,7 +52,7 @@ struct DScene {
     int has_env, has_cdf;
     const float* albedo_map;
     uint32_t map_w, map_h;
-    uint32_t stack_limit;   // traversal stack entries per ray; 0 or >= 64 = all 64
+    uint32_t stack_limit;   // traversal stack entries per ray, in [1, 64]
     // bindless textures (RGBA8 UNORM) and their (first texel, width, height, 0)
     const uchar4* tex;
     const uint4* tex_info;

@@ -60,6 +60,9 @@ struct Soa {
 // Persistent multi-view pool: per-call view table in device memory.
 constexpr uint32_t kMaxViews = 1024;
 constexpr uint32_t kIdle = 0xFFFFFFFFu;
+constexpr int kCtrChunks = 7;                    // Soa::counts: pool chunks run in this render
+constexpr uint64_t kMaxChunks = 1u << 20;       // bound on pool chunks per render
+constexpr int kErrQueueTimeout = 4;              // error-flag bit: the work queue did not drain
 
 struct PView {
     ViewParams vp;
@@ -205,8 +208,11 @@ __device__ __forceinline__ void add_stats(unsigned long long* dst, uint32_t rays
 
 // stats (profiling only): [0] rays, [1] nodes, [2] triangles
 // kLevels: 1 = flat BVH, 2 = two-level (one kernel per scene kind).
-template <bool kStats, int kLevels>
-__global__ void __launch_bounds__(128) k_extend(DScene sc, Soa s, int cur, int* err, unsigned long long* stats) {
+// Registers capped for 8 resident blocks per SM on flat scenes (64
+// registers), 5 on two-level ones.
+template <bool kStats, int kLevels, bool kAlpha>
+__global__ void __launch_bounds__(128, kLevels == 1 ? 8 : 5) k_extend(DScene sc, Soa s, int cur, int* err,
+                                                                       unsigned long long* stats) {
     const uint32_t count = s.counts[cur];
     const uint32_t* q = s.q_ray[cur];
     int e = 0;
@@ -215,7 +221,7 @@ __global__ void __launch_bounds__(128) k_extend(DScene sc, Soa s, int cur, int* 
     for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < count; i += gridDim.x * blockDim.x) {
         const uint32_t p = q[i];
         const float4 ro = s.ro[p], rd = s.rd[p];
-        const Hit h = scene_closest<kStats, kLevels>(sc, ld3(ro), ld3(rd), 0.001f, 10000.0f, tc, e);
+        const Hit h = scene_closest<kStats, kLevels, kAlpha>(sc, ld3(ro), ld3(rd), 0.001f, 10000.0f, tc, e);
         s.hit[p] = make_float4(h.t, h.u, h.v, __uint_as_float(h.prim));
         s.hit_inst[p] = h.inst;
         nr++;
@@ -332,6 +338,36 @@ __global__ void k_ray_keys(const LaunchBlock* lb, Soa s, int cur) {
     }
 }
 
+// Shading order by material (OHAO_PT_FLAG_SORT_MATERIAL): 8-bit key of each
+// queued path after its closest-hit query, so that k_shade's warps see
+// paths that take the same branches together: bit 7 miss, bits 6-5 the
+// path's phase (primary, specular chain, diffuse chain), then for hits bit
+// 4 metallic >= 0.5, bit 3 a textured material, bits 2-0 the roughness in
+// eighths. The stable sort keeps the queue order within a key.
+__global__ void k_material_keys(DScene sc, Soa s, int cur) {
+    const uint32_t count = s.counts[cur];
+    const uint32_t* q = s.q_ray[cur];
+    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < count; i += gridDim.x * blockDim.x) {
+        const uint32_t p = q[i];
+        const uint32_t phase = s.flags[p] & 3u;
+        const uint32_t prim = __float_as_uint(s.hit[p].w);
+        uint32_t key;
+        if (prim == 0xFFFFFFFFu) {
+            key = 0x80u | (phase << 5);
+        } else {
+            const DInst& in = sc.inst[s.hit_inst[p]];
+            const uint32_t mid = __ldg(sc.mat_ids + (__ldg(&in.custom) & 0xFFFFFFu) + prim);
+            const float4 m0 = __ldg(sc.mats + mid * 3), m1 = __ldg(sc.mats + mid * 3 + 1), m2 = __ldg(sc.mats + mid * 3 + 2);
+            const bool tex = (__float_as_uint(m0.w) & __float_as_uint(m1.z) & __float_as_uint(m1.w) &
+                              __float_as_uint(m2.x)) != 0xFFFFFFFFu;
+            const uint32_t rough = static_cast<uint32_t>(fminf(fmaxf(m1.x, 0.0f), 0.999f) * 8.0f);
+            key = (phase << 5) | (m1.y >= 0.5f ? 16u : 0u) | (tex ? 8u : 0u) | rough;
+        }
+        s.skA[i] = key;
+        s.svA[i] = p;
+    }
+}
+
 __global__ void k_copy_queue(Soa s, int cur) {
     const uint32_t count = s.counts[cur];
     for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < count; i += gridDim.x * blockDim.x)
@@ -349,7 +385,24 @@ __global__ void k_pool_init(Soa s, uint32_t cap) {
         s.counts[1] = 0;
         s.counts[3] = cap;
         s.counts[4] = 0;
+        s.counts[kCtrChunks] = 0;
     }
+}
+
+// End of one pool chunk inside the render's CUDA graph: the graph's while
+// loop runs another chunk until the work queue is drained (no path in
+// flight, nothing left to claim), and gives up after kMaxChunks chunks with
+// the queue-timeout error bit. No host round trip between chunks.
+__global__ void k_pool_continue(cudaGraphConditionalHandle loop, const LaunchBlock* lb, Soa s, int* err) {
+    const uint32_t pending = s.counts[0], done = s.counts[3], claimed = s.counts[4];
+    const bool drained = pending == 0 && done == 0 && claimed >= lb->total_pix;
+    const uint32_t chunks = ++s.counts[kCtrChunks];
+    bool more = !drained;
+    if (more && chunks >= kMaxChunks) {
+        atomicOr(err, kErrQueueTimeout);
+        more = false;
+    }
+    cudaGraphSetConditional(loop, more ? 1u : 0u);
 }
 
 // Pool regeneration (after the shadow pass of an iteration): a finished
@@ -422,8 +475,9 @@ __global__ void __launch_bounds__(128) k_regen(PathParams pp, const LaunchBlock*
 }
 
 // stats (profiling only): [3] shadow rays, [4] nodes, [5] triangles
-template <bool kStats, int kLevels>
-__global__ void __launch_bounds__(128) k_shadow(DScene sc, Soa s, int* err, unsigned long long* stats) {
+template <bool kStats, int kLevels, bool kAlpha>
+__global__ void __launch_bounds__(128, kLevels == 1 ? 8 : 5) k_shadow(DScene sc, Soa s, int* err,
+                                                                       unsigned long long* stats) {
     const uint32_t count = s.counts[2];
     int e = 0;
     TravCount tc{0, 0};
@@ -436,12 +490,12 @@ __global__ void __launch_bounds__(128) k_shadow(DScene sc, Soa s, int* err, unsi
         if (f & kFlagShL) {
             const float4 d = s.shL[p];
             nr++;
-            if (!scene_occluded<kStats, kLevels>(sc, org, ld3(d), 0.001f, d.w, tc, e)) rad = rad + ld3(s.shLc[p]);
+            if (!scene_occluded<kStats, kLevels, kAlpha>(sc, org, ld3(d), 0.001f, d.w, tc, e)) rad = rad + ld3(s.shLc[p]);
         }
         if (f & kFlagShE) {
             const float4 d = s.shE[p];
             nr++;
-            if (!scene_occluded<kStats, kLevels>(sc, org, ld3(d), 0.001f, d.w, tc, e)) rad = rad + ld3(s.shEc[p]);
+            if (!scene_occluded<kStats, kLevels, kAlpha>(sc, org, ld3(d), 0.001f, d.w, tc, e)) rad = rad + ld3(s.shEc[p]);
         }
         s.rad[p] = f4(rad, 0.0f);
         s.flags[p] = f & ~(kFlagShL | kFlagShE);
@@ -479,7 +533,7 @@ struct WarpFetch {
     }
 };
 
-template <bool kStats, int kLevels>
+template <bool kStats, int kLevels, bool kAlpha>
 __global__ void __launch_bounds__(128) k_extend_fetch(DScene sc, Soa s, int cur, int refill, int* err,
                                                       unsigned long long* stats) {
     const uint32_t count = s.counts[cur];
@@ -507,7 +561,7 @@ __global__ void __launch_bounds__(128) k_extend_fetch(DScene sc, Soa s, int cur,
             if (wf.drained) break;
             continue;
         }
-        if (active && walk_step<kLevels, kStats>(sc, w, r, 0.001f, 10000.0f, st_node, st_t, e, &tc)) {
+        if (active && walk_step<kLevels, kStats, kAlpha>(sc, w, r, 0.001f, 10000.0f, st_node, st_t, e, &tc)) {
             s.hit[p] = make_float4(w.best.t, w.best.u, w.best.v, __uint_as_float(w.best.prim));
             s.hit_inst[p] = w.best.inst;
             active = false;
@@ -528,7 +582,7 @@ __device__ __forceinline__ void start_shadow(const DScene& sc, const Soa& s, uin
     if (!(d.w > 0.001f)) w.have_node = false;   // the next step ends the walk unoccluded
 }
 
-template <bool kStats, int kLevels>
+template <bool kStats, int kLevels, bool kAlpha>
 __global__ void __launch_bounds__(128) k_shadow_fetch(DScene sc, Soa s, int refill, int* err,
                                                       unsigned long long* stats) {
     const uint32_t count = s.counts[2];
@@ -560,7 +614,7 @@ __global__ void __launch_bounds__(128) k_shadow_fetch(DScene sc, Soa s, int refi
             if (wf.drained) break;
             continue;
         }
-        if (active && probe_step<kLevels, kStats>(sc, w, r, 0.001f, tmax, st_node, e, &tc)) {
+        if (active && probe_step<kLevels, kStats, kAlpha>(sc, w, r, 0.001f, tmax, st_node, e, &tc)) {
             if (which == 0) visL = !w.hit;
             if (which == 0 && (f & kFlagShE)) {
                 which = 1;
@@ -623,12 +677,12 @@ __global__ void __launch_bounds__(128) k_trace(DScene sc, const float* __restric
         TravCount tc{0, 0};
         uint32_t* h = hits + static_cast<size_t>(i) * 5;
         if (any) {
-            const bool occ = stats ? scene_occluded<true>(sc, ld3(a), ld3(b), a.w, b.w, tc, e)
-                                   : scene_occluded<false>(sc, ld3(a), ld3(b), a.w, b.w, tc, e);
+            const bool occ = stats ? scene_occluded<true, 0, true>(sc, ld3(a), ld3(b), a.w, b.w, tc, e)
+                                   : scene_occluded<false, 0, true>(sc, ld3(a), ld3(b), a.w, b.w, tc, e);
             h[0] = occ ? 1u : 0u; h[1] = 0u; h[2] = 0u; h[3] = 0xFFFFFFFFu; h[4] = 0xFFFFFFFFu;
         } else {
-            const Hit r = stats ? scene_closest<true>(sc, ld3(a), ld3(b), a.w, b.w, tc, e)
-                                : scene_closest<false>(sc, ld3(a), ld3(b), a.w, b.w, tc, e);
+            const Hit r = stats ? scene_closest<true, 0, true>(sc, ld3(a), ld3(b), a.w, b.w, tc, e)
+                                : scene_closest<false, 0, true>(sc, ld3(a), ld3(b), a.w, b.w, tc, e);
             if (r.prim != 0xFFFFFFFFu) {
                 h[0] = __float_as_uint(r.t); h[1] = __float_as_uint(r.u); h[2] = __float_as_uint(r.v);
                 h[3] = r.inst; h[4] = r.prim;
@@ -708,15 +762,15 @@ void init_launch_shapes() {
     cudaDeviceGetAttribute(&g_num_sms, cudaDevAttrMultiProcessorCount, dev);
     if (g_num_sms <= 0) g_num_sms = 152;
     int b = 0;
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, k_extend<false, 1>, 128, 0);
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, k_extend<false, 1, false>, 128, 0);
     g_blocks_extend[0] = std::max(1, b) * g_num_sms;
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, k_extend<false, 2>, 128, 0);
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, k_extend<false, 2, false>, 128, 0);
     g_blocks_extend[1] = std::max(1, b) * g_num_sms;
     cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, k_shade<false>, 128, 0);
     g_blocks_shade = std::max(1, b) * g_num_sms;
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, k_shadow<false, 1>, 128, 0);
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, k_shadow<false, 1, false>, 128, 0);
     g_blocks_shadow[0] = std::max(1, b) * g_num_sms;
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, k_shadow<false, 2>, 128, 0);
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, k_shadow<false, 2, false>, 128, 0);
     g_blocks_shadow[1] = std::max(1, b) * g_num_sms;
     cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, k_trace, 128, 0);
     g_blocks_trace = std::max(1, b) * g_num_sms;
@@ -727,61 +781,61 @@ void init_launch_shapes() {
         g_blocks_extend[k] *= kTraversalWaves;
         g_blocks_shadow[k] *= kTraversalWaves;
     }
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, k_extend_fetch<false, 1>, 128, 0);
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, k_extend_fetch<false, 1, false>, 128, 0);
     g_blocks_fetch[0] = std::max(1, b) * g_num_sms;
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, k_extend_fetch<false, 2>, 128, 0);
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, k_extend_fetch<false, 2, false>, 128, 0);
     g_blocks_fetch[1] = std::max(1, b) * g_num_sms;
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, k_shadow_fetch<false, 1>, 128, 0);
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, k_shadow_fetch<false, 1, false>, 128, 0);
     g_blocks_fetch[2] = std::max(1, b) * g_num_sms;
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, k_shadow_fetch<false, 2>, 128, 0);
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, k_shadow_fetch<false, 2, false>, 128, 0);
     g_blocks_fetch[3] = std::max(1, b) * g_num_sms;
 }
 
-// persistent-warp closest-hit / any-hit kernels for the scene kind (the
-// caller zeroes the fetch counter first)
+// Kernel selection: statistics on/off x flat / two-level x alpha test
+// compiled in or not (opaque rays keep the traversal at its register count).
+#define OHAO_LAUNCH_TRAVERSAL(KERNEL, GRID, ...)                                                       \
+    do {                                                                                               \
+        const int lv = sc.two_level ? 2 : 1;                                                           \
+        const bool al = sc.alpha_test != 0;                                                            \
+        if (stats) {                                                                                   \
+            if (lv == 2) { if (al) KERNEL<true, 2, true><<<GRID[1], 128, 0, st>>>(__VA_ARGS__);         \
+                           else KERNEL<true, 2, false><<<GRID[1], 128, 0, st>>>(__VA_ARGS__); }        \
+            else { if (al) KERNEL<true, 1, true><<<GRID[0], 128, 0, st>>>(__VA_ARGS__);                 \
+                   else KERNEL<true, 1, false><<<GRID[0], 128, 0, st>>>(__VA_ARGS__); }                \
+        } else {                                                                                       \
+            if (lv == 2) { if (al) KERNEL<false, 2, true><<<GRID[1], 128, 0, st>>>(__VA_ARGS__);        \
+                           else KERNEL<false, 2, false><<<GRID[1], 128, 0, st>>>(__VA_ARGS__); }       \
+            else { if (al) KERNEL<false, 1, true><<<GRID[0], 128, 0, st>>>(__VA_ARGS__);                \
+                   else KERNEL<false, 1, false><<<GRID[0], 128, 0, st>>>(__VA_ARGS__); }               \
+        }                                                                                              \
+    } while (0)
+
+// persistent-warp closest-hit / any-hit kernels (the caller zeroes the
+// fetch counters first)
 void launch_extend_fetch(const DScene& sc, const Soa& s, int cur, int refill, int* d_err, unsigned long long* stats,
                          cudaStream_t st) {
-    const int two = sc.two_level ? 1 : 0;
-    if (stats) {
-        if (two) k_extend_fetch<true, 2><<<g_blocks_fetch[1], 128, 0, st>>>(sc, s, cur, refill, d_err, stats);
-        else k_extend_fetch<true, 1><<<g_blocks_fetch[0], 128, 0, st>>>(sc, s, cur, refill, d_err, stats);
-    } else {
-        if (two) k_extend_fetch<false, 2><<<g_blocks_fetch[1], 128, 0, st>>>(sc, s, cur, refill, d_err, nullptr);
-        else k_extend_fetch<false, 1><<<g_blocks_fetch[0], 128, 0, st>>>(sc, s, cur, refill, d_err, nullptr);
-    }
+    OHAO_LAUNCH_TRAVERSAL(k_extend_fetch, g_blocks_fetch, sc, s, cur, refill, d_err, stats);
 }
 void launch_shadow_fetch(const DScene& sc, const Soa& s, int refill, int* d_err, unsigned long long* stats,
                          cudaStream_t st) {
-    const int two = sc.two_level ? 1 : 0;
-    if (stats) {
-        if (two) k_shadow_fetch<true, 2><<<g_blocks_fetch[3], 128, 0, st>>>(sc, s, refill, d_err, stats);
-        else k_shadow_fetch<true, 1><<<g_blocks_fetch[2], 128, 0, st>>>(sc, s, refill, d_err, stats);
-    } else {
-        if (two) k_shadow_fetch<false, 2><<<g_blocks_fetch[3], 128, 0, st>>>(sc, s, refill, d_err, nullptr);
-        else k_shadow_fetch<false, 1><<<g_blocks_fetch[2], 128, 0, st>>>(sc, s, refill, d_err, nullptr);
-    }
+    OHAO_LAUNCH_TRAVERSAL(k_shadow_fetch, (g_blocks_fetch + 2), sc, s, refill, d_err, stats);
 }
-
-// closest-hit / any-hit kernels specialised for the scene kind
+// one-ray-per-thread closest-hit / any-hit kernels
 void launch_extend(const DScene& sc, const Soa& s, int cur, int* d_err, unsigned long long* stats, cudaStream_t st) {
-    const int two = sc.two_level ? 1 : 0;
-    if (stats) {
-        if (two) k_extend<true, 2><<<g_blocks_extend[1], 128, 0, st>>>(sc, s, cur, d_err, stats);
-        else k_extend<true, 1><<<g_blocks_extend[0], 128, 0, st>>>(sc, s, cur, d_err, stats);
-    } else {
-        if (two) k_extend<false, 2><<<g_blocks_extend[1], 128, 0, st>>>(sc, s, cur, d_err, nullptr);
-        else k_extend<false, 1><<<g_blocks_extend[0], 128, 0, st>>>(sc, s, cur, d_err, nullptr);
-    }
+    OHAO_LAUNCH_TRAVERSAL(k_extend, g_blocks_extend, sc, s, cur, d_err, stats);
 }
 void launch_shadow(const DScene& sc, const Soa& s, int* d_err, unsigned long long* stats, cudaStream_t st) {
-    const int two = sc.two_level ? 1 : 0;
-    if (stats) {
-        if (two) k_shadow<true, 2><<<g_blocks_shadow[1], 128, 0, st>>>(sc, s, d_err, stats);
-        else k_shadow<true, 1><<<g_blocks_shadow[0], 128, 0, st>>>(sc, s, d_err, stats);
-    } else {
-        if (two) k_shadow<false, 2><<<g_blocks_shadow[1], 128, 0, st>>>(sc, s, d_err, nullptr);
-        else k_shadow<false, 1><<<g_blocks_shadow[0], 128, 0, st>>>(sc, s, d_err, nullptr);
-    }
+    OHAO_LAUNCH_TRAVERSAL(k_shadow, g_blocks_shadow, sc, s, d_err, stats);
+}
+
+constexpr uint32_t kFlagSortMaterial = OHAO_PT_FLAG_SORT_MATERIAL;
+
+// Reorders ray queue `cur` by the material key of k_material_keys (two
+// 4-bit radix passes; the sorted pairs end in skA/svA).
+void sort_queue_by_material(const DScene& sc, const Soa& s, int cur, uint32_t cap, cudaStream_t st) {
+    k_material_keys<<<g_blocks_shade, 128, 0, st>>>(sc, s, cur);
+    rsort::sort_pairs(s.skA, s.svA, s.skB, s.svB, s.shist, s.counts + cur, cap, 8, st);
+    k_copy_queue<<<g_blocks_shade, 128, 0, st>>>(s, cur);
 }
 
 struct EvTimer {
@@ -866,6 +920,11 @@ ohao_status wavefront_render(const DScene& sc, const RenderView& view, const Pat
             if (fetch) launch_extend_fetch(sc, s, cur, static_cast<int>(pp.refill), d_err, profile ? dstats : nullptr, st);
             else launch_extend(sc, s, cur, d_err, profile ? dstats : nullptr, st);
             tm.end(0, a);
+            if (pp.flags & kFlagSortMaterial) {
+                tm.begin(3, a);
+                sort_queue_by_material(sc, s, cur, capacity, st);
+                tm.end(3, a);
+            }
             cudaMemsetAsync(s.counts + (cur ^ 1), 0, 4, st);
             cudaMemsetAsync(s.counts + 2, 0, 4, st);
             tm.begin(1, a);
@@ -929,10 +988,12 @@ ohao_status trace_rays(const DScene& sc, const float* rays, uint32_t n, uint32_t
 // regenerate -> extend -> shade -> shadow, where regenerate folds finished
 // paths into their pixel's running mean (samples of a pixel stay in one slot,
 // in sample order, so the result equals the per-view wavefront bit for bit)
-// and refills idle slots from the queue. A chunk of kChunk iterations is
-// captured once into a CUDA graph and replayed until the queue is drained;
-// the host reads four counters between chunks. The autotuner picks the pool
-// capacity.
+// and refills idle slots from the queue. A render is one CUDA graph launch:
+// a conditional while node whose body is a chunk of kChunk iterations and a
+// one-thread kernel that decides on the device whether another chunk is
+// needed (no host round trip). Where the driver refuses conditional nodes,
+// one chunk per graph is replayed from the host, which reads four counters
+// between chunks. The autotuner picks the pool shape.
 // ---------------------------------------------------------------------------
 namespace {
 constexpr int kChunk = 8;                       // iterations per graph replay (even)
@@ -950,7 +1011,6 @@ const PoolVariant kPool[] = {
 };
 constexpr int kNumPool = sizeof(kPool) / sizeof(kPool[0]);
 constexpr int kDefaultPool = 1;
-constexpr uint64_t kMaxChunks = 1u << 20;       // bound on graph replays per call
 }  // namespace
 
 struct PersistentState {
@@ -962,6 +1022,7 @@ struct PersistentState {
     uint32_t cap = 0;
     int variant = -1;
     cudaGraphExec_t graph = nullptr;
+    bool graph_whole = false;                   // the graph holds the whole render (device while loop)
     DScene graph_scene{};
     PathParams graph_pp{};
     int* graph_err = nullptr;
@@ -1066,6 +1127,7 @@ void enqueue_chunk(const DScene& sc, const PathParams& pp, const LaunchBlock* lb
         } else {
             launch_extend(sc, s, cur, d_err, nullptr, st);
         }
+        if (pp.flags & kFlagSortMaterial) sort_queue_by_material(sc, s, cur, cap, st);
         cudaMemsetAsync(s.counts + (cur ^ 1), 0, 4, st);
         cudaMemsetAsync(s.counts + 2, 0, 8, st);   // shadow and done counts
         k_shade<true><<<g_blocks_shade, 128, 0, st>>>(sc, pp, ViewParams{}, 0u, 1u, s, cur, nullptr, 0u, lb);
@@ -1106,11 +1168,43 @@ ohao_status run_pool(PersistentState* s, int variant, const DScene& sc, const Pa
                 err = "persistent: capture stream";
                 return OHAO_ERR_CUDA;
             }
+            // The whole render as one graph: a conditional while node whose
+            // body is one chunk followed by k_pool_continue.
+            s->graph_whole = false;
             cudaGraph_t g = nullptr;
-            cudaStreamBeginCapture(cap_st, cudaStreamCaptureModeThreadLocal);
-            enqueue_chunk(sc, pp, s->d_lb, soa, cap, kPool[variant], d_err, cap_st);
-            cudaError_t e = cudaStreamEndCapture(cap_st, &g);
+            cudaError_t e = cudaGraphCreate(&g, 0);
+            cudaGraphConditionalHandle loop{};
+            if (e == cudaSuccess) e = cudaGraphConditionalHandleCreate(&loop, g, 1u, cudaGraphCondAssignDefault);
+            cudaGraphNodeParams cp{};
+            cp.type = cudaGraphNodeTypeConditional;
+            cp.conditional.handle = loop;
+            cp.conditional.type = cudaGraphCondTypeWhile;
+            cp.conditional.size = 1;
+            cudaGraphNode_t node = nullptr;
+            if (e == cudaSuccess) e = cudaGraphAddNode(&node, g, nullptr, nullptr, 0, &cp);
+            if (e == cudaSuccess) {
+                cudaGraph_t body = cp.conditional.phGraph_out[0];
+                e = cudaStreamBeginCaptureToGraph(cap_st, body, nullptr, nullptr, 0, cudaStreamCaptureModeThreadLocal);
+                if (e == cudaSuccess) {
+                    enqueue_chunk(sc, pp, s->d_lb, soa, cap, kPool[variant], d_err, cap_st);
+                    k_pool_continue<<<1, 1, 0, cap_st>>>(loop, s->d_lb, soa, d_err);
+                    cudaGraph_t captured = nullptr;
+                    e = cudaStreamEndCapture(cap_st, &captured);
+                }
+            }
             if (e == cudaSuccess) e = cudaGraphInstantiate(&s->graph, g, 0);
+            if (e == cudaSuccess) {
+                s->graph_whole = true;
+            } else {
+                // fall back to one chunk per graph, replayed from the host
+                cudaGetLastError();
+                s->graph = nullptr;
+                if (g) { cudaGraphDestroy(g); g = nullptr; }
+                cudaStreamBeginCapture(cap_st, cudaStreamCaptureModeThreadLocal);
+                enqueue_chunk(sc, pp, s->d_lb, soa, cap, kPool[variant], d_err, cap_st);
+                e = cudaStreamEndCapture(cap_st, &g);
+                if (e == cudaSuccess) e = cudaGraphInstantiate(&s->graph, g, 0);
+            }
             if (g) cudaGraphDestroy(g);
             cudaStreamDestroy(cap_st);
             if (e != cudaSuccess) {
@@ -1122,6 +1216,11 @@ ohao_status run_pool(PersistentState* s, int variant, const DScene& sc, const Pa
             s->graph_err = d_err;
             s->graph_scene = sc;
             s->graph_pp = pp;
+        }
+        if (s->graph_whole) {   // one launch renders every view; completion is stream-ordered
+            const cudaError_t e = cudaGraphLaunch(s->graph, st);
+            if (e != cudaSuccess) { err = std::string("persistent graph launch: ") + cudaGetErrorString(e); return OHAO_ERR_CUDA; }
+            return OHAO_OK;
         }
     }
     for (uint64_t chunk = 0;; ++chunk) {

@@ -366,3 +366,39 @@ def test_degenerate_view_sizes(gpu_lib, oracle, two_level):
         torch.cuda.synchronize()
         for k in range(len(sd.views)):
             assert np.array_equal(accs[k].cpu().numpy(), ref[k]), f"{name} view {sizes[k]}"
+
+
+@pytest.mark.parametrize("two_level", [False, True])
+def test_traversal_shapes_and_material_sort_same_image(gpu_lib, two_level):
+    """The per-view wavefront in every traversal shape (one ray per thread;
+    persistent warps refilled at 1, 4 or 16 idle lanes) and with the
+    material-sorted shading order, and the persistent pool with the material
+    sort: accumulators bit-identical, closest-hit visit counts identical."""
+    import torch
+    og = gpu_lib
+    sd = small_instanced(side=24) if two_level else small_env_scene(freq=16)
+    fl = 1 if two_level else 0
+    pt = gpu_tracer(og, sd, flatten_limit=fl)
+    v = sd.views[0]
+    ref, ref_counts = None, None
+    for refill in (33, 1, 4, 16):
+        for flags in (0, og.FLAG_SORT_MATERIAL):
+            acc = torch.zeros((v.width * v.height, 4), dtype=torch.float32, device="cuda")
+            pt.render([og.make_view(v, accum=acc)],
+                      og.make_settings(spp=3, max_bounces=4, sampler=1, wavefront_refill=refill,
+                                       flags=flags | og.FLAG_PROFILE, mode=og.MODE_WAVEFRONT))
+            torch.cuda.synchronize()
+            p = pt.profile()
+            counts = (p.rays_closest, p.nodes_closest, p.tris_closest, p.rays_shadow)
+            if ref is None:
+                ref, ref_counts = acc.clone(), counts
+            assert torch.equal(acc, ref), f"refill {refill} flags {flags}"
+            assert counts == ref_counts, f"refill {refill} flags {flags}: {counts} != {ref_counts}"
+    for name in ("pool_2M_sorted_chunk8", "pool_4M_unsorted_fetch4_chunk8"):
+        pt.launch_config = name
+        accs = [torch.zeros((v.width * v.height, 4), dtype=torch.float32, device="cuda") for _ in range(2)]
+        pt.render([og.make_view(v, accum=a) for a in accs],
+                  og.make_settings(spp=3, max_bounces=4, sampler=1, flags=og.FLAG_SORT_MATERIAL,
+                                   mode=og.MODE_PERSISTENT))
+        torch.cuda.synchronize()
+        assert torch.equal(accs[0], ref) and torch.equal(accs[1], ref), name
