@@ -143,7 +143,8 @@ OHAO_D bool walk_step(const DScene& sc, Walk& w, const RayPre& r, float tmin, fl
             }
             const uint32_t rem = hit & imask;
             if (rem) {
-                if (!order_children(rem, tn, n, st_node, st_t, w.sp, w.cur, w.cur_tn, stack_limit(sc))) {
+                ArrStack ast{st_node, st_t};
+                if (!order_children(rem, tn, n, ast, w.sp, w.cur, w.cur_tn, stack_limit(sc))) {
                     err = 1;
                     return true;
                 }

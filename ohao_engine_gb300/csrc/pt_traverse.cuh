@@ -55,6 +55,52 @@ struct NodeRec {
     uint4 q0, q1, q2, q3, q4;
 };
 
+// Traversal stack of (node, t_near) entries. The first kSh entries of a ray
+// live in shared memory -- one column per thread, entry i at
+// sh[i * kShStride], so a warp's accesses are conflict-free whatever mix of
+// depths its lanes are at -- and the rest in local memory. kSh = 0 keeps the
+// whole stack in local memory.
+constexpr int kShStride = 128;   // threads per block of the traversal kernels
+template <int kSh>
+struct TravStack {
+    uint2* sh;
+    uint32_t ln[kStackSize - kSh];
+    float lt[kStackSize - kSh];
+    OHAO_D void put(int i, uint32_t n, float t) {
+        if (kSh > 0 && i < kSh) {
+            sh[i * kShStride] = make_uint2(n, __float_as_uint(t));
+        } else {
+            ln[i - kSh] = n;
+            lt[i - kSh] = t;
+        }
+    }
+    OHAO_D void get(int i, uint32_t& n, float& t) const {
+        if (kSh > 0 && i < kSh) {
+            const uint2 e = sh[i * kShStride];
+            n = e.x;
+            t = __uint_as_float(e.y);
+        } else {
+            n = ln[i - kSh];
+            t = lt[i - kSh];
+        }
+    }
+    OHAO_D void put_node(int i, uint32_t n) {
+        if (kSh > 0 && i < kSh) sh[i * kShStride].x = n;
+        else ln[i - kSh] = n;
+    }
+    OHAO_D uint32_t get_node(int i) const { return (kSh > 0 && i < kSh) ? sh[i * kShStride].x : ln[i - kSh]; }
+};
+
+// The same interface over two caller-owned local arrays.
+struct ArrStack {
+    uint32_t* node;
+    float* t;
+    OHAO_D void put(int i, uint32_t n, float tn) { node[i] = n; t[i] = tn; }
+    OHAO_D void get(int i, uint32_t& n, float& tn) const { n = node[i]; tn = t[i]; }
+    OHAO_D void put_node(int i, uint32_t n) { node[i] = n; }
+    OHAO_D uint32_t get_node(int i) const { return node[i]; }
+};
+
 OHAO_D NodeRec load_node(const uint4* __restrict__ nodes, uint32_t ni) {
     const uint4* p = nodes + static_cast<size_t>(ni) * 5;
     NodeRec n;
@@ -140,8 +186,9 @@ OHAO_D float pick8(const float v[8], int i) {
 // Orders the internal children `rem`: pushes all but the nearest (far first,
 // ties: lower slot first) and returns the nearest in (cur, cur_tn).
 // Returns false on stack overflow.
-OHAO_D bool order_children(uint32_t rem, const float tn[8], const NodeRec& n, uint32_t* st_node, float* st_t, int& sp,
-                           uint32_t& cur, float& cur_tn, int lim) {
+template <class Stack>
+OHAO_D bool order_children(uint32_t rem, const float tn[8], const NodeRec& n, Stack& stk, int& sp, uint32_t& cur,
+                           float& cur_tn, int lim) {
     while (__popc(rem) > 1) {
         float bt = 0.0f;
         int bi = -1;
@@ -149,8 +196,7 @@ OHAO_D bool order_children(uint32_t rem, const float tn[8], const NodeRec& n, ui
         for (int i = 0; i < 8; ++i)
             if (((rem >> i) & 1u) && (bi < 0 || tn[i] > bt)) { bt = tn[i]; bi = i; }
         if (sp >= lim) return false;
-        st_node[sp] = n.q1.x + (byte_of(n.q1.z, n.q1.w, bi) & 7u);
-        st_t[sp] = bt;
+        stk.put(sp, n.q1.x + (byte_of(n.q1.z, n.q1.w, bi) & 7u), bt);
         sp++;
         rem &= ~(1u << bi);
     }
@@ -161,10 +207,10 @@ OHAO_D bool order_children(uint32_t rem, const float tn[8], const NodeRec& n, ui
 }
 
 // Closest hit in one BVH (flat, or a BLAS inside instance inst_override).
-template <bool kStats, bool kAlpha = false>
+template <bool kStats, bool kAlpha, class Stack>
 OHAO_D void bvh_closest(const DScene& sc, const uint4* __restrict__ nodes, const float4* __restrict__ tris,
-                        const RayPre& r, float tmin, float tmax, Hit& best, uint32_t inst_override, uint32_t* st_node,
-                        float* st_t, int stack_base, int lim, TravCount& cnt, int& err) {
+                        const RayPre& r, float tmin, float tmax, Hit& best, uint32_t inst_override, Stack& stk,
+                        int stack_base, int lim, TravCount& cnt, int& err) {
     if (stack_base >= lim) { err = 1; return; }
     int sp = stack_base;
     uint32_t cur = 0u;
@@ -200,21 +246,20 @@ OHAO_D void bvh_closest(const DScene& sc, const uint4* __restrict__ nodes, const
             }
             const uint32_t rem = hit & imask;
             if (rem) {
-                if (!order_children(rem, tn, n, st_node, st_t, sp, cur, cur_tn, lim)) { err = 1; return; }
+                if (!order_children(rem, tn, n, stk, sp, cur, cur_tn, lim)) { err = 1; return; }
                 continue;
             }
         }
         if (sp == stack_base) return;
         sp--;
-        cur = st_node[sp];
-        cur_tn = st_t[sp];
+        stk.get(sp, cur, cur_tn);
     }
 }
 
 // Any hit in one BVH.
-template <bool kStats, bool kAlpha = false>
+template <bool kStats, bool kAlpha, class Stack>
 OHAO_D bool bvh_any(const DScene& sc, const uint4* __restrict__ nodes, const float4* __restrict__ tris, const RayPre& r,
-                    float tmin, float tmax, uint32_t* st_node, int stack_base, int lim, TravCount& cnt, int& err) {
+                    float tmin, float tmax, Stack& stk, int stack_base, int lim, TravCount& cnt, int& err) {
     if (stack_base >= lim) { err = 1; return false; }
     int sp = stack_base;
     uint32_t cur = 0u;
@@ -249,14 +294,14 @@ OHAO_D bool bvh_any(const DScene& sc, const uint4* __restrict__ nodes, const flo
                 for (int i = 0; i < 8; ++i)
                     if (((rem >> i) & 1u) && (bi < 0 || tn[i] > bt)) { bt = tn[i]; bi = i; }
                 if (sp >= lim) { err = 1; return false; }
-                st_node[sp++] = n.q1.x + (byte_of(n.q1.z, n.q1.w, bi) & 7u);
+                stk.put_node(sp++, n.q1.x + (byte_of(n.q1.z, n.q1.w, bi) & 7u));
                 rem &= ~(1u << bi);
             }
             cur = n.q1.x + (byte_of(n.q1.z, n.q1.w, __ffs(rem) - 1) & 7u);
             continue;
         }
         if (sp == stack_base) return false;
-        cur = st_node[--sp];
+        cur = stk.get_node(--sp);
     }
 }
 
@@ -277,20 +322,26 @@ OHAO_D void xform_dir(const float m[12], V3 d, V3& o) {
 // traversal at its own register count).
 // kAlpha: rays without gl_RayFlagsOpaqueEXT are possible (the alpha test
 // of non-opaque instances is compiled in; it runs when sc.alpha_test).
-template <bool kStats, int kLevels = 0, bool kAlpha = false>
-OHAO_D Hit scene_closest(const DScene& sc, V3 o, V3 d, float tmin, float tmax, TravCount& cnt, int& err) {
+// kSh: stack entries of a flat traversal kept in shared memory (sh: this
+// thread's column; the two-level traversal keeps its stack in local memory).
+template <bool kStats, int kLevels = 0, bool kAlpha = false, int kSh = 0>
+OHAO_D Hit scene_closest(const DScene& sc, V3 o, V3 d, float tmin, float tmax, TravCount& cnt, int& err,
+                         uint2* sh = nullptr) {
     Hit best;
     best.t = 0.0f; best.u = 0.0f; best.v = 0.0f;
     best.inst = 0xFFFFFFFFu; best.prim = 0xFFFFFFFFu;
     if (!(tmax > tmin) || sc.nnodes == 0) return best;
-    uint32_t st_node[kStackSize];
-    float st_t[kStackSize];
     const RayPre r = ray_pre(o, d);
     if (kLevels == 1 || (kLevels == 0 && !sc.two_level)) {
-        bvh_closest<kStats, kAlpha>(sc, sc.nodes, sc.tris, r, tmin, tmax, best, 0xFFFFFFFFu, st_node, st_t, 0, stack_limit(sc),
-                            cnt, err);
+        TravStack<kSh> stk;
+        stk.sh = sh;
+        bvh_closest<kStats, kAlpha>(sc, sc.nodes, sc.tris, r, tmin, tmax, best, 0xFFFFFFFFu, stk, 0, stack_limit(sc),
+                                    cnt, err);
         return best;
     }
+    uint32_t st_node[kStackSize];
+    float st_t[kStackSize];
+    ArrStack ast{st_node, st_t};
     // Two-level: one loop whose every iteration visits one node (TLAS or
     // BLAS) or enters one instance, so the lanes of a warp stay on the same
     // code whatever level each ray is in. Order of visits per ray: at a TLAS
@@ -352,7 +403,7 @@ OHAO_D Hit scene_closest(const DScene& sc, V3 o, V3 d, float tmin, float tmax, T
                 }
                 const uint32_t rem = hit & imask;
                 if (rem) {
-                    if (!order_children(rem, tn, n, st_node, st_t, sp, cur, cur_tn, stack_limit(sc))) {
+                    if (!order_children(rem, tn, n, ast, sp, cur, cur_tn, stack_limit(sc))) {
                         err = 1;
                         return best;
                     }
@@ -426,13 +477,17 @@ OHAO_D Hit scene_closest(const DScene& sc, V3 o, V3 d, float tmin, float tmax, T
     }
 }
 
-template <bool kStats, int kLevels = 0, bool kAlpha = false>
-OHAO_D bool scene_occluded(const DScene& sc, V3 o, V3 d, float tmin, float tmax, TravCount& cnt, int& err) {
+template <bool kStats, int kLevels = 0, bool kAlpha = false, int kSh = 0>
+OHAO_D bool scene_occluded(const DScene& sc, V3 o, V3 d, float tmin, float tmax, TravCount& cnt, int& err,
+                           uint2* sh = nullptr) {
     if (!(tmax > tmin) || sc.nnodes == 0) return false;
-    uint32_t st_node[kStackSize];
     const RayPre r = ray_pre(o, d);
-    if (kLevels == 1 || (kLevels == 0 && !sc.two_level))
-        return bvh_any<kStats, kAlpha>(sc, sc.nodes, sc.tris, r, tmin, tmax, st_node, 0, stack_limit(sc), cnt, err);
+    if (kLevels == 1 || (kLevels == 0 && !sc.two_level)) {
+        TravStack<kSh> stk;
+        stk.sh = sh;
+        return bvh_any<kStats, kAlpha>(sc, sc.nodes, sc.tris, r, tmin, tmax, stk, 0, stack_limit(sc), cnt, err);
+    }
+    uint32_t st_node[kStackSize];
     // Two-level, as one loop (see scene_closest): at a TLAS node the internal
     // children but the last (slot order) are pushed, its instance leaves are
     // entered in slot order, then the last internal child is visited.

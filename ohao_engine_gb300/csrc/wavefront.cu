@@ -209,19 +209,24 @@ __device__ __forceinline__ void add_stats(unsigned long long* dst, uint32_t rays
 // stats (profiling only): [0] rays, [1] nodes, [2] triangles
 // kLevels: 1 = flat BVH, 2 = two-level (one kernel per scene kind).
 // Registers capped for 8 resident blocks per SM on flat scenes (64
-// registers), 5 on two-level ones.
+// registers), 5 on two-level ones. On flat scenes the first
+// kShStackEntries stack entries of each ray live in shared memory.
+constexpr int kShStackEntries = 8;
 template <bool kStats, int kLevels, bool kAlpha>
 __global__ void __launch_bounds__(128, kLevels == 1 ? 8 : 5) k_extend(DScene sc, Soa s, int cur, int* err,
                                                                        unsigned long long* stats) {
     const uint32_t count = s.counts[cur];
     const uint32_t* q = s.q_ray[cur];
+    constexpr int kSh = kLevels == 1 ? kShStackEntries : 0;
+    __shared__ uint2 s_stack[kSh > 0 ? kSh * kShStride : 1];
     int e = 0;
     TravCount tc{0, 0};
     uint32_t nr = 0;
     for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < count; i += gridDim.x * blockDim.x) {
         const uint32_t p = q[i];
         const float4 ro = s.ro[p], rd = s.rd[p];
-        const Hit h = scene_closest<kStats, kLevels, kAlpha>(sc, ld3(ro), ld3(rd), 0.001f, 10000.0f, tc, e);
+        const Hit h = scene_closest<kStats, kLevels, kAlpha, kSh>(sc, ld3(ro), ld3(rd), 0.001f, 10000.0f, tc, e,
+                                                                  s_stack + threadIdx.x);
         s.hit[p] = make_float4(h.t, h.u, h.v, __uint_as_float(h.prim));
         s.hit_inst[p] = h.inst;
         nr++;
@@ -479,6 +484,8 @@ template <bool kStats, int kLevels, bool kAlpha>
 __global__ void __launch_bounds__(128, kLevels == 1 ? 8 : 5) k_shadow(DScene sc, Soa s, int* err,
                                                                        unsigned long long* stats) {
     const uint32_t count = s.counts[2];
+    constexpr int kSh = kLevels == 1 ? kShStackEntries : 0;
+    __shared__ uint2 s_stack[kSh > 0 ? kSh * kShStride : 1];
     int e = 0;
     TravCount tc{0, 0};
     uint32_t nr = 0;
@@ -490,12 +497,14 @@ __global__ void __launch_bounds__(128, kLevels == 1 ? 8 : 5) k_shadow(DScene sc,
         if (f & kFlagShL) {
             const float4 d = s.shL[p];
             nr++;
-            if (!scene_occluded<kStats, kLevels, kAlpha>(sc, org, ld3(d), 0.001f, d.w, tc, e)) rad = rad + ld3(s.shLc[p]);
+            if (!scene_occluded<kStats, kLevels, kAlpha, kSh>(sc, org, ld3(d), 0.001f, d.w, tc, e, s_stack + threadIdx.x))
+                rad = rad + ld3(s.shLc[p]);
         }
         if (f & kFlagShE) {
             const float4 d = s.shE[p];
             nr++;
-            if (!scene_occluded<kStats, kLevels, kAlpha>(sc, org, ld3(d), 0.001f, d.w, tc, e)) rad = rad + ld3(s.shEc[p]);
+            if (!scene_occluded<kStats, kLevels, kAlpha, kSh>(sc, org, ld3(d), 0.001f, d.w, tc, e, s_stack + threadIdx.x))
+                rad = rad + ld3(s.shEc[p]);
         }
         s.rad[p] = f4(rad, 0.0f);
         s.flags[p] = f & ~(kFlagShL | kFlagShE);
