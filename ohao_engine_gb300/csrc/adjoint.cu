@@ -390,7 +390,7 @@ __device__ ChainOut replay_chain(const DScene& sc, const PathParams& pp, Rng& rn
             break;
         }
         Surf s;
-        hit_shade(sc, ro, rd, h, s);
+        hit_shade<false>(sc, ro, rd, h, s);
         LocalMat lm;
         local_mat(sc, s, lm, R.pv);
         D3 G = d3c(length(s.color) > 0.001f ? s.color : v3s(0.0f));
@@ -573,7 +573,7 @@ __global__ void __launch_bounds__(128) k_adjoint(const __grid_constant__ DScene 
         const Hit h = ah.h;
         if (h.prim == 0xFFFFFFFFu) continue;   // primary miss: no parameter dependence
         Surf s0;
-        hit_shade(sc, ps.ro, ps.rd, h, s0);
+        hit_shade<false>(sc, ps.ro, ps.rd, h, s0);
         LocalMat m0;
         Prov p0;
         local_mat(sc, s0, m0, p0);

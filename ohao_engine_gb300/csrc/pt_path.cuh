@@ -206,6 +206,9 @@ OHAO_D V3 albedo_map_sample(const float* __restrict__ map, uint32_t mw, uint32_t
     return v3(out[0], out[1], out[2]);
 }
 // pt_closesthit.rchit:37-162
+// kTex: bindless textures compiled in (scenes without them keep the shading
+// step at its register count; the tile albedo map is read either way).
+template <bool kTex = true>
 OHAO_D void hit_shade(const DScene& sc, V3 o, V3 d, const Hit& h, Surf& s) {
     s.hit = true;
     const float t = h.t;
@@ -257,14 +260,14 @@ OHAO_D void hit_shade(const DScene& sc, V3 o, V3 d, const Hit& h, Surf& s) {
     if (dtex != kNone) {
         if (dtex == 0u && sc.map_w > 0) {
             alb = alb * albedo_map_sample(sc.albedo_map, sc.map_w, sc.map_h, s.tu, s.tv);
-        } else {
+        } else if (kTex) {
             const float4 c = tex_sample(sc, dtex, s.tu, s.tv);
             alb = alb * v3(pow_def(c.x, 2.2f), pow_def(c.y, 2.2f), pow_def(c.z, 2.2f));
         }
     }
     // tangent-space normal map in the Frisvad basis of the shading normal
     // (pt_closesthit.rchit:116-133)
-    if (ntex != kNone) {
+    if (kTex && ntex != kNone) {
         const float4 c = tex_sample(sc, ntex, s.tu, s.tv);
         const V3 mapN = normalize(v3(c.x * 2.0f - 1.0f, c.y * 2.0f - 1.0f, c.z * 2.0f - 1.0f));
         V3 T, B;
@@ -284,7 +287,7 @@ OHAO_D void hit_shade(const DScene& sc, V3 o, V3 d, const Hit& h, Surf& s) {
     // roughness / metallic factors from the ORM texture's G and B
     // (pt_closesthit.rchit:139-148)
     float rough = m1.x, metal = m1.y;
-    if (rmtex != kNone) {
+    if (kTex && rmtex != kNone) {
         const float4 c = tex_sample(sc, rmtex, s.tu, s.tv);
         rough = rough * c.y;
         metal = metal * c.z;
@@ -293,7 +296,7 @@ OHAO_D void hit_shade(const DScene& sc, V3 o, V3 d, const Hit& h, Surf& s) {
     // emission: the sRGB-decoded emissive texture (pt_closesthit.rchit:150-156)
     // plus the material's slot-2 emission (not the reference's)
     V3 emis = v3s(0.0f);
-    if (etex != kNone) {
+    if (kTex && etex != kNone) {
         const float4 c = tex_sample(sc, etex, s.tu, s.tv);
         emis = v3(pow_def(c.x, 2.2f), pow_def(c.y, 2.2f), pow_def(c.z, 2.2f));
     }
@@ -701,6 +704,7 @@ OHAO_D void start_diffuse_chain(const PathParams& pp, Rng& rng, uint32_t& dim, P
 // One step: consume the closest-hit result of the path's current ray, add
 // the radiance terms the shader adds here, emit up to two shadow queries and
 // set up the next ray (or finish). Returns true when a next ray is pending.
+template <bool kTex = true>
 OHAO_D bool path_step(const DScene& sc, const PathParams& pp, const ViewParams& vw, uint32_t px, uint32_t py,
                       uint32_t sidx, PathState& ps, const Hit& h, ShadowReq& qL, ShadowReq& qE, AovOut* aov) {
     qL.valid = false;
@@ -708,7 +712,7 @@ OHAO_D bool path_step(const DScene& sc, const PathParams& pp, const ViewParams& 
     Rng rng = make_rng(pp, px, py, sidx, ps.rng);
     uint32_t dim = ps.dim;
     Surf s;
-    if (h.prim != 0xFFFFFFFFu) hit_shade(sc, ps.ro, ps.rd, h, s);
+    if (h.prim != 0xFFFFFFFFu) hit_shade<kTex>(sc, ps.ro, ps.rd, h, s);
     else miss_shade(sc, pp, ps.rd, s);
 
     if (ps.phase == kPhasePrimary) {

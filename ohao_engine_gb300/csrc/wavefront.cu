@@ -242,7 +242,7 @@ __global__ void __launch_bounds__(128, kLevels == 1 ? 8 : 5) k_extend(DScene sc,
 // (scene and state loads, 21% of issue slots at 128 registers and 4 blocks),
 // and 32 warps hide more of it than the spills cost (sphere_1m: 376 -> 402
 // Msamples/s; 10 or 12 blocks gain under 1% more).
-template <bool kPool>
+template <bool kPool, bool kTex>
 __global__ void __launch_bounds__(128, 8) k_shade(DScene sc, PathParams pp, ViewParams vp_plain, uint32_t w0,
                                                uint32_t npix_plain, Soa s, int cur, float* aov_plain, uint32_t aov_k,
                                                const LaunchBlock* lb) {
@@ -281,7 +281,8 @@ __global__ void __launch_bounds__(128, 8) k_shade(DScene sc, PathParams pp, View
         ShadowReq qL, qE;
         AovOut ao;
         const bool want_aov = aov != nullptr && primary && k == aov_k;
-        const bool more = path_step(sc, pp, vp, px, py, pp.sample_base + k, ps, h, qL, qE, want_aov ? &ao : nullptr);
+        const bool more = path_step<kTex>(sc, pp, vp, px, py, pp.sample_base + k, ps, h, qL, qE,
+                                          want_aov ? &ao : nullptr);
         uint32_t extra = 0;
         if (qL.valid) {
             extra |= kFlagShL;
@@ -484,8 +485,7 @@ template <bool kStats, int kLevels, bool kAlpha>
 __global__ void __launch_bounds__(128, kLevels == 1 ? 8 : 5) k_shadow(DScene sc, Soa s, int* err,
                                                                        unsigned long long* stats) {
     const uint32_t count = s.counts[2];
-    constexpr int kSh = kLevels == 1 ? kShStackEntries : 0;
-    __shared__ uint2 s_stack[kSh > 0 ? kSh * kShStride : 1];
+    constexpr int kSh = 0;   // a shared-memory stack measured slower for shadow rays (less L1 for nodes)
     int e = 0;
     TravCount tc{0, 0};
     uint32_t nr = 0;
@@ -497,13 +497,13 @@ __global__ void __launch_bounds__(128, kLevels == 1 ? 8 : 5) k_shadow(DScene sc,
         if (f & kFlagShL) {
             const float4 d = s.shL[p];
             nr++;
-            if (!scene_occluded<kStats, kLevels, kAlpha, kSh>(sc, org, ld3(d), 0.001f, d.w, tc, e, s_stack + threadIdx.x))
+            if (!scene_occluded<kStats, kLevels, kAlpha, kSh>(sc, org, ld3(d), 0.001f, d.w, tc, e, nullptr))
                 rad = rad + ld3(s.shLc[p]);
         }
         if (f & kFlagShE) {
             const float4 d = s.shE[p];
             nr++;
-            if (!scene_occluded<kStats, kLevels, kAlpha, kSh>(sc, org, ld3(d), 0.001f, d.w, tc, e, s_stack + threadIdx.x))
+            if (!scene_occluded<kStats, kLevels, kAlpha, kSh>(sc, org, ld3(d), 0.001f, d.w, tc, e, nullptr))
                 rad = rad + ld3(s.shEc[p]);
         }
         s.rad[p] = f4(rad, 0.0f);
@@ -775,7 +775,7 @@ void init_launch_shapes() {
     g_blocks_extend[0] = std::max(1, b) * g_num_sms;
     cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, k_extend<false, 2, false>, 128, 0);
     g_blocks_extend[1] = std::max(1, b) * g_num_sms;
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, k_shade<false>, 128, 0);
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, k_shade<false, false>, 128, 0);
     g_blocks_shade = std::max(1, b) * g_num_sms;
     cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, k_shadow<false, 1, false>, 128, 0);
     g_blocks_shadow[0] = std::max(1, b) * g_num_sms;
@@ -937,8 +937,10 @@ ohao_status wavefront_render(const DScene& sc, const RenderView& view, const Pat
             cudaMemsetAsync(s.counts + (cur ^ 1), 0, 4, st);
             cudaMemsetAsync(s.counts + 2, 0, 4, st);
             tm.begin(1, a);
-            k_shade<false><<<g_blocks_shade, 128, 0, st>>>(sc, pp, view.vp, static_cast<uint32_t>(w0), npix, s, cur,
-                                                           view.aov, spp - 1, nullptr);
+            if (sc.ntex) k_shade<false, true><<<g_blocks_shade, 128, 0, st>>>(sc, pp, view.vp, static_cast<uint32_t>(w0), npix,
+                                                                          s, cur, view.aov, spp - 1, nullptr);
+            else k_shade<false, false><<<g_blocks_shade, 128, 0, st>>>(sc, pp, view.vp, static_cast<uint32_t>(w0), npix, s,
+                                                                       cur, view.aov, spp - 1, nullptr);
             tm.end(1, a);
             tm.begin(2, a);
             if (fetch) launch_shadow_fetch(sc, s, static_cast<int>(pp.refill), d_err, profile ? dstats : nullptr, st);
@@ -1139,7 +1141,8 @@ void enqueue_chunk(const DScene& sc, const PathParams& pp, const LaunchBlock* lb
         if (pp.flags & kFlagSortMaterial) sort_queue_by_material(sc, s, cur, cap, st);
         cudaMemsetAsync(s.counts + (cur ^ 1), 0, 4, st);
         cudaMemsetAsync(s.counts + 2, 0, 8, st);   // shadow and done counts
-        k_shade<true><<<g_blocks_shade, 128, 0, st>>>(sc, pp, ViewParams{}, 0u, 1u, s, cur, nullptr, 0u, lb);
+        if (sc.ntex) k_shade<true, true><<<g_blocks_shade, 128, 0, st>>>(sc, pp, ViewParams{}, 0u, 1u, s, cur, nullptr, 0u, lb);
+        else k_shade<true, false><<<g_blocks_shade, 128, 0, st>>>(sc, pp, ViewParams{}, 0u, 1u, s, cur, nullptr, 0u, lb);
         if (fetch) {
             launch_shadow_fetch(sc, s, pv.refill, d_err, nullptr, st);
         } else {
