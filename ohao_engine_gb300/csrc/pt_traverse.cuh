@@ -8,8 +8,9 @@
 // Child boxes are tested in the node's quantised frame: one FMA per slab side
 // (t = q * (2^e / d) + (origin - o) / d) with per-axis conservative margins
 // folded into the offsets. Near/far planes are chosen once per node by
-// swapping the lo/hi byte words of axes with a negative direction. Bytes are
-// converted to float exactly with a byte permute into 2^23 + b and one add.
+// swapping the lo/hi byte words of axes with a negative direction. A byte q
+// enters the FMA as the float 2^23 + 256 q (one byte permute, exact), the
+// 2^15 a it carries being taken out of the offset once per node.
 //
 // Visit order (kept identical to the host oracle, so node/triangle visit
 // counts match): leaves of a node are tested first, in slot order; then the
@@ -30,6 +31,7 @@ namespace ohao {
 
 constexpr float kTravRelSlack = 0x1p-14f;
 constexpr float kTravAbsScale = 0x1p-21f;
+constexpr float kTravBiasMargin = 0x1p-8f;   // covers the rounding of the biased slab offsets
 constexpr int kStackSize = 64;
 
 // Stack entries a ray may use: the scene's limit, which the host sets in
@@ -130,25 +132,33 @@ OHAO_D float min3f(float a, float b, float c) {
     return d;
 }
 
-// exact uint8 -> float: bits (0x4B000000 | b) encode 2^23 + b
-OHAO_D float u8f(uint32_t word, int b) {
-    return __uint_as_float(__byte_perm(word, 0x4B000000u, 0x7440u | static_cast<uint32_t>(b))) - 8388608.0f;
+// byte b of `word` (q) as the float 2^23 + 256 q, exactly: one byte permute
+// into the bits 0x4B00qq00 (no conversion instruction, no add)
+OHAO_D float u8f_biased(uint32_t word, int b) {
+    return __uint_as_float(__byte_perm(word, 0x4B000000u, 0x7604u | (static_cast<uint32_t>(b) << 4)));
 }
 
 // Hit mask of the 8 child boxes; tn[i] = conservative entry distance.
 OHAO_D uint32_t node_test(const NodeRec& n, const RayPre& r, float tmin, float tbest, float tn[8]) {
     const float org[3] = {__uint_as_float(n.q0.x), __uint_as_float(n.q0.y), __uint_as_float(n.q0.z)};
+    // Slab side of child plane q (a byte): t = q * a + b +- m. With x = 2^23 +
+    // 256 q (the byte permuted into the mantissa) and A = a / 256, x * A =
+    // 2^15 a + q a, so t = fma(x, A, b +- m - 2^15 a): one FMA per side. The
+    // offset b +- m - 2^15 a is rounded once (error <= 2^-24 |b +- m| + 2^-9
+    // |a|), which the extra 2^-8 |a| of margin covers.
     float a[3], bn[3], bf[3];
 #pragma unroll
     for (int k = 0; k < 3; ++k) {
         const int e = static_cast<int>(static_cast<int8_t>((n.q0.w >> (8 * k)) & 0xFFu));
         const float s = __int_as_float((e + 127) << 23);
-        a[k] = s * r.invd[k];
+        const float ak = s * r.invd[k];
         const float b = (org[k] - r.o[k]) * r.invd[k];
-        float m = 255.0f * fabsf(a[k]) + fabsf(b);
+        float m = 255.0f * fabsf(ak) + fabsf(b);
         m = m * kTravAbsScale;
-        bn[k] = b - m;
-        bf[k] = b + m;
+        m = m + fabsf(ak) * kTravBiasMargin;
+        a[k] = ak * 0x1p-8f;
+        bn[k] = fmaf(-0x1p15f, ak, b - m);
+        bf[k] = fmaf(-0x1p15f, ak, b + m);
     }
     // near / far byte words per axis (slots 0-3, 4-7)
     const bool nx = r.invd[0] < 0.0f, ny = r.invd[1] < 0.0f, nz = r.invd[2] < 0.0f;
@@ -163,9 +173,9 @@ OHAO_D uint32_t node_test(const NodeRec& n, const RayPre& r, float tmin, float t
 #pragma unroll
     for (int i = 0; i < 8; ++i) {
         const int b = i & 3;
-        const float qnx = u8f(i < 4 ? nx0 : nx1, b), qfx = u8f(i < 4 ? fx0 : fx1, b);
-        const float qny = u8f(i < 4 ? ny0 : ny1, b), qfy = u8f(i < 4 ? fy0 : fy1, b);
-        const float qnz = u8f(i < 4 ? nz0 : nz1, b), qfz = u8f(i < 4 ? fz0 : fz1, b);
+        const float qnx = u8f_biased(i < 4 ? nx0 : nx1, b), qfx = u8f_biased(i < 4 ? fx0 : fx1, b);
+        const float qny = u8f_biased(i < 4 ? ny0 : ny1, b), qfy = u8f_biased(i < 4 ? fy0 : fy1, b);
+        const float qnz = u8f_biased(i < 4 ? nz0 : nz1, b), qfz = u8f_biased(i < 4 ? fz0 : fz1, b);
         const float t0 = max3f(fmaf(qnx, a[0], bn[0]), fmaf(qny, a[1], bn[1]), fmaf(qnz, a[2], bn[2]));
         const float t1 = min3f(fmaf(qfx, a[0], bf[0]), fmaf(qfy, a[1], bf[1]), fmaf(qfz, a[2], bf[2]));
         tn[i] = t0;

@@ -463,24 +463,30 @@ struct NodeHits {
 
 constexpr float kTravRelSlack = 0x1p-14f;   // relative slack on tbest
 constexpr float kTravAbsScale = 0x1p-21f;   // per-node absolute margin factor
+constexpr float kTravBiasMargin = 0x1p-8f;  // extra margin for the biased slab offsets
 
 inline NodeHits node_test(const WideNode& n, const RayPre& r, float tmin, float tbest) {
     NodeHits h;
+    // t = q a + b -+ m evaluated as fma(2^23 + 256 q, a / 256, b -+ m - 2^15 a):
+    // the offset rounded once, the extra 2^-8 |a| of margin covering it
     float a[3], bn[3], bf[3];
     for (int k = 0; k < 3; ++k) {
         float s = std::ldexp(1.0f, n.exps[k]);
-        a[k] = s * r.invd[k];
+        float ak = s * r.invd[k];
         float b = (n.origin[k] - r.o[k]) * r.invd[k];
-        float m = 255.0f * std::fabs(a[k]) + std::fabs(b);
+        float m = 255.0f * std::fabs(ak) + std::fabs(b);
         m = m * kTravAbsScale;
-        bn[k] = b - m;
-        bf[k] = b + m;
+        m = m + std::fabs(ak) * kTravBiasMargin;
+        a[k] = ak * 0x1p-8f;
+        bn[k] = fma_(-0x1p15f, ak, b - m);
+        bf[k] = fma_(-0x1p15f, ak, b + m);
     }
     float tlimit = tbest + tbest * kTravRelSlack;
     for (int i = 0; i < 8; ++i) {
         float tn = 0.0f, tf = 0.0f;
         for (int k = 0; k < 3; ++k) {
-            float lo = static_cast<float>(n.qlo[k][i]), hi = static_cast<float>(n.qhi[k][i]);
+            float lo = 8388608.0f + 256.0f * static_cast<float>(n.qlo[k][i]);
+            float hi = 8388608.0f + 256.0f * static_cast<float>(n.qhi[k][i]);
             float qn = r.invd[k] < 0.0f ? hi : lo, qf = r.invd[k] < 0.0f ? lo : hi;
             float vn = fma_(qn, a[k], bn[k]), vf = fma_(qf, a[k], bf[k]);
             tn = (k == 0) ? vn : std::fmax(tn, vn);
