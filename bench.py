@@ -1105,9 +1105,10 @@ def case_instanced_pool(arg):
 
 def case_traversal_shapes(arg):
     """Per-view wavefront on sphere_1m (1920x1080, 1 spp, depth 4) in each
-    traversal shape: one ray per thread, or persistent warps refilled at
-    1/2/4/8/16 idle lanes; CUDA-event ms per frame (3 warm-up, 20 timed,
-    L2 flushed), and the images' bit identity."""
+    traversal shape -- one ray per thread, or persistent warps refilled at
+    1/2/4/8/16 idle lanes -- and queue order (queue order, material-binned
+    shading, ray-binned bounces); CUDA-event ms per frame (3 warm-up, 20
+    timed, L2 flushed), and the images' bit identity."""
     import torch
     import ohao_engine_gb300 as og
     from ohao_engine_gb300 import scenes
@@ -1119,8 +1120,8 @@ def case_traversal_shapes(arg):
     acc = torch.zeros((npix, 4), dtype=torch.float32, device="cuda")
     flush = torch.empty(64 * 1024 * 1024, dtype=torch.float32, device="cuda")
     ref = None
-    for refill, flags in ((33, 0), (33, og.FLAG_SORT_MATERIAL), (1, 0), (4, 0), (8, 0), (16, 0),
-                          (8, og.FLAG_SORT_MATERIAL)):
+    m, r = og.FLAG_SORT_MATERIAL, og.FLAG_SORT_RAYS
+    for refill, flags in ((33, 0), (33, m), (33, r), (33, m | r), (1, 0), (4, 0), (8, 0), (16, 0), (8, m), (8, r)):
         st = og.make_settings(spp=1, max_bounces=4, wavefront_refill=refill, flags=flags)
         times = _time_steps(lambda k: pt.render([og.make_view(v, accum=acc)], st), 3, 20, flush)
         same = True
@@ -1131,7 +1132,8 @@ def case_traversal_shapes(arg):
         pt.render([og.make_view(v, accum=acc)], og.make_settings(spp=1, max_bounces=4, wavefront_refill=refill,
                                                                  flags=og.FLAG_PROFILE | flags))
         p = pt.profile()
-        print(f"refill {refill:2d} sort {int(flags != 0)}: {sum(times) / len(times):.3f} ms/frame  extend "
+        order = ("material " if flags & m else "") + ("rays " if flags & r else "") or "queue "
+        print(f"refill {refill:2d} order {order:15s}: {sum(times) / len(times):.3f} ms/frame  extend "
               f"{p.extend_ms:.3f} ms shadow {p.shadow_ms:.3f} ms shade {p.shade_ms:.3f} ms other {p.other_ms:.3f} ms  "
               f"identical={same}")
 

@@ -110,11 +110,16 @@ typedef struct ohao_pt_view {
  * BLASes take the alpha test of pt_anyhit.rahit:17-50 (closest-hit and
  * shadow rays alike). Off by default, as in the reference. */
 #define OHAO_PT_FLAG_ALPHA_TEST (1u << 10)
-/* Shade each bounce's ray queue in material order (sorted on the device by
- * a key of hit/miss, path phase, metallic, textured, roughness) instead of
+/* Shade each bounce's ray queue in material order (binned on the device by
+ * a key of hit/miss, path phase, metallic, roughness, textured) instead of
  * queue order; the image is the same. Not the reference's (its shading
  * order is the hardware's). */
 #define OHAO_PT_FLAG_SORT_MATERIAL (1u << 11)
+/* Trace each bounce's rays grouped by direction octant and origin (a
+ * device-side binning of the ray queue) instead of queue order; the image
+ * is the same. Per-view wavefront only: the persistent pool's launch
+ * configuration sets its own ray order. Not the reference's. */
+#define OHAO_PT_FLAG_SORT_RAYS (1u << 12)
 /* Not the offline reference estimator: the first specular bounce (stage B)
  * draws the half-vector from the GGX distribution of visible normals with
  * weight F * G2/G1 (pt_raygen_realtime.rgen:723-800, ggx_aniso.glsl:56-133)

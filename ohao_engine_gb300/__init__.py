@@ -31,6 +31,7 @@ FLAG_FIREFLY_CLAMP = 1 << 2
 FLAG_ENV_FIXED_V = 1 << 8
 FLAG_ALPHA_TEST = 1 << 10     # non-opaque rays: alpha test on OHAO_BLAS_FLAG_NO_OPAQUE geometry
 FLAG_SORT_MATERIAL = 1 << 11  # shade each ray queue in material order (same image)
+FLAG_SORT_RAYS = 1 << 12      # trace each bounce's rays grouped by direction and origin (same image)
 BLAS_FLAG_NO_OPAQUE = 1
 FLAG_GGX_VNDF = 1 << 9        # VNDF sampling of the first specular bounce (not the offline estimator)
 FLAG_PROFILE = 1 << 16

@@ -234,6 +234,11 @@ ohao::DScene make_scene(const ohao_pt_ctx* c) {
     s.tex_info = c->tex_info.as<uint4>();
     s.ntex = c->ntex;
     s.alpha_test = 0;
+    for (int a = 0; a < 3; ++a) {
+        const float ext = c->flat.root_box[3 + a] - c->flat.root_box[a];
+        s.box_lo[a] = c->flat.root_box[a];
+        s.box_inv[a] = ext > 0.0f ? 4.0f / ext : 0.0f;
+    }
     return s;
 }
 

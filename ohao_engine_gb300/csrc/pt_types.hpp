@@ -58,6 +58,8 @@ struct DScene {
     const uint4* tex_info;
     uint32_t ntex;
     uint32_t alpha_test;    // non-opaque rays: alpha-test kInstNoOpaque instances
+    float box_lo[3];        // the scene's bounding box: low corner and 4 / extent per axis
+    float box_inv[3];
 };
 
 struct PathParams {

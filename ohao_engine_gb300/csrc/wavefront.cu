@@ -344,33 +344,104 @@ __global__ void k_ray_keys(const LaunchBlock* lb, Soa s, int cur) {
     }
 }
 
-// Shading order by material (OHAO_PT_FLAG_SORT_MATERIAL): 8-bit key of each
-// queued path after its closest-hit query, so that k_shade's warps see
-// paths that take the same branches together: bit 7 miss, bits 6-5 the
+// Ray-queue binning: a counting sort of queue `cur` into kBins bins of a
+// small key, so that a warp's lanes take the same branches (material key,
+// before shading) or walk similar parts of the BVH (ray key, before a
+// bounce's traversal). Not stable -- the order inside a bin follows the
+// atomics -- which changes nothing but the order paths are processed in:
+// every path's result is its own. Three kernels: keys + block histograms,
+// the bins' exclusive prefix, scatter with one range reservation per bin
+// and block tile.
+constexpr int kBins = 512;
+constexpr int kBinTile = 1024;   // entries per block tile of the scatter (8 per thread)
+
+// Material key (OHAO_PT_FLAG_SORT_MATERIAL): bit 5 miss, bits 4-3 the
 // path's phase (primary, specular chain, diffuse chain), then for hits bit
-// 4 metallic >= 0.5, bit 3 a textured material, bits 2-0 the roughness in
-// eighths. The stable sort keeps the queue order within a key.
-__global__ void k_material_keys(DScene sc, Soa s, int cur) {
+// 2 metallic >= 0.5, bit 1 roughness >= 0.5, bit 0 a textured material.
+// Ray key (OHAO_PT_FLAG_SORT_RAYS): direction octant (bits 8-6) and the
+// origin's quarter of the scene box per axis (bits 5-0).
+template <int kMode>
+__device__ __forceinline__ uint32_t bin_key(const DScene& sc, const Soa& s, uint32_t p) {
+    if (kMode == 0) {
+        const uint32_t phase = s.flags[p] & 3u;
+        const uint32_t prim = __float_as_uint(s.hit[p].w);
+        if (prim == 0xFFFFFFFFu) return 32u | (phase << 3);
+        const DInst& in = sc.inst[s.hit_inst[p]];
+        const uint32_t mid = __ldg(sc.mat_ids + (__ldg(&in.custom) & 0xFFFFFFu) + prim);
+        const float4 m0 = __ldg(sc.mats + mid * 3), m1 = __ldg(sc.mats + mid * 3 + 1), m2 = __ldg(sc.mats + mid * 3 + 2);
+        const bool tex = (__float_as_uint(m0.w) & __float_as_uint(m1.z) & __float_as_uint(m1.w) &
+                          __float_as_uint(m2.x)) != 0xFFFFFFFFu;
+        return (phase << 3) | (m1.y >= 0.5f ? 4u : 0u) | (m1.x >= 0.5f ? 2u : 0u) | (tex ? 1u : 0u);
+    } else {
+        const float4 o = s.ro[p], d = s.rd[p];
+        const uint32_t oct = (d.x < 0.0f ? 4u : 0u) | (d.y < 0.0f ? 2u : 0u) | (d.z < 0.0f ? 1u : 0u);
+        auto quarter = [&](float v, int a) {
+            const float f = (v - sc.box_lo[a]) * sc.box_inv[a];
+            return static_cast<uint32_t>(fminf(fmaxf(f, 0.0f), 3.0f));
+        };
+        return (oct << 6) | (quarter(o.x, 0) << 4) | (quarter(o.y, 1) << 2) | quarter(o.z, 2);
+    }
+}
+
+template <int kMode>
+__global__ void __launch_bounds__(128) k_bin_count(DScene sc, Soa s, int cur, uint32_t* bins) {
+    __shared__ uint32_t h[kBins];
+    for (int b = threadIdx.x; b < kBins; b += blockDim.x) h[b] = 0u;
+    __syncthreads();
     const uint32_t count = s.counts[cur];
     const uint32_t* q = s.q_ray[cur];
     for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < count; i += gridDim.x * blockDim.x) {
         const uint32_t p = q[i];
-        const uint32_t phase = s.flags[p] & 3u;
-        const uint32_t prim = __float_as_uint(s.hit[p].w);
-        uint32_t key;
-        if (prim == 0xFFFFFFFFu) {
-            key = 0x80u | (phase << 5);
-        } else {
-            const DInst& in = sc.inst[s.hit_inst[p]];
-            const uint32_t mid = __ldg(sc.mat_ids + (__ldg(&in.custom) & 0xFFFFFFu) + prim);
-            const float4 m0 = __ldg(sc.mats + mid * 3), m1 = __ldg(sc.mats + mid * 3 + 1), m2 = __ldg(sc.mats + mid * 3 + 2);
-            const bool tex = (__float_as_uint(m0.w) & __float_as_uint(m1.z) & __float_as_uint(m1.w) &
-                              __float_as_uint(m2.x)) != 0xFFFFFFFFu;
-            const uint32_t rough = static_cast<uint32_t>(fminf(fmaxf(m1.x, 0.0f), 0.999f) * 8.0f);
-            key = (phase << 5) | (m1.y >= 0.5f ? 16u : 0u) | (tex ? 8u : 0u) | rough;
-        }
+        const uint32_t key = bin_key<kMode>(sc, s, p);
         s.skA[i] = key;
         s.svA[i] = p;
+        atomicAdd(&h[key], 1u);
+    }
+    __syncthreads();
+    for (int b = threadIdx.x; b < kBins; b += blockDim.x)
+        if (h[b]) atomicAdd(&bins[b], h[b]);
+}
+
+// cursors[b] = sum of bins[0..b)
+__global__ void __launch_bounds__(kBins) k_bin_prefix(const uint32_t* bins, uint32_t* cursors) {
+    __shared__ uint32_t v[kBins];
+    const int b = threadIdx.x;
+    v[b] = bins[b];
+    __syncthreads();
+    for (int off = 1; off < kBins; off <<= 1) {
+        const uint32_t x = b >= off ? v[b - off] : 0u;
+        __syncthreads();
+        v[b] += x;
+        __syncthreads();
+    }
+    cursors[b] = v[b] - bins[b];
+}
+
+__global__ void __launch_bounds__(128) k_bin_scatter(Soa s, int cur, uint32_t* cursors) {
+    __shared__ uint32_t tc[kBins], tb[kBins];
+    const uint32_t count = s.counts[cur];
+    uint32_t* q = s.q_ray[cur];
+    constexpr int kPer = kBinTile / 128;
+    for (uint32_t t0 = blockIdx.x * kBinTile; t0 < count; t0 += gridDim.x * kBinTile) {   // uniform per block
+        for (int b = threadIdx.x; b < kBins; b += blockDim.x) tc[b] = 0u;
+        __syncthreads();
+        uint32_t key[kPer], rank[kPer];
+#pragma unroll
+        for (int j = 0; j < kPer; ++j) {
+            const uint32_t i = t0 + j * 128 + threadIdx.x;
+            key[j] = i < count ? s.skA[i] : 0u;
+            rank[j] = i < count ? atomicAdd(&tc[key[j]], 1u) : 0u;
+        }
+        __syncthreads();
+        for (int b = threadIdx.x; b < kBins; b += blockDim.x)
+            if (tc[b]) tb[b] = atomicAdd(&cursors[b], tc[b]);
+        __syncthreads();
+#pragma unroll
+        for (int j = 0; j < kPer; ++j) {
+            const uint32_t i = t0 + j * 128 + threadIdx.x;
+            if (i < count) q[tb[key[j]] + rank[j]] = s.svA[i];
+        }
+        __syncthreads();
     }
 }
 
@@ -749,7 +820,8 @@ Soa carve_soa_at(Carve& c, uint32_t cap) {
     s.svA = c.take<uint32_t>(cap);
     s.skB = c.take<uint32_t>(cap);
     s.svB = c.take<uint32_t>(cap);
-    s.shist = c.take<uint32_t>(16 * static_cast<size_t>(rsort::tiles_for(cap)));
+    // radix-sort tile histograms, or the binning's counts and cursors
+    s.shist = c.take<uint32_t>(std::max<size_t>(16 * static_cast<size_t>(rsort::tiles_for(cap)), 2 * static_cast<size_t>(kBins)));
     return s;
 }
 
@@ -838,13 +910,19 @@ void launch_shadow(const DScene& sc, const Soa& s, int* d_err, unsigned long lon
 }
 
 constexpr uint32_t kFlagSortMaterial = OHAO_PT_FLAG_SORT_MATERIAL;
+constexpr uint32_t kFlagSortRays = OHAO_PT_FLAG_SORT_RAYS;
 
-// Reorders ray queue `cur` by the material key of k_material_keys (two
-// 4-bit radix passes; the sorted pairs end in skA/svA).
-void sort_queue_by_material(const DScene& sc, const Soa& s, int cur, uint32_t cap, cudaStream_t st) {
-    k_material_keys<<<g_blocks_shade, 128, 0, st>>>(sc, s, cur);
-    rsort::sort_pairs(s.skA, s.svA, s.skB, s.svB, s.shist, s.counts + cur, cap, 8, st);
-    k_copy_queue<<<g_blocks_shade, 128, 0, st>>>(s, cur);
+// Bins ray queue `cur` by the key of kMode (0 material, 1 ray); the bin
+// counts and cursors live in the first 2 * kBins words of s.shist.
+template <int kMode>
+void bin_queue(const DScene& sc, const Soa& s, int cur, uint32_t cap, cudaStream_t st) {
+    uint32_t* bins = s.shist;
+    uint32_t* cursors = s.shist + kBins;
+    cudaMemsetAsync(bins, 0, kBins * sizeof(uint32_t), st);
+    k_bin_count<kMode><<<g_blocks_shade, 128, 0, st>>>(sc, s, cur, bins);
+    k_bin_prefix<<<1, kBins, 0, st>>>(bins, cursors);
+    const uint32_t tiles = (cap + kBinTile - 1) / kBinTile;
+    k_bin_scatter<<<std::min<uint32_t>(tiles, static_cast<uint32_t>(g_num_sms) * 8u), 128, 0, st>>>(s, cur, cursors);
 }
 
 struct EvTimer {
@@ -924,6 +1002,11 @@ ohao_status wavefront_render(const DScene& sc, const RenderView& view, const Pat
         int cur = 0;
         const bool fetch = pp.refill > 0 && sc.nnodes > 0;
         for (uint32_t it = 0; it < niters; ++it) {
+            if (it > 0 && (pp.flags & kFlagSortRays)) {   // bounce rays grouped by direction and origin
+                tm.begin(3, a);
+                bin_queue<1>(sc, s, cur, capacity, st);
+                tm.end(3, a);
+            }
             if (fetch) cudaMemsetAsync(s.counts + kCtrExtendFetch, 0, 8, st);   // both fetch counters
             tm.begin(0, a);
             if (fetch) launch_extend_fetch(sc, s, cur, static_cast<int>(pp.refill), d_err, profile ? dstats : nullptr, st);
@@ -931,7 +1014,7 @@ ohao_status wavefront_render(const DScene& sc, const RenderView& view, const Pat
             tm.end(0, a);
             if (pp.flags & kFlagSortMaterial) {
                 tm.begin(3, a);
-                sort_queue_by_material(sc, s, cur, capacity, st);
+                bin_queue<0>(sc, s, cur, capacity, st);
                 tm.end(3, a);
             }
             cudaMemsetAsync(s.counts + (cur ^ 1), 0, 4, st);
@@ -1138,7 +1221,7 @@ void enqueue_chunk(const DScene& sc, const PathParams& pp, const LaunchBlock* lb
         } else {
             launch_extend(sc, s, cur, d_err, nullptr, st);
         }
-        if (pp.flags & kFlagSortMaterial) sort_queue_by_material(sc, s, cur, cap, st);
+        if (pp.flags & kFlagSortMaterial) bin_queue<0>(sc, s, cur, cap, st);
         cudaMemsetAsync(s.counts + (cur ^ 1), 0, 4, st);
         cudaMemsetAsync(s.counts + 2, 0, 8, st);   // shadow and done counts
         if (sc.ntex) k_shade<true, true><<<g_blocks_shade, 128, 0, st>>>(sc, pp, ViewParams{}, 0u, 1u, s, cur, nullptr, 0u, lb);

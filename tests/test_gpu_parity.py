@@ -371,9 +371,10 @@ def test_degenerate_view_sizes(gpu_lib, oracle, two_level):
 @pytest.mark.parametrize("two_level", [False, True])
 def test_traversal_shapes_and_material_sort_same_image(gpu_lib, two_level):
     """The per-view wavefront in every traversal shape (one ray per thread;
-    persistent warps refilled at 1, 4 or 16 idle lanes) and with the
-    material-sorted shading order, and the persistent pool with the material
-    sort: accumulators bit-identical, closest-hit visit counts identical."""
+    persistent warps refilled at 1, 4 or 16 idle lanes), with the
+    material-binned shading order and the ray-binned bounce order, and the
+    persistent pool with the material binning: accumulators bit-identical,
+    closest-hit visit counts identical."""
     import torch
     og = gpu_lib
     sd = small_instanced(side=24) if two_level else small_env_scene(freq=16)
@@ -382,7 +383,7 @@ def test_traversal_shapes_and_material_sort_same_image(gpu_lib, two_level):
     v = sd.views[0]
     ref, ref_counts = None, None
     for refill in (33, 1, 4, 16):
-        for flags in (0, og.FLAG_SORT_MATERIAL):
+        for flags in (0, og.FLAG_SORT_MATERIAL, og.FLAG_SORT_RAYS, og.FLAG_SORT_MATERIAL | og.FLAG_SORT_RAYS):
             acc = torch.zeros((v.width * v.height, 4), dtype=torch.float32, device="cuda")
             pt.render([og.make_view(v, accum=acc)],
                       og.make_settings(spp=3, max_bounces=4, sampler=1, wavefront_refill=refill,
