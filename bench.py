@@ -46,6 +46,9 @@ def parse():
     ap.add_argument("--workload", default="sphere_1m", choices=["sphere_1m", "cornell", "instanced", "studio", "denoise"])
     ap.add_argument("--cpu-seconds", type=float, default=12.0)
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--shade-order", default="material", choices=["material", "queue"],
+                    help="shade each ray queue in material order (binned on the device) or in queue order; "
+                         "the image is the same")
     ap.add_argument("--no-gates", action="store_true",
                     help="skip the gates (configs 3-5 and the FP64 comparisons) after the headline")
     ap.add_argument("--case", default=None, choices=sorted(CASES),
@@ -572,9 +575,11 @@ def run_ours(args):
     acc = torch.zeros((npix, 4), dtype=torch.float32, device="cuda")
     flush = torch.empty(64 * 1024 * 1024, dtype=torch.float32, device="cuda")   # 256 MB > L2
 
+    order = og.FLAG_SORT_MATERIAL if args.shade_order == "material" else 0
+
     def step(k, flags=0):
         s = og.make_settings(spp=spp_step, max_bounces=sd.max_bounces, sample_index_base=k * spp_step,
-                             sampler=og.SAMPLER_PCG, flags=flags)
+                             sampler=og.SAMPLER_PCG, flags=flags | order)
         pt.render([og.make_view(v, accum=acc, history=k * spp_step)], s)
 
     for k in range(args.warmup):
@@ -640,13 +645,14 @@ def run_ours(args):
     hnp = host.numpy()
     e2e_times = []
     base = 2 * args.steps + args.warmup
-    s0 = og.make_settings(spp=spp_step, max_bounces=sd.max_bounces, sample_index_base=0, sampler=og.SAMPLER_PCG)
+    s0 = og.make_settings(spp=spp_step, max_bounces=sd.max_bounces, sample_index_base=0, sampler=og.SAMPLER_PCG,
+                          flags=order)
     pt.render_host([og.make_view(v, history=0)], s0, [hnp])
     for k in range(args.steps):
         flush.zero_()
         torch.cuda.synchronize()
         s = og.make_settings(spp=spp_step, max_bounces=sd.max_bounces, sample_index_base=(base + k) * spp_step,
-                             sampler=og.SAMPLER_PCG)
+                             sampler=og.SAMPLER_PCG, flags=order)
         t0 = time.perf_counter()
         pt.render_host([og.make_view(v, history=1 + k * spp_step)], s, [hnp])
         e2e_times.append(time.perf_counter() - t0)
@@ -667,6 +673,7 @@ def run_ours(args):
                 "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded)",
                 "config": {"workload": desc, "l2": "flushed between timed steps (256 MB write)",
                            "path": "plain wavefront", "parallelism": f"replicas x{world}",
+                           "shade_order": args.shade_order,
                            "bvh_build_s": build_s, "scene_upload_s": upload_s,
                            "rays_per_step": {"closest": rays_c / len(prof_ms), "shadow": rays_s / len(prof_ms)}},
                 "clocks": clocks, "e2e": e2e, "gpu_launches": int(round(launches_per_step * args.steps)),

@@ -20,6 +20,7 @@
 
 #include "../../include/ohao_pt.h"
 #include "bvh_internal.hpp"
+#include "env_guide.hpp"
 #include "pt_types.hpp"
 
 namespace {
@@ -74,6 +75,9 @@ struct ohao_pt_ctx {
     std::string last_error;
     // geometry
     DevBuf pos, normals, uvs, indices, mat_ids, mats, lights, env, marg, cond, albedo_map;
+    DevBuf guide_marg, guide_cond;   // env_guide.hpp tables; has_guide when both are current
+    bool has_guide = false;
+    uint32_t guide_mm = 0, guide_mc = 0;
     uint32_t nverts = 0, ntris = 0, nmats = 0, nlights = 0;
     uint32_t max_mat_id = 0;              // largest per-triangle material id
     uint32_t env_w = 0, env_h = 0;
@@ -223,6 +227,10 @@ ohao::DScene make_scene(const ohao_pt_ctx* c) {
     s.env_h = c->env_h;
     s.marg = c->marg.as<float>();
     s.cond = c->cond.as<float>();
+    s.guide_marg = c->has_guide ? c->guide_marg.as<uint16_t>() : nullptr;
+    s.guide_cond = c->has_guide ? c->guide_cond.as<uint16_t>() : nullptr;
+    s.guide_mm = c->guide_mm;
+    s.guide_mc = c->guide_mc;
     s.env_intensity = c->env_intensity;
     s.has_env = c->has_env ? 1 : 0;
     s.has_cdf = c->has_cdf ? 1 : 0;
@@ -653,16 +661,38 @@ ohao_status ohao_pt_set_lights(ohao_pt_ctx* ctx, const ohao_gpu_light* l, uint32
     return s;
 }
 
+// Guide tables for the device's inverse-CDF searches (env_guide.hpp), when
+// the marginal and every conditional row are non-decreasing; otherwise the
+// device searches whole rows. Either way it samples the same texels.
+static ohao_status build_env_guides(ohao_pt_ctx* ctx, const float* marg, const float* cond, uint32_t w, uint32_t h) {
+    namespace eg = ohao_env_guide;
+    if (w > eg::kMaxEntries || h > eg::kMaxEntries || !eg::monotone(marg, h)) return OHAO_OK;
+    for (uint32_t y = 0; y < h; ++y)
+        if (!eg::monotone(cond + static_cast<size_t>(y) * w, w)) return OHAO_OK;
+    const uint32_t mm = eg::cells_for(h), mc = eg::cells_for(w);
+    std::vector<uint16_t> gm(mm + 1), gc(static_cast<size_t>(h) * (mc + 1));
+    eg::build(marg, h, mm, gm.data());
+    for (uint32_t y = 0; y < h; ++y)
+        eg::build(cond + static_cast<size_t>(y) * w, w, mc, gc.data() + static_cast<size_t>(y) * (mc + 1));
+    ohao_status s = upload(ctx, ctx->guide_marg, gm.data(), gm.size() * 2, "env marginal guide");
+    if (s == OHAO_OK) s = upload(ctx, ctx->guide_cond, gc.data(), gc.size() * 2, "env conditional guide");
+    if (s != OHAO_OK) return s;
+    ctx->guide_mm = mm;
+    ctx->guide_mc = mc;
+    ctx->has_guide = true;
+    return OHAO_OK;
+}
+
 ohao_status ohao_pt_set_env(ohao_pt_ctx* ctx, const float* rgba, uint32_t w, uint32_t h, const float* marg,
                             const float* cond, float integral, float intensity) {
     if (!ctx) return OHAO_ERR_INVALID_ARG;
     (void)integral;
     if (!rgba || w == 0 || h == 0) {
-        ctx->has_env = ctx->has_cdf = false;
+        ctx->has_env = ctx->has_cdf = ctx->has_guide = false;
         ctx->env_w = ctx->env_h = 0;
         return OHAO_OK;
     }
-    ctx->has_env = ctx->has_cdf = false;   // until every upload below has succeeded
+    ctx->has_env = ctx->has_cdf = ctx->has_guide = false;   // until every upload below has succeeded
     ctx->env_w = ctx->env_h = 0;
     ohao_status s = upload(ctx, ctx->env, rgba, static_cast<size_t>(w) * h * 16, "env");
     if (s != OHAO_OK) return s;
@@ -670,6 +700,7 @@ ohao_status ohao_pt_set_env(ohao_pt_ctx* ctx, const float* rgba, uint32_t w, uin
         if ((s = upload(ctx, ctx->marg, marg, static_cast<size_t>(h) * 4, "env marginal")) != OHAO_OK) return s;
         if ((s = upload(ctx, ctx->cond, cond, static_cast<size_t>(w) * h * 4, "env conditional")) != OHAO_OK) return s;
         ctx->has_cdf = true;
+        if ((s = build_env_guides(ctx, marg, cond, w, h)) != OHAO_OK) return s;
     }
     ctx->has_env = true;
     ctx->env_w = w;

@@ -12,6 +12,7 @@
 // The shadow rays a step emits (light NEE, env NEE) are resolved before the
 // next step of the same path, so radiance is summed in the shader's order.
 #pragma once
+#include "env_guide.hpp"
 #include "pt_device.cuh"
 
 namespace ohao {
@@ -99,12 +100,23 @@ struct Surf {
     float tu, tv;
 };
 
+// env_sampling.glsl:15-37: the first CDF entry >= u (the last entry if
+// none), searched between a guide table's bounds where the scene has one.
 OHAO_D int search_marg(const DScene& sc, float u) {
+    if (sc.guide_marg)
+        return ohao_env_guide::search([&](int i) { return __ldg(sc.marg + i); },
+                                      [&](uint32_t j) { return static_cast<int>(__ldg(sc.guide_marg + j)); },
+                                      sc.guide_mm, u);
     int lo = 0, hi = static_cast<int>(sc.env_h) - 1;
     while (lo < hi) { int mid = (lo + hi) / 2; if (__ldg(sc.marg + mid) < u) lo = mid + 1; else hi = mid; }
     return lo;
 }
-OHAO_D int search_cond(const DScene& sc, uint32_t base, float u) {
+OHAO_D int search_cond(const DScene& sc, uint32_t row, uint32_t base, float u) {
+    if (sc.guide_cond) {
+        const uint16_t* g = sc.guide_cond + static_cast<size_t>(row) * (sc.guide_mc + 1);
+        return ohao_env_guide::search([&](int i) { return __ldg(sc.cond + base + i); },
+                                      [&](uint32_t j) { return static_cast<int>(__ldg(g + j)); }, sc.guide_mc, u);
+    }
     int lo = 0, hi = static_cast<int>(sc.env_w) - 1;
     while (lo < hi) { int mid = (lo + hi) / 2; if (__ldg(sc.cond + base + mid) < u) lo = mid + 1; else hi = mid; }
     return lo;
@@ -114,7 +126,7 @@ OHAO_D void sample_env(const DScene& sc, float u1, float u2, V3& dir, float& pdf
     const uint32_t W = sc.env_w, H = sc.env_h;
     const int y = search_marg(sc, u1);
     const uint32_t base = static_cast<uint32_t>(y) * W;
-    const int x = search_cond(sc, base, u2);
+    const int x = search_cond(sc, static_cast<uint32_t>(y), base, u2);
     const float u = (static_cast<float>(x) + 0.5f) / static_cast<float>(W);
     const float v = (static_cast<float>(y) + 0.5f) / static_cast<float>(H);
     const float phi = (u - 0.5f) * kTWOPI;

@@ -48,6 +48,11 @@ struct DScene {
     uint32_t env_w, env_h;
     const float* marg;
     const float* cond;
+    // guide tables of the inverse-CDF searches (env_guide.hpp), or null:
+    // guide_mm + 1 entries for the marginal, guide_mc + 1 per row
+    const uint16_t* guide_marg;
+    const uint16_t* guide_cond;
+    uint32_t guide_mm, guide_mc;
     float env_intensity;
     int has_env, has_cdf;
     const float* albedo_map;

@@ -344,15 +344,15 @@ __global__ void k_ray_keys(const LaunchBlock* lb, Soa s, int cur) {
     }
 }
 
-// Ray-queue binning: a counting sort of queue `cur` into kBins bins of a
+// Ray-queue binning: a counting sort of queue `cur` into at most kBinsMax bins of a
 // small key, so that a warp's lanes take the same branches (material key,
 // before shading) or walk similar parts of the BVH (ray key, before a
 // bounce's traversal). Not stable -- the order inside a bin follows the
 // atomics -- which changes nothing but the order paths are processed in:
-// every path's result is its own. Three kernels: keys + block histograms,
-// the bins' exclusive prefix, scatter with one range reservation per bin
-// and block tile.
-constexpr int kBins = 512;
+// every path's result is its own. Two kernels: keys + block histograms,
+// then the scatter (each block scans the bin counts itself and reserves one
+// range per bin and block tile).
+constexpr int kBinsMax = 512;
 constexpr int kBinTile = 1024;   // entries per block tile of the scatter (8 per thread)
 
 // Material key (OHAO_PT_FLAG_SORT_MATERIAL): bit 5 miss, bits 4-3 the
@@ -383,10 +383,27 @@ __device__ __forceinline__ uint32_t bin_key(const DScene& sc, const Soa& s, uint
     }
 }
 
+// h[key] += 1 for every active lane, one shared-memory atomic per distinct
+// key of the warp (the keys are few, so per-lane atomics would serialise on
+// the same words); returns the lane's slot among the entries it added.
+__device__ __forceinline__ uint32_t warp_bin_add(uint32_t* h, uint32_t key) {
+    const uint32_t peers = __match_any_sync(__activemask(), key);
+    const int leader = __ffs(peers) - 1;
+    const uint32_t lane = threadIdx.x & 31u;
+    uint32_t base = 0u;
+    if (static_cast<int>(lane) == leader) base = atomicAdd(&h[key], static_cast<uint32_t>(__popc(peers)));
+    base = __shfl_sync(peers, base, leader);
+    return base + static_cast<uint32_t>(__popc(peers & ((1u << lane) - 1u)));
+}
+
+// Bins of each key: 6-bit material keys, 9-bit ray keys.
+template <int kMode> constexpr int kBinsOf = kMode == 0 ? 64 : 512;
+
 template <int kMode>
 __global__ void __launch_bounds__(128) k_bin_count(DScene sc, Soa s, int cur, uint32_t* bins) {
-    __shared__ uint32_t h[kBins];
-    for (int b = threadIdx.x; b < kBins; b += blockDim.x) h[b] = 0u;
+    constexpr int kB = kBinsOf<kMode>;
+    __shared__ uint32_t h[kB];
+    for (int b = threadIdx.x; b < kB; b += blockDim.x) h[b] = 0u;
     __syncthreads();
     const uint32_t count = s.counts[cur];
     const uint32_t* q = s.q_ray[cur];
@@ -395,46 +412,64 @@ __global__ void __launch_bounds__(128) k_bin_count(DScene sc, Soa s, int cur, ui
         const uint32_t key = bin_key<kMode>(sc, s, p);
         s.skA[i] = key;
         s.svA[i] = p;
-        atomicAdd(&h[key], 1u);
+        warp_bin_add(h, key);
     }
     __syncthreads();
-    for (int b = threadIdx.x; b < kBins; b += blockDim.x)
+    for (int b = threadIdx.x; b < kB; b += blockDim.x)
         if (h[b]) atomicAdd(&bins[b], h[b]);
 }
 
-// cursors[b] = sum of bins[0..b)
-__global__ void __launch_bounds__(kBins) k_bin_prefix(const uint32_t* bins, uint32_t* cursors) {
-    __shared__ uint32_t v[kBins];
-    const int b = threadIdx.x;
-    v[b] = bins[b];
-    __syncthreads();
-    for (int off = 1; off < kBins; off <<= 1) {
-        const uint32_t x = b >= off ? v[b - off] : 0u;
-        __syncthreads();
-        v[b] += x;
-        __syncthreads();
-    }
-    cursors[b] = v[b] - bins[b];
-}
-
-__global__ void __launch_bounds__(128) k_bin_scatter(Soa s, int cur, uint32_t* cursors) {
-    __shared__ uint32_t tc[kBins], tb[kBins];
+// Scatter of the keyed entries into queue `cur` in bin order. Every block
+// takes the bins' exclusive prefix from the counts itself (warp 0: kB / 32
+// consecutive bins per lane, then a shuffle scan), and reserves each block
+// tile's range of a bin with one atomic on that bin's cursor (zero at entry).
+template <int kMode>
+__global__ void __launch_bounds__(128) k_bin_scatter(Soa s, int cur, const uint32_t* bins, uint32_t* cursors) {
+    constexpr int kB = kBinsOf<kMode>;
+    constexpr int kPerLane = kB / 32;
+    __shared__ uint32_t base[kB], tc[kB], tb[kB];
     const uint32_t count = s.counts[cur];
+    if (blockIdx.x * kBinTile >= count) return;   // uniform per block
+    if (threadIdx.x < 32) {
+        const int lane = threadIdx.x;
+        uint32_t v[kPerLane], sum = 0u;
+#pragma unroll
+        for (int j = 0; j < kPerLane; ++j) {
+            v[j] = bins[lane * kPerLane + j];
+            sum += v[j];
+        }
+        uint32_t incl = sum;
+#pragma unroll
+        for (int off = 1; off < 32; off <<= 1) {
+            const uint32_t x = __shfl_up_sync(0xFFFFFFFFu, incl, off);
+            if (lane >= off) incl += x;
+        }
+        uint32_t run = incl - sum;
+#pragma unroll
+        for (int j = 0; j < kPerLane; ++j) {
+            base[lane * kPerLane + j] = run;
+            run += v[j];
+        }
+    }
     uint32_t* q = s.q_ray[cur];
     constexpr int kPer = kBinTile / 128;
     for (uint32_t t0 = blockIdx.x * kBinTile; t0 < count; t0 += gridDim.x * kBinTile) {   // uniform per block
-        for (int b = threadIdx.x; b < kBins; b += blockDim.x) tc[b] = 0u;
+        for (int b = threadIdx.x; b < kB; b += blockDim.x) tc[b] = 0u;
         __syncthreads();
         uint32_t key[kPer], rank[kPer];
 #pragma unroll
         for (int j = 0; j < kPer; ++j) {
             const uint32_t i = t0 + j * 128 + threadIdx.x;
-            key[j] = i < count ? s.skA[i] : 0u;
-            rank[j] = i < count ? atomicAdd(&tc[key[j]], 1u) : 0u;
+            key[j] = 0u;
+            rank[j] = 0u;
+            if (i < count) {
+                key[j] = s.skA[i];
+                rank[j] = warp_bin_add(tc, key[j]);
+            }
         }
         __syncthreads();
-        for (int b = threadIdx.x; b < kBins; b += blockDim.x)
-            if (tc[b]) tb[b] = atomicAdd(&cursors[b], tc[b]);
+        for (int b = threadIdx.x; b < kB; b += blockDim.x)
+            if (tc[b]) tb[b] = base[b] + atomicAdd(&cursors[b], tc[b]);
         __syncthreads();
 #pragma unroll
         for (int j = 0; j < kPer; ++j) {
@@ -821,7 +856,7 @@ Soa carve_soa_at(Carve& c, uint32_t cap) {
     s.skB = c.take<uint32_t>(cap);
     s.svB = c.take<uint32_t>(cap);
     // radix-sort tile histograms, or the binning's counts and cursors
-    s.shist = c.take<uint32_t>(std::max<size_t>(16 * static_cast<size_t>(rsort::tiles_for(cap)), 2 * static_cast<size_t>(kBins)));
+    s.shist = c.take<uint32_t>(std::max<size_t>(16 * static_cast<size_t>(rsort::tiles_for(cap)), 2 * static_cast<size_t>(kBinsMax)));
     return s;
 }
 
@@ -912,35 +947,44 @@ void launch_shadow(const DScene& sc, const Soa& s, int* d_err, unsigned long lon
 constexpr uint32_t kFlagSortMaterial = OHAO_PT_FLAG_SORT_MATERIAL;
 constexpr uint32_t kFlagSortRays = OHAO_PT_FLAG_SORT_RAYS;
 
+constexpr int kBinLaunches = 2;   // kernels bin_queue launches
+
 // Bins ray queue `cur` by the key of kMode (0 material, 1 ray); the bin
-// counts and cursors live in the first 2 * kBins words of s.shist.
+// counts and cursors live in the first 2 * kBinsOf<kMode> words of s.shist.
 template <int kMode>
 void bin_queue(const DScene& sc, const Soa& s, int cur, uint32_t cap, cudaStream_t st) {
+    constexpr int kB = kBinsOf<kMode>;
     uint32_t* bins = s.shist;
-    uint32_t* cursors = s.shist + kBins;
-    cudaMemsetAsync(bins, 0, kBins * sizeof(uint32_t), st);
+    uint32_t* cursors = s.shist + kB;
+    cudaMemsetAsync(bins, 0, 2 * kB * sizeof(uint32_t), st);
     k_bin_count<kMode><<<g_blocks_shade, 128, 0, st>>>(sc, s, cur, bins);
-    k_bin_prefix<<<1, kBins, 0, st>>>(bins, cursors);
     const uint32_t tiles = (cap + kBinTile - 1) / kBinTile;
-    k_bin_scatter<<<std::min<uint32_t>(tiles, static_cast<uint32_t>(g_num_sms) * 8u), 128, 0, st>>>(s, cur, cursors);
+    k_bin_scatter<kMode><<<std::min<uint32_t>(tiles, static_cast<uint32_t>(g_num_sms) * 8u), 128, 0, st>>>(
+        s, cur, bins, cursors);
 }
 
+// Profile-mode CUDA events around each section of a render, by kind (0
+// extend, 1 shade, 2 shadow, 3 other) with the kernel launches inside it.
 struct EvTimer {
+    struct Sect {
+        cudaEvent_t a, b;
+        int launches;
+    };
     bool on;
     cudaStream_t st;
-    std::vector<std::pair<cudaEvent_t, cudaEvent_t>> ev[4];
+    std::vector<Sect> ev[4];
     void begin(int kind, cudaEvent_t& a) {
         if (!on) return;
         cudaEventCreate(&a);
         cudaEventRecord(a, st);
         (void)kind;
     }
-    void end(int kind, cudaEvent_t a) {
+    void end(int kind, cudaEvent_t a, int launches = 1) {
         if (!on) return;
         cudaEvent_t b;
         cudaEventCreate(&b);
         cudaEventRecord(b, st);
-        ev[kind].push_back({a, b});
+        ev[kind].push_back({a, b, launches});
     }
     void collect(ProfileAcc* p) {
         if (!on || !p) return;
@@ -948,13 +992,13 @@ struct EvTimer {
         for (int k = 0; k < 4; ++k) {
             for (auto& e : ev[k]) {
                 float ms = 0;
-                cudaEventElapsedTime(&ms, e.first, e.second);
-                if (k == 0) { p->extend_ms += ms; p->extend_launches++; }
-                if (k == 1) { p->shade_ms += ms; p->shade_launches++; }
-                if (k == 2) { p->shadow_ms += ms; p->shadow_launches++; }
-                if (k == 3) { p->other_ms += ms; p->other_launches++; }
-                cudaEventDestroy(e.first);
-                cudaEventDestroy(e.second);
+                cudaEventElapsedTime(&ms, e.a, e.b);
+                if (k == 0) { p->extend_ms += ms; p->extend_launches += e.launches; }
+                if (k == 1) { p->shade_ms += ms; p->shade_launches += e.launches; }
+                if (k == 2) { p->shadow_ms += ms; p->shadow_launches += e.launches; }
+                if (k == 3) { p->other_ms += ms; p->other_launches += e.launches; }
+                cudaEventDestroy(e.a);
+                cudaEventDestroy(e.b);
             }
             ev[k].clear();
         }
@@ -1005,7 +1049,7 @@ ohao_status wavefront_render(const DScene& sc, const RenderView& view, const Pat
             if (it > 0 && (pp.flags & kFlagSortRays)) {   // bounce rays grouped by direction and origin
                 tm.begin(3, a);
                 bin_queue<1>(sc, s, cur, capacity, st);
-                tm.end(3, a);
+                tm.end(3, a, kBinLaunches);
             }
             if (fetch) cudaMemsetAsync(s.counts + kCtrExtendFetch, 0, 8, st);   // both fetch counters
             tm.begin(0, a);
@@ -1015,7 +1059,7 @@ ohao_status wavefront_render(const DScene& sc, const RenderView& view, const Pat
             if (pp.flags & kFlagSortMaterial) {
                 tm.begin(3, a);
                 bin_queue<0>(sc, s, cur, capacity, st);
-                tm.end(3, a);
+                tm.end(3, a, kBinLaunches);
             }
             cudaMemsetAsync(s.counts + (cur ^ 1), 0, 4, st);
             cudaMemsetAsync(s.counts + 2, 0, 4, st);
