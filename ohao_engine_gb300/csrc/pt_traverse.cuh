@@ -114,9 +114,10 @@ OHAO_D NodeRec load_node(const uint4* __restrict__ nodes, uint32_t ni) {
     return n;
 }
 
+// byte i (0-7) of the 8-byte word hi4:lo4: one byte permute (selector i in
+// its low nibble picks the byte) and a mask
 OHAO_D uint32_t byte_of(uint32_t lo4, uint32_t hi4, int i) {
-    const uint32_t w = (i < 4) ? lo4 : hi4;
-    return (w >> ((i & 3) * 8)) & 0xFFu;
+    return __byte_perm(lo4, hi4, static_cast<uint32_t>(i)) & 0xFFu;
 }
 
 // three-input min / max of sm_100+ (one instruction each; NaN operands are
@@ -130,6 +131,16 @@ OHAO_D float min3f(float a, float b, float c) {
     float d;
     asm("min.f32 %0, %1, %2, %3;" : "=f"(d) : "f"(a), "f"(b), "f"(c));
     return d;
+}
+
+// Two independent fp32 FMAs in one paired instruction of sm_100+
+// (fma.rn.f32x2): each half is rounded exactly as fmaf rounds it.
+OHAO_D void fma2(float x0, float x1, float y0, float y1, float z0, float z1, float& d0, float& d1) {
+    asm("{.reg .b64 x, y, z, d;\n\t"
+        "mov.b64 x, {%2, %3};\n\tmov.b64 y, {%4, %5};\n\tmov.b64 z, {%6, %7};\n\t"
+        "fma.rn.f32x2 d, x, y, z;\n\tmov.b64 {%0, %1}, d;\n\t}"
+        : "=f"(d0), "=f"(d1)
+        : "f"(x0), "f"(x1), "f"(y0), "f"(y1), "f"(z0), "f"(z1));
 }
 
 // byte b of `word` (q) as the float 2^23 + 256 q, exactly: one byte permute
@@ -176,8 +187,13 @@ OHAO_D uint32_t node_test(const NodeRec& n, const RayPre& r, float tmin, float t
         const float qnx = u8f_biased(i < 4 ? nx0 : nx1, b), qfx = u8f_biased(i < 4 ? fx0 : fx1, b);
         const float qny = u8f_biased(i < 4 ? ny0 : ny1, b), qfy = u8f_biased(i < 4 ? fy0 : fy1, b);
         const float qnz = u8f_biased(i < 4 ? nz0 : nz1, b), qfz = u8f_biased(i < 4 ? fz0 : fz1, b);
-        const float t0 = max3f(fmaf(qnx, a[0], bn[0]), fmaf(qny, a[1], bn[1]), fmaf(qnz, a[2], bn[2]));
-        const float t1 = min3f(fmaf(qfx, a[0], bf[0]), fmaf(qfy, a[1], bf[1]), fmaf(qfz, a[2], bf[2]));
+        // near and far side of each axis in one paired FMA
+        float vnx, vfx, vny, vfy, vnz, vfz;
+        fma2(qnx, qfx, a[0], a[0], bn[0], bf[0], vnx, vfx);
+        fma2(qny, qfy, a[1], a[1], bn[1], bf[1], vny, vfy);
+        fma2(qnz, qfz, a[2], a[2], bn[2], bf[2], vnz, vfz);
+        const float t0 = max3f(vnx, vny, vnz);
+        const float t1 = min3f(vfx, vfy, vfz);
         tn[i] = t0;
         const uint32_t meta = byte_of(n.q1.z, n.q1.w, i);
         // t0 <= t1, t0 <= tlimit and t1 >= tmin at once (tmin <= tlimit always)
