@@ -15,7 +15,9 @@
 // [pixels][C8] FP32. Weights W [cout_n][k_pad] BF16, k = tap*cin8 + ci
 // (tap = 3*dy + dx), and the transposed copy Wt [cin_n][k2_pad],
 // k2 = tap*cout8 + co, for the data gradient.
+#include <cuda.h>
 #include <cuda_bf16.h>
+#include <cudaTypedefs.h>
 
 #include <algorithm>
 
@@ -438,6 +440,16 @@ __global__ void __launch_bounds__(kThreads) k_conv_halo(ConvArgs a, int* err_fla
     const uint32_t hbase = umma::smem_u32(halo);
     const int kchunks = a.k_pad / kBK;
     const int kreal = 9 * a.cin8;
+    // A descriptor offset (16-byte units) of each K step of 16: descriptors
+    // are linear in the start address, so the MMA loop adds it to a base
+    __shared__ uint32_t s_off[9 * 256 / 16];
+    for (int k = threadIdx.x; k < kreal / 16; k += kThreads) {
+        const int k0 = k * 16;
+        const int tap = k0 / a.cin8, cb = (k0 - tap * a.cin8) >> 3;
+        const int dy = tap / 3, dx = tap % 3;
+        s_off[k] = static_cast<uint32_t>(((dy * cb_count + cb) * kHaloX + dx) * 16) >> 4;
+    }
+    const uint64_t da0 = umma::smem_desc(hbase, kHaloX * 16, 128);
     bool ok = true;
     for (int kc = 0; kc < kchunks && ok; ++kc) {
         const int s = kc % kStages;
@@ -462,13 +474,8 @@ __global__ void __launch_bounds__(kThreads) k_conv_halo(ConvArgs a, int* err_fla
             for (int i = 0; i < kBK / 16; ++i) {
                 const int k0 = kc * kBK + i * 16;
                 if (k0 >= kreal) break;   // zero-padded tail of K
-                const int tap = k0 / a.cin8, cb = (k0 - tap * a.cin8) >> 3;
-                const int dy = tap / 3, dx = tap % 3;
-                const uint64_t da =
-                    umma::smem_desc(hbase + static_cast<uint32_t>(((dy * cb_count + cb) * kHaloX + dx) * 16),
-                                    kHaloX * 16, 128);
                 const uint64_t db = umma::smem_desc(sbu + i * 256, 128, 1024);
-                umma::mma_bf16(tmem, da, db, idesc, k0 > 0);
+                umma::mma_bf16(tmem, da0 + s_off[k0 >> 4], db, idesc, k0 > 0);
             }
             umma::mma_commit(&ss.bar[s]);
         }
@@ -508,6 +515,256 @@ __global__ void __launch_bounds__(kThreads) k_conv_halo(ConvArgs a, int* err_fla
     umma::tc_fence_before();
     __syncthreads();
     if (warp == 0) umma::tmem_dealloc(tmem, ncols);
+}
+
+// Forward convolution with TMA-filled neighbourhoods, warp-specialised and
+// persistent (the wide levels' layers; the upsample + concatenation layers
+// after their upsampled source is written out at full resolution by
+// k_upsample2). A tile is R image rows y0 .. y0+R-1 (R = 1, 2 or 4) of 128
+// output pixels x0 .. x0+127; its (R+2) x 130-pixel input neighbourhood is
+// laid out [channel block][row 0..R+1][x 0..129][8 channels] (one slab of
+// ws_slab(R) bytes per channel block), filled by one TMA box per channel
+// block (8 channels x 130 x (R+2) rows; zero outside the image, which is the
+// padding) and read by tap descriptors: output row r, tap (dy, dx), channel
+// block cb starts at cb * slab + ((r + dy) * 130 + dx) * 16, SBO 128 B (the
+// next 8 pixels), LBO slab (the next 8 channels). The R rows share the fill
+// ((R+2)/R input rows per output row instead of 3). The layer's weights stay
+// in shared memory. Roles: warp 0 issues the TMA boxes into a ring of
+// nstages neighbourhood buffers, warp 1 issues the MMAs of a tile into one of
+// two sets of R tensor-memory accumulators, warps 2-5 (one per 32-lane
+// quarter of tensor memory) read the accumulators, add the bias, apply ReLU
+// and store while the next tile is being multiplied. mbarriers hand over
+// each buffer and accumulator set; every wait is bounded and also ends when
+// another role has given up (ws.abort).
+constexpr int kTmaX = kBM + 2;
+constexpr int kWsThreads = 192;       // 6 warps
+constexpr int kWsMaxStages = 4;
+
+__host__ __device__ inline uint32_t ws_slab(int rows) {   // (R+2) * 130 * 16 B, rounded up to 128 B
+    return (static_cast<uint32_t>(rows + 2) * kTmaX * 16u + 127u) & ~127u;
+}
+
+constexpr int kWsMaxKSteps = 9 * 256 / 16;   // K steps of 16 for cin8 <= 256
+
+struct WsSmem {
+    // descriptor offsets (16-byte units) of each K step: A within a
+    // neighbourhood buffer (channel block, tap), B within the weights
+    uint32_t off_a[kWsMaxKSteps], off_b[kWsMaxKSteps];
+    uint64_t full[kWsMaxStages], empty[kWsMaxStages];
+    uint64_t acc_full[2], acc_empty[2];
+    uint64_t drain;
+    uint32_t tmem;
+    int abort;
+};
+
+// weights after the nstages neighbourhood buffers, on a 1024-byte boundary
+__host__ __device__ inline uint32_t ws_weights_off(int cb_total, int nstages, int rows) {
+    return (static_cast<uint32_t>(nstages) * static_cast<uint32_t>(cb_total) * ws_slab(rows) + 1023u) & ~1023u;
+}
+__host__ __device__ inline uint32_t ws_smem_bytes(int cb_total, int nstages, int rows, int bn, int k_pad) {
+    return ws_weights_off(cb_total, nstages, rows) +
+           static_cast<uint32_t>(k_pad / kBK) * static_cast<uint32_t>(bn) * kBK * 2;
+}
+
+// bounded wait that also gives up when another role has aborted
+__device__ __forceinline__ bool ws_wait(uint64_t* bar, uint32_t parity, volatile int* abort) {
+    for (uint32_t i = 0; i < umma::kSpinLimit; ++i) {
+        if (umma::mbar_try_wait(bar, parity)) return true;
+        if ((i & 63u) == 63u && *abort) return false;
+    }
+    *abort = 1;
+    return false;
+}
+
+__global__ void __launch_bounds__(kWsThreads) k_conv_ws(ConvArgs a, const __grid_constant__ CUtensorMap tm_a,
+                                                        const __grid_constant__ CUtensorMap tm_b, int cb_a, int ntiles,
+                                                        int nstages, int rows, int* err_flag) {
+    extern __shared__ __align__(1024) uint8_t dsm_raw[];
+    __shared__ WsSmem ws;
+    // offsets are from a 1024-byte aligned base (TMA boxes land on 128-byte
+    // boundaries); the launch adds 1024 bytes of slack
+    uint8_t* dsm = reinterpret_cast<uint8_t*>((reinterpret_cast<uintptr_t>(dsm_raw) + 1023u) & ~uintptr_t{1023});
+    const int bn = a.bn;
+    const int cb_total = a.cin8 / 8;
+    const uint32_t slab = ws_slab(rows);
+    const uint32_t w_off = ws_weights_off(cb_total, nstages, rows);
+    const uint32_t stage_bytes = static_cast<uint32_t>(cb_total) * slab;
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    uint32_t ncols = 32;
+    while (ncols < static_cast<uint32_t>(bn)) ncols <<= 1;
+    const uint32_t set_cols = static_cast<uint32_t>(rows) * ncols;   // one accumulator set: R accumulators
+    if (threadIdx.x == 0) {
+        for (int s = 0; s < nstages; ++s) {
+            umma::mbar_init(&ws.full[s], 1);
+            umma::mbar_init(&ws.empty[s], 1);
+        }
+        for (int k = 0; k < 2; ++k) {
+            umma::mbar_init(&ws.acc_full[k], 1);
+            umma::mbar_init(&ws.acc_empty[k], 4);
+        }
+        umma::mbar_init(&ws.drain, 1);
+        ws.abort = 0;
+        umma::mbar_fence_init();
+        umma::tma_prefetch_desc(&tm_a);
+        if (cb_a < cb_total) umma::tma_prefetch_desc(&tm_b);
+    }
+    if (warp == 0) umma::tmem_alloc(&ws.tmem, 2 * set_cols);
+    // resident weights: chunk kc of 64 K at w_off + kc * bn * 128, in the
+    // K-major core-matrix order of k_conv (row n, 16-byte vector kb at
+    // ((n/8)*8 + kb)*128 + (n%8)*16)
+    const int ksteps = 9 * a.cin8 / 16;
+    for (int k = threadIdx.x; k < ksteps; k += kWsThreads) {
+        const int k0 = k * 16;
+        const int tap = k0 / a.cin8, cb = (k0 - tap * a.cin8) >> 3;
+        const int dy = tap / 3, dx = tap - 3 * (tap / 3);
+        ws.off_a[k] = (static_cast<uint32_t>(cb) * slab + static_cast<uint32_t>((dy * kTmaX + dx) * 16)) >> 4;
+        ws.off_b[k] = (static_cast<uint32_t>(k0 / kBK) * static_cast<uint32_t>(bn) * 128u + ((k0 % kBK) / 16) * 256u) >> 4;
+    }
+    const int kchunks = a.k_pad / kBK;
+    for (int L = threadIdx.x; L < kchunks * bn * 8; L += kWsThreads) {
+        const int kc = L / (bn * 8), l = L - kc * bn * 8;
+        const int r = l & 7, kb = (l >> 3) & 7, nb = l >> 6;
+        *reinterpret_cast<uint4*>(dsm + w_off + static_cast<uint32_t>(L) * 16) =
+            *reinterpret_cast<const uint4*>(a.w + static_cast<int64_t>(nb * 8 + r) * a.k_pad + kc * kBK + kb * 8);
+    }
+    umma::fence_async_smem();
+    umma::tc_fence_before();
+    __syncthreads();
+    umma::tc_fence_after();
+    const uint32_t tmem = ws.tmem;
+    const int xtiles = (a.g.w + kBM - 1) / kBM;
+    const int ygroups = (a.g.h + rows - 1) / rows;
+    const int first = static_cast<int>(blockIdx.x), step = static_cast<int>(gridDim.x);
+    volatile int* abort = &ws.abort;
+
+    if (warp == 0) {
+        if (lane == 0) {   // producer: TMA boxes of tile i into stage i % nstages
+            const uint32_t bytes = static_cast<uint32_t>(cb_total) * static_cast<uint32_t>(rows + 2) * kTmaX * 16u;
+            int i = 0, issued = 0;
+            for (int t = first; t < ntiles; t += step, ++i) {
+                const int s = i % nstages;
+                if (i >= nstages && !ws_wait(&ws.empty[s], static_cast<uint32_t>(i / nstages - 1) & 1u, abort)) break;
+                const int x0 = (t % xtiles) * kBM;
+                const int ny = t / xtiles;
+                const int y0 = (ny % ygroups) * rows, n = ny / ygroups;
+                uint8_t* dst = dsm + static_cast<uint32_t>(s) * stage_bytes;
+                umma::mbar_arrive_expect_tx(&ws.full[s], bytes);
+                for (int j = 0; j < cb_total; ++j) {
+                    if (j < cb_a)
+                        umma::tma_load_4d(dst + static_cast<uint32_t>(j) * slab, &tm_a, j * 8, x0 - 1, y0 - 1, n,
+                                          &ws.full[s]);
+                    else
+                        umma::tma_load_4d(dst + static_cast<uint32_t>(j) * slab, &tm_b, (j - cb_a) * 8, x0 - 1,
+                                          y0 - 1, n, &ws.full[s]);
+                }
+                issued = i + 1;
+            }
+            // copies in flight land before the CTA's shared memory is released:
+            // the last nstages issued tiles' fills (bounded, regardless of abort)
+            for (int k = issued - nstages > 0 ? issued - nstages : 0; k < issued; ++k)
+                if (!umma::mbar_wait(&ws.full[k % nstages], static_cast<uint32_t>(k / nstages) & 1u))
+                    atomicOr(err_flag, 2);
+        }
+    } else if (warp == 1) {
+        if (lane == 0) {   // MMA issuer: tile i from stage i % nstages into accumulator set i & 1
+            const uint32_t idesc = umma::idesc_bf16(kBM, static_cast<uint32_t>(bn), false, false);
+            // descriptors are linear in the start address (its low 14 bits,
+            // in 16-byte units; every address here is below 256 KB), so a K
+            // step's descriptor is a base plus the step's offset
+            const uint64_t db0 = umma::smem_desc(umma::smem_u32(dsm + w_off), 128, 1024);
+            int i = 0;
+            for (int t = first; t < ntiles; t += step, ++i) {
+                const int s = i % nstages, acc = i & 1;
+                if (!ws_wait(&ws.full[s], static_cast<uint32_t>(i / nstages) & 1u, abort)) break;
+                if (i >= 2 && !ws_wait(&ws.acc_empty[acc], static_cast<uint32_t>((i >> 1) - 1) & 1u, abort)) break;
+                umma::tc_fence_after();
+                const uint64_t da0 = umma::smem_desc(umma::smem_u32(dsm + static_cast<uint32_t>(s) * stage_bytes), slab, 128);
+                for (int r = 0; r < rows; ++r) {
+                    const uint32_t d = tmem + static_cast<uint32_t>(acc) * set_cols + static_cast<uint32_t>(r) * ncols;
+                    const uint64_t dar = da0 + static_cast<uint64_t>(r * kTmaX);   // output row r: input rows r + dy
+                    for (int k = 0; k < ksteps; ++k)
+                        umma::mma_bf16(d, dar + ws.off_a[k], db0 + ws.off_b[k], idesc, k > 0);
+                }
+                umma::mma_commit(&ws.empty[s]);       // the stage is read
+                umma::mma_commit(&ws.acc_full[acc]);  // the accumulator set is complete
+            }
+            // every MMA issued has completed before the columns are freed
+            // (bounded, regardless of abort)
+            umma::mma_commit(&ws.drain);
+            if (!umma::mbar_wait(&ws.drain, 0)) atomicOr(err_flag, 2);
+        }
+    } else {
+        // epilogue: warp w reads tensor-memory lanes 32 (w % 4) .. +31
+        const int q = warp & 3;
+        const int row = q * 32 + lane;
+        int i = 0;
+        for (int t = first; t < ntiles; t += step, ++i) {
+            const int acc = i & 1;
+            // the whole warp leaves together (tcgen05.ld below is warp-collective)
+            if (!__all_sync(0xFFFFFFFFu, ws_wait(&ws.acc_full[acc], static_cast<uint32_t>(i >> 1) & 1u, abort))) break;
+            umma::tc_fence_after();
+            const int x0 = (t % xtiles) * kBM;
+            const int ny = t / xtiles;
+            const int y0 = (ny % ygroups) * rows, n = ny / ygroups;
+            for (int r = 0; r < rows; ++r) {
+                const int y = y0 + r;
+                const bool live = x0 + row < a.g.w && y < a.g.h;
+                const int64_t p = (static_cast<int64_t>(n) * a.g.h + y) * a.g.w + x0 + row;
+                const uint32_t trow = tmem + static_cast<uint32_t>(acc) * set_cols + static_cast<uint32_t>(r) * ncols +
+                                      (static_cast<uint32_t>(q * 32) << 16);
+                for (int c0 = 0; c0 < bn; c0 += 32) {
+                    float v[32];
+                    umma::tmem_ld32(trow + c0, v);   // warp-collective: every lane loads, the row test comes after
+#pragma unroll
+                    for (int c8 = 0; c8 < 32; c8 += 8) {
+                        const int c = c0 + c8;
+                        if (live && c < a.cout8) {
+                            float o[8];
+#pragma unroll
+                            for (int k = 0; k < 8; ++k) {
+                                float x = v[c8 + k] + ((c + k < a.cout) ? a.bias[c + k] : 0.0f);
+                                if (a.relu) x = fmaxf(x, 0.0f);
+                                o[k] = (c + k < a.cout) ? x : 0.0f;
+                            }
+                            if (a.yf) {
+                                float4* op = reinterpret_cast<float4*>(a.yf + p * a.cout8 + c);
+                                op[0] = make_float4(o[0], o[1], o[2], o[3]);
+                                op[1] = make_float4(o[4], o[5], o[6], o[7]);
+                            } else {
+                                *reinterpret_cast<uint4*>(a.yout + p * a.cout8 + c) = pack8(o);
+                            }
+                        }
+                    }
+                }
+            }
+            umma::tc_fence_before();
+            __syncwarp();
+            if (lane == 0) umma::mbar_arrive(&ws.acc_empty[acc]);
+        }
+    }
+    __syncwarp();
+    umma::tc_fence_before();
+    __syncthreads();
+    if (threadIdx.x == 0 && ws.abort) atomicOr(err_flag, 2);
+    if (warp == 0) umma::tmem_dealloc(tmem, 2 * set_cols);
+}
+
+// out[p][c] = in[low-resolution pixel of p][c]: the nearest 2x upsample of
+// an NHWC BF16 tensor, 8 channels (16 bytes) per thread.
+__global__ void k_upsample2(const __nv_bfloat16* __restrict__ in, __nv_bfloat16* __restrict__ out, Geo g, int cs) {
+    const int vpp = cs / 8;
+    const int64_t total = g.npix * vpp;
+    for (int64_t i = blockIdx.x * static_cast<int64_t>(blockDim.x) + threadIdx.x; i < total;
+         i += static_cast<int64_t>(gridDim.x) * blockDim.x) {
+        const int cv = static_cast<int>(i % vpp);
+        const int64_t p = i / vpp;
+        const int x = static_cast<int>(p % g.w);
+        const int64_t t = p / g.w;
+        const int y = static_cast<int>(t % g.h);
+        const int64_t n = t / g.h;
+        const int64_t lq = (n * (g.h >> 1) + (y >> 1)) * (g.w >> 1) + (x >> 1);
+        reinterpret_cast<uint4*>(out)[i] = reinterpret_cast<const uint4*>(in)[lq * vpp + cv];
+    }
 }
 
 // ---- elementwise kernels ----
@@ -771,14 +1028,119 @@ size_t conv_halo_smem_bytes(int cin8, int bn) {
     return ((halo_bytes(cin8) + 1023) & ~static_cast<size_t>(1023)) + static_cast<size_t>(kStages) * bn * kBK * 2 + 1024;
 }
 
+namespace {
+
+// cuTensorMapEncodeTiled through the runtime's driver entry point (no link
+// against the driver library); null when the driver does not offer it.
+PFN_cuTensorMapEncodeTiled_v12000 tensor_map_encoder() {
+    static const PFN_cuTensorMapEncodeTiled_v12000 fn = [] {
+        void* p = nullptr;
+        cudaDriverEntryPointQueryResult q{};
+        if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &p, 12000, cudaEnableDefault, &q) !=
+                cudaSuccess ||
+            q != cudaDriverEntryPointSuccess) {
+            cudaGetLastError();
+            return static_cast<PFN_cuTensorMapEncodeTiled_v12000>(nullptr);
+        }
+        return reinterpret_cast<PFN_cuTensorMapEncodeTiled_v12000>(p);
+    }();
+    return fn;
+}
+
+// NHWC BF16 activations [n][h][w][cs] as the 4-D tensor (cs, w, h, n) with
+// a box of 8 channels x bx pixels x br rows x 1 image.
+bool encode_activations(CUtensorMap* m, const __nv_bfloat16* base, int cs, int w, int h, int n, int bx, int br) {
+    const auto enc = tensor_map_encoder();
+    if (!enc || (reinterpret_cast<uintptr_t>(base) & 15u) || cs % 8) return false;
+    const cuuint64_t dims[4] = {static_cast<cuuint64_t>(cs), static_cast<cuuint64_t>(w), static_cast<cuuint64_t>(h),
+                                static_cast<cuuint64_t>(n)};
+    const cuuint64_t strides[3] = {static_cast<cuuint64_t>(cs) * 2, static_cast<cuuint64_t>(cs) * 2 * w,
+                                   static_cast<cuuint64_t>(cs) * 2 * w * h};
+    const cuuint32_t box[4] = {8u, static_cast<cuuint32_t>(bx), static_cast<cuuint32_t>(br), 1u};
+    const cuuint32_t es[4] = {1u, 1u, 1u, 1u};
+    return enc(m, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 4, const_cast<__nv_bfloat16*>(base), dims, strides, box, es,
+               CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_128B,
+               CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) == CUDA_SUCCESS;
+}
+
+// The warp-specialised TMA forward (k_conv_ws) when the layer fits it:
+// false leaves the layer to the other kernels. An upsample + concatenation
+// layer first writes its upsampled source at full resolution into
+// a.up_scratch.
+bool try_conv_ws(const ConvArgs& a, int* err_flag, cudaStream_t st) {
+    const bool single = a.c1 == 0 && !a.up0;
+    const bool concat = a.up0 && a.c1 > 0 && a.up_scratch && a.c0 % 8 == 0 && a.c0s == a.c0 && a.g.w % 2 == 0 &&
+                        a.g.h % 2 == 0;
+    if (!(single || concat) || a.n_tiles != 1 || a.cin8 % 16 != 0 || a.cin8 > 256 || a.g.w < kHaloMinW) return false;
+    int ncols = 32;
+    while (ncols < a.bn) ncols <<= 1;
+    const int cb_total = a.cin8 / 8;
+    // the most rows per tile (then the most stages, >= 2 where possible)
+    // whose buffers fit the shared memory and whose two accumulator sets fit
+    // the tensor memory
+    int rows = 0, nstages = 0;
+    size_t smem = 0;
+    for (int r : {4, 2, 1}) {
+        if (2 * r * ncols > 512) continue;
+        for (int s = kWsMaxStages; s >= 1; --s) {
+            const size_t b = static_cast<size_t>(ws_smem_bytes(cb_total, s, r, a.bn, a.k_pad)) + 1024;   // + base alignment
+            if (b <= 227 * 1024 && (s >= 2 || r == 1)) {
+                rows = r;
+                nstages = s;
+                smem = b;
+                break;
+            }
+        }
+        if (rows) break;
+    }
+    if (!rows) return false;
+    CUtensorMap ta{}, tb{};
+    int cb_a = cb_total;
+    if (single) {
+        if (!encode_activations(&ta, a.x0, a.c0s, a.g.w, a.g.h, a.g.n, kTmaX, rows + 2)) return false;
+        tb = ta;
+    } else {
+        cb_a = a.c0 / 8;
+        if (!encode_activations(&ta, a.up_scratch, a.c0s, a.g.w, a.g.h, a.g.n, kTmaX, rows + 2)) return false;
+        if (!encode_activations(&tb, a.x1, a.c1s, a.g.w, a.g.h, a.g.n, kTmaX, rows + 2)) return false;
+    }
+    if (cudaFuncSetAttribute(k_conv_ws, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(smem)) !=
+            cudaSuccess ||
+        cudaFuncSetAttribute(k_conv_ws, cudaFuncAttributePreferredSharedMemoryCarveout,
+                             cudaSharedmemCarveoutMaxShared) != cudaSuccess) {
+        cudaGetLastError();
+        return false;
+    }
+    int dev = 0, sms = 0, per_sm = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_conv_ws, kWsThreads, smem);
+    if (sms <= 0 || per_sm <= 0) {
+        cudaGetLastError();
+        return false;
+    }
+    // resident CTAs whose accumulator sets fit the SM's 512 tensor-memory
+    // columns together, so that no CTA's allocation waits for another to finish
+    per_sm = std::min(per_sm, 512 / (2 * rows * ncols));
+    if (concat)
+        k_upsample2<<<grid_for(a.g.npix * (a.c0s / 8), 256), 256, 0, st>>>(a.x0, a.up_scratch, a.g, a.c0s);
+    const int64_t tiles = static_cast<int64_t>(a.g.n) * ((a.g.h + rows - 1) / rows) * ((a.g.w + kBM - 1) / kBM);
+    const int grid = static_cast<int>(std::min<int64_t>(tiles, static_cast<int64_t>(sms) * per_sm));
+    k_conv_ws<<<grid, kWsThreads, smem, st>>>(a, ta, tb, cb_a, static_cast<int>(tiles), nstages, rows, err_flag);
+    return true;
+}
+
+}  // namespace
+
 cudaError_t launch_conv(int mode, const ConvArgs& a, int wgrad_splits, int* err_flag, cudaStream_t st) {
+    if (mode == kFwd && try_conv_ws(a, err_flag, st)) return cudaGetLastError();
     const size_t smem = conv_smem_bytes(a.bn);
     const size_t hsmem = conv_halo_smem_bytes(a.cin8, a.bn);
     // the neighbourhood kernel for wide rows of single-source inputs; the
     // upsample + skip-concatenation layers stay on the gather (measured: their
     // large neighbourhoods leave one or two CTAs per SM and the two sources
     // split the fill's warps)
-    if (mode == kFwd && a.g.w >= kHaloMinW && a.c1 == 0 && a.cin8 % 16 == 0 && a.n_tiles == 1 &&
+    if (mode == kFwd && a.g.w >= kHaloMinW && a.c1 == 0 && a.cin8 % 16 == 0 && a.cin8 <= 256 && a.n_tiles == 1 &&
         hsmem <= 227 * 1024) {
         cudaFuncSetAttribute(k_conv_halo, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(hsmem));
         const int64_t tiles = static_cast<int64_t>(a.g.n) * a.g.h * ((a.g.w + kBM - 1) / kBM);

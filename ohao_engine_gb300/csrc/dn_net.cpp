@@ -100,6 +100,7 @@ struct ohao_dn_ctx {
     bool grads_ready = false;
     int adam_t = 0;
     Buf err_flag, loss_acc;
+    Buf up_scratch;       // the upsampled source of an upsample + concatenation layer's forward
     Geo g0{0, 0, 0, 0};   // grid of the last forward
 };
 
@@ -213,6 +214,13 @@ ohao_status alloc_acts(ohao_dn_ctx* ctx, bool grads) {
         if (grads && !t.grad.p) DN_CK(t.grad.alloc(pix * t.c8 * 4), "activation grads");
     }
     if (grads) ctx->grads_ready = true;
+    if (!ctx->up_scratch.p) {   // the largest upsampled source, at its layer's resolution
+        size_t bytes = 0;
+        for (const Layer& l : ctx->L)
+            if (l.up0)
+                bytes = std::max(bytes, static_cast<size_t>(ctx->max_pixels >> (2 * l.level)) * ctx->T[l.in0].c8 * 2);
+        if (bytes) DN_CK(ctx->up_scratch.alloc(bytes), "upsample scratch");
+    }
     return OHAO_OK;
 }
 
@@ -291,6 +299,8 @@ ohao_status forward(ohao_dn_ctx* ctx, const Geo& g0, cudaStream_t st) {
             ConvArgs a = conv_args(ctx, l, g0);
             a.bn = l.s.cout_n;
             a.n_tiles = 1;
+            if (l.up0 && static_cast<size_t>(a.g.npix) * a.c0s * 2 <= ctx->up_scratch.n)
+                a.up_scratch = ctx->up_scratch.as<__nv_bfloat16>();
             DN_CK(launch_conv(kFwd, a, 1, ctx->err_flag.as<int>(), st), "conv forward");
         } else {
             const Tensor& ti = ctx->T[op.idx];

@@ -55,6 +55,9 @@ struct ConvArgs {
     float* dx1;
     // weight-gradient output (accumulated, FP32 [cout][k_pad])
     float* dw;
+    // forward of an upsample + concatenation layer: room for its upsampled
+    // source at full resolution ([pix][c0s] BF16), or null
+    __nv_bfloat16* up_scratch;
     int bn;                         // MMA N of this launch (<= 256, multiple of 16)
     int n_tiles;                    // N tiles (forward/data grad: grid.y; weight grad: grid.x)
 };
