@@ -11,13 +11,14 @@
 // ReLU and the BF16 store (forward), the scatter into the input gradients
 // (data gradient), or FP32 atomics into the weight gradient.
 //
-// Shapes: activations [pixels][C8] BF16 with C8 = round_up(C, 8); gradients
-// [pixels][C8] FP32. Weights W [cout_n][k_pad] BF16, k = tap*cin8 + ci
+// Shapes: BF16 activations are channel-blocked, [n][C8/8][h][w][8] with
+// C8 = round_up(C, 8): the 8 channels [8 cb, 8 cb + 8) of pixel (n, y, x)
+// are 16 bytes at element offset ((n * C8/8 + cb) * h * w + y * w + x) * 8,
+// so a row of one channel block is contiguous (the neighbourhood fill of
+// k_conv_ws copies 130-pixel runs with single bulk copies). Gradients are [pixels][C8] FP32. Weights W [cout_n][k_pad] BF16, k = tap*cin8 + ci
 // (tap = 3*dy + dx), and the transposed copy Wt [cin_n][k2_pad],
 // k2 = tap*cout8 + co, for the data gradient.
-#include <cuda.h>
 #include <cuda_bf16.h>
-#include <cudaTypedefs.h>
 
 #include <algorithm>
 
@@ -74,18 +75,29 @@ __device__ __forceinline__ Pix pix_of(const Geo& g, int p) {
     return r;
 }
 
+// Element offset of channel block cb of pixel rem = y * w + x of image n in
+// a channel-blocked tensor of cbs blocks and hw = h * w pixels per image.
+__device__ __forceinline__ int64_t blk(int64_t n, int cb, int cbs, int64_t hw, int64_t rem) {
+    return ((n * cbs + cb) * hw + rem) * 8;
+}
+
 // 8 input channels [c0, c0+8) of the (possibly upsampled + concatenated)
-// convolution input at pixel (n, qy, qx) = flat index q of the full-res grid.
-__device__ __forceinline__ uint4 load_input8(const ConvArgs& a, int q, int n, int qy, int qx, int c0) {
+// convolution input at pixel (n, qy, qx) of the full-res grid.
+__device__ __forceinline__ uint4 load_input8(const ConvArgs& a, int n, int qy, int qx, int c0) {
     if (c0 < a.c0) {
         if (a.up0) {   // nearest 2x upsample of a half-resolution source
-            const int lq = (n * (a.g.h >> 1) + (qy >> 1)) * (a.g.w >> 1) + (qx >> 1);
-            return *reinterpret_cast<const uint4*>(a.x0 + static_cast<int64_t>(lq) * a.c0s + c0);
+            const int hw2 = (a.g.w >> 1);
+            return *reinterpret_cast<const uint4*>(
+                a.x0 + blk(n, c0 >> 3, a.c0s >> 3, static_cast<int64_t>(a.g.h >> 1) * hw2,
+                           static_cast<int64_t>(qy >> 1) * hw2 + (qx >> 1)));
         }
-        return *reinterpret_cast<const uint4*>(a.x0 + static_cast<int64_t>(q) * a.c0s + c0);
+        return *reinterpret_cast<const uint4*>(
+            a.x0 + blk(n, c0 >> 3, a.c0s >> 3, static_cast<int64_t>(a.g.h) * a.g.w, static_cast<int64_t>(qy) * a.g.w + qx));
     }
     if (c0 - a.c0 < a.c1)
-        return *reinterpret_cast<const uint4*>(a.x1 + static_cast<int64_t>(q) * a.c1s + (c0 - a.c0));
+        return *reinterpret_cast<const uint4*>(a.x1 + blk(n, (c0 - a.c0) >> 3, a.c1s >> 3,
+                                                          static_cast<int64_t>(a.g.h) * a.g.w,
+                                                          static_cast<int64_t>(qy) * a.g.w + qx));
     return make_uint4(0, 0, 0, 0);
 }
 
@@ -96,8 +108,10 @@ __device__ __forceinline__ uint4 load_dz8(const ConvArgs& a, int64_t q, int c0) 
     const float4 g0 = gp[0], g1 = gp[1];
     float f[8] = {g0.x, g0.y, g0.z, g0.w, g1.x, g1.y, g1.z, g1.w};
     if (a.relu) {
+        const int64_t hw = static_cast<int64_t>(a.g.h) * a.g.w;
+        const int64_t n = q / hw;
         float yv[8];
-        unpack8(*reinterpret_cast<const uint4*>(a.y + q * a.cout8 + c0), yv);
+        unpack8(*reinterpret_cast<const uint4*>(a.y + blk(n, c0 >> 3, a.cout8 >> 3, hw, q - n * hw)), yv);
 #pragma unroll
         for (int i = 0; i < 8; ++i)
             if (!(yv[i] > 0.0f)) f[i] = 0.0f;
@@ -138,7 +152,7 @@ __device__ __forceinline__ void gather(const ConvArgs& a, const Pix (&rows)[kRow
             const int qy = rows[it].y + ty, qx = rows[it].x + tx;
             if (kvalid && rows[it].n >= 0 && qy >= 0 && qy < a.g.h && qx >= 0 && qx < a.g.w) {
                 const int q = (rows[it].n * a.g.h + qy) * a.g.w + qx;
-                if constexpr (kMode == kFwd) v[it] = load_input8(a, q, rows[it].n, qy, qx, c0);
+                if constexpr (kMode == kFwd) v[it] = load_input8(a, rows[it].n, qy, qx, c0);
                 else v[it] = load_dz8(a, q, c0);
             }
         }
@@ -178,7 +192,7 @@ __device__ __forceinline__ void gather(const ConvArgs& a, const Pix (&rows)[kRow
                 const int tap = f / a.cin8, c0 = f - tap * a.cin8;
                 const int qy = pp.y + tap / 3 - 1, qx = pp.x + tap % 3 - 1;
                 if (qy >= 0 && qy < a.g.h && qx >= 0 && qx < a.g.w)
-                    w = load_input8(a, (pp.n * a.g.h + qy) * a.g.w + qx, pp.n, qy, qx, c0);
+                    w = load_input8(a, pp.n, qy, qx, c0);
             }
             *reinterpret_cast<uint4*>(sb + L * 16) = w;
         }
@@ -286,6 +300,8 @@ __global__ void __launch_bounds__(kThreads) k_conv(ConvArgs a, int* err_flag) {
         const uint32_t trow = tmem + (static_cast<uint32_t>(warp * 32) << 16);
         if constexpr (kMode == kFwd) {
             const int64_t p = mtile * kBM + row;
+            const int64_t hw = static_cast<int64_t>(a.g.h) * a.g.w;
+            const int64_t pn = p / hw;
             for (int c = 0; c < bn; c += 8) {
                 float v[8];
                 umma::tmem_ld8(trow + c, v);
@@ -302,7 +318,7 @@ __global__ void __launch_bounds__(kThreads) k_conv(ConvArgs a, int* err_flag) {
                         o[0] = make_float4(v[0], v[1], v[2], v[3]);
                         o[1] = make_float4(v[4], v[5], v[6], v[7]);
                     } else {
-                        *reinterpret_cast<uint4*>(a.yout + p * a.cout8 + co) = pack8(v);
+                        *reinterpret_cast<uint4*>(a.yout + blk(pn, co >> 3, a.cout8 >> 3, hw, p - pn * hw)) = pack8(v);
                     }
                 }
             }
@@ -429,7 +445,7 @@ __global__ void __launch_bounds__(kThreads) k_conv_halo(ConvArgs a, int* err_fla
                 const int qy = y - 1 + r, qx = x0 - 1 + j;
                 dst[u] = static_cast<uint32_t>(((r * cb_count + cb) * kHaloX + j) * 16);
                 if (qy >= 0 && qy < a.g.h && qx >= 0 && qx < a.g.w)
-                    v[u] = load_input8(a, (n * a.g.h + qy) * a.g.w + qx, n, qy, qx, cb * 8);
+                    v[u] = load_input8(a, n, qy, qx, cb * 8);
             }
         }
 #pragma unroll
@@ -507,7 +523,8 @@ __global__ void __launch_bounds__(kThreads) k_conv_halo(ConvArgs a, int* err_fla
                     o[0] = make_float4(v[0], v[1], v[2], v[3]);
                     o[1] = make_float4(v[4], v[5], v[6], v[7]);
                 } else {
-                    *reinterpret_cast<uint4*>(a.yout + p * a.cout8 + c) = pack8(v);
+                    *reinterpret_cast<uint4*>(a.yout + blk(n, c >> 3, a.cout8 >> 3, static_cast<int64_t>(a.g.h) * a.g.w,
+                                                           static_cast<int64_t>(y) * a.g.w + x0 + row)) = pack8(v);
                 }
             }
         }
@@ -517,31 +534,33 @@ __global__ void __launch_bounds__(kThreads) k_conv_halo(ConvArgs a, int* err_fla
     if (warp == 0) umma::tmem_dealloc(tmem, ncols);
 }
 
-// Forward convolution with TMA-filled neighbourhoods, warp-specialised and
+// Forward convolution with bulk-copied neighbourhoods, warp-specialised and
 // persistent (the wide levels' layers; the upsample + concatenation layers
 // after their upsampled source is written out at full resolution by
 // k_upsample2). A tile is R image rows y0 .. y0+R-1 (R = 1, 2 or 4) of 128
 // output pixels x0 .. x0+127; its (R+2) x 130-pixel input neighbourhood is
 // laid out [channel block][row 0..R+1][x 0..129][8 channels] (one slab of
-// ws_slab(R) bytes per channel block), filled by one TMA box per channel
-// block (8 channels x 130 x (R+2) rows; zero outside the image, which is the
-// padding) and read by tap descriptors: output row r, tap (dy, dx), channel
-// block cb starts at cb * slab + ((r + dy) * 130 + dx) * 16, SBO 128 B (the
-// next 8 pixels), LBO slab (the next 8 channels). The R rows share the fill
-// ((R+2)/R input rows per output row instead of 3). The layer's weights stay
-// in shared memory. Roles: warp 0 issues the TMA boxes into a ring of
-// nstages neighbourhood buffers, warp 1 issues the MMAs of a tile into one of
-// two sets of R tensor-memory accumulators, warps 2-5 (one per 32-lane
-// quarter of tensor memory) read the accumulators, add the bias, apply ReLU
-// and store while the next tile is being multiplied. mbarriers hand over
-// each buffer and accumulator set; every wait is bounded and also ends when
-// another role has given up (ws.abort).
-constexpr int kTmaX = kBM + 2;
-constexpr int kWsThreads = 192;       // 6 warps
+// ws_slab(R) bytes per channel block). In the channel-blocked layout a row
+// of a channel block is contiguous, so the fill is one cp.async.bulk per
+// (channel block, row), with zeros written where the neighbourhood leaves
+// the image (the padding). Tap descriptors read it in place: output row r,
+// tap (dy, dx), channel block cb starts at cb * slab + ((r + dy) * 130 + dx)
+// * 16, SBO 128 B (the next 8 pixels), LBO slab (the next 8 channels). The R
+// rows share the fill ((R+2)/R input rows per output row instead of 3). The
+// layer's weights and bias stay in shared memory. Roles: warp 0 fills a ring
+// of nstages neighbourhood buffers, warp 1 issues the MMAs of a tile into
+// one of two sets of R tensor-memory accumulators, warps 2-9 (two per
+// 32-lane quarter of tensor memory, alternate rows) read the accumulators,
+// add the bias, apply ReLU and store while the next tile is being
+// multiplied. mbarriers hand over each buffer and accumulator set; every
+// wait is bounded and also ends when another role has given up (ws.abort).
+constexpr int kWsX = kBM + 2;   // neighbourhood width: 128 output pixels and the two side columns
+constexpr int kWsEpiWarps = 8;        // two per 32-lane quarter of tensor memory
+constexpr int kWsThreads = 64 + 32 * kWsEpiWarps;   // producer, MMA issuer, epilogue
 constexpr int kWsMaxStages = 4;
 
 __host__ __device__ inline uint32_t ws_slab(int rows) {   // (R+2) * 130 * 16 B, rounded up to 128 B
-    return (static_cast<uint32_t>(rows + 2) * kTmaX * 16u + 127u) & ~127u;
+    return (static_cast<uint32_t>(rows + 2) * kWsX * 16u + 127u) & ~127u;
 }
 
 constexpr int kWsMaxKSteps = 9 * 256 / 16;   // K steps of 16 for cin8 <= 256
@@ -550,6 +569,7 @@ struct WsSmem {
     // descriptor offsets (16-byte units) of each K step: A within a
     // neighbourhood buffer (channel block, tap), B within the weights
     uint32_t off_a[kWsMaxKSteps], off_b[kWsMaxKSteps];
+    float bias[256];   // the layer's bias, zero past cout
     uint64_t full[kWsMaxStages], empty[kWsMaxStages];
     uint64_t acc_full[2], acc_empty[2];
     uint64_t drain;
@@ -576,13 +596,13 @@ __device__ __forceinline__ bool ws_wait(uint64_t* bar, uint32_t parity, volatile
     return false;
 }
 
-__global__ void __launch_bounds__(kWsThreads) k_conv_ws(ConvArgs a, const __grid_constant__ CUtensorMap tm_a,
-                                                        const __grid_constant__ CUtensorMap tm_b, int cb_a, int ntiles,
-                                                        int nstages, int rows, int* err_flag) {
+__global__ void __launch_bounds__(kWsThreads) k_conv_ws(ConvArgs a, const __nv_bfloat16* __restrict__ src_a,
+                                                        const __nv_bfloat16* __restrict__ src_b, int cb_a, int cbs_a,
+                                                        int cbs_b, int ntiles, int nstages, int rows, int* err_flag) {
     extern __shared__ __align__(1024) uint8_t dsm_raw[];
     __shared__ WsSmem ws;
-    // offsets are from a 1024-byte aligned base (TMA boxes land on 128-byte
-    // boundaries); the launch adds 1024 bytes of slack
+    // offsets are from a 1024-byte aligned base (the copies need 16-byte
+    // alignment); the launch adds 1024 bytes of slack
     uint8_t* dsm = reinterpret_cast<uint8_t*>((reinterpret_cast<uintptr_t>(dsm_raw) + 1023u) & ~uintptr_t{1023});
     const int bn = a.bn;
     const int cb_total = a.cin8 / 8;
@@ -600,13 +620,11 @@ __global__ void __launch_bounds__(kWsThreads) k_conv_ws(ConvArgs a, const __grid
         }
         for (int k = 0; k < 2; ++k) {
             umma::mbar_init(&ws.acc_full[k], 1);
-            umma::mbar_init(&ws.acc_empty[k], 4);
+            umma::mbar_init(&ws.acc_empty[k], kWsEpiWarps);
         }
         umma::mbar_init(&ws.drain, 1);
         ws.abort = 0;
         umma::mbar_fence_init();
-        umma::tma_prefetch_desc(&tm_a);
-        if (cb_a < cb_total) umma::tma_prefetch_desc(&tm_b);
     }
     if (warp == 0) umma::tmem_alloc(&ws.tmem, 2 * set_cols);
     // resident weights: chunk kc of 64 K at w_off + kc * bn * 128, in the
@@ -617,9 +635,10 @@ __global__ void __launch_bounds__(kWsThreads) k_conv_ws(ConvArgs a, const __grid
         const int k0 = k * 16;
         const int tap = k0 / a.cin8, cb = (k0 - tap * a.cin8) >> 3;
         const int dy = tap / 3, dx = tap - 3 * (tap / 3);
-        ws.off_a[k] = (static_cast<uint32_t>(cb) * slab + static_cast<uint32_t>((dy * kTmaX + dx) * 16)) >> 4;
+        ws.off_a[k] = (static_cast<uint32_t>(cb) * slab + static_cast<uint32_t>((dy * kWsX + dx) * 16)) >> 4;
         ws.off_b[k] = (static_cast<uint32_t>(k0 / kBK) * static_cast<uint32_t>(bn) * 128u + ((k0 % kBK) / 16) * 256u) >> 4;
     }
+    for (int c = threadIdx.x; c < bn; c += kWsThreads) ws.bias[c] = c < a.cout ? a.bias[c] : 0.0f;
     const int kchunks = a.k_pad / kBK;
     for (int L = threadIdx.x; L < kchunks * bn * 8; L += kWsThreads) {
         const int kc = L / (bn * 8), l = L - kc * bn * 8;
@@ -638,33 +657,63 @@ __global__ void __launch_bounds__(kWsThreads) k_conv_ws(ConvArgs a, const __grid
     volatile int* abort = &ws.abort;
 
     if (warp == 0) {
-        if (lane == 0) {   // producer: TMA boxes of tile i into stage i % nstages
-            const uint32_t bytes = static_cast<uint32_t>(cb_total) * static_cast<uint32_t>(rows + 2) * kTmaX * 16u;
-            int i = 0, issued = 0;
-            for (int t = first; t < ntiles; t += step, ++i) {
-                const int s = i % nstages;
-                if (i >= nstages && !ws_wait(&ws.empty[s], static_cast<uint32_t>(i / nstages - 1) & 1u, abort)) break;
-                const int x0 = (t % xtiles) * kBM;
-                const int ny = t / xtiles;
-                const int y0 = (ny % ygroups) * rows, n = ny / ygroups;
-                uint8_t* dst = dsm + static_cast<uint32_t>(s) * stage_bytes;
-                umma::mbar_arrive_expect_tx(&ws.full[s], bytes);
-                for (int j = 0; j < cb_total; ++j) {
-                    if (j < cb_a)
-                        umma::tma_load_4d(dst + static_cast<uint32_t>(j) * slab, &tm_a, j * 8, x0 - 1, y0 - 1, n,
-                                          &ws.full[s]);
-                    else
-                        umma::tma_load_4d(dst + static_cast<uint32_t>(j) * slab, &tm_b, (j - cb_a) * 8, x0 - 1,
-                                          y0 - 1, n, &ws.full[s]);
+        // producer: the neighbourhood of tile i into stage i % nstages, one
+        // bulk copy per (channel block, row) -- a row of a channel block is
+        // contiguous in the channel-blocked layout -- and zeros where the
+        // neighbourhood leaves the image (the padding)
+        const int nitems = cb_total * (rows + 2);
+        const int64_t hw = static_cast<int64_t>(a.g.h) * a.g.w;
+        int i = 0, issued = 0;
+        for (int t = first; t < ntiles; t += step, ++i) {
+            const int s = i % nstages;
+            if (i >= nstages &&
+                !__all_sync(0xFFFFFFFFu, ws_wait(&ws.empty[s], static_cast<uint32_t>(i / nstages - 1) & 1u, abort)))
+                break;
+            const int x0 = (t % xtiles) * kBM;
+            const int ny = t / xtiles;
+            const int y0 = (ny % ygroups) * rows, n = ny / ygroups;
+            uint8_t* dst = dsm + static_cast<uint32_t>(s) * stage_bytes;
+            const int lo = x0 - 1 > 0 ? x0 - 1 : 0;                              // valid columns lo..hi
+            const int hi = x0 + kBM < a.g.w - 1 ? x0 + kBM : a.g.w - 1;
+            const int j_lo = lo - (x0 - 1), j_hi = hi - (x0 - 1);                // their entries in a row
+            const uint32_t nbytes = static_cast<uint32_t>(hi - lo + 1) * 16u;
+            uint32_t mine = 0;
+            for (int it = lane; it < nitems; it += 32) {
+                const int cb = it / (rows + 2), r = it - cb * (rows + 2);
+                const int y = y0 - 1 + r;
+                uint4* rowp = reinterpret_cast<uint4*>(dst + static_cast<uint32_t>(cb) * slab +
+                                                       static_cast<uint32_t>(r * kWsX) * 16u);
+                if (y < 0 || y >= a.g.h) {
+                    for (int j = 0; j < kWsX; ++j) rowp[j] = make_uint4(0, 0, 0, 0);
+                } else {
+                    for (int j = 0; j < j_lo; ++j) rowp[j] = make_uint4(0, 0, 0, 0);
+                    for (int j = j_hi + 1; j < kWsX; ++j) rowp[j] = make_uint4(0, 0, 0, 0);
+                    mine += nbytes;
                 }
-                issued = i + 1;
             }
-            // copies in flight land before the CTA's shared memory is released:
-            // the last nstages issued tiles' fills (bounded, regardless of abort)
+            umma::fence_async_smem();   // the zeros, for the MMAs' async-proxy reads
+            const uint32_t total = __reduce_add_sync(0xFFFFFFFFu, mine);
+            __syncwarp();
+            if (lane == 0) umma::mbar_arrive_expect_tx(&ws.full[s], total);
+            __syncwarp();
+            for (int it = lane; it < nitems; it += 32) {
+                const int cb = it / (rows + 2), r = it - cb * (rows + 2);
+                const int y = y0 - 1 + r;
+                if (y < 0 || y >= a.g.h) continue;
+                const __nv_bfloat16* src = cb < cb_a ? src_a + blk(n, cb, cbs_a, hw, static_cast<int64_t>(y) * a.g.w + lo)
+                                                     : src_b + blk(n, cb - cb_a, cbs_b, hw,
+                                                                   static_cast<int64_t>(y) * a.g.w + lo);
+                umma::bulk_load(dst + static_cast<uint32_t>(cb) * slab + static_cast<uint32_t>(r * kWsX + j_lo) * 16u,
+                                src, nbytes, &ws.full[s]);
+            }
+            issued = i + 1;
+        }
+        // copies in flight land before the CTA's shared memory is released:
+        // the last nstages issued tiles' fills (bounded, regardless of abort)
+        if (lane == 0)
             for (int k = issued - nstages > 0 ? issued - nstages : 0; k < issued; ++k)
                 if (!umma::mbar_wait(&ws.full[k % nstages], static_cast<uint32_t>(k / nstages) & 1u))
                     atomicOr(err_flag, 2);
-        }
     } else if (warp == 1) {
         if (lane == 0) {   // MMA issuer: tile i from stage i % nstages into accumulator set i & 1
             const uint32_t idesc = umma::idesc_bf16(kBM, static_cast<uint32_t>(bn), false, false);
@@ -681,7 +730,8 @@ __global__ void __launch_bounds__(kWsThreads) k_conv_ws(ConvArgs a, const __grid
                 const uint64_t da0 = umma::smem_desc(umma::smem_u32(dsm + static_cast<uint32_t>(s) * stage_bytes), slab, 128);
                 for (int r = 0; r < rows; ++r) {
                     const uint32_t d = tmem + static_cast<uint32_t>(acc) * set_cols + static_cast<uint32_t>(r) * ncols;
-                    const uint64_t dar = da0 + static_cast<uint64_t>(r * kTmaX);   // output row r: input rows r + dy
+                    const uint64_t dar = da0 + static_cast<uint64_t>(r * kWsX);   // output row r: input rows r + dy
+#pragma unroll 4
                     for (int k = 0; k < ksteps; ++k)
                         umma::mma_bf16(d, dar + ws.off_a[k], db0 + ws.off_b[k], idesc, k > 0);
                 }
@@ -694,9 +744,12 @@ __global__ void __launch_bounds__(kWsThreads) k_conv_ws(ConvArgs a, const __grid
             if (!umma::mbar_wait(&ws.drain, 0)) atomicOr(err_flag, 2);
         }
     } else {
-        // epilogue: warp w reads tensor-memory lanes 32 (w % 4) .. +31
-        const int q = warp & 3;
+        // epilogue: warp w reads tensor-memory lanes 32 (w % 4) .. +31 of the
+        // output rows r = half, half + 2, ... of the tile (two warps per quarter)
+        const int q = warp & 3, half = (warp - 2) >> 2;
         const int row = q * 32 + lane;
+        const int64_t hw = static_cast<int64_t>(a.g.h) * a.g.w;
+        const int cbo = a.cout8 >> 3;
         int i = 0;
         for (int t = first; t < ntiles; t += step, ++i) {
             const int acc = i & 1;
@@ -706,33 +759,32 @@ __global__ void __launch_bounds__(kWsThreads) k_conv_ws(ConvArgs a, const __grid
             const int x0 = (t % xtiles) * kBM;
             const int ny = t / xtiles;
             const int y0 = (ny % ygroups) * rows, n = ny / ygroups;
-            for (int r = 0; r < rows; ++r) {
+            for (int r = half; r < rows; r += 2) {
                 const int y = y0 + r;
                 const bool live = x0 + row < a.g.w && y < a.g.h;
-                const int64_t p = (static_cast<int64_t>(n) * a.g.h + y) * a.g.w + x0 + row;
+                const int64_t rem = static_cast<int64_t>(y) * a.g.w + x0 + row;
                 const uint32_t trow = tmem + static_cast<uint32_t>(acc) * set_cols + static_cast<uint32_t>(r) * ncols +
                                       (static_cast<uint32_t>(q * 32) << 16);
                 for (int c0 = 0; c0 < bn; c0 += 32) {
                     float v[32];
                     umma::tmem_ld32(trow + c0, v);   // warp-collective: every lane loads, the row test comes after
+                    if (!live) continue;
 #pragma unroll
                     for (int c8 = 0; c8 < 32; c8 += 8) {
                         const int c = c0 + c8;
-                        if (live && c < a.cout8) {
-                            float o[8];
+                        if (c >= a.cout8) break;
+                        float o[8];
 #pragma unroll
-                            for (int k = 0; k < 8; ++k) {
-                                float x = v[c8 + k] + ((c + k < a.cout) ? a.bias[c + k] : 0.0f);
-                                if (a.relu) x = fmaxf(x, 0.0f);
-                                o[k] = (c + k < a.cout) ? x : 0.0f;
-                            }
-                            if (a.yf) {
-                                float4* op = reinterpret_cast<float4*>(a.yf + p * a.cout8 + c);
-                                op[0] = make_float4(o[0], o[1], o[2], o[3]);
-                                op[1] = make_float4(o[4], o[5], o[6], o[7]);
-                            } else {
-                                *reinterpret_cast<uint4*>(a.yout + p * a.cout8 + c) = pack8(o);
-                            }
+                        for (int k = 0; k < 8; ++k) {
+                            const float x = v[c8 + k] + ws.bias[c + k];   // bias is zero past cout
+                            o[k] = a.relu ? fmaxf(x, 0.0f) : x;
+                        }
+                        if (a.yf) {
+                            float4* op = reinterpret_cast<float4*>(a.yf + (n * hw + rem) * a.cout8 + c);
+                            op[0] = make_float4(o[0], o[1], o[2], o[3]);
+                            op[1] = make_float4(o[4], o[5], o[6], o[7]);
+                        } else {
+                            *reinterpret_cast<uint4*>(a.yout + blk(n, c >> 3, cbo, hw, rem)) = pack8(o);
                         }
                     }
                 }
@@ -749,21 +801,21 @@ __global__ void __launch_bounds__(kWsThreads) k_conv_ws(ConvArgs a, const __grid
     if (warp == 0) umma::tmem_dealloc(tmem, 2 * set_cols);
 }
 
-// out[p][c] = in[low-resolution pixel of p][c]: the nearest 2x upsample of
-// an NHWC BF16 tensor, 8 channels (16 bytes) per thread.
+// out(n, cb, y, x) = in(n, cb, y/2, x/2): the nearest 2x upsample of a
+// channel-blocked BF16 tensor of cs channels, 8 channels (16 bytes) per thread.
 __global__ void k_upsample2(const __nv_bfloat16* __restrict__ in, __nv_bfloat16* __restrict__ out, Geo g, int cs) {
-    const int vpp = cs / 8;
-    const int64_t total = g.npix * vpp;
+    const int cbs = cs / 8;
+    const int64_t total = g.npix * cbs;
+    const int w2 = g.w >> 1;
+    const int64_t hw2 = static_cast<int64_t>(g.h >> 1) * w2;
     for (int64_t i = blockIdx.x * static_cast<int64_t>(blockDim.x) + threadIdx.x; i < total;
          i += static_cast<int64_t>(gridDim.x) * blockDim.x) {
-        const int cv = static_cast<int>(i % vpp);
-        const int64_t p = i / vpp;
-        const int x = static_cast<int>(p % g.w);
-        const int64_t t = p / g.w;
+        const int x = static_cast<int>(i % g.w);
+        int64_t t = i / g.w;
         const int y = static_cast<int>(t % g.h);
-        const int64_t n = t / g.h;
-        const int64_t lq = (n * (g.h >> 1) + (y >> 1)) * (g.w >> 1) + (x >> 1);
-        reinterpret_cast<uint4*>(out)[i] = reinterpret_cast<const uint4*>(in)[lq * vpp + cv];
+        t /= g.h;   // n * cbs + cb
+        reinterpret_cast<uint4*>(out)[i] =
+            reinterpret_cast<const uint4*>(in)[t * hw2 + static_cast<int64_t>(y >> 1) * w2 + (x >> 1)];
     }
 }
 
@@ -772,23 +824,22 @@ __global__ void k_pool_fwd(const __nv_bfloat16* __restrict__ x, __nv_bfloat16* _
     const int64_t total = lo.npix * (c8 / 8);
     for (int64_t i = blockIdx.x * static_cast<int64_t>(blockDim.x) + threadIdx.x; i < total;
          i += static_cast<int64_t>(gridDim.x) * blockDim.x) {
-        const int cv = static_cast<int>(i % (c8 / 8));
-        const int64_t p = i / (c8 / 8);
-        const int lx = static_cast<int>(p % lo.w);
-        const int64_t t = p / lo.w;
+        // i runs over the output in its channel-blocked order
+        const int lx = static_cast<int>(i % lo.w);
+        int64_t t = i / lo.w;
         const int ly = static_cast<int>(t % lo.h);
-        const int64_t n = t / lo.h;
+        t /= lo.h;   // n * (c8 / 8) + channel block
         const int W = lo.w * 2, H = lo.h * 2;
         float m[8];
         for (int j = 0; j < 8; ++j) m[j] = -3.0e38f;
         for (int dy = 0; dy < 2; ++dy)
             for (int dx = 0; dx < 2; ++dx) {
-                const int64_t q = (n * H + ly * 2 + dy) * W + lx * 2 + dx;
+                const int64_t q = (t * H + ly * 2 + dy) * W + lx * 2 + dx;
                 float f[8];
-                unpack8(*reinterpret_cast<const uint4*>(x + q * c8 + cv * 8), f);
+                unpack8(*reinterpret_cast<const uint4*>(x + q * 8), f);
                 for (int j = 0; j < 8; ++j) m[j] = fmaxf(m[j], f[j]);
             }
-        *reinterpret_cast<uint4*>(y + p * c8 + cv * 8) = pack8(m);
+        *reinterpret_cast<uint4*>(y + i * 8) = pack8(m);
     }
 }
 
@@ -807,11 +858,12 @@ __global__ void k_pool_bwd(const __nv_bfloat16* __restrict__ x, const float* __r
         const int W = lo.w * 2, H = lo.h * 2;
         float best = -3.0e38f;
         int64_t bq = 0;
+        const int64_t hw = static_cast<int64_t>(H) * W;
         for (int ddy = 0; ddy < 2; ++ddy)
             for (int ddx = 0; ddx < 2; ++ddx) {
-                const int64_t q = (n * H + ly * 2 + ddy) * W + lx * 2 + ddx;
-                const float v = __bfloat162float(x[q * c8 + c]);
-                if (v > best) { best = v; bq = q; }
+                const int64_t rem = static_cast<int64_t>(ly * 2 + ddy) * W + lx * 2 + ddx;
+                const float v = __bfloat162float(x[blk(n, c >> 3, c8 >> 3, hw, rem) + (c & 7)]);
+                if (v > best) { best = v; bq = n * hw + rem; }
             }
         dx[bq * c8 + c] += dy[p * c8 + c];
     }
@@ -853,9 +905,10 @@ __global__ void k_pack(const float4* __restrict__ rad, const float* __restrict__
         }
         float lo8[8], hi8[8];
         for (int j = 0; j < 8; ++j) { lo8[j] = f[j]; hi8[j] = f[8 + j]; }
-        uint4* o = reinterpret_cast<uint4*>(x + (img_offset + i) * 16);
-        o[0] = pack8(lo8);
-        o[1] = pack8(hi8);
+        // image img_offset / (wp hp), two channel blocks
+        const int64_t n = img_offset / total;
+        *reinterpret_cast<uint4*>(x + blk(n, 0, 2, total, i)) = pack8(lo8);
+        *reinterpret_cast<uint4*>(x + blk(n, 1, 2, total, i)) = pack8(hi8);
     }
     (void)npix_img;
 }
@@ -938,7 +991,11 @@ __global__ void k_bias_grad(const float* __restrict__ dy, const __nv_bfloat16* _
     for (int64_t p = blockIdx.x * static_cast<int64_t>(blockDim.x) + threadIdx.x; p < g.npix;
          p += static_cast<int64_t>(gridDim.x) * blockDim.x) {
         float v = dy[p * cout8 + co];
-        if (relu && !(__bfloat162float(y[p * cout8 + co]) > 0.0f)) v = 0.0f;
+        if (relu) {
+            const int64_t hw = static_cast<int64_t>(g.h) * g.w;
+            const int64_t n = p / hw;
+            if (!(__bfloat162float(y[blk(n, co >> 3, cout8 >> 3, hw, p - n * hw) + (co & 7)]) > 0.0f)) v = 0.0f;
+        }
         s += v;
     }
     for (int off = 16; off > 0; off >>= 1) s += __shfl_down_sync(0xFFFFFFFFu, s, off);
@@ -1030,40 +1087,7 @@ size_t conv_halo_smem_bytes(int cin8, int bn) {
 
 namespace {
 
-// cuTensorMapEncodeTiled through the runtime's driver entry point (no link
-// against the driver library); null when the driver does not offer it.
-PFN_cuTensorMapEncodeTiled_v12000 tensor_map_encoder() {
-    static const PFN_cuTensorMapEncodeTiled_v12000 fn = [] {
-        void* p = nullptr;
-        cudaDriverEntryPointQueryResult q{};
-        if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &p, 12000, cudaEnableDefault, &q) !=
-                cudaSuccess ||
-            q != cudaDriverEntryPointSuccess) {
-            cudaGetLastError();
-            return static_cast<PFN_cuTensorMapEncodeTiled_v12000>(nullptr);
-        }
-        return reinterpret_cast<PFN_cuTensorMapEncodeTiled_v12000>(p);
-    }();
-    return fn;
-}
-
-// NHWC BF16 activations [n][h][w][cs] as the 4-D tensor (cs, w, h, n) with
-// a box of 8 channels x bx pixels x br rows x 1 image.
-bool encode_activations(CUtensorMap* m, const __nv_bfloat16* base, int cs, int w, int h, int n, int bx, int br) {
-    const auto enc = tensor_map_encoder();
-    if (!enc || (reinterpret_cast<uintptr_t>(base) & 15u) || cs % 8) return false;
-    const cuuint64_t dims[4] = {static_cast<cuuint64_t>(cs), static_cast<cuuint64_t>(w), static_cast<cuuint64_t>(h),
-                                static_cast<cuuint64_t>(n)};
-    const cuuint64_t strides[3] = {static_cast<cuuint64_t>(cs) * 2, static_cast<cuuint64_t>(cs) * 2 * w,
-                                   static_cast<cuuint64_t>(cs) * 2 * w * h};
-    const cuuint32_t box[4] = {8u, static_cast<cuuint32_t>(bx), static_cast<cuuint32_t>(br), 1u};
-    const cuuint32_t es[4] = {1u, 1u, 1u, 1u};
-    return enc(m, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 4, const_cast<__nv_bfloat16*>(base), dims, strides, box, es,
-               CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_128B,
-               CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) == CUDA_SUCCESS;
-}
-
-// The warp-specialised TMA forward (k_conv_ws) when the layer fits it:
+// The warp-specialised forward (k_conv_ws) when the layer fits it:
 // false leaves the layer to the other kernels. An upsample + concatenation
 // layer first writes its upsampled source at full resolution into
 // a.up_scratch.
@@ -1084,7 +1108,7 @@ bool try_conv_ws(const ConvArgs& a, int* err_flag, cudaStream_t st) {
         if (2 * r * ncols > 512) continue;
         for (int s = kWsMaxStages; s >= 1; --s) {
             const size_t b = static_cast<size_t>(ws_smem_bytes(cb_total, s, r, a.bn, a.k_pad)) + 1024;   // + base alignment
-            if (b <= 227 * 1024 && (s >= 2 || r == 1)) {
+            if (b + sizeof(WsSmem) <= 227 * 1024 && (s >= 2 || r == 1)) {
                 rows = r;
                 nstages = s;
                 smem = b;
@@ -1094,16 +1118,10 @@ bool try_conv_ws(const ConvArgs& a, int* err_flag, cudaStream_t st) {
         if (rows) break;
     }
     if (!rows) return false;
-    CUtensorMap ta{}, tb{};
-    int cb_a = cb_total;
-    if (single) {
-        if (!encode_activations(&ta, a.x0, a.c0s, a.g.w, a.g.h, a.g.n, kTmaX, rows + 2)) return false;
-        tb = ta;
-    } else {
-        cb_a = a.c0 / 8;
-        if (!encode_activations(&ta, a.up_scratch, a.c0s, a.g.w, a.g.h, a.g.n, kTmaX, rows + 2)) return false;
-        if (!encode_activations(&tb, a.x1, a.c1s, a.g.w, a.g.h, a.g.n, kTmaX, rows + 2)) return false;
-    }
+    const int cb_a = single ? cb_total : a.c0 / 8;
+    const __nv_bfloat16* src_a = single ? a.x0 : a.up_scratch;
+    const __nv_bfloat16* src_b = single ? a.x0 : a.x1;
+    if ((reinterpret_cast<uintptr_t>(src_a) | reinterpret_cast<uintptr_t>(src_b)) & 15u) return false;
     if (cudaFuncSetAttribute(k_conv_ws, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(smem)) !=
             cudaSuccess ||
         cudaFuncSetAttribute(k_conv_ws, cudaFuncAttributePreferredSharedMemoryCarveout,
@@ -1126,7 +1144,9 @@ bool try_conv_ws(const ConvArgs& a, int* err_flag, cudaStream_t st) {
         k_upsample2<<<grid_for(a.g.npix * (a.c0s / 8), 256), 256, 0, st>>>(a.x0, a.up_scratch, a.g, a.c0s);
     const int64_t tiles = static_cast<int64_t>(a.g.n) * ((a.g.h + rows - 1) / rows) * ((a.g.w + kBM - 1) / kBM);
     const int grid = static_cast<int>(std::min<int64_t>(tiles, static_cast<int64_t>(sms) * per_sm));
-    k_conv_ws<<<grid, kWsThreads, smem, st>>>(a, ta, tb, cb_a, static_cast<int>(tiles), nstages, rows, err_flag);
+    const int cbs_a = a.c0s / 8, cbs_b = concat ? a.c1s / 8 : cbs_a;
+    k_conv_ws<<<grid, kWsThreads, smem, st>>>(a, src_a, src_b, cb_a, cbs_a, cbs_b, static_cast<int>(tiles), nstages,
+                                              rows, err_flag);
     return true;
 }
 

@@ -567,11 +567,16 @@ ohao_status ohao_dn_tensor(ohao_dn_ctx* ctx, int32_t index, int32_t grad, float*
     } else if (t.f32) {
         DN_CK(cudaMemcpy(host, t.act.p, cnt * 4, cudaMemcpyDeviceToHost), "tensor");
     } else {
+        // channel-blocked [n][c8/8][h][w][8] on the device -> [pixel][c8]
         std::vector<uint16_t> b(cnt);
         DN_CK(cudaMemcpy(b.data(), t.act.p, cnt * 2, cudaMemcpyDeviceToHost), "tensor");
+        const uint64_t hw = static_cast<uint64_t>(g.h) * g.w;
+        const uint64_t cbs = static_cast<uint64_t>(t.c8) / 8;
         for (uint64_t i = 0; i < cnt; ++i) {
+            const uint64_t lane = i & 7, rem = (i >> 3) % hw, nc = (i >> 3) / hw;
+            const uint64_t n = nc / cbs, cb = nc % cbs;
             const uint32_t u = static_cast<uint32_t>(b[i]) << 16;
-            std::memcpy(host + i, &u, 4);
+            std::memcpy(host + (n * hw + rem) * t.c8 + cb * 8 + lane, &u, 4);
         }
     }
     return OHAO_OK;
