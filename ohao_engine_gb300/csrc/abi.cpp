@@ -108,8 +108,15 @@ struct ohao_pt_ctx {
     DevBuf host_grad_bufs[2];             // ohao_pt_adjoint_host: map and roughness gradients
     ohao_pt_profile profile{};
     ohao::PersistentState* persistent = nullptr;
+    // ohao_pt_render_host: history uploads run on their own stream, so that
+    // they overlap the render up to its first read of the accumulator
+    cudaStream_t upload_stream = nullptr;
+    std::vector<cudaEvent_t> upload_after, upload_done;   // per view: stream order in, upload landed
     ~ohao_pt_ctx() {
         if (persistent) ohao::persistent_destroy(persistent);
+        for (cudaEvent_t e : upload_after) cudaEventDestroy(e);
+        for (cudaEvent_t e : upload_done) cudaEventDestroy(e);
+        if (upload_stream) cudaStreamDestroy(upload_stream);
         for (auto* b : host_accum_bufs) delete b;
         for (auto* b : host_display_bufs) delete b;
         for (auto* b : host_target_bufs) delete b;
@@ -792,6 +799,7 @@ static std::vector<ohao::RenderView> to_render_views(const ohao_pt_view* views, 
         rv.history = views[v].history;
         rv.path_out = views[v].path_radiance;
         rv.aov = views[v].aov;
+        rv.accum_ready = nullptr;
     }
     return out;
 }
@@ -806,8 +814,11 @@ static ohao_status ensure_persistent(ohao_pt_ctx* ctx) {
     return OHAO_OK;
 }
 
+// ready: per view, an event recorded when its accumulator's history is in
+// place (or null: it is); the render waits for it before reading it.
 static ohao_status render_views(ohao_pt_ctx* ctx, const ohao_pt_view* views, uint32_t n_views,
-                                const ohao_pt_settings* st, float* const* dev_accum, cudaStream_t cs) {
+                                const ohao_pt_settings* st, float* const* dev_accum, cudaStream_t cs,
+                                const cudaEvent_t* ready = nullptr) {
     const bool profile = (st->flags & OHAO_PT_FLAG_PROFILE) != 0;
     ohao::ProfileAcc acc;
     ohao::DScene sc = make_scene(ctx);
@@ -815,8 +826,14 @@ static ohao_status render_views(ohao_pt_ctx* ctx, const ohao_pt_view* views, uin
     sc.alpha_test = (st->flags & OHAO_PT_FLAG_ALPHA_TEST) && any_non_opaque(ctx) ? 1u : 0u;
     ohao::PathParams pp{st->max_bounces, st->sampler, st->flags, st->clamp_luminance, st->aniso_strength,
                         st->aniso_rotation, st->sample_index_base, wavefront_refill(st)};
-    const std::vector<ohao::RenderView> rvs = to_render_views(views, n_views, dev_accum);
+    std::vector<ohao::RenderView> rvs = to_render_views(views, n_views, dev_accum);
+    if (ready)
+        for (uint32_t v = 0; v < n_views; ++v) rvs[v].accum_ready = ready[v];
     if (use_persistent(st, n_views)) {
+        // the pool folds paths into the accumulators from its first chunk on
+        if (ready)
+            for (uint32_t v = 0; v < n_views; ++v)
+                if (ready[v]) CK(cudaStreamWaitEvent(cs, ready[v], 0), "wait for the history upload");
         ohao_status s = ensure_persistent(ctx);
         if (s != OHAO_OK) return s;
         if (n_views > ohao::persistent_max_views())
@@ -911,16 +928,41 @@ ohao_status ohao_pt_render_host(ohao_pt_ctx* ctx, const ohao_pt_view* views, uin
     cudaStream_t cs = reinterpret_cast<cudaStream_t>(stream);
     CK(cudaSetDevice(ctx->device), "set device");
     while (ctx->host_accum_bufs.size() < n_views) ctx->host_accum_bufs.push_back(new DevBuf());
+    if (!ctx->upload_stream) CK(cudaStreamCreateWithFlags(&ctx->upload_stream, cudaStreamNonBlocking), "upload stream");
+    while (ctx->upload_done.size() < n_views) {
+        cudaEvent_t a = nullptr, b = nullptr;
+        CK(cudaEventCreateWithFlags(&a, cudaEventDisableTiming), "upload event");
+        if (cudaEventCreateWithFlags(&b, cudaEventDisableTiming) != cudaSuccess) {
+            cudaEventDestroy(a);
+            return fail(ctx, OHAO_ERR_CUDA, "upload event");
+        }
+        ctx->upload_after.push_back(a);
+        ctx->upload_done.push_back(b);
+    }
     std::vector<float*> acc(n_views);
+    std::vector<cudaEvent_t> ready(n_views, nullptr);
     for (uint32_t v = 0; v < n_views; ++v) {
         if (!host_accum[v]) return fail(ctx, OHAO_ERR_INVALID_ARG, "render_host: null host buffer");
         const size_t bytes = static_cast<size_t>(views[v].width) * views[v].height * 16;
         CK(ctx->host_accum_bufs[v]->ensure(bytes), "host accum");
         acc[v] = ctx->host_accum_bufs[v]->as<float>();
-        if (views[v].history > 0)
-            CK(cudaMemcpyAsync(acc[v], host_accum[v], bytes, cudaMemcpyHostToDevice, cs), "accum upload");
+        if (views[v].history > 0) {
+            // after everything already on the caller's stream (an earlier
+            // call's download of the same buffer), on the upload stream
+            CK(cudaEventRecord(ctx->upload_after[v], cs), "upload order");
+            CK(cudaStreamWaitEvent(ctx->upload_stream, ctx->upload_after[v], 0), "upload order");
+            CK(cudaMemcpyAsync(acc[v], host_accum[v], bytes, cudaMemcpyHostToDevice, ctx->upload_stream),
+               "accum upload");
+            CK(cudaEventRecord(ctx->upload_done[v], ctx->upload_stream), "upload done");
+            ready[v] = ctx->upload_done[v];
+        }
     }
-    if ((s = render_views(ctx, views, n_views, st, acc.data(), cs)) != OHAO_OK) return s;
+    if ((s = render_views(ctx, views, n_views, st, acc.data(), cs, ready.data())) != OHAO_OK) {
+        // nothing may still write the buffers once the call has returned
+        for (uint32_t v = 0; v < n_views; ++v)
+            if (ready[v]) cudaStreamWaitEvent(cs, ready[v], 0);
+        return s;
+    }
     for (uint32_t v = 0; v < n_views; ++v) {
         const size_t npix = static_cast<size_t>(views[v].width) * views[v].height;
         CK(cudaMemcpyAsync(host_accum[v], acc[v], npix * 16, cudaMemcpyDeviceToHost, cs), "accum download");

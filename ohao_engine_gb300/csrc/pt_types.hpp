@@ -89,6 +89,10 @@ struct RenderView {
     uint32_t history;
     float* path_out;     // device [spp][npix][4] or null
     float* aov;          // device [npix][OHAO_PT_AOV_FLOATS] or null
+    // recorded when `accum` holds its history (an upload still in flight on
+    // another stream): the render waits for it before it first reads the
+    // accumulator; null = already there
+    cudaEvent_t accum_ready;
 };
 
 struct ProfileAcc {

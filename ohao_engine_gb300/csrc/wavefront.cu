@@ -1075,6 +1075,7 @@ ohao_status wavefront_render(const DScene& sc, const RenderView& view, const Pat
             tm.end(2, a);
             cur ^= 1;
         }
+        if (view.accum_ready) cudaStreamWaitEvent(st, view.accum_ready, 0);   // the history upload has landed
         tm.begin(3, a);
         k_finalize<<<std::max(1u, std::min(4096u, (npix + 255) / 256)), 256, 0, st>>>(
             pp, static_cast<uint32_t>(w0), n, view.vp.width, view.vp.height, s, view.accum, view.history, view.path_out);

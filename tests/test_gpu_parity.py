@@ -156,6 +156,41 @@ def test_progressive_accumulation_and_host_path(gpu_lib, oracle):
     assert np.array_equal(host, ref)
 
 
+@pytest.mark.parametrize("mode", ["wavefront", "persistent"])
+def test_host_path_with_history(gpu_lib, oracle, mode):
+    """ohao_pt_render_host continuing a host accumulator (history > 0): its
+    upload overlaps the render on another stream, and the result equals the
+    device-buffer render of the same samples bit for bit; on a small frame
+    it equals the oracle's accumulation, on a 1024^2 frame (an upload long
+    enough to still be in flight) the device path."""
+    import torch
+    og = gpu_lib
+    m = og.MODE_WAVEFRONT if mode == "wavefront" else og.MODE_PERSISTENT
+    sd = scenes.cornell(24, 24, 1)
+    pt = gpu_tracer(og, sd)
+    v = sd.views[0]
+    g1, _, _ = render_paths_gpu(og, pt, v, 2, dict(max_bounces=4, sample_index_base=0), history=0)
+    g2, _, _ = render_paths_gpu(og, pt, v, 3, dict(max_bounces=4, sample_index_base=2), history=2)
+    host = oracle.accumulate(g1).astype(np.float32)
+    pt.render_host([og.make_view(v, history=2)], og.make_settings(spp=3, max_bounces=4, sample_index_base=2, mode=m),
+                   [host])
+    assert np.array_equal(host, oracle.accumulate(np.concatenate([g1, g2])))
+    big = scenes.cornell(1024, 1024, 1)
+    pt2 = gpu_tracer(og, big)
+    vb = big.views[0]
+    n = vb.width * vb.height
+    acc = torch.zeros((n, 4), dtype=torch.float32, device="cuda")
+    pt2.render([og.make_view(vb, accum=acc)], og.make_settings(spp=2, max_bounces=2, mode=m))
+    host_b = acc.cpu().numpy().copy()
+    pt2.render([og.make_view(vb, accum=acc, history=2)],
+               og.make_settings(spp=1, max_bounces=2, sample_index_base=2, mode=m))
+    for _ in range(2):   # twice: the second call's upload follows the first call's download of the same buffer
+        h = host_b.copy()
+        pt2.render_host([og.make_view(vb, history=2)],
+                        og.make_settings(spp=1, max_bounces=2, sample_index_base=2, mode=m), [h])
+        assert np.array_equal(h, acc.cpu().numpy())
+
+
 def test_aov_first_hit(gpu_lib, oracle):
     sd = scenes.cornell(20, 20, 1)
     pt = gpu_tracer(gpu_lib, sd)
