@@ -598,7 +598,8 @@ __device__ __forceinline__ bool ws_wait(uint64_t* bar, uint32_t parity, volatile
 
 __global__ void __launch_bounds__(kWsThreads) k_conv_ws(ConvArgs a, const __nv_bfloat16* __restrict__ src_a,
                                                         const __nv_bfloat16* __restrict__ src_b, int cb_a, int cbs_a,
-                                                        int cbs_b, int ntiles, int nstages, int rows, int* err_flag) {
+                                                        int cbs_b, int ntiles, int nstages, int rows, int co0,
+                                                        int* err_flag) {
     extern __shared__ __align__(1024) uint8_t dsm_raw[];
     __shared__ WsSmem ws;
     // offsets are from a 1024-byte aligned base (the copies need 16-byte
@@ -638,13 +639,13 @@ __global__ void __launch_bounds__(kWsThreads) k_conv_ws(ConvArgs a, const __nv_b
         ws.off_a[k] = (static_cast<uint32_t>(cb) * slab + static_cast<uint32_t>((dy * kWsX + dx) * 16)) >> 4;
         ws.off_b[k] = (static_cast<uint32_t>(k0 / kBK) * static_cast<uint32_t>(bn) * 128u + ((k0 % kBK) / 16) * 256u) >> 4;
     }
-    for (int c = threadIdx.x; c < bn; c += kWsThreads) ws.bias[c] = c < a.cout ? a.bias[c] : 0.0f;
+    for (int c = threadIdx.x; c < bn; c += kWsThreads) ws.bias[c] = co0 + c < a.cout ? a.bias[co0 + c] : 0.0f;
     const int kchunks = a.k_pad / kBK;
     for (int L = threadIdx.x; L < kchunks * bn * 8; L += kWsThreads) {
         const int kc = L / (bn * 8), l = L - kc * bn * 8;
         const int r = l & 7, kb = (l >> 3) & 7, nb = l >> 6;
         *reinterpret_cast<uint4*>(dsm + w_off + static_cast<uint32_t>(L) * 16) =
-            *reinterpret_cast<const uint4*>(a.w + static_cast<int64_t>(nb * 8 + r) * a.k_pad + kc * kBK + kb * 8);
+            *reinterpret_cast<const uint4*>(a.w + static_cast<int64_t>(co0 + nb * 8 + r) * a.k_pad + kc * kBK + kb * 8);
     }
     umma::fence_async_smem();
     umma::tc_fence_before();
@@ -771,8 +772,8 @@ __global__ void __launch_bounds__(kWsThreads) k_conv_ws(ConvArgs a, const __nv_b
                     if (!live) continue;
 #pragma unroll
                     for (int c8 = 0; c8 < 32; c8 += 8) {
-                        const int c = c0 + c8;
-                        if (c >= a.cout8) break;
+                        const int c = c0 + c8, cg = co0 + c;   // this launch's and the layer's channel
+                        if (cg >= a.cout8) break;
                         float o[8];
 #pragma unroll
                         for (int k = 0; k < 8; ++k) {
@@ -780,11 +781,11 @@ __global__ void __launch_bounds__(kWsThreads) k_conv_ws(ConvArgs a, const __nv_b
                             o[k] = a.relu ? fmaxf(x, 0.0f) : x;
                         }
                         if (a.yf) {
-                            float4* op = reinterpret_cast<float4*>(a.yf + (n * hw + rem) * a.cout8 + c);
+                            float4* op = reinterpret_cast<float4*>(a.yf + (n * hw + rem) * a.cout8 + cg);
                             op[0] = make_float4(o[0], o[1], o[2], o[3]);
                             op[1] = make_float4(o[4], o[5], o[6], o[7]);
                         } else {
-                            *reinterpret_cast<uint4*>(a.yout + blk(n, c >> 3, cbo, hw, rem)) = pack8(o);
+                            *reinterpret_cast<uint4*>(a.yout + blk(n, cg >> 3, cbo, hw, rem)) = pack8(o);
                         }
                     }
                 }
@@ -1096,28 +1097,40 @@ bool try_conv_ws(const ConvArgs& a, int* err_flag, cudaStream_t st) {
     const bool concat = a.up0 && a.c1 > 0 && a.up_scratch && a.c0 % 8 == 0 && a.c0s == a.c0 && a.g.w % 2 == 0 &&
                         a.g.h % 2 == 0;
     if (!(single || concat) || a.n_tiles != 1 || a.cin8 % 16 != 0 || a.cin8 > 256 || a.g.w < kHaloMinW) return false;
-    int ncols = 32;
-    while (ncols < a.bn) ncols <<= 1;
     const int cb_total = a.cin8 / 8;
-    // the most rows per tile (then the most stages, >= 2 where possible)
-    // whose buffers fit the shared memory and whose two accumulator sets fit
-    // the tensor memory
-    int rows = 0, nstages = 0;
+    // the fewest launches over the output channels (each one all of the
+    // tile's pixels and bn / nsplit channels), then the most rows per tile,
+    // then the most stages (>= 2 where possible), whose buffers and weights
+    // fit the shared memory and whose two accumulator sets fit the tensor
+    // memory
+    int nsplit = 0, bn = 0, rows = 0, nstages = 0, ncols = 32;
     size_t smem = 0;
-    for (int r : {4, 2, 1}) {
-        if (2 * r * ncols > 512) continue;
-        for (int s = kWsMaxStages; s >= 1; --s) {
-            const size_t b = static_cast<size_t>(ws_smem_bytes(cb_total, s, r, a.bn, a.k_pad)) + 1024;   // + base alignment
-            if (b + sizeof(WsSmem) <= 227 * 1024 && (s >= 2 || r == 1)) {
-                rows = r;
-                nstages = s;
-                smem = b;
-                break;
+    for (int sp : {1, 2, 4}) {
+        const int b = a.bn / sp;
+        if (a.bn % sp || b % 16) continue;
+        int nc = 32;
+        while (nc < b) nc <<= 1;
+        for (int r : {4, 2, 1}) {
+            if (2 * r * nc > 512) continue;
+            for (int s2 = kWsMaxStages; s2 >= 1; --s2) {
+                const size_t by = static_cast<size_t>(ws_smem_bytes(cb_total, s2, r, b, a.k_pad)) + 1024;   // + base alignment
+                if (by + sizeof(WsSmem) <= 227 * 1024 && (s2 >= 2 || r == 1)) {
+                    rows = r;
+                    nstages = s2;
+                    smem = by;
+                    break;
+                }
             }
+            if (rows) break;
         }
-        if (rows) break;
+        if (rows) {
+            nsplit = sp;
+            bn = b;
+            ncols = nc;
+            break;
+        }
     }
-    if (!rows) return false;
+    if (!nsplit) return false;
     const int cb_a = single ? cb_total : a.c0 / 8;
     const __nv_bfloat16* src_a = single ? a.x0 : a.up_scratch;
     const __nv_bfloat16* src_b = single ? a.x0 : a.x1;
@@ -1145,8 +1158,11 @@ bool try_conv_ws(const ConvArgs& a, int* err_flag, cudaStream_t st) {
     const int64_t tiles = static_cast<int64_t>(a.g.n) * ((a.g.h + rows - 1) / rows) * ((a.g.w + kBM - 1) / kBM);
     const int grid = static_cast<int>(std::min<int64_t>(tiles, static_cast<int64_t>(sms) * per_sm));
     const int cbs_a = a.c0s / 8, cbs_b = concat ? a.c1s / 8 : cbs_a;
-    k_conv_ws<<<grid, kWsThreads, smem, st>>>(a, src_a, src_b, cb_a, cbs_a, cbs_b, static_cast<int>(tiles), nstages,
-                                              rows, err_flag);
+    ConvArgs part = a;
+    part.bn = bn;
+    for (int k = 0; k < nsplit; ++k)
+        k_conv_ws<<<grid, kWsThreads, smem, st>>>(part, src_a, src_b, cb_a, cbs_a, cbs_b, static_cast<int>(tiles),
+                                                  nstages, rows, k * bn, err_flag);
     return true;
 }
 

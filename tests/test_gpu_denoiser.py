@@ -41,10 +41,13 @@ def _rel(a, b):
     return np.linalg.norm(a - b) / max(np.linalg.norm(b), 1e-30)
 
 
-# "wide": rows of >= 96 pixels (levels 0-2 here) run the single-source
-# forward convolutions on the shared-memory neighbourhood kernel, the
-# concatenation layers and narrow levels on the gather
-@pytest.fixture(scope="module", params=[(2, 32, 48), (1, 16, 512)], ids=["narrow", "wide"])
+# Forward kernels by row width: "narrow" runs every layer on the gather
+# (rows < 96 pixels); "wide" (levels 0-2 >= 96 pixels) runs the
+# warp-specialised kernel with 4-, 2- and 1-row tiles, two-source
+# (upsampled + skip) layers and a layer split over its output channels;
+# "wider" (every level >= 96 pixels) also the deep levels, split in two and
+# four launches, and the neighbourhood and gather kernels of level 3.
+@pytest.fixture(scope="module", params=[(2, 32, 48), (1, 16, 512), (1, 16, 1536)], ids=["narrow", "wide", "wider"])
 def trained_step(gpu_lib, request):
     from ohao_engine_gb300.denoise import Denoiser
     n, h, w = request.param
