@@ -27,19 +27,20 @@ namespace ohao {
 
 namespace {
 
+// Path state by slot p, in 32-byte pairs of 16-byte records, so that a
+// path read out of queue order (after binning) touches one DRAM sector per
+// pair instead of one per field:
+//   ray[2p] = origin, ray[2p+1] = (direction, last pdf)
+//   tr[2p]  = throughput, tr[2p+1] = radiance
+//   hm[2p]  = (rng, dim, flags, hit instance), hm[2p+1] = hit (t, u, v, prim bits)
+// flags = phase | bounce<<2 | delta<<10 | shL<<11 | shE<<12.
 struct Soa {
-    uint32_t* rng;
-    uint32_t* dim;
-    uint32_t* flags;     // phase | bounce<<2 | delta<<10 | shL<<11 | shE<<12
-    float4* ro;          // origin
-    float4* rd;          // dir, w = last pdf
-    float4* thr;
-    float4* rad;
+    float4* ray;
+    float4* tr;
+    uint4* hm;
     float4* fhP;
     float4* fhN;
     float4* fhA;
-    float4* hit;         // t, u, v, prim bits
-    uint32_t* hit_inst;
     float4* sh_org;
     float4* shL;         // dir, tmax
     float4* shLc;        // contribution
@@ -98,6 +99,15 @@ __device__ __forceinline__ uint32_t find_view(const LaunchBlock* lb, uint32_t g)
 constexpr uint32_t kFlagDelta = 1u << 10, kFlagShL = 1u << 11, kFlagShE = 1u << 12;
 
 __device__ __forceinline__ float4 f4(V3 v, float w) { return make_float4(v.x, v.y, v.z, w); }
+__device__ __forceinline__ float4 ld_hit(const Soa& s, uint32_t p) {
+    const uint4 h = s.hm[2 * p + 1];
+    return make_float4(__uint_as_float(h.x), __uint_as_float(h.y), __uint_as_float(h.z), __uint_as_float(h.w));
+}
+// the hit record and its instance, as extend writes them
+__device__ __forceinline__ void st_hit(const Soa& s, uint32_t p, const Hit& h) {
+    s.hm[2 * p + 1] = make_uint4(__float_as_uint(h.t), __float_as_uint(h.u), __float_as_uint(h.v), h.prim);
+    s.hm[2 * p].w = h.inst;
+}
 
 // The first-hit record (fhP, fhN, fhAlb) is written by the primary step and
 // read only while the specular chain runs (the diffuse chain starts from it),
@@ -105,13 +115,12 @@ __device__ __forceinline__ float4 f4(V3 v, float w) { return make_float4(v.x, v.
 // primary step, and on the load when the path is in its specular chain.
 __device__ __forceinline__ void store_state(const Soa& s, uint32_t p, const PathState& ps, uint32_t extra_flags,
                                             bool with_first_hit) {
-    s.rng[p] = ps.rng;
-    s.dim[p] = ps.dim;
-    s.flags[p] = ps.phase | (ps.bounce << 2) | (ps.delta ? kFlagDelta : 0u) | extra_flags;
-    s.ro[p] = f4(ps.ro, 0.0f);
-    s.rd[p] = f4(ps.rd, ps.last_pdf);
-    s.thr[p] = f4(ps.thr, 0.0f);
-    s.rad[p] = f4(ps.rad, 0.0f);
+    // the hit instance (w) is the next extend's to write
+    s.hm[2 * p] = make_uint4(ps.rng, ps.dim, ps.phase | (ps.bounce << 2) | (ps.delta ? kFlagDelta : 0u) | extra_flags, 0u);
+    s.ray[2 * p] = f4(ps.ro, 0.0f);
+    s.ray[2 * p + 1] = f4(ps.rd, ps.last_pdf);
+    s.tr[2 * p] = f4(ps.thr, 0.0f);
+    s.tr[2 * p + 1] = f4(ps.rad, 0.0f);
     if (with_first_hit) {
         s.fhP[p] = f4(ps.fhP, 0.0f);
         s.fhN[p] = f4(ps.fhN, 0.0f);
@@ -119,18 +128,19 @@ __device__ __forceinline__ void store_state(const Soa& s, uint32_t p, const Path
     }
 }
 __device__ __forceinline__ void load_state(const Soa& s, uint32_t p, PathState& ps) {
-    ps.rng = s.rng[p];
-    ps.dim = s.dim[p];
-    const uint32_t f = s.flags[p];
+    const uint4 m = s.hm[2 * p];
+    ps.rng = m.x;
+    ps.dim = m.y;
+    const uint32_t f = m.z;
     ps.phase = f & 3u;
     ps.bounce = (f >> 2) & 0xFFu;
     ps.delta = (f & kFlagDelta) != 0u;
-    const float4 ro = s.ro[p], rd = s.rd[p];
+    const float4 ro = s.ray[2 * p], rd = s.ray[2 * p + 1];
     ps.ro = ld3(ro);
     ps.rd = ld3(rd);
     ps.last_pdf = rd.w;
-    ps.thr = ld3(s.thr[p]);
-    ps.rad = ld3(s.rad[p]);
+    ps.thr = ld3(s.tr[2 * p]);
+    ps.rad = ld3(s.tr[2 * p + 1]);
     if (ps.phase == kPhaseSpec) {
         ps.fhP = ld3(s.fhP[p]);
         ps.fhN = ld3(s.fhN[p]);
@@ -224,11 +234,10 @@ __global__ void __launch_bounds__(128, kLevels == 1 ? 8 : 5) k_extend(DScene sc,
     uint32_t nr = 0;
     for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < count; i += gridDim.x * blockDim.x) {
         const uint32_t p = q[i];
-        const float4 ro = s.ro[p], rd = s.rd[p];
+        const float4 ro = s.ray[2 * p], rd = s.ray[2 * p + 1];
         const Hit h = scene_closest<kStats, kLevels, kAlpha, kSh>(sc, ld3(ro), ld3(rd), 0.001f, 10000.0f, tc, e,
                                                                   s_stack + threadIdx.x);
-        s.hit[p] = make_float4(h.t, h.u, h.v, __uint_as_float(h.prim));
-        s.hit_inst[p] = h.inst;
+        st_hit(s, p, h);
         nr++;
     }
     if (e) atomicOr(err, 1);
@@ -274,9 +283,9 @@ __global__ void __launch_bounds__(128, 8) k_shade(DScene sc, PathParams pp, View
         pix = py * vp.width + px;
         PathState ps;
         load_state(s, p, ps);
-        const float4 hv = s.hit[p];
+        const float4 hv = ld_hit(s, p);
         Hit h;
-        h.t = hv.x; h.u = hv.y; h.v = hv.z; h.prim = __float_as_uint(hv.w); h.inst = s.hit_inst[p];
+        h.t = hv.x; h.u = hv.y; h.v = hv.z; h.prim = __float_as_uint(hv.w); h.inst = s.hm[2 * p].w;
         const bool primary = ps.phase == kPhasePrimary;
         ShadowReq qL, qE;
         AovOut ao;
@@ -329,7 +338,7 @@ __global__ void k_ray_keys(const LaunchBlock* lb, Soa s, int cur) {
     const uint32_t* q = s.q_ray[cur];
     for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < count; i += gridDim.x * blockDim.x) {
         const uint32_t p = q[i];
-        const float4 o = s.ro[p], d = s.rd[p];
+        const float4 o = s.ray[2 * p], d = s.ray[2 * p + 1];
         const uint32_t oct = (d.x < 0.0f ? 4u : 0u) | (d.y < 0.0f ? 2u : 0u) | (d.z < 0.0f ? 1u : 0u);
         // a point 1/8 of the scene box along the ray: groups primary rays of
         // one camera by image region and secondary rays by origin and direction
@@ -363,17 +372,18 @@ constexpr int kBinTile = 1024;   // entries per block tile of the scatter (8 per
 template <int kMode>
 __device__ __forceinline__ uint32_t bin_key(const DScene& sc, const Soa& s, uint32_t p) {
     if (kMode == 0) {
-        const uint32_t phase = s.flags[p] & 3u;
-        const uint32_t prim = __float_as_uint(s.hit[p].w);
+        const uint4 m = s.hm[2 * p];
+        const uint32_t phase = m.z & 3u;
+        const uint32_t prim = s.hm[2 * p + 1].w;
         if (prim == 0xFFFFFFFFu) return 32u | (phase << 3);
-        const DInst& in = sc.inst[s.hit_inst[p]];
+        const DInst& in = sc.inst[m.w];
         const uint32_t mid = __ldg(sc.mat_ids + (__ldg(&in.custom) & 0xFFFFFFu) + prim);
         const float4 m0 = __ldg(sc.mats + mid * 3), m1 = __ldg(sc.mats + mid * 3 + 1), m2 = __ldg(sc.mats + mid * 3 + 2);
         const bool tex = (__float_as_uint(m0.w) & __float_as_uint(m1.z) & __float_as_uint(m1.w) &
                           __float_as_uint(m2.x)) != 0xFFFFFFFFu;
         return (phase << 3) | (m1.y >= 0.5f ? 4u : 0u) | (m1.x >= 0.5f ? 2u : 0u) | (tex ? 1u : 0u);
     } else {
-        const float4 o = s.ro[p], d = s.rd[p];
+        const float4 o = s.ray[2 * p], d = s.ray[2 * p + 1];
         const uint32_t oct = (d.x < 0.0f ? 4u : 0u) | (d.y < 0.0f ? 2u : 0u) | (d.z < 0.0f ? 1u : 0u);
         auto quarter = [&](float v, int a) {
             const float f = (v - sc.box_lo[a]) * sc.box_inv[a];
@@ -537,7 +547,7 @@ __global__ void __launch_bounds__(128) k_regen(PathParams pp, const LaunchBlock*
             uint32_t px, py;
             rank_pixel(g - pv.pix_begin, pv.vp.width, pv.vp.height, px, py);
             const uint32_t pix = py * pv.vp.width + px;
-            const V3 L = firefly(pp, ld3(s.rad[p]));
+            const V3 L = firefly(pp, ld3(s.tr[2 * p + 1]));
             if (pv.path_out)
                 reinterpret_cast<float4*>(pv.path_out)[static_cast<size_t>(k) * pv.npix + pix] = f4(L, 0.0f);
             if (pv.history + k == 0) {
@@ -597,9 +607,9 @@ __global__ void __launch_bounds__(128, kLevels == 1 ? 8 : 5) k_shadow(DScene sc,
     uint32_t nr = 0;
     for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < count; i += gridDim.x * blockDim.x) {
         const uint32_t p = s.q_sh[i];
-        const uint32_t f = s.flags[p];
+        const uint32_t f = s.hm[2 * p].z;
         const V3 org = ld3(s.sh_org[p]);
-        V3 rad = ld3(s.rad[p]);
+        V3 rad = ld3(s.tr[2 * p + 1]);
         if (f & kFlagShL) {
             const float4 d = s.shL[p];
             nr++;
@@ -612,8 +622,8 @@ __global__ void __launch_bounds__(128, kLevels == 1 ? 8 : 5) k_shadow(DScene sc,
             if (!scene_occluded<kStats, kLevels, kAlpha, kSh>(sc, org, ld3(d), 0.001f, d.w, tc, e, nullptr))
                 rad = rad + ld3(s.shEc[p]);
         }
-        s.rad[p] = f4(rad, 0.0f);
-        s.flags[p] = f & ~(kFlagShL | kFlagShE);
+        s.tr[2 * p + 1] = f4(rad, 0.0f);
+        s.hm[2 * p].z = f & ~(kFlagShL | kFlagShE);
     }
     if (e) atomicOr(err, 1);
     if (kStats) add_stats(stats + 3, nr, tc);
@@ -667,7 +677,7 @@ __global__ void __launch_bounds__(128) k_extend_fetch(DScene sc, Soa s, int cur,
         const uint32_t i = wf.claim(!active, s.counts + kCtrExtendFetch, count, refill);
         if (i != 0xFFFFFFFFu) {
             p = q[i];
-            r = ray_pre(ld3(s.ro[p]), ld3(s.rd[p]));
+            r = ray_pre(ld3(s.ray[2 * p]), ld3(s.ray[2 * p + 1]));
             walk_begin<kLevels>(sc, w, r);
             active = true;
             nr++;
@@ -677,8 +687,7 @@ __global__ void __launch_bounds__(128) k_extend_fetch(DScene sc, Soa s, int cur,
             continue;
         }
         if (active && walk_step<kLevels, kStats, kAlpha>(sc, w, r, 0.001f, 10000.0f, st_node, st_t, e, &tc)) {
-            s.hit[p] = make_float4(w.best.t, w.best.u, w.best.v, __uint_as_float(w.best.prim));
-            s.hit_inst[p] = w.best.inst;
+            st_hit(s, p, w.best);
             active = false;
         }
     }
@@ -717,7 +726,7 @@ __global__ void __launch_bounds__(128) k_shadow_fetch(DScene sc, Soa s, int refi
         const uint32_t i = wf.claim(!active, s.counts + kCtrShadowFetch, count, refill);
         if (i != 0xFFFFFFFFu) {
             p = s.q_sh[i];
-            f = s.flags[p];
+            f = s.hm[2 * p].z;
             which = (f & kFlagShL) ? 0 : 1;
             start_shadow<kLevels>(sc, s, p, which, w, r);
             tmax = which == 0 ? s.shL[p].w : s.shE[p].w;
@@ -738,11 +747,11 @@ __global__ void __launch_bounds__(128) k_shadow_fetch(DScene sc, Soa s, int refi
                 nr++;
             } else {
                 const bool visE = which == 1 && !w.hit;
-                V3 rad = ld3(s.rad[p]);
+                V3 rad = ld3(s.tr[2 * p + 1]);
                 if (visL) rad = rad + ld3(s.shLc[p]);
                 if (visE) rad = rad + ld3(s.shEc[p]);
-                s.rad[p] = f4(rad, 0.0f);
-                s.flags[p] = f & ~(kFlagShL | kFlagShE);
+                s.tr[2 * p + 1] = f4(rad, 0.0f);
+                s.hm[2 * p].z = f & ~(kFlagShL | kFlagShE);
                 active = false;
             }
         }
@@ -766,7 +775,7 @@ __global__ void k_finalize(PathParams pp, uint32_t w0, uint32_t n, uint32_t widt
         float4 acc = reinterpret_cast<float4*>(accum)[pidx];
         for (uint64_t k = k0; k <= k1; ++k) {
             const uint32_t slot = static_cast<uint32_t>(k * npix + p - lo);
-            const V3 L = firefly(pp, ld3(s.rad[slot]));
+            const V3 L = firefly(pp, ld3(s.tr[2 * slot + 1]));
             if (path_out) reinterpret_cast<float4*>(path_out)[k * npix + pidx] = f4(L, 0.0f);
             if (history + k == 0) {
                 acc = make_float4(L.x, L.y, L.z, 1.0f);
@@ -826,18 +835,13 @@ struct Carve {
 
 Soa carve_soa_at(Carve& c, uint32_t cap) {
     Soa s;
-    s.rng = c.take<uint32_t>(cap);
-    s.dim = c.take<uint32_t>(cap);
-    s.flags = c.take<uint32_t>(cap);
-    s.ro = c.take<float4>(cap);
-    s.rd = c.take<float4>(cap);
-    s.thr = c.take<float4>(cap);
-    s.rad = c.take<float4>(cap);
+    s.ray = c.take<float4>(2 * static_cast<size_t>(cap));
+    s.tr = c.take<float4>(2 * static_cast<size_t>(cap));
+    s.hm = c.take<uint4>(2 * static_cast<size_t>(cap));
     s.fhP = c.take<float4>(cap);
     s.fhN = c.take<float4>(cap);
     s.fhA = c.take<float4>(cap);
-    s.hit = c.take<float4>(cap);
-    s.hit_inst = c.take<uint32_t>(cap);
+
     s.sh_org = c.take<float4>(cap);
     s.shL = c.take<float4>(cap);
     s.shLc = c.take<float4>(cap);
