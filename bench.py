@@ -1113,7 +1113,7 @@ def case_instanced_pool(arg):
 def case_traversal_shapes(arg):
     """Per-view wavefront on sphere_1m (1920x1080, 1 spp, depth 4) in each
     traversal shape -- one ray per thread, or persistent warps refilled at
-    1/2/4/8/16 idle lanes -- and queue order (queue order, material-binned
+    1-32 idle lanes -- and queue order (queue order, material-binned
     shading, ray-binned bounces); CUDA-event ms per frame (3 warm-up, 20
     timed, L2 flushed), and the images' bit identity."""
     import torch
@@ -1128,7 +1128,8 @@ def case_traversal_shapes(arg):
     flush = torch.empty(64 * 1024 * 1024, dtype=torch.float32, device="cuda")
     ref = None
     m, r = og.FLAG_SORT_MATERIAL, og.FLAG_SORT_RAYS
-    for refill, flags in ((33, 0), (33, m), (33, r), (33, m | r), (1, 0), (4, 0), (8, 0), (16, 0), (8, m), (8, r)):
+    for refill, flags in ((33, 0), (33, m), (33, r), (1, 0), (4, 0), (8, 0), (16, 0), (24, 0), (32, 0), (16, m),
+                          (24, m), (32, m)):
         st = og.make_settings(spp=1, max_bounces=4, wavefront_refill=refill, flags=flags)
         times = _time_steps(lambda k: pt.render([og.make_view(v, accum=acc)], st), 3, 20, flush)
         same = True

@@ -232,6 +232,56 @@ OHAO_D bool order_children(uint32_t rem, const float tn[8], const NodeRec& n, St
     return true;
 }
 
+// One step of the closest-hit walk of one BVH (flat, or a BLAS inside
+// instance inst_override): the node (cur, cur_tn) -- culled against the best
+// hit, else tested, its triangle leaves intersected and its internal
+// children ordered (the nearest becomes the next node) -- or else a pop.
+// Returns true when the walk is over (the stack is back at stack_base, or it
+// overflowed: err).
+template <bool kStats, bool kAlpha, class Stack>
+OHAO_D bool closest_step(const DScene& sc, const uint4* __restrict__ nodes, const float4* __restrict__ tris,
+                         const RayPre& r, float tmin, float tmax, Hit& best, uint32_t inst_override, Stack& stk,
+                         int stack_base, int lim, TravCount& cnt, int& err, int& sp, uint32_t& cur, float& cur_tn) {
+    const float tb = best.prim != 0xFFFFFFFFu ? best.t : tmax;
+    if (cur_tn <= tb + tb * kTravRelSlack) {
+        const NodeRec n = load_node(nodes, cur);
+        if (kStats) cnt.nodes++;
+        float tn[8];
+        const uint32_t hit = node_test(n, r, tmin, tb, tn);
+        const uint32_t imask = n.q0.w >> 24;
+        uint32_t lm = hit & ~imask;
+        while (lm) {
+            const int i = __ffs(lm) - 1;
+            lm &= lm - 1;
+            const uint32_t meta = byte_of(n.q1.z, n.q1.w, i);
+            const uint32_t c = meta >> 5, off = meta & 31u;
+            for (uint32_t q = 0; q < c; ++q) {
+                const float4* tp = tris + static_cast<size_t>(n.q1.y + off + q) * 3;
+                const float4 v0 = __ldg(tp), v1 = __ldg(tp + 1), v2 = __ldg(tp + 2);
+                if (kStats) cnt.tris++;
+                float t, u, v;
+                if (!tri_intersect(r, v0, v1, v2, tmin, tmax, t, u, v)) continue;
+                const uint32_t prim = __float_as_uint(v0.w);
+                const uint32_t inst = (inst_override != 0xFFFFFFFFu) ? inst_override : __float_as_uint(v1.w);
+                if (kAlpha && sc.alpha_test && !alpha_accept(sc, inst, prim, u, v)) continue;
+                if (best.prim == 0xFFFFFFFFu || t < best.t ||
+                    (t == best.t && key_less(inst, prim, best.inst, best.prim))) {
+                    best.t = t; best.u = u; best.v = v; best.inst = inst; best.prim = prim;
+                }
+            }
+        }
+        const uint32_t rem = hit & imask;
+        if (rem) {
+            if (!order_children(rem, tn, n, stk, sp, cur, cur_tn, lim)) { err = 1; return true; }
+            return false;
+        }
+    }
+    if (sp == stack_base) return true;
+    sp--;
+    stk.get(sp, cur, cur_tn);
+    return false;
+}
+
 // Closest hit in one BVH (flat, or a BLAS inside instance inst_override).
 template <bool kStats, bool kAlpha, class Stack>
 OHAO_D void bvh_closest(const DScene& sc, const uint4* __restrict__ nodes, const float4* __restrict__ tris,
@@ -241,44 +291,8 @@ OHAO_D void bvh_closest(const DScene& sc, const uint4* __restrict__ nodes, const
     int sp = stack_base;
     uint32_t cur = 0u;
     float cur_tn = -INFINITY;
-    while (true) {
-        const float tb = best.prim != 0xFFFFFFFFu ? best.t : tmax;
-        if (cur_tn <= tb + tb * kTravRelSlack) {
-            const NodeRec n = load_node(nodes, cur);
-            if (kStats) cnt.nodes++;
-            float tn[8];
-            const uint32_t hit = node_test(n, r, tmin, tb, tn);
-            const uint32_t imask = n.q0.w >> 24;
-            uint32_t lm = hit & ~imask;
-            while (lm) {
-                const int i = __ffs(lm) - 1;
-                lm &= lm - 1;
-                const uint32_t meta = byte_of(n.q1.z, n.q1.w, i);
-                const uint32_t c = meta >> 5, off = meta & 31u;
-                for (uint32_t q = 0; q < c; ++q) {
-                    const float4* tp = tris + static_cast<size_t>(n.q1.y + off + q) * 3;
-                    const float4 v0 = __ldg(tp), v1 = __ldg(tp + 1), v2 = __ldg(tp + 2);
-                    if (kStats) cnt.tris++;
-                    float t, u, v;
-                    if (!tri_intersect(r, v0, v1, v2, tmin, tmax, t, u, v)) continue;
-                    const uint32_t prim = __float_as_uint(v0.w);
-                    const uint32_t inst = (inst_override != 0xFFFFFFFFu) ? inst_override : __float_as_uint(v1.w);
-                    if (kAlpha && sc.alpha_test && !alpha_accept(sc, inst, prim, u, v)) continue;
-                    if (best.prim == 0xFFFFFFFFu || t < best.t ||
-                        (t == best.t && key_less(inst, prim, best.inst, best.prim))) {
-                        best.t = t; best.u = u; best.v = v; best.inst = inst; best.prim = prim;
-                    }
-                }
-            }
-            const uint32_t rem = hit & imask;
-            if (rem) {
-                if (!order_children(rem, tn, n, stk, sp, cur, cur_tn, lim)) { err = 1; return; }
-                continue;
-            }
-        }
-        if (sp == stack_base) return;
-        sp--;
-        stk.get(sp, cur, cur_tn);
+    while (!closest_step<kStats, kAlpha>(sc, nodes, tris, r, tmin, tmax, best, inst_override, stk, stack_base, lim,
+                                         cnt, err, sp, cur, cur_tn)) {
     }
 }
 
