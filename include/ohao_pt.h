@@ -160,10 +160,12 @@ typedef struct ohao_pt_settings {
      * deep traversals stop with OHAO_ERR_DEVICE_CHECK instead of finishing;
      * it exists to exercise that check. Not the reference's. */
     uint32_t trace_stack_limit;
-    /* Traversal shape of the per-view wavefront: 0 = the library's default;
-     * 1..32 = persistent warps over the ray queue, a warp claiming new rays
-     * once at least this many of its lanes are idle; 33 = one ray per
-     * thread over a grid-stride loop. Every shape gives the same image. */
+    /* Traversal shape of the per-view wavefront: 0 = the library's default
+     * (one ray per thread on a flat BVH, persistent warps refilled at 8 idle
+     * lanes on a two-level one); 1..32 = persistent warps over the ray
+     * queue, a warp claiming new rays once at least this many of its lanes
+     * are idle; 33 = one ray per thread over a grid-stride loop. Every shape
+     * gives the same image. */
     uint32_t wavefront_refill;
     uint32_t reserved[5];
 } ohao_pt_settings;
