@@ -599,7 +599,7 @@ __device__ __forceinline__ bool ws_wait(uint64_t* bar, uint32_t parity, volatile
 __global__ void __launch_bounds__(kWsThreads) k_conv_ws(ConvArgs a, const __nv_bfloat16* __restrict__ src_a,
                                                         const __nv_bfloat16* __restrict__ src_b, int cb_a, int cbs_a,
                                                         int cbs_b, int ntiles, int nstages, int rows, int co0,
-                                                        int* err_flag) {
+                                                        int stack, int* err_flag) {
     extern __shared__ __align__(1024) uint8_t dsm_raw[];
     __shared__ WsSmem ws;
     // offsets are from a 1024-byte aligned base (the copies need 16-byte
@@ -613,7 +613,15 @@ __global__ void __launch_bounds__(kWsThreads) k_conv_ws(ConvArgs a, const __nv_b
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     uint32_t ncols = 32;
     while (ncols < static_cast<uint32_t>(bn)) ncols <<= 1;
-    const uint32_t set_cols = static_cast<uint32_t>(rows) * ncols;   // one accumulator set: R accumulators
+    // one accumulator set: R accumulators of ncols columns; stacked (see
+    // below): R + 4 slots of bn columns, slot R + 1 - r for output row r
+    // (r = -2 .. R+1), rounded up to a power of two
+    uint32_t set_cols = static_cast<uint32_t>(rows) * ncols;
+    if (stack) {
+        set_cols = 32;
+        while (set_cols < static_cast<uint32_t>((rows + 4) * bn)) set_cols <<= 1;
+    }
+    const int cbh = cb_total >> 1;   // K steps of 16 channels per tap
     if (threadIdx.x == 0) {
         for (int s = 0; s < nstages; ++s) {
             umma::mbar_init(&ws.full[s], 1);
@@ -640,18 +648,47 @@ __global__ void __launch_bounds__(kWsThreads) k_conv_ws(ConvArgs a, const __nv_b
         ws.off_b[k] = (static_cast<uint32_t>(k0 / kBK) * static_cast<uint32_t>(bn) * 128u + ((k0 % kBK) / 16) * 256u) >> 4;
     }
     for (int c = threadIdx.x; c < bn; c += kWsThreads) ws.bias[c] = co0 + c < a.cout ? a.bias[co0 + c] : 0.0f;
-    const int kchunks = a.k_pad / kBK;
-    for (int L = threadIdx.x; L < kchunks * bn * 8; L += kWsThreads) {
-        const int kc = L / (bn * 8), l = L - kc * bn * 8;
-        const int r = l & 7, kb = (l >> 3) & 7, nb = l >> 6;
-        *reinterpret_cast<uint4*>(dsm + w_off + static_cast<uint32_t>(L) * 16) =
-            *reinterpret_cast<const uint4*>(a.w + static_cast<int64_t>(co0 + nb * 8 + r) * a.k_pad + kc * kBK + kb * 8);
+    if (!stack) {
+        const int kchunks = a.k_pad / kBK;
+        for (int L = threadIdx.x; L < kchunks * bn * 8; L += kWsThreads) {
+            const int kc = L / (bn * 8), l = L - kc * bn * 8;
+            const int r = l & 7, kb = (l >> 3) & 7, nb = l >> 6;
+            *reinterpret_cast<uint4*>(dsm + w_off + static_cast<uint32_t>(L) * 16) = *reinterpret_cast<const uint4*>(
+                a.w + static_cast<int64_t>(co0 + nb * 8 + r) * a.k_pad + kc * kBK + kb * 8);
+        }
+    } else {
+        // stacked weights: for each (dx, channel-block pair c) a B tile of
+        // 3 bn rows (row dy * bn + co: the tap (dy, dx) of output channel co)
+        // x 16 channels, K-major core matrices (8 rows x 16 B; LBO 128 B =
+        // the next 8 channels, SBO 256 B = the next 8 rows)
+        const int nrow = 3 * bn;
+        for (int L = threadIdx.x; L < 3 * cbh * nrow * 2; L += kWsThreads) {
+            const int blk_i = L / (nrow * 2), l = L - blk_i * nrow * 2;
+            const int dx = blk_i / cbh, c = blk_i - dx * cbh;
+            const int n = l >> 1, kb = l & 1;
+            const int dy = n / bn, co = n - dy * bn;
+            const uint32_t off = static_cast<uint32_t>(blk_i) * static_cast<uint32_t>(nrow) * 32u +
+                                 static_cast<uint32_t>(((n >> 3) * 2 + kb) * 128 + (n & 7) * 16);
+            *reinterpret_cast<uint4*>(dsm + w_off + off) = *reinterpret_cast<const uint4*>(
+                a.w + static_cast<int64_t>(co0 + co) * a.k_pad + (dy * 3 + dx) * a.cin8 + c * 16 + kb * 8);
+        }
     }
     umma::fence_async_smem();
     umma::tc_fence_before();
     __syncthreads();
     umma::tc_fence_after();
     const uint32_t tmem = ws.tmem;
+    if (stack) {   // the accumulators start at zero: every MMA of the stacked form adds
+        if (warp >= 2) {
+            const uint32_t q = static_cast<uint32_t>(warp & 3), half = static_cast<uint32_t>((warp - 2) >> 2);
+            for (uint32_t col = half * 32u; col < 2u * set_cols; col += 64u)
+                umma::tmem_zero32(tmem + ((q * 32u) << 16) + col);
+            umma::tmem_st_wait();
+        }
+        umma::tc_fence_before();
+        __syncthreads();
+        umma::tc_fence_after();
+    }
     const int xtiles = (a.g.w + kBM - 1) / kBM;
     const int ygroups = (a.g.h + rows - 1) / rows;
     const int first = static_cast<int>(blockIdx.x), step = static_cast<int>(gridDim.x);
@@ -717,7 +754,7 @@ __global__ void __launch_bounds__(kWsThreads) k_conv_ws(ConvArgs a, const __nv_b
                     atomicOr(err_flag, 2);
     } else if (warp == 1) {
         if (lane == 0) {   // MMA issuer: tile i from stage i % nstages into accumulator set i & 1
-            const uint32_t idesc = umma::idesc_bf16(kBM, static_cast<uint32_t>(bn), false, false);
+            const uint32_t idesc = umma::idesc_bf16(kBM, static_cast<uint32_t>(stack ? 3 * bn : bn), false, false);
             // descriptors are linear in the start address (its low 14 bits,
             // in 16-byte units; every address here is below 256 KB), so a K
             // step's descriptor is a base plus the step's offset
@@ -729,12 +766,33 @@ __global__ void __launch_bounds__(kWsThreads) k_conv_ws(ConvArgs a, const __nv_b
                 if (i >= 2 && !ws_wait(&ws.acc_empty[acc], static_cast<uint32_t>((i >> 1) - 1) & 1u, abort)) break;
                 umma::tc_fence_after();
                 const uint64_t da0 = umma::smem_desc(umma::smem_u32(dsm + static_cast<uint32_t>(s) * stage_bytes), slab, 128);
-                for (int r = 0; r < rows; ++r) {
-                    const uint32_t d = tmem + static_cast<uint32_t>(acc) * set_cols + static_cast<uint32_t>(r) * ncols;
-                    const uint64_t dar = da0 + static_cast<uint64_t>(r * kWsX);   // output row r: input rows r + dy
+                if (!stack) {
+                    for (int r = 0; r < rows; ++r) {
+                        const uint32_t d = tmem + static_cast<uint32_t>(acc) * set_cols + static_cast<uint32_t>(r) * ncols;
+                        const uint64_t dar = da0 + static_cast<uint64_t>(r * kWsX);   // output row r: input rows r + dy
 #pragma unroll 4
-                    for (int k = 0; k < ksteps; ++k)
-                        umma::mma_bf16(d, dar + ws.off_a[k], db0 + ws.off_b[k], idesc, k > 0);
+                        for (int k = 0; k < ksteps; ++k)
+                            umma::mma_bf16(d, dar + ws.off_a[k], db0 + ws.off_b[k], idesc, k > 0);
+                    }
+                } else {
+                    // stacked: neighbourhood row ri (input row y0 - 1 + ri) times
+                    // the three vertical taps at once -- N = 3 bn columns: the
+                    // slots of output rows ri, ri - 1, ri - 2 (taps dy = 0, 1, 2),
+                    // adjacent because slot(r) = R + 1 - r
+                    const uint64_t dbs = umma::smem_desc(umma::smem_u32(dsm + w_off), 128, 256);
+                    const uint64_t b_step = static_cast<uint64_t>(3 * bn * 32) >> 4;
+                    for (int ri = 0; ri < rows + 2; ++ri) {
+                        const uint32_t d = tmem + static_cast<uint32_t>(acc) * set_cols +
+                                           static_cast<uint32_t>((rows + 1 - ri) * bn);
+                        uint64_t db = dbs;
+                        for (int dx = 0; dx < 3; ++dx) {
+                            const uint64_t da = da0 + static_cast<uint64_t>(ri * kWsX + dx);
+                            for (int c = 0; c < cbh; ++c) {
+                                umma::mma_bf16(d, da + static_cast<uint64_t>(2 * c) * (slab >> 4), db, idesc, true);
+                                db += b_step;
+                            }
+                        }
+                    }
                 }
                 umma::mma_commit(&ws.empty[s]);       // the stage is read
                 umma::mma_commit(&ws.acc_full[acc]);  // the accumulator set is complete
@@ -764,11 +822,13 @@ __global__ void __launch_bounds__(kWsThreads) k_conv_ws(ConvArgs a, const __nv_b
                 const int y = y0 + r;
                 const bool live = x0 + row < a.g.w && y < a.g.h;
                 const int64_t rem = static_cast<int64_t>(y) * a.g.w + x0 + row;
-                const uint32_t trow = tmem + static_cast<uint32_t>(acc) * set_cols + static_cast<uint32_t>(r) * ncols +
-                                      (static_cast<uint32_t>(q * 32) << 16);
+                const uint32_t col = stack ? static_cast<uint32_t>((rows + 1 - r) * bn) : static_cast<uint32_t>(r) * ncols;
+                const uint32_t trow = tmem + static_cast<uint32_t>(acc) * set_cols + col + (static_cast<uint32_t>(q * 32) << 16);
                 for (int c0 = 0; c0 < bn; c0 += 32) {
                     float v[32];
-                    umma::tmem_ld32(trow + c0, v);   // warp-collective: every lane loads, the row test comes after
+                    // warp-collective: every lane loads, the row test comes after
+                    if (bn - c0 >= 32) umma::tmem_ld32(trow + c0, v);
+                    else umma::tmem_ld16(trow + c0, v);   // a 16-column slot: its neighbour is another row's
                     if (!live) continue;
 #pragma unroll
                     for (int c8 = 0; c8 < 32; c8 += 8) {
@@ -789,6 +849,20 @@ __global__ void __launch_bounds__(kWsThreads) k_conv_ws(ConvArgs a, const __nv_b
                         }
                     }
                 }
+            }
+            if (stack) {
+                // back to zero for the set's next tile: the slots of this
+                // warp's rows (read above) and, per half, two of the four
+                // slots no output row reads (rows -2, -1, R, R+1)
+                const uint32_t tq = tmem + static_cast<uint32_t>(acc) * set_cols + (static_cast<uint32_t>(q * 32) << 16);
+                auto zero_slot = [&](int slot) {
+                    for (int c = 0; c < bn; c += 16) umma::tmem_zero16(tq + static_cast<uint32_t>(slot * bn + c));
+                };
+                for (int r = half; r < rows; r += 2) zero_slot(rows + 1 - r);
+                const int g0 = half ? rows + 2 : 0;
+                zero_slot(g0);
+                zero_slot(g0 + 1);
+                umma::tmem_st_wait();
             }
             umma::tc_fence_before();
             __syncwarp();
@@ -1150,9 +1224,15 @@ bool try_conv_ws(const ConvArgs& a, int* err_flag, cudaStream_t st) {
         cudaGetLastError();
         return false;
     }
+    // stacked taps (one MMA per input row and horizontal tap covers the
+    // three vertical taps, N = 3 bn): 16 or 32 output channels and an even
+    // number of rows per tile, whose R + 4 slots fit a set of 256 columns
+    const int stack = ((bn == 32 || bn == 16) && (rows == 4 || rows == 2)) ? 1 : 0;
     // resident CTAs whose accumulator sets fit the SM's 512 tensor-memory
     // columns together, so that no CTA's allocation waits for another to finish
-    per_sm = std::min(per_sm, 512 / (2 * rows * ncols));
+    int stack_cols = 32;
+    while (stack_cols < (rows + 4) * bn) stack_cols <<= 1;
+    per_sm = std::min(per_sm, 512 / (2 * (stack ? stack_cols : rows * ncols)));
     if (concat)
         k_upsample2<<<grid_for(a.g.npix * (a.c0s / 8), 256), 256, 0, st>>>(a.x0, a.up_scratch, a.g, a.c0s);
     const int64_t tiles = static_cast<int64_t>(a.g.n) * ((a.g.h + rows - 1) / rows) * ((a.g.w + kBM - 1) / kBM);
@@ -1162,7 +1242,7 @@ bool try_conv_ws(const ConvArgs& a, int* err_flag, cudaStream_t st) {
     part.bn = bn;
     for (int k = 0; k < nsplit; ++k)
         k_conv_ws<<<grid, kWsThreads, smem, st>>>(part, src_a, src_b, cb_a, cbs_a, cbs_b, static_cast<int>(tiles),
-                                                  nstages, rows, k * bn, err_flag);
+                                                  nstages, rows, k * bn, stack, err_flag);
     return true;
 }
 
