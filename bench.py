@@ -352,13 +352,20 @@ def gate_adjoint(flush, warmup=3, steps=3):
             "adjoint_over_coordinate_fd": adj_rate / fd_rate, "clocks": clocks}, sd
 
 
-def gate_denoiser(flush, n_scenes=20, iters=3000, crop=128, batch=8, variants=6, ref_spp=4096):
+# camera samples whose first-hit features the denoiser takes beside its
+# 1-spp radiance
+AOV_SPP = 8
+
+
+def gate_denoiser(flush, n_scenes=20, iters=3000, crop=128, batch=8, variants=6, ref_spp=4096, aov_spp=AOV_SPP):
     """Config 5: the U-Net trained here by the library's own tcgen05
     kernels (bounded: n_scenes scenes x variants 1-spp renders against a
     1024-spp target, `iters` Adam steps), then judged on the 1920x1080
     headline frame against a ref_spp render: RMSE after the reference's
     display transform of the denoised 1-spp image and of plain accumulation,
-    with CUDA-event wall time of each."""
+    with CUDA-event wall time of each. The denoiser's first-hit inputs are
+    the mean over aov_spp camera samples (ohao_pt_aov; 1: the 1-spp render's
+    own record), their time counted in the denoised image's."""
     import torch
     import ohao_engine_gb300 as og
     from ohao_engine_gb300 import scenes
@@ -370,7 +377,8 @@ def gate_denoiser(flush, n_scenes=20, iters=3000, crop=128, batch=8, variants=6,
         sd = training_scene(seed, side=side, freq=64)
         pt = og.PathTracer()
         pt.load_scene(sd)
-        pairs = [render_pair(pt, sd.views[0], side, side, 1, 1024 if k == 0 else 1, seed_base=4096 * k)
+        pairs = [render_pair(pt, sd.views[0], side, side, 1, 1024 if k == 0 else 1, seed_base=4096 * k,
+                             aov_spp=aov_spp)
                  for k in range(variants)]
         data.append(([p[0] for p in pairs], [p[1] for p in pairs], pairs[0][2]))
         pt.close()
@@ -427,9 +435,13 @@ def gate_denoiser(flush, n_scenes=20, iters=3000, crop=128, batch=8, variants=6,
     noisy = torch.zeros((npix, 4), dtype=torch.float32, device="cuda")
     aov = torch.zeros((npix, og.AOV_FLOATS), dtype=torch.float32, device="cuda")
     out = torch.zeros((npix, 4), dtype=torch.float32, device="cuda")
-    render_ms = min(_time_steps(lambda k: pt.render([og.make_view(v, accum=noisy, aov=aov)],
-                                                    og.make_settings(spp=1, max_bounces=4, sample_index_base=0)),
-                                1, 3, flush))
+    def render_1spp(k):
+        pt.render([og.make_view(v, accum=noisy, aov=aov if aov_spp <= 1 else None)],
+                  og.make_settings(spp=1, max_bounces=4, sample_index_base=0))
+        if aov_spp > 1:
+            pt.aov(og.make_view(v), og.make_settings(spp=aov_spp, max_bounces=4, sample_index_base=1 << 19), aov)
+
+    render_ms = min(_time_steps(render_1spp, 1, 3, flush))
     infer_ms = min(_time_steps(lambda k: dn.infer([noisy], [aov], [out], v.width, v.height), 2, 5, flush))
     clocks = clk.stop()
     den = rmse(out)
@@ -443,7 +455,9 @@ def gate_denoiser(flush, n_scenes=20, iters=3000, crop=128, batch=8, variants=6,
     dn.close()
     res = {"workload": "U-Net 32/48/64/96/128 (BF16 tcgen05, FP32 accumulation) trained here: "
                        f"{n_scenes} scenes x 256^2 ({variants} x 1 spp vs 1024 spp), {iters} Adam steps of "
-                       f"{batch}x{crop}^2 crops; judged on sphere_1m 1920x1080 against {ref_spp} spp",
+                       f"{batch}x{crop}^2 crops; judged on sphere_1m 1920x1080 against {ref_spp} spp; "
+                       f"first-hit inputs averaged over {aov_spp} camera samples",
+           "aov_spp": aov_spp,
            "training": {"data_s": data_s, "train_s": train_s, "iters": iters,
                         "loss_first100": float(np.mean(losses[:100])), "loss_last100": float(np.mean(losses[-100:]))},
            "reference_render_s": ref_s,

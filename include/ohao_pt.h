@@ -275,6 +275,18 @@ ohao_status ohao_pt_get_profile(const ohao_pt_ctx* ctx, ohao_pt_profile* out);
  * pt_raygen.rgen:1262-1269) over npix device RGBA32F texels into device
  * RGBA8: for an accumulator written elsewhere, or a denoised image. */
 ohao_status ohao_pt_display(const float* d_rgba32f, uint32_t npix, uint8_t* d_rgba8, ohao_stream stream);
+
+/* First-hit features (the record of ohao_pt_view.aov) averaged over st->spp
+ * camera samples per pixel, sample indices st->sample_index_base + k, into
+ * d_aov ([height*width][OHAO_PT_AOV_FLOATS] floats, device): albedo,
+ * encoded normal, roughness and metallic averaged over the samples, the hit
+ * flag as the fraction of samples that hit, the view depth averaged over
+ * the samples that hit (1e30 if none). One sample gives the record a render
+ * writes for that sample, bit for bit. Costs one closest-hit traversal and
+ * one surface evaluation per sample: auxiliary inputs for a denoiser of a
+ * low-sample radiance image. Not the reference's. */
+ohao_status ohao_pt_aov(ohao_pt_ctx* ctx, const ohao_pt_view* view, const ohao_pt_settings* st, float* d_aov,
+                        ohao_stream stream);
 /* Times the compiled launch shapes of the persistent multi-view kernel
  * (block size, blocks per SM, pixels per work-queue claim) on these views
  * and keeps the fastest for later renders of this context. The views'

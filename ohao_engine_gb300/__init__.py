@@ -48,7 +48,7 @@ EXPORTED_SYMBOLS = [
     "ohao_pt_get_profile", "ohao_pt_trace", "ohao_pt_bvh_info", "ohao_pt_bvh_download", "ohao_bvh_build_noalloc",
     "ohao_pt_autotune", "ohao_pt_launch_config", "ohao_pt_launch_config_at", "ohao_pt_set_launch_config",
     "ohao_pt_backward", "ohao_pt_adjoint", "ohao_pt_display", "ohao_pt_set_geometry_device",
-    "ohao_pt_adjoint_host", "ohao_pt_set_textures", "ohao_pt_set_blas_flags",
+    "ohao_pt_adjoint_host", "ohao_pt_set_textures", "ohao_pt_set_blas_flags", "ohao_pt_aov",
 ]
 
 
@@ -135,6 +135,7 @@ def load_library(path: str | None = None):
         "ohao_pt_adjoint": ([vp, C.POINTER(View), u32, C.POINTER(Settings), C.POINTER(vp), vp, vp,
                                    C.POINTER(f32), vp], i32),
         "ohao_pt_display": ([vp, u32, vp, vp], i32),
+        "ohao_pt_aov": ([vp, C.POINTER(View), C.POINTER(Settings), vp, vp], i32),
         "ohao_pt_set_textures": ([vp, vp, u32], i32),
         "ohao_pt_set_blas_flags": ([vp, u32, u32], i32),
         "ohao_pt_adjoint_host": ([vp, C.POINTER(View), u32, C.POINTER(Settings), C.POINTER(vp), vp, vp,
@@ -439,6 +440,15 @@ class PathTracer:
                                            for a, v in zip(host_accum, views)])
         self._ck(self._L.ohao_pt_render_host(self.h, arr, len(views), C.byref(settings), ptrs,
                                              _ptr(stream) if stream is not None else None), "render_host")
+
+    def aov(self, view, settings: Settings, out, stream=None):
+        """ohao_pt_aov: first-hit features of `view` averaged over
+        settings.spp camera samples into the device buffer `out`
+        (AOV_FLOATS per pixel)."""
+        arr = _view_array([view], settings)
+        self._ck(self._L.ohao_pt_aov(self.h, arr, C.byref(settings),
+                                     _ptr(_buffer(out, view.width * view.height * AOV_FLOATS, "aov")),
+                                     _ptr(stream) if stream is not None else None), "aov")
 
     def autotune(self, views, settings: Settings, stream=None) -> float:
         arr = _view_array(views, settings)

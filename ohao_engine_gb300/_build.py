@@ -24,7 +24,7 @@ NVCC_FLAGS = ["-O3", "-lineinfo", "-std=c++20", "-fmad=false", "--extended-lambd
               "-Xcompiler", "-ffp-contract=off", "-Xptxas", "-warn-spills"]
 CXX_FLAGS = ["-O2", "-std=c++20", "-fPIC", "-ffp-contract=off", "-Wall"]
 
-CU_SOURCES = ["bvh_build.cu", "scene_kernels.cu", "wavefront.cu", "adjoint.cu", "dn_kernels.cu", "display.cu"]
+CU_SOURCES = ["bvh_build.cu", "scene_kernels.cu", "wavefront.cu", "adjoint.cu", "dn_kernels.cu", "display.cu", "aov.cu"]
 CPP_SOURCES = ["abi.cpp", "dn_net.cpp"]
 
 

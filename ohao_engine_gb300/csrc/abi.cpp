@@ -123,6 +123,12 @@ struct ohao_pt_ctx {
     }
 };
 
+namespace ohao {
+// aov.cu: mean first-hit features over nsamp camera samples per pixel
+cudaError_t launch_aov_mean(const DScene& sc, const PathParams& pp, const ViewParams& vp, uint32_t nsamp, float* out,
+                            int* err, cudaStream_t st);
+}  // namespace ohao
+
 namespace {
 
 ohao_status fail(ohao_pt_ctx* c, ohao_status s, const std::string& msg) {
@@ -919,6 +925,24 @@ ohao_status ohao_pt_render(ohao_pt_ctx* ctx, const ohao_pt_view* views, uint32_t
     for (uint32_t v = 0; v < n_views; ++v)
         if (views[v].display)
             CK(ohao::launch_display(acc[v], views[v].width * views[v].height, views[v].display, cs), "display");
+    return check_device_error(ctx, cs);
+}
+
+ohao_status ohao_pt_aov(ohao_pt_ctx* ctx, const ohao_pt_view* view, const ohao_pt_settings* st, float* d_aov,
+                        ohao_stream stream) {
+    ohao_status s = validate_render(ctx, view, 1, st);
+    if (s != OHAO_OK) return s;
+    if (!d_aov) return fail(ctx, OHAO_ERR_INVALID_ARG, "aov: null output");
+    cudaStream_t cs = reinterpret_cast<cudaStream_t>(stream);
+    CK(cudaSetDevice(ctx->device), "set device");
+    ohao::DScene sc = make_scene(ctx);
+    sc.stack_limit = stack_limit_of(st);
+    sc.alpha_test = (st->flags & OHAO_PT_FLAG_ALPHA_TEST) && any_non_opaque(ctx) ? 1u : 0u;
+    const ohao::PathParams pp{st->max_bounces, st->sampler, st->flags, st->clamp_luminance, st->aniso_strength,
+                              st->aniso_rotation, st->sample_index_base, wavefront_refill(ctx, st)};
+    float* none = nullptr;
+    const std::vector<ohao::RenderView> rv = to_render_views(view, 1, &none);
+    CK(ohao::launch_aov_mean(sc, pp, rv[0].vp, st->spp, d_aov, ctx->err_flag.as<int>(), cs), "aov");
     return check_device_error(ctx, cs);
 }
 

@@ -698,6 +698,29 @@ struct AovOut {
     float depth, hit, rough, metal;
 };
 
+// First-hit features of a camera ray's surface (or of its miss).
+OHAO_D void aov_of(const Surf& s, const ViewParams& vw, AovOut& ao) {
+    if (s.hit) {
+        ao.albedo = s.albedo;
+        ao.normal = s.N * 0.5f + v3s(0.5f);
+        // view-space depth: -(inverse(invView) * pos).z for a rigid invView
+        const float* iv = vw.inv_view;
+        const V3 c = v3(iv[12], iv[13], iv[14]);
+        const V3 fz = v3(iv[8], iv[9], iv[10]);
+        ao.depth = dot(s.pos - c, fz) * -1.0f;
+        ao.hit = 1.0f;
+        ao.rough = s.rough;
+        ao.metal = s.metal;
+    } else {
+        ao.albedo = s.color;
+        ao.normal = v3s(0.0f);
+        ao.depth = 1e30f;
+        ao.hit = 0.0f;
+        ao.rough = 0.0f;
+        ao.metal = 0.0f;
+    }
+}
+
 // Starts the diffuse chain from the stored first hit (pt_raygen.rgen:836-853).
 OHAO_D void start_diffuse_chain(const PathParams& pp, Rng& rng, uint32_t& dim, PathState& ps) {
     const float d0 = rng.s1(dim), d1 = rng.s1(dim + 1);
@@ -728,27 +751,7 @@ OHAO_D bool path_step(const DScene& sc, const PathParams& pp, const ViewParams& 
     else miss_shade(sc, pp, ps.rd, s);
 
     if (ps.phase == kPhasePrimary) {
-        if (aov) {
-            if (s.hit) {
-                aov->albedo = s.albedo;
-                aov->normal = s.N * 0.5f + v3s(0.5f);
-                // view-space depth: -(inverse(invView) * pos).z for a rigid invView
-                const float* iv = vw.inv_view;
-                const V3 c = v3(iv[12], iv[13], iv[14]);
-                const V3 fz = v3(iv[8], iv[9], iv[10]);
-                aov->depth = dot(s.pos - c, fz) * -1.0f;
-                aov->hit = 1.0f;
-                aov->rough = s.rough;
-                aov->metal = s.metal;
-            } else {
-                aov->albedo = s.color;
-                aov->normal = v3s(0.0f);
-                aov->depth = 1e30f;
-                aov->hit = 0.0f;
-                aov->rough = 0.0f;
-                aov->metal = 0.0f;
-            }
-        }
+        if (aov) aov_of(s, vw, *aov);
         if (!s.hit) {
             ps.rad = s.color;
             ps.phase = kPhaseDone;

@@ -169,17 +169,21 @@ def tonemap(rgb):
     return y ** (1.0 / 2.2)
 
 
-def render_pair(pt, view, width, height, spp_noisy, spp_ref, seed_base, max_bounces=4):
+def render_pair(pt, view, width, height, spp_noisy, spp_ref, seed_base, max_bounces=4, aov_spp=1):
     """(noisy accum, aov, reference accum) device tensors of one view: the
-    noisy image at spp_noisy (with the first-hit AOVs) and an independent
-    reference at spp_ref."""
+    noisy image at spp_noisy, its first-hit AOVs (the render's record of its
+    last sample, or with aov_spp > 1 the mean over aov_spp camera samples of
+    their own, ohao_pt_aov) and an independent reference at spp_ref."""
     import torch
     npix = width * height
     noisy = torch.zeros((npix, 4), dtype=torch.float32, device="cuda")
     aov = torch.zeros((npix, AOV_FLOATS), dtype=torch.float32, device="cuda")
     ref = torch.zeros((npix, 4), dtype=torch.float32, device="cuda")
-    pt.render([make_view(view, accum=noisy, aov=aov)],
+    pt.render([make_view(view, accum=noisy, aov=aov if aov_spp <= 1 else None)],
               make_settings(spp=spp_noisy, max_bounces=max_bounces, sample_index_base=seed_base))
+    if aov_spp > 1:
+        pt.aov(make_view(view), make_settings(spp=aov_spp, max_bounces=max_bounces,
+                                              sample_index_base=seed_base + (1 << 19)), aov)
     pt.render([make_view(view, accum=ref)],
               make_settings(spp=spp_ref, max_bounces=max_bounces, sample_index_base=seed_base + (1 << 20)))
     return noisy, aov, ref
