@@ -126,6 +126,23 @@ typedef struct ohao_pt_view {
  * instead of the roughness-scaled cosine jitter; not differentiated by
  * ohao_pt_backward / ohao_pt_adjoint. */
 #define OHAO_PT_FLAG_GGX_VNDF (1u << 9)
+/* Emitter MIS, not the reference's (which adds emission only where a BSDF
+ * ray hits it and never lets a BSDF ray find a GPULight):
+ *  - the emissive triangles (material slot-2 emission or an emissive
+ *    texture; of visible instances of opaque BLASes) become one more choice
+ *    of the light NEE (lights + 1 choices), a triangle chosen by power
+ *    (area x luminance of the slot-2 emission, + area with an emissive
+ *    texture) and a uniform point on it, both faces emitting;
+ *  - BSDF rays of the chains find sphere and area GPULights (each light
+ *    crossed, from its emitting side; the lights stay transparent);
+ *  - both sides of these emitters are weighted by the balance heuristic
+ *    between the light-NEE pdf and the BSDF pdf the estimator's env MIS
+ *    uses (pt_raygen.rgen:466-479 and 557-562), weight 1 on the BSDF side
+ *    after a delta bounce, as for the environment.
+ * Camera rays see no GPULight, as in the reference. Not differentiated by
+ * ohao_pt_backward / ohao_pt_adjoint. The emissive table is built on the
+ * first render that sets the flag after a build or material change. */
+#define OHAO_PT_FLAG_EMITTER_MIS (1u << 13)
 #define OHAO_PT_FLAG_PROFILE (1u << 16)      /* record per-kernel CUDA-event times */
 /* ohao_pt_adjoint: replay the gradient with fresh samples (sample indices
  * from sample_index_base + spp) instead of the rendered ones, so that it

@@ -34,6 +34,7 @@ FLAG_SORT_MATERIAL = 1 << 11  # shade each ray queue in material order (same ima
 FLAG_SORT_RAYS = 1 << 12      # trace each bounce's rays grouped by direction and origin (same image)
 BLAS_FLAG_NO_OPAQUE = 1
 FLAG_GGX_VNDF = 1 << 9        # VNDF sampling of the first specular bounce (not the offline estimator)
+FLAG_EMITTER_MIS = 1 << 13     # emissive triangles in the light NEE, sphere / area lights hit by BSDF rays, MIS
 FLAG_PROFILE = 1 << 16
 FLAG_ADJOINT_DECORRELATE = 1 << 17
 FLAG_ADJOINT_LDR_LOSS = 1 << 18   # loss on display values (the reference's mseRGB), targets in [0, 1]

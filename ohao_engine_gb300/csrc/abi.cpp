@@ -107,6 +107,12 @@ struct ohao_pt_ctx {
     std::vector<DevBuf*> host_accum_bufs, host_display_bufs, host_target_bufs;
     DevBuf host_grad_bufs[2];             // ohao_pt_adjoint_host: map and roughness gradients
     ohao_pt_profile profile{};
+    // emitter MIS: the emissive-triangle table (pt_types.hpp DScene::emis_*),
+    // built by the first render with OHAO_PT_FLAG_EMITTER_MIS after a build
+    // or a change of the materials' emission
+    DevBuf emis_tri, emis_cdf, emis_rank, emis_inst;
+    uint32_t nemis = 0;
+    bool emis_dirty = true;
     ohao::PersistentState* persistent = nullptr;
     // ohao_pt_render_host: history uploads run on their own stream, so that
     // they overlap the render up to its first read of the accumulator
@@ -418,6 +424,7 @@ ohao_status ohao_pt_build(ohao_pt_ctx* ctx, ohao_stream stream) {
     cudaStream_t st = reinterpret_cast<cudaStream_t>(stream);
     CK(cudaSetDevice(ctx->device), "set device");
     ctx->built = false;   // a build that fails part way leaves no usable structure
+    ctx->emis_dirty = true;
     // BLAS ranges were checked when created; geometry set since may be smaller
     for (const auto& b : ctx->blas)
         if (static_cast<uint64_t>(b.first_index) + b.index_count > static_cast<uint64_t>(ctx->ntris) * 3)
@@ -614,6 +621,7 @@ ohao_status ohao_pt_set_materials(ohao_pt_ctx* ctx, const float* m, uint32_t n) 
     if (!material_indices_valid(m, n))
         return fail(ctx, OHAO_ERR_INVALID_ARG, "set_materials: a texture index is neither 0xFFFFFFFF nor below 65536");
     ohao_status s = upload(ctx, ctx->mats, m, static_cast<size_t>(n) * 48, "materials");
+    ctx->emis_dirty = true;
     ctx->nmats = s == OHAO_OK ? n : 0;   // a failed upload may have released the table
     if (s == OHAO_OK) ctx->mats_host.assign(m, m + static_cast<size_t>(n) * 12);
     else ctx->mats_host.clear();
@@ -627,6 +635,11 @@ ohao_status ohao_pt_update_materials(ohao_pt_ctx* ctx, const float* m, uint32_t 
     if (!material_indices_valid(m, n))
         return fail(ctx, OHAO_ERR_INVALID_ARG, "update_materials: a texture index is neither 0xFFFFFFFF nor below 65536");
     if (n) CK(cudaMemcpy(ctx->mats.as<char>() + static_cast<size_t>(first) * 48, m, static_cast<size_t>(n) * 48, cudaMemcpyHostToDevice), "materials");
+    for (size_t i = 0; i < n && !ctx->emis_dirty; ++i) {   // the emission fields: emissive texture, slot-2 emission
+        const float* o = &ctx->mats_host[(first + i) * 12];
+        const float* q = m + i * 12;
+        if (std::memcmp(o + 7, q + 7, 4) != 0 || std::memcmp(o + 9, q + 9, 12) != 0) ctx->emis_dirty = true;
+    }
     std::copy(m, m + static_cast<size_t>(n) * 12, ctx->mats_host.begin() + static_cast<size_t>(first) * 12);
     summarise_material_textures(ctx);
     return OHAO_OK;
@@ -795,6 +808,140 @@ static bool any_non_opaque(const ohao_pt_ctx* ctx) {
     return false;
 }
 
+// Light-NEE weight of a material's emission: the luminance of its slot-2
+// emission (negative channels as 0), + 1 with an emissive texture; > 0 makes
+// the material's triangles emissive for emitter MIS.
+static float emission_weight(const float* m) {
+    uint32_t etex;
+    std::memcpy(&etex, m + 7, 4);
+    float l = 0.2126f * std::max(m[9], 0.0f) + 0.7152f * std::max(m[10], 0.0f) + 0.0722f * std::max(m[11], 0.0f);
+    if (etex != 0xFFFFFFFFu) l = l + 1.0f;
+    return l;
+}
+
+// The emissive-triangle table of emitter MIS. Entries run over the
+// instances in order (visible, invertible instances of opaque BLASes only)
+// and over each one's emissive triangles in order: world-space corner p0
+// (the instance transform applied as the flat build applies it), edges
+// p1 - p0, p2 - p0, the (instance, prim) ids, and the pdf per unit area of
+// choosing a point there: (its CDF step) / area, where the CDF runs over
+// area x emission_weight (in double, rounded to float, the last entry 1).
+static ohao_status build_emitter_table(ohao_pt_ctx* ctx) {
+    ctx->nemis = 0;
+    const uint32_t nm = ctx->nmats, nt = ctx->ntris;
+    std::vector<float> wmat(nm);
+    bool any = false;
+    for (uint32_t m = 0; m < nm; ++m) {
+        wmat[m] = emission_weight(&ctx->mats_host[static_cast<size_t>(m) * 12]);
+        any = any || wmat[m] > 0.0f;
+    }
+    if (!any || nt == 0 || ctx->instances.empty()) {
+        ctx->emis_dirty = false;
+        return OHAO_OK;
+    }
+    std::vector<uint32_t> mids(nt), idx(static_cast<size_t>(nt) * 3);
+    std::vector<float> pos(static_cast<size_t>(ctx->nverts) * 3);
+    CK(cudaDeviceSynchronize(), "emitter table");
+    CK(cudaMemcpy(mids.data(), ctx->mat_ids.p, mids.size() * 4, cudaMemcpyDeviceToHost), "emitter table");
+    CK(cudaMemcpy(idx.data(), ctx->indices.p, idx.size() * 4, cudaMemcpyDeviceToHost), "emitter table");
+    CK(cudaMemcpy(pos.data(), ctx->pos.p, pos.size() * 4, cudaMemcpyDeviceToHost), "emitter table");
+    std::vector<uint32_t> rank(nt);
+    uint32_t cnt = 0;
+    for (uint32_t g = 0; g < nt; ++g) {
+        const bool em = wmat[mids[g]] > 0.0f;
+        rank[g] = cnt | (em ? 0x80000000u : 0u);
+        cnt += em ? 1u : 0u;
+    }
+    const uint32_t ninst = static_cast<uint32_t>(ctx->instances.size());
+    std::vector<uint32_t> itab(static_cast<size_t>(ninst) * 2);
+    std::vector<float> tri;     // 12 floats per entry
+    std::vector<float> area;
+    std::vector<double> acc;
+    double total = 0.0;
+    for (uint32_t ii = 0; ii < ninst; ++ii) {
+        const ohao_pt_instance& in = ctx->instances[ii];
+        const BlasDesc& b = ctx->blas[in.blas];
+        const uint32_t first = in.custom_index & 0xFFFFFFu, count = b.index_count / 3;
+        itab[2 * ii] = 0xFFFFFFFFu;
+        itab[2 * ii + 1] = 0u;
+        if (!(in.mask & 0xFFu) || !instance_invertible(in.transform) || (b.flags & OHAO_BLAS_FLAG_NO_OPAQUE) ||
+            static_cast<uint64_t>(first) + count > nt)
+            continue;
+        itab[2 * ii] = static_cast<uint32_t>(area.size());
+        itab[2 * ii + 1] = count ? (rank[first] & 0x7FFFFFFFu) : 0u;
+        const float* x = in.transform;
+        for (uint32_t p = 0; p < count; ++p) {
+            if (!(rank[first + p] & 0x80000000u)) continue;
+            float w[3][3];
+            for (int k = 0; k < 3; ++k) {
+                const float* v = &pos[static_cast<size_t>(idx[b.first_index + 3 * p + k]) * 3];
+                for (int r = 0; r < 3; ++r)
+                    w[k][r] = ((x[r * 4] * v[0] + x[r * 4 + 1] * v[1]) + x[r * 4 + 2] * v[2]) + x[r * 4 + 3];
+            }
+            float e1[3], e2[3];
+            for (int r = 0; r < 3; ++r) {
+                e1[r] = w[1][r] - w[0][r];
+                e2[r] = w[2][r] - w[0][r];
+            }
+            const float cx = e1[1] * e2[2] - e1[2] * e2[1], cy = e1[2] * e2[0] - e1[0] * e2[2],
+                        cz = e1[0] * e2[1] - e1[1] * e2[0];
+            const float a = 0.5f * std::sqrt((cx * cx + cy * cy) + cz * cz);
+            total += static_cast<double>(a * wmat[mids[first + p]]);
+            acc.push_back(total);
+            area.push_back(a);
+            uint32_t ib = ii, pb = p;
+            float ibf, pbf;
+            std::memcpy(&ibf, &ib, 4);
+            std::memcpy(&pbf, &pb, 4);
+            const float e[12] = {w[0][0], w[0][1], w[0][2], 0.0f, e1[0], e1[1], e1[2], ibf, e2[0], e2[1], e2[2], pbf};
+            tri.insert(tri.end(), e, e + 12);
+        }
+    }
+    const size_t ne = area.size();
+    if (ne == 0 || !(total > 0.0) || ne >= (1ull << 31)) {
+        ctx->emis_dirty = false;
+        return OHAO_OK;
+    }
+    std::vector<float> cdf(ne);
+    for (size_t i = 0; i < ne; ++i) cdf[i] = static_cast<float>(acc[i] / total);
+    cdf[ne - 1] = 1.0f;
+    for (size_t i = 0; i < ne; ++i) {
+        const float pmf = cdf[i] - (i ? cdf[i - 1] : 0.0f);
+        tri[12 * i + 3] = area[i] > 0.0f ? pmf / area[i] : 0.0f;
+    }
+    ohao_status s;
+    if ((s = upload(ctx, ctx->emis_tri, tri.data(), tri.size() * 4, "emitter table")) != OHAO_OK) return s;
+    if ((s = upload(ctx, ctx->emis_cdf, cdf.data(), cdf.size() * 4, "emitter table")) != OHAO_OK) return s;
+    if ((s = upload(ctx, ctx->emis_rank, rank.data(), rank.size() * 4, "emitter table")) != OHAO_OK) return s;
+    if ((s = upload(ctx, ctx->emis_inst, itab.data(), itab.size() * 4, "emitter table")) != OHAO_OK) return s;
+    ctx->nemis = static_cast<uint32_t>(ne);
+    ctx->emis_dirty = false;
+    return OHAO_OK;
+}
+
+// The scene as a render with these settings sees it: stack limit, alpha
+// test, and the emitter-MIS table (built here when out of date).
+static ohao_status render_scene(ohao_pt_ctx* ctx, const ohao_pt_settings* st, ohao::DScene& sc) {
+    sc = make_scene(ctx);
+    sc.stack_limit = stack_limit_of(st);
+    sc.alpha_test = (st->flags & OHAO_PT_FLAG_ALPHA_TEST) && any_non_opaque(ctx) ? 1u : 0u;
+    if (st->flags & OHAO_PT_FLAG_EMITTER_MIS) {
+        if (ctx->emis_dirty) {
+            const ohao_status s = build_emitter_table(ctx);
+            if (s != OHAO_OK) return s;
+        }
+        sc.emitter_mis = 1u;
+        sc.nemis = ctx->nemis;
+        if (ctx->nemis) {
+            sc.emis_tri = ctx->emis_tri.as<float4>();
+            sc.emis_cdf = ctx->emis_cdf.as<float>();
+            sc.emis_rank = ctx->emis_rank.as<uint32_t>();
+            sc.emis_inst = ctx->emis_inst.as<uint2>();
+        }
+    }
+    return OHAO_OK;
+}
+
 static std::vector<ohao::RenderView> to_render_views(const ohao_pt_view* views, uint32_t n, float* const* dev_accum) {
     std::vector<ohao::RenderView> out(n);
     for (uint32_t v = 0; v < n; ++v) {
@@ -829,9 +976,11 @@ static ohao_status render_views(ohao_pt_ctx* ctx, const ohao_pt_view* views, uin
                                 const cudaEvent_t* ready = nullptr) {
     const bool profile = (st->flags & OHAO_PT_FLAG_PROFILE) != 0;
     ohao::ProfileAcc acc;
-    ohao::DScene sc = make_scene(ctx);
-    sc.stack_limit = stack_limit_of(st);
-    sc.alpha_test = (st->flags & OHAO_PT_FLAG_ALPHA_TEST) && any_non_opaque(ctx) ? 1u : 0u;
+    ohao::DScene sc;
+    {
+        const ohao_status s = render_scene(ctx, st, sc);
+        if (s != OHAO_OK) return s;
+    }
     ohao::PathParams pp{st->max_bounces, st->sampler, st->flags, st->clamp_luminance, st->aniso_strength,
                         st->aniso_rotation, st->sample_index_base, wavefront_refill(ctx, st)};
     std::vector<ohao::RenderView> rvs = to_render_views(views, n_views, dev_accum);
@@ -888,8 +1037,10 @@ ohao_status ohao_pt_autotune(ohao_pt_ctx* ctx, const ohao_pt_view* views, uint32
     ohao::PathParams pp{st->max_bounces, st->sampler, st->flags, st->clamp_luminance, st->aniso_strength,
                         st->aniso_rotation, st->sample_index_base, wavefront_refill(ctx, st)};
     const std::vector<ohao::RenderView> rvs = to_render_views(views, n_views, acc.data());
+    ohao::DScene sc;
+    if ((s = render_scene(ctx, st, sc)) != OHAO_OK) return s;
     std::string err;
-    s = ohao::persistent_autotune(ctx->persistent, make_scene(ctx), rvs.data(), n_views, pp, st->spp,
+    s = ohao::persistent_autotune(ctx->persistent, sc, rvs.data(), n_views, pp, st->spp,
                                   ctx->flat.root_box, cs, ctx->err_flag.as<int>(), best_ms, err);
     if (s != OHAO_OK) return fail(ctx, s, err);
     return check_device_error(ctx, cs);
@@ -1014,6 +1165,8 @@ static ohao_status validate_backward(ohao_pt_ctx* ctx, const ohao_pt_view* views
         return fail(ctx, OHAO_ERR_INVALID_ARG, "backward: max_bounces above 16");
     if (st->flags & OHAO_PT_FLAG_GGX_VNDF)
         return fail(ctx, OHAO_ERR_INVALID_ARG, "backward: the replay differentiates the offline estimator; clear GGX_VNDF");
+    if (st->flags & OHAO_PT_FLAG_EMITTER_MIS)
+        return fail(ctx, OHAO_ERR_INVALID_ARG, "backward: the replay differentiates the offline estimator; clear EMITTER_MIS");
     if ((st->flags & OHAO_PT_FLAG_ALPHA_TEST) || material_uses_textures(ctx))
         return fail(ctx, OHAO_ERR_UNSUPPORTED,
                     "backward: bindless textures and the alpha test are not differentiated (the tile albedo map is)");

@@ -217,6 +217,19 @@ OHAO_D V3 albedo_map_sample(const float* __restrict__ map, uint32_t mw, uint32_t
     }
     return v3(out[0], out[1], out[2]);
 }
+// Emission of a surface point: the sRGB-decoded emissive texture
+// (pt_closesthit.rchit:150-156) plus the material's slot-2 emission (not the
+// reference's). m2 = the material's third float4, etex its emissive texture.
+template <bool kTex>
+OHAO_D V3 emission_of(const DScene& sc, uint32_t etex, float4 m2, float tu, float tv) {
+    V3 emis = v3s(0.0f);
+    if (kTex && etex != 0xFFFFFFFFu) {
+        const float4 c = tex_sample(sc, etex, tu, tv);
+        emis = v3(pow_def(c.x, 2.2f), pow_def(c.y, 2.2f), pow_def(c.z, 2.2f));
+    }
+    return emis + v3(m2.y, m2.z, m2.w);
+}
+
 // pt_closesthit.rchit:37-162
 // kTex: bindless textures compiled in (scenes without them keep the shading
 // step at its register count; the tile albedo map is read either way).
@@ -305,14 +318,7 @@ OHAO_D void hit_shade(const DScene& sc, V3 o, V3 d, const Hit& h, Surf& s) {
         metal = metal * c.z;
     }
     rough = gmaxf(rough, 0.04f);
-    // emission: the sRGB-decoded emissive texture (pt_closesthit.rchit:150-156)
-    // plus the material's slot-2 emission (not the reference's)
-    V3 emis = v3s(0.0f);
-    if (kTex && etex != kNone) {
-        const float4 c = tex_sample(sc, etex, s.tu, s.tv);
-        emis = v3(pow_def(c.x, 2.2f), pow_def(c.y, 2.2f), pow_def(c.z, 2.2f));
-    }
-    s.color = emis + v3(m2.y, m2.z, m2.w);
+    s.color = emission_of<kTex>(sc, etex, m2, s.tu, s.tv);
     // payload.attenuation = (rough, clamp(metal,0,1), curv) -> unpackHitPbr
     const float ax = rough, ay = gclampf(metal, 0.0f, 1.0f);
     float rr, mm;
@@ -418,89 +424,160 @@ struct ShadowReq {
 
 // Light choice and sample point of a light NEE (the draws and geometry of
 // pt_raygen.rgen:305-383), shared by the forward step and the adjoint.
+// mis_pdf: the solid-angle pdf of the sample when the emitter can also be
+// reached by a BSDF ray (emitter MIS: emissive triangles, sphere and area
+// lights), else 0.
 struct LightSample {
     bool valid;       // NdotL > 0 && weight > 0
     V3 L, Le;
-    float weight, shadowDist, NdotL, n;
+    float weight, shadowDist, NdotL, n, mis_pdf;
 };
 
+// Number of choices of the light NEE: the analytic lights, plus the emissive
+// triangles as one more choice under emitter MIS.
+template <bool kMis>
+OHAO_D uint32_t light_choices(const DScene& sc) {
+    return sc.nlights + ((kMis && sc.nemis != 0u) ? 1u : 0u);
+}
+
+// First entry of the emissive-triangle CDF above u (the last when none is).
+OHAO_D uint32_t emis_search(const DScene& sc, float u) {
+    uint32_t lo = 0, hi = sc.nemis - 1u;
+    while (lo < hi) {
+        const uint32_t mid = (lo + hi) >> 1;
+        if (__ldg(sc.emis_cdf + mid) <= u) lo = mid + 1u;
+        else hi = mid;
+    }
+    return lo;
+}
+
+// Emission of triangle prim of instance inst at barycentrics (u, v): the
+// value hit_shade gives a ray that hits that point.
+template <bool kTex>
+OHAO_D V3 emission_at(const DScene& sc, uint32_t inst, uint32_t prim, float u, float v) {
+    const uint32_t gtri = (sc.inst[inst].custom & 0xFFFFFFu) + prim;
+    const uint32_t mid = __ldg(sc.mat_ids + gtri);
+    const float4 m1 = __ldg(sc.mats + mid * 3 + 1), m2 = __ldg(sc.mats + mid * 3 + 2);
+    const uint32_t etex = __float_as_uint(m1.w);
+    float tu = 0.0f, tv = 0.0f;
+    if (kTex && etex != 0xFFFFFFFFu) {
+        const float w = 1.0f - u - v;
+        const uint32_t i0 = __ldg(sc.indices + gtri * 3), i1 = __ldg(sc.indices + gtri * 3 + 1),
+                       i2 = __ldg(sc.indices + gtri * 3 + 2);
+        const float2 uv0 = __ldg(sc.uvs + i0), uv1 = __ldg(sc.uvs + i1), uv2 = __ldg(sc.uvs + i2);
+        tu = w * uv0.x + u * uv1.x + v * uv2.x;
+        tv = w * uv0.y + u * uv1.y + v * uv2.y;
+    }
+    return emission_of<kTex>(sc, etex, m2, tu, tv);
+}
+
+template <bool kTex = true, bool kMis = false>
 OHAO_D LightSample sample_light(const DScene& sc, Rng& rng, uint32_t& dim, V3 P, V3 N) {
     LightSample out;
-    const uint32_t n = sc.nlights;
-    uint32_t li = static_cast<uint32_t>(rng.s1(dim) * static_cast<float>(n));
+    out.mis_pdf = 0.0f;
+    const uint32_t n = light_choices<kMis>(sc);
+    const float usel = rng.s1(dim);
+    uint32_t li = static_cast<uint32_t>(usel * static_cast<float>(n));
     dim += 1;
     li = min(li, n - 1u);
-    const float4 L0 = __ldg(sc.lights + li * 5), L1 = __ldg(sc.lights + li * 5 + 1), L2 = __ldg(sc.lights + li * 5 + 2),
-                 L3 = __ldg(sc.lights + li * 5 + 3), L4 = __ldg(sc.lights + li * 5 + 4);
-    const float ltype = L0.w;
-    const V3 lc = v3(L0.x, L0.y, L0.z);
-    const V3 lcol = v3(L1.x, L1.y, L1.z);
-    const float lint = L1.w;
-    const float lrad = L2.w;
-    const V3 ldir = normalize(v3(L2.x, L2.y, L2.z));
-    const float outerAngle = L3.w;
-    const float r = gmaxf(lrad, 0.01f);
-    const float area = 4.0f * 3.14159f * r * r;
-    const V3 Le = lcol * lint / gmaxf(area, 0.01f);
-    V3 L;
+    V3 L, Le;
     float shadowDist, weight;
-    if (ltype < 0.5f) {
-        const float u1 = rng.s1(dim), u2 = rng.s1(dim + 1);
-        dim += 2;
-        const float cosT = 1.0f - 2.0f * u1;
-        const float sinT = sqrtf(gmaxf(0.0f, 1.0f - cosT * cosT));
-        const float phi = 6.2831853f * u2;
-        float sp, cp;
-        sincos_f(phi, &sp, &cp);
-        const V3 off = v3(sinT * cp, sinT * sp, cosT) * r;
-        const V3 lp = lc + off;
-        const V3 ln = normalize(off);
-        const V3 tl = lp - P;
-        const float ld = length(tl);
-        L = tl / ld;
-        const float lcos = gmaxf(dot(-L, ln), 0.0f);
-        const float la = 4.0f * 3.14159f * r * r;
-        weight = lcos * la / (ld * ld);
-        shadowDist = ld - 0.02f;
-    } else if (ltype < 1.5f) {
-        L = -ldir;
-        weight = 1.0f;
-        shadowDist = 10000.0f;
-    } else if (ltype < 2.5f) {
-        const float u1 = rng.s1(dim), u2 = rng.s1(dim + 1);
-        dim += 2;
-        const float cosT = 1.0f - 2.0f * u1;
-        const float sinT = sqrtf(gmaxf(0.0f, 1.0f - cosT * cosT));
-        const float phi = 6.2831853f * u2;
-        float sp, cp;
-        sincos_f(phi, &sp, &cp);
-        const V3 off = v3(sinT * cp, sinT * sp, cosT) * r;
-        const V3 lp = lc + off;
-        const V3 tl = lp - P;
-        const float ld = length(tl);
-        L = tl / ld;
-        shadowDist = ld - 0.02f;
-        const float cosA = dot(-L, ldir);
-        const float innerCos = cos_f(lrad * 0.017453292f);
-        const float outerCos = cos_f(outerAngle * 0.017453292f);
-        float spot = gclampf((cosA - outerCos) / (innerCos - outerCos + 0.001f), 0.0f, 1.0f);
-        spot = spot * spot;
-        const float la = 4.0f * 3.14159f * r * r;
-        weight = la / (ld * ld) * spot;
-    } else {
-        const V3 e1 = v3(L3.x, L3.y, L3.z);
-        const V3 e2 = v3(L4.x, L4.y, L4.z);
-        const float ar = L4.w;
+    if (kMis && li == sc.nlights) {
+        // an emissive triangle, chosen by power with what is left of the
+        // choice's draw, at a uniform point (barycentrics sqrt(a0)(1 - a1),
+        // sqrt(a0) a1); both faces emit
+        const uint32_t e = emis_search(sc, usel * static_cast<float>(n) - static_cast<float>(sc.nlights));
+        const float4 A = __ldg(sc.emis_tri + 3 * e), B = __ldg(sc.emis_tri + 3 * e + 1),
+                     C = __ldg(sc.emis_tri + 3 * e + 2);
         const float a0 = rng.s1(dim), a1 = rng.s1(dim + 1);
         dim += 2;
-        const V3 lp = lc + e1 * a0 + e2 * a1;
-        const V3 ln = normalize(cross(e1, e2));
+        const float su = sqrtf(a0);
+        const float b1 = su * (1.0f - a1), b2 = su * a1;
+        const V3 e1 = v3(B.x, B.y, B.z), e2 = v3(C.x, C.y, C.z);
+        const V3 lp = v3(A.x, A.y, A.z) + e1 * b1 + e2 * b2;
+        const V3 ng = normalize(cross(e1, e2));
         const V3 tl = lp - P;
         const float ld = length(tl);
         L = tl / ld;
-        const float lcos = gmaxf(dot(-L, ln), 0.0f);
-        weight = lcos * ar / (ld * ld);
+        const float lcos = fabsf(dot(L, ng));
+        Le = emission_at<kTex>(sc, __float_as_uint(B.w), __float_as_uint(C.w), b1, b2);
+        weight = lcos / (A.w * (ld * ld));
         shadowDist = ld - 0.02f;
+        out.mis_pdf = A.w * (ld * ld) / (lcos * static_cast<float>(n));
+    } else {
+        const float4 L0 = __ldg(sc.lights + li * 5), L1 = __ldg(sc.lights + li * 5 + 1),
+                     L2 = __ldg(sc.lights + li * 5 + 2), L3 = __ldg(sc.lights + li * 5 + 3),
+                     L4 = __ldg(sc.lights + li * 5 + 4);
+        const float ltype = L0.w;
+        const V3 lc = v3(L0.x, L0.y, L0.z);
+        const V3 lcol = v3(L1.x, L1.y, L1.z);
+        const float lint = L1.w;
+        const float lrad = L2.w;
+        const V3 ldir = normalize(v3(L2.x, L2.y, L2.z));
+        const float outerAngle = L3.w;
+        const float r = gmaxf(lrad, 0.01f);
+        const float area = 4.0f * 3.14159f * r * r;
+        Le = lcol * lint / gmaxf(area, 0.01f);
+        if (ltype < 0.5f) {
+            const float u1 = rng.s1(dim), u2 = rng.s1(dim + 1);
+            dim += 2;
+            const float cosT = 1.0f - 2.0f * u1;
+            const float sinT = sqrtf(gmaxf(0.0f, 1.0f - cosT * cosT));
+            const float phi = 6.2831853f * u2;
+            float sp, cp;
+            sincos_f(phi, &sp, &cp);
+            const V3 off = v3(sinT * cp, sinT * sp, cosT) * r;
+            const V3 lp = lc + off;
+            const V3 ln = normalize(off);
+            const V3 tl = lp - P;
+            const float ld = length(tl);
+            L = tl / ld;
+            const float lcos = gmaxf(dot(-L, ln), 0.0f);
+            const float la = 4.0f * 3.14159f * r * r;
+            weight = lcos * la / (ld * ld);
+            shadowDist = ld - 0.02f;
+            if (kMis) out.mis_pdf = (ld * ld) / (lcos * la * static_cast<float>(n));
+        } else if (ltype < 1.5f) {
+            L = -ldir;
+            weight = 1.0f;
+            shadowDist = 10000.0f;
+        } else if (ltype < 2.5f) {
+            const float u1 = rng.s1(dim), u2 = rng.s1(dim + 1);
+            dim += 2;
+            const float cosT = 1.0f - 2.0f * u1;
+            const float sinT = sqrtf(gmaxf(0.0f, 1.0f - cosT * cosT));
+            const float phi = 6.2831853f * u2;
+            float sp, cp;
+            sincos_f(phi, &sp, &cp);
+            const V3 off = v3(sinT * cp, sinT * sp, cosT) * r;
+            const V3 lp = lc + off;
+            const V3 tl = lp - P;
+            const float ld = length(tl);
+            L = tl / ld;
+            shadowDist = ld - 0.02f;
+            const float cosA = dot(-L, ldir);
+            const float innerCos = cos_f(lrad * 0.017453292f);
+            const float outerCos = cos_f(outerAngle * 0.017453292f);
+            float spot = gclampf((cosA - outerCos) / (innerCos - outerCos + 0.001f), 0.0f, 1.0f);
+            spot = spot * spot;
+            const float la = 4.0f * 3.14159f * r * r;
+            weight = la / (ld * ld) * spot;
+        } else {
+            const V3 e1 = v3(L3.x, L3.y, L3.z);
+            const V3 e2 = v3(L4.x, L4.y, L4.z);
+            const float ar = L4.w;
+            const float a0 = rng.s1(dim), a1 = rng.s1(dim + 1);
+            dim += 2;
+            const V3 lp = lc + e1 * a0 + e2 * a1;
+            const V3 ln = normalize(cross(e1, e2));
+            const V3 tl = lp - P;
+            const float ld = length(tl);
+            L = tl / ld;
+            const float lcos = gmaxf(dot(-L, ln), 0.0f);
+            weight = lcos * ar / (ld * ld);
+            shadowDist = ld - 0.02f;
+            if (kMis) out.mis_pdf = (ld * ld) / (lcos * ar * static_cast<float>(n));
+        }
     }
     out.NdotL = gmaxf(dot(N, L), 0.0f);
     out.valid = out.NdotL > 0.0f && weight > 0.0f;
@@ -512,16 +589,33 @@ OHAO_D LightSample sample_light(const DScene& sc, Rng& rng, uint32_t& dim, V3 P,
     return out;
 }
 
+// The BSDF pdf the estimator gives direction L at a surface (the one its env
+// MIS uses, pt_raygen.rgen:466-479): the diffuse and GGX lobes mixed by the
+// specular choice probability.
+OHAO_D float bsdf_pdf(V3 inDir, V3 N, V3 F0, float rough, float metal, float NdotL, float NdotH, float VdotH,
+                      float D) {
+    const float cosI = fabsf(dot(normalize(inDir), N));
+    const V3 fres = F0 + (1.0f - F0) * pow5f(1.0f - cosI);
+    float sp = maxc(fres) * (1.0f - rough * 0.9f);
+    sp = gmixf(sp, 1.0f, metal);
+    const float pdfD = NdotL / kPI;
+    const float pdfS = D * NdotH / (4.0f * VdotH + 1e-4f);
+    return gmixf(pdfD, pdfS, sp);
+}
+
 // Analytic light NEE; contribution precomputed as if visible. thr == null at
-// bounce 0 (pt_raygen.rgen:305-434; 585-705; 893-1013).
+// bounce 0 (pt_raygen.rgen:305-434; 585-705; 893-1013). Under emitter MIS a
+// sample of an emitter that BSDF rays can reach is weighted by the balance
+// heuristic against bsdf_pdf.
+template <bool kTex = true, bool kMis = false>
 OHAO_D void nee_light(const DScene& sc, const PathParams& pp, Rng& rng, uint32_t& dim, V3 P, V3 N, V3 inDir, V3 albedo,
                       float rough, float metal, V3 F0, const V3* thr, ShadowReq& req) {
     req.valid = false;
-    const LightSample ls = sample_light(sc, rng, dim, P, N);
+    const LightSample ls = sample_light<kTex, kMis>(sc, rng, dim, P, N);
     if (!ls.valid) return;
     const V3 L = ls.L, Le = ls.Le;
     const float NdotL = ls.NdotL, weight = ls.weight, shadowDist = ls.shadowDist;
-    const uint32_t n = sc.nlights;
+    const float n = ls.n;
     const V3 V = normalize(-inDir);
     const V3 H = normalize(L + V);
     const float NdotH = gmaxf(dot(N, H), 0.001f);
@@ -542,13 +636,82 @@ OHAO_D void nee_light(const DScene& sc, const PathParams& pp, Rng& rng, uint32_t
     const V3 kD = (1.0f - F) * (1.0f - metal);
     const V3 diff = kD * albedo / 3.14159f;
     V3 c;
-    if (thr == nullptr) c = Le * (diff + spec) * NdotL * weight * static_cast<float>(n);
-    else c = *thr * Le * (diff + spec) * NdotL * weight * static_cast<float>(n);
+    if (thr == nullptr) c = Le * (diff + spec) * NdotL * weight * n;
+    else c = *thr * Le * (diff + spec) * NdotL * weight * n;
+    if (kMis && ls.mis_pdf > 0.0f)
+        c = c * mis_balance(ls.mis_pdf, bsdf_pdf(inDir, N, F0, rough, metal, NdotL, NdotH, VdotH, D));
     req.valid = true;
     req.org = P + N * 0.01f;
     req.dir = L;
     req.tmax = shadowDist;
     req.contrib = firefly(pp, c);
+}
+
+// Emitter MIS, BSDF side: the sphere and area lights that the ray (ro, rd)
+// crosses before tmax (lights stay transparent to it, as to every ray of the
+// reference, so each one crossed counts), each seen from its emitting side
+// and weighted against its light-NEE pdf (weight 1 after a delta bounce).
+OHAO_D V3 light_hits(const DScene& sc, V3 ro, V3 rd, float tmax, bool delta, float last_pdf, float n) {
+    V3 sum = v3s(0.0f);
+    for (uint32_t li = 0; li < sc.nlights; ++li) {
+        const float4 L0 = __ldg(sc.lights + li * 5);
+        const float ltype = L0.w;
+        if (ltype >= 0.5f && ltype < 2.5f) continue;   // directional and spot lights cannot be hit
+        const float4 L1 = __ldg(sc.lights + li * 5 + 1), L2 = __ldg(sc.lights + li * 5 + 2);
+        const V3 lc = v3(L0.x, L0.y, L0.z);
+        const float r = gmaxf(L2.w, 0.01f);
+        const float area = 4.0f * 3.14159f * r * r;
+        const V3 Le = v3(L1.x, L1.y, L1.z) * L1.w / gmaxf(area, 0.01f);
+        float t, lcos, la;
+        if (ltype < 0.5f) {
+            const V3 oc = ro - lc;
+            const float b = dot(oc, rd);
+            const float c = dot(oc, oc) - r * r;
+            const float disc = b * b - c;
+            if (!(disc >= 0.0f)) continue;
+            t = -b - sqrtf(disc);
+            if (!(t > 0.001f && t < tmax)) continue;
+            const V3 ln = normalize(ro + rd * t - lc);
+            lcos = dot(-rd, ln);
+            la = 4.0f * 3.14159f * r * r;
+        } else {
+            const float4 L3 = __ldg(sc.lights + li * 5 + 3), L4 = __ldg(sc.lights + li * 5 + 4);
+            const V3 e1 = v3(L3.x, L3.y, L3.z), e2 = v3(L4.x, L4.y, L4.z);
+            const V3 nn = cross(e1, e2);
+            const V3 ln = normalize(nn);
+            lcos = dot(-rd, ln);
+            if (!(lcos > 0.0f)) continue;
+            t = dot(lc - ro, ln) / -lcos;
+            if (!(t > 0.001f && t < tmax)) continue;
+            const V3 rel = ro + rd * t - lc;
+            const float inv = 1.0f / dot(nn, nn);
+            const float a = dot(cross(rel, e2), nn) * inv;
+            const float b = dot(cross(e1, rel), nn) * inv;
+            if (!(a >= 0.0f && a <= 1.0f && b >= 0.0f && b <= 1.0f)) continue;
+            la = L4.w;
+        }
+        if (!(lcos > 0.0f)) continue;
+        float w = 1.0f;
+        if (!delta) w = mis_balance(last_pdf, (t * t) / (lcos * la * n));
+        sum = sum + Le * w;
+    }
+    return sum;
+}
+
+// Emitter MIS, BSDF side: the light-NEE pdf of a ray (direction rd) that hit
+// global triangle gtri of instance inst at distance t, or 0 when that
+// triangle is not in the emissive table.
+OHAO_D float emis_pdf_at(const DScene& sc, uint32_t inst, uint32_t gtri, V3 rd, float t, float n) {
+    const uint32_t r = __ldg(sc.emis_rank + gtri);
+    if (!(r & 0x80000000u)) return 0.0f;
+    const uint2 ib = __ldg(sc.emis_inst + inst);
+    if (ib.x == 0xFFFFFFFFu) return 0.0f;
+    const uint32_t e = ib.x + (r & 0x7FFFFFFFu) - ib.y;
+    const float4 A = __ldg(sc.emis_tri + 3 * e), B = __ldg(sc.emis_tri + 3 * e + 1), C = __ldg(sc.emis_tri + 3 * e + 2);
+    if (!(A.w > 0.0f)) return 0.0f;
+    const V3 ng = normalize(cross(v3(B.x, B.y, B.z), v3(C.x, C.y, C.z)));
+    const float lcos = fabsf(dot(rd, ng));
+    return A.w * (t * t) / (lcos * n);
 }
 
 // Env NEE sample (pt_raygen.rgen:439-451): direction, pdf, and the radiance
@@ -739,7 +902,8 @@ OHAO_D void start_diffuse_chain(const PathParams& pp, Rng& rng, uint32_t& dim, P
 // One step: consume the closest-hit result of the path's current ray, add
 // the radiance terms the shader adds here, emit up to two shadow queries and
 // set up the next ray (or finish). Returns true when a next ray is pending.
-template <bool kTex = true>
+// kMis: emitter MIS (OHAO_PT_FLAG_EMITTER_MIS) compiled in.
+template <bool kTex = true, bool kMis = false>
 OHAO_D bool path_step(const DScene& sc, const PathParams& pp, const ViewParams& vw, uint32_t px, uint32_t py,
                       uint32_t sidx, PathState& ps, const Hit& h, ShadowReq& qL, ShadowReq& qE, AovOut* aov) {
     qL.valid = false;
@@ -763,7 +927,8 @@ OHAO_D bool path_step(const DScene& sc, const PathParams& pp, const ViewParams& 
         const float rough = s.rough, metal = s.metal;
         const V3 F0 = vmix(v3s(0.04f), alb, metal);
         if (length(em) > 0.001f) ps.rad = ps.rad + em;
-        if (sc.nlights > 0) nee_light(sc, pp, rng, dim, P, N, ps.rd, alb, rough, metal, F0, nullptr, qL);
+        if (light_choices<kMis>(sc) > 0)
+            nee_light<kTex, kMis>(sc, pp, rng, dim, P, N, ps.rd, alb, rough, metal, F0, nullptr, qL);
         if (sc.has_cdf) nee_env(sc, pp, rng, dim, P, N, ps.rd, alb, rough, metal, F0, nullptr, qE);
         // stage B init (505-543)
         const V3 inDir = ps.rd;
@@ -835,6 +1000,9 @@ OHAO_D bool path_step(const DScene& sc, const PathParams& pp, const ViewParams& 
     // chain bounce (stage B or C body)
     const bool specChain = (ps.phase == kPhaseSpec);
     bool end_chain = false;
+    const float nsel = static_cast<float>(light_choices<kMis>(sc));
+    if (kMis && sc.emitter_mis)
+        ps.rad = ps.rad + ps.thr * light_hits(sc, ps.ro, ps.rd, s.hit ? h.t : 10000.0f, ps.delta, ps.last_pdf, nsel);
     if (!s.hit) {
         float w = 1.0f;
         if (s.env_pdf > 0.0f && sc.has_cdf && !ps.delta) w = mis_balance(ps.last_pdf, s.env_pdf);
@@ -842,10 +1010,19 @@ OHAO_D bool path_step(const DScene& sc, const PathParams& pp, const ViewParams& 
         end_chain = true;
     } else {
         const V3 bP = s.pos, bN = s.N, bAlb = s.albedo, bE = s.color;
-        if (length(bE) > 0.001f) ps.rad = ps.rad + ps.thr * bE;
+        if (length(bE) > 0.001f) {
+            float w = 1.0f;
+            if (kMis && sc.nemis != 0u && !ps.delta) {
+                const float pdf = emis_pdf_at(sc, h.inst, s.gtri, ps.rd, h.t, nsel);
+                if (pdf > 0.0f) w = mis_balance(ps.last_pdf, pdf);
+            }
+            if (kMis) ps.rad = ps.rad + ps.thr * bE * w;
+            else ps.rad = ps.rad + ps.thr * bE;
+        }
         const float bR = s.rough, bM = s.metal;
         const V3 bF0 = vmix(v3s(0.04f), bAlb, bM);
-        if (sc.nlights > 0) nee_light(sc, pp, rng, dim, bP, bN, ps.rd, bAlb, bR, bM, bF0, &ps.thr, qL);
+        if (light_choices<kMis>(sc) > 0)
+            nee_light<kTex, kMis>(sc, pp, rng, dim, bP, bN, ps.rd, bAlb, bR, bM, bF0, &ps.thr, qL);
         if (sc.has_cdf) nee_env(sc, pp, rng, dim, bP, bN, ps.rd, bAlb, bR, bM, bF0, &ps.thr, qE);
         bool killed = false;
         if (ps.bounce > 1) {   // Russian roulette (766-771)

@@ -65,6 +65,16 @@ struct DScene {
     uint32_t alpha_test;    // non-opaque rays: alpha-test kInstNoOpaque instances
     float box_lo[3];        // the scene's bounding box: low corner and 4 / extent per axis
     float box_inv[3];
+    // emitter MIS (OHAO_PT_FLAG_EMITTER_MIS; all zero / null otherwise):
+    // the emissive triangles are one more choice of the light NEE, sampled
+    // by power, and sphere / area lights are found by BSDF rays; both sides
+    // weighted by the balance heuristic
+    uint32_t emitter_mis;   // the flag is set on this render
+    uint32_t nemis;         // emissive-triangle entries (0: none)
+    const float4* emis_tri; // 3 per entry: (p0, pdf per area), (p1 - p0, instance bits), (p2 - p0, prim bits)
+    const float* emis_cdf;  // nemis entries, non-decreasing, the last 1
+    const uint32_t* emis_rank;  // per global triangle: bit 31 emissive, low bits its rank among the emissive ones
+    const uint2* emis_inst;     // per instance: (first entry or 0xFFFFFFFF, rank of its first triangle)
 };
 
 struct PathParams {

@@ -64,7 +64,10 @@ void orc_scene_set_geometry(Scene* s, const float* pos, uint32_t pos_stride_byte
     s->indices.assign(idx, idx + static_cast<size_t>(ntris) * 3);
     s->mat_ids.assign(matid, matid + ntris);
 }
-void orc_scene_set_materials(Scene* s, const float* m, uint32_t n) { s->mats.assign(m, m + static_cast<size_t>(n) * 12); }
+void orc_scene_set_materials(Scene* s, const float* m, uint32_t n) {
+    s->mats.assign(m, m + static_cast<size_t>(n) * 12);
+    if (!s->instances.empty()) s->build_emitters();
+}
 void orc_scene_set_lights(Scene* s, const float* l, uint32_t n) {
     s->lights.resize(n);
     if (n) std::memcpy(s->lights.data(), l, static_cast<size_t>(n) * 80);
@@ -491,6 +494,59 @@ void orc_display_rgba8(const float* rgba, uint64_t npix, uint8_t* out) {
 
 void orc_pow_def(const float* x, uint64_t n, float y, float* out) {
     for (uint64_t i = 0; i < n; ++i) out[i] = pow_def(x[i], y);
+}
+
+// Emitter-MIS table: returns the entry count; when tri / cdf are non-null
+// writes 12 floats per entry (p0, pdf_area, p1 - p0, instance bits,
+// p2 - p0, prim bits) and the CDF.
+uint32_t orc_emitter_table(const Scene* s, float* tri, float* cdf) {
+    const size_t n = s->emis.size();
+    for (size_t i = 0; tri && i < n; ++i) {
+        const auto& E = s->emis[i];
+        float* o = tri + 12 * i;
+        for (int a = 0; a < 3; ++a) { o[a] = E.p0[a]; o[4 + a] = E.e1[a]; o[8 + a] = E.e2[a]; }
+        o[3] = E.pdf_area;
+        std::memcpy(o + 7, &E.inst, 4);
+        std::memcpy(o + 11, &E.prim, 4);
+    }
+    if (cdf && n) std::memcpy(cdf, s->emis_cdf.data(), n * 4);
+    return static_cast<uint32_t>(n);
+}
+
+// n light-NEE draws at P (shading normal N) under settings flags, draw k
+// from the PCG stream of pixel (k, 0), sample `seed`. Per draw 15 floats:
+// L (3), Le (3), weight, choices, mis_pdf, valid, then the BSDF side of
+// emitter MIS for a ray from P along L: the emissive-table pdf at its
+// closest hit (0 when it hits no table triangle), and the weighted radiance
+// of the sphere / area lights it crosses with a BSDF pdf of 1 (3), and
+// the distance of that closest hit (-1: none).
+void orc_light_samples(const Scene* s, uint32_t flags, const float* P, const float* N, uint32_t n, uint32_t seed,
+                       float* out) {
+    Settings st;
+    st.flags = flags;
+    PathTracer<float> pt(*s, st);
+    const V3<float> p(P[0], P[1], P[2]), nn(N[0], N[1], N[2]);
+    const float nsel = float(pt.light_choices());
+    for (uint32_t k = 0; k < n; ++k) {
+        Sampler smp;
+        smp.init(kSamplerPCG, k, 0, seed);
+        uint32_t dim = 0;
+        const auto ls = pt.sample_light(smp, dim, p, nn);
+        float* o = out + static_cast<size_t>(k) * 15;
+        o[0] = ls.L.x; o[1] = ls.L.y; o[2] = ls.L.z;
+        o[3] = ls.Le.x; o[4] = ls.Le.y; o[5] = ls.Le.z;
+        o[6] = ls.weight; o[7] = ls.n; o[8] = ls.mis_pdf; o[9] = ls.valid ? 1.0f : 0.0f;
+        o[10] = 0.0f;
+        const float of[3] = {P[0], P[1], P[2]}, df[3] = {ls.L.x, ls.L.y, ls.L.z};
+        const HitRec h = s->closest(of, df, 0.001f, 10000.0f);
+        if (h.hit()) {
+            const uint32_t gtri = (s->instances[h.inst].custom & 0xFFFFFFu) + h.prim;
+            o[10] = pt.emis_pdf_at(h.inst, gtri, ls.L, h.t, nsel);
+        }
+        const V3<float> lh = pt.light_hits(p, ls.L, h.hit() ? h.t : 10000.0f, false, 1.0f, nsel);
+        o[11] = lh.x; o[12] = lh.y; o[13] = lh.z;
+        o[14] = h.hit() ? h.t : -1.0f;
+    }
 }
 
 int orc_num_threads() {

@@ -36,6 +36,7 @@ constexpr uint32_t kFlagFireflyClamp = 1u << 2;   // pt_raygen.rgen:58
 constexpr uint32_t kFlagEnvFixedV = 1u << 8;      // "fixed" env lookup mode (not reference)
 constexpr uint32_t kFlagVndf = 1u << 9;           // VNDF stage-B sampling (pt_raygen_realtime.rgen:723-800)
 constexpr uint32_t kFlagAlphaTest = 1u << 10;     // rays without gl_RayFlagsOpaqueEXT (pt_anyhit.rahit runs)
+constexpr uint32_t kFlagEmitterMis = 1u << 13;    // emitter MIS (not reference)
 constexpr uint32_t kSamplerPCG = 0, kSamplerSobol = 1;
 constexpr uint32_t kNoTex = 0xFFFFFFFFu;
 
@@ -178,6 +179,102 @@ struct Scene {
         return static_cast<const Scene*>(self)->alpha_accept(inst, prim, u, v);
     }
     HitFilter alpha_filter() const { return HitFilter{this, &Scene::alpha_accept_cb}; }
+    // Emitter MIS (not the reference's): the emissive triangles as one more
+    // choice of the light NEE. Entries run over the instances in order
+    // (visible, invertible instances of opaque BLASes) and each one's
+    // emissive triangles in order; pdf_area = (CDF step) / area, the CDF over
+    // area x emission_weight accumulated in double and rounded to float.
+    struct EmisTri { float p0[3], e1[3], e2[3], pdf_area; uint32_t inst, prim; };
+    std::vector<EmisTri> emis;
+    std::vector<float> emis_cdf;
+    std::vector<uint32_t> emis_rank;   // per global triangle: bit 31 emissive, low bits its rank
+    std::vector<uint32_t> emis_first;  // per instance: first entry (0xFFFFFFFF: none), rank of its first triangle
+
+    // luminance of the slot-2 emission (negative channels as 0), + 1 with an
+    // emissive texture
+    static float emission_weight(const float* m) {
+        float l = 0.2126f * std::max(m[9], 0.0f) + 0.7152f * std::max(m[10], 0.0f) + 0.0722f * std::max(m[11], 0.0f);
+        if (f2u(m[7]) != kNoTex) l = l + 1.0f;
+        return l;
+    }
+    void build_emitters() {
+        emis.clear();
+        emis_cdf.clear();
+        emis_rank.assign(mat_ids.size(), 0u);
+        emis_first.assign(instances.size() * 2, 0u);
+        const size_t nt = mat_ids.size();
+        uint32_t cnt = 0;
+        for (size_t g = 0; g < nt; ++g) {
+            const uint32_t mid = mat_ids[g];
+            const bool em = static_cast<size_t>(mid) * 12 + 12 <= mats.size() && emission_weight(&mats[mid * 12]) > 0.0f;
+            emis_rank[g] = cnt | (em ? 0x80000000u : 0u);
+            if (em) ++cnt;
+        }
+        std::vector<double> acc;
+        std::vector<float> area;
+        double total = 0.0;
+        for (uint32_t ii = 0; ii < instances.size(); ++ii) {
+            const Instance& in = instances[ii];
+            const Blas& bl = blases[in.blas];
+            const uint32_t first = in.custom & 0xFFFFFFu, count = bl.index_count / 3;
+            emis_first[2 * ii] = 0xFFFFFFFFu;
+            if (!(in.mask & 0xFFu) || !instance_invertible(in.xform) || bl.no_opaque ||
+                static_cast<uint64_t>(first) + count > nt)
+                continue;
+            emis_first[2 * ii] = static_cast<uint32_t>(emis.size());
+            emis_first[2 * ii + 1] = count ? (emis_rank[first] & 0x7FFFFFFFu) : 0u;
+            for (uint32_t p = 0; p < count; ++p) {
+                if (!(emis_rank[first + p] & 0x80000000u)) continue;
+                float v[3][3], w[3][3];
+                fetch_tri(bl.first_index, p, v);
+                for (int k = 0; k < 3; ++k) affine_xform_point(in.xform, v[k], w[k]);
+                EmisTri E;
+                for (int a = 0; a < 3; ++a) {
+                    E.p0[a] = w[0][a];
+                    E.e1[a] = w[1][a] - w[0][a];
+                    E.e2[a] = w[2][a] - w[0][a];
+                }
+                const float cx = E.e1[1] * E.e2[2] - E.e1[2] * E.e2[1];
+                const float cy = E.e1[2] * E.e2[0] - E.e1[0] * E.e2[2];
+                const float cz = E.e1[0] * E.e2[1] - E.e1[1] * E.e2[0];
+                const float a = 0.5f * std::sqrt((cx * cx + cy * cy) + cz * cz);
+                total += static_cast<double>(a * emission_weight(&mats[mat_ids[first + p] * 12]));
+                acc.push_back(total);
+                area.push_back(a);
+                E.inst = ii;
+                E.prim = p;
+                E.pdf_area = 0.0f;
+                emis.push_back(E);
+            }
+        }
+        if (emis.empty() || !(total > 0.0)) {
+            emis.clear();
+            return;
+        }
+        emis_cdf.resize(emis.size());
+        for (size_t i = 0; i < emis.size(); ++i) emis_cdf[i] = static_cast<float>(acc[i] / total);
+        emis_cdf.back() = 1.0f;
+        for (size_t i = 0; i < emis.size(); ++i) {
+            const float pmf = emis_cdf[i] - (i ? emis_cdf[i - 1] : 0.0f);
+            emis[i].pdf_area = area[i] > 0.0f ? pmf / area[i] : 0.0f;
+        }
+    }
+    // first entry whose CDF value is above u (the last when none is)
+    uint32_t emis_search(float u) const {
+        uint32_t lo = 0, hi = static_cast<uint32_t>(emis.size()) - 1u;
+        while (lo < hi) {
+            const uint32_t mid = (lo + hi) >> 1;
+            if (emis_cdf[mid] <= u) lo = mid + 1u;
+            else hi = mid;
+        }
+        return lo;
+    }
+    // the entry of a hit on global triangle gtri of instance inst, or -1
+    int64_t emis_entry(uint32_t inst, uint32_t gtri) const {
+        if (emis.empty() || !(emis_rank[gtri] & 0x80000000u) || emis_first[2 * inst] == 0xFFFFFFFFu) return -1;
+        return static_cast<int64_t>(emis_first[2 * inst] + (emis_rank[gtri] & 0x7FFFFFFFu) - emis_first[2 * inst + 1]);
+    }
+
     // acceleration structure
     std::vector<Instance> instances;
     std::vector<Blas> blases;
@@ -268,6 +365,7 @@ struct Scene {
             tlas_inst.resize(ids.size());
             for (size_t j = 0; j < ids.size(); ++j) tlas_inst[j] = ids[tlas.prim_order[j]];
         }
+        build_emitters();
     }
 
     // World box of an instance: min/max of its transform applied to every
@@ -494,8 +592,8 @@ struct Surf {                 // RayPayload after closest hit / miss
     R rough = 0, metal = 0;
     R dist = -1;
     R envPdf = 0;
-    // provenance for the adjoint
-    uint32_t gtri = 0, matid = 0;
+    // provenance for the adjoint and emitter MIS
+    uint32_t gtri = 0, matid = 0, inst = 0;
     float uv[2] = {0, 0};
 };
 
@@ -627,6 +725,7 @@ struct PathTracer {
         R w = R(1) - u - v;
         uint32_t gtri = (in.custom & 0xFFFFFFu) + h.prim;
         s.gtri = gtri;
+        s.inst = h.inst;
         uint32_t i0 = sc.indices[gtri * 3 + 0], i1 = sc.indices[gtri * 3 + 1], i2 = sc.indices[gtri * 3 + 2];
         R tu = w * R(sc.uvs[2 * i0]) + u * R(sc.uvs[2 * i1]) + v * R(sc.uvs[2 * i2]);
         R tv = w * R(sc.uvs[2 * i0 + 1]) + u * R(sc.uvs[2 * i1 + 1]) + v * R(sc.uvs[2 * i2 + 1]);
@@ -791,18 +890,71 @@ struct PathTracer {
     }
 
     // Light choice and sample point of a light NEE (the draws and geometry of
-    // pt_raygen.rgen:305-383); valid = NdotL > 0 && weight > 0.
+    // pt_raygen.rgen:305-383); valid = NdotL > 0 && weight > 0. mis_pdf: the
+    // solid-angle pdf of an emitter-MIS sample (emissive triangle, sphere or
+    // area light), else 0.
     struct LightSmp {
         bool valid = false;
         V3<R> L, Le;
-        R weight = 0, shadowDist = 0, NdotL = 0, n = 0;
+        R weight = 0, shadowDist = 0, NdotL = 0, n = 0, mis_pdf = 0;
     };
+    bool emitter_mis() const { return (st.flags & kFlagEmitterMis) != 0u; }
+    // choices of the light NEE: the lights, + the emissive triangles as one
+    uint32_t light_choices() const {
+        return static_cast<uint32_t>(sc.lights.size()) + ((emitter_mis() && !sc.emis.empty()) ? 1u : 0u);
+    }
+    // emission of triangle prim of instance inst at barycentrics (u, v), as
+    // closest_hit evaluates it
+    V3<R> emission_at(uint32_t inst, uint32_t prim, R u, R v) const {
+        const Instance& in = sc.instances[inst];
+        const uint32_t gtri = (in.custom & 0xFFFFFFu) + prim;
+        const float* m = &sc.mats[static_cast<size_t>(sc.mat_ids[gtri]) * 12];
+        const uint32_t emisTex = f2u(m[7]);
+        V3<R> emis(R(0));
+        if (emisTex != kNoTex) {
+            const R w = R(1) - u - v;
+            const uint32_t i0 = sc.indices[gtri * 3 + 0], i1 = sc.indices[gtri * 3 + 1], i2 = sc.indices[gtri * 3 + 2];
+            const R tu = w * R(sc.uvs[2 * i0]) + u * R(sc.uvs[2 * i1]) + v * R(sc.uvs[2 * i2]);
+            const R tv = w * R(sc.uvs[2 * i0 + 1]) + u * R(sc.uvs[2 * i1 + 1]) + v * R(sc.uvs[2 * i2 + 1]);
+            float c[4];
+            sc.tex_sample(emisTex, static_cast<float>(tu), static_cast<float>(tv), c);
+            emis = V3<R>(m_pow(R(c[0]), R(2.2f)), m_pow(R(c[1]), R(2.2f)), m_pow(R(c[2]), R(2.2f)));
+        }
+        return emis + V3<R>(R(m[9]), R(m[10]), R(m[11]));
+    }
     LightSmp sample_light(Sampler& smp, uint32_t& dim, V3<R> P, V3<R> N) const {
         LightSmp out;
-        const uint32_t n = static_cast<uint32_t>(sc.lights.size());
-        uint32_t li = static_cast<uint32_t>(smp.s1(dim) * float(n));
+        const uint32_t n = light_choices();
+        const uint32_t nl = static_cast<uint32_t>(sc.lights.size());
+        const float usel = smp.s1(dim);
+        uint32_t li = static_cast<uint32_t>(usel * float(n));
         dim += 1;
         li = std::min(li, n - 1u);
+        if (emitter_mis() && li == nl) {
+            // an emissive triangle by power (the rest of the choice's draw),
+            // a uniform point on it; both faces emit
+            const auto& E = sc.emis[sc.emis_search(usel * float(n) - float(nl))];
+            R a0 = R(smp.s1(dim)), a1 = R(smp.s1(dim + 1)); dim += 2;
+            R su = m_sqrt(a0);
+            R b1 = su * (R(1) - a1), b2 = su * a1;
+            V3<R> e1(R(E.e1[0]), R(E.e1[1]), R(E.e1[2])), e2(R(E.e2[0]), R(E.e2[1]), R(E.e2[2]));
+            V3<R> lp = V3<R>(R(E.p0[0]), R(E.p0[1]), R(E.p0[2])) + e1 * b1 + e2 * b2;
+            V3<R> ng = normalize(cross(e1, e2));
+            V3<R> tl = lp - P;
+            R ld = length(tl);
+            V3<R> L = tl / ld;
+            R lcos = std::fabs(dot(L, ng));
+            R weight = lcos / (R(E.pdf_area) * (ld * ld));
+            out.mis_pdf = R(E.pdf_area) * (ld * ld) / (lcos * R(float(n)));
+            out.NdotL = gmax(dot(N, L), R(0));
+            out.valid = out.NdotL > R(0) && weight > R(0);
+            out.L = L;
+            out.Le = emission_at(E.inst, E.prim, b1, b2);
+            out.weight = weight;
+            out.shadowDist = ld - R(0.02f);
+            out.n = R(float(n));
+            return out;
+        }
         const Light& L0 = sc.lights[li];
         R ltype = R(L0.pos_type[3]);
         V3<R> lc(R(L0.pos_type[0]), R(L0.pos_type[1]), R(L0.pos_type[2]));
@@ -831,6 +983,7 @@ struct PathTracer {
             R la = R(4) * R(3.14159f) * r * r;
             weight = lcos * la / (ld * ld);
             shadowDist = ld - R(0.02f);
+            if (emitter_mis()) out.mis_pdf = (ld * ld) / (lcos * la * R(float(n)));
         } else if (ltype < R(1.5f)) {
             L = -ldir;
             weight = R(1);
@@ -867,6 +1020,7 @@ struct PathTracer {
             R lcos = gmax(dot(-L, ln), R(0));
             weight = lcos * ar / (ld * ld);
             shadowDist = ld - R(0.02f);
+            if (emitter_mis()) out.mis_pdf = (ld * ld) / (lcos * ar * R(float(n)));
         }
         out.NdotL = gmax(dot(N, L), R(0));
         out.valid = out.NdotL > R(0) && weight > R(0);
@@ -889,7 +1043,7 @@ struct PathTracer {
         const LightSmp ls = sample_light(smp, dim, P, N);
         const V3<R> L = ls.L, Le = ls.Le;
         const R NdotL = ls.NdotL, weight = ls.weight;
-        const uint32_t n = static_cast<uint32_t>(sc.lights.size());
+        const R n = ls.n;
         if (ls.valid) {
             Surf<R> sh;
             if (shadow(P + N * R(0.01f), L, ls.shadowDist, sh, ts)) {
@@ -913,11 +1067,84 @@ struct PathTracer {
                 V3<R> kD = (R(1) - F) * (R(1) - metal);
                 V3<R> diff = kD * albedo / R(3.14159f);
                 out.valid = true;
-                if (bounce0) out.contrib = Le * (diff + spec) * NdotL * weight * R(float(n));
-                else out.contrib = *thr * Le * (diff + spec) * NdotL * weight * R(float(n));
+                if (bounce0) out.contrib = Le * (diff + spec) * NdotL * weight * n;
+                else out.contrib = *thr * Le * (diff + spec) * NdotL * weight * n;
+                if (ls.mis_pdf > R(0))
+                    out.contrib = out.contrib * mis(ls.mis_pdf, bsdf_pdf(inDir, N, F0, rough, metal, NdotL, NdotH, VdotH, D));
             }
         }
         return out;
+    }
+
+    // The BSDF pdf of the estimator's env MIS (pt_raygen.rgen:466-479).
+    static R bsdf_pdf(V3<R> inDir, V3<R> N, V3<R> F0, R rough, R metal, R NdotL, R NdotH, R VdotH, R D) {
+        R cosI = std::fabs(dot(normalize(inDir), N));
+        V3<R> fres = F0 + (R(1) - F0) * pow5(R(1) - cosI);
+        R sp = maxc(fres) * (R(1) - rough * R(0.9f));
+        sp = gmix(sp, R(1), metal);
+        R pdfD = NdotL / PI;
+        R pdfS = D * NdotH / (R(4) * VdotH + R(1e-4f));
+        return gmix(pdfD, pdfS, sp);
+    }
+
+    // Emitter MIS, BSDF side: the sphere and area lights the ray crosses
+    // before tmax (lights stay transparent), each from its emitting side,
+    // weighted against its light-NEE pdf (1 after a delta bounce).
+    V3<R> light_hits(V3<R> ro, V3<R> rd, R tmax, bool delta, R lastPdf, R n) const {
+        V3<R> sum(R(0));
+        for (const Light& Lt : sc.lights) {
+            const R ltype = R(Lt.pos_type[3]);
+            if (ltype >= R(0.5f) && ltype < R(2.5f)) continue;
+            V3<R> lc(R(Lt.pos_type[0]), R(Lt.pos_type[1]), R(Lt.pos_type[2]));
+            R r = gmax(R(Lt.dir_param[3]), R(0.01f));
+            R area = R(4) * R(3.14159f) * r * r;
+            V3<R> Le = V3<R>(R(Lt.col_int[0]), R(Lt.col_int[1]), R(Lt.col_int[2])) * R(Lt.col_int[3]) / gmax(area, R(0.01f));
+            R t, lcos, la;
+            if (ltype < R(0.5f)) {
+                V3<R> oc = ro - lc;
+                R b = dot(oc, rd);
+                R c = dot(oc, oc) - r * r;
+                R disc = b * b - c;
+                if (!(disc >= R(0))) continue;
+                t = -b - m_sqrt(disc);
+                if (!(t > R(0.001f) && t < tmax)) continue;
+                V3<R> ln = normalize(ro + rd * t - lc);
+                lcos = dot(-rd, ln);
+                la = R(4) * R(3.14159f) * r * r;
+            } else {
+                V3<R> e1(R(Lt.extra[0]), R(Lt.extra[1]), R(Lt.extra[2]));
+                V3<R> e2(R(Lt.extra2[0]), R(Lt.extra2[1]), R(Lt.extra2[2]));
+                V3<R> nn = cross(e1, e2);
+                V3<R> ln = normalize(nn);
+                lcos = dot(-rd, ln);
+                if (!(lcos > R(0))) continue;
+                t = dot(lc - ro, ln) / -lcos;
+                if (!(t > R(0.001f) && t < tmax)) continue;
+                V3<R> rel = ro + rd * t - lc;
+                R inv = R(1) / dot(nn, nn);
+                R a = dot(cross(rel, e2), nn) * inv;
+                R bb = dot(cross(e1, rel), nn) * inv;
+                if (!(a >= R(0) && a <= R(1) && bb >= R(0) && bb <= R(1))) continue;
+                la = R(Lt.extra2[3]);
+            }
+            if (!(lcos > R(0))) continue;
+            R w = R(1);
+            if (!delta) w = mis(lastPdf, (t * t) / (lcos * la * n));
+            sum = sum + Le * w;
+        }
+        return sum;
+    }
+
+    // Emitter MIS, BSDF side: the light-NEE pdf of a hit on an emissive-table
+    // triangle (0 for any other).
+    R emis_pdf_at(uint32_t inst, uint32_t gtri, V3<R> rd, R t, R n) const {
+        const int64_t e = sc.emis_entry(inst, gtri);
+        if (e < 0) return R(0);
+        const auto& E = sc.emis[static_cast<size_t>(e)];
+        if (!(E.pdf_area > 0.0f)) return R(0);
+        V3<R> ng = normalize(cross(V3<R>(R(E.e1[0]), R(E.e1[1]), R(E.e1[2])), V3<R>(R(E.e2[0]), R(E.e2[1]), R(E.e2[2]))));
+        R lcos = std::fabs(dot(rd, ng));
+        return R(E.pdf_area) * (t * t) / (lcos * n);
     }
 
     // Env NEE with balance MIS (pt_raygen.rgen:438-500, 708-763, 1016-1071).
@@ -1020,9 +1247,12 @@ struct PathTracer {
     void chain(Sampler& smp, uint32_t& dim, bool specChain, V3<R> ro, V3<R> rd, V3<R> thr, R lastPdf, bool lastDelta,
                V3<R>& radiance, TravStats* ts) const {
         const bool useEnvMis = sc.has_cdf;   // pc.control.w > 0 && pc.tuning.y > 0
+        const uint32_t nsel = light_choices();
         for (uint32_t bounce = 1; bounce <= st.max_bounces; ++bounce) {
             Surf<R> s;
             trace(ro, rd, s, ts);
+            if (emitter_mis())
+                radiance = radiance + thr * light_hits(ro, rd, s.hit ? s.dist : R(10000), lastDelta, lastPdf, R(float(nsel)));
             if (!s.hit) {
                 R w = R(1);
                 if (s.envPdf > R(0) && useEnvMis && !lastDelta) w = mis(lastPdf, s.envPdf);
@@ -1030,10 +1260,21 @@ struct PathTracer {
                 break;
             }
             V3<R> bP = s.hitPos, bN = s.N, bAlb = s.albedo, bE = s.color;
-            if (length(bE) > R(0.001f)) radiance = radiance + thr * bE;
+            if (length(bE) > R(0.001f)) {
+                if (emitter_mis()) {
+                    R w = R(1);
+                    if (!sc.emis.empty() && !lastDelta) {
+                        const R pdf = emis_pdf_at(s.inst, s.gtri, rd, s.dist, R(float(nsel)));
+                        if (pdf > R(0)) w = mis(lastPdf, pdf);
+                    }
+                    radiance = radiance + thr * bE * w;
+                } else {
+                    radiance = radiance + thr * bE;
+                }
+            }
             R bR = s.rough, bM = s.metal;
             V3<R> bF0 = vmix(V3<R>(R(0.04f)), bAlb, bM);
-            if (!sc.lights.empty()) {
+            if (nsel > 0) {
                 NeeOut o = nee_light(smp, dim, bP, bN, rd, bAlb, bR, bM, bF0, &thr, ts);
                 if (o.valid) radiance = radiance + clampc(o.contrib);
             }
@@ -1134,7 +1375,7 @@ struct PathTracer {
             R rough = s.rough, metal = s.metal;
             V3<R> F0 = vmix(V3<R>(R(0.04f)), alb, metal);
             if (length(em) > R(0.001f)) radiance = radiance + em;
-            if (!sc.lights.empty()) {
+            if (light_choices() > 0) {
                 NeeOut o = nee_light(smp, dim, P, N, rayDir, alb, rough, metal, F0, nullptr, ts);
                 if (o.valid) radiance = radiance + clampc(o.contrib);
             }

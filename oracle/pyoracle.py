@@ -56,6 +56,9 @@ def lib():
         L.orc_scene_set_textures.argtypes = [vp, vp, vp, u32]
         L.orc_scene_set_blas_flags.argtypes = [vp, u32, u32]
         L.orc_alpha_accept.argtypes = [vp, vp, vp, vp, u32, vp]
+        L.orc_emitter_table.argtypes = [vp, vp, vp]
+        L.orc_emitter_table.restype = u32
+        L.orc_light_samples.argtypes = [vp, u32, vp, vp, u32, u32, vp]
         L.orc_scene_add_blas.argtypes = [vp, u32, u32]
         L.orc_scene_add_blas.restype = u32
         L.orc_scene_set_instances.argtypes = [vp, vp, u32]
@@ -282,6 +285,28 @@ class OracleScene:
         lib().orc_render_paths(self.h, _p(view.inv_view), _p(view.inv_proj), view.width, view.height, _p(st),
                                sample_base, spp, _p(pix), npix, _p(out), int(fp64), nthreads, _p(s))
         return (out, s) if stats else out
+
+    def emitter_table(self):
+        """Emitter-MIS table: (entries [n, 12] float32: p0, pdf per area,
+        p1 - p0, instance bits, p2 - p0, prim bits; CDF [n])."""
+        L = lib()
+        n = L.orc_emitter_table(self.h, None, None)
+        tri = np.zeros((n, 12), np.float32)
+        cdf = np.zeros(n, np.float32)
+        if n:
+            L.orc_emitter_table(self.h, _p(tri), _p(cdf))
+        return tri, cdf
+
+    def light_samples(self, flags: int, P, N, n: int, seed: int = 0):
+        """n light-NEE draws at P (normal N): [n, 15] float32 = L, Le,
+        weight, choices, mis_pdf, valid, the emissive-table pdf at the
+        closest hit along L from P, the weighted sphere / area light radiance
+        along it (BSDF pdf 1), that hit's distance (-1: none)."""
+        out = np.zeros((n, 15), np.float32)
+        P = np.ascontiguousarray(P, np.float32)
+        N = np.ascontiguousarray(N, np.float32)
+        lib().orc_light_samples(self.h, flags, _p(P), _p(N), n, seed, _p(out))
+        return out
 
     def detached_paths(self, view, settings: dict, sample_base: int, spp: int, pixels=None, materials=None,
                        albedo_map=None, nthreads: int = 0):
