@@ -1124,6 +1124,38 @@ def case_instanced_pool(arg):
     print(f"instanced 4 views 384^2 x 4 spp, {pt.launch_config}: {ms:.3f} ms per call")
 
 
+def case_emitter_mis(arg):
+    """Emitter MIS on scenes.emitters (512x320, glossy floor of roughness
+    0.25, an area and a sphere light): for the reference estimator and with
+    OHAO_PT_FLAG_EMITTER_MIS, CUDA-event ms per 4-spp frame and the
+    per-pixel variance of one path (64 paths per pixel; mean and median
+    over the pixels)."""
+    import torch
+    import ohao_engine_gb300 as og
+    from ohao_engine_gb300 import scenes
+    sd = scenes.emitters(width=512, height=320, floor_rough=0.25)
+    pt = og.PathTracer()
+    pt.load_scene(sd)
+    v = sd.views[0]
+    npix = v.width * v.height
+    acc = torch.zeros((npix, 4), dtype=torch.float32, device="cuda")
+    paths = torch.zeros((64, npix, 4), dtype=torch.float32, device="cuda")
+    stats = {}
+    for name, flags in (("reference", 0), ("emitter MIS", og.FLAG_EMITTER_MIS)):
+        pt.render([og.make_view(v, accum=acc, path_radiance=paths)],
+                  og.make_settings(spp=64, max_bounces=4, flags=flags, sample_index_base=1 << 16))
+        var = paths[..., :3].var(dim=0).sum(-1)
+        mean = paths[..., :3].mean(dim=0)
+        ms = _timed_calls(lambda: pt.render([og.make_view(v, accum=acc)], og.make_settings(spp=4, max_bounces=4,
+                                                                                          flags=flags)), 10)
+        stats[name] = (float(var.mean()), float(var.median()), mean)
+        print(f"{name:12s}: {ms:.3f} ms per 4-spp frame; per-pixel path variance mean {stats[name][0]:.3f} "
+              f"median {stats[name][1]:.4f}")
+    r, m = stats["reference"], stats["emitter MIS"]
+    print(f"variance ratio (reference / MIS): mean {r[0] / m[0]:.2f}, median {r[1] / m[1]:.2f}; mean radiance "
+          f"{float(r[2].mean()):.4f} / {float(m[2].mean()):.4f}")
+
+
 def case_traversal_shapes(arg):
     """Per-view wavefront on sphere_1m (1920x1080, 1 spp, depth 4) in each
     traversal shape -- one ray per thread, or persistent warps refilled at
@@ -1161,7 +1193,7 @@ def case_traversal_shapes(arg):
 
 
 CASES = {"traversal_shapes": case_traversal_shapes, "denoise_infer": case_denoise_infer, "adjoint": case_adjoint, "instanced_view": case_instanced_view,
-         "instanced_pool": case_instanced_pool}
+         "instanced_pool": case_instanced_pool, "emitter_mis": case_emitter_mis}
 
 
 def run_case(args):

@@ -79,50 +79,7 @@ def rel_err(a, b, floor=1e-6):
     return np.abs(a - b) / np.maximum(np.maximum(np.abs(a), np.abs(b)), floor)
 
 
+
 def emitter_scene(width=40, height=24, lights=("area", "sphere"), env=False):
-    """Emitter-MIS scene: a floor, a metal box, a near-mirror panel, two
-    emissive quads (small and bright overhead, large and dim on a wall) in
-    BLAS 0; one emissive triangle in BLAS 1, instanced scaled and moved,
-    and again masked out; the same triangle in BLAS 2, non-opaque. Optional
-    area and sphere GPULights and an environment."""
-    b = scenes._Builder()
-    mats = [scenes.material((0.7, 0.7, 0.7), rough=0.9),
-            scenes.material((0.6, 0.3, 0.2), rough=0.3, metal=1.0),
-            scenes.material((0.8, 0.8, 0.8), emissive=(40.0, 30.0, 20.0)),
-            scenes.material((0.5, 0.5, 0.5), emissive=(1.0, 1.5, 2.0)),
-            scenes.material((0.2, 0.6, 0.3), rough=0.02),
-            scenes.material((0.9, 0.9, 0.9), emissive=(5.0, 4.0, 6.0))]
-    h = 3.0
-    b.quad((-h, -1, -h), (-h, -1, h), (h, -1, h), (h, -1, -h), (0, 1, 0), 0)
-    scenes._box(b, (0.6, -1.0, -0.3), (0.6, 0.8, 0.6), 20.0, 1)
-    b.quad((1.6, -1.0, 0.8), (1.6, -1.0, -0.8), (1.6, 0.4, -0.8), (1.6, 0.4, 0.8), (-1, 0, 0), 4)
-    b.quad((-0.3, 1.2, 0.2), (0.3, 1.2, 0.2), (0.3, 1.2, -0.2), (-0.3, 1.2, -0.2), (0, -1, 0), 2)
-    b.quad((-2.5, -1.0, -1.5), (-2.5, -1.0, 1.5), (-2.5, 1.0, 1.5), (-2.5, 1.0, -1.5), (1, 0, 0), 3)
-    n0 = b.ntri * 3
-    b.add(np.array([(0.0, 0.0, 0.0), (1.0, 0.0, 0.0), (0.0, 0.0, 1.0)]), np.tile([0.0, -1.0, 0.0], (3, 1)),
-          np.array([(0, 0), (1, 0), (0, 1)], np.float64), [[0, 1, 2]], 5)
-    P, N, U, I, M = b.arrays()
-    inst = scenes.identity_instance(4)
-    x = np.zeros((3, 4), np.float32)
-    x[:, :3] = np.diag([0.8, 1.0, 0.6])
-    x[:, 3] = (-1.2, 0.9, 0.6)
-    for k in (1, 2, 3):
-        inst[k]["blas"] = 1 if k < 3 else 2
-        inst[k]["custom_index"] = n0 // 3
-        inst[k]["xform"] = x.reshape(-1)
-    inst[2]["mask"] = 0
-    inst[3]["xform"][3] = 1.5      # the non-opaque copy elsewhere
-    ls = []
-    if "area" in lights:
-        ls.append(scenes.area_light((0.9, 1.1, 0.9), (0.0, 0.0, -0.3), (0.4, 0.0, 0.0), 12.0, (1.0, 0.9, 0.7)))
-    if "sphere" in lights:
-        L = np.zeros(20, np.float32)
-        L[0:4] = (-0.8, 0.6, 1.2, 0.0)
-        L[4:8] = (0.7, 0.8, 1.0, 8.0)
-        L[11] = 0.2
-        ls.append(L)
-    lights_arr = np.stack(ls) if ls else np.zeros((0, 20), np.float32)
-    envmap = scenes.sky_env(64, 32, seed=4, peak=200.0, radius_deg=4.0) if env else None
-    view = scenes.look_at_view((0.2, 0.6, 4.0), (0.0, -0.2, 0.0), fov_y_deg=50.0, width=width, height=height)
-    return scenes.SceneData("emitters", P, N, U, I, M, np.stack(mats), lights_arr, envmap, 1.0,
-                            [(0, n0), (n0, 3), (n0, 3)], inst, [view], spp=4, max_bounces=4, blas_flags=[0, 0, 1])
+    """scenes.emitters at a test size."""
+    return scenes.emitters(width=width, height=height, lights=lights, env=env)
