@@ -408,8 +408,8 @@ ohao_status ohao_pt_bvh_download(ohao_pt_ctx* ctx, int32_t which, void* nodes, v
  * on it and must be serialised by the caller. The first call on a device
  * resolves the array's device address (cached per device ordinal; a
  * cudaDeviceReset of that device invalidates it, so the library is not used
- * on a device after a reset) and should come before any stream capture.
- * Every call blocks the host until its build on `stream` has finished. */
+ * on a device after a reset). Every call blocks the host until its build on
+ * `stream` has finished. */
 #define OHAO_BVH_NOALLOC_MAX_PRIMS 65536u
 ohao_status ohao_bvh_build_noalloc(const float* d_boxes, uint32_t n, void* d_nodes, uint32_t* d_prim_order,
                                    float* d_root_box, uint32_t* out_nnodes, uint32_t* out_height, ohao_stream stream);
