@@ -379,8 +379,8 @@ typedef struct ohao_bvh8_node {
     uint32_t child_base;       /* first internal child node */
     uint32_t tri_base;         /* first primitive of this node's leaves */
     uint8_t meta[8];           /* 0 empty; 0x80|rank internal; (count<<5)|offset leaf */
-    uint8_t qlo[3][8];
-    uint8_t qhi[3][8];
+    uint8_t qlo[3][8];         /* child box per axis on the grid, rounded outward; */
+    uint8_t qhi[3][8];         /* an empty slot holds qlo 255, qhi 0 (no ray enters it) */
 } ohao_bvh8_node;               /* 80 bytes */
 typedef struct ohao_bvh_tri {
     float v0[3]; uint32_t prim;

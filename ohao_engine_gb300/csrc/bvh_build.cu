@@ -410,6 +410,10 @@ __global__ void k_layout_level(TreeView t, const uint32_t* __restrict__ order, c
                 bytes[32 + a * 8 + k] = static_cast<uint8_t>(fmax(0.0, ql));
                 bytes[56 + a * 8 + k] = static_cast<uint8_t>(fmin(255.0, qh));
             }
+            for (int k = cnt; k < 8; ++k) {   // unused slot: the inverted box 255..0, which no ray enters
+                bytes[32 + a * 8 + k] = 0xFFu;
+                bytes[56 + a * 8 + k] = 0u;
+            }
         }
         uint32_t nint = 0, nleaf = 0;
         for (int k = 0; k < cnt; ++k) {

@@ -195,9 +195,10 @@ OHAO_D uint32_t node_test(const NodeRec& n, const RayPre& r, float tmin, float t
         const float t0 = max3f(vnx, vny, vnz);
         const float t1 = min3f(vfx, vfy, vfz);
         tn[i] = t0;
-        const uint32_t meta = byte_of(n.q1.z, n.q1.w, i);
-        // t0 <= t1, t0 <= tlimit and t1 >= tmin at once (tmin <= tlimit always)
-        if (meta != 0u && fmaxf(t0, tmin) <= fminf(t1, tlimit)) hit |= 1u << i;
+        // t0 <= t1, t0 <= tlimit and t1 >= tmin at once (tmin <= tlimit always).
+        // Unused slots hold the inverted box 255..0, which fails this test (and
+        // were it to pass, the slot is a leaf of no triangles: no effect).
+        if (fmaxf(t0, tmin) <= fminf(t1, tlimit)) hit |= 1u << i;
     }
     return hit;
 }

@@ -17,7 +17,8 @@
 //   6. layout: a node's internal children are contiguous, followed by their
 //      subtrees in slot order; leaf primitives of a node are contiguous;
 //   7. child boxes quantized to 8 bits per side on a per-axis power-of-two
-//      grid anchored at the node's lower corner, rounded outward.
+//      grid anchored at the node's lower corner, rounded outward; unused
+//      slots hold the inverted box (lo 255, hi 0) and meta 0.
 // Closest hit: smallest t in (tmin, tmax) by the watertight ray/triangle test
 // of Woop, Benthin and Wald (JCGT 2013); equal t resolves to the smallest
 // (instance, primitive) pair, so the answer does not depend on traversal
@@ -315,6 +316,10 @@ private:
                 double qh = std::ceil(std::ldexp(static_cast<double>(cb.hi[a]) - static_cast<double>(nb.lo[a]), -e[a]));
                 w.qlo[a][k] = static_cast<uint8_t>(std::max(0.0, ql));
                 w.qhi[a][k] = static_cast<uint8_t>(std::min(255.0, qh));
+            }
+            for (uint32_t k = c.cnt; k < 8; ++k) {   // unused slot: the inverted box 255..0
+                w.qlo[a][k] = 255;
+                w.qhi[a][k] = 0;
             }
         }
         // slots
