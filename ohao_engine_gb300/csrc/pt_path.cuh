@@ -902,8 +902,10 @@ OHAO_D void start_diffuse_chain(const PathParams& pp, Rng& rng, uint32_t& dim, P
 // One step: consume the closest-hit result of the path's current ray, add
 // the radiance terms the shader adds here, emit up to two shadow queries and
 // set up the next ray (or finish). Returns true when a next ray is pending.
-// kMis: emitter MIS (OHAO_PT_FLAG_EMITTER_MIS) compiled in.
-template <bool kTex = true, bool kMis = false>
+// kMis: emitter MIS (OHAO_PT_FLAG_EMITTER_MIS) compiled in. kPhase: 0 any
+// path, 1 only paths at their camera ray, 2 only paths in a chain (a caller
+// that knows its queue holds one kind compiles the other branch out).
+template <bool kTex = true, bool kMis = false, int kPhase = 0>
 OHAO_D bool path_step(const DScene& sc, const PathParams& pp, const ViewParams& vw, uint32_t px, uint32_t py,
                       uint32_t sidx, PathState& ps, const Hit& h, ShadowReq& qL, ShadowReq& qE, AovOut* aov) {
     qL.valid = false;
@@ -914,7 +916,7 @@ OHAO_D bool path_step(const DScene& sc, const PathParams& pp, const ViewParams& 
     if (h.prim != 0xFFFFFFFFu) hit_shade<kTex>(sc, ps.ro, ps.rd, h, s);
     else miss_shade(sc, pp, ps.rd, s);
 
-    if (ps.phase == kPhasePrimary) {
+    if (kPhase == 1 || (kPhase == 0 && ps.phase == kPhasePrimary)) {
         if (aov) aov_of(s, vw, *aov);
         if (!s.hit) {
             ps.rad = s.color;

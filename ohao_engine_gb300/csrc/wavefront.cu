@@ -251,7 +251,7 @@ __global__ void __launch_bounds__(128, kLevels == 1 ? 8 : 5) k_extend(DScene sc,
 // (scene and state loads, 21% of issue slots at 128 registers and 4 blocks),
 // and 32 warps hide more of it than the spills cost (sphere_1m: 376 -> 402
 // Msamples/s; 10 or 12 blocks gain under 1% more).
-template <bool kPool, bool kTex, bool kMis>
+template <bool kPool, bool kTex, bool kMis, int kPhase>
 __global__ void __launch_bounds__(128, 8) k_shade(DScene sc, PathParams pp, ViewParams vp_plain, uint32_t w0,
                                                uint32_t npix_plain, Soa s, int cur, float* aov_plain, uint32_t aov_k,
                                                const LaunchBlock* lb) {
@@ -290,8 +290,8 @@ __global__ void __launch_bounds__(128, 8) k_shade(DScene sc, PathParams pp, View
         ShadowReq qL, qE;
         AovOut ao;
         const bool want_aov = aov != nullptr && primary && k == aov_k;
-        const bool more = path_step<kTex, kMis>(sc, pp, vp, px, py, pp.sample_base + k, ps, h, qL, qE,
-                                                want_aov ? &ao : nullptr);
+        const bool more = path_step<kTex, kMis, kPhase>(sc, pp, vp, px, py, pp.sample_base + k, ps, h, qL, qE,
+                                                        want_aov ? &ao : nullptr);
         uint32_t extra = 0;
         if (qL.valid) {
             extra |= kFlagShL;
@@ -323,8 +323,11 @@ __global__ void __launch_bounds__(128, 8) k_shade(DScene sc, PathParams pp, View
     }
 }
 
-// The shading step for the scene's features: bindless textures, emitter MIS.
-template <bool kPool>
+// The shading step for the scene's features (bindless textures, emitter MIS)
+// and its queue (phase 1: every path at its camera ray, the first step of a
+// per-view wave; 2: every path in a chain, its later steps; 0: mixed, the
+// pool).
+template <bool kPool, int kPhase>
 void launch_shade(const DScene& sc, const PathParams& pp, const ViewParams& vp, uint32_t w0, uint32_t npix, const Soa& s,
                   int cur, float* aov, uint32_t aov_k, const LaunchBlock* lb, cudaStream_t st);
 
@@ -945,7 +948,7 @@ void init_launch_shapes() {
     g_blocks_extend[0] = std::max(1, b) * g_num_sms;
     cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, k_extend<false, 2, false>, 128, 0);
     g_blocks_extend[1] = std::max(1, b) * g_num_sms;
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, k_shade<false, false, false>, 128, 0);
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, k_shade<false, false, false, 2>, 128, 0);
     g_blocks_shade = std::max(1, b) * g_num_sms;
     cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, k_shadow<false, 1, false>, 128, 0);
     g_blocks_shadow[0] = std::max(1, b) * g_num_sms;
@@ -972,16 +975,16 @@ void init_launch_shapes() {
     g_blocks_refill = std::max(1, b) * g_num_sms;
 }
 
-template <bool kPool>
+template <bool kPool, int kPhase>
 void launch_shade(const DScene& sc, const PathParams& pp, const ViewParams& vp, uint32_t w0, uint32_t npix, const Soa& s,
                   int cur, float* aov, uint32_t aov_k, const LaunchBlock* lb, cudaStream_t st) {
     const dim3 g(g_blocks_shade), b(128);
     if (sc.emitter_mis) {
-        if (sc.ntex) k_shade<kPool, true, true><<<g, b, 0, st>>>(sc, pp, vp, w0, npix, s, cur, aov, aov_k, lb);
-        else k_shade<kPool, false, true><<<g, b, 0, st>>>(sc, pp, vp, w0, npix, s, cur, aov, aov_k, lb);
+        if (sc.ntex) k_shade<kPool, true, true, kPhase><<<g, b, 0, st>>>(sc, pp, vp, w0, npix, s, cur, aov, aov_k, lb);
+        else k_shade<kPool, false, true, kPhase><<<g, b, 0, st>>>(sc, pp, vp, w0, npix, s, cur, aov, aov_k, lb);
     } else {
-        if (sc.ntex) k_shade<kPool, true, false><<<g, b, 0, st>>>(sc, pp, vp, w0, npix, s, cur, aov, aov_k, lb);
-        else k_shade<kPool, false, false><<<g, b, 0, st>>>(sc, pp, vp, w0, npix, s, cur, aov, aov_k, lb);
+        if (sc.ntex) k_shade<kPool, true, false, kPhase><<<g, b, 0, st>>>(sc, pp, vp, w0, npix, s, cur, aov, aov_k, lb);
+        else k_shade<kPool, false, false, kPhase><<<g, b, 0, st>>>(sc, pp, vp, w0, npix, s, cur, aov, aov_k, lb);
     }
 }
 
@@ -1164,7 +1167,12 @@ ohao_status wavefront_render(const DScene& sc, const RenderView& view, const Pat
             cudaMemsetAsync(s.counts + (cur ^ 1), 0, 4, st);
             cudaMemsetAsync(s.counts + 2, 0, 4, st);
             tm.begin(1, a);
-            launch_shade<false>(sc, pp, view.vp, static_cast<uint32_t>(w0), npix, s, cur, view.aov, spp - 1, nullptr, st);
+            if (it == 0)   // the wave's camera rays: every path at its first step
+                launch_shade<false, 1>(sc, pp, view.vp, static_cast<uint32_t>(w0), npix, s, cur, view.aov, spp - 1,
+                                       nullptr, st);
+            else
+                launch_shade<false, 2>(sc, pp, view.vp, static_cast<uint32_t>(w0), npix, s, cur, view.aov, spp - 1,
+                                       nullptr, st);
             tm.end(1, a);
             tm.begin(2, a);
             if (fetch) launch_shadow_fetch(sc, s, static_cast<int>(pp.refill), d_err, profile ? dstats : nullptr, st);
@@ -1366,7 +1374,7 @@ void enqueue_chunk(const DScene& sc, const PathParams& pp, const LaunchBlock* lb
         if (pp.flags & kFlagSortMaterial) bin_queue<0>(sc, s, cur, cap, st);
         cudaMemsetAsync(s.counts + (cur ^ 1), 0, 4, st);
         cudaMemsetAsync(s.counts + 2, 0, 8, st);   // shadow and done counts
-        launch_shade<true>(sc, pp, ViewParams{}, 0u, 1u, s, cur, nullptr, 0u, lb, st);
+        launch_shade<true, 0>(sc, pp, ViewParams{}, 0u, 1u, s, cur, nullptr, 0u, lb, st);
         if (fetch) {
             launch_shadow_fetch(sc, s, pv.refill, d_err, nullptr, st);
         } else {
