@@ -117,12 +117,16 @@ struct ohao_pt_ctx {
     // ohao_pt_render_host: history uploads run on their own stream, so that
     // they overlap the render up to its first read of the accumulator
     cudaStream_t upload_stream = nullptr;
+    // per-view wavefront: the stream each step's shadow rays run on, beside
+    // the next step's closest-hit rays (created on first use)
+    cudaStream_t shadow_stream = nullptr;
     std::vector<cudaEvent_t> upload_after, upload_done;   // per view: stream order in, upload landed
     ~ohao_pt_ctx() {
         if (persistent) ohao::persistent_destroy(persistent);
         for (cudaEvent_t e : upload_after) cudaEventDestroy(e);
         for (cudaEvent_t e : upload_done) cudaEventDestroy(e);
         if (upload_stream) cudaStreamDestroy(upload_stream);
+        if (shadow_stream) cudaStreamDestroy(shadow_stream);
         for (auto* b : host_accum_bufs) delete b;
         for (auto* b : host_display_bufs) delete b;
         for (auto* b : host_target_bufs) delete b;
@@ -1002,10 +1006,12 @@ static ohao_status render_views(ohao_pt_ctx* ctx, const ohao_pt_view* views, uin
     } else {
         const uint32_t cap = ohao::wavefront_default_capacity();
         CK(ctx->scratch.ensure(ohao::wavefront_scratch_bytes(cap)), "render scratch");
+        if (!ctx->shadow_stream) CK(cudaStreamCreateWithFlags(&ctx->shadow_stream, cudaStreamNonBlocking), "shadow stream");
         for (uint32_t v = 0; v < n_views; ++v) {
             std::string err;
             const ohao_status s = ohao::wavefront_render(sc, rvs[v], pp, st->spp, ctx->scratch.p, ctx->scratch.n, cap,
-                                                         cs, profile, &acc, ctx->err_flag.as<int>(), err);
+                                                         cs, profile, &acc, ctx->err_flag.as<int>(), err,
+                                                         ctx->shadow_stream);
             if (s != OHAO_OK) return fail(ctx, s, err);
         }
     }

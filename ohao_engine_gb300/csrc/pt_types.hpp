@@ -118,9 +118,11 @@ cudaError_t launch_display(const float* accum, uint32_t npix, uint8_t* rgba8, cu
 // wavefront.cu
 size_t wavefront_scratch_bytes(uint32_t capacity);
 uint32_t wavefront_default_capacity();
+// aux (optional): a second stream on which each step's shadow rays run beside
+// the next step's closest-hit rays
 ohao_status wavefront_render(const DScene& sc, const RenderView& view, const PathParams& pp, uint32_t spp,
                              void* scratch, size_t scratch_bytes, uint32_t capacity, cudaStream_t st, bool profile,
-                             ProfileAcc* prof, int* d_err, std::string& err);
+                             ProfileAcc* prof, int* d_err, std::string& err, cudaStream_t aux = nullptr);
 ohao_status trace_rays(const DScene& sc, const float* rays, uint32_t n, uint32_t* hits, int any_hit, uint32_t* stats,
                        cudaStream_t st, int* d_err, std::string& err);
 

@@ -1121,7 +1121,7 @@ uint32_t wavefront_default_capacity() { return 1u << 21; }
 
 ohao_status wavefront_render(const DScene& sc, const RenderView& view, const PathParams& pp, uint32_t spp,
                              void* scratch, size_t scratch_bytes, uint32_t capacity, cudaStream_t st, bool profile,
-                             ProfileAcc* prof, int* d_err, std::string& err) {
+                             ProfileAcc* prof, int* d_err, std::string& err, cudaStream_t aux) {
     init_launch_shapes();
     if (scratch_bytes < wavefront_scratch_bytes(capacity)) {
         err = "wavefront scratch too small";
@@ -1140,6 +1140,20 @@ ohao_status wavefront_render(const DScene& sc, const RenderView& view, const Pat
         cudaEventCreate(&t_all1);
         cudaEventRecord(t_all0, st);
     }
+    // Shadow rays of step k and closest-hit rays of step k + 1 are
+    // independent (different path fields, different queues and fetch
+    // counters), so with an auxiliary stream the shadow kernel runs beside
+    // the next extend and is joined before the next binning and shading: the
+    // small queues of a frame's last steps then share the GPU instead of
+    // running one after the other. Profiled renders stay serial (their
+    // per-kernel timers are on one stream).
+    const bool overlap = aux != nullptr && !profile;
+    cudaEvent_t ev_shaded = nullptr, ev_shadowed = nullptr;
+    if (overlap) {
+        cudaEventCreateWithFlags(&ev_shaded, cudaEventDisableTiming);
+        cudaEventCreateWithFlags(&ev_shadowed, cudaEventDisableTiming);
+    }
+    cudaStream_t sh_st = overlap ? aux : st;
     for (uint64_t w0 = 0; w0 < total; w0 += capacity) {
         const uint32_t n = static_cast<uint32_t>(std::min<uint64_t>(capacity, total - w0));
         cudaEvent_t a;
@@ -1154,11 +1168,12 @@ ohao_status wavefront_render(const DScene& sc, const RenderView& view, const Pat
                 bin_queue<1>(sc, s, cur, capacity, st);
                 tm.end(3, a, kBinLaunches);
             }
-            if (fetch) cudaMemsetAsync(s.counts + kCtrExtendFetch, 0, 8, st);   // both fetch counters
+            if (fetch) cudaMemsetAsync(s.counts + kCtrExtendFetch, 0, 4, st);
             tm.begin(0, a);
             if (fetch) launch_extend_fetch(sc, s, cur, static_cast<int>(pp.refill), d_err, profile ? dstats : nullptr, st);
             else launch_extend(sc, s, cur, d_err, profile ? dstats : nullptr, st);
             tm.end(0, a);
+            if (overlap && it > 0) cudaStreamWaitEvent(st, ev_shadowed, 0);   // step it - 1's shadow rays done
             if (pp.flags & kFlagSortMaterial) {
                 tm.begin(3, a);
                 bin_queue<0>(sc, s, cur, capacity, st);
@@ -1174,17 +1189,28 @@ ohao_status wavefront_render(const DScene& sc, const RenderView& view, const Pat
                 launch_shade<false, 2>(sc, pp, view.vp, static_cast<uint32_t>(w0), npix, s, cur, view.aov, spp - 1,
                                        nullptr, st);
             tm.end(1, a);
+            if (overlap) {
+                cudaEventRecord(ev_shaded, st);
+                cudaStreamWaitEvent(sh_st, ev_shaded, 0);
+            }
             tm.begin(2, a);
-            if (fetch) launch_shadow_fetch(sc, s, static_cast<int>(pp.refill), d_err, profile ? dstats : nullptr, st);
-            else launch_shadow(sc, s, d_err, profile ? dstats : nullptr, st);
+            if (fetch) cudaMemsetAsync(s.counts + kCtrShadowFetch, 0, 4, sh_st);
+            if (fetch) launch_shadow_fetch(sc, s, static_cast<int>(pp.refill), d_err, profile ? dstats : nullptr, sh_st);
+            else launch_shadow(sc, s, d_err, profile ? dstats : nullptr, sh_st);
             tm.end(2, a);
+            if (overlap) cudaEventRecord(ev_shadowed, sh_st);
             cur ^= 1;
         }
+        if (overlap) cudaStreamWaitEvent(st, ev_shadowed, 0);   // the wave's last shadow rays
         if (view.accum_ready) cudaStreamWaitEvent(st, view.accum_ready, 0);   // the history upload has landed
         tm.begin(3, a);
         k_finalize<<<std::max(1u, std::min(4096u, (npix + 255) / 256)), 256, 0, st>>>(
             pp, static_cast<uint32_t>(w0), n, view.vp.width, view.vp.height, s, view.accum, view.history, view.path_out);
         tm.end(3, a);
+    }
+    if (overlap) {   // released once their pending records complete
+        cudaEventDestroy(ev_shaded);
+        cudaEventDestroy(ev_shadowed);
     }
     const cudaError_t e = cudaGetLastError();
     if (e != cudaSuccess) {
