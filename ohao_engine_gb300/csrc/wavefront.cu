@@ -80,7 +80,7 @@ struct LaunchBlock {
     uint32_t nviews;
     uint32_t total_pix;
     uint32_t spp;
-    uint32_t pad;
+    uint32_t max_chunks;      // bound on this render's chunks (a generous multiple of the work's own bound)
     float box_lo[4];          // scene bounds for the ray-reordering key
     float box_scale[4];       // 128 / extent per axis
     PView views[kMaxViews];
@@ -521,14 +521,14 @@ __global__ void k_pool_init(Soa s, uint32_t cap) {
 
 // End of one pool chunk inside the render's CUDA graph: the graph's while
 // loop runs another chunk until the work queue is drained (no path in
-// flight, nothing left to claim), and gives up after kMaxChunks chunks with
+// flight, nothing left to claim), and gives up after the render's chunk bound with
 // the queue-timeout error bit. No host round trip between chunks.
 __global__ void k_pool_continue(cudaGraphConditionalHandle loop, const LaunchBlock* lb, Soa s, int* err) {
     const uint32_t pending = s.counts[0], done = s.counts[3], claimed = s.counts[4];
     const bool drained = pending == 0 && done == 0 && claimed >= lb->total_pix;
     const uint32_t chunks = ++s.counts[kCtrChunks];
     bool more = !drained;
-    if (more && chunks >= kMaxChunks) {
+    if (more && chunks >= lb->max_chunks) {
         atomicOr(err, kErrQueueTimeout);
         more = false;
     }
@@ -1284,6 +1284,9 @@ constexpr int kDefaultPool = 1;
 }  // namespace
 
 struct PersistentState {
+    // a chunk's shadow rays run on aux beside the next step's closest-hit rays
+    cudaStream_t aux = nullptr;
+    cudaEvent_t ev_shaded = nullptr, ev_shadowed = nullptr;
     LaunchBlock* d_lb = nullptr;
     LaunchBlock* h_lb = nullptr;                // pinned staging
     uint32_t* h_counts = nullptr;               // pinned readback
@@ -1303,7 +1306,10 @@ PersistentState* persistent_create() {
     auto* s = new PersistentState();
     if (cudaMalloc(&s->d_lb, sizeof(LaunchBlock)) != cudaSuccess ||
         cudaMallocHost(&s->h_lb, sizeof(LaunchBlock)) != cudaSuccess ||
-        cudaMallocHost(&s->h_counts, 64) != cudaSuccess) {
+        cudaMallocHost(&s->h_counts, 64) != cudaSuccess ||
+        cudaStreamCreateWithFlags(&s->aux, cudaStreamNonBlocking) != cudaSuccess ||
+        cudaEventCreateWithFlags(&s->ev_shaded, cudaEventDisableTiming) != cudaSuccess ||
+        cudaEventCreateWithFlags(&s->ev_shadowed, cudaEventDisableTiming) != cudaSuccess) {
         persistent_destroy(s);
         return nullptr;
     }
@@ -1317,6 +1323,9 @@ void persistent_destroy(PersistentState* s) {
     if (s->d_lb) cudaFree(s->d_lb);
     if (s->h_lb) cudaFreeHost(s->h_lb);
     if (s->h_counts) cudaFreeHost(s->h_counts);
+    if (s->ev_shaded) cudaEventDestroy(s->ev_shaded);
+    if (s->ev_shadowed) cudaEventDestroy(s->ev_shadowed);
+    if (s->aux) cudaStreamDestroy(s->aux);
     delete s;
 }
 
@@ -1340,8 +1349,8 @@ bool persistent_select(PersistentState* s, const char* name) {
 
 namespace {
 
-ohao_status stage_views(PersistentState* s, const RenderView* views, uint32_t n, uint32_t spp, const float* box,
-                        cudaStream_t st, std::string& err) {
+ohao_status stage_views(PersistentState* s, const RenderView* views, uint32_t n, uint32_t spp, uint32_t max_bounces,
+                        const float* box, cudaStream_t st, std::string& err) {
     if (n == 0 || n > kMaxViews) {
         err = "persistent render: view count outside [1, 1024]";
         return OHAO_ERR_INVALID_ARG;
@@ -1372,6 +1381,16 @@ ohao_status stage_views(PersistentState* s, const RenderView* views, uint32_t n,
         return OHAO_ERR_INVALID_ARG;
     }
     lb.total_pix = static_cast<uint32_t>(off);
+    // While the work queue is not exhausted every slot of the smallest pool
+    // (2^20) advances one step per iteration, and a path takes at most
+    // 1 + 2 max_bounces steps plus its regeneration: a bound on the
+    // iterations, then on the chunks, taken four times over.
+    {
+        const uint64_t steps = 2ull + 2ull * max_bounces + 1ull;
+        const uint64_t iters = (off * spp * steps + (1ull << 20) - 1) / (1ull << 20) + steps + 2;
+        const uint64_t chunks = 4 * ((iters + kChunk - 1) / kChunk + 2);
+        lb.max_chunks = static_cast<uint32_t>(std::min<uint64_t>(chunks, kMaxChunks));
+    }
     const size_t bytes = offsetof(LaunchBlock, views) + sizeof(PView) * n;
     if (cudaMemcpyAsync(s->d_lb, s->h_lb, bytes, cudaMemcpyHostToDevice, st) != cudaSuccess) {
         err = "persistent render: view table upload failed";
@@ -1380,9 +1399,42 @@ ohao_status stage_views(PersistentState* s, const RenderView* views, uint32_t n,
     return OHAO_OK;
 }
 
+constexpr int kCtrNewBegin = 8;   // Soa::counts: queue index of the first camera ray regenerated this step
+
+// One chunk of pool steps. With persistent-warp traversal and no ray
+// reordering, and an auxiliary stream, each step's shadow rays run on aux
+// beside the next step's closest-hit rays of the paths that continue; after
+// the join, regeneration appends new camera rays to the queue and a second
+// extend claims just those (its fetch counter starts at their first index),
+// so a regenerated path still traces in the step it was started. Otherwise
+// the steps run serially: regeneration, extend, shading, shadow rays.
 void enqueue_chunk(const DScene& sc, const PathParams& pp, const LaunchBlock* lb, const Soa& s, uint32_t cap,
-                   const PoolVariant& pv, int* d_err, cudaStream_t st) {
+                   const PoolVariant& pv, int* d_err, cudaStream_t st, cudaStream_t aux, cudaEvent_t ev_shaded,
+                   cudaEvent_t ev_shadowed) {
     const bool fetch = pv.refill > 0 && sc.nnodes > 0;
+    if (aux && fetch && !pv.reorder) {
+        for (int it = 0; it < kChunk; ++it) {
+            const int cur = it & 1;
+            cudaMemsetAsync(s.counts + kCtrExtendFetch, 0, 4, st);
+            launch_extend_fetch(sc, s, cur, pv.refill, d_err, nullptr, st);    // continuing rays
+            if (it > 0) cudaStreamWaitEvent(st, ev_shadowed, 0);                // the last step's shadow rays
+            cudaMemcpyAsync(s.counts + kCtrNewBegin, s.counts + cur, 4, cudaMemcpyDeviceToDevice, st);
+            k_regen<<<g_blocks_shade, 128, 0, st>>>(pp, lb, s, cur);
+            cudaMemcpyAsync(s.counts + kCtrExtendFetch, s.counts + kCtrNewBegin, 4, cudaMemcpyDeviceToDevice, st);
+            launch_extend_fetch(sc, s, cur, pv.refill, d_err, nullptr, st);    // the new camera rays
+            if (pp.flags & kFlagSortMaterial) bin_queue<0>(sc, s, cur, cap, st);
+            cudaMemsetAsync(s.counts + (cur ^ 1), 0, 4, st);
+            cudaMemsetAsync(s.counts + 2, 0, 8, st);   // shadow and done counts
+            launch_shade<true, 0>(sc, pp, ViewParams{}, 0u, 1u, s, cur, nullptr, 0u, lb, st);
+            cudaEventRecord(ev_shaded, st);
+            cudaStreamWaitEvent(aux, ev_shaded, 0);
+            cudaMemsetAsync(s.counts + kCtrShadowFetch, 0, 4, aux);
+            launch_shadow_fetch(sc, s, pv.refill, d_err, nullptr, aux);
+            cudaEventRecord(ev_shadowed, aux);
+        }
+        cudaStreamWaitEvent(st, ev_shadowed, 0);   // the chunk ends with its shadow rays done
+        return;
+    }
     for (int it = 0; it < kChunk; ++it) {
         const int cur = it & 1;
         k_regen<<<g_blocks_shade, 128, 0, st>>>(pp, lb, s, cur);
@@ -1456,7 +1508,8 @@ ohao_status run_pool(PersistentState* s, int variant, const DScene& sc, const Pa
                 cudaGraph_t body = cp.conditional.phGraph_out[0];
                 e = cudaStreamBeginCaptureToGraph(cap_st, body, nullptr, nullptr, 0, cudaStreamCaptureModeThreadLocal);
                 if (e == cudaSuccess) {
-                    enqueue_chunk(sc, pp, s->d_lb, soa, cap, kPool[variant], d_err, cap_st);
+                    enqueue_chunk(sc, pp, s->d_lb, soa, cap, kPool[variant], d_err, cap_st, s->aux, s->ev_shaded,
+                                  s->ev_shadowed);
                     k_pool_continue<<<1, 1, 0, cap_st>>>(loop, s->d_lb, soa, d_err);
                     cudaGraph_t captured = nullptr;
                     e = cudaStreamEndCapture(cap_st, &captured);
@@ -1471,7 +1524,8 @@ ohao_status run_pool(PersistentState* s, int variant, const DScene& sc, const Pa
                 s->graph = nullptr;
                 if (g) { cudaGraphDestroy(g); g = nullptr; }
                 cudaStreamBeginCapture(cap_st, cudaStreamCaptureModeThreadLocal);
-                enqueue_chunk(sc, pp, s->d_lb, soa, cap, kPool[variant], d_err, cap_st);
+                enqueue_chunk(sc, pp, s->d_lb, soa, cap, kPool[variant], d_err, cap_st, s->aux, s->ev_shaded,
+                              s->ev_shadowed);
                 e = cudaStreamEndCapture(cap_st, &g);
                 if (e == cudaSuccess) e = cudaGraphInstantiate(&s->graph, g, 0);
             }
@@ -1494,7 +1548,7 @@ ohao_status run_pool(PersistentState* s, int variant, const DScene& sc, const Pa
         }
     }
     for (uint64_t chunk = 0;; ++chunk) {
-        if (chunk >= kMaxChunks) {
+        if (chunk >= s->h_lb->max_chunks) {
             err = "persistent render: work queue did not drain within the iteration bound";
             return OHAO_ERR_TIMEOUT;
         }
@@ -1502,7 +1556,7 @@ ohao_status run_pool(PersistentState* s, int variant, const DScene& sc, const Pa
             const cudaError_t e = cudaGraphLaunch(s->graph, st);
             if (e != cudaSuccess) { err = std::string("persistent graph launch: ") + cudaGetErrorString(e); return OHAO_ERR_CUDA; }
         } else {
-            enqueue_chunk(sc, pp, s->d_lb, soa, cap, kPool[variant], d_err, st);
+            enqueue_chunk(sc, pp, s->d_lb, soa, cap, kPool[variant], d_err, st, s->aux, s->ev_shaded, s->ev_shadowed);
         }
         cudaMemcpyAsync(s->h_counts, soa.counts, 5 * sizeof(uint32_t), cudaMemcpyDeviceToHost, st);
         const cudaError_t e = cudaStreamSynchronize(st);
@@ -1518,7 +1572,7 @@ ohao_status run_pool(PersistentState* s, int variant, const DScene& sc, const Pa
 ohao_status persistent_render(PersistentState* s, const DScene& sc, const RenderView* views, uint32_t n,
                               const PathParams& pp, uint32_t spp, const float* scene_box, cudaStream_t st, int* d_err,
                               bool profile, ProfileAcc* prof, std::string& err) {
-    ohao_status r = stage_views(s, views, n, spp, scene_box, st, err);
+    ohao_status r = stage_views(s, views, n, spp, pp.max_bounces, scene_box, st, err);
     if (r != OHAO_OK) return r;
     cudaEvent_t e0 = nullptr, e1 = nullptr;
     if (profile) {
@@ -1544,7 +1598,7 @@ ohao_status persistent_render(PersistentState* s, const DScene& sc, const Render
 ohao_status persistent_autotune(PersistentState* s, const DScene& sc, const RenderView* views, uint32_t n,
                                 const PathParams& pp, uint32_t spp, const float* scene_box, cudaStream_t st, int* d_err,
                                 float* best_ms, std::string& err) {
-    ohao_status r = stage_views(s, views, n, spp, scene_box, st, err);
+    ohao_status r = stage_views(s, views, n, spp, pp.max_bounces, scene_box, st, err);
     if (r != OHAO_OK) return r;
     float best = 1e30f;
     int bi = kDefaultPool;
