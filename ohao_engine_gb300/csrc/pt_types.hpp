@@ -91,6 +91,8 @@ struct ViewParams {
     float inv_view[16];
     float inv_proj[16];
     uint32_t width, height;
+    uint32_t pix_base;   // per-view wavefront: first pixel rank of the range a wave lane renders (0: the view)
+    uint32_t pad;
 };
 
 struct RenderView {
@@ -118,11 +120,17 @@ cudaError_t launch_display(const float* accum, uint32_t npix, uint8_t* rgba8, cu
 // wavefront.cu
 size_t wavefront_scratch_bytes(uint32_t capacity);
 uint32_t wavefront_default_capacity();
-// aux (optional): a second stream on which each step's shadow rays run beside
-// the next step's closest-hit rays
+// Streams of the per-view wavefront besides the caller's: aux0 runs each
+// step's shadow rays beside the next step's closest-hit rays; main1 / aux1
+// render the second half of the view's pixels beside the first (two lanes,
+// each with half of the scratch). Null members: that part runs serially.
+struct WaveStreams {
+    cudaStream_t aux0, main1, aux1;
+};
+size_t wavefront_lanes_scratch_bytes(uint32_t capacity);   // two lanes of capacity / 2 paths
 ohao_status wavefront_render(const DScene& sc, const RenderView& view, const PathParams& pp, uint32_t spp,
                              void* scratch, size_t scratch_bytes, uint32_t capacity, cudaStream_t st, bool profile,
-                             ProfileAcc* prof, int* d_err, std::string& err, cudaStream_t aux = nullptr);
+                             ProfileAcc* prof, int* d_err, std::string& err, const WaveStreams* ws = nullptr);
 ohao_status trace_rays(const DScene& sc, const float* rays, uint32_t n, uint32_t* hits, int any_hit, uint32_t* stats,
                        cudaStream_t st, int* d_err, std::string& err);
 

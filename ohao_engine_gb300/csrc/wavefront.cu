@@ -194,7 +194,7 @@ __global__ void k_generate(ViewParams vp, PathParams pp, uint32_t w0, uint32_t n
     if (i == 0) s.counts[0] = n;
     if (i >= n) return;
     const uint32_t lin = w0 + i;
-    const uint32_t k = lin / npix, p = lin - k * npix;
+    const uint32_t k = lin / npix, p = vp.pix_base + (lin - k * npix);   // npix: the lane's pixels
     uint32_t px, py;
     rank_pixel(p, vp.width, vp.height, px, py);
     PathState ps;
@@ -273,7 +273,7 @@ __global__ void __launch_bounds__(128, 8) k_shade(DScene sc, PathParams pp, View
         } else {
             const uint32_t lin = w0 + p;
             k = lin / npix_plain;
-            pix = lin - k * npix_plain;
+            pix = vp_plain.pix_base + (lin - k * npix_plain);
             vpp = &vp_plain;
             aov = aov_plain;
         }
@@ -822,22 +822,24 @@ __global__ void __launch_bounds__(128) k_shadow_fetch(DScene sc, Soa s, int refi
 }
 
 // p: the pixel's work rank (slots are rank-major); outputs at its index.
-__global__ void k_finalize(PathParams pp, uint32_t w0, uint32_t n, uint32_t width, uint32_t height, Soa s,
+// One wave of a lane: npix = the lane's pixel count, ranks from vp.pix_base.
+__global__ void k_finalize(PathParams pp, uint32_t w0, uint32_t n, ViewParams vp, uint32_t npix, Soa s,
                            float* accum, uint32_t history, float* path_out) {
-    const uint32_t npix = width * height;
+    const uint32_t width = vp.width, height = vp.height;
+    const uint32_t view_npix = width * height;
     for (uint32_t p = blockIdx.x * blockDim.x + threadIdx.x; p < npix; p += gridDim.x * blockDim.x) {
         const uint64_t lo = w0, hi = static_cast<uint64_t>(w0) + n;   // [lo, hi)
         uint64_t k0 = (lo > p) ? (lo - p + npix - 1) / npix : 0;
         if (k0 * npix + p >= hi) continue;
         const uint64_t k1 = (hi - 1 - p) / npix;
         uint32_t px, py;
-        rank_pixel(p, width, height, px, py);
+        rank_pixel(vp.pix_base + p, width, height, px, py);
         const uint32_t pidx = py * width + px;
         float4 acc = reinterpret_cast<float4*>(accum)[pidx];
         for (uint64_t k = k0; k <= k1; ++k) {
             const uint32_t slot = static_cast<uint32_t>(k * npix + p - lo);
             const V3 L = firefly(pp, ld3(s.tr[2 * slot + 1]));
-            if (path_out) reinterpret_cast<float4*>(path_out)[k * npix + pidx] = f4(L, 0.0f);
+            if (path_out) reinterpret_cast<float4*>(path_out)[k * view_npix + pidx] = f4(L, 0.0f);
             if (history + k == 0) {
                 acc = make_float4(L.x, L.y, L.z, 1.0f);
             } else {
@@ -1119,18 +1121,39 @@ size_t wavefront_scratch_bytes(uint32_t cap) {
 
 uint32_t wavefront_default_capacity() { return 1u << 21; }
 
+size_t wavefront_lanes_scratch_bytes(uint32_t capacity) {
+    Carve c{nullptr};
+    carve_soa_at(c, capacity / 2);
+    carve_soa_at(c, capacity / 2);
+    return c.off;
+}
+
 ohao_status wavefront_render(const DScene& sc, const RenderView& view, const PathParams& pp, uint32_t spp,
                              void* scratch, size_t scratch_bytes, uint32_t capacity, cudaStream_t st, bool profile,
-                             ProfileAcc* prof, int* d_err, std::string& err, cudaStream_t aux) {
+                             ProfileAcc* prof, int* d_err, std::string& err, const WaveStreams* ws) {
     init_launch_shapes();
-    if (scratch_bytes < wavefront_scratch_bytes(capacity)) {
+    const uint32_t npix = view.vp.width * view.vp.height;
+    // Two lanes (a view of >= 64 pixels, not profiled): the pixel ranks are
+    // split at a multiple of 32 (whole 8x4 tiles) and each half renders all
+    // its samples on its own stream with half of the scratch, beside the
+    // other; the halves share no pixel, so each pixel's samples still fold
+    // in order within one lane.
+    const int nl = (ws && ws->main1 && !profile && npix >= 64) ? 2 : 1;
+    const uint32_t wcap = nl == 2 ? capacity / 2 : capacity;
+    if (scratch_bytes < (nl == 2 ? wavefront_lanes_scratch_bytes(capacity) : wavefront_scratch_bytes(capacity))) {
         err = "wavefront scratch too small";
         return OHAO_ERR_INVALID_ARG;
     }
-    const uint32_t npix = view.vp.width * view.vp.height;
-    const uint64_t total = static_cast<uint64_t>(npix) * spp;
-    Soa s = carve_soa(scratch, capacity);
-    unsigned long long* dstats = reinterpret_cast<unsigned long long*>(s.counts + 16);
+    Soa lane_soa[2];
+    {
+        Carve c{static_cast<char*>(scratch)};
+        lane_soa[0] = carve_soa_at(c, wcap);
+        if (nl == 2) lane_soa[1] = carve_soa_at(c, wcap);
+    }
+    const uint32_t half = (npix / 2) & ~31u;
+    const uint32_t pix_base[2] = {0u, nl == 2 ? half : 0u};
+    const uint32_t pix_count[2] = {nl == 2 ? half : npix, npix - half};
+    unsigned long long* dstats = reinterpret_cast<unsigned long long*>(lane_soa[0].counts + 16);
     if (profile) cudaMemsetAsync(dstats, 0, 8 * sizeof(unsigned long long), st);
     const uint32_t niters = 1 + 2 * pp.max_bounces;
     EvTimer tm{profile, st, {}};
@@ -1147,71 +1170,101 @@ ohao_status wavefront_render(const DScene& sc, const RenderView& view, const Pat
     // small queues of a frame's last steps then share the GPU instead of
     // running one after the other. Profiled renders stay serial (their
     // per-kernel timers are on one stream).
-    const bool overlap = aux != nullptr && !profile;
-    cudaEvent_t ev_shaded = nullptr, ev_shadowed = nullptr;
-    if (overlap) {
-        cudaEventCreateWithFlags(&ev_shaded, cudaEventDisableTiming);
-        cudaEventCreateWithFlags(&ev_shadowed, cudaEventDisableTiming);
+    cudaStream_t main_st[2] = {st, nl == 2 ? ws->main1 : st};
+    cudaStream_t sh_st[2] = {st, st};
+    bool overlap[2] = {false, false};
+    cudaEvent_t ev_shaded[2] = {nullptr, nullptr}, ev_shadowed[2] = {nullptr, nullptr}, ev_fork = nullptr,
+                ev_join = nullptr;
+    for (int l = 0; l < nl; ++l) {
+        const cudaStream_t aux = ws ? (l == 0 ? ws->aux0 : ws->aux1) : nullptr;
+        overlap[l] = aux != nullptr && !profile;
+        if (overlap[l]) {
+            sh_st[l] = aux;
+            cudaEventCreateWithFlags(&ev_shaded[l], cudaEventDisableTiming);
+            cudaEventCreateWithFlags(&ev_shadowed[l], cudaEventDisableTiming);
+        } else {
+            sh_st[l] = main_st[l];
+        }
     }
-    cudaStream_t sh_st = overlap ? aux : st;
-    for (uint64_t w0 = 0; w0 < total; w0 += capacity) {
-        const uint32_t n = static_cast<uint32_t>(std::min<uint64_t>(capacity, total - w0));
+    if (nl == 2) {   // the second lane starts after the caller's work on st
+        cudaEventCreateWithFlags(&ev_fork, cudaEventDisableTiming);
+        cudaEventCreateWithFlags(&ev_join, cudaEventDisableTiming);
+        cudaEventRecord(ev_fork, st);
+        cudaStreamWaitEvent(main_st[1], ev_fork, 0);
+    }
+    const bool fetch = pp.refill > 0 && sc.nnodes > 0;
+    // one wave of lane l: paths [w0, w0 + n) of the lane's (sample, pixel) space
+    auto run_wave = [&](int l, uint64_t w0, uint32_t n) {
+        const Soa& s = lane_soa[l];
+        const cudaStream_t ms = main_st[l], ss = sh_st[l];
+        ViewParams vp = view.vp;
+        vp.pix_base = pix_base[l];
+        const uint32_t pn = pix_count[l];
         cudaEvent_t a;
         tm.begin(3, a);
-        k_generate<<<(n + 255) / 256, 256, 0, st>>>(view.vp, pp, static_cast<uint32_t>(w0), n, npix, s);
+        k_generate<<<(n + 255) / 256, 256, 0, ms>>>(vp, pp, static_cast<uint32_t>(w0), n, pn, s);
         tm.end(3, a);
         int cur = 0;
-        const bool fetch = pp.refill > 0 && sc.nnodes > 0;
         for (uint32_t it = 0; it < niters; ++it) {
             if (it > 0 && (pp.flags & kFlagSortRays)) {   // bounce rays grouped by direction and origin
                 tm.begin(3, a);
-                bin_queue<1>(sc, s, cur, capacity, st);
+                bin_queue<1>(sc, s, cur, wcap, ms);
                 tm.end(3, a, kBinLaunches);
             }
-            if (fetch) cudaMemsetAsync(s.counts + kCtrExtendFetch, 0, 4, st);
+            if (fetch) cudaMemsetAsync(s.counts + kCtrExtendFetch, 0, 4, ms);
             tm.begin(0, a);
-            if (fetch) launch_extend_fetch(sc, s, cur, static_cast<int>(pp.refill), d_err, profile ? dstats : nullptr, st);
-            else launch_extend(sc, s, cur, d_err, profile ? dstats : nullptr, st);
+            if (fetch) launch_extend_fetch(sc, s, cur, static_cast<int>(pp.refill), d_err, profile ? dstats : nullptr, ms);
+            else launch_extend(sc, s, cur, d_err, profile ? dstats : nullptr, ms);
             tm.end(0, a);
-            if (overlap && it > 0) cudaStreamWaitEvent(st, ev_shadowed, 0);   // step it - 1's shadow rays done
+            if (overlap[l] && it > 0) cudaStreamWaitEvent(ms, ev_shadowed[l], 0);   // step it - 1's shadow rays done
             if (pp.flags & kFlagSortMaterial) {
                 tm.begin(3, a);
-                bin_queue<0>(sc, s, cur, capacity, st);
+                bin_queue<0>(sc, s, cur, wcap, ms);
                 tm.end(3, a, kBinLaunches);
             }
-            cudaMemsetAsync(s.counts + (cur ^ 1), 0, 4, st);
-            cudaMemsetAsync(s.counts + 2, 0, 4, st);
+            cudaMemsetAsync(s.counts + (cur ^ 1), 0, 4, ms);
+            cudaMemsetAsync(s.counts + 2, 0, 4, ms);
             tm.begin(1, a);
             if (it == 0)   // the wave's camera rays: every path at its first step
-                launch_shade<false, 1>(sc, pp, view.vp, static_cast<uint32_t>(w0), npix, s, cur, view.aov, spp - 1,
-                                       nullptr, st);
+                launch_shade<false, 1>(sc, pp, vp, static_cast<uint32_t>(w0), pn, s, cur, view.aov, spp - 1, nullptr, ms);
             else
-                launch_shade<false, 2>(sc, pp, view.vp, static_cast<uint32_t>(w0), npix, s, cur, view.aov, spp - 1,
-                                       nullptr, st);
+                launch_shade<false, 2>(sc, pp, vp, static_cast<uint32_t>(w0), pn, s, cur, view.aov, spp - 1, nullptr, ms);
             tm.end(1, a);
-            if (overlap) {
-                cudaEventRecord(ev_shaded, st);
-                cudaStreamWaitEvent(sh_st, ev_shaded, 0);
+            if (overlap[l]) {
+                cudaEventRecord(ev_shaded[l], ms);
+                cudaStreamWaitEvent(ss, ev_shaded[l], 0);
             }
             tm.begin(2, a);
-            if (fetch) cudaMemsetAsync(s.counts + kCtrShadowFetch, 0, 4, sh_st);
-            if (fetch) launch_shadow_fetch(sc, s, static_cast<int>(pp.refill), d_err, profile ? dstats : nullptr, sh_st);
-            else launch_shadow(sc, s, d_err, profile ? dstats : nullptr, sh_st);
+            if (fetch) cudaMemsetAsync(s.counts + kCtrShadowFetch, 0, 4, ss);
+            if (fetch) launch_shadow_fetch(sc, s, static_cast<int>(pp.refill), d_err, profile ? dstats : nullptr, ss);
+            else launch_shadow(sc, s, d_err, profile ? dstats : nullptr, ss);
             tm.end(2, a);
-            if (overlap) cudaEventRecord(ev_shadowed, sh_st);
+            if (overlap[l]) cudaEventRecord(ev_shadowed[l], ss);
             cur ^= 1;
         }
-        if (overlap) cudaStreamWaitEvent(st, ev_shadowed, 0);   // the wave's last shadow rays
-        if (view.accum_ready) cudaStreamWaitEvent(st, view.accum_ready, 0);   // the history upload has landed
+        if (overlap[l]) cudaStreamWaitEvent(ms, ev_shadowed[l], 0);   // the wave's last shadow rays
+        if (view.accum_ready) cudaStreamWaitEvent(ms, view.accum_ready, 0);   // the history upload has landed
         tm.begin(3, a);
-        k_finalize<<<std::max(1u, std::min(4096u, (npix + 255) / 256)), 256, 0, st>>>(
-            pp, static_cast<uint32_t>(w0), n, view.vp.width, view.vp.height, s, view.accum, view.history, view.path_out);
+        k_finalize<<<std::max(1u, std::min(4096u, (pn + 255) / 256)), 256, 0, ms>>>(
+            pp, static_cast<uint32_t>(w0), n, vp, pn, s, view.accum, view.history, view.path_out);
         tm.end(3, a);
+    };
+    const uint64_t lane_total[2] = {static_cast<uint64_t>(pix_count[0]) * spp,
+                                    nl == 2 ? static_cast<uint64_t>(pix_count[1]) * spp : 0ull};
+    for (uint64_t w0 = 0; w0 < lane_total[0] || w0 < lane_total[1]; w0 += wcap)
+        for (int l = 0; l < nl; ++l)
+            if (w0 < lane_total[l])
+                run_wave(l, w0, static_cast<uint32_t>(std::min<uint64_t>(wcap, lane_total[l] - w0)));
+    if (nl == 2) {   // the caller's stream continues after both lanes
+        cudaEventRecord(ev_join, main_st[1]);
+        cudaStreamWaitEvent(st, ev_join, 0);
     }
-    if (overlap) {   // released once their pending records complete
-        cudaEventDestroy(ev_shaded);
-        cudaEventDestroy(ev_shadowed);
+    for (int l = 0; l < nl; ++l) {   // released once their pending records complete
+        if (ev_shaded[l]) cudaEventDestroy(ev_shaded[l]);
+        if (ev_shadowed[l]) cudaEventDestroy(ev_shadowed[l]);
     }
+    if (ev_fork) cudaEventDestroy(ev_fork);
+    if (ev_join) cudaEventDestroy(ev_join);
     const cudaError_t e = cudaGetLastError();
     if (e != cudaSuccess) {
         err = std::string("wavefront launch failed: ") + cudaGetErrorString(e);
