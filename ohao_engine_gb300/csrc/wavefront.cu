@@ -1133,12 +1133,15 @@ ohao_status wavefront_render(const DScene& sc, const RenderView& view, const Pat
                              ProfileAcc* prof, int* d_err, std::string& err, const WaveStreams* ws) {
     init_launch_shapes();
     const uint32_t npix = view.vp.width * view.vp.height;
-    // Two lanes (a view of >= 64 pixels, not profiled): the pixel ranks are
-    // split at a multiple of 32 (whole 8x4 tiles) and each half renders all
-    // its samples on its own stream with half of the scratch, beside the
-    // other; the halves share no pixel, so each pixel's samples still fold
-    // in order within one lane.
-    const int nl = (ws && ws->main1 && !profile && npix >= 64) ? 2 : 1;
+    // Two lanes (a view of >= 64 pixels, one ray per thread in traversal,
+    // not profiled): the pixel ranks are split at a multiple of 32 (whole 8x4
+    // tiles) and each half renders all its samples on its own stream with
+    // half of the scratch, beside the other; the halves share no pixel, so
+    // each pixel's samples still fold in order within one lane. Persistent-
+    // warp traversal keeps one lane: its grids fill the GPU by themselves,
+    // and two of them side by side measured 3% slower on the instanced scene.
+    const bool fetch = pp.refill > 0 && sc.nnodes > 0;
+    const int nl = (ws && ws->main1 && !profile && !fetch && npix >= 64) ? 2 : 1;
     const uint32_t wcap = nl == 2 ? capacity / 2 : capacity;
     if (scratch_bytes < (nl == 2 ? wavefront_lanes_scratch_bytes(capacity) : wavefront_scratch_bytes(capacity))) {
         err = "wavefront scratch too small";
@@ -1192,7 +1195,6 @@ ohao_status wavefront_render(const DScene& sc, const RenderView& view, const Pat
         cudaEventRecord(ev_fork, st);
         cudaStreamWaitEvent(main_st[1], ev_fork, 0);
     }
-    const bool fetch = pp.refill > 0 && sc.nnodes > 0;
     // one wave of lane l: paths [w0, w0 + n) of the lane's (sample, pixel) space
     auto run_wave = [&](int l, uint64_t w0, uint32_t n) {
         const Soa& s = lane_soa[l];
