@@ -621,10 +621,12 @@ def run_ours(args):
 
     # profiled pass: per-kernel CUDA events + traversal visit counters
     prof_ms = []
+    lanes = 1
     for k in range(args.steps):
         flush.zero_()
         step(args.warmup + args.steps + k, flags=og.FLAG_PROFILE)
         p = pt.profile()
+        lanes = max(lanes, int(p.lanes))
         prof_ms.append((p.extend_ms, p.extend_launches, p.nodes_closest, p.tris_closest, p.shadow_ms,
                         p.shadow_launches, p.nodes_shadow, p.tris_shadow, p.shade_ms, p.other_ms, p.total_ms,
                         p.shade_launches, p.other_launches, p.rays_closest, p.rays_shadow))
@@ -634,7 +636,8 @@ def run_ours(args):
     ext_bytes = sum(80 * x[2] + 48 * x[3] for x in prof_ms)
     sh_ms = sum(x[4] for x in prof_ms)
     sh_bytes = sum(80 * x[6] + 48 * x[7] for x in prof_ms)
-    launches_per_step = (sum(x[1] + x[5] + x[11] + x[12] for x in prof_ms)) / len(prof_ms)
+    # the timed steps run `lanes` pixel lanes, each with the profiled pass's kernel sequence
+    launches_per_step = lanes * (sum(x[1] + x[5] + x[11] + x[12] for x in prof_ms)) / len(prof_ms)
     rays_c = sum(x[13] for x in prof_ms)
     rays_s = sum(x[14] for x in prof_ms)
     peak, peak_kind = peaks()
@@ -688,6 +691,7 @@ def run_ours(args):
                 "config": {"workload": desc, "l2": "flushed between timed steps (256 MB write)",
                            "path": "plain wavefront", "parallelism": f"replicas x{world}",
                            "shade_order": args.shade_order,
+                           "pixel_lanes": lanes, "shadow_rays": "beside the next step's closest-hit rays (second stream)",
                            "bvh_build_s": build_s, "scene_upload_s": upload_s,
                            "rays_per_step": {"closest": rays_c / len(prof_ms), "shadow": rays_s / len(prof_ms)}},
                 "clocks": clocks, "e2e": e2e, "gpu_launches": int(round(launches_per_step * args.steps)),

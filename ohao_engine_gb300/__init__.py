@@ -89,7 +89,8 @@ class Profile(C.Structure):
                 ("other_ms", C.c_float), ("total_ms", C.c_float), ("extend_launches", C.c_uint32),
                 ("shadow_launches", C.c_uint32), ("shade_launches", C.c_uint32), ("other_launches", C.c_uint32),
                 ("rays_closest", C.c_uint64), ("rays_shadow", C.c_uint64), ("nodes_closest", C.c_uint64),
-                ("tris_closest", C.c_uint64), ("nodes_shadow", C.c_uint64), ("tris_shadow", C.c_uint64)]
+                ("tris_closest", C.c_uint64), ("nodes_shadow", C.c_uint64), ("tris_shadow", C.c_uint64),
+                ("lanes", C.c_uint32), ("reserved", C.c_uint32)]
 
 
 _lib = None

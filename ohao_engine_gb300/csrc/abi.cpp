@@ -1029,6 +1029,8 @@ static ohao_status render_views(ohao_pt_ctx* ctx, const ohao_pt_view* views, uin
         p.rays_closest = acc.rays_closest; p.rays_shadow = acc.rays_shadow;
         p.nodes_closest = acc.nodes_closest; p.tris_closest = acc.tris_closest;
         p.nodes_shadow = acc.nodes_shadow; p.tris_shadow = acc.tris_shadow;
+        p.lanes = acc.lanes;
+        p.reserved = 0;
     }
     return OHAO_OK;
 }

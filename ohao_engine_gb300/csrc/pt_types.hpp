@@ -112,6 +112,7 @@ struct ProfileAcc {
     uint32_t extend_launches = 0, shadow_launches = 0, shade_launches = 0, other_launches = 0;
     uint64_t rays_closest = 0, rays_shadow = 0;
     uint64_t nodes_closest = 0, tris_closest = 0, nodes_shadow = 0, tris_shadow = 0;
+    uint32_t lanes = 1;     // pixel lanes the unprofiled render would run
 };
 
 // display.cu: RGBA8 display image of npix RGBA32F texels

@@ -1141,7 +1141,9 @@ ohao_status wavefront_render(const DScene& sc, const RenderView& view, const Pat
     // warp traversal keeps one lane: its grids fill the GPU by themselves,
     // and two of them side by side measured 3% slower on the instanced scene.
     const bool fetch = pp.refill > 0 && sc.nnodes > 0;
-    const int nl = (ws && ws->main1 && !profile && !fetch && npix >= 64) ? 2 : 1;
+    const int lanes_unprofiled = (ws && ws->main1 && !fetch && npix >= 64) ? 2 : 1;
+    const int nl = profile ? 1 : lanes_unprofiled;
+    if (profile) prof->lanes = std::max<uint32_t>(prof->lanes, static_cast<uint32_t>(lanes_unprofiled));
     const uint32_t wcap = nl == 2 ? capacity / 2 : capacity;
     if (scratch_bytes < (nl == 2 ? wavefront_lanes_scratch_bytes(capacity) : wavefront_scratch_bytes(capacity))) {
         err = "wavefront scratch too small";
