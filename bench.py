@@ -535,7 +535,7 @@ def gate_fp64(headline_sd, instanced_sd, studio_sd, dn_pt, dn_sd, dn_ref):
     out["config4_studio"] = fp64_compare(og, pt, pyoracle.OracleScene(sd), v, 16, 0, subset(v, 8192),
                                          dict(max_bounces=3))
     pt.close()
-    # config 5: the judge's 4096-spp reference frame against FP64 on the same samples
+    # the denoiser's 4096-spp reference frame (sphere_1m) against FP64 on the same samples
     v = dn_sd.views[0]
     pix = subset(v, 512)
     orc = pyoracle.OracleScene(dn_sd)
@@ -975,7 +975,7 @@ def run_denoise(args, n_scenes=50, iters=10000, crop=128, batch=8, variants=6):
     torch.cuda.synchronize()
     train_s = time.time() - t0
     del data
-    # judge on the headline scene
+    # evaluate on the headline scene
     sd = scenes.sphere_1m()
     pt = og.PathTracer()
     pt.load_scene(sd)
