@@ -117,19 +117,19 @@ struct ohao_pt_ctx {
     // ohao_pt_render_host: history uploads run on their own stream, so that
     // they overlap the render up to its first read of the accumulator
     cudaStream_t upload_stream = nullptr;
-    // per-view wavefront (created on first use): the stream each step's
-    // shadow rays run on beside the next step's closest-hit rays, and the
-    // streams of the second pixel lane
-    cudaStream_t shadow_stream = nullptr, lane_stream = nullptr, lane_shadow_stream = nullptr;
+    // per-view wavefront (created on first use): the streams of the pixel
+    // lanes after the first, and each lane's stream for its shadow rays
+    ohao::WaveStreams wave{};
     std::vector<cudaEvent_t> upload_after, upload_done;   // per view: stream order in, upload landed
     ~ohao_pt_ctx() {
         if (persistent) ohao::persistent_destroy(persistent);
         for (cudaEvent_t e : upload_after) cudaEventDestroy(e);
         for (cudaEvent_t e : upload_done) cudaEventDestroy(e);
         if (upload_stream) cudaStreamDestroy(upload_stream);
-        if (shadow_stream) cudaStreamDestroy(shadow_stream);
-        if (lane_stream) cudaStreamDestroy(lane_stream);
-        if (lane_shadow_stream) cudaStreamDestroy(lane_shadow_stream);
+        for (int l = 0; l < ohao::kWaveLanes; ++l) {
+            if (wave.main[l]) cudaStreamDestroy(wave.main[l]);
+            if (wave.aux[l]) cudaStreamDestroy(wave.aux[l]);
+        }
         for (auto* b : host_accum_bufs) delete b;
         for (auto* b : host_display_bufs) delete b;
         for (auto* b : host_target_bufs) delete b;
@@ -1010,9 +1010,13 @@ static ohao_status render_views(ohao_pt_ctx* ctx, const ohao_pt_view* views, uin
         const uint32_t cap = ohao::wavefront_default_capacity();
         CK(ctx->scratch.ensure(std::max(ohao::wavefront_scratch_bytes(cap), ohao::wavefront_lanes_scratch_bytes(cap))),
            "render scratch");
-        for (cudaStream_t* sp : {&ctx->shadow_stream, &ctx->lane_stream, &ctx->lane_shadow_stream})
-            if (!*sp) CK(cudaStreamCreateWithFlags(sp, cudaStreamNonBlocking), "wavefront streams");
-        const ohao::WaveStreams ws{ctx->shadow_stream, ctx->lane_stream, ctx->lane_shadow_stream};
+        for (int l = 0; l < ohao::kWaveLanes; ++l) {
+            if (l > 0 && !ctx->wave.main[l])
+                CK(cudaStreamCreateWithFlags(&ctx->wave.main[l], cudaStreamNonBlocking), "wavefront streams");
+            if (!ctx->wave.aux[l])
+                CK(cudaStreamCreateWithFlags(&ctx->wave.aux[l], cudaStreamNonBlocking), "wavefront streams");
+        }
+        const ohao::WaveStreams& ws = ctx->wave;
         for (uint32_t v = 0; v < n_views; ++v) {
             std::string err;
             const ohao_status s = ohao::wavefront_render(sc, rvs[v], pp, st->spp, ctx->scratch.p, ctx->scratch.n, cap,

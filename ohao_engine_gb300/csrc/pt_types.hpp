@@ -121,14 +121,17 @@ cudaError_t launch_display(const float* accum, uint32_t npix, uint8_t* rgba8, cu
 // wavefront.cu
 size_t wavefront_scratch_bytes(uint32_t capacity);
 uint32_t wavefront_default_capacity();
-// Streams of the per-view wavefront besides the caller's: aux0 runs each
-// step's shadow rays beside the next step's closest-hit rays; main1 / aux1
-// render the second half of the view's pixels beside the first (two lanes,
-// each with half of the scratch). Null members: that part runs serially.
+// Pixel lanes of the per-view wavefront, and its streams besides the
+// caller's: lane l renders a slice of the view's pixels on main[l] (lane 0 on
+// the caller's stream; main[0] unused), each with capacity / kWaveLanes paths
+// of the scratch, and runs each step's shadow rays on aux[l] beside its next
+// step's closest-hit rays. Null members: that part runs serially.
+constexpr int kWaveLanes = 4;
 struct WaveStreams {
-    cudaStream_t aux0, main1, aux1;
+    cudaStream_t main[kWaveLanes];
+    cudaStream_t aux[kWaveLanes];
 };
-size_t wavefront_lanes_scratch_bytes(uint32_t capacity);   // two lanes of capacity / 2 paths
+size_t wavefront_lanes_scratch_bytes(uint32_t capacity);   // kWaveLanes lanes of capacity / kWaveLanes paths
 ohao_status wavefront_render(const DScene& sc, const RenderView& view, const PathParams& pp, uint32_t spp,
                              void* scratch, size_t scratch_bytes, uint32_t capacity, cudaStream_t st, bool profile,
                              ProfileAcc* prof, int* d_err, std::string& err, const WaveStreams* ws = nullptr);

@@ -1123,8 +1123,7 @@ uint32_t wavefront_default_capacity() { return 1u << 21; }
 
 size_t wavefront_lanes_scratch_bytes(uint32_t capacity) {
     Carve c{nullptr};
-    carve_soa_at(c, capacity / 2);
-    carve_soa_at(c, capacity / 2);
+    for (int l = 0; l < kWaveLanes; ++l) carve_soa_at(c, capacity / kWaveLanes);
     return c.off;
 }
 
@@ -1133,31 +1132,34 @@ ohao_status wavefront_render(const DScene& sc, const RenderView& view, const Pat
                              ProfileAcc* prof, int* d_err, std::string& err, const WaveStreams* ws) {
     init_launch_shapes();
     const uint32_t npix = view.vp.width * view.vp.height;
-    // Two lanes (a view of >= 64 pixels, one ray per thread in traversal,
-    // not profiled): the pixel ranks are split at a multiple of 32 (whole 8x4
-    // tiles) and each half renders all its samples on its own stream with
-    // half of the scratch, beside the other; the halves share no pixel, so
-    // each pixel's samples still fold in order within one lane. Persistent-
-    // warp traversal keeps one lane: its grids fill the GPU by themselves,
-    // and two of them side by side measured 3% slower on the instanced scene.
+    // kWaveLanes lanes (a view of >= 64 pixels per lane, one ray per thread
+    // in traversal, not profiled): the pixel ranks are split at multiples of
+    // 32 (whole 8x4 tiles) and each slice renders all its samples on its own
+    // stream with its share of the scratch, beside the others; the slices
+    // share no pixel, so each pixel's samples still fold in order within one
+    // lane. Persistent-warp traversal keeps one lane: its grids fill the GPU
+    // by themselves, and two of them side by side measured 3% slower on the
+    // instanced scene.
     const bool fetch = pp.refill > 0 && sc.nnodes > 0;
-    const int lanes_unprofiled = (ws && ws->main1 && !fetch && npix >= 64) ? 2 : 1;
+    const int lanes_unprofiled = (ws && ws->main[1] && !fetch && npix >= 64u * kWaveLanes) ? kWaveLanes : 1;
     const int nl = profile ? 1 : lanes_unprofiled;
     if (profile) prof->lanes = std::max<uint32_t>(prof->lanes, static_cast<uint32_t>(lanes_unprofiled));
-    const uint32_t wcap = nl == 2 ? capacity / 2 : capacity;
-    if (scratch_bytes < (nl == 2 ? wavefront_lanes_scratch_bytes(capacity) : wavefront_scratch_bytes(capacity))) {
+    const uint32_t wcap = capacity / static_cast<uint32_t>(nl);
+    if (scratch_bytes < (nl > 1 ? wavefront_lanes_scratch_bytes(capacity) : wavefront_scratch_bytes(capacity))) {
         err = "wavefront scratch too small";
         return OHAO_ERR_INVALID_ARG;
     }
-    Soa lane_soa[2];
+    Soa lane_soa[kWaveLanes];
+    uint32_t pix_base[kWaveLanes + 1], pix_count[kWaveLanes];
     {
         Carve c{static_cast<char*>(scratch)};
-        lane_soa[0] = carve_soa_at(c, wcap);
-        if (nl == 2) lane_soa[1] = carve_soa_at(c, wcap);
+        for (int l = 0; l < nl; ++l) {
+            lane_soa[l] = carve_soa_at(c, wcap);
+            pix_base[l] = static_cast<uint32_t>(static_cast<uint64_t>(npix) * l / nl) & ~31u;
+        }
+        pix_base[nl] = npix;
+        for (int l = 0; l < nl; ++l) pix_count[l] = pix_base[l + 1] - pix_base[l];
     }
-    const uint32_t half = (npix / 2) & ~31u;
-    const uint32_t pix_base[2] = {0u, nl == 2 ? half : 0u};
-    const uint32_t pix_count[2] = {nl == 2 ? half : npix, npix - half};
     unsigned long long* dstats = reinterpret_cast<unsigned long long*>(lane_soa[0].counts + 16);
     if (profile) cudaMemsetAsync(dstats, 0, 8 * sizeof(unsigned long long), st);
     const uint32_t niters = 1 + 2 * pp.max_bounces;
@@ -1175,13 +1177,12 @@ ohao_status wavefront_render(const DScene& sc, const RenderView& view, const Pat
     // small queues of a frame's last steps then share the GPU instead of
     // running one after the other. Profiled renders stay serial (their
     // per-kernel timers are on one stream).
-    cudaStream_t main_st[2] = {st, nl == 2 ? ws->main1 : st};
-    cudaStream_t sh_st[2] = {st, st};
-    bool overlap[2] = {false, false};
-    cudaEvent_t ev_shaded[2] = {nullptr, nullptr}, ev_shadowed[2] = {nullptr, nullptr}, ev_fork = nullptr,
-                ev_join = nullptr;
+    cudaStream_t main_st[kWaveLanes], sh_st[kWaveLanes];
+    bool overlap[kWaveLanes] = {};
+    cudaEvent_t ev_shaded[kWaveLanes] = {}, ev_shadowed[kWaveLanes] = {}, ev_join[kWaveLanes] = {}, ev_fork = nullptr;
     for (int l = 0; l < nl; ++l) {
-        const cudaStream_t aux = ws ? (l == 0 ? ws->aux0 : ws->aux1) : nullptr;
+        main_st[l] = l == 0 ? st : ws->main[l];
+        const cudaStream_t aux = ws ? ws->aux[l] : nullptr;
         overlap[l] = aux != nullptr && !profile;
         if (overlap[l]) {
             sh_st[l] = aux;
@@ -1191,11 +1192,13 @@ ohao_status wavefront_render(const DScene& sc, const RenderView& view, const Pat
             sh_st[l] = main_st[l];
         }
     }
-    if (nl == 2) {   // the second lane starts after the caller's work on st
+    if (nl > 1) {   // the other lanes start after the caller's work on st
         cudaEventCreateWithFlags(&ev_fork, cudaEventDisableTiming);
-        cudaEventCreateWithFlags(&ev_join, cudaEventDisableTiming);
         cudaEventRecord(ev_fork, st);
-        cudaStreamWaitEvent(main_st[1], ev_fork, 0);
+        for (int l = 1; l < nl; ++l) {
+            cudaEventCreateWithFlags(&ev_join[l], cudaEventDisableTiming);
+            cudaStreamWaitEvent(main_st[l], ev_fork, 0);
+        }
     }
     // one wave of lane l: paths [w0, w0 + n) of the lane's (sample, pixel) space
     auto run_wave = [&](int l, uint64_t w0, uint32_t n) {
@@ -1253,22 +1256,25 @@ ohao_status wavefront_render(const DScene& sc, const RenderView& view, const Pat
             pp, static_cast<uint32_t>(w0), n, vp, pn, s, view.accum, view.history, view.path_out);
         tm.end(3, a);
     };
-    const uint64_t lane_total[2] = {static_cast<uint64_t>(pix_count[0]) * spp,
-                                    nl == 2 ? static_cast<uint64_t>(pix_count[1]) * spp : 0ull};
-    for (uint64_t w0 = 0; w0 < lane_total[0] || w0 < lane_total[1]; w0 += wcap)
+    uint64_t lane_total[kWaveLanes], most = 0;
+    for (int l = 0; l < nl; ++l) {
+        lane_total[l] = static_cast<uint64_t>(pix_count[l]) * spp;
+        most = std::max(most, lane_total[l]);
+    }
+    for (uint64_t w0 = 0; w0 < most; w0 += wcap)
         for (int l = 0; l < nl; ++l)
             if (w0 < lane_total[l])
                 run_wave(l, w0, static_cast<uint32_t>(std::min<uint64_t>(wcap, lane_total[l] - w0)));
-    if (nl == 2) {   // the caller's stream continues after both lanes
-        cudaEventRecord(ev_join, main_st[1]);
-        cudaStreamWaitEvent(st, ev_join, 0);
+    for (int l = 1; l < nl; ++l) {   // the caller's stream continues after every lane
+        cudaEventRecord(ev_join[l], main_st[l]);
+        cudaStreamWaitEvent(st, ev_join[l], 0);
     }
     for (int l = 0; l < nl; ++l) {   // released once their pending records complete
         if (ev_shaded[l]) cudaEventDestroy(ev_shaded[l]);
         if (ev_shadowed[l]) cudaEventDestroy(ev_shadowed[l]);
+        if (ev_join[l]) cudaEventDestroy(ev_join[l]);
     }
     if (ev_fork) cudaEventDestroy(ev_fork);
-    if (ev_join) cudaEventDestroy(ev_join);
     const cudaError_t e = cudaGetLastError();
     if (e != cudaSuccess) {
         err = std::string("wavefront launch failed: ") + cudaGetErrorString(e);
