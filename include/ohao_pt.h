@@ -195,8 +195,9 @@ typedef struct ohao_pt_profile {
     uint64_t rays_closest, rays_shadow;
     uint64_t nodes_closest, tris_closest;   /* BVH nodes / triangles visited by closest-hit rays */
     uint64_t nodes_shadow, tris_shadow;     /* ... by shadow (any-hit) rays */
-    uint32_t lanes;            /* pixel lanes the same call runs unprofiled (per-view wavefront: 1 or 2,
-                                  each with this profile's kernel sequence); profiled calls run one */
+    uint32_t lanes;            /* pixel lanes the same call runs unprofiled (per-view wavefront: 1, or 4
+                                  with one ray per thread in traversal; each lane runs this profile's
+                                  kernel sequence over its slice of the pixels); profiled calls run one */
     uint32_t reserved;
 } ohao_pt_profile;
 
