@@ -169,3 +169,44 @@ def test_flag_off_is_the_reference_choice(oracle):
     assert np.all(s[:, 7] == len(sd.lights)) and np.all(s[:, 8] == 0.0)
     s = o.light_samples(EMITTER_MIS, (0.0, -0.5, 0.0), (0.0, 1.0, 0.0), 256, seed=1)
     assert np.all(s[:, 7] == len(sd.lights) + 1) and np.all(s[s[:, 9] == 1, 8] > 0)
+
+
+def test_degenerate_and_negative_emitters(oracle):
+    """A zero-area emissive triangle keeps its table slot with pdf 0 (the
+    search never lands on a zero CDF step, and a BSDF hit on it takes weight
+    1); negative emission channels count as 0 in the power; a material whose
+    emission is all non-positive is not an emitter."""
+    from ohao_engine_gb300 import scenes
+    sd = emitter_scene(lights=())
+    n0 = sd.blas[0][1] // 3                      # BLAS 0's triangles; the instanced triangle follows
+    idx = sd.indices.reshape(-1, 3)
+    deg, nonpos = len(sd.materials), len(sd.materials) + 1
+    sd.materials = np.concatenate([sd.materials,
+                                   scenes.material((0.5, 0.5, 0.5), emissive=(8.0, -3.0, 2.0))[None],
+                                   scenes.material((0.5, 0.5, 0.5), emissive=(-1.0, 0.0, -2.0))[None]])
+    # two new triangles appended to BLAS 0: collinear corners, and a plain one
+    nv = sd.pos.shape[0]
+    new_pos = np.array([(0.0, 0.5, 0.0), (0.5, 0.5, 0.0), (1.0, 0.5, 0.0),
+                        (0.0, 0.9, 0.0), (0.5, 0.9, 0.0), (0.0, 0.9, 0.5)], np.float32)
+    sd.pos = np.concatenate([sd.pos, new_pos])
+    sd.normals = np.concatenate([sd.normals, np.tile(np.array([0.0, 1.0, 0.0, 0.0], np.float32), (6, 1))])
+    sd.uvs = np.concatenate([sd.uvs, np.zeros((6, 2), np.float32)])
+    new_idx = np.array([[nv, nv + 1, nv + 2], [nv + 3, nv + 4, nv + 5]], np.uint32)
+    sd.indices = np.ascontiguousarray(np.concatenate([idx[:n0], new_idx, idx[n0:]]).reshape(-1))
+    sd.mat_ids = np.ascontiguousarray(np.concatenate([sd.mat_ids[:n0], [deg, nonpos], sd.mat_ids[n0:]]).astype(np.uint32))
+    sd.blas = [(0, 3 * (n0 + 2)), (3 * (n0 + 2), 3), (3 * (n0 + 2), 3)]
+    inst = sd.instances.copy()
+    for k in (1, 2, 3):
+        inst[k]["custom_index"] = n0 + 2
+    sd.instances = inst
+    o = oracle.OracleScene(sd)
+    tri, cdf = o.emitter_table()
+    pairs = list(zip(tri[:, 7].view(np.uint32).tolist(), tri[:, 11].view(np.uint32).tolist()))
+    assert (0, n0) in pairs, "the degenerate emitter keeps its slot"
+    assert (0, n0 + 1) not in pairs, "non-positive emission is no emitter"
+    k = pairs.index((0, n0))
+    assert tri[k, 3] == 0.0
+    step = np.diff(np.concatenate([[0.0], cdf.astype(np.float64)]))
+    assert step[k] == 0.0
+    s = o.light_samples(EMITTER_MIS, (0.2, -0.6, 0.3), (0.0, 1.0, 0.0), 20000, seed=9)
+    assert np.all(np.isfinite(s[s[:, 9] == 1]))
